@@ -1,0 +1,383 @@
+"""Benchmark: 1080p stabilized frames/s of the plain FP32 GPU path.
+
+Workload (one step = one frame): the 1920x1080 synthetic stream (seeded
+Gaussian blobs advected by a smooth flow re-drawn every 30 frames, processed
+frames with colour shift and flicker; RGBA8 in and out).  Per frame: load the
+next frame (RGBA8 -> float, flow features), compute the forward and backward
+flow at full resolution through the Correlation (81 displacements) and Warp
+kernels, then the stabilization pass (five warps, adaptive combination,
+consistency weights, 2-level pyramid solve with 75 + 150 iterations) and the
+RGBA8 output — VideoStabilizer::doOneStep with its defaults.
+
+value : frames/s with every input frame already resident in HBM (RGBA8).
+e2e   : the same through the public C ABI with host buffers: each step copies
+        the next frame pair from pinned host memory and reads the stabilized
+        frame back, inside the timed region.
+The per-step working set (~0.6 GB) is far larger than L2, so no flush is
+needed between steps.
+
+--impl reference: the reference's CPU path on the host cores (the CPU
+restatement in oracle/, which for the two custom ops is bit-identical to the
+reference's correlation.cc / warp.cc; the reference has no CPU code for the
+stabilization pass).
+
+Multi-GPU: the path does not shard within a stream (frame t needs the
+stabilized frame t-1), so N ranks run N independent replica streams (weak
+scaling); rank 0 prints the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "video-stream-consistency_gb300"
+W, H = 1920, 1080
+METRIC = "1080p stabilized frames/s (plain FP32 GPU path: correlation + warp + mask + blend)"
+# Solver Jacobi step, per pixel: reads O, U, lap(P), A, consWt (5 x 12 B),
+# writes O, U (2 x 12 B).
+SOLVER_BYTES_PER_PX = 84
+
+
+def import_pkg():
+    if "vsc_gb300" in sys.modules:
+        return sys.modules["vsc_gb300"]
+    spec = importlib.util.spec_from_file_location("vsc_gb300", PKG / "__init__.py",
+                                                  submodule_search_locations=[str(PKG)])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["vsc_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (burst copy)"
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().strip().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def reduce_max(value: float, ws: int, device=None) -> float:
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def make_frames(n: int, seed: int, device: str):
+    vsc = import_pkg()
+    from vsc_gb300 import synth
+
+    s = synth.SyntheticStream(W, H, seed=seed, device=device)
+    return [s.frame(i) for i in range(n)]
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline_sample(frames, threads: int, n_frames: int = 10):
+    """The CPU path timed on a bounded sample: n_frames full 1080p steps."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+
+    O.set_threads(threads)
+    n_frames = max(1, min(n_frames, len(frames) - 2))
+    orig = [O.rgba_to_float(o) for o, _ in frames[: n_frames + 2]]
+    proc = [O.rgba_to_float(p) for _, p in frames[: n_frames + 2]]
+    last = proc[2]
+    t0 = time.perf_counter()
+    for t in range(1, n_frames + 1):
+        ff = O.flow_estimate(orig[t], orig[t + 1])
+        fb = O.flow_estimate(orig[t + 1], orig[t])
+        last, _ = O.stab_pass(orig[t - 1:t + 2], proc[t - 1:t + 2], ff, fb, last)
+    dt = time.perf_counter() - t0
+    return {"value": n_frames / dt, "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": f"{n_frames} consecutive 1920x1080 frames of the same stream: flow (fwd+bwd, the "
+                      f"restated Correlation/Warp ops) + stabilization pass + RGBA8 output, OpenMP over "
+                      f"{threads} host threads",
+            "seconds": dt}
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+
+    O.build(ref=False)
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    n = min(args.steps + args.warmup + 2, 120)
+    frames = make_frames(n, seed=0, device="cpu")
+    orig = [O.rgba_to_float(o) for o, _ in frames]
+    proc = [O.rgba_to_float(p) for _, p in frames]
+    last = proc[2]
+
+    def step(t):
+        nonlocal last
+        i = 1 + (t % (n - 2))
+        ff = O.flow_estimate(orig[i], orig[i + 1])
+        fb = O.flow_estimate(orig[i + 1], orig[i])
+        last, rgba = O.stab_pass(orig[i - 1:i + 2], proc[i - 1:i + 2], ff, fb, last)
+        return rgba
+
+    for t in range(args.warmup):
+        step(t)
+    t0 = time.perf_counter()
+    for t in range(args.steps):
+        step(args.warmup + t)
+    dt = time.perf_counter() - t0
+    v = args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "1920x1080 synthetic stream, plain method (flow at full resolution, 2-level "
+                               "pyramid, 150 iterations), RGBA8 in/out", "width": W, "height": H},
+        "cpu_baseline": {"value": v, "unit": "frames/s", "cores": threads, "kind": "port",
+                         "sample": f"each step one 1920x1080 frame on {threads} host threads (OpenMP): the CPU "
+                                   "restatement, bit-identical to the reference's CPU Correlation/Warp ops; the "
+                                   "reference has no CPU stabilization pass"},
+        "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    vsc = import_pkg()
+    vsc.build()
+    vsc.load()
+
+    n_frames = min(args.steps + args.warmup + 3, 120)
+    frames = make_frames(n_frames, seed=rank, device=str(dev))
+    stream = torch.cuda.Stream(device=dev)
+
+    # ---- device-resident run -------------------------------------------------
+    dev_frames = [(torch.from_numpy(o).to(dev), torch.from_numpy(p).to(dev)) for o, p in frames]
+    out_dev = torch.empty((H, W, 4), dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+    st = vsc.Stabilizer(W, H, stream=stream)
+    for i in range(3):
+        st.load_frame(*dev_frames[i])
+    nxt = 3
+    launches_per_step = 0
+
+    def step_dev():
+        nonlocal nxt, launches_per_step
+        st.step(out_dev)
+        n = st.last_launches
+        st.load_frame(*dev_frames[nxt % n_frames])
+        launches_per_step = n + st.last_launches
+        nxt += 1
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step_dev()
+    stream.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(ws)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step_dev()
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    barrier(ws)
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    ms_max = reduce_max(ms, ws, dev)
+    value = ws * args.steps / (ms_max / 1000.0)
+
+    # ---- end to end through the public API with pinned host buffers ------------
+    pinned = [(torch.from_numpy(o).pin_memory(), torch.from_numpy(p).pin_memory()) for o, p in frames]
+    out_host = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory()
+    st2 = vsc.Stabilizer(W, H, stream=stream)
+    for i in range(3):
+        st2.load_frame(pinned[i][0].numpy(), pinned[i][1].numpy())
+    nxt2 = 3
+
+    def step_e2e():
+        nonlocal nxt2
+        st2.step(out_host)  # reads the result back (synchronises the stream)
+        o, p = pinned[nxt2 % n_frames]
+        st2.load_frame(o.numpy(), p.numpy())
+        nxt2 += 1
+
+    for _ in range(args.warmup):
+        step_e2e()
+    stream.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_e2e()
+    stream.synchronize()
+    t_e2e = time.perf_counter() - t0
+    barrier(ws)
+    t_e2e = reduce_max(t_e2e, ws, dev)
+    e2e = {"value": ws * args.steps / t_e2e, "unit": "frames/s", "h2d_bytes_per_step": 2 * W * H * 4,
+           "d2h_bytes_per_step": W * H * 4}
+
+    # ---- roofline of the dominant kernel: the full-resolution solver step ------
+    peak, peak_src = peaks()
+    g = torch.Generator(device=dev).manual_seed(1)
+    P = torch.rand((H, W, 3), device=dev, generator=g)
+    A = torch.rand((H, W, 3), device=dev, generator=g)
+    Wt = torch.rand((H, W, 3), device=dev, generator=g) * 2
+    O = P.clone()
+    wsp = torch.empty(vsc.consist_out_workspace_size(W, H) // 4, dtype=torch.float32, device=dev)
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            vsc.get_consist_out(P, A, Wt, 150, 0.15, 0.15, O, workspace=wsp, stream=stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record(stream)
+    vsc.get_consist_out(P, A, Wt, 1, 0.15, 0.15, O, workspace=wsp, stream=stream)
+    ev[1].record(stream)
+    ev[2].record(stream)
+    vsc.get_consist_out(P, A, Wt, 151, 0.15, 0.15, O, workspace=wsp, stream=stream)
+    ev[3].record(stream)
+    ev[3].synchronize()
+    per_launch_ms = (ev[2 + 0].elapsed_time(ev[3]) - ev[0].elapsed_time(ev[1])) / 150.0
+    alg_bytes = SOLVER_BYTES_PER_PX * W * H
+    achieved = alg_bytes / (per_launch_ms / 1000.0) / 1e9
+    roofline = {"bound": "hbm", "kernel": "solver_iter_kernel (one Jacobi step of kernel_consist_out at "
+                                          "1920x1080)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": SOLVER_TRAFFIC_BYTES, "algorithmic_bytes_per_launch": alg_bytes,
+                "launch_ms": per_launch_ms, "peak_source": peak_src}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "1920x1080 synthetic stream (plain method: flow at full resolution via "
+                               "Correlation md=4 + Warp, 2-level pyramid, 75+150 solver iterations), RGBA8 in/out",
+                   "width": W, "height": H, "frames_generated": n_frames,
+                   "l2": "per-step working set ~0.6 GB > 129 MB L2; no flush",
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "roofline": roofline, "clocks": clk,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_sample(frames, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line))
+    st.close()
+    st2.close()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum of one solver launch at
+# 1920x1080, from the ncu capture summarised in profiles/ (None until captured).
+SOLVER_TRAFFIC_BYTES = None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

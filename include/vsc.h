@@ -1,0 +1,213 @@
+/*
+ * vsc.h — C ABI of the GB300 (sm_103a) implementation of the per-frame hot
+ * path of video-stream-consistency: the Correlation and Warp optical-flow
+ * operators and the per-frame stabilization pass.
+ *
+ * Every entry point:
+ *   - takes plain device (or, where stated, host) pointers, sizes and a CUDA
+ *     stream (vsc_stream_t is a cudaStream_t; NULL is the legacy default
+ *     stream), enqueues its work on that stream and returns without
+ *     synchronising the device;
+ *   - returns a vsc_status, never exits or throws; vsc_last_error() gives
+ *     the calling thread's message for the last failure;
+ *   - is reentrant: no entry point keeps hidden per-call state, so calls from
+ *     several threads on several streams may run concurrently.
+ *
+ * Each declaration names the reference interface (file:line, relative to
+ * the reference project root) it replaces.
+ */
+#ifndef VSC_H
+#define VSC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define VSC_API __declspec(dllexport)
+#else
+#define VSC_API __attribute__((visibility("default")))
+#endif
+
+typedef enum vsc_status {
+    VSC_OK = 0,
+    VSC_EINVAL = 1,        /* bad pointer, shape, attribute or size */
+    VSC_ECUDA = 2,         /* a CUDA runtime call or launch failed */
+    VSC_ETIMEOUT = 3,      /* a bounded device-side wait gave up */
+    VSC_ENOMEM = 4,        /* device or workspace memory exhausted / too small */
+    VSC_EUNSUPPORTED = 5,  /* valid request this build does not implement */
+    VSC_ESTATE = 6         /* call out of order (e.g. step before the frame window is full) */
+} vsc_status;
+
+typedef void* vsc_stream_t;
+
+/* Message of the calling thread's last failure ("" after success). */
+VSC_API const char* vsc_last_error(void);
+/* 10000*major + 100*minor + patch */
+VSC_API int vsc_version(void);
+
+/* ========================================================================
+ * ONNX Runtime custom ops (domain "custom")
+ * ======================================================================== */
+
+/* custom::Correlation.  Replaces CorrelationKernel::Compute /
+ * ComputeCUDA (src/ort_custom_ops/include/ort_custom_ops/opticalflow/
+ * correlation.h:35-50, src/ort_custom_ops/src/opticalflow/correlation_cuda.cc:29-137,
+ * correlation_cuda.cu:333-442; CPU semantics correlation.cc:45-275).
+ *   f1, f2 : device, N x C x H x W float (NCHW)
+ *   out    : device, legacy = 0: N x P x P x H x W, out[n][i][j][h][w] =
+ *            sum_c f1[n][c][h][w] * f2[n][c][h+i-md][w+j-md] (0 outside);
+ *            legacy = 1: N x P*P x H x W, the same sums divided by C
+ *            (the original PWC-Net layer, correlation_cuda.cu:182-331);
+ *            P = 2*max_displacement + 1.
+ * The channel sum is taken in channel order with separately rounded
+ * products and sums, so legacy = 0 equals the reference CPU op bit for bit.
+ * No workspace: the NCHW->NHWC temporaries of the reference
+ * (correlation_cuda.cu:365-391) are folded into the kernel's tile loads. */
+VSC_API vsc_status vsc_correlation_fwd(const float* f1, const float* f2, float* out, int64_t N, int64_t C, int64_t H,
+    int64_t W, int64_t max_displacement, int64_t legacy, vsc_stream_t stream);
+
+/* custom::Warp.  Replaces WarpKernel::Compute / ComputeCUDA
+ * (warp.h:18-31, warp_cuda.cc:28-77, warp_cuda.cu:28-98; CPU semantics
+ * warp.cc:25-133).
+ *   input : device, N x C x H x W float;  flow : device, N x 2 x H x W
+ *   (channel 0 = x displacement, 1 = y);  out : device, N x C x H x W.
+ * Bilinear backward warp with zero padding; an output is 0 unless the
+ * bilinear weight of its in-map taps exceeds 0.999.  Single-precision
+ * weights: within 2^-21 * max|input| of the reference's double-weight CPU op. */
+VSC_API vsc_status vsc_warp_fwd(const float* input, const float* flow, float* out, int64_t N, int64_t C, int64_t H,
+    int64_t W, vsc_stream_t stream);
+
+/* ========================================================================
+ * Stabilization kernels (src/stabilization/flowconsistency.cuh:3-50)
+ * ======================================================================== */
+
+/* A device image: interleaved float, element (x, y, c) at
+ * data[(y*width + x)*channels + c].  Mirrors GPUImage / GPUImageWrapper
+ * (src/stabilization/gpuimage.h:8-31, gpuimagewrapper.h:8-25). */
+typedef struct vsc_image {
+    float* data;
+    int32_t width;
+    int32_t height;
+    int32_t channels;
+} vsc_image;
+
+/* RGBA8 (device) -> 3-channel float image, value = float(double(v)/255.0).
+ * Replaces kernel_to_float_image / char_to_cuda_float_image (gpuimage.cu:39-104). */
+VSC_API vsc_status vsc_char_to_float_image(const uint8_t* rgba, const vsc_image* out, vsc_stream_t stream);
+
+/* 3-channel float image -> RGBA8 (device), (uint8)floor(|v|*255) with the
+ * reference's mod-256 wrap, alpha = 1.  Replaces kernel_to_char_image /
+ * cuda_float_to_char_image (gpuimage.cu:54-67, :107-135). */
+VSC_API vsc_status vsc_float_to_char_image(const vsc_image* in, uint8_t* rgba, vsc_stream_t stream);
+
+/* Backward warp of a 3-channel image by a 2- or 3-channel flow, sample
+ * position clamped to [0,w-3] x [0,h-3].  Replaces get_warp_result /
+ * kernel_warp (flowconsistency.cu:77-114, :301-312). */
+VSC_API vsc_status vsc_get_warp_result(const vsc_image* input, const vsc_image* flow, const vsc_image* input_warp,
+    vsc_stream_t stream);
+
+/* Adaptive temporal combination.  Replaces get_adap_comb / kernel_adap_comb
+ * (flowconsistency.cu:116-166, :314-333). */
+VSC_API vsc_status vsc_get_adap_comb(const vsc_image* crnt_in, const vsc_image* crnt_pr, const vsc_image* prev_warp_in,
+    const vsc_image* prev_warp_pr, const vsc_image* next_warp_in, const vsc_image* next_warp_pr,
+    const vsc_image* adap_cmb_in, const vsc_image* adap_cmb_pr, const vsc_image* last_stab_warp, float alpha,
+    vsc_stream_t stream);
+
+/* Consistency weights gamma*exp(-beta*(I - adapCmbIn)^2), < 0.001 -> 0.
+ * Replaces get_consist_wt / kernel_consist_wt (flowconsistency.cu:168-191, :335-348). */
+VSC_API vsc_status vsc_get_consist_wt(const vsc_image* adap_cmb_in, const vsc_image* crnt_in,
+    const vsc_image* consis_wt, float beta, float gamma, vsc_stream_t stream);
+
+/* Bilinear resample, source coordinate ox*Win/Wout, edge taps clamped.
+ * Replaces get_bilinear / kernel_bilinear (flowconsistency.cu:50-75, :288-299). */
+VSC_API vsc_status vsc_get_bilinear(const vsc_image* input, const vsc_image* output, vsc_stream_t stream);
+
+/* Bytes of device workspace vsc_get_consist_out needs for a width x height image. */
+VSC_API size_t vsc_consist_out_workspace_size(int32_t width, int32_t height);
+
+/* num_iter gradient-descent steps with momentum on the blend energy
+ * (Jacobi form; consis_out holds the initial solution and receives the
+ * result).  Replaces get_consist_out / kernel_consist_out
+ * (flowconsistency.cu:193-258, :350-374).  workspace: device memory of at
+ * least vsc_consist_out_workspace_size bytes, or NULL to let the library
+ * take it from the stream-ordered memory pool of the current device. */
+VSC_API vsc_status vsc_get_consist_out(const vsc_image* crnt_pr, const vsc_image* prev_stab_warp,
+    const vsc_image* cons_wt, int32_t num_iter, float step_size, float mom_fac, const vsc_image* consis_out,
+    void* workspace, size_t workspace_bytes, vsc_stream_t stream);
+
+/* ========================================================================
+ * Per-frame orchestrator (src/stabilization/videostabilizer.{h,cpp})
+ * ======================================================================== */
+
+/* Mirrors hyperParams (videostabilizer.h:38-46). */
+typedef struct vsc_hyper_params {
+    float alpha;
+    float beta;
+    float gamma;
+    int32_t pyramid_levels;
+    int32_t num_iter;
+    float step_size;
+    float mom_fac;
+} vsc_hyper_params;
+
+/* VideoStabilizer::initHyperParams defaults (videostabilizer.cpp:104-112). */
+VSC_API void vsc_default_hyper_params(vsc_hyper_params* hp);
+
+typedef struct vsc_stabilizer vsc_stabilizer;
+
+typedef struct vsc_stabilizer_config {
+    int32_t width;
+    int32_t height;
+    int32_t batch_size;     /* flow batch (-b); this build supports 1 */
+    int32_t compute_flow;   /* 1: flows computed from the original frames by the
+                               library's flow estimator (built on the two ops);
+                               0: flows supplied with vsc_stabilizer_set_flows */
+    int32_t flow_downscale; /* FLOWDOWNSCALE (videostabilizer.cpp:74-98); 1 = full size */
+    int32_t flow_channels;  /* channels (2 or 3) of supplied flows when compute_flow = 0 */
+} vsc_stabilizer_config;
+
+/* Replaces the VideoStabilizer constructor (videostabilizer.cpp:46-102).
+ * All device memory is allocated here, once; the stream is used for every
+ * later call on this stabilizer. */
+VSC_API vsc_status vsc_stabilizer_create(const vsc_stabilizer_config* cfg, vsc_stream_t stream,
+    vsc_stabilizer** out);
+VSC_API vsc_status vsc_stabilizer_destroy(vsc_stabilizer* s);
+
+/* The live hyper-parameters (getHyperParams, videostabilizer.h:110). */
+VSC_API vsc_hyper_params* vsc_stabilizer_hyper_params(vsc_stabilizer* s);
+
+/* Append frame i to the window (loadFrame + imageToGPU, stabilizefiles.cpp:72-96):
+ * RGBA8 original and per-frame processed images, width x height x 4, on the
+ * host (on_device = 0; pinned memory gives asynchronous copies) or device. */
+VSC_API vsc_status vsc_stabilizer_load_frame(vsc_stabilizer* s, const uint8_t* orig_rgba, const uint8_t* proc_rgba,
+    int32_t on_device);
+
+/* Flows for the next step when compute_flow = 0 (FileStabilizer::retrieveOpticalFlow,
+ * stabilizefiles.cpp:134-149): fwd = flow of frame t to t+1, bwd = flow of t to t-1,
+ * width x height x flow_channels float, host or device. */
+VSC_API vsc_status vsc_stabilizer_set_flows(vsc_stabilizer* s, const float* fwd, const float* bwd,
+    int32_t on_device);
+
+/* One frame: doOneStep (videostabilizer.cpp:167-265) for the middle frame of
+ * the 3-frame window; writes its RGBA8 stabilized image to out_rgba (host or
+ * device), keeps the FP32 result as the next step's previous stabilized
+ * frame, and drops the oldest frame from the window. */
+VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int32_t out_on_device);
+
+/* Device pointers to internal state, for inspection (valid until the next call):
+ * which = 0: last stabilized frame (float HWC3), 1: forward flow, 2: backward flow
+ * (float HWC, 3 channels when computed), 3: adapCmbPr, 4: consWt. */
+VSC_API vsc_status vsc_stabilizer_buffer(vsc_stabilizer* s, int32_t which, const float** dev_ptr);
+
+/* Number of kernels the last vsc_stabilizer_step enqueued. */
+VSC_API int32_t vsc_stabilizer_last_launches(vsc_stabilizer* s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VSC_H */

@@ -1,0 +1,220 @@
+"""Stabilization pass on the GPU through the C ABI, against the CPU
+restatement of flowconsistency.cu / gpuimage.cu / videostabilizer.cpp.
+
+Tolerance: none — every kernel of the pass (frame I/O, warps, adaptive
+combination, consistency weights, pyramid, solver, flow estimator) is
+bit-exact to the restatement, so the comparisons are exact equality."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+RNG = np.random.Generator(np.random.PCG64(4321))
+
+
+def _t(a, dev):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def _img(h, w, c=3, lo=0.0, hi=1.0):
+    return RNG.uniform(lo, hi, (h, w, c)).astype(np.float32)
+
+
+def test_rgba_round_trip(vsc, oracle, cuda):
+    rgba = RNG.integers(0, 256, (37, 53, 4), dtype=np.uint8)
+    f = vsc.char_to_float_image(_t(rgba, cuda))
+    assert np.array_equal(f.cpu().numpy(), oracle.rgba_to_float(rgba))
+    back = vsc.float_to_char_image(f).cpu().numpy()
+    assert np.array_equal(back, oracle.float_to_rgba(oracle.rgba_to_float(rgba)))
+    special = np.array([1.0, 1.01, -0.5, 2.0, np.nan, 1e30, 0.999, -1.0, 256.0 / 255.0, np.inf, -np.inf, 1e-40],
+                       np.float32).reshape(2, 2, 3)
+    got = vsc.float_to_char_image(_t(special, cuda)).cpu().numpy()
+    assert np.array_equal(got, oracle.float_to_rgba(special))
+
+
+@pytest.mark.parametrize("h,w,fc,scale", [(24, 32, 3, 4.0), (17, 29, 2, 12.0), (5, 4, 3, 50.0), (64, 96, 2, 0.5)])
+def test_warp_result(vsc, oracle, cuda, h, w, fc, scale):
+    img = _img(h, w)
+    flow = RNG.normal(0, scale, (h, w, fc)).astype(np.float32)
+    got = vsc.get_warp_result(_t(img, cuda), _t(flow, cuda)).cpu().numpy()
+    assert np.array_equal(got, oracle.stab_warp(img, flow))
+
+
+def test_adap_comb_and_weights(vsc, oracle, cuda):
+    h, w = 31, 47
+    base = _img(h, w)
+    ims = [np.clip(base + RNG.normal(0, s, base.shape), 0, 1).astype(np.float32)
+           for s in (0.0, 0.02, 0.005, 0.03, 0.01, 0.02, 0.004)]
+    ain, apr = vsc.get_adap_comb(*[_t(a, cuda) for a in ims], 6800.0)
+    oin, opr = oracle.adap_comb(*ims, 6800.0)
+    assert np.array_equal(ain.cpu().numpy(), oin)
+    assert np.array_equal(apr.cpu().numpy(), opr)
+    wt = vsc.get_consist_wt(ain, _t(ims[0], cuda), 6800.0, 2.0).cpu().numpy()
+    owt = oracle.consist_wt(ims[0], oin, 6800.0, 2.0)
+    assert np.array_equal(wt, owt)
+    # all clamp branches taken: 0 (below 1e-3), 0.45 / 0.3 caps, and free values
+    assert (owt == 0).any() and (owt > 0).any()
+
+
+@pytest.mark.parametrize("src,dst", [((64, 48), (32, 24)), ((33, 21), (16, 10)), ((16, 10), (33, 21)),
+                                     ((1920, 1080), (960, 540)), ((960, 540), (1920, 1080))])
+def test_bilinear(vsc, oracle, cuda, src, dst):
+    img = _img(src[1], src[0])
+    got = vsc.get_bilinear(_t(img, cuda), dst[0], dst[1]).cpu().numpy()
+    assert np.array_equal(got, oracle.bilinear(img, dst[0], dst[1]))
+
+
+@pytest.mark.parametrize("h,w,iters", [(9, 11, 0), (9, 11, 1), (9, 11, 2), (40, 56, 75), (3, 3, 5), (2, 2, 4),
+                                       (67, 33, 150)])
+def test_consist_out(vsc, oracle, cuda, h, w, iters):
+    import torch
+
+    P, A, Wt, O0 = _img(h, w), _img(h, w), _img(h, w, hi=2.0), _img(h, w)
+    O = _t(O0, cuda)
+    vsc.get_consist_out(_t(P, cuda), _t(A, cuda), _t(Wt, cuda), iters, 0.15, 0.15, O)
+    ref = oracle.consist_out(P, A, Wt, iters, 0.15, 0.15, O0)
+    assert np.array_equal(O.cpu().numpy(), ref)
+    # caller-provided workspace gives the same bits
+    ws = torch.empty(vsc.consist_out_workspace_size(w, h) // 4, dtype=torch.float32, device=cuda)
+    O2 = _t(O0, cuda)
+    vsc.get_consist_out(_t(P, cuda), _t(A, cuda), _t(Wt, cuda), iters, 0.15, 0.15, O2, workspace=ws)
+    assert np.array_equal(O2.cpu().numpy(), ref)
+
+
+def _frames(w, h, n, seed):
+    from vsc_gb300 import synth
+
+    s = synth.SyntheticStream(w, h, seed=seed)
+    return [s.frame(i) for i in range(n)]
+
+
+def _run_oracle_stream(oracle, frames, flows=None, hp=None, downscale=1):
+    """The reference's driver loop (stabilizefiles.cpp:108-131 with
+    videostabilizer.cpp:136-265) over the restatement."""
+    orig = [oracle.rgba_to_float(o) for o, _ in frames]
+    proc = [oracle.rgba_to_float(p) for _, p in frames]
+    h, w = orig[0].shape[:2]
+    last = proc[2]
+    outs = []
+    for t in range(1, len(frames) - 1):
+        if flows is not None:
+            ff, fb = flows[t]
+        elif downscale > 1:
+            fw, fh = int(round(w / downscale)), int(round(h / downscale))
+            small = [_nearest(orig[t], fw, fh), _nearest(orig[t + 1], fw, fh)]
+            ff = oracle.bilinear(oracle.flow_estimate(small[0], small[1]), w, h)
+            fb = oracle.bilinear(oracle.flow_estimate(small[1], small[0]), w, h)
+        else:
+            ff = oracle.flow_estimate(orig[t], orig[t + 1])
+            fb = oracle.flow_estimate(orig[t + 1], orig[t])
+        out, rgba = oracle.stab_pass(orig[t - 1:t + 2], proc[t - 1:t + 2], ff, fb, last, hp)
+        outs.append((out, rgba, ff, fb))
+        last = out
+    return outs
+
+
+def _nearest(img, ow, oh):
+    h, w = img.shape[:2]
+    xs = np.minimum(w - 1, ((2 * np.arange(ow) + 1) * w) // (2 * ow))
+    ys = np.minimum(h - 1, ((2 * np.arange(oh) + 1) * h) // (2 * oh))
+    return np.ascontiguousarray(img[ys][:, xs])
+
+
+@pytest.mark.parametrize("w,h", [(96, 64), (70, 45)])
+def test_stabilizer_computed_flow_stream(vsc, oracle, cuda, w, h):
+    frames = _frames(w, h, 6, seed=11)
+    ref = _run_oracle_stream(oracle, frames)
+    st = vsc.Stabilizer(w, h)
+    for i in range(3):
+        st.load_frame(*frames[i])
+    for k, t in enumerate(range(1, len(frames) - 1)):
+        out = st.step()
+        r_out, r_rgba, r_ff, r_fb = ref[k]
+        assert np.array_equal(st.buffer(1).cpu().numpy(), r_ff), f"fwd flow, step {k}"
+        assert np.array_equal(st.buffer(2).cpu().numpy(), r_fb), f"bwd flow, step {k}"
+        assert np.array_equal(st.buffer(0).cpu().numpy(), r_out), f"stabilized, step {k}"
+        assert np.array_equal(out.cpu().numpy(), r_rgba), f"rgba, step {k}"
+        if t + 2 < len(frames):
+            st.load_frame(*frames[t + 2])
+    st.close()
+
+
+def test_stabilizer_external_flows_host_io(vsc, oracle, cuda):
+    """File mode (-f): 2-channel flows supplied per step, host frames in/out."""
+    import torch
+
+    w, h = 80, 48
+    frames = _frames(w, h, 5, seed=12)
+    flows = {t: (RNG.normal(0, 3, (h, w, 2)).astype(np.float32), RNG.normal(0, 3, (h, w, 2)).astype(np.float32))
+             for t in range(1, 4)}
+    ref = _run_oracle_stream(oracle, frames, flows=flows)
+    st = vsc.Stabilizer(w, h, compute_flow=False, flow_channels=2)
+    for i in range(3):
+        st.load_frame(*frames[i])
+    for k, t in enumerate(range(1, 4)):
+        st.set_flows(torch.from_numpy(flows[t][0]), torch.from_numpy(flows[t][1]))
+        out = torch.empty((h, w, 4), dtype=torch.uint8)
+        st.step(out)
+        assert np.array_equal(out.numpy(), ref[k][1])
+        if t + 2 < len(frames):
+            st.load_frame(*frames[t + 2])
+    with pytest.raises(vsc.VscError, match="ESTATE"):
+        st.step()
+    st.close()
+
+
+def test_stabilizer_hyper_params_and_downscale(vsc, oracle, cuda):
+    w, h = 128, 72
+    frames = _frames(w, h, 4, seed=13)
+    hp = oracle.default_hyper()
+    hp.pyramid_levels, hp.num_iter, hp.gamma = 3, 40, 1.0
+    ref = _run_oracle_stream(oracle, frames, hp=hp, downscale=2)
+    st = vsc.Stabilizer(w, h, flow_downscale=2)
+    p = st.hyper_params
+    p.pyramid_levels, p.num_iter, p.gamma = 3, 40, 1.0
+    for i in range(3):
+        st.load_frame(*frames[i])
+    out = st.step().cpu().numpy()
+    assert np.array_equal(st.buffer(1).cpu().numpy(), ref[0][2])
+    assert np.array_equal(out, ref[0][1])
+    st.close()
+
+
+def test_stabilizer_state_errors(vsc, cuda):
+    st = vsc.Stabilizer(32, 32)
+    f = np.zeros((32, 32, 4), np.uint8)
+    st.load_frame(f, f)
+    with pytest.raises(vsc.VscError, match="ESTATE"):
+        st.step()
+    st.load_frame(f, f)
+    st.load_frame(f, f)
+    with pytest.raises(vsc.VscError, match="ESTATE"):
+        st.load_frame(f, f)
+    st.hyper_params.pyramid_levels = 9
+    with pytest.raises(vsc.VscError, match="EINVAL"):
+        st.step()
+    st.hyper_params.pyramid_levels = 2
+    st.step()
+    st.close()
+
+
+def test_full_hd_step_deterministic(vsc, cuda):
+    """1920x1080 (the benchmark size): two stabilizers fed the same frames
+    give identical outputs and internal state."""
+    frames = _frames(1920, 1080, 4, seed=14)
+    outs = []
+    for _ in range(2):
+        st = vsc.Stabilizer(1920, 1080)
+        for i in range(3):
+            st.load_frame(*frames[i])
+        o1 = st.step()
+        st.load_frame(*frames[3])
+        o2 = st.step()
+        outs.append((o1.cpu().numpy(), o2.cpu().numpy(), st.buffer(0).cpu().numpy()))
+        st.close()
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
+    assert outs[0][1][..., 3].max() == 1

@@ -1,0 +1,340 @@
+"""Python front end of libvsc, the GB300 (sm_103a) implementation of the
+video-stream-consistency per-frame hot path.
+
+Everything here is a thin ctypes layer over the C ABI in include/vsc.h; the
+computation happens in the CUDA kernels of csrc/.  Device buffers are torch
+CUDA tensors (torch provides allocation and streams only).  There is no CPU
+fallback: if libvsc.so has not been built, every call raises.
+
+Names mirror the reference interfaces they replace:
+  correlation / warp          custom::Correlation / custom::Warp
+                              (src/ort_custom_ops/include/ort_custom_ops/opticalflow/*.h)
+  get_warp_result, get_adap_comb, get_consist_wt, get_bilinear,
+  get_consist_out             src/stabilization/flowconsistency.cuh:3-50
+  char_to_float_image, float_to_char_image
+                              src/stabilization/gpuimage.cu:70-135
+  Stabilizer                  VideoStabilizer (src/stabilization/videostabilizer.h:63-110)
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "libvsc.so"
+
+VSC_OK, VSC_EINVAL, VSC_ECUDA, VSC_ETIMEOUT, VSC_ENOMEM, VSC_EUNSUPPORTED, VSC_ESTATE = range(7)
+STATUS_NAMES = ["VSC_OK", "VSC_EINVAL", "VSC_ECUDA", "VSC_ETIMEOUT", "VSC_ENOMEM", "VSC_EUNSUPPORTED", "VSC_ESTATE"]
+
+# every symbol include/vsc.h declares (checked by the tests)
+EXPORTED = [
+    "vsc_last_error", "vsc_version", "vsc_correlation_fwd", "vsc_warp_fwd", "vsc_char_to_float_image",
+    "vsc_float_to_char_image", "vsc_get_warp_result", "vsc_get_adap_comb", "vsc_get_consist_wt",
+    "vsc_get_bilinear", "vsc_consist_out_workspace_size", "vsc_get_consist_out", "vsc_default_hyper_params",
+    "vsc_stabilizer_create", "vsc_stabilizer_destroy", "vsc_stabilizer_hyper_params", "vsc_stabilizer_load_frame",
+    "vsc_stabilizer_set_flows", "vsc_stabilizer_step", "vsc_stabilizer_buffer", "vsc_stabilizer_last_launches",
+]
+
+
+class VscError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        name = STATUS_NAMES[status] if 0 <= status < len(STATUS_NAMES) else str(status)
+        super().__init__(f"{name}: {message}")
+        self.status = status
+
+
+class Image(C.Structure):
+    """vsc_image: interleaved float HWC device image (GPUImageWrapper)."""
+
+    _fields_ = [("data", C.c_void_p), ("width", C.c_int32), ("height", C.c_int32), ("channels", C.c_int32)]
+
+
+class HyperParams(C.Structure):
+    """vsc_hyper_params (hyperParams, videostabilizer.h:38-46)."""
+
+    _fields_ = [
+        ("alpha", C.c_float), ("beta", C.c_float), ("gamma", C.c_float), ("pyramid_levels", C.c_int32),
+        ("num_iter", C.c_int32), ("step_size", C.c_float), ("mom_fac", C.c_float),
+    ]
+
+
+class StabilizerConfig(C.Structure):
+    _fields_ = [
+        ("width", C.c_int32), ("height", C.c_int32), ("batch_size", C.c_int32), ("compute_flow", C.c_int32),
+        ("flow_downscale", C.c_int32), ("flow_channels", C.c_int32),
+    ]
+
+
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    """Compile libvsc.so for sm_103a (see build.py)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("_vsc_build", PKG_DIR / "build.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)
+
+
+def load():
+    """Load libvsc.so; raises if it has not been built (no fallback path)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"libvsc.so not built ({LIB_PATH}); run the package build first")
+    L = C.CDLL(str(LIB_PATH))
+    vp, i32, i64, f32 = C.c_void_p, C.c_int32, C.c_int64, C.c_float
+    IP = C.POINTER(Image)
+    L.vsc_last_error.restype = C.c_char_p
+    L.vsc_last_error.argtypes = []
+    L.vsc_version.restype = C.c_int
+    for fn, args in {
+        "vsc_correlation_fwd": [vp, vp, vp, i64, i64, i64, i64, i64, i64, vp],
+        "vsc_warp_fwd": [vp, vp, vp, i64, i64, i64, i64, vp],
+        "vsc_char_to_float_image": [vp, IP, vp],
+        "vsc_float_to_char_image": [IP, vp, vp],
+        "vsc_get_warp_result": [IP, IP, IP, vp],
+        "vsc_get_adap_comb": [IP] * 9 + [f32, vp],
+        "vsc_get_consist_wt": [IP, IP, IP, f32, f32, vp],
+        "vsc_get_bilinear": [IP, IP, vp],
+        "vsc_get_consist_out": [IP, IP, IP, i32, f32, f32, IP, vp, C.c_size_t, vp],
+        "vsc_stabilizer_create": [C.POINTER(StabilizerConfig), vp, C.POINTER(vp)],
+        "vsc_stabilizer_destroy": [vp],
+        "vsc_stabilizer_load_frame": [vp, vp, vp, i32],
+        "vsc_stabilizer_set_flows": [vp, vp, vp, i32],
+        "vsc_stabilizer_step": [vp, vp, i32],
+        "vsc_stabilizer_buffer": [vp, i32, C.POINTER(vp)],
+    }.items():
+        f = getattr(L, fn)
+        f.argtypes = args
+        f.restype = C.c_int
+    L.vsc_consist_out_workspace_size.restype = C.c_size_t
+    L.vsc_consist_out_workspace_size.argtypes = [i32, i32]
+    L.vsc_default_hyper_params.restype = None
+    L.vsc_default_hyper_params.argtypes = [C.POINTER(HyperParams)]
+    L.vsc_stabilizer_hyper_params.restype = C.POINTER(HyperParams)
+    L.vsc_stabilizer_hyper_params.argtypes = [vp]
+    L.vsc_stabilizer_last_launches.restype = C.c_int32
+    L.vsc_stabilizer_last_launches.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def _check(status: int) -> None:
+    if status != VSC_OK:
+        raise VscError(status, load().vsc_last_error().decode())
+
+
+def _stream(stream=None):
+    import torch
+
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _f32(t, name):
+    import torch
+
+    if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()):
+        raise ValueError(f"{name}: expected a contiguous float32 CUDA tensor")
+    return t
+
+
+def image(t) -> Image:
+    """vsc_image view of a contiguous float32 CUDA tensor of shape (H, W, C)."""
+    _f32(t, "image")
+    h, w, c = t.shape
+    return Image(t.data_ptr(), w, h, c)
+
+
+# ---- custom ops ---------------------------------------------------------------
+
+def correlation(f1, f2, max_displacement: int = 4, legacy: int = 0, out=None, stream=None):
+    """custom::Correlation on N x C x H x W float tensors."""
+    import torch
+
+    _f32(f1, "f1")
+    _f32(f2, "f2")
+    N, Cc, H, W = f1.shape
+    P = 2 * max_displacement + 1
+    shape = (N, P * P, H, W) if legacy else (N, P, P, H, W)
+    if out is None:
+        out = torch.empty(shape, dtype=torch.float32, device=f1.device)
+    _check(load().vsc_correlation_fwd(f1.data_ptr(), f2.data_ptr(), out.data_ptr(), N, Cc, H, W,
+                                      max_displacement, legacy, _stream(stream)))
+    return out
+
+
+def warp(x, flow, out=None, stream=None):
+    """custom::Warp: x N x C x H x W, flow N x 2 x H x W."""
+    import torch
+
+    _f32(x, "input")
+    _f32(flow, "flow")
+    N, Cc, H, W = x.shape
+    if out is None:
+        out = torch.empty_like(x)
+    _check(load().vsc_warp_fwd(x.data_ptr(), flow.data_ptr(), out.data_ptr(), N, Cc, H, W, _stream(stream)))
+    return out
+
+
+# ---- stabilization kernels ----------------------------------------------------
+
+def char_to_float_image(rgba, stream=None):
+    import torch
+
+    h, w = rgba.shape[:2]
+    out = torch.empty((h, w, 3), dtype=torch.float32, device=rgba.device)
+    _check(load().vsc_char_to_float_image(rgba.data_ptr(), C.byref(image(out)), _stream(stream)))
+    return out
+
+
+def float_to_char_image(img, stream=None):
+    import torch
+
+    h, w = img.shape[:2]
+    out = torch.empty((h, w, 4), dtype=torch.uint8, device=img.device)
+    _check(load().vsc_float_to_char_image(C.byref(image(img)), out.data_ptr(), _stream(stream)))
+    return out
+
+
+def get_warp_result(inp, flow, stream=None):
+    import torch
+
+    out = torch.empty_like(inp)
+    _check(load().vsc_get_warp_result(C.byref(image(inp)), C.byref(image(flow)), C.byref(image(out)),
+                                      _stream(stream)))
+    return out
+
+
+def get_adap_comb(crnt_in, crnt_pr, prev_in, prev_pr, next_in, next_pr, last_stab_warp, alpha, stream=None):
+    import torch
+
+    ain = torch.empty_like(crnt_in)
+    apr = torch.empty_like(crnt_in)
+    ims = [image(t) for t in (crnt_in, crnt_pr, prev_in, prev_pr, next_in, next_pr, ain, apr, last_stab_warp)]
+    _check(load().vsc_get_adap_comb(*[C.byref(i) for i in ims], float(alpha), _stream(stream)))
+    return ain, apr
+
+
+def get_consist_wt(adap_in, crnt_in, beta, gamma, stream=None):
+    import torch
+
+    out = torch.empty_like(crnt_in)
+    _check(load().vsc_get_consist_wt(C.byref(image(adap_in)), C.byref(image(crnt_in)), C.byref(image(out)),
+                                     float(beta), float(gamma), _stream(stream)))
+    return out
+
+
+def get_bilinear(inp, ow: int, oh: int, stream=None):
+    import torch
+
+    out = torch.empty((oh, ow, inp.shape[2]), dtype=torch.float32, device=inp.device)
+    _check(load().vsc_get_bilinear(C.byref(image(inp)), C.byref(image(out)), _stream(stream)))
+    return out
+
+
+def consist_out_workspace_size(w: int, h: int) -> int:
+    return int(load().vsc_consist_out_workspace_size(w, h))
+
+
+def get_consist_out(crnt_pr, prev_stab_warp, cons_wt, num_iter, step_size, mom_fac, consis_out, workspace=None,
+                    stream=None):
+    """In place on consis_out (initial solution in, result out)."""
+    ws = workspace.data_ptr() if workspace is not None else None
+    nbytes = workspace.numel() * workspace.element_size() if workspace is not None else 0
+    _check(load().vsc_get_consist_out(C.byref(image(crnt_pr)), C.byref(image(prev_stab_warp)),
+                                      C.byref(image(cons_wt)), int(num_iter), float(step_size), float(mom_fac),
+                                      C.byref(image(consis_out)), ws, nbytes, _stream(stream)))
+    return consis_out
+
+
+def default_hyper_params() -> HyperParams:
+    hp = HyperParams()
+    load().vsc_default_hyper_params(C.byref(hp))
+    return hp
+
+
+class _DeviceView:
+    """Zero-copy view of library-owned device memory (float32), for torch.as_tensor."""
+
+    def __init__(self, ptr: int, shape):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": "<f4", "data": (ptr, False),
+                                         "version": 3, "strides": None}
+
+
+class Stabilizer:
+    """VideoStabilizer without Qt: feed RGBA frames, get stabilized RGBA frames.
+
+    compute_flow=True computes flows with the library's estimator (built on
+    the Correlation and Warp kernels); otherwise call set_flows before each
+    step.
+    """
+
+    def __init__(self, width, height, compute_flow=True, flow_downscale=1, flow_channels=3, stream=None):
+        import torch
+
+        self.width, self.height = width, height
+        self._stream_obj = stream if stream is not None else torch.cuda.current_stream()
+        cfg = StabilizerConfig(width, height, 1, 1 if compute_flow else 0, flow_downscale, flow_channels)
+        h = C.c_void_p()
+        _check(load().vsc_stabilizer_create(C.byref(cfg), _stream(self._stream_obj), C.byref(h)))
+        self._h = h
+
+    @property
+    def hyper_params(self) -> HyperParams:
+        return load().vsc_stabilizer_hyper_params(self._h).contents
+
+    def load_frame(self, orig_rgba, proc_rgba):
+        """orig/proc: uint8 (H, W, 4) tensors on the device, or numpy arrays / CPU tensors."""
+        import numpy as np
+
+        on_dev = 1 if getattr(orig_rgba, "is_cuda", False) else 0
+        if on_dev:
+            a, b = orig_rgba.data_ptr(), proc_rgba.data_ptr()
+        else:
+            oa = np.ascontiguousarray(orig_rgba if isinstance(orig_rgba, np.ndarray) else orig_rgba.numpy())
+            pa = np.ascontiguousarray(proc_rgba if isinstance(proc_rgba, np.ndarray) else proc_rgba.numpy())
+            self._keep = (oa, pa)
+            a, b = oa.ctypes.data, pa.ctypes.data
+        _check(load().vsc_stabilizer_load_frame(self._h, a, b, on_dev))
+
+    def set_flows(self, fwd, bwd):
+        _check(load().vsc_stabilizer_set_flows(self._h, fwd.data_ptr(), bwd.data_ptr(), 1 if fwd.is_cuda else 0))
+
+    def step(self, out=None):
+        """Stabilize the window's middle frame; returns the RGBA result."""
+        import torch
+
+        if out is None:
+            out = torch.empty((self.height, self.width, 4), dtype=torch.uint8, device="cuda")
+        _check(load().vsc_stabilizer_step(self._h, out.data_ptr(), 1 if out.is_cuda else 0))
+        return out
+
+    def buffer(self, which: int, channels: int = 3):
+        """Copy of internal state: 0 last stabilized, 1 fwd flow, 2 bwd flow, 3 adapCmbPr, 4 consWt."""
+        import torch
+
+        p = C.c_void_p()
+        _check(load().vsc_stabilizer_buffer(self._h, which, C.byref(p)))
+        self._stream_obj.synchronize()
+        view = _DeviceView(p.value, (self.height, self.width, channels))
+        return torch.as_tensor(view, device="cuda").clone()
+
+    @property
+    def last_launches(self) -> int:
+        return int(load().vsc_stabilizer_last_launches(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().vsc_stabilizer_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,725 @@
+// C ABI of the library (declared in include/vsc.h): argument validation,
+// error reporting, workspace handling and the per-frame orchestrator.
+//
+// The orchestrator mirrors VideoStabilizer (src/stabilization/
+// videostabilizer.{h,cpp}) without Qt: a 3-frame window (k = 1, batch 1) of
+// original and processed frames kept on the device as float HWC3, flows
+// either computed by the library's estimator or supplied by the caller, the
+// FP32 feedback of the previous stabilized frame, and the multi-scale solve.
+// All device memory is allocated once at creation; a step enqueues its
+// kernels on the stabilizer's stream and synchronises only when the caller
+// asked for the result in host memory.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "vsc_internal.h"
+
+namespace vsc {
+
+namespace {
+thread_local std::string g_err;
+}
+
+void clear_error() { g_err.clear(); }
+
+vsc_status set_error(vsc_status st, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return st;
+}
+
+vsc_status check_cuda(cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess)
+        return VSC_OK;
+    cudaGetLastError();  // clear a sticky launch-configuration error
+    return set_error(e == cudaErrorMemoryAllocation ? VSC_ENOMEM : VSC_ECUDA, "%s: %s (%d)", what,
+        cudaGetErrorString(e), static_cast<int>(e));
+}
+
+namespace {
+
+constexpr int64_t kMaxDim = 1 << 20;
+
+bool dims_ok(int64_t v) { return v > 0 && v <= kMaxDim; }
+
+vsc_status check_image(const vsc_image* im, const char* name, int channels_lo, int channels_hi)
+{
+    if (!im)
+        return set_error(VSC_EINVAL, "%s: null image descriptor", name);
+    if (!im->data)
+        return set_error(VSC_EINVAL, "%s: null data pointer", name);
+    if (!dims_ok(im->width) || !dims_ok(im->height))
+        return set_error(VSC_EINVAL, "%s: invalid size %dx%d", name, im->width, im->height);
+    if (im->channels < channels_lo || im->channels > channels_hi)
+        return set_error(VSC_EINVAL, "%s: %d channels (expected %d..%d)", name, im->channels, channels_lo,
+            channels_hi);
+    return VSC_OK;
+}
+
+vsc_status same_size(const vsc_image* a, const vsc_image* b, const char* name)
+{
+    if (a->width != b->width || a->height != b->height)
+        return set_error(VSC_EINVAL, "%s: size %dx%d differs from %dx%d", name, b->width, b->height, a->width,
+            a->height);
+    return VSC_OK;
+}
+
+Img img(const vsc_image* i) { return Img{i->data, i->width, i->height, i->channels}; }
+
+cudaStream_t cs(vsc_stream_t s) { return static_cast<cudaStream_t>(s); }
+
+// Private stream-ordered pool per device for workspaces the caller did not provide.
+cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t st)
+{
+    static std::mutex mu;
+    static cudaMemPool_t pools[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    if (dev < 0 || dev >= 64)
+        return cudaErrorInvalidDevice;
+    cudaMemPool_t pool;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!pools[dev]) {
+            cudaMemPoolProps props;
+            std::memset(&props, 0, sizeof(props));
+            props.allocType = cudaMemAllocationTypePinned;
+            props.handleTypes = cudaMemHandleTypeNone;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            e = cudaMemPoolCreate(&pools[dev], &props);
+            if (e != cudaSuccess)
+                return e;
+            uint64_t keep = ~0ULL;
+            cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        pool = pools[dev];
+    }
+    return cudaMallocFromPoolAsync(p, bytes, pool, st);
+}
+
+}  // namespace
+}  // namespace vsc
+
+using namespace vsc;
+
+extern "C" {
+
+VSC_API const char* vsc_last_error(void) { return vsc::g_err.c_str(); }
+
+VSC_API int vsc_version(void) { return 100; }
+
+// ---- ops ------------------------------------------------------------------
+
+VSC_API vsc_status vsc_correlation_fwd(const float* f1, const float* f2, float* out, int64_t N, int64_t C, int64_t H,
+    int64_t W, int64_t max_displacement, int64_t legacy, vsc_stream_t stream)
+{
+    clear_error();
+    if (!f1 || !f2 || !out)
+        return set_error(VSC_EINVAL, "correlation: null pointer");
+    if (!dims_ok(N) || !dims_ok(C) || !dims_ok(H) || !dims_ok(W))
+        return set_error(VSC_EINVAL, "correlation: invalid shape %lldx%lldx%lldx%lld", (long long)N, (long long)C,
+            (long long)H, (long long)W);
+    if (max_displacement < 0 || max_displacement > 32)
+        return set_error(VSC_EINVAL, "correlation: max_displacement %lld outside [0, 32]", (long long)max_displacement);
+    if (legacy != 0 && legacy != 1)
+        return set_error(VSC_EINVAL, "correlation: legacy must be 0 or 1");
+    if (N > 65535 || H * W > (int64_t(1) << 31) / 4)
+        return set_error(VSC_EINVAL, "correlation: shape too large");
+    return check_cuda(launch_correlation(f1, f2, out, (int)N, (int)C, (int)H, (int)W, (int)max_displacement,
+                          (int)legacy, cs(stream)),
+        "correlation launch");
+}
+
+VSC_API vsc_status vsc_warp_fwd(const float* input, const float* flow, float* out, int64_t N, int64_t C, int64_t H,
+    int64_t W, vsc_stream_t stream)
+{
+    clear_error();
+    if (!input || !flow || !out)
+        return set_error(VSC_EINVAL, "warp: null pointer");
+    if (!dims_ok(N) || !dims_ok(C) || !dims_ok(H) || !dims_ok(W))
+        return set_error(VSC_EINVAL, "warp: invalid shape %lldx%lldx%lldx%lld", (long long)N, (long long)C,
+            (long long)H, (long long)W);
+    if (N > 65535 || (C + 7) / 8 > 65535 || H * W > (int64_t(1) << 31))
+        return set_error(VSC_EINVAL, "warp: shape too large");
+    return check_cuda(launch_warp_op(input, flow, out, (int)N, (int)C, (int)H, (int)W, cs(stream)), "warp launch");
+}
+
+// ---- stabilization kernels -------------------------------------------------
+
+VSC_API vsc_status vsc_char_to_float_image(const uint8_t* rgba, const vsc_image* out, vsc_stream_t stream)
+{
+    clear_error();
+    vsc_status s = check_image(out, "out", 3, 3);
+    if (s)
+        return s;
+    if (!rgba || (reinterpret_cast<uintptr_t>(rgba) & 3))
+        return set_error(VSC_EINVAL, "rgba: null or not 4-byte aligned");
+    return check_cuda(launch_rgba_to_float(rgba, out->data, (int64_t)out->width * out->height, cs(stream)),
+        "to_float launch");
+}
+
+VSC_API vsc_status vsc_float_to_char_image(const vsc_image* in, uint8_t* rgba, vsc_stream_t stream)
+{
+    clear_error();
+    vsc_status s = check_image(in, "in", 3, 3);
+    if (s)
+        return s;
+    if (!rgba || (reinterpret_cast<uintptr_t>(rgba) & 3))
+        return set_error(VSC_EINVAL, "rgba: null or not 4-byte aligned");
+    return check_cuda(launch_float_to_rgba(in->data, rgba, (int64_t)in->width * in->height, cs(stream)),
+        "to_char launch");
+}
+
+VSC_API vsc_status vsc_get_warp_result(const vsc_image* input, const vsc_image* flow, const vsc_image* input_warp,
+    vsc_stream_t stream)
+{
+    clear_error();
+    vsc_status s;
+    if ((s = check_image(input, "input", 3, 3)) || (s = check_image(flow, "flow", 2, 3)) ||
+        (s = check_image(input_warp, "input_warp", 3, 3)) || (s = same_size(input, flow, "flow")) ||
+        (s = same_size(input, input_warp, "input_warp")))
+        return s;
+    if (input->width < 2 || input->height < 2)
+        return set_error(VSC_EINVAL, "warp_result: image must be at least 2x2");
+    return check_cuda(launch_stab_warp(img(input), img(flow), img(input_warp), cs(stream)), "warp_result launch");
+}
+
+VSC_API vsc_status vsc_get_adap_comb(const vsc_image* crnt_in, const vsc_image* crnt_pr, const vsc_image* prev_warp_in,
+    const vsc_image* prev_warp_pr, const vsc_image* next_warp_in, const vsc_image* next_warp_pr,
+    const vsc_image* adap_cmb_in, const vsc_image* adap_cmb_pr, const vsc_image* last_stab_warp, float alpha,
+    vsc_stream_t stream)
+{
+    clear_error();
+    const vsc_image* all[9] = {crnt_in, crnt_pr, prev_warp_in, prev_warp_pr, next_warp_in, next_warp_pr, adap_cmb_in,
+        adap_cmb_pr, last_stab_warp};
+    static const char* names[9] = {"crntIn", "crntPr", "prevWarpIn", "prevWarpPr", "nextWarpIn", "nextWarpPr",
+        "adapCmbIn", "adapCmbPr", "lastStabWarp"};
+    for (int i = 0; i < 9; ++i) {
+        vsc_status s = check_image(all[i], names[i], 3, 3);
+        if (s)
+            return s;
+        if ((s = same_size(crnt_in, all[i], names[i])))
+            return s;
+    }
+    return check_cuda(launch_adap_comb(img(crnt_in), img(crnt_pr), img(prev_warp_in), img(prev_warp_pr),
+                          img(next_warp_in), img(next_warp_pr), img(adap_cmb_in), img(adap_cmb_pr),
+                          img(last_stab_warp), alpha, cs(stream)),
+        "adap_comb launch");
+}
+
+VSC_API vsc_status vsc_get_consist_wt(const vsc_image* adap_cmb_in, const vsc_image* crnt_in,
+    const vsc_image* consis_wt, float beta, float gamma, vsc_stream_t stream)
+{
+    clear_error();
+    vsc_status s;
+    if ((s = check_image(adap_cmb_in, "adapCmbIn", 3, 3)) || (s = check_image(crnt_in, "crntIn", 3, 3)) ||
+        (s = check_image(consis_wt, "consisWt", 3, 3)) || (s = same_size(crnt_in, adap_cmb_in, "adapCmbIn")) ||
+        (s = same_size(crnt_in, consis_wt, "consisWt")))
+        return s;
+    return check_cuda(
+        launch_consist_wt(img(adap_cmb_in), img(crnt_in), img(consis_wt), beta, gamma, cs(stream)),
+        "consist_wt launch");
+}
+
+VSC_API vsc_status vsc_get_bilinear(const vsc_image* input, const vsc_image* output, vsc_stream_t stream)
+{
+    clear_error();
+    vsc_status s;
+    if ((s = check_image(input, "input", 1, 4)) || (s = check_image(output, "output", 1, 4)))
+        return s;
+    if (input->channels != output->channels)
+        return set_error(VSC_EINVAL, "bilinear: channel count differs (%d vs %d)", input->channels,
+            output->channels);
+    return check_cuda(launch_bilinear(img(input), img(output), cs(stream)), "bilinear launch");
+}
+
+VSC_API size_t vsc_consist_out_workspace_size(int32_t width, int32_t height)
+{
+    if (!dims_ok(width) || !dims_ok(height))
+        return 0;
+    return solver_workspace_floats(width, height) * sizeof(float);
+}
+
+VSC_API vsc_status vsc_get_consist_out(const vsc_image* crnt_pr, const vsc_image* prev_stab_warp,
+    const vsc_image* cons_wt, int32_t num_iter, float step_size, float mom_fac, const vsc_image* consis_out,
+    void* workspace, size_t workspace_bytes, vsc_stream_t stream)
+{
+    clear_error();
+    vsc_status s;
+    if ((s = check_image(crnt_pr, "crntPr", 3, 3)) || (s = check_image(prev_stab_warp, "prevStabWarp", 3, 3)) ||
+        (s = check_image(cons_wt, "consWt", 3, 3)) || (s = check_image(consis_out, "consisOut", 3, 3)) ||
+        (s = same_size(consis_out, crnt_pr, "crntPr")) || (s = same_size(consis_out, prev_stab_warp, "prevStabWarp")) ||
+        (s = same_size(consis_out, cons_wt, "consWt")))
+        return s;
+    if (num_iter < 0)
+        return set_error(VSC_EINVAL, "consist_out: negative iteration count");
+    const int w = consis_out->width, h = consis_out->height;
+    const size_t need = vsc_consist_out_workspace_size(w, h);
+    void* ws = workspace;
+    bool pooled = false;
+    if (ws) {
+        if (workspace_bytes < need)
+            return set_error(VSC_ENOMEM, "consist_out: workspace of %zu bytes, need %zu", workspace_bytes, need);
+        if (reinterpret_cast<uintptr_t>(ws) & 15)
+            return set_error(VSC_EINVAL, "consist_out: workspace not 16-byte aligned");
+    } else if (num_iter > 0) {
+        if ((s = check_cuda(pool_alloc(&ws, need, cs(stream)), "consist_out workspace")))
+            return s;
+        pooled = true;
+    }
+    cudaError_t e = run_solver(crnt_pr->data, prev_stab_warp->data, cons_wt->data, consis_out->data, w, h, num_iter,
+        step_size, mom_fac, static_cast<float*>(ws), cs(stream), nullptr);
+    if (pooled)
+        cudaFreeAsync(ws, cs(stream));
+    return check_cuda(e, "consist_out launch");
+}
+
+VSC_API void vsc_default_hyper_params(vsc_hyper_params* hp)
+{
+    if (!hp)
+        return;
+    hp->alpha = 6800.0f;
+    hp->beta = 6800.0f;
+    hp->gamma = 2.0f;
+    hp->pyramid_levels = 2;
+    hp->num_iter = 150;
+    hp->step_size = 0.15f;
+    hp->mom_fac = 0.15f;
+}
+
+}  // extern "C"
+
+// ---- orchestrator -----------------------------------------------------------
+
+struct vsc_stabilizer {
+    int w = 0, h = 0, fc = 3;
+    bool compute_flow = true;
+    int downscale = 1, fw = 0, fh = 0;  // flow size
+    int device = 0;
+    cudaStream_t st = nullptr;
+    vsc_hyper_params hp{};
+    int levels_alloc = 0;
+
+    float* orig[3] = {};
+    float* proc[3] = {};
+    float* feat[3] = {};
+    int head = 0, count = 0;
+    bool started = false;
+    bool flows_set = false;
+
+    uint8_t* stage[2] = {};  // device staging for host RGBA uploads
+    uint8_t* out_rgba = nullptr;
+    float* small = nullptr;  // frame resized to the flow size (downscale mode)
+    float* flow_fwd = nullptr;
+    float* flow_bwd = nullptr;
+    float* flow_small = nullptr;  // flow at the flow size before upsampling
+    float* last_stab[2] = {};
+    int ls_cur = 0;
+    float* adap_pr = nullptr;
+    float* cons_wt = nullptr;
+    float* pyrP[8] = {};
+    float* pyrA[8] = {};
+    float* pyrW[8] = {};
+    float* pyrO[8] = {};
+    int lw[8] = {}, lh[8] = {};
+    float* solver_ws = nullptr;
+    float* feat_scratch = nullptr;
+    float* flow_scratch = nullptr;
+    FlowDims fd{};
+    int last_launches = 0;
+    bool ok = true;
+};
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev)
+            cudaSetDevice(dev);
+        else
+            prev = -1;
+    }
+    ~DeviceGuard()
+    {
+        if (prev >= 0)
+            cudaSetDevice(prev);
+    }
+};
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t elems)
+{
+    return cudaMalloc(reinterpret_cast<void**>(p), std::max<size_t>(elems, 1) * sizeof(T));
+}
+
+void free_all(vsc_stabilizer* s)
+{
+    auto f = [](void* p) {
+        if (p)
+            cudaFree(p);
+    };
+    for (int i = 0; i < 3; ++i) {
+        f(s->orig[i]);
+        f(s->proc[i]);
+        f(s->feat[i]);
+    }
+    f(s->stage[0]);
+    f(s->stage[1]);
+    f(s->out_rgba);
+    f(s->small);
+    f(s->flow_fwd);
+    f(s->flow_bwd);
+    f(s->flow_small);
+    f(s->last_stab[0]);
+    f(s->last_stab[1]);
+    f(s->adap_pr);
+    f(s->cons_wt);
+    for (int j = 0; j < 8; ++j) {
+        f(s->pyrP[j]);
+        f(s->pyrA[j]);
+        f(s->pyrW[j]);
+        f(s->pyrO[j]);
+    }
+    f(s->solver_ws);
+    f(s->feat_scratch);
+    f(s->flow_scratch);
+}
+
+vsc_status alloc_all(vsc_stabilizer* s)
+{
+    const size_t n3 = static_cast<size_t>(s->w) * s->h * 3;
+    cudaError_t e = cudaSuccess;
+    auto A = [&](cudaError_t r) {
+        if (e == cudaSuccess)
+            e = r;
+    };
+    for (int i = 0; i < 3; ++i) {
+        A(dalloc(&s->orig[i], n3));
+        A(dalloc(&s->proc[i], n3));
+    }
+    A(dalloc(&s->stage[0], static_cast<size_t>(s->w) * s->h * 4));
+    A(dalloc(&s->stage[1], static_cast<size_t>(s->w) * s->h * 4));
+    A(dalloc(&s->out_rgba, static_cast<size_t>(s->w) * s->h * 4));
+    A(dalloc(&s->flow_fwd, static_cast<size_t>(s->w) * s->h * s->fc));
+    A(dalloc(&s->flow_bwd, static_cast<size_t>(s->w) * s->h * s->fc));
+    A(dalloc(&s->last_stab[0], n3));
+    A(dalloc(&s->last_stab[1], n3));
+    A(dalloc(&s->adap_pr, n3));
+    A(dalloc(&s->cons_wt, n3));
+    s->levels_alloc = 8;
+    s->lw[0] = s->w;
+    s->lh[0] = s->h;
+    for (int j = 1; j < 8; ++j) {
+        s->lw[j] = s->lw[j - 1] / 2;
+        s->lh[j] = s->lh[j - 1] / 2;
+    }
+    for (int j = 1; j < 8; ++j) {
+        if (s->lw[j] < 2 || s->lh[j] < 2) {
+            s->levels_alloc = j;
+            break;
+        }
+        const size_t m = static_cast<size_t>(s->lw[j]) * s->lh[j] * 3;
+        A(dalloc(&s->pyrP[j], m));
+        A(dalloc(&s->pyrA[j], m));
+        A(dalloc(&s->pyrW[j], m));
+        A(dalloc(&s->pyrO[j], m));
+    }
+    A(dalloc(&s->solver_ws, solver_workspace_floats(s->w, s->h)));
+    if (s->compute_flow) {
+        s->fd = flow_dims(s->fw, s->fh);
+        for (int i = 0; i < 3; ++i)
+            A(dalloc(&s->feat[i], s->fd.feat_floats));
+        A(dalloc(&s->feat_scratch, flow_feature_scratch_floats(s->fd)));
+        A(dalloc(&s->flow_scratch, flow_estimate_scratch_floats(s->fd)));
+        if (s->downscale > 1) {
+            A(dalloc(&s->small, static_cast<size_t>(s->fw) * s->fh * 3));
+            A(dalloc(&s->flow_small, static_cast<size_t>(s->fw) * s->fh * 3));
+        }
+        A(flow_upload_weights());
+    }
+    return check_cuda(e, "stabilizer allocation");
+}
+
+}  // namespace
+
+extern "C" {
+
+VSC_API vsc_status vsc_stabilizer_create(const vsc_stabilizer_config* cfg, vsc_stream_t stream, vsc_stabilizer** out)
+{
+    clear_error();
+    if (!cfg || !out)
+        return set_error(VSC_EINVAL, "stabilizer_create: null argument");
+    *out = nullptr;
+    if (cfg->width < 8 || cfg->height < 8 || cfg->width > 16384 || cfg->height > 16384)
+        return set_error(VSC_EINVAL, "stabilizer_create: size %dx%d outside [8, 16384]", cfg->width, cfg->height);
+    if (cfg->batch_size != 1)
+        return set_error(VSC_EUNSUPPORTED, "stabilizer_create: batch_size %d (only 1 is supported)", cfg->batch_size);
+    if (cfg->flow_downscale < 1 || cfg->flow_downscale > 8)
+        return set_error(VSC_EINVAL, "stabilizer_create: flow_downscale %d outside [1, 8]", cfg->flow_downscale);
+    if (!cfg->compute_flow && cfg->flow_channels != 2 && cfg->flow_channels != 3)
+        return set_error(VSC_EINVAL, "stabilizer_create: flow_channels must be 2 or 3");
+    vsc_stabilizer* s = new (std::nothrow) vsc_stabilizer();
+    if (!s)
+        return set_error(VSC_ENOMEM, "stabilizer_create: out of host memory");
+    s->w = cfg->width;
+    s->h = cfg->height;
+    s->compute_flow = cfg->compute_flow != 0;
+    s->fc = s->compute_flow ? 3 : cfg->flow_channels;
+    s->downscale = s->compute_flow ? cfg->flow_downscale : 1;
+    // videostabilizer.cpp:92-94: round(width / factor)
+    s->fw = static_cast<int>(std::lround(static_cast<float>(s->w) / static_cast<float>(s->downscale)));
+    s->fh = static_cast<int>(std::lround(static_cast<float>(s->h) / static_cast<float>(s->downscale)));
+    s->st = cs(stream);
+    cudaGetDevice(&s->device);
+    vsc_default_hyper_params(&s->hp);
+    vsc_status st = alloc_all(s);
+    if (st != VSC_OK) {
+        free_all(s);
+        delete s;
+        return st;
+    }
+    *out = s;
+    return VSC_OK;
+}
+
+VSC_API vsc_status vsc_stabilizer_destroy(vsc_stabilizer* s)
+{
+    clear_error();
+    if (!s)
+        return VSC_OK;
+    DeviceGuard g(s->device);
+    cudaStreamSynchronize(s->st);
+    free_all(s);
+    delete s;
+    return VSC_OK;
+}
+
+VSC_API vsc_hyper_params* vsc_stabilizer_hyper_params(vsc_stabilizer* s) { return s ? &s->hp : nullptr; }
+
+VSC_API vsc_status vsc_stabilizer_load_frame(vsc_stabilizer* s, const uint8_t* orig_rgba, const uint8_t* proc_rgba,
+    int32_t on_device)
+{
+    clear_error();
+    if (!s || !orig_rgba || !proc_rgba)
+        return set_error(VSC_EINVAL, "load_frame: null argument");
+    if (s->count >= 3)
+        return set_error(VSC_ESTATE, "load_frame: window full; call vsc_stabilizer_step first");
+    if (on_device && ((reinterpret_cast<uintptr_t>(orig_rgba) & 3) || (reinterpret_cast<uintptr_t>(proc_rgba) & 3)))
+        return set_error(VSC_EINVAL, "load_frame: device frames must be 4-byte aligned");
+    DeviceGuard g(s->device);
+    const int slot = (s->head + s->count) % 3;
+    const int64_t npix = static_cast<int64_t>(s->w) * s->h;
+    const uint8_t* src[2] = {orig_rgba, proc_rgba};
+    float* dst[2] = {s->orig[slot], s->proc[slot]};
+    int nl = 0;
+    for (int k = 0; k < 2; ++k) {
+        const uint8_t* dsrc = src[k];
+        if (!on_device) {
+            vsc_status st = check_cuda(cudaMemcpyAsync(s->stage[k], src[k], static_cast<size_t>(npix) * 4,
+                                           cudaMemcpyHostToDevice, s->st),
+                "load_frame upload");
+            if (st)
+                return st;
+            dsrc = s->stage[k];
+        }
+        vsc_status st = check_cuda(launch_rgba_to_float(dsrc, dst[k], npix, s->st), "load_frame convert");
+        if (st)
+            return st;
+        ++nl;
+    }
+    if (s->compute_flow) {
+        const float* fimg = s->orig[slot];
+        if (s->downscale > 1) {
+            vsc_status st = check_cuda(launch_resize_nearest(s->orig[slot], s->w, s->h, s->small, s->fw, s->fh, s->st),
+                "load_frame resize");
+            if (st)
+                return st;
+            ++nl;
+            fimg = s->small;
+        }
+        vsc_status st = check_cuda(
+            launch_flow_features(fimg, s->fw, s->fh, s->fd, s->feat[slot], s->feat_scratch, s->st, &nl),
+            "load_frame features");
+        if (st)
+            return st;
+    }
+    s->count += 1;
+    s->last_launches = nl;
+    return VSC_OK;
+}
+
+VSC_API vsc_status vsc_stabilizer_set_flows(vsc_stabilizer* s, const float* fwd, const float* bwd, int32_t on_device)
+{
+    clear_error();
+    if (!s || !fwd || !bwd)
+        return set_error(VSC_EINVAL, "set_flows: null argument");
+    if (s->compute_flow)
+        return set_error(VSC_ESTATE, "set_flows: this stabilizer computes its own flow");
+    DeviceGuard g(s->device);
+    const size_t bytes = static_cast<size_t>(s->w) * s->h * s->fc * sizeof(float);
+    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    vsc_status st = check_cuda(cudaMemcpyAsync(s->flow_fwd, fwd, bytes, kind, s->st), "set_flows fwd");
+    if (st)
+        return st;
+    st = check_cuda(cudaMemcpyAsync(s->flow_bwd, bwd, bytes, kind, s->st), "set_flows bwd");
+    if (st)
+        return st;
+    s->flows_set = true;
+    return VSC_OK;
+}
+
+VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int32_t out_on_device)
+{
+    clear_error();
+    if (!s)
+        return set_error(VSC_EINVAL, "step: null stabilizer");
+    if (s->count < 3)
+        return set_error(VSC_ESTATE, "step: window holds %d of 3 frames", s->count);
+    if (!s->compute_flow && !s->flows_set)
+        return set_error(VSC_ESTATE, "step: flows not set for this step");
+    const vsc_hyper_params hp = s->hp;
+    const int L = hp.pyramid_levels;
+    if (L < 1 || L > s->levels_alloc)
+        return set_error(VSC_EINVAL, "step: pyramid_levels %d outside [1, %d]", L, s->levels_alloc);
+    if (hp.num_iter < 0)
+        return set_error(VSC_EINVAL, "step: negative num_iter");
+    if (out_rgba && out_on_device && (reinterpret_cast<uintptr_t>(out_rgba) & 3))
+        return set_error(VSC_EINVAL, "step: device output must be 4-byte aligned");
+    DeviceGuard g(s->device);
+    const int s0 = s->head, s1 = (s->head + 1) % 3, s2 = (s->head + 2) % 3;
+    const size_t n3b = static_cast<size_t>(s->w) * s->h * 3 * sizeof(float);
+    cudaStream_t st = s->st;
+    int nl = 0;
+    cudaError_t e = cudaSuccess;
+    auto run = [&](cudaError_t r) {
+        if (e == cudaSuccess)
+            e = r;
+    };
+
+    // preloadProcessedFrames (videostabilizer.cpp:152): the first previous
+    // stabilized frame is the processed image of the last preloaded frame.
+    if (!s->started)
+        run(cudaMemcpyAsync(s->last_stab[s->ls_cur], s->proc[s2], n3b, cudaMemcpyDeviceToDevice, st));
+
+    // retrieveOpticalFlow (videostabilizer.cpp:267-279): forward flow runs
+    // frame pair (t, t+1); the "backward" flow runs (t+1, t) (flowmodel.cpp:139-143).
+    if (s->compute_flow) {
+        float* ff = s->downscale > 1 ? s->flow_small : s->flow_fwd;
+        run(launch_flow_from_features(s->feat[s1], s->feat[s2], s->fw, s->fh, s->fd, ff, s->flow_scratch, st, &nl));
+        if (s->downscale > 1) {
+            run(launch_bilinear(Img{s->flow_small, s->fw, s->fh, 3}, Img{s->flow_fwd, s->w, s->h, 3}, st));
+            ++nl;
+        }
+        float* fb = s->downscale > 1 ? s->flow_small : s->flow_bwd;
+        run(launch_flow_from_features(s->feat[s2], s->feat[s1], s->fw, s->fh, s->fd, fb, s->flow_scratch, st, &nl));
+        if (s->downscale > 1) {
+            run(launch_bilinear(Img{s->flow_small, s->fw, s->fh, 3}, Img{s->flow_bwd, s->w, s->h, 3}, st));
+            ++nl;
+        }
+    }
+
+    float* ls_in = s->last_stab[s->ls_cur];
+    float* ls_out = s->last_stab[s->ls_cur ^ 1];
+    run(launch_fused_front(s->orig[s0], s->orig[s1], s->orig[s2], s->proc[s0], s->proc[s1], s->proc[s2], ls_in,
+        s->flow_fwd, s->flow_bwd, s->fc, s->adap_pr, s->cons_wt, s->w, s->h, hp.alpha, hp.beta, hp.gamma, st));
+    ++nl;
+
+    // pyramid (videostabilizer.cpp:203-217)
+    float* P[8];
+    float* A[8];
+    float* W[8];
+    float* O[8];
+    P[0] = s->proc[s1];
+    A[0] = s->adap_pr;
+    W[0] = s->cons_wt;
+    O[0] = ls_out;
+    for (int j = 1; j < L; ++j) {
+        P[j] = s->pyrP[j];
+        A[j] = s->pyrA[j];
+        W[j] = s->pyrW[j];
+        O[j] = s->pyrO[j];
+        run(launch_pyr_down3(P[j - 1], A[j - 1], W[j - 1], s->lw[j - 1], s->lh[j - 1], P[j], A[j], W[j], s->lw[j],
+            s->lh[j], st));
+        ++nl;
+    }
+    // The solution is initialised with the processed frame and carried down
+    // with the same bilinear chain, so at the coarsest level it equals P.
+    run(cudaMemcpyAsync(O[L - 1], P[L - 1], static_cast<size_t>(s->lw[L - 1]) * s->lh[L - 1] * 3 * sizeof(float),
+        cudaMemcpyDeviceToDevice, st));
+    uint8_t* rgba_dev = (out_rgba && out_on_device) ? out_rgba : s->out_rgba;
+    for (int j = L - 1; j >= 0; --j) {
+        if (j != L - 1) {
+            run(launch_bilinear(Img{O[j + 1], s->lw[j + 1], s->lh[j + 1], 3}, Img{O[j], s->lw[j], s->lh[j], 3}, st));
+            ++nl;
+        }
+        run(run_solver(P[j], A[j], W[j], O[j], s->lw[j], s->lh[j], hp.num_iter / (j + 1), hp.step_size, hp.mom_fac,
+            s->solver_ws, st, &nl, j == 0 ? rgba_dev : nullptr));
+    }
+    vsc_status stt = check_cuda(e, "step");
+    if (stt)
+        return stt;
+    s->ls_cur ^= 1;
+    s->started = true;
+    s->flows_set = false;
+    s->head = (s->head + 1) % 3;
+    s->count -= 1;
+    s->last_launches = nl;
+    if (out_rgba && !out_on_device) {
+        stt = check_cuda(cudaMemcpyAsync(out_rgba, s->out_rgba, static_cast<size_t>(s->w) * s->h * 4,
+                             cudaMemcpyDeviceToHost, st),
+            "step download");
+        if (stt)
+            return stt;
+        return check_cuda(cudaStreamSynchronize(st), "step synchronize");
+    }
+    return VSC_OK;
+}
+
+VSC_API vsc_status vsc_stabilizer_buffer(vsc_stabilizer* s, int32_t which, const float** dev_ptr)
+{
+    clear_error();
+    if (!s || !dev_ptr)
+        return set_error(VSC_EINVAL, "buffer: null argument");
+    switch (which) {
+        case 0:
+            *dev_ptr = s->last_stab[s->ls_cur];
+            return VSC_OK;
+        case 1:
+            *dev_ptr = s->flow_fwd;
+            return VSC_OK;
+        case 2:
+            *dev_ptr = s->flow_bwd;
+            return VSC_OK;
+        case 3:
+            *dev_ptr = s->adap_pr;
+            return VSC_OK;
+        case 4:
+            *dev_ptr = s->cons_wt;
+            return VSC_OK;
+        default:
+            return set_error(VSC_EINVAL, "buffer: unknown buffer %d", which);
+    }
+}
+
+VSC_API int32_t vsc_stabilizer_last_launches(vsc_stabilizer* s) { return s ? s->last_launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,462 @@
+// Weight-free optical-flow estimator built from the two operators.
+//
+// The reference computes flow with a PWC-Net ONNX graph that calls
+// custom::Warp and custom::Correlation (model-conversion/pwc_pytorch/
+// pwcnet.py:418-430, :950-967; src/stabilization/flowmodel.cpp:121-168).
+// Its trained weights are not part of the reference tree, so this module
+// keeps the graph's operator skeleton and replaces the learned parts:
+//   pyramid   : 1/4 .. 1/64 of the frame resized to a multiple of 64
+//               (convert_onnx.py:15-20), channels {32, 64, 96, 128, 196};
+//   features  : L2-normalised random projections of 3x3 RGB patches made
+//               zero-mean per colour (weights from a splitmix64 stream
+//               seeded per level): correlations are patch NCCs;
+//   per level : upsample the coarser flow (x2), Warp the second frame's
+//               features by it, Correlation (max displacement 4) against the
+//               first frame's features, arg-max over the 81 displacements
+//               minus a small-displacement prior, soft 3x3 centroid, and a
+//               confidence-weighted 3x3 mean of the refinement;
+//   output    : bilinear upsampling of the 1/4-level flow to the frame size,
+//               3-channel (u, v, 0) like the reference's computed flows.
+// All arithmetic follows the CPU restatement operation for operation
+// (-fmad=false), so the estimated flow matches it bit for bit.
+#include "vsc_internal.h"
+#include "vsc_math.cuh"
+
+#include <algorithm>
+#include <mutex>
+
+namespace vsc {
+namespace {
+
+constexpr int kLevelC[kFlowLevels] = {32, 64, 96, 128, 196};
+constexpr int kWeightOff[kFlowLevels] = {0, 32 * 27, 96 * 27, 192 * 27, 320 * 27};
+constexpr int kWeightTotal = 516 * 27;
+// decoder constants: soft-centroid sharpness, confidence floor of the
+// smoothing, small-displacement prior per level (x4 per coarser level)
+constexpr float kTemp = 20.0f;
+constexpr float kEps = 0.1f;
+constexpr float kLevelPrior[kFlowLevels] = {0.01f, 0.01f * 4.0f, 0.01f * 16.0f, 0.01f * 64.0f, 0.01f * 256.0f};
+
+__constant__ float c_flow_w[kWeightTotal];
+
+uint64_t splitmix64(uint64_t* s)
+{
+    uint64_t z = (*s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// bilinear sample with half-pixel centres (align_corners = False), 3 channels
+__device__ __forceinline__ void sample_hp3(const float* __restrict__ src, int sw, int sh, float sx, float sy,
+    float* res)
+{
+    if (sx < 0.0f)
+        sx = 0.0f;
+    if (sy < 0.0f)
+        sy = 0.0f;
+    int x0 = static_cast<int>(floorf(sx)), y0 = static_cast<int>(floorf(sy));
+    if (x0 > sw - 1)
+        x0 = sw - 1;
+    if (y0 > sh - 1)
+        y0 = sh - 1;
+    const int x1 = x0 + 1 < sw ? x0 + 1 : sw - 1;
+    const int y1 = y0 + 1 < sh ? y0 + 1 : sh - 1;
+    const float lx = sx - static_cast<float>(x0), ly = sy - static_cast<float>(y0);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float v00 = src[(static_cast<int64_t>(y0) * sw + x0) * 3 + k];
+        const float v01 = src[(static_cast<int64_t>(y0) * sw + x1) * 3 + k];
+        const float v10 = src[(static_cast<int64_t>(y1) * sw + x0) * 3 + k];
+        const float v11 = src[(static_cast<int64_t>(y1) * sw + x1) * 3 + k];
+        const float top = (1.0f - lx) * v00 + lx * v01;
+        const float bot = (1.0f - lx) * v10 + lx * v11;
+        res[k] = (1.0f - ly) * top + ly * bot;
+    }
+}
+
+__global__ void level0_image_kernel(const float* __restrict__ img, int w, int h, float* __restrict__ lev, int lw,
+    int lh)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= lw || y >= lh)
+        return;
+    const int pw = lw * 4, ph = lh * 4;
+    const float scx = static_cast<float>(w) / static_cast<float>(pw);
+    const float scy = static_cast<float>(h) / static_cast<float>(ph);
+    float acc[3] = {0.0f, 0.0f, 0.0f};
+    for (int j = 0; j < 4; ++j) {
+        const float sy = (static_cast<float>(y * 4 + j) + 0.5f) * scy - 0.5f;
+        for (int i = 0; i < 4; ++i) {
+            const float sx = (static_cast<float>(x * 4 + i) + 0.5f) * scx - 0.5f;
+            float v[3];
+            sample_hp3(img, w, h, sx, sy, v);
+            acc[0] += v[0];
+            acc[1] += v[1];
+            acc[2] += v[2];
+        }
+    }
+    float* o = lev + (static_cast<int64_t>(y) * lw + x) * 3;
+    o[0] = acc[0] * 0.0625f;
+    o[1] = acc[1] * 0.0625f;
+    o[2] = acc[2] * 0.0625f;
+}
+
+__global__ void pool2_kernel(const float* __restrict__ s, float* __restrict__ d, int cw, int chh)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= cw || y >= chh)
+        return;
+    const int fw = cw * 2;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float a = s[(static_cast<int64_t>(2 * y) * fw + 2 * x) * 3 + k];
+        const float b = s[(static_cast<int64_t>(2 * y) * fw + 2 * x + 1) * 3 + k];
+        const float c = s[(static_cast<int64_t>(2 * y + 1) * fw + 2 * x) * 3 + k];
+        const float e = s[(static_cast<int64_t>(2 * y + 1) * fw + 2 * x + 1) * 3 + k];
+        d[(static_cast<int64_t>(y) * cw + x) * 3 + k] = ((a + b) + (c + e)) * 0.25f;
+    }
+}
+
+__global__ void features_kernel(const float* __restrict__ im, int lw, int lh, int lc, int woff, float* __restrict__ out)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= lw || y >= lh)
+        return;
+    const int64_t plane = static_cast<int64_t>(lw) * lh;
+    float p[27];
+#pragma unroll
+    for (int ky = -1; ky <= 1; ++ky) {
+        const int yy = clampi(y + ky, 0, lh - 1);
+#pragma unroll
+        for (int kx = -1; kx <= 1; ++kx) {
+            const int xx = clampi(x + kx, 0, lw - 1);
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch)
+                p[((ky + 1) * 3 + (kx + 1)) * 3 + ch] = im[(static_cast<int64_t>(yy) * lw + xx) * 3 + ch] - 0.5f;
+        }
+    }
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        float m = 0.0f;
+#pragma unroll
+        for (int k = ch; k < 27; k += 3)
+            m += p[k];
+        m = __fdiv_rn(m, 9.0f);
+#pragma unroll
+        for (int k = ch; k < 27; k += 3)
+            p[k] = p[k] - m;
+    }
+    float* o = out + static_cast<int64_t>(y) * lw + x;
+    float ss = 0.0f;
+    for (int c = 0; c < lc; ++c) {
+        float f = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 27; ++k)
+            f += c_flow_w[woff + c * 27 + k] * p[k];
+        o[c * plane] = f;
+        ss += f * f;
+    }
+    const float nrm = __fsqrt_rn(ss + 1e-12f);
+    for (int c = 0; c < lc; ++c)
+        o[c * plane] = __fdiv_rn(o[c * plane], nrm);
+}
+
+__global__ void up2_kernel(const float* __restrict__ in, int sw, int sh, float* __restrict__ out, int dw, int dh)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= dw || y >= dh)
+        return;
+    const int64_t sp = static_cast<int64_t>(sw) * sh, dp = static_cast<int64_t>(dw) * dh;
+    float sx = (static_cast<float>(x) + 0.5f) * 0.5f - 0.5f;
+    float sy = (static_cast<float>(y) + 0.5f) * 0.5f - 0.5f;
+    if (sx < 0.0f)
+        sx = 0.0f;
+    if (sy < 0.0f)
+        sy = 0.0f;
+    int x0 = static_cast<int>(floorf(sx)), y0 = static_cast<int>(floorf(sy));
+    if (x0 > sw - 1)
+        x0 = sw - 1;
+    if (y0 > sh - 1)
+        y0 = sh - 1;
+    const int x1 = x0 + 1 < sw ? x0 + 1 : sw - 1;
+    const int y1 = y0 + 1 < sh ? y0 + 1 : sh - 1;
+    const float lx = sx - static_cast<float>(x0), ly = sy - static_cast<float>(y0);
+#pragma unroll
+    for (int ch = 0; ch < 2; ++ch) {
+        const float* s = in + ch * sp;
+        const float top = (1.0f - lx) * s[static_cast<int64_t>(y0) * sw + x0] + lx * s[static_cast<int64_t>(y0) * sw + x1];
+        const float bot = (1.0f - lx) * s[static_cast<int64_t>(y1) * sw + x0] + lx * s[static_cast<int64_t>(y1) * sw + x1];
+        out[ch * dp + static_cast<int64_t>(y) * dw + x] = ((1.0f - ly) * top + ly * bot) * 2.0f;
+    }
+}
+
+__global__ void decode_kernel(const float* __restrict__ cv, float* __restrict__ res, float* __restrict__ conf,
+    int64_t plane, float prior)
+{
+    const int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (p >= plane)
+        return;
+    int best = 0;
+    float cmax = cv[p] - prior * 32.0f;
+    float csum = cv[p];
+    for (int d = 1; d < 81; ++d) {
+        const int ddx = d % 9 - 4, ddy = d / 9 - 4;
+        const float raw = cv[d * plane + p];
+        csum += raw;
+        const float v = raw - prior * static_cast<float>(ddx * ddx + ddy * ddy);
+        if (v > cmax) {
+            cmax = v;
+            best = d;
+        }
+    }
+    const int by = best / 9, bx = best % 9;
+    float sw = 0.0f, sx = 0.0f, sy = 0.0f;
+    for (int ny = by - 1; ny <= by + 1; ++ny) {
+        if (ny < 0 || ny > 8)
+            continue;
+        for (int nx = bx - 1; nx <= bx + 1; ++nx) {
+            if (nx < 0 || nx > 8)
+                continue;
+            const float sc =
+                cv[(ny * 9 + nx) * plane + p] - prior * static_cast<float>((nx - 4) * (nx - 4) + (ny - 4) * (ny - 4));
+            const float e = expf_cw((sc - cmax) * kTemp);
+            sw += e;
+            sx += e * static_cast<float>(nx - 4);
+            sy += e * static_cast<float>(ny - 4);
+        }
+    }
+    res[p] = __fdiv_rn(sx, sw);
+    res[plane + p] = __fdiv_rn(sy, sw);
+    const float k = cv[best * plane + p] - __fdiv_rn(csum, 81.0f);
+    conf[p] = k > 0.0f ? k : 0.0f;
+}
+
+// confidence-weighted 3x3 mean (edge clamp) of the refinement, added to the
+// upsampled coarser flow (zero at the coarsest level)
+__global__ void smooth_kernel(const float* __restrict__ res, const float* __restrict__ conf,
+    const float* __restrict__ up, float* __restrict__ out, int lw, int lh)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= lw || y >= lh)
+        return;
+    const int64_t plane = static_cast<int64_t>(lw) * lh;
+    float sx = 0.0f, sy = 0.0f, sw = 0.0f;
+#pragma unroll
+    for (int ky = -1; ky <= 1; ++ky) {
+        const int yy = clampi(y + ky, 0, lh - 1);
+#pragma unroll
+        for (int kx = -1; kx <= 1; ++kx) {
+            const int xx = clampi(x + kx, 0, lw - 1);
+            const int64_t q = static_cast<int64_t>(yy) * lw + xx;
+            const float c = conf[q];
+            sx += c * res[q];
+            sy += c * res[plane + q];
+            sw += c;
+        }
+    }
+    const int64_t p = static_cast<int64_t>(y) * lw + x;
+    const float den = sw + kEps;
+    const float ux = up ? up[p] : 0.0f;
+    const float uy = up ? up[plane + p] : 0.0f;
+    out[p] = ux + __fdiv_rn(sx, den);
+    out[plane + p] = uy + __fdiv_rn(sy, den);
+}
+
+__global__ void final_flow_kernel(const float* __restrict__ S, int lw, int lh, float* __restrict__ out, int w, int h)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h)
+        return;
+    const int64_t plane = static_cast<int64_t>(lw) * lh;
+    const float rx = static_cast<float>(lw) / static_cast<float>(w);
+    const float ry = static_cast<float>(lh) / static_cast<float>(h);
+    const float gx = static_cast<float>(w) / static_cast<float>(lw);
+    const float gy = static_cast<float>(h) / static_cast<float>(lh);
+    float sx = (static_cast<float>(x) + 0.5f) * rx - 0.5f;
+    float sy = (static_cast<float>(y) + 0.5f) * ry - 0.5f;
+    if (sx < 0.0f)
+        sx = 0.0f;
+    if (sy < 0.0f)
+        sy = 0.0f;
+    int x0 = static_cast<int>(floorf(sx)), y0 = static_cast<int>(floorf(sy));
+    if (x0 > lw - 1)
+        x0 = lw - 1;
+    if (y0 > lh - 1)
+        y0 = lh - 1;
+    const int x1 = x0 + 1 < lw ? x0 + 1 : lw - 1;
+    const int y1 = y0 + 1 < lh ? y0 + 1 : lh - 1;
+    const float lx = sx - static_cast<float>(x0), ly = sy - static_cast<float>(y0);
+    float r[2];
+#pragma unroll
+    for (int ch = 0; ch < 2; ++ch) {
+        const float* s = S + ch * plane;
+        const float top = (1.0f - lx) * s[static_cast<int64_t>(y0) * lw + x0] + lx * s[static_cast<int64_t>(y0) * lw + x1];
+        const float bot = (1.0f - lx) * s[static_cast<int64_t>(y1) * lw + x0] + lx * s[static_cast<int64_t>(y1) * lw + x1];
+        r[ch] = (1.0f - ly) * top + ly * bot;
+    }
+    float* o = out + (static_cast<int64_t>(y) * w + x) * 3;
+    o[0] = r[0] * gx;
+    o[1] = r[1] * gy;
+    o[2] = 0.0f;
+}
+
+inline dim3 g2(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h + b.y - 1) / b.y); }
+
+}  // namespace
+
+FlowDims flow_dims(int w, int h)
+{
+    FlowDims d;
+    const int pw = ((w + 63) / 64) * 64, ph = ((h + 63) / 64) * 64;
+    size_t off = 0;
+    d.max_plane = 0;
+    d.max_c = 0;
+    for (int l = 0; l < kFlowLevels; ++l) {
+        d.lw[l] = pw >> (l + 2);
+        d.lh[l] = ph >> (l + 2);
+        d.lc[l] = kLevelC[l];
+        d.off[l] = off;
+        off += static_cast<size_t>(d.lw[l]) * d.lh[l] * d.lc[l];
+        const size_t plane = static_cast<size_t>(d.lw[l]) * d.lh[l];
+        if (plane > d.max_plane)
+            d.max_plane = plane;
+        if (d.lc[l] > d.max_c)
+            d.max_c = d.lc[l];
+    }
+    d.feat_floats = off;
+    return d;
+}
+
+cudaError_t flow_upload_weights()
+{
+    // Once per device: the constant bank is per device (and per context).
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev >= 0 && dev < 64 && done[dev])
+        return cudaSuccess;
+    static float host_w[kWeightTotal];
+    for (int l = 0; l < kFlowLevels; ++l) {
+        uint64_t s = 0x5653432D464C4F57ULL ^ (static_cast<uint64_t>(l + 1) * 0x9E3779B97F4A7C15ULL);
+        for (int i = 0; i < kLevelC[l] * 27; ++i) {
+            const uint64_t z = splitmix64(&s);
+            host_w[kWeightOff[l] + i] = static_cast<float>(static_cast<uint32_t>(z >> 40)) * (1.0f / 8388608.0f) - 1.0f;
+        }
+    }
+    e = cudaMemcpyToSymbol(c_flow_w, host_w, sizeof(host_w));
+    if (e == cudaSuccess && dev >= 0 && dev < 64)
+        done[dev] = true;
+    return e;
+}
+
+size_t flow_feature_scratch_floats(const FlowDims& d)
+{
+    size_t n = 0;
+    for (int l = 0; l < kFlowLevels; ++l)
+        n += static_cast<size_t>(d.lw[l]) * d.lh[l] * 3;
+    return n;
+}
+
+cudaError_t launch_flow_features(const float* img, int w, int h, const FlowDims& d, float* feats, float* scratch,
+    cudaStream_t st, int* launches)
+{
+    const dim3 b(32, 8);
+    float* lev[kFlowLevels];
+    size_t off = 0;
+    for (int l = 0; l < kFlowLevels; ++l) {
+        lev[l] = scratch + off;
+        off += static_cast<size_t>(d.lw[l]) * d.lh[l] * 3;
+    }
+    level0_image_kernel<<<g2(d.lw[0], d.lh[0], b), b, 0, st>>>(img, w, h, lev[0], d.lw[0], d.lh[0]);
+    int nl = 1;
+    for (int l = 1; l < kFlowLevels; ++l) {
+        pool2_kernel<<<g2(d.lw[l], d.lh[l], b), b, 0, st>>>(lev[l - 1], lev[l], d.lw[l], d.lh[l]);
+        ++nl;
+    }
+    for (int l = 0; l < kFlowLevels; ++l) {
+        features_kernel<<<g2(d.lw[l], d.lh[l], b), b, 0, st>>>(lev[l], d.lw[l], d.lh[l], d.lc[l], kWeightOff[l],
+            feats + d.off[l]);
+        ++nl;
+    }
+    if (launches)
+        *launches += nl;
+    return cudaGetLastError();
+}
+
+size_t flow_estimate_scratch_floats(const FlowDims& d)
+{
+    size_t maxcl = 0;
+    for (int l = 0; l < kFlowLevels; ++l) {
+        const size_t v = static_cast<size_t>(d.lw[l]) * d.lh[l] * d.lc[l];
+        if (v > maxcl)
+            maxcl = v;
+    }
+    // up (2 ch) + refinement and confidence (3) + two smoothed flows (2 + 2),
+    // warped features, cost volume
+    return 9 * d.max_plane + maxcl + 81 * d.max_plane;
+}
+
+cudaError_t launch_flow_from_features(const float* featA, const float* featB, int w, int h, const FlowDims& d,
+    float* flow_out, float* scratch, cudaStream_t st, int* launches)
+{
+    const dim3 b(32, 8);
+    float* up = scratch;
+    float* raw = up + 2 * d.max_plane;
+    float* sm[2] = {raw + 3 * d.max_plane, raw + 5 * d.max_plane};
+    float* warped = raw + 7 * d.max_plane;
+    size_t maxcl = 0;
+    for (int l = 0; l < kFlowLevels; ++l)
+        maxcl = std::max(maxcl, static_cast<size_t>(d.lw[l]) * d.lh[l] * d.lc[l]);
+    float* cv = warped + maxcl;
+    int nl = 0;
+    int cur = 0;
+    cudaError_t e;
+    for (int l = kFlowLevels - 1; l >= 0; --l) {
+        const int lw = d.lw[l], lh = d.lh[l], lc = d.lc[l];
+        const int64_t plane = static_cast<int64_t>(lw) * lh;
+        const float* fa = featA + d.off[l];
+        const float* fb = featB + d.off[l];
+        const float* upp = nullptr;
+        const float* fb_use = fb;
+        if (l < kFlowLevels - 1) {
+            up2_kernel<<<g2(lw, lh, b), b, 0, st>>>(sm[cur], d.lw[l + 1], d.lh[l + 1], up, lw, lh);
+            ++nl;
+            e = launch_warp_op(fb, up, warped, 1, lc, lh, lw, st);
+            if (e != cudaSuccess)
+                return e;
+            ++nl;
+            upp = up;
+            fb_use = warped;
+        }
+        e = launch_correlation(fa, fb_use, cv, 1, lc, lh, lw, 4, 0, st);
+        if (e != cudaSuccess)
+            return e;
+        ++nl;
+        decode_kernel<<<static_cast<unsigned>((plane + 255) / 256), 256, 0, st>>>(cv, raw, raw + 2 * plane, plane,
+            kLevelPrior[l]);
+        ++nl;
+        cur ^= 1;
+        smooth_kernel<<<g2(lw, lh, b), b, 0, st>>>(raw, raw + 2 * plane, upp, sm[cur], lw, lh);
+        ++nl;
+    }
+    final_flow_kernel<<<g2(w, h, b), b, 0, st>>>(sm[cur], d.lw[0], d.lh[0], flow_out, w, h);
+    ++nl;
+    if (launches)
+        *launches += nl;
+    return cudaGetLastError();
+}
+
+}  // namespace vsc

@@ -1,0 +1,81 @@
+// Internal declarations shared by the library's translation units.
+//
+// Kernels live in the .cu files; the launchers declared here validate
+// nothing (the C-ABI layer in vsc_api.cpp does) and only enqueue work on the
+// given stream, returning the launch error.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/vsc.h"
+
+namespace vsc {
+
+// ---- error plumbing (vsc_api.cpp) ----------------------------------------
+vsc_status set_error(vsc_status st, const char* fmt, ...);
+vsc_status check_cuda(cudaError_t e, const char* what);
+void clear_error();
+
+// ---- ops (vsc_ops.cu) -----------------------------------------------------
+cudaError_t launch_correlation(const float* f1, const float* f2, float* out, int N, int C, int H, int W, int md,
+    int legacy, cudaStream_t st);
+cudaError_t launch_warp_op(const float* in, const float* flow, float* out, int N, int C, int H, int W,
+    cudaStream_t st);
+
+// ---- stabilization (vsc_stab.cu) -------------------------------------------
+struct Img {
+    float* d;
+    int w, h, c;
+};
+cudaError_t launch_rgba_to_float(const uint8_t* rgba, float* out, int64_t npix, cudaStream_t st);
+cudaError_t launch_float_to_rgba(const float* in, uint8_t* rgba, int64_t npix, cudaStream_t st);
+cudaError_t launch_stab_warp(Img in, Img flow, Img out, cudaStream_t st);
+cudaError_t launch_adap_comb(Img ci, Img cp, Img pwi, Img pwp, Img nwi, Img nwp, Img ai, Img ap, Img lsw, float alpha,
+    cudaStream_t st);
+cudaError_t launch_consist_wt(Img ai, Img ci, Img wt, float beta, float gamma, cudaStream_t st);
+cudaError_t launch_bilinear(Img in, Img out, cudaStream_t st);
+// Nearest-neighbour resize of a float HWC3 image for the FLOWDOWNSCALE mode
+// (the reference scales the QImage with Qt::FastTransformation,
+// flowmodel.cpp:126-133): source = min(iw-1, ((2x+1)*iw) / (2*ow)).
+cudaError_t launch_resize_nearest(const float* in, int iw, int ih, float* out, int ow, int oh, cudaStream_t st);
+
+// Solver.  The workspace holds the momentum image, the Laplacian of the
+// processed image and the second Jacobi buffer: 3 * w*h*3 floats.
+size_t solver_workspace_floats(int w, int h);
+// Runs num_iter iterations; O holds the initial solution and receives the
+// result.  Returns the number of kernels launched through *launches.
+cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,
+    float step, float mom, float* workspace, cudaStream_t st, int* launches, uint8_t* rgba_out = nullptr);
+
+// Fused five-warp + adaptive combination + consistency weights for the
+// orchestrator: writes adapCmbPr and consWt only.
+cudaError_t launch_fused_front(const float* o0, const float* o1, const float* o2, const float* p0, const float* p1,
+    const float* p2, const float* last_stab, const float* flow_fwd, const float* flow_bwd, int fc, float* adap_pr,
+    float* cons_wt, int w, int h, float alpha, float beta, float gamma, cudaStream_t st);
+// P, A, Wt of the next coarser pyramid level, one launch.
+cudaError_t launch_pyr_down3(const float* P, const float* A, const float* Wt, int iw, int ih, float* Pd, float* Ad,
+    float* Wd, int ow, int oh, cudaStream_t st);
+
+// ---- flow estimator (vsc_flow.cu) ------------------------------------------
+constexpr int kFlowLevels = 5;
+struct FlowDims {
+    int lw[kFlowLevels], lh[kFlowLevels], lc[kFlowLevels];
+    size_t off[kFlowLevels];  // float offset of each level's features
+    size_t feat_floats;       // all levels, one frame
+    size_t max_plane;         // largest lw*lh
+    int max_c;
+};
+FlowDims flow_dims(int w, int h);
+cudaError_t flow_upload_weights();
+// scratch for one frame's feature extraction: level images
+size_t flow_feature_scratch_floats(const FlowDims& d);
+cudaError_t launch_flow_features(const float* img, int w, int h, const FlowDims& d, float* feats, float* scratch,
+    cudaStream_t st, int* launches);
+// scratch for one flow: up/raw/smooth flows, warped features, cost volume
+size_t flow_estimate_scratch_floats(const FlowDims& d);
+cudaError_t launch_flow_from_features(const float* featA, const float* featB, int w, int h, const FlowDims& d,
+    float* flow_out, float* scratch, cudaStream_t st, int* launches);
+
+}  // namespace vsc

@@ -1,0 +1,47 @@
+// Device arithmetic shared by the kernels.
+//
+// All translation units are compiled with -fmad=false: a product followed by
+// a sum is rounded twice, exactly as the reference's expressions read, so the
+// kernels reproduce the CPU restatement bit for bit.  Where a fused
+// multiply-add is intended it is written explicitly (fmaf).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vsc {
+
+// exp(x) in single precision: Cody & Waite range reduction x = k*ln2 + r with
+// ln2 split into a 16-bit head and its tail, the degree-7 Taylor polynomial
+// of exp(r) on |r| <= ln2/2 in Horner form (truncation < 1e-8 relative,
+// result within 0.6 ulp of exp), and scaling by 2^k through the exponent
+// field.  Results below 2^-126 flush to zero — every caller clamps values
+// below 1e-3 to zero, so the flush never reaches an output.
+__device__ __forceinline__ float expf_cw(float x)
+{
+    if (x != x)
+        return x;
+    if (x > 88.72283f)
+        return __int_as_float(0x7f800000);
+    if (x < -87.33654f)
+        return 0.0f;
+    const float kf = rintf(__fmul_rn(x, 1.44269502f));
+    float r = fmaf(kf, -0.693145751953125f, x);
+    r = fmaf(kf, -1.42860682e-6f, r);
+    float p = 1.98412701e-4f;
+    p = fmaf(p, r, 1.38888892e-3f);
+    p = fmaf(p, r, 8.33333377e-3f);
+    p = fmaf(p, r, 4.16666679e-2f);
+    p = fmaf(p, r, 1.66666672e-1f);
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
+    int k = static_cast<int>(kf);
+    if (k > 127) {
+        p = p * 2.0f;
+        k -= 1;
+    }
+    return p * __int_as_float((k + 127) << 23);
+}
+
+}  // namespace vsc
