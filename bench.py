@@ -43,8 +43,11 @@ PKG = ROOT / "video-stream-consistency_gb300"
 W, H = 1920, 1080
 METRIC = "1080p stabilized frames/s (plain FP32 GPU path: correlation + warp + mask + blend)"
 # Solver Jacobi step, per pixel: reads O, U, lap(P), A, consWt (5 x 12 B),
-# writes O, U (2 x 12 B).
+# writes O, U (2 x 12 B); the kernel performs SOLVER_ITERS_PER_LAUNCH steps
+# per launch (temporal blocking), so its algorithmic bytes per launch are that
+# many steps' worth ("effective" bandwidth can exceed the HBM peak).
 SOLVER_BYTES_PER_PX = 84
+SOLVER_ITERS_PER_LAUNCH = 8
 
 
 def import_pkg():
@@ -218,6 +221,54 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def solver_roofline(vsc, dev, stream, iters: int = 144):
+    """Times the dominant kernel — the full-resolution solver — with CUDA
+    events on its stream: per-launch time from a 1-launch and a
+    (1 + n)-launch solve of the same size."""
+    import torch
+
+    peak, peak_src = peaks()
+    g = torch.Generator(device=dev).manual_seed(1)
+    P = torch.rand((H, W, 3), device=dev, generator=g)
+    A = torch.rand((H, W, 3), device=dev, generator=g)
+    Wt = torch.rand((H, W, 3), device=dev, generator=g) * 2
+    O = P.clone()
+    wsp = torch.empty(vsc.consist_out_workspace_size(W, H) // 4, dtype=torch.float32, device=dev)
+    T = SOLVER_ITERS_PER_LAUNCH
+    torch.cuda.synchronize()
+    for _ in range(2):
+        vsc.get_consist_out(P, A, Wt, iters, 0.15, 0.15, O, workspace=wsp, stream=stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record(stream)
+    vsc.get_consist_out(P, A, Wt, T, 0.15, 0.15, O, workspace=wsp, stream=stream)
+    ev[1].record(stream)
+    ev[2].record(stream)
+    vsc.get_consist_out(P, A, Wt, T + iters, 0.15, 0.15, O, workspace=wsp, stream=stream)
+    ev[3].record(stream)
+    ev[3].synchronize()
+    n_launch = iters // T
+    per_launch_ms = (ev[2].elapsed_time(ev[3]) - ev[0].elapsed_time(ev[1])) / n_launch
+    alg_bytes = SOLVER_BYTES_PER_PX * W * H * T  # T Jacobi steps per launch
+    achieved = alg_bytes / (per_launch_ms / 1000.0) / 1e9
+    return {"bound": "hbm", "kernel": f"solver_tb_kernel ({T} Jacobi steps of kernel_consist_out per launch at "
+                                      f"1920x1080; effective bytes = {SOLVER_BYTES_PER_PX} B/px per step)",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": SOLVER_TRAFFIC_BYTES, "algorithmic_bytes_per_launch": alg_bytes,
+            "launch_ms": per_launch_ms, "ms_per_jacobi_step": per_launch_ms / T, "peak_source": peak_src}
+
+
+def run_solver_only(args):
+    """--kernel solver: only the 1920x1080 solver (for profiler captures)."""
+    import torch
+
+    vsc = import_pkg()
+    vsc.build()
+    vsc.load()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    print(json.dumps(solver_roofline(vsc, dev, stream, iters=args.steps * SOLVER_ITERS_PER_LAUNCH)))
+
+
 # ---------------------------------------------------------------------------
 def run_gpu(args):
     import torch
@@ -277,6 +328,15 @@ def run_gpu(args):
     ms_max = reduce_max(ms, ws, dev)
     value = ws * args.steps / (ms_max / 1000.0)
 
+    # ---- per-stage device time (separate pass; stage events synchronise) -------
+    st.enable_timing(True)
+    stages = []
+    for _ in range(5):
+        step_dev()
+        stages.append(st.stage_ms())
+    st.enable_timing(False)
+    stages_ms = {k: statistics.median(d[k] for d in stages) for k in stages[0]}
+
     # ---- end to end through the public API with pinned host buffers ------------
     pinned = [(torch.from_numpy(o).pin_memory(), torch.from_numpy(p).pin_memory()) for o, p in frames]
     out_host = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory()
@@ -307,33 +367,7 @@ def run_gpu(args):
     e2e = {"value": ws * args.steps / t_e2e, "unit": "frames/s", "h2d_bytes_per_step": 2 * W * H * 4,
            "d2h_bytes_per_step": W * H * 4}
 
-    # ---- roofline of the dominant kernel: the full-resolution solver step ------
-    peak, peak_src = peaks()
-    g = torch.Generator(device=dev).manual_seed(1)
-    P = torch.rand((H, W, 3), device=dev, generator=g)
-    A = torch.rand((H, W, 3), device=dev, generator=g)
-    Wt = torch.rand((H, W, 3), device=dev, generator=g) * 2
-    O = P.clone()
-    wsp = torch.empty(vsc.consist_out_workspace_size(W, H) // 4, dtype=torch.float32, device=dev)
-    with torch.cuda.stream(stream):
-        for _ in range(2):
-            vsc.get_consist_out(P, A, Wt, 150, 0.15, 0.15, O, workspace=wsp, stream=stream)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-    ev[0].record(stream)
-    vsc.get_consist_out(P, A, Wt, 1, 0.15, 0.15, O, workspace=wsp, stream=stream)
-    ev[1].record(stream)
-    ev[2].record(stream)
-    vsc.get_consist_out(P, A, Wt, 151, 0.15, 0.15, O, workspace=wsp, stream=stream)
-    ev[3].record(stream)
-    ev[3].synchronize()
-    per_launch_ms = (ev[2 + 0].elapsed_time(ev[3]) - ev[0].elapsed_time(ev[1])) / 150.0
-    alg_bytes = SOLVER_BYTES_PER_PX * W * H
-    achieved = alg_bytes / (per_launch_ms / 1000.0) / 1e9
-    roofline = {"bound": "hbm", "kernel": "solver_iter_kernel (one Jacobi step of kernel_consist_out at "
-                                          "1920x1080)",
-                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": SOLVER_TRAFFIC_BYTES, "algorithmic_bytes_per_launch": alg_bytes,
-                "launch_ms": per_launch_ms, "peak_source": peak_src}
+    roofline = solver_roofline(vsc, dev, stream)
 
     line = {
         "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
@@ -345,6 +379,7 @@ def run_gpu(args):
                    "l2": "per-step working set ~0.6 GB > 129 MB L2; no flush",
                    "parallelism": f"replicas x{ws}"},
         "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "roofline": roofline, "clocks": clk,
+        "stages_ms": stages_ms,
     }
     if rank == 0 and ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_sample(frames, os.cpu_count() or 1)
@@ -370,11 +405,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--kernel", choices=["step", "solver"], default="step",
+                    help="solver: time only the 1920x1080 solver (profiler target)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.kernel == "solver":
+        run_solver_only(args)
     else:
         run_gpu(args)
 

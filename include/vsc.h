@@ -49,6 +49,19 @@ VSC_API const char* vsc_last_error(void);
 /* 10000*major + 100*minor + patch */
 VSC_API int vsc_version(void);
 
+/* Device-side waits in this library are bounded: a kernel that gives up
+ * records it in a device flag and returns instead of hanging.  Reads and
+ * clears the flag of the current device (synchronous): VSC_ETIMEOUT if a
+ * kernel gave up since the last call, whose outputs are then invalid.
+ * No reference counterpart: the reference exits the process on CUDA errors
+ * (flowconsistency.cu:25-31). */
+VSC_API vsc_status vsc_check_device(void);
+
+/* Self-test of that path: one CTA waits at most `spins` polls on a barrier
+ * nothing completes, then records the timeout; vsc_check_device then
+ * returns VSC_ETIMEOUT.  No fault, trap or hang is involved. */
+VSC_API vsc_status vsc_selftest_bounded_wait(int32_t spins, vsc_stream_t stream);
+
 /* ========================================================================
  * ONNX Runtime custom ops (domain "custom")
  * ======================================================================== */
@@ -168,6 +181,10 @@ typedef struct vsc_stabilizer_config {
                                0: flows supplied with vsc_stabilizer_set_flows */
     int32_t flow_downscale; /* FLOWDOWNSCALE (videostabilizer.cpp:74-98); 1 = full size */
     int32_t flow_channels;  /* channels (2 or 3) of supplied flows when compute_flow = 0 */
+    int32_t use_graphs;     /* 1: after the first step, each step replays a CUDA graph
+                               captured on first use (needs a non-default stream);
+                               the graph is re-captured when the hyper-parameters or
+                               the device output pointer change */
 } vsc_stabilizer_config;
 
 /* Replaces the VideoStabilizer constructor (videostabilizer.cpp:46-102).
@@ -203,8 +220,18 @@ VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int
  * (float HWC, 3 channels when computed), 3: adapCmbPr, 4: consWt. */
 VSC_API vsc_status vsc_stabilizer_buffer(vsc_stabilizer* s, int32_t which, const float** dev_ptr);
 
-/* Number of kernels the last vsc_stabilizer_step enqueued. */
+/* Number of kernels the last vsc_stabilizer_step (or load_frame) enqueued. */
 VSC_API int32_t vsc_stabilizer_last_launches(vsc_stabilizer* s);
+
+/* Per-stage device timing, the counterpart of the reference's load / optflow /
+ * stabilize accumulators (videostabilizer.h:72-76, stabilizefiles.cpp:121-128).
+ * Off by default; when on, CUDA events are recorded between the stages. */
+VSC_API vsc_status vsc_stabilizer_enable_timing(vsc_stabilizer* s, int32_t on);
+/* ms[0] last load_frame (upload, conversion, flow features), ms[1] flow
+ * (forward + backward), ms[2] warps + adaptive combination + consistency
+ * weights + pyramid, ms[3] coarse pyramid levels of the solve, ms[4]
+ * full-resolution solve and RGBA8 output; n >= 5.  Synchronises the stream. */
+VSC_API vsc_status vsc_stabilizer_stage_ms(vsc_stabilizer* s, float* ms, int32_t n);
 
 #ifdef __cplusplus
 }

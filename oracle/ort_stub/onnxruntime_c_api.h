@@ -69,11 +69,34 @@ typedef struct OrtKernelContext {
 
 typedef struct OrtSessionOptions OrtSessionOptions;
 typedef struct OrtCustomOpDomain OrtCustomOpDomain;
-typedef struct OrtCustomOp OrtCustomOp;
+struct OrtApi;
+
+/* The custom-op function table (the leading members of ORT's OrtCustomOp,
+ * in its order). */
+typedef struct OrtCustomOp {
+    uint32_t version;
+    void*(ORT_API_CALL* CreateKernel)(const struct OrtCustomOp* op, const struct OrtApi* api,
+                                      const OrtKernelInfo* info);
+    const char*(ORT_API_CALL* GetName)(const struct OrtCustomOp* op);
+    const char*(ORT_API_CALL* GetExecutionProviderType)(const struct OrtCustomOp* op);
+    ONNXTensorElementDataType(ORT_API_CALL* GetInputType)(const struct OrtCustomOp* op, size_t index);
+    size_t(ORT_API_CALL* GetInputTypeCount)(const struct OrtCustomOp* op);
+    ONNXTensorElementDataType(ORT_API_CALL* GetOutputType)(const struct OrtCustomOp* op, size_t index);
+    size_t(ORT_API_CALL* GetOutputTypeCount)(const struct OrtCustomOp* op);
+    void(ORT_API_CALL* KernelCompute)(void* op_kernel, OrtKernelContext* context);
+    void(ORT_API_CALL* KernelDestroy)(void* op_kernel);
+} OrtCustomOp;
 
 typedef struct OrtApi {
     OrtStatusPtr(ORT_API_CALL* KernelInfoGetAttribute_int64)(const OrtKernelInfo* info, const char* name,
                                                             int64_t* out);
+    OrtStatusPtr(ORT_API_CALL* CreateCustomOpDomain)(const char* domain, OrtCustomOpDomain** out);
+    OrtStatusPtr(ORT_API_CALL* CustomOpDomain_Add)(OrtCustomOpDomain* domain, const OrtCustomOp* op);
+    OrtStatusPtr(ORT_API_CALL* AddCustomOpDomain)(OrtSessionOptions* options, OrtCustomOpDomain* domain);
+    void(ORT_API_CALL* ReleaseCustomOpDomain)(OrtCustomOpDomain* domain);
+    const char*(ORT_API_CALL* GetErrorMessage)(const OrtStatus* status);
+    OrtStatusPtr(ORT_API_CALL* CreateStatus)(int code, const char* msg);
+    OrtStatusPtr(ORT_API_CALL* GetAvailableProviders)(char*** out_ptr, int* provider_length);
 } OrtApi;
 
 typedef struct OrtApiBase {

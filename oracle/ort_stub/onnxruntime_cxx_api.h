@@ -106,10 +106,57 @@ private:
     OrtKernelContext* c_;
 };
 
-/* Op descriptors derive from this; the stub never instantiates them through
- * the ORT C op table, so the template only has to exist. */
+/* Op descriptors derive from this.  As in ORT, the base fills the C
+ * function table (OrtCustomOp) with thunks into the derived descriptor and
+ * its kernel type; CreateKernel(api, info) and Compute(context) are the
+ * derived classes' own. */
 template <typename TOp, typename TKernel>
-struct CustomOpBase {
+struct CustomOpBase : OrtCustomOp {
+    CustomOpBase()
+    {
+        OrtCustomOp::version = ORT_API_VERSION;
+        OrtCustomOp::CreateKernel = [](const OrtCustomOp* this_, const OrtApi* api, const OrtKernelInfo* info) {
+            return static_cast<void*>(static_cast<const TOp*>(this_)->CreateKernel(*api, info));
+        };
+        OrtCustomOp::GetName = [](const OrtCustomOp* this_) { return static_cast<const TOp*>(this_)->GetName(); };
+        OrtCustomOp::GetExecutionProviderType = [](const OrtCustomOp* this_) {
+            return static_cast<const TOp*>(this_)->GetExecutionProviderType();
+        };
+        OrtCustomOp::GetInputType = [](const OrtCustomOp* this_, size_t i) {
+            return static_cast<const TOp*>(this_)->GetInputType(i);
+        };
+        OrtCustomOp::GetInputTypeCount = [](const OrtCustomOp* this_) {
+            return static_cast<const TOp*>(this_)->GetInputTypeCount();
+        };
+        OrtCustomOp::GetOutputType = [](const OrtCustomOp* this_, size_t i) {
+            return static_cast<const TOp*>(this_)->GetOutputType(i);
+        };
+        OrtCustomOp::GetOutputTypeCount = [](const OrtCustomOp* this_) {
+            return static_cast<const TOp*>(this_)->GetOutputTypeCount();
+        };
+        OrtCustomOp::KernelCompute = [](void* k, OrtKernelContext* ctx) { static_cast<TKernel*>(k)->Compute(ctx); };
+        OrtCustomOp::KernelDestroy = [](void* k) { delete static_cast<TKernel*>(k); };
+    }
 };
+
+/* Api access as in ORT's C++ wrapper under ORT_API_MANUAL_INIT. */
+inline const OrtApi*& GlobalApi()
+{
+    static const OrtApi* api = nullptr;
+    return api;
+}
+inline void InitApi(const OrtApi* api) { GlobalApi() = api; }
+inline const OrtApi& GetApi() { return *GlobalApi(); }
+
+inline std::vector<std::string> GetAvailableProviders()
+{
+    char** names = nullptr;
+    int n = 0;
+    std::vector<std::string> out;
+    if (GetApi().GetAvailableProviders(&names, &n) == nullptr)
+        for (int i = 0; i < n; ++i)
+            out.emplace_back(names[i]);
+    return out;
+}
 
 }  // namespace Ort

@@ -398,8 +398,10 @@ void vo_bilinear(const float* in, int iw, int ih, float* out, int ow, int oh, in
         for (int ox = 0; ox < ow; ++ox) {
             const float xx = (float)ox * (float)iw / (float)ow;
             const float yy = (float)oy * (float)ih / (float)oh;
-            const int ix = (int)floorf(xx);
-            const int iy = (int)floorf(yy);
+            int ix = (int)floorf(xx);
+            int iy = (int)floorf(yy);
+            ix = ix < iw - 1 ? ix : iw - 1; /* index guard; xx < iw for all sizes used */
+            iy = iy < ih - 1 ? iy : ih - 1;
             const float fx = xx - (float)ix;
             const float fy = yy - (float)iy;
             const int ix1 = ix + 1 < iw - 1 ? ix + 1 : iw - 1;

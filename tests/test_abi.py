@@ -46,7 +46,7 @@ def test_version_and_defaults(vsc):
     hp = vsc.default_hyper_params()
     assert (hp.alpha, hp.beta, hp.gamma, hp.pyramid_levels, hp.num_iter) == (6800.0, 6800.0, 2.0, 2, 150)
     assert abs(hp.step_size - 0.15) < 1e-7 and abs(hp.mom_fac - 0.15) < 1e-7
-    assert vsc.consist_out_workspace_size(1920, 1080) == 1920 * 1080 * 9 * 4
+    assert vsc.consist_out_workspace_size(1920, 1080) == 1920 * 1080 * 12 * 4
     assert vsc.consist_out_workspace_size(0, 10) == 0
 
 
@@ -99,10 +99,10 @@ def test_stabilizer_rejects_bad_config(vsc):
     L = vsc.load()
     h = C.c_void_p()
     for cfg, code, word in [
-        (vsc.StabilizerConfig(4, 4, 1, 1, 1, 3), vsc.VSC_EINVAL, "size"),
-        (vsc.StabilizerConfig(64, 64, 2, 1, 1, 3), vsc.VSC_EUNSUPPORTED, "batch"),
-        (vsc.StabilizerConfig(64, 64, 1, 1, 0, 3), vsc.VSC_EINVAL, "downscale"),
-        (vsc.StabilizerConfig(64, 64, 1, 0, 1, 4), vsc.VSC_EINVAL, "flow_channels"),
+        (vsc.StabilizerConfig(4, 4, 1, 1, 1, 3, 1), vsc.VSC_EINVAL, "size"),
+        (vsc.StabilizerConfig(64, 64, 2, 1, 1, 3, 1), vsc.VSC_EUNSUPPORTED, "batch"),
+        (vsc.StabilizerConfig(64, 64, 1, 1, 0, 3, 1), vsc.VSC_EINVAL, "downscale"),
+        (vsc.StabilizerConfig(64, 64, 1, 0, 1, 4, 1), vsc.VSC_EINVAL, "flow_channels"),
     ]:
         rc, msg = _status(vsc, L.vsc_stabilizer_create(C.byref(cfg), None, C.byref(h)))
         assert rc == code and word in msg, (rc, msg)

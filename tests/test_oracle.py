@@ -136,6 +136,16 @@ def test_rgba_conversions(oracle):
     assert q.tolist() == [[255, 1, 127], [254, 0, 255], [254, 255, 0]]
 
 
+def test_byte_to_float_single_precision_division():
+    """gpuimage.cu:49 converts with a double division; for every byte value
+    the single-precision quotient v / 255.0f is the same float (the kernels
+    build their table that way, without FP64)."""
+    v = np.arange(256)
+    a = (v.astype(np.float64) / 255.0).astype(np.float32)
+    b = v.astype(np.float32) / np.float32(255.0)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
 def test_bilinear_quirks(oracle):
     img = RNG.random((12, 16, 3)).astype(np.float32)
     down = oracle.bilinear(img, 8, 6)

@@ -35,6 +35,27 @@ def test_rgba_round_trip(vsc, oracle, cuda):
     assert np.array_equal(got, oracle.float_to_rgba(special))
 
 
+def test_rgba_unaligned_and_ragged(vsc, oracle, cuda):
+    """Pointers off the 16-byte grid and pixel counts not divisible by 4 take
+    the one-pixel-per-thread kernels; results are the same bits."""
+    import ctypes as C
+    import torch
+
+    rgba = RNG.integers(0, 256, (7, 9, 4), dtype=np.uint8)  # 63 pixels
+    ref = oracle.rgba_to_float(rgba)
+    big = torch.zeros(63 * 4 + 4, dtype=torch.uint8, device=cuda)
+    big[4:] = torch.from_numpy(rgba.reshape(-1)).to(cuda)
+    outbuf = torch.zeros(63 * 3 + 1, dtype=torch.float32, device=cuda)
+    img = vsc.Image(outbuf.data_ptr() + 4, 9, 7, 3)
+    vsc._check(vsc.load().vsc_char_to_float_image(C.c_void_p(big.data_ptr() + 4), C.byref(img), None))
+    torch.cuda.synchronize()
+    assert np.array_equal(outbuf[1:].cpu().numpy().reshape(7, 9, 3), ref)
+    back = torch.zeros(63 * 4 + 4, dtype=torch.uint8, device=cuda)
+    vsc._check(vsc.load().vsc_float_to_char_image(C.byref(img), C.c_void_p(back.data_ptr() + 4), None))
+    torch.cuda.synchronize()
+    assert np.array_equal(back[4:].cpu().numpy().reshape(7, 9, 4), oracle.float_to_rgba(ref))
+
+
 @pytest.mark.parametrize("h,w,fc,scale", [(24, 32, 3, 4.0), (17, 29, 2, 12.0), (5, 4, 3, 50.0), (64, 96, 2, 0.5)])
 def test_warp_result(vsc, oracle, cuda, h, w, fc, scale):
     img = _img(h, w)
@@ -43,20 +64,22 @@ def test_warp_result(vsc, oracle, cuda, h, w, fc, scale):
     assert np.array_equal(got, oracle.stab_warp(img, flow))
 
 
-def test_adap_comb_and_weights(vsc, oracle, cuda):
+@pytest.mark.parametrize("alpha,beta,gamma", [(6800.0, 6800.0, 2.0), (20.0, 6800.0, 2.0), (50.0, 900.0, 0.5)])
+def test_adap_comb_and_weights(vsc, oracle, cuda, alpha, beta, gamma):
     h, w = 31, 47
     base = _img(h, w)
     ims = [np.clip(base + RNG.normal(0, s, base.shape), 0, 1).astype(np.float32)
-           for s in (0.0, 0.02, 0.005, 0.03, 0.01, 0.02, 0.004)]
-    ain, apr = vsc.get_adap_comb(*[_t(a, cuda) for a in ims], 6800.0)
-    oin, opr = oracle.adap_comb(*ims, 6800.0)
+           for s in (0.0, 0.08, 0.1, 0.005, 0.12, 0.01, 0.004)]
+    ain, apr = vsc.get_adap_comb(*[_t(a, cuda) for a in ims], alpha)
+    oin, opr = oracle.adap_comb(*ims, alpha)
     assert np.array_equal(ain.cpu().numpy(), oin)
     assert np.array_equal(apr.cpu().numpy(), opr)
-    wt = vsc.get_consist_wt(ain, _t(ims[0], cuda), 6800.0, 2.0).cpu().numpy()
-    owt = oracle.consist_wt(ims[0], oin, 6800.0, 2.0)
+    wt = vsc.get_consist_wt(ain, _t(ims[0], cuda), beta, gamma).cpu().numpy()
+    owt = oracle.consist_wt(ims[0], oin, beta, gamma)
     assert np.array_equal(wt, owt)
-    # all clamp branches taken: 0 (below 1e-3), 0.45 / 0.3 caps, and free values
-    assert (owt == 0).any() and (owt > 0).any()
+    if alpha < beta:
+        # both branches of the 1e-3 clamp are exercised
+        assert (owt == 0).any() and (owt > 0).any()
 
 
 @pytest.mark.parametrize("src,dst", [((64, 48), (32, 24)), ((33, 21), (16, 10)), ((16, 10), (33, 21)),
@@ -67,8 +90,11 @@ def test_bilinear(vsc, oracle, cuda, src, dst):
     assert np.array_equal(got, oracle.bilinear(img, dst[0], dst[1]))
 
 
+# widths divisible by 4 take the persistent TMA-fed kernel, others the
+# per-tile kernel; iteration counts not divisible by 8 end in a short launch
 @pytest.mark.parametrize("h,w,iters", [(9, 11, 0), (9, 11, 1), (9, 11, 2), (40, 56, 75), (3, 3, 5), (2, 2, 4),
-                                       (67, 33, 150)])
+                                       (67, 33, 150), (48, 200, 13), (540, 960, 75), (1080, 1920, 9),
+                                       (17, 4, 3), (100, 64, 150)])
 def test_consist_out(vsc, oracle, cuda, h, w, iters):
     import torch
 
@@ -82,6 +108,22 @@ def test_consist_out(vsc, oracle, cuda, h, w, iters):
     O2 = _t(O0, cuda)
     vsc.get_consist_out(_t(P, cuda), _t(A, cuda), _t(Wt, cuda), iters, 0.15, 0.15, O2, workspace=ws)
     assert np.array_equal(O2.cpu().numpy(), ref)
+
+
+def test_bounded_wait_timeout_is_reported(vsc, oracle, cuda):
+    """Failure detection without a fault: a kernel whose bounded wait runs out
+    records it; the host reads VSC_ETIMEOUT once, the context stays usable."""
+    import torch
+
+    vsc.check_device()  # clear anything earlier
+    vsc._check(vsc.load().vsc_selftest_bounded_wait(2000, None))
+    torch.cuda.synchronize()
+    with pytest.raises(vsc.VscError, match="ETIMEOUT"):
+        vsc.check_device()
+    vsc.check_device()  # cleared
+    f = RNG.standard_normal((1, 3, 6, 6)).astype(np.float32)
+    out = vsc.correlation(_t(f, cuda), _t(f, cuda), 4).cpu().numpy()
+    assert np.array_equal(out, oracle.correlation(f, f, 4))
 
 
 def _frames(w, h, n, seed):
@@ -139,6 +181,46 @@ def test_stabilizer_computed_flow_stream(vsc, oracle, cuda, w, h):
         assert np.array_equal(out.cpu().numpy(), r_rgba), f"rgba, step {k}"
         if t + 2 < len(frames):
             st.load_frame(*frames[t + 2])
+    st.close()
+
+
+@pytest.mark.parametrize("use_graphs", [True, False])
+def test_stabilizer_graph_replay_side_stream(vsc, oracle, cuda, use_graphs):
+    """On a non-default stream steps after the first replay captured CUDA
+    graphs (one per window rotation / feedback parity); every step must still
+    equal the restatement, and hyper-parameter edits must be honoured."""
+    import torch
+
+    w, h = 96, 64
+    frames = _frames(w, h, 10, seed=21)
+    ref = _run_oracle_stream(oracle, frames[:8])
+    hp = oracle.default_hyper()
+    hp.num_iter = 37
+    side = torch.cuda.Stream()
+    st = vsc.Stabilizer(w, h, stream=side, use_graphs=use_graphs)
+    for i in range(3):
+        st.load_frame(*frames[i])
+    outs = []
+    for t in range(1, 7):
+        with torch.cuda.stream(side):
+            out = st.step()
+        side.synchronize()
+        outs.append((out.cpu().numpy(), st.buffer(0).cpu().numpy()))
+        st.load_frame(*frames[t + 2])
+    for k in range(6):
+        assert np.array_equal(outs[k][0], ref[k][1]), f"step {k}"
+        assert np.array_equal(outs[k][1], ref[k][0]), f"step {k}"
+    # a hyper-parameter change takes effect on the next (re-captured) step
+    st.hyper_params.num_iter = 37
+    with torch.cuda.stream(side):
+        out = st.step()
+    side.synchronize()
+    orig = [oracle.rgba_to_float(o) for o, _ in frames[6:9]]
+    proc = [oracle.rgba_to_float(p) for _, p in frames[6:9]]
+    ff = oracle.flow_estimate(orig[1], orig[2])
+    fb = oracle.flow_estimate(orig[2], orig[1])
+    _, rgba = oracle.stab_pass(orig, proc, ff, fb, outs[-1][1], hp)
+    assert np.array_equal(out.cpu().numpy(), rgba)
     st.close()
 
 

@@ -33,6 +33,7 @@ EXPORTED = [
     "vsc_get_bilinear", "vsc_consist_out_workspace_size", "vsc_get_consist_out", "vsc_default_hyper_params",
     "vsc_stabilizer_create", "vsc_stabilizer_destroy", "vsc_stabilizer_hyper_params", "vsc_stabilizer_load_frame",
     "vsc_stabilizer_set_flows", "vsc_stabilizer_step", "vsc_stabilizer_buffer", "vsc_stabilizer_last_launches",
+    "vsc_stabilizer_enable_timing", "vsc_stabilizer_stage_ms", "vsc_check_device", "vsc_selftest_bounded_wait",
 ]
 
 
@@ -61,7 +62,7 @@ class HyperParams(C.Structure):
 class StabilizerConfig(C.Structure):
     _fields_ = [
         ("width", C.c_int32), ("height", C.c_int32), ("batch_size", C.c_int32), ("compute_flow", C.c_int32),
-        ("flow_downscale", C.c_int32), ("flow_channels", C.c_int32),
+        ("flow_downscale", C.c_int32), ("flow_channels", C.c_int32), ("use_graphs", C.c_int32),
     ]
 
 
@@ -107,6 +108,10 @@ def load():
         "vsc_stabilizer_set_flows": [vp, vp, vp, i32],
         "vsc_stabilizer_step": [vp, vp, i32],
         "vsc_stabilizer_buffer": [vp, i32, C.POINTER(vp)],
+        "vsc_stabilizer_enable_timing": [vp, i32],
+        "vsc_check_device": [],
+        "vsc_selftest_bounded_wait": [i32, vp],
+        "vsc_stabilizer_stage_ms": [vp, C.POINTER(C.c_float), i32],
     }.items():
         f = getattr(L, fn)
         f.argtypes = args
@@ -252,6 +257,11 @@ def get_consist_out(crnt_pr, prev_stab_warp, cons_wt, num_iter, step_size, mom_f
     return consis_out
 
 
+def check_device() -> None:
+    """Raises VscError(VSC_ETIMEOUT) if a kernel's bounded wait gave up."""
+    _check(load().vsc_check_device())
+
+
 def default_hyper_params() -> HyperParams:
     hp = HyperParams()
     load().vsc_default_hyper_params(C.byref(hp))
@@ -274,12 +284,14 @@ class Stabilizer:
     step.
     """
 
-    def __init__(self, width, height, compute_flow=True, flow_downscale=1, flow_channels=3, stream=None):
+    def __init__(self, width, height, compute_flow=True, flow_downscale=1, flow_channels=3, stream=None,
+                 use_graphs=True):
         import torch
 
         self.width, self.height = width, height
         self._stream_obj = stream if stream is not None else torch.cuda.current_stream()
-        cfg = StabilizerConfig(width, height, 1, 1 if compute_flow else 0, flow_downscale, flow_channels)
+        cfg = StabilizerConfig(width, height, 1, 1 if compute_flow else 0, flow_downscale, flow_channels,
+                               1 if use_graphs else 0)
         h = C.c_void_p()
         _check(load().vsc_stabilizer_create(C.byref(cfg), _stream(self._stream_obj), C.byref(h)))
         self._h = h
@@ -323,6 +335,17 @@ class Stabilizer:
         self._stream_obj.synchronize()
         view = _DeviceView(p.value, (self.height, self.width, channels))
         return torch.as_tensor(view, device="cuda").clone()
+
+    STAGES = ("load", "flow", "front", "coarse_solve", "full_solve")
+
+    def enable_timing(self, on: bool = True):
+        _check(load().vsc_stabilizer_enable_timing(self._h, 1 if on else 0))
+
+    def stage_ms(self) -> dict:
+        """Device time of the stages of the last load_frame and step (ms)."""
+        buf = (C.c_float * 5)()
+        _check(load().vsc_stabilizer_stage_ms(self._h, buf, 5))
+        return dict(zip(self.STAGES, list(buf)))
 
     @property
     def last_launches(self) -> int:

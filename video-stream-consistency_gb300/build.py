@@ -1,4 +1,5 @@
-"""Build recipe of the CUDA library: libvsc.so, in-tree, for sm_103a only.
+"""Build recipe of the CUDA library: libvsc.so, in-tree, for sm_103a only
+(and, where ONNX Runtime headers exist, the custom-op library libvsc_ort.so).
 
 Each translation unit is compiled by nvcc in parallel and linked into a
 shared library next to this file.  Flags that matter for results:
@@ -21,7 +22,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libvsc.so"
 INCLUDE = PKG.parent / "include"
 
-SOURCES = ["vsc_ops.cu", "vsc_stab.cu", "vsc_flow.cu", "vsc_api.cpp"]
+SOURCES = ["vsc_ops.cu", "vsc_stab.cu", "vsc_solver.cu", "vsc_flow.cu", "vsc_api.cpp"]
 HEADERS = ["vsc_internal.h", "vsc_math.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -68,6 +69,22 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
     return LIB
+
+
+def build_ort(ort_include: str, out: Path | None = None, extra_sources=()) -> Path:
+    """Build the ONNX Runtime custom-op library (csrc/ort/vsc_ort_ops.cpp)
+    against the ONNX Runtime headers in ort_include, linked to libvsc.so.
+    extra_sources are compiled into the same library (the tests add a
+    stand-in runtime)."""
+    lib = build()
+    out = Path(out) if out else PKG / "libvsc_ort.so"
+    srcs = [str(CSRC / "ort" / "vsc_ort_ops.cpp"), *map(str, extra_sources)]
+    cmd = [nvcc(), *ARCH, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-I", str(INCLUDE),
+           "-I", str(ort_include), *srcs, "-o", str(out), "-L", str(PKG), "-lvsc", f"-Xlinker=-rpath={PKG}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"ORT adapter build failed:\n{r.stdout}\n{r.stderr}")
+    return out
 
 
 if __name__ == "__main__":

@@ -52,7 +52,7 @@ vsc_status check_cuda(cudaError_t e, const char* what)
 
 namespace {
 
-constexpr int64_t kMaxDim = 1 << 20;
+constexpr int64_t kMaxDim = 1 << 16;
 
 bool dims_ok(int64_t v) { return v > 0 && v <= kMaxDim; }
 
@@ -291,6 +291,26 @@ VSC_API vsc_status vsc_get_consist_out(const vsc_image* crnt_pr, const vsc_image
     return check_cuda(e, "consist_out launch");
 }
 
+VSC_API vsc_status vsc_check_device(void)
+{
+    clear_error();
+    int flagged = 0;
+    vsc_status st = check_cuda(check_device_timeout(&flagged), "check_device");
+    if (st)
+        return st;
+    if (flagged)
+        return set_error(VSC_ETIMEOUT, "a kernel's bounded wait gave up (its results are invalid)");
+    return VSC_OK;
+}
+
+VSC_API vsc_status vsc_selftest_bounded_wait(int32_t spins, vsc_stream_t stream)
+{
+    clear_error();
+    if (spins < 1 || spins > (1 << 20))
+        return set_error(VSC_EINVAL, "selftest_bounded_wait: spins outside [1, 2^20]");
+    return check_cuda(launch_bounded_wait_selftest(spins, cs(stream)), "selftest launch");
+}
+
 VSC_API void vsc_default_hyper_params(vsc_hyper_params* hp)
 {
     if (!hp)
@@ -344,7 +364,22 @@ struct vsc_stabilizer {
     float* flow_scratch = nullptr;
     FlowDims fd{};
     int last_launches = 0;
-    bool ok = true;
+    // stage timing (off by default): events around load_frame and the stages of a step
+    bool timing = false;
+    cudaEvent_t ev[7] = {};
+    // CUDA graphs of the step, one per ring position / feedback parity /
+    // output / hyper-parameters / timing combination
+    bool use_graphs = false;
+    struct GraphEntry {
+        bool valid = false;
+        int head = 0, ls_cur = 0, nl = 0;
+        uint8_t* rgba = nullptr;
+        vsc_hyper_params hp{};
+        bool timing = false;
+        cudaGraphExec_t exec = nullptr;
+        uint64_t used = 0;
+    } graphs[8];
+    uint64_t graph_clock = 0;
 };
 
 namespace {
@@ -365,6 +400,14 @@ struct DeviceGuard {
     }
 };
 
+enum { kEvLoad0, kEvLoad1, kEvStep0, kEvFlow, kEvFront, kEvCoarse, kEvStep1 };
+
+void mark(vsc_stabilizer* s, int which)
+{
+    if (s->timing)
+        cudaEventRecord(s->ev[which], s->st);
+}
+
 template <typename T>
 cudaError_t dalloc(T** p, size_t elems)
 {
@@ -380,14 +423,13 @@ void free_all(vsc_stabilizer* s)
     for (int i = 0; i < 3; ++i) {
         f(s->orig[i]);
         f(s->proc[i]);
-        f(s->feat[i]);
     }
+    f(s->feat[0]);
     f(s->stage[0]);
     f(s->stage[1]);
     f(s->out_rgba);
     f(s->small);
     f(s->flow_fwd);
-    f(s->flow_bwd);
     f(s->flow_small);
     f(s->last_stab[0]);
     f(s->last_stab[1]);
@@ -402,6 +444,17 @@ void free_all(vsc_stabilizer* s)
     f(s->solver_ws);
     f(s->feat_scratch);
     f(s->flow_scratch);
+    for (cudaEvent_t& e : s->ev)
+        if (e) {
+            cudaEventDestroy(e);
+            e = nullptr;
+        }
+    for (auto& g : s->graphs)
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+            g.valid = false;
+        }
 }
 
 vsc_status alloc_all(vsc_stabilizer* s)
@@ -419,8 +472,10 @@ vsc_status alloc_all(vsc_stabilizer* s)
     A(dalloc(&s->stage[0], static_cast<size_t>(s->w) * s->h * 4));
     A(dalloc(&s->stage[1], static_cast<size_t>(s->w) * s->h * 4));
     A(dalloc(&s->out_rgba, static_cast<size_t>(s->w) * s->h * 4));
-    A(dalloc(&s->flow_fwd, static_cast<size_t>(s->w) * s->h * s->fc));
-    A(dalloc(&s->flow_bwd, static_cast<size_t>(s->w) * s->h * s->fc));
+    // forward and backward flow contiguous: the estimator writes both in one launch
+    A(dalloc(&s->flow_fwd, 2 * static_cast<size_t>(s->w) * s->h * s->fc));
+    if (e == cudaSuccess)
+        s->flow_bwd = s->flow_fwd + static_cast<size_t>(s->w) * s->h * s->fc;
     A(dalloc(&s->last_stab[0], n3));
     A(dalloc(&s->last_stab[1], n3));
     A(dalloc(&s->adap_pr, n3));
@@ -446,13 +501,18 @@ vsc_status alloc_all(vsc_stabilizer* s)
     A(dalloc(&s->solver_ws, solver_workspace_floats(s->w, s->h)));
     if (s->compute_flow) {
         s->fd = flow_dims(s->fw, s->fh);
-        for (int i = 0; i < 3; ++i)
-            A(dalloc(&s->feat[i], s->fd.feat_floats));
+        // the three frames' features in one allocation, so a flow pair can
+        // address them as a strided batch
+        A(dalloc(&s->feat[0], 3 * s->fd.feat_floats));
+        if (e == cudaSuccess) {
+            s->feat[1] = s->feat[0] + s->fd.feat_floats;
+            s->feat[2] = s->feat[1] + s->fd.feat_floats;
+        }
         A(dalloc(&s->feat_scratch, flow_feature_scratch_floats(s->fd)));
-        A(dalloc(&s->flow_scratch, flow_estimate_scratch_floats(s->fd)));
+        A(dalloc(&s->flow_scratch, 2 * flow_estimate_scratch_floats(s->fd)));
         if (s->downscale > 1) {
             A(dalloc(&s->small, static_cast<size_t>(s->fw) * s->fh * 3));
-            A(dalloc(&s->flow_small, static_cast<size_t>(s->fw) * s->fh * 3));
+            A(dalloc(&s->flow_small, 2 * static_cast<size_t>(s->fw) * s->fh * 3));
         }
         A(flow_upload_weights());
     }
@@ -489,6 +549,7 @@ VSC_API vsc_status vsc_stabilizer_create(const vsc_stabilizer_config* cfg, vsc_s
     s->fw = static_cast<int>(std::lround(static_cast<float>(s->w) / static_cast<float>(s->downscale)));
     s->fh = static_cast<int>(std::lround(static_cast<float>(s->h) / static_cast<float>(s->downscale)));
     s->st = cs(stream);
+    s->use_graphs = cfg->use_graphs != 0;
     cudaGetDevice(&s->device);
     vsc_default_hyper_params(&s->hp);
     vsc_status st = alloc_all(s);
@@ -528,6 +589,7 @@ VSC_API vsc_status vsc_stabilizer_load_frame(vsc_stabilizer* s, const uint8_t* o
     DeviceGuard g(s->device);
     const int slot = (s->head + s->count) % 3;
     const int64_t npix = static_cast<int64_t>(s->w) * s->h;
+    mark(s, kEvLoad0);
     const uint8_t* src[2] = {orig_rgba, proc_rgba};
     float* dst[2] = {s->orig[slot], s->proc[slot]};
     int nl = 0;
@@ -562,6 +624,7 @@ VSC_API vsc_status vsc_stabilizer_load_frame(vsc_stabilizer* s, const uint8_t* o
         if (st)
             return st;
     }
+    mark(s, kEvLoad1);
     s->count += 1;
     s->last_launches = nl;
     return VSC_OK;
@@ -587,24 +650,14 @@ VSC_API vsc_status vsc_stabilizer_set_flows(vsc_stabilizer* s, const float* fwd,
     return VSC_OK;
 }
 
-VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int32_t out_on_device)
+}  // extern "C"
+
+namespace {
+
+// All device work of one doOneStep, enqueued on the stabilizer's stream.
+cudaError_t enqueue_step(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t* rgba_dev, int* launches)
 {
-    clear_error();
-    if (!s)
-        return set_error(VSC_EINVAL, "step: null stabilizer");
-    if (s->count < 3)
-        return set_error(VSC_ESTATE, "step: window holds %d of 3 frames", s->count);
-    if (!s->compute_flow && !s->flows_set)
-        return set_error(VSC_ESTATE, "step: flows not set for this step");
-    const vsc_hyper_params hp = s->hp;
     const int L = hp.pyramid_levels;
-    if (L < 1 || L > s->levels_alloc)
-        return set_error(VSC_EINVAL, "step: pyramid_levels %d outside [1, %d]", L, s->levels_alloc);
-    if (hp.num_iter < 0)
-        return set_error(VSC_EINVAL, "step: negative num_iter");
-    if (out_rgba && out_on_device && (reinterpret_cast<uintptr_t>(out_rgba) & 3))
-        return set_error(VSC_EINVAL, "step: device output must be 4-byte aligned");
-    DeviceGuard g(s->device);
     const int s0 = s->head, s1 = (s->head + 1) % 3, s2 = (s->head + 2) % 3;
     const size_t n3b = static_cast<size_t>(s->w) * s->h * 3 * sizeof(float);
     cudaStream_t st = s->st;
@@ -615,6 +668,7 @@ VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int
             e = r;
     };
 
+    mark(s, kEvStep0);
     // preloadProcessedFrames (videostabilizer.cpp:152): the first previous
     // stabilized frame is the processed image of the last preloaded frame.
     if (!s->started)
@@ -623,20 +677,20 @@ VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int
     // retrieveOpticalFlow (videostabilizer.cpp:267-279): forward flow runs
     // frame pair (t, t+1); the "backward" flow runs (t+1, t) (flowmodel.cpp:139-143).
     if (s->compute_flow) {
-        float* ff = s->downscale > 1 ? s->flow_small : s->flow_fwd;
-        run(launch_flow_from_features(s->feat[s1], s->feat[s2], s->fw, s->fh, s->fd, ff, s->flow_scratch, st, &nl));
-        if (s->downscale > 1) {
+        const bool small = s->downscale > 1;
+        const int64_t fs = static_cast<int64_t>(s->fw) * s->fh * 3;
+        run(launch_flow_pair(s->feat[s1], s->feat[s2] - s->feat[s1], s->feat[s2], s->feat[s1] - s->feat[s2], s->fw,
+            s->fh, s->fd, small ? s->flow_small : s->flow_fwd, small ? fs : s->flow_bwd - s->flow_fwd,
+            s->flow_scratch, st, &nl));
+        if (small) {
+            // flowmodel.cpp:158-161: bilinear upsampling, vectors not rescaled
             run(launch_bilinear(Img{s->flow_small, s->fw, s->fh, 3}, Img{s->flow_fwd, s->w, s->h, 3}, st));
-            ++nl;
-        }
-        float* fb = s->downscale > 1 ? s->flow_small : s->flow_bwd;
-        run(launch_flow_from_features(s->feat[s2], s->feat[s1], s->fw, s->fh, s->fd, fb, s->flow_scratch, st, &nl));
-        if (s->downscale > 1) {
-            run(launch_bilinear(Img{s->flow_small, s->fw, s->fh, 3}, Img{s->flow_bwd, s->w, s->h, 3}, st));
-            ++nl;
+            run(launch_bilinear(Img{s->flow_small + fs, s->fw, s->fh, 3}, Img{s->flow_bwd, s->w, s->h, 3}, st));
+            nl += 2;
         }
     }
 
+    mark(s, kEvFlow);
     float* ls_in = s->last_stab[s->ls_cur];
     float* ls_out = s->last_stab[s->ls_cur ^ 1];
     run(launch_fused_front(s->orig[s0], s->orig[s1], s->orig[s2], s->proc[s0], s->proc[s1], s->proc[s2], ls_in,
@@ -665,8 +719,10 @@ VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int
     // with the same bilinear chain, so at the coarsest level it equals P.
     run(cudaMemcpyAsync(O[L - 1], P[L - 1], static_cast<size_t>(s->lw[L - 1]) * s->lh[L - 1] * 3 * sizeof(float),
         cudaMemcpyDeviceToDevice, st));
-    uint8_t* rgba_dev = (out_rgba && out_on_device) ? out_rgba : s->out_rgba;
+    mark(s, kEvFront);
     for (int j = L - 1; j >= 0; --j) {
+        if (j == 0)
+            mark(s, kEvCoarse);
         if (j != L - 1) {
             run(launch_bilinear(Img{O[j + 1], s->lw[j + 1], s->lh[j + 1], 3}, Img{O[j], s->lw[j], s->lh[j], 3}, st));
             ++nl;
@@ -674,6 +730,101 @@ VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int
         run(run_solver(P[j], A[j], W[j], O[j], s->lw[j], s->lh[j], hp.num_iter / (j + 1), hp.step_size, hp.mom_fac,
             s->solver_ws, st, &nl, j == 0 ? rgba_dev : nullptr));
     }
+    mark(s, kEvStep1);
+    *launches = nl;
+    return e;
+}
+
+bool same_hp(const vsc_hyper_params& a, const vsc_hyper_params& b) { return std::memcmp(&a, &b, sizeof(a)) == 0; }
+
+// Replays (capturing on first use) the step graph for the current state.
+// Returns false when graphs cannot be used; the caller then enqueues directly.
+bool launch_step_graph(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t* rgba_dev, int* launches,
+    cudaError_t* err)
+{
+    *err = cudaSuccess;
+    auto* hit = static_cast<vsc_stabilizer::GraphEntry*>(nullptr);
+    for (auto& g : s->graphs)
+        if (g.valid && g.head == s->head && g.ls_cur == s->ls_cur && g.rgba == rgba_dev && g.timing == s->timing &&
+            same_hp(g.hp, hp))
+            hit = &g;
+    if (!hit) {
+        auto* slot = &s->graphs[0];
+        for (auto& g : s->graphs)
+            if (!g.valid || g.used < slot->used)
+                slot = &g;
+        if (slot->exec) {
+            cudaGraphExecDestroy(slot->exec);
+            slot->exec = nullptr;
+        }
+        slot->valid = false;
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        int nl = 0;
+        const cudaError_t ee = enqueue_step(s, hp, rgba_dev, &nl);
+        const cudaError_t ec = cudaStreamEndCapture(s->st, &graph);
+        if (ee != cudaSuccess || ec != cudaSuccess || !graph) {
+            if (graph)
+                cudaGraphDestroy(graph);
+            cudaGetLastError();
+            return false;
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&slot->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) {
+            cudaGetLastError();
+            slot->exec = nullptr;
+            return false;
+        }
+        slot->valid = true;
+        slot->head = s->head;
+        slot->ls_cur = s->ls_cur;
+        slot->rgba = rgba_dev;
+        slot->timing = s->timing;
+        slot->hp = hp;
+        slot->nl = nl;
+        hit = slot;
+    }
+    hit->used = ++s->graph_clock;
+    *launches = hit->nl;
+    *err = cudaGraphLaunch(hit->exec, s->st);
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int32_t out_on_device)
+{
+    clear_error();
+    if (!s)
+        return set_error(VSC_EINVAL, "step: null stabilizer");
+    if (s->count < 3)
+        return set_error(VSC_ESTATE, "step: window holds %d of 3 frames", s->count);
+    if (!s->compute_flow && !s->flows_set)
+        return set_error(VSC_ESTATE, "step: flows not set for this step");
+    const vsc_hyper_params hp = s->hp;
+    const int L = hp.pyramid_levels;
+    if (L < 1 || L > s->levels_alloc)
+        return set_error(VSC_EINVAL, "step: pyramid_levels %d outside [1, %d]", L, s->levels_alloc);
+    if (hp.num_iter < 0)
+        return set_error(VSC_EINVAL, "step: negative num_iter");
+    if (out_rgba && out_on_device && (reinterpret_cast<uintptr_t>(out_rgba) & 3))
+        return set_error(VSC_EINVAL, "step: device output must be 4-byte aligned");
+    DeviceGuard g(s->device);
+    uint8_t* rgba_dev = (out_rgba && out_on_device) ? out_rgba : s->out_rgba;
+    int nl = 0;
+    cudaError_t e = cudaSuccess;
+    // The first step (which seeds the feedback frame) runs directly; later
+    // steps replay a captured graph when the stream allows capture.
+    const bool graphed = s->use_graphs && s->started && s->st != nullptr &&
+                         launch_step_graph(s, hp, rgba_dev, &nl, &e);
+    if (!graphed)
+        e = enqueue_step(s, hp, rgba_dev, &nl);
     vsc_status stt = check_cuda(e, "step");
     if (stt)
         return stt;
@@ -685,11 +836,11 @@ VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int
     s->last_launches = nl;
     if (out_rgba && !out_on_device) {
         stt = check_cuda(cudaMemcpyAsync(out_rgba, s->out_rgba, static_cast<size_t>(s->w) * s->h * 4,
-                             cudaMemcpyDeviceToHost, st),
+                             cudaMemcpyDeviceToHost, s->st),
             "step download");
         if (stt)
             return stt;
-        return check_cuda(cudaStreamSynchronize(st), "step synchronize");
+        return check_cuda(cudaStreamSynchronize(s->st), "step synchronize");
     }
     return VSC_OK;
 }
@@ -721,5 +872,40 @@ VSC_API vsc_status vsc_stabilizer_buffer(vsc_stabilizer* s, int32_t which, const
 }
 
 VSC_API int32_t vsc_stabilizer_last_launches(vsc_stabilizer* s) { return s ? s->last_launches : 0; }
+
+VSC_API vsc_status vsc_stabilizer_enable_timing(vsc_stabilizer* s, int32_t on)
+{
+    clear_error();
+    if (!s)
+        return set_error(VSC_EINVAL, "enable_timing: null stabilizer");
+    DeviceGuard g(s->device);
+    if (on && !s->ev[0])
+        for (cudaEvent_t& e : s->ev) {
+            vsc_status st = check_cuda(cudaEventCreate(&e), "enable_timing");
+            if (st)
+                return st;
+        }
+    s->timing = on != 0;
+    return VSC_OK;
+}
+
+VSC_API vsc_status vsc_stabilizer_stage_ms(vsc_stabilizer* s, float* ms, int32_t n)
+{
+    clear_error();
+    if (!s || !ms || n < 5)
+        return set_error(VSC_EINVAL, "stage_ms: null argument or n < 5");
+    if (!s->timing)
+        return set_error(VSC_ESTATE, "stage_ms: timing not enabled");
+    DeviceGuard g(s->device);
+    vsc_status st = check_cuda(cudaStreamSynchronize(s->st), "stage_ms");
+    if (st)
+        return st;
+    const int pairs[5][2] = {{kEvLoad0, kEvLoad1}, {kEvStep0, kEvFlow}, {kEvFlow, kEvFront}, {kEvFront, kEvCoarse},
+        {kEvCoarse, kEvStep1}};
+    for (int i = 0; i < 5; ++i)
+        if ((st = check_cuda(cudaEventElapsedTime(&ms[i], s->ev[pairs[i][0]], s->ev[pairs[i][1]]), "stage_ms")))
+            return st;
+    return VSC_OK;
+}
 
 }  // extern "C"

@@ -122,12 +122,23 @@ __global__ void pool2_kernel(const float* __restrict__ s, float* __restrict__ d,
     }
 }
 
-__global__ void features_kernel(const float* __restrict__ im, int lw, int lh, int lc, int woff, float* __restrict__ out)
+// Block (32 pixels of one row) x (8 channel groups).  Every thread builds
+// its pixel's zero-mean patch; the warp of group g computes channels
+// g, g+8, g+16, ... (uniform constant-bank reads); the squared norm is then
+// summed by one thread per pixel in channel order, as the restatement does.
+constexpr int kFeatGroups = 8;
+constexpr int kFeatMaxC = 196;
+
+__global__ void __launch_bounds__(32 * kFeatGroups) features_kernel(const float* __restrict__ im, int lw, int lh,
+    int lc, int woff, float* __restrict__ out)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= lw || y >= lh)
-        return;
+    __shared__ float sf[kFeatMaxC][32];
+    __shared__ float snrm[32];
+    const int tx = threadIdx.x, g = threadIdx.y;
+    const int x = blockIdx.x * 32 + tx;
+    const int y = blockIdx.y;
+    const bool ok = x < lw;
+    const int xc = ok ? x : lw - 1;
     const int64_t plane = static_cast<int64_t>(lw) * lh;
     float p[27];
 #pragma unroll
@@ -135,7 +146,7 @@ __global__ void features_kernel(const float* __restrict__ im, int lw, int lh, in
         const int yy = clampi(y + ky, 0, lh - 1);
 #pragma unroll
         for (int kx = -1; kx <= 1; ++kx) {
-            const int xx = clampi(x + kx, 0, lw - 1);
+            const int xx = clampi(xc + kx, 0, lw - 1);
 #pragma unroll
             for (int ch = 0; ch < 3; ++ch)
                 p[((ky + 1) * 3 + (kx + 1)) * 3 + ch] = im[(static_cast<int64_t>(yy) * lw + xx) * 3 + ch] - 0.5f;
@@ -152,27 +163,40 @@ __global__ void features_kernel(const float* __restrict__ im, int lw, int lh, in
         for (int k = ch; k < 27; k += 3)
             p[k] = p[k] - m;
     }
-    float* o = out + static_cast<int64_t>(y) * lw + x;
-    float ss = 0.0f;
-    for (int c = 0; c < lc; ++c) {
+    for (int c = g; c < lc; c += kFeatGroups) {
         float f = 0.0f;
 #pragma unroll
         for (int k = 0; k < 27; ++k)
             f += c_flow_w[woff + c * 27 + k] * p[k];
-        o[c * plane] = f;
-        ss += f * f;
+        sf[c][tx] = f;
     }
-    const float nrm = __fsqrt_rn(ss + 1e-12f);
-    for (int c = 0; c < lc; ++c)
-        o[c * plane] = __fdiv_rn(o[c * plane], nrm);
+    __syncthreads();
+    if (g == 0) {
+        float ss = 0.0f;
+        for (int c = 0; c < lc; ++c) {
+            const float f = sf[c][tx];
+            ss += f * f;
+        }
+        snrm[tx] = __fsqrt_rn(ss + 1e-12f);
+    }
+    __syncthreads();
+    if (!ok)
+        return;
+    const float nrm = snrm[tx];
+    float* o = out + static_cast<int64_t>(y) * lw + x;
+    for (int c = g; c < lc; c += kFeatGroups)
+        o[c * plane] = __fdiv_rn(sf[c][tx], nrm);
 }
 
-__global__ void up2_kernel(const float* __restrict__ in, int sw, int sh, float* __restrict__ out, int dw, int dh)
+__global__ void up2_kernel(const float* __restrict__ in, int sw, int sh, float* __restrict__ out, int dw, int dh,
+    int64_t bs)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= dw || y >= dh)
         return;
+    in += blockIdx.z * bs;
+    out += blockIdx.z * bs;
     const int64_t sp = static_cast<int64_t>(sw) * sh, dp = static_cast<int64_t>(dw) * dh;
     float sx = (static_cast<float>(x) + 0.5f) * 0.5f - 0.5f;
     float sy = (static_cast<float>(y) + 0.5f) * 0.5f - 0.5f;
@@ -198,11 +222,14 @@ __global__ void up2_kernel(const float* __restrict__ in, int sw, int sh, float* 
 }
 
 __global__ void decode_kernel(const float* __restrict__ cv, float* __restrict__ res, float* __restrict__ conf,
-    int64_t plane, float prior)
+    int64_t plane, float prior, int64_t bs)
 {
     const int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (p >= plane)
         return;
+    cv += blockIdx.z * bs;
+    res += blockIdx.z * bs;
+    conf += blockIdx.z * bs;
     int best = 0;
     float cmax = cv[p] - prior * 32.0f;
     float csum = cv[p];
@@ -241,12 +268,17 @@ __global__ void decode_kernel(const float* __restrict__ cv, float* __restrict__ 
 // confidence-weighted 3x3 mean (edge clamp) of the refinement, added to the
 // upsampled coarser flow (zero at the coarsest level)
 __global__ void smooth_kernel(const float* __restrict__ res, const float* __restrict__ conf,
-    const float* __restrict__ up, float* __restrict__ out, int lw, int lh)
+    const float* __restrict__ up, float* __restrict__ out, int lw, int lh, int64_t bs)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= lw || y >= lh)
         return;
+    res += blockIdx.z * bs;
+    conf += blockIdx.z * bs;
+    out += blockIdx.z * bs;
+    if (up)
+        up += blockIdx.z * bs;
     const int64_t plane = static_cast<int64_t>(lw) * lh;
     float sx = 0.0f, sy = 0.0f, sw = 0.0f;
 #pragma unroll
@@ -270,12 +302,15 @@ __global__ void smooth_kernel(const float* __restrict__ res, const float* __rest
     out[plane + p] = uy + __fdiv_rn(sy, den);
 }
 
-__global__ void final_flow_kernel(const float* __restrict__ S, int lw, int lh, float* __restrict__ out, int w, int h)
+__global__ void final_flow_kernel(const float* __restrict__ S, int lw, int lh, float* __restrict__ out, int w, int h,
+    int64_t bs, int64_t so)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h)
         return;
+    S += blockIdx.z * bs;
+    out += blockIdx.z * so;
     const int64_t plane = static_cast<int64_t>(lw) * lh;
     const float rx = static_cast<float>(lw) / static_cast<float>(w);
     const float ry = static_cast<float>(lh) / static_cast<float>(h);
@@ -387,8 +422,8 @@ cudaError_t launch_flow_features(const float* img, int w, int h, const FlowDims&
         ++nl;
     }
     for (int l = 0; l < kFlowLevels; ++l) {
-        features_kernel<<<g2(d.lw[l], d.lh[l], b), b, 0, st>>>(lev[l], d.lw[l], d.lh[l], d.lc[l], kWeightOff[l],
-            feats + d.off[l]);
+        features_kernel<<<dim3((d.lw[l] + 31) / 32, d.lh[l]), dim3(32, kFeatGroups), 0, st>>>(lev[l], d.lw[l], d.lh[l],
+            d.lc[l], kWeightOff[l], feats + d.off[l]);
         ++nl;
     }
     if (launches)
@@ -409,10 +444,11 @@ size_t flow_estimate_scratch_floats(const FlowDims& d)
     return 9 * d.max_plane + maxcl + 81 * d.max_plane;
 }
 
-cudaError_t launch_flow_from_features(const float* featA, const float* featB, int w, int h, const FlowDims& d,
-    float* flow_out, float* scratch, cudaStream_t st, int* launches)
+cudaError_t launch_flow_pair(const float* featA, int64_t sA, const float* featB, int64_t sB, int w, int h,
+    const FlowDims& d, float* flow_out, int64_t s_out, float* scratch, cudaStream_t st, int* launches)
 {
     const dim3 b(32, 8);
+    const int64_t bs = static_cast<int64_t>(flow_estimate_scratch_floats(d));  // per-direction scratch
     float* up = scratch;
     float* raw = up + 2 * d.max_plane;
     float* sm[2] = {raw + 3 * d.max_plane, raw + 5 * d.max_plane};
@@ -431,28 +467,36 @@ cudaError_t launch_flow_from_features(const float* featA, const float* featB, in
         const float* fb = featB + d.off[l];
         const float* upp = nullptr;
         const float* fb_use = fb;
+        int64_t sb_use = sB;
         if (l < kFlowLevels - 1) {
-            up2_kernel<<<g2(lw, lh, b), b, 0, st>>>(sm[cur], d.lw[l + 1], d.lh[l + 1], up, lw, lh);
+            dim3 g = g2(lw, lh, b);
+            g.z = 2;
+            up2_kernel<<<g, b, 0, st>>>(sm[cur], d.lw[l + 1], d.lh[l + 1], up, lw, lh, bs);
             ++nl;
-            e = launch_warp_op(fb, up, warped, 1, lc, lh, lw, st);
+            e = launch_warp_op(fb, up, warped, 2, lc, lh, lw, st, sB, bs, bs);
             if (e != cudaSuccess)
                 return e;
             ++nl;
             upp = up;
             fb_use = warped;
+            sb_use = bs;
         }
-        e = launch_correlation(fa, fb_use, cv, 1, lc, lh, lw, 4, 0, st);
+        e = launch_correlation(fa, fb_use, cv, 2, lc, lh, lw, 4, 0, st, sA, sb_use, bs);
         if (e != cudaSuccess)
             return e;
         ++nl;
-        decode_kernel<<<static_cast<unsigned>((plane + 255) / 256), 256, 0, st>>>(cv, raw, raw + 2 * plane, plane,
-            kLevelPrior[l]);
+        decode_kernel<<<dim3(static_cast<unsigned>((plane + 255) / 256), 1, 2), 256, 0, st>>>(cv, raw, raw + 2 * plane,
+            plane, kLevelPrior[l], bs);
         ++nl;
         cur ^= 1;
-        smooth_kernel<<<g2(lw, lh, b), b, 0, st>>>(raw, raw + 2 * plane, upp, sm[cur], lw, lh);
+        dim3 g = g2(lw, lh, b);
+        g.z = 2;
+        smooth_kernel<<<g, b, 0, st>>>(raw, raw + 2 * plane, upp, sm[cur], lw, lh, bs);
         ++nl;
     }
-    final_flow_kernel<<<g2(w, h, b), b, 0, st>>>(sm[cur], d.lw[0], d.lh[0], flow_out, w, h);
+    dim3 g = g2(w, h, b);
+    g.z = 2;
+    final_flow_kernel<<<g, b, 0, st>>>(sm[cur], d.lw[0], d.lh[0], flow_out, w, h, bs, s_out);
     ++nl;
     if (launches)
         *launches += nl;

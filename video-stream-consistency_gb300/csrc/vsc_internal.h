@@ -19,10 +19,12 @@ vsc_status check_cuda(cudaError_t e, const char* what);
 void clear_error();
 
 // ---- ops (vsc_ops.cu) -----------------------------------------------------
+// Batch n of each tensor starts at base + n * stride (elements; may be
+// negative).  Strides of -1 mean contiguous N x C x H x W batches.
 cudaError_t launch_correlation(const float* f1, const float* f2, float* out, int N, int C, int H, int W, int md,
-    int legacy, cudaStream_t st);
+    int legacy, cudaStream_t st, int64_t s1 = -1, int64_t s2 = -1, int64_t so = -1);
 cudaError_t launch_warp_op(const float* in, const float* flow, float* out, int N, int C, int H, int W,
-    cudaStream_t st);
+    cudaStream_t st, int64_t sin = -1, int64_t sfl = -1, int64_t sout = -1);
 
 // ---- stabilization (vsc_stab.cu) -------------------------------------------
 struct Img {
@@ -41,13 +43,20 @@ cudaError_t launch_bilinear(Img in, Img out, cudaStream_t st);
 // flowmodel.cpp:126-133): source = min(iw-1, ((2x+1)*iw) / (2*ow)).
 cudaError_t launch_resize_nearest(const float* in, int iw, int ih, float* out, int ow, int oh, cudaStream_t st);
 
-// Solver.  The workspace holds the momentum image, the Laplacian of the
-// processed image and the second Jacobi buffer: 3 * w*h*3 floats.
+// Solver.  The workspace holds the Laplacian of the processed image, two
+// momentum images and the second Jacobi buffer: 4 * w*h*3 floats.
 size_t solver_workspace_floats(int w, int h);
 // Runs num_iter iterations; O holds the initial solution and receives the
 // result.  Returns the number of kernels launched through *launches.
 cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,
     float step, float mom, float* workspace, cudaStream_t st, int* launches, uint8_t* rgba_out = nullptr);
+
+// Device-side bounded waits record a timeout in a device flag instead of
+// hanging; this reads and clears it for the current device.
+cudaError_t check_device_timeout(int* flagged);
+// A kernel whose bounded wait on an mbarrier that nobody arrives on gives up
+// after `spins` polls (the timeout path, without any fault).
+cudaError_t launch_bounded_wait_selftest(int spins, cudaStream_t st);
 
 // Fused five-warp + adaptive combination + consistency weights for the
 // orchestrator: writes adapCmbPr and consWt only.
@@ -73,9 +82,12 @@ cudaError_t flow_upload_weights();
 size_t flow_feature_scratch_floats(const FlowDims& d);
 cudaError_t launch_flow_features(const float* img, int w, int h, const FlowDims& d, float* feats, float* scratch,
     cudaStream_t st, int* launches);
-// scratch for one flow: up/raw/smooth flows, warped features, cost volume
+// scratch for one flow direction: up/raw/smooth flows, warped features, cost volume
 size_t flow_estimate_scratch_floats(const FlowDims& d);
-cudaError_t launch_flow_from_features(const float* featA, const float* featB, int w, int h, const FlowDims& d,
-    float* flow_out, float* scratch, cudaStream_t st, int* launches);
+// Two flows in the same launches (batch index z): direction n runs A_n =
+// featA + n*sA against B_n = featB + n*sB and writes flow_out + n*s_out
+// (w x h x 3).  scratch holds 2 * flow_estimate_scratch_floats(d).
+cudaError_t launch_flow_pair(const float* featA, int64_t sA, const float* featB, int64_t sB, int w, int h,
+    const FlowDims& d, float* flow_out, int64_t s_out, float* scratch, cudaStream_t st, int* launches);
 
 }  // namespace vsc

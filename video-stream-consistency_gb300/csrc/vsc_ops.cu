@@ -11,9 +11,10 @@
 // inputs (no temporaries), and every thread keeps 4 adjacent pixels x
 // (2md+1) horizontal displacements of one vertical displacement in
 // registers.  Per channel a thread reads 1 + ceil((4+2md)/4) 128-bit words
-// of shared memory for 4*(2md+1) multiply-adds.  Sums run in channel order
-// with separately rounded products and sums (-fmad=false), which is the
-// reference CPU op's arithmetic, so results match it bit for bit.
+// of shared memory for 4*(2md+1) multiply-adds, issued as packed f32x2
+// multiplies and adds on pixel pairs.  Sums run in channel order with
+// separately rounded products and sums, which is the reference CPU op's
+// arithmetic, so results match it bit for bit.
 //
 // Warp (warp.cc:71-133, warp_cuda.cu:28-98): one thread per pixel and group
 // of 8 channels; the flow, the four bilinear weights and the 0.999 edge mask
@@ -40,8 +41,8 @@ struct CorrGeom {
 
 template <int MD>
 __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
-    corr_tile_kernel(const float* __restrict__ f1, const float* __restrict__ f2, float* __restrict__ out, int C, int H,
-        int W, int legacy)
+    corr_tile_kernel(const float* __restrict__ in1, const float* __restrict__ in2, float* __restrict__ out, int C,
+        int H, int W, int legacy, int vec_store, int64_t sa, int64_t sb, int64_t so)
 {
     using G = CorrGeom<MD>;
     constexpr int P = G::P;
@@ -59,15 +60,14 @@ __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
     const int X0 = blockIdx.x * kCorrTW;
     const int Y0 = blockIdx.y * kCorrTH;
     const int64_t HW = static_cast<int64_t>(H) * W;
-    const float* a_n = f1 + static_cast<int64_t>(n) * C * HW;
-    const float* b_n = f2 + static_cast<int64_t>(n) * C * HW;
+    const float* a_n = in1 + n * sa;  // batch strides in elements (may be negative)
+    const float* b_n = in2 + n * sb;
 
-    float acc[P][4];
+    // acc[j][0] = pixels (0, 1), acc[j][1] = pixels (2, 3) of displacement j
+    f2 acc[P][2];
 #pragma unroll
     for (int j = 0; j < P; ++j)
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-            acc[j][i] = 0.0f;
+        acc[j][0] = acc[j][1] = pk(0.0f, 0.0f);
 
     for (int c0 = 0; c0 < C; c0 += kCorrCC) {
         const int cc = min(kCorrCC, C - c0);
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
         __syncthreads();
         for (int c = 0; c < cc; ++c) {
             const float4 av = *reinterpret_cast<const float4*>(&s1[(c * kCorrTH + ty) * kCorrTW + 4 * tx]);
-            const float a[4] = {av.x, av.y, av.z, av.w};
+            const f2 a01 = pk(av.x, av.y), a23 = pk(av.z, av.w);
             float b[4 * G::NB];
             const float* brow = &s2[(c * G::RH + ty + tz) * G::S2W + 4 * tx];
 #pragma unroll
@@ -108,11 +108,19 @@ __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
                 b[4 * q + 2] = bv.z;
                 b[4 * q + 3] = bv.w;
             }
+#if VSC_PACKED_MATH
 #pragma unroll
-            for (int j = 0; j < P; ++j)
+            for (int j = 0; j < P; ++j) {
+                acc[j][0] = add2(acc[j][0], mul2(a01, pk(b[j], b[j + 1])));
+                acc[j][1] = add2(acc[j][1], mul2(a23, pk(b[j + 2], b[j + 3])));
+            }
+#else
 #pragma unroll
-                for (int i = 0; i < 4; ++i)
-                    acc[j][i] = acc[j][i] + a[i] * b[i + j];
+            for (int j = 0; j < P; ++j) {
+                acc[j][0] = pk(lo_of(acc[j][0]) + av.x * b[j], hi_of(acc[j][0]) + av.y * b[j + 1]);
+                acc[j][1] = pk(lo_of(acc[j][1]) + av.z * b[j + 2], hi_of(acc[j][1]) + av.w * b[j + 3]);
+            }
+#endif
         }
         __syncthreads();
     }
@@ -123,21 +131,22 @@ __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
     const int dy = tz - MD;
     const bool yok = (y + dy >= 0) && (y + dy < H);
     const int x0 = X0 + 4 * tx;
-    const float invc = legacy ? static_cast<float>(C) : 1.0f;
+    const float fc = static_cast<float>(C);
 #pragma unroll
     for (int j = 0; j < P; ++j) {
         const int dx = j - MD;
         float r[4];
+        const float sums[4] = {lo_of(acc[j][0]), hi_of(acc[j][0]), lo_of(acc[j][1]), hi_of(acc[j][1])};
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const int xs = x0 + i + dx;
-            float v = (yok && xs >= 0 && xs < W) ? acc[j][i] : 0.0f;
+            float v = (yok && xs >= 0 && xs < W) ? sums[i] : 0.0f;
             if (legacy)
-                v = __fdiv_rn(v, invc);
+                v = __fdiv_rn(v, fc);
             r[i] = v;
         }
-        float* dst = out + (static_cast<int64_t>(n) * P * P + tz * P + j) * HW + static_cast<int64_t>(y) * W + x0;
-        if ((W & 3) == 0 && x0 + 3 < W) {
+        float* dst = out + n * so + static_cast<int64_t>(tz * P + j) * HW + static_cast<int64_t>(y) * W + x0;
+        if (vec_store && x0 + 3 < W) {
             *reinterpret_cast<float4*>(dst) = make_float4(r[0], r[1], r[2], r[3]);
         } else {
 #pragma unroll
@@ -149,8 +158,8 @@ __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
 }
 
 // Any max_displacement: one thread per output element, channel-order sum.
-__global__ void corr_generic_kernel(const float* __restrict__ f1, const float* __restrict__ f2, float* __restrict__ out,
-    int N, int C, int H, int W, int md, int legacy)
+__global__ void corr_generic_kernel(const float* __restrict__ in1, const float* __restrict__ in2,
+    float* __restrict__ out, int N, int C, int H, int W, int md, int legacy)
 {
     const int P = 2 * md + 1;
     const int64_t HW = static_cast<int64_t>(H) * W;
@@ -165,8 +174,8 @@ __global__ void corr_generic_kernel(const float* __restrict__ f1, const float* _
         const int y2 = y + d / P - md, x2 = x + d % P - md;
         float acc = 0.0f;
         if (y2 >= 0 && y2 < H && x2 >= 0 && x2 < W) {
-            const float* a = f1 + static_cast<int64_t>(n) * C * HW + pix;
-            const float* b = f2 + static_cast<int64_t>(n) * C * HW + static_cast<int64_t>(y2) * W + x2;
+            const float* a = in1 + static_cast<int64_t>(n) * C * HW + pix;
+            const float* b = in2 + static_cast<int64_t>(n) * C * HW + static_cast<int64_t>(y2) * W + x2;
             for (int c = 0; c < C; ++c)
                 acc = acc + __ldg(a + c * HW) * __ldg(b + c * HW);
         }
@@ -178,18 +187,20 @@ __global__ void corr_generic_kernel(const float* __restrict__ f1, const float* _
 
 template <int MD>
 cudaError_t launch_corr_tile(const float* f1, const float* f2, float* out, int N, int C, int H, int W, int legacy,
-    cudaStream_t st)
+    int64_t s1, int64_t s2, int64_t so, cudaStream_t st)
 {
     dim3 block(8, kCorrTH, 2 * MD + 1);
     dim3 grid((W + kCorrTW - 1) / kCorrTW, (H + kCorrTH - 1) / kCorrTH, N);
-    corr_tile_kernel<MD><<<grid, block, 0, st>>>(f1, f2, out, C, H, W, legacy);
+    // 128-bit stores need rows that start on 16 bytes: W % 4 == 0 and aligned outputs
+    const int vec = ((W & 3) == 0) && ((reinterpret_cast<uintptr_t>(out) & 15) == 0) && ((so & 3) == 0);
+    corr_tile_kernel<MD><<<grid, block, 0, st>>>(f1, f2, out, C, H, W, legacy, vec, s1, s2, so);
     return cudaGetLastError();
 }
 
 constexpr int kWarpCG = 8;  // channels per thread
 
 __global__ void warp_op_kernel(const float* __restrict__ in, const float* __restrict__ flow, float* __restrict__ out,
-    int C, int H, int W)
+    int C, int H, int W, int64_t sin, int64_t sfl, int64_t sout)
 {
     const int64_t HW = static_cast<int64_t>(H) * W;
     const int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
@@ -198,7 +209,7 @@ __global__ void warp_op_kernel(const float* __restrict__ in, const float* __rest
     const int n = blockIdx.z;
     const int c0 = blockIdx.y * kWarpCG;
     const int y = static_cast<int>(p / W), x = static_cast<int>(p % W);
-    const float* fl = flow + static_cast<int64_t>(n) * 2 * HW;
+    const float* fl = flow + n * sfl;
     const float xf = static_cast<float>(x) + __ldg(fl + p);
     const float yf = static_cast<float>(y) + __ldg(fl + HW + p);
     const float fxl = floorf(xf), fyt = floorf(yf);
@@ -222,7 +233,7 @@ __global__ void warp_op_kernel(const float* __restrict__ in, const float* __rest
     const int64_t oTL = static_cast<int64_t>(yt) * W + xl;
     const int cend = min(C, c0 + kWarpCG);
     for (int c = c0; c < cend; ++c) {
-        const float* src = in + (static_cast<int64_t>(n) * C + c) * HW;
+        const float* src = in + n * sin + static_cast<int64_t>(c) * HW;
         float val = 0.0f;
         if (take) {
             val += tl ? wTL * __ldg(src + oTL) : 0.0f;
@@ -230,27 +241,34 @@ __global__ void warp_op_kernel(const float* __restrict__ in, const float* __rest
             val += bl ? wBL * __ldg(src + oTL + W) : 0.0f;
             val += br ? wBR * __ldg(src + oTL + W + 1) : 0.0f;
         }
-        out[(static_cast<int64_t>(n) * C + c) * HW + p] = val;
+        out[n * sout + static_cast<int64_t>(c) * HW + p] = val;
     }
 }
 
 }  // namespace
 
 cudaError_t launch_correlation(const float* f1, const float* f2, float* out, int N, int C, int H, int W, int md,
-    int legacy, cudaStream_t st)
+    int legacy, cudaStream_t st, int64_t s1, int64_t s2, int64_t so)
 {
+    const int64_t HW = static_cast<int64_t>(H) * W;
+    const int64_t P = 2 * md + 1;
+    if (s1 < 0 && s2 < 0 && so < 0) {  // contiguous N x C x H x W batches
+        s1 = s2 = C * HW;
+        so = P * P * HW;
+    }
     switch (md) {
         case 1:
-            return launch_corr_tile<1>(f1, f2, out, N, C, H, W, legacy, st);
+            return launch_corr_tile<1>(f1, f2, out, N, C, H, W, legacy, s1, s2, so, st);
         case 2:
-            return launch_corr_tile<2>(f1, f2, out, N, C, H, W, legacy, st);
+            return launch_corr_tile<2>(f1, f2, out, N, C, H, W, legacy, s1, s2, so, st);
         case 3:
-            return launch_corr_tile<3>(f1, f2, out, N, C, H, W, legacy, st);
+            return launch_corr_tile<3>(f1, f2, out, N, C, H, W, legacy, s1, s2, so, st);
         case 4:
-            return launch_corr_tile<4>(f1, f2, out, N, C, H, W, legacy, st);
+            return launch_corr_tile<4>(f1, f2, out, N, C, H, W, legacy, s1, s2, so, st);
         default: {
-            const int64_t P = 2 * md + 1;
-            const int64_t total = static_cast<int64_t>(N) * P * P * H * W;
+            if (s1 != C * HW || s2 != C * HW || so != P * P * HW)
+                return cudaErrorInvalidValue;  // the generic kernel takes contiguous batches only
+            const int64_t total = static_cast<int64_t>(N) * P * P * HW;
             const int64_t blocks = (total + 255) / 256;
             corr_generic_kernel<<<static_cast<unsigned>(blocks < 152 * 64 ? blocks : 152 * 64), 256, 0, st>>>(
                 f1, f2, out, N, C, H, W, md, legacy);
@@ -260,11 +278,15 @@ cudaError_t launch_correlation(const float* f1, const float* f2, float* out, int
 }
 
 cudaError_t launch_warp_op(const float* in, const float* flow, float* out, int N, int C, int H, int W,
-    cudaStream_t st)
+    cudaStream_t st, int64_t sin, int64_t sfl, int64_t sout)
 {
     const int64_t HW = static_cast<int64_t>(H) * W;
+    if (sin < 0 && sfl < 0 && sout < 0) {
+        sin = sout = C * HW;
+        sfl = 2 * HW;
+    }
     dim3 grid(static_cast<unsigned>((HW + 255) / 256), (C + kWarpCG - 1) / kWarpCG, N);
-    warp_op_kernel<<<grid, 256, 0, st>>>(in, flow, out, C, H, W);
+    warp_op_kernel<<<grid, 256, 0, st>>>(in, flow, out, C, H, W, sin, sfl, sout);
     return cudaGetLastError();
 }
 

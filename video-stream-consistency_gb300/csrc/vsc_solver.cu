@@ -1,0 +1,623 @@
+// The blend solver of the stabilization pass (reference: kernel_consist_out
+// and get_consist_out, src/stabilization/flowconsistency.cu:193-258, :350-374).
+//
+// Differences from the reference's schedule (results are the CPU
+// restatement's, bit for bit):
+//   - Jacobi iteration: the reference updates consisOut in place
+//     (flowconsistency.cu:370), so neighbours read a timing-dependent mix of
+//     old and new values; here every pixel reads the previous iterate;
+//   - the Laplacian of the processed image, which the reference recomputes in
+//     every iteration, is computed once per solve (same expression, same bits);
+//   - several iterations per launch on register-resident tiles (temporal
+//     blocking) instead of one launch per iteration.
+#include "vsc_internal.h"
+#include "vsc_math.cuh"
+
+#include <cuda.h>  // CUtensorMap (the encoder is fetched from the driver at run time)
+
+#include <algorithm>
+#include <mutex>
+
+namespace vsc {
+namespace {
+
+inline dim3 grid2d(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h + b.y - 1) / b.y); }
+
+// ---- kernel_consist_out (flowconsistency.cu:193-258) ------------------------
+// Laplacian of the processed image with the reference's neighbour rule and
+// summation order (right, left, bottom, top, then - cnt * centre).
+__global__ void lap_pr_kernel(const float* __restrict__ P, float* __restrict__ L, int w, int h)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h)
+        return;
+    const int64_t i0 = pix_index(x, y, w) * 3;
+    const int64_t rs = static_cast<int64_t>(w) * 3;
+    for (int c = 0; c < 3; ++c) {
+        const int64_t i = i0 + c;
+        int cnt = 0;
+        float lap = 0.0f;
+        if ((x + 1) < (w - 1)) {
+            lap += P[i + 3];
+            cnt += 1;
+        }
+        if ((x - 1) >= 0) {
+            lap += P[i - 3];
+            cnt += 1;
+        }
+        if ((y + 1) < (h - 1)) {
+            lap += P[i + rs];
+            cnt += 1;
+        }
+        if ((y - 1) >= 0) {
+            lap += P[i - rs];
+            cnt += 1;
+        }
+        lap -= static_cast<float>(cnt) * P[i];
+        L[i] = lap;
+    }
+}
+
+// ---- temporally blocked solver --------------------------------------------
+// kTbT Jacobi iterations per launch on a kTbEX x kTbEY extended tile; the
+// interior (the tile minus a kTbT-wide ring) is exact after kTbT iterations
+// and is written back.  Each of the 512 threads owns a 2x2 pixel block and
+// keeps its state (O, U) and the per-pixel constants (lap P, A, consWt) in
+// registers as horizontal pixel pairs; O is published to shared memory
+// (double-buffered) for the rows of the neighbouring warps, and horizontal
+// neighbours travel by warp shuffle (one warp spans the full tile width).
+// Tiles away from the image border run the update on pixel pairs with the
+// packed single-precision instructions (add/sub/mul .rn.f32x2: two IEEE
+// operations, each rounded as the scalar one would be); border tiles apply
+// the reference's neighbour-validity rule per pixel.  Either way the result
+// equals the one-iteration-per-launch Jacobi bit for bit.
+#ifndef VSC_SOLVER_T
+#define VSC_SOLVER_T 8
+#endif
+constexpr int kTbEX = 64;
+constexpr int kTbEY = 32;
+constexpr int kTbT = VSC_SOLVER_T;             // iterations per launch
+constexpr int kTbPX = kTbEX + 4;               // shared row pitch (2-column apron each side)
+constexpr int kTbPlane = kTbPX * (kTbEY + 2);  // one colour plane with a 1-row apron
+constexpr int kTbSmem = 2 * 3 * kTbPlane * static_cast<int>(sizeof(float));
+static_assert(2 * kTbT < kTbEY, "tile too small for the iteration count");
+
+// One Jacobi step of a pixel pair with all four neighbours valid (cnt = 4).
+__device__ __forceinline__ f2 jacobi_pair(f2 o, f2& u, f2 a, f2 wt, f2 lp, f2 right, f2 left, f2 down, f2 up,
+    f2 four, f2 step2, f2 mom2, bool mom_on)
+{
+    f2 lap = add2(pk(0.0f, 0.0f), right);
+    lap = add2(lap, left);
+    lap = add2(lap, down);
+    lap = add2(lap, up);
+    lap = sub2(lap, mul2(four, o));
+    const f2 tmp_1 = mul2(wt, sub2(o, a));
+    const f2 tmp_2 = sub2(lap, lp);
+    const f2 sg = mul2(step2, sub2(tmp_2, tmp_1));
+    f2 out = add2(o, sg);
+    if (mom_on)
+        out = add2(out, mul2(mom2, u));
+    u = sg;
+    return out;
+}
+
+// One Jacobi step of one pixel with the reference's validity rule.
+__device__ __forceinline__ float jacobi_px(float o, float& u, float a, float wt, float lp, float right, float left,
+    float down, float up, bool vr, bool vl, bool vd, bool vu, float cnt, float step, float mom, bool mom_on)
+{
+    float lap = 0.0f;
+    lap += vr ? right : 0.0f;
+    lap += vl ? left : 0.0f;
+    lap += vd ? down : 0.0f;
+    lap += vu ? up : 0.0f;
+    lap -= cnt * o;
+    const float tmp_1 = wt * (o - a);
+    const float tmp_2 = lap - lp;
+    const float sg = step * (tmp_2 - tmp_1);
+    float out = o + sg;
+    if (mom_on)
+        out = out + mom * u;
+    u = sg;
+    return out;
+}
+
+struct TbState {
+    f2 o[2][3], u[2][3], a[2][3], wt[2][3], lp[2][3];  // [row][channel], pair = (left, right) pixel
+};
+
+template <bool kBorder>
+__device__ __forceinline__ void tb_iterate(TbState& s, const bool (&vr)[4], const bool (&vl)[4],
+    const bool (&vd)[4], const bool (&vu)[4], const float (&cnt)[4], float* smem, int T, int k0, float step,
+    float mom, int px0, int py0)
+{
+    const f2 four = pk(4.0f, 4.0f), step2 = pk(step, step), mom2 = pk(mom, mom);
+    for (int k = 0; k < T; ++k) {
+        const int cur = k & 1;
+        const bool mom_on = (k0 + k) > 0;
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            const float* S = smem + (cur * 3 + ch) * kTbPlane;
+            const f2 up = *reinterpret_cast<const f2*>(&S[py0 * kTbPX + px0 + 2]);
+            const f2 dn = *reinterpret_cast<const f2*>(&S[(py0 + 3) * kTbPX + px0 + 2]);
+            const f2 r0p = s.o[0][ch], r1p = s.o[1][ch];
+            const float o0 = lo_of(r0p), o1 = hi_of(r0p), o2 = lo_of(r1p), o3 = hi_of(r1p);
+            const float l0 = __shfl_up_sync(0xffffffffu, o1, 1);
+            const float l1 = __shfl_up_sync(0xffffffffu, o3, 1);
+            const float r0 = __shfl_down_sync(0xffffffffu, o0, 1);
+            const float r1 = __shfl_down_sync(0xffffffffu, o2, 1);
+            f2 n0, n1;
+            if (!kBorder) {
+                n0 = jacobi_pair(r0p, s.u[0][ch], s.a[0][ch], s.wt[0][ch], s.lp[0][ch], pk(o1, r0), pk(l0, o0), r1p,
+                    up, four, step2, mom2, mom_on);
+                n1 = jacobi_pair(r1p, s.u[1][ch], s.a[1][ch], s.wt[1][ch], s.lp[1][ch], pk(o3, r1), pk(l1, o2), dn,
+                    r0p, four, step2, mom2, mom_on);
+            } else {
+                float u0 = lo_of(s.u[0][ch]), u1 = hi_of(s.u[0][ch]), u2 = lo_of(s.u[1][ch]), u3 = hi_of(s.u[1][ch]);
+                const float m0 = jacobi_px(o0, u0, lo_of(s.a[0][ch]), lo_of(s.wt[0][ch]), lo_of(s.lp[0][ch]), o1, l0,
+                    o2, lo_of(up), vr[0], vl[0], vd[0], vu[0], cnt[0], step, mom, mom_on);
+                const float m1 = jacobi_px(o1, u1, hi_of(s.a[0][ch]), hi_of(s.wt[0][ch]), hi_of(s.lp[0][ch]), r0, o0,
+                    o3, hi_of(up), vr[1], vl[1], vd[1], vu[1], cnt[1], step, mom, mom_on);
+                const float m2 = jacobi_px(o2, u2, lo_of(s.a[1][ch]), lo_of(s.wt[1][ch]), lo_of(s.lp[1][ch]), o3, l1,
+                    lo_of(dn), o0, vr[2], vl[2], vd[2], vu[2], cnt[2], step, mom, mom_on);
+                const float m3 = jacobi_px(o3, u3, hi_of(s.a[1][ch]), hi_of(s.wt[1][ch]), hi_of(s.lp[1][ch]), r1, o2,
+                    hi_of(dn), o1, vr[3], vl[3], vd[3], vu[3], cnt[3], step, mom, mom_on);
+                s.u[0][ch] = pk(u0, u1);
+                s.u[1][ch] = pk(u2, u3);
+                n0 = pk(m0, m1);
+                n1 = pk(m2, m3);
+            }
+            s.o[0][ch] = n0;
+            s.o[1][ch] = n1;
+            float* D = smem + ((cur ^ 1) * 3 + ch) * kTbPlane;
+            *reinterpret_cast<f2*>(&D[(py0 + 1) * kTbPX + px0 + 2]) = n0;
+            *reinterpret_cast<f2*>(&D[(py0 + 2) * kTbPX + px0 + 2]) = n1;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
+    solver_tb_kernel(const float* __restrict__ Oin, float* __restrict__ Oout, const float* __restrict__ Uin,
+        float* __restrict__ Uout, const float* __restrict__ L, const float* __restrict__ A,
+        const float* __restrict__ Wt, int w, int h, int T, int k0, float step, float mom, uint8_t* __restrict__ rgba)
+{
+    extern __shared__ __align__(16) float smem[];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * 32 + tx;
+    const int ox = blockIdx.x * (kTbEX - 2 * T) - T;
+    const int oy = blockIdx.y * (kTbEY - 2 * T) - T;
+    const int px0 = 2 * tx, py0 = 2 * ty;
+
+    // both buffers start at zero, aprons included (apron cells are only read
+    // by pixels of the outermost ring, whose results are never written back)
+    for (int i = tid; i < 2 * 3 * kTbPlane; i += blockDim.x * blockDim.y)
+        smem[i] = 0.0f;
+    __syncthreads();
+
+    TbState s;
+    float cnt[4];
+    bool vr[4], vl[4], vd[4], vu[4], inimg[4];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        float v[5][3][2];
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const int q = 2 * r + c;
+            const int gx = ox + px0 + c;
+            const int gy = oy + py0 + r;
+            inimg[q] = gx >= 0 && gx < w && gy >= 0 && gy < h;
+            vr[q] = (gx + 1) < (w - 1);
+            vl[q] = (gx - 1) >= 0;
+            vd[q] = (gy + 1) < (h - 1);
+            vu[q] = (gy - 1) >= 0;
+            cnt[q] = static_cast<float>(static_cast<int>(vr[q]) + static_cast<int>(vl[q]) +
+                                        static_cast<int>(vd[q]) + static_cast<int>(vu[q]));
+            const int64_t idx = inimg[q] ? pix_index(gx, gy, w) * 3 : 0;
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+                v[0][ch][c] = inimg[q] ? Oin[idx + ch] : 0.0f;
+                v[1][ch][c] = inimg[q] ? Uin[idx + ch] : 0.0f;
+                v[2][ch][c] = inimg[q] ? A[idx + ch] : 0.0f;
+                v[3][ch][c] = inimg[q] ? Wt[idx + ch] : 0.0f;
+                v[4][ch][c] = inimg[q] ? L[idx + ch] : 0.0f;
+            }
+        }
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            s.o[r][ch] = pk(v[0][ch][0], v[0][ch][1]);
+            s.u[r][ch] = pk(v[1][ch][0], v[1][ch][1]);
+            s.a[r][ch] = pk(v[2][ch][0], v[2][ch][1]);
+            s.wt[r][ch] = pk(v[3][ch][0], v[3][ch][1]);
+            s.lp[r][ch] = pk(v[4][ch][0], v[4][ch][1]);
+            float* S = smem + ch * kTbPlane;
+            *reinterpret_cast<f2*>(&S[(py0 + 1 + r) * kTbPX + px0 + 2]) = s.o[r][ch];
+        }
+    }
+    __syncthreads();
+
+    // tiles whose every pixel has all four neighbours take the packed path
+    const bool interior = VSC_PACKED_MATH && ox >= 1 && oy >= 1 && ox + kTbEX - 1 <= w - 3 && oy + kTbEY - 1 <= h - 3;
+    if (interior)
+        tb_iterate<false>(s, vr, vl, vd, vu, cnt, smem, T, k0, step, mom, px0, py0);
+    else
+        tb_iterate<true>(s, vr, vl, vd, vu, cnt, smem, T, k0, step, mom, px0, py0);
+
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int r = q >> 1, c = q & 1;
+        const int px = px0 + c, py = py0 + r;
+        if (!inimg[q] || px < T || px >= kTbEX - T || py < T || py >= kTbEY - T)
+            continue;
+        const int64_t p = pix_index(ox + px, oy + py, w);
+        float ov[3];
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            ov[ch] = c ? hi_of(s.o[r][ch]) : lo_of(s.o[r][ch]);
+            Oout[p * 3 + ch] = ov[ch];
+            Uout[p * 3 + ch] = c ? hi_of(s.u[r][ch]) : lo_of(s.u[r][ch]);
+        }
+        if (rgba)
+            reinterpret_cast<uint32_t*>(rgba)[p] = pack_rgba(ov[0], ov[1], ov[2]);
+    }
+}
+
+// ---- persistent, TMA-fed solver ----------------------------------------------
+// Same tile, same per-pixel arithmetic as solver_tb_kernel, but one CTA per
+// SM walks a list of tiles and the five input tiles (O, U, A, consWt, lap P:
+// 32 rows x 192 floats of the interleaved images each) of its NEXT tile are
+// fetched by TMA into shared memory while the current tile iterates, so
+// global-memory latency no longer serialises with the compute.  The tile
+// origin is fixed by the 8-pixel ring (kTbT), whatever the iteration count
+// of the launch, which keeps the TMA x coordinate (3 * origin floats) on the
+// 16-byte grid.  Needs width % 4 == 0 (16-byte row pitch) and 16-byte
+// aligned images; other sizes use solver_tb_kernel.
+constexpr int kIW = kTbEX - 2 * kTbT;                  // interior width  (48)
+constexpr int kIH = kTbEY - 2 * kTbT;                  // interior height (16)
+constexpr int kStageFloats = kTbEY * kTbEX * 3;        // one input tile
+constexpr int kStageBytes = kStageFloats * static_cast<int>(sizeof(float));
+constexpr int kPsSmem = 5 * kStageBytes + kTbSmem + 16;
+constexpr int kWaitSpins = 1 << 22;                    // bounded mbarrier wait (about a second)
+static_assert((3 * kTbT) % 4 == 0 && (3 * kIW) % 4 == 0, "TMA x coordinates must be 16-byte aligned");
+
+__device__ int g_device_timeout;  // set by a kernel whose bounded wait gave up
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n"
+        " .reg .pred p;\n"
+        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Spins at most `spins` polls (with back-off); false if the phase never completed.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int spins)
+{
+    for (int i = 0; i < spins; ++i) {
+        if (mbar_try_wait(bar, parity))
+            return true;
+        if (i > 32)
+            __nanosleep(256);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void issue_tile(float* stage, const CUtensorMap* m0, const CUtensorMap* m1,
+    const CUtensorMap* m2, const CUtensorMap* m3, const CUtensorMap* m4, int tile, int tiles_x, uint64_t* bar)
+{
+    const int ox = (tile % tiles_x) * kIW - kTbT;
+    const int oy = (tile / tiles_x) * kIH - kTbT;
+    mbar_expect_tx(bar, 5 * kStageBytes);
+    tma_load_2d(stage + 0 * kStageFloats, m0, 3 * ox, oy, bar);
+    tma_load_2d(stage + 1 * kStageFloats, m1, 3 * ox, oy, bar);
+    tma_load_2d(stage + 2 * kStageFloats, m2, 3 * ox, oy, bar);
+    tma_load_2d(stage + 3 * kStageFloats, m3, 3 * ox, oy, bar);
+    tma_load_2d(stage + 4 * kStageFloats, m4, 3 * ox, oy, bar);
+}
+
+__global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
+    solver_persistent_kernel(const __grid_constant__ CUtensorMap mO, const __grid_constant__ CUtensorMap mU,
+        const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mW,
+        const __grid_constant__ CUtensorMap mL, float* __restrict__ Oout, float* __restrict__ Uout, int w, int h,
+        int T, int k0, float step, float mom, uint8_t* __restrict__ rgba, int tiles_x, int ntiles)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* stage = reinterpret_cast<float*>(smem_raw);
+    float* obuf = stage + 5 * kStageFloats;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(obuf + 2 * 3 * kTbPlane);
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * 32 + tx;
+    const int px0 = 2 * tx, py0 = 2 * ty;
+
+    for (int i = tid; i < 2 * 3 * kTbPlane; i += blockDim.x * blockDim.y)
+        obuf[i] = 0.0f;
+    if (tid == 0)
+        mbar_init(bar, 1);
+    __syncthreads();
+    int tile = blockIdx.x;
+    if (tid == 0 && tile < ntiles)
+        issue_tile(stage, &mO, &mU, &mA, &mW, &mL, tile, tiles_x, bar);
+    uint32_t parity = 0;
+    for (; tile < ntiles; tile += gridDim.x) {
+        const int ox = (tile % tiles_x) * kIW - kTbT;
+        const int oy = (tile / tiles_x) * kIH - kTbT;
+        if (!mbar_wait_bounded(bar, parity, kWaitSpins)) {
+            if (tid == 0)
+                atomicExch(&g_device_timeout, 1);
+            mbar_wait_bounded(bar, parity, kWaitSpins);  // let copies still in flight land
+            return;
+        }
+        parity ^= 1;
+
+        TbState s;
+        float cnt[4];
+        bool vr[4], vl[4], vd[4], vu[4], inimg[4];
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int row = py0 + r;
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                const int q = 2 * r + c;
+                const int gx = ox + px0 + c, gy = oy + row;
+                inimg[q] = gx >= 0 && gx < w && gy >= 0 && gy < h;
+                vr[q] = (gx + 1) < (w - 1);
+                vl[q] = (gx - 1) >= 0;
+                vd[q] = (gy + 1) < (h - 1);
+                vu[q] = (gy - 1) >= 0;
+                cnt[q] = static_cast<float>(static_cast<int>(vr[q]) + static_cast<int>(vl[q]) +
+                                            static_cast<int>(vd[q]) + static_cast<int>(vu[q]));
+            }
+            // six consecutive floats: both pixels' RGB (TMA zero-fills outside the image)
+            f2 (*dst[5])[3] = {s.o, s.u, s.a, s.wt, s.lp};
+#pragma unroll
+            for (int arr = 0; arr < 5; ++arr) {
+                const float* src = stage + arr * kStageFloats + row * (3 * kTbEX) + 3 * px0;
+                const float2 v01 = *reinterpret_cast<const float2*>(src);
+                const float2 v23 = *reinterpret_cast<const float2*>(src + 2);
+                const float2 v45 = *reinterpret_cast<const float2*>(src + 4);
+                dst[arr][r][0] = pk(v01.x, v23.y);
+                dst[arr][r][1] = pk(v01.y, v45.x);
+                dst[arr][r][2] = pk(v23.x, v45.y);
+            }
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch)
+                *reinterpret_cast<f2*>(&obuf[ch * kTbPlane + (row + 1) * kTbPX + px0 + 2]) = s.o[r][ch];
+        }
+        __syncthreads();  // staging consumed, O published
+        if (tid == 0 && tile + static_cast<int>(gridDim.x) < ntiles) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue_tile(stage, &mO, &mU, &mA, &mW, &mL, tile + gridDim.x, tiles_x, bar);
+        }
+
+        const bool interior =
+            VSC_PACKED_MATH && ox >= 1 && oy >= 1 && ox + kTbEX - 1 <= w - 3 && oy + kTbEY - 1 <= h - 3;
+        if (interior)
+            tb_iterate<false>(s, vr, vl, vd, vu, cnt, obuf, T, k0, step, mom, px0, py0);
+        else
+            tb_iterate<true>(s, vr, vl, vd, vu, cnt, obuf, T, k0, step, mom, px0, py0);
+
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int r = q >> 1, c = q & 1;
+            const int px = px0 + c, py = py0 + r;
+            if (!inimg[q] || px < kTbT || px >= kTbEX - kTbT || py < kTbT || py >= kTbEY - kTbT)
+                continue;
+            const int64_t p = pix_index(ox + px, oy + py, w);
+            float ov[3];
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+                ov[ch] = c ? hi_of(s.o[r][ch]) : lo_of(s.o[r][ch]);
+                Oout[p * 3 + ch] = ov[ch];
+                Uout[p * 3 + ch] = c ? hi_of(s.u[r][ch]) : lo_of(s.u[r][ch]);
+            }
+            if (rgba)
+                reinterpret_cast<uint32_t*>(rgba)[p] = pack_rgba(ov[0], ov[1], ov[2]);
+        }
+    }
+}
+
+// An mbarrier nobody arrives on, waited for with a bounded spin: exercises
+// the timeout path of the bounded waits (sets g_device_timeout, returns).
+__global__ void bounded_wait_selftest_kernel(int spins)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0)
+        mbar_init(&bar, 1);
+    __syncthreads();
+    if (!mbar_wait_bounded(&bar, 0, spins) && threadIdx.x == 0)
+        atomicExch(&g_device_timeout, 1);
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+    CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+// 2D map over an interleaved w x h x 3 float image: x = float index in a row.
+bool encode_image_map(CUtensorMap* m, const float* base, int w, int h)
+{
+    EncodeTiledFn fn = encode_fn();
+    if (!fn)
+        return false;
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(w) * 3, static_cast<cuuint64_t>(h)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(w) * 3 * sizeof(float)};
+    const cuuint32_t box[2] = {3 * kTbEX, kTbEY};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+struct DeviceInfo {
+    int sms = 0;
+    bool tb_smem = false, ps_smem = false;
+};
+
+// The solver kernels need more than 48 KB of dynamic shared memory; the
+// opt-in is a per-device function attribute, set once per device together
+// with the SM count the persistent kernel sizes its grid by.
+cudaError_t device_info(DeviceInfo** out)
+{
+    static std::mutex mu;
+    static DeviceInfo info[64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    if (dev < 0 || dev >= 64)
+        return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    DeviceInfo& d = info[dev];
+    if (!d.sms) {
+        if ((e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+            return e;
+        if ((e = cudaFuncSetAttribute(solver_tb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTbSmem)) !=
+            cudaSuccess)
+            return e;
+        d.ps_smem = cudaFuncSetAttribute(solver_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                        kPsSmem) == cudaSuccess;
+        cudaGetLastError();
+    }
+    *out = &d;
+    return cudaSuccess;
+}
+
+bool aligned16p(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+}  // namespace
+
+size_t solver_workspace_floats(int w, int h) { return static_cast<size_t>(w) * h * 3 * 4; }
+
+cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,
+    float step, float mom, float* workspace, cudaStream_t st, int* launches, uint8_t* rgba_out)
+{
+    const size_t n = static_cast<size_t>(w) * h * 3;
+    float* L = workspace;
+    float* U[2] = {workspace + n, workspace + 2 * n};
+    float* O2 = workspace + 3 * n;
+    int nl = 0;
+    if (num_iter <= 0) {
+        if (rgba_out) {
+            cudaError_t e = launch_float_to_rgba(O, rgba_out, static_cast<int64_t>(w) * h, st);
+            if (launches)
+                *launches += 1;
+            return e;
+        }
+        return cudaSuccess;
+    }
+    DeviceInfo* di = nullptr;
+    cudaError_t e0 = device_info(&di);
+    if (e0 != cudaSuccess)
+        return e0;
+    const dim3 b(32, 8);
+    lap_pr_kernel<<<grid2d(w, h, b), b, 0, st>>>(P, L, w, h);
+    ++nl;
+    // Launches of up to kTbT iterations; ping-pong O between O and O2 and U
+    // between its two buffers so that the last launch writes O.
+    const int nlaunch = (num_iter + kTbT - 1) / kTbT;
+    float* cur = (nlaunch % 2 == 0) ? O : O2;
+    if (cur != O) {
+        cudaError_t e = cudaMemcpyAsync(O2, O, n * sizeof(float), cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess)
+            return e;
+    }
+    // TMA path: 16-byte row pitch and aligned images
+    bool tma = di->ps_smem && (w % 4) == 0 && aligned16p(O) && aligned16p(O2) && aligned16p(U[0]) &&
+               aligned16p(U[1]) && aligned16p(A) && aligned16p(Wt) && aligned16p(L);
+    CUtensorMap mO[2], mU[2], mA, mW, mL;
+    if (tma)
+        tma = encode_image_map(&mO[0], O, w, h) && encode_image_map(&mO[1], O2, w, h) &&
+              encode_image_map(&mU[0], U[0], w, h) && encode_image_map(&mU[1], U[1], w, h) &&
+              encode_image_map(&mA, A, w, h) && encode_image_map(&mW, Wt, w, h) && encode_image_map(&mL, L, w, h);
+    const int tiles_x = (w + kIW - 1) / kIW, tiles_y = (h + kIH - 1) / kIH;
+    const int ntiles = tiles_x * tiles_y;
+    int k0 = 0;
+    for (int li = 0; li < nlaunch; ++li) {
+        const int T = std::min(kTbT, num_iter - k0);
+        float* nxt = (cur == O) ? O2 : O;
+        uint8_t* rg = (li == nlaunch - 1) ? rgba_out : nullptr;
+        if (tma) {
+            const int grid = std::min(ntiles, di->sms);
+            solver_persistent_kernel<<<grid, dim3(32, kTbEY / 2), kPsSmem, st>>>(mO[cur == O ? 0 : 1], mU[li & 1], mA,
+                mW, mL, nxt, U[(li + 1) & 1], w, h, T, k0, step, mom, rg, tiles_x, ntiles);
+        } else {
+            const dim3 grid((w + (kTbEX - 2 * T) - 1) / (kTbEX - 2 * T), (h + (kTbEY - 2 * T) - 1) / (kTbEY - 2 * T));
+            solver_tb_kernel<<<grid, dim3(32, kTbEY / 2), kTbSmem, st>>>(cur, nxt, U[li & 1], U[(li + 1) & 1], L, A,
+                Wt, w, h, T, k0, step, mom, rg);
+        }
+        ++nl;
+        k0 += T;
+        cur = nxt;
+    }
+    if (launches)
+        *launches += nl;
+    return cudaGetLastError();
+}
+
+cudaError_t check_device_timeout(int* flagged)
+{
+    int v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_device_timeout, sizeof(int));
+    if (e != cudaSuccess)
+        return e;
+    if (v) {
+        const int zero = 0;
+        e = cudaMemcpyToSymbol(g_device_timeout, &zero, sizeof(int));
+    }
+    *flagged = v;
+    return e;
+}
+
+cudaError_t launch_bounded_wait_selftest(int spins, cudaStream_t st)
+{
+    bounded_wait_selftest_kernel<<<1, 32, 0, st>>>(spins);
+    return cudaGetLastError();
+}
+
+}  // namespace vsc

@@ -5,55 +5,81 @@
 // layout.  Every kernel keeps the reference's per-pixel expression order and
 // is compiled with -fmad=false, so it reproduces the CPU restatement of the
 // reference bit for bit.  Differences from the reference's schedule:
-//   - the solver is a Jacobi iteration (the reference updates consisOut in
-//     place, flowconsistency.cu:370, so neighbours read a timing-dependent
-//     mix of old and new values);
-//   - the Laplacian of the processed image, which the reference recomputes
-//     in every iteration, is computed once per solve (same expression, same
-//     bits);
+//   - the solver lives in vsc_solver.cu;
 //   - the orchestrator uses one fused kernel for the five warps, the
 //     adaptive combination and the consistency weights (the reference runs
 //     seven kernels with a device synchronisation after each).
 #include "vsc_internal.h"
 #include "vsc_math.cuh"
 
+
 namespace vsc {
 namespace {
 
-__device__ __forceinline__ int64_t pix_index(int x, int y, int w) { return static_cast<int64_t>(y) * w + x; }
 
 // ---- frame I/O (gpuimage.cu:39-67) ---------------------------------------
-__global__ void rgba_to_float_kernel(const uint8_t* __restrict__ rgba, float* __restrict__ out, int64_t npix)
+// float(double(v) / 255.0) equals the single-precision quotient v / 255.0f
+// for every byte value (checked exhaustively by the tests), so the table is
+// built with one IEEE float division per entry.
+__device__ __forceinline__ void build_lut(float* lut)
+{
+    for (int v = threadIdx.x; v < 256; v += blockDim.x)
+        lut[v] = __fdiv_rn(static_cast<float>(v), 255.0f);
+    __syncthreads();
+}
+
+// 4 pixels per thread: one 16-byte RGBA load, three 16-byte float stores.
+__global__ void rgba_to_float4_kernel(const uint4* __restrict__ rgba, float4* __restrict__ out, int64_t nquad)
 {
     __shared__ float lut[256];
-    for (int v = threadIdx.x; v < 256; v += blockDim.x)
-        lut[v] = static_cast<float>(static_cast<double>(v) / 255.0);
-    __syncthreads();
+    build_lut(lut);
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-    if (i >= npix)
+    if (i >= nquad)
         return;
-    const uchar4 px = reinterpret_cast<const uchar4*>(rgba)[i];
-    out[i * 3 + 0] = lut[px.x];
-    out[i * 3 + 1] = lut[px.y];
-    out[i * 3 + 2] = lut[px.z];
+    const uint4 px = rgba[i];
+    const uint32_t w[4] = {px.x, px.y, px.z, px.w};
+    float f[12];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        f[3 * k + 0] = lut[w[k] & 0xff];
+        f[3 * k + 1] = lut[(w[k] >> 8) & 0xff];
+        f[3 * k + 2] = lut[(w[k] >> 16) & 0xff];
+    }
+    out[3 * i + 0] = make_float4(f[0], f[1], f[2], f[3]);
+    out[3 * i + 1] = make_float4(f[4], f[5], f[6], f[7]);
+    out[3 * i + 2] = make_float4(f[8], f[9], f[10], f[11]);
 }
 
-__device__ __forceinline__ uint8_t quantize(float v)
+__global__ void rgba_to_float_kernel(const uint8_t* __restrict__ rgba, float* __restrict__ out, int64_t first,
+    int64_t npix)
 {
-    return static_cast<uint8_t>(__float2uint_rd(fabsf(v) * 255.0f));
-}
-
-__global__ void float_to_rgba_kernel(const float* __restrict__ in, uint8_t* __restrict__ rgba, int64_t npix)
-{
-    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    __shared__ float lut[256];
+    build_lut(lut);
+    const int64_t i = first + blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (i >= npix)
         return;
-    uchar4 px;
-    px.x = quantize(in[i * 3 + 0]);
-    px.y = quantize(in[i * 3 + 1]);
-    px.z = quantize(in[i * 3 + 2]);
-    px.w = 1;
-    reinterpret_cast<uchar4*>(rgba)[i] = px;
+    out[i * 3 + 0] = lut[rgba[i * 4 + 0]];
+    out[i * 3 + 1] = lut[rgba[i * 4 + 1]];
+    out[i * 3 + 2] = lut[rgba[i * 4 + 2]];
+}
+
+__global__ void float4_to_rgba_kernel(const float4* __restrict__ in, uint4* __restrict__ rgba, int64_t nquad)
+{
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= nquad)
+        return;
+    const float4 a = in[3 * i + 0], b = in[3 * i + 1], c = in[3 * i + 2];
+    rgba[i] = make_uint4(pack_rgba(a.x, a.y, a.z), pack_rgba(a.w, b.x, b.y), pack_rgba(b.z, b.w, c.x),
+        pack_rgba(c.y, c.z, c.w));
+}
+
+__global__ void float_to_rgba_kernel(const float* __restrict__ in, uint8_t* __restrict__ rgba, int64_t first,
+    int64_t npix)
+{
+    const int64_t i = first + blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= npix)
+        return;
+    reinterpret_cast<uint32_t*>(rgba)[i] = pack_rgba(in[i * 3 + 0], in[i * 3 + 1], in[i * 3 + 2]);
 }
 
 // ---- kernel_warp (flowconsistency.cu:77-114) --------------------------------
@@ -161,8 +187,9 @@ __device__ __forceinline__ void bilinear_px(const float* __restrict__ in, int iw
 {
     const float xx = static_cast<float>(ox) * static_cast<float>(iw) / static_cast<float>(ow);
     const float yy = static_cast<float>(oy) * static_cast<float>(ih) / static_cast<float>(oh);
-    const int ix = static_cast<int>(floorf(xx));
-    const int iy = static_cast<int>(floorf(yy));
+    // xx < iw for every size the API accepts; the clamp only guards the index
+    const int ix = min(static_cast<int>(floorf(xx)), iw - 1);
+    const int iy = min(static_cast<int>(floorf(yy)), ih - 1);
     const float fx = xx - static_cast<float>(ix);
     const float fy = yy - static_cast<float>(iy);
     const int ix1 = min(ix + 1, iw - 1);
@@ -198,99 +225,6 @@ __global__ void pyr_down3_kernel(const float* __restrict__ P, const float* __res
     bilinear_px(P, iw, ih, ow, oh, 3, ox, oy, Pd + o);
     bilinear_px(A, iw, ih, ow, oh, 3, ox, oy, Ad + o);
     bilinear_px(Wt, iw, ih, ow, oh, 3, ox, oy, Wd + o);
-}
-
-// ---- kernel_consist_out (flowconsistency.cu:193-258) ------------------------
-// Laplacian of the processed image with the reference's neighbour rule and
-// summation order (right, left, bottom, top, then - cnt * centre).
-__global__ void lap_pr_kernel(const float* __restrict__ P, float* __restrict__ L, int w, int h)
-{
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= w || y >= h)
-        return;
-    const int64_t i0 = pix_index(x, y, w) * 3;
-    const int64_t rs = static_cast<int64_t>(w) * 3;
-    for (int c = 0; c < 3; ++c) {
-        const int64_t i = i0 + c;
-        int cnt = 0;
-        float lap = 0.0f;
-        if ((x + 1) < (w - 1)) {
-            lap += P[i + 3];
-            cnt += 1;
-        }
-        if ((x - 1) >= 0) {
-            lap += P[i - 3];
-            cnt += 1;
-        }
-        if ((y + 1) < (h - 1)) {
-            lap += P[i + rs];
-            cnt += 1;
-        }
-        if ((y - 1) >= 0) {
-            lap += P[i - rs];
-            cnt += 1;
-        }
-        lap -= static_cast<float>(cnt) * P[i];
-        L[i] = lap;
-    }
-}
-
-// One Jacobi step: reads Oc, writes On and U.
-__global__ void solver_iter_kernel(const float* __restrict__ Oc, float* __restrict__ On, float* __restrict__ U,
-    const float* __restrict__ L, const float* __restrict__ A, const float* __restrict__ Wt, int w, int h, float step,
-    float mom, int is_mom, uint8_t* __restrict__ rgba)
-{
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= w || y >= h)
-        return;
-    const int64_t p = pix_index(x, y, w);
-    const int64_t rs = static_cast<int64_t>(w) * 3;
-    float res[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const int64_t i = p * 3 + c;
-        int cnt = 0;
-        float lap_out = 0.0f;
-        if ((x + 1) < (w - 1)) {
-            lap_out += Oc[i + 3];
-            cnt += 1;
-        }
-        if ((x - 1) >= 0) {
-            lap_out += Oc[i - 3];
-            cnt += 1;
-        }
-        if ((y + 1) < (h - 1)) {
-            lap_out += Oc[i + rs];
-            cnt += 1;
-        }
-        if ((y - 1) >= 0) {
-            lap_out += Oc[i - rs];
-            cnt += 1;
-        }
-        const float o = Oc[i];
-        lap_out -= static_cast<float>(cnt) * o;
-        const float tmp_1 = Wt[i] * (o - A[i]);
-        const float tmp_2 = lap_out - L[i];
-        const float grad_val = tmp_2 - tmp_1;
-        float out_val;
-        if (is_mom)
-            out_val = o + step * grad_val + mom * U[i];
-        else
-            out_val = o + step * grad_val;
-        U[i] = step * grad_val;
-        On[i] = out_val;
-        res[c] = out_val;
-    }
-    if (rgba) {
-        uchar4 px;
-        px.x = quantize(res[0]);
-        px.y = quantize(res[1]);
-        px.z = quantize(res[2]);
-        px.w = 1;
-        reinterpret_cast<uchar4*>(rgba)[p] = px;
-    }
 }
 
 // ---- fused front end of doOneStep (videostabilizer.cpp:182-198) --------------
@@ -341,15 +275,33 @@ inline dim3 grid2d(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h +
 
 }  // namespace
 
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
 cudaError_t launch_rgba_to_float(const uint8_t* rgba, float* out, int64_t npix, cudaStream_t st)
 {
-    rgba_to_float_kernel<<<static_cast<unsigned>((npix + 255) / 256), 256, 0, st>>>(rgba, out, npix);
+    int64_t done = 0;
+    if (aligned16(rgba) && aligned16(out) && npix >= 4) {
+        const int64_t nq = npix / 4;
+        rgba_to_float4_kernel<<<static_cast<unsigned>((nq + 255) / 256), 256, 0, st>>>(
+            reinterpret_cast<const uint4*>(rgba), reinterpret_cast<float4*>(out), nq);
+        done = nq * 4;
+    }
+    if (done < npix)
+        rgba_to_float_kernel<<<static_cast<unsigned>((npix - done + 255) / 256), 256, 0, st>>>(rgba, out, done, npix);
     return cudaGetLastError();
 }
 
 cudaError_t launch_float_to_rgba(const float* in, uint8_t* rgba, int64_t npix, cudaStream_t st)
 {
-    float_to_rgba_kernel<<<static_cast<unsigned>((npix + 255) / 256), 256, 0, st>>>(in, rgba, npix);
+    int64_t done = 0;
+    if (aligned16(rgba) && aligned16(in) && npix >= 4) {
+        const int64_t nq = npix / 4;
+        float4_to_rgba_kernel<<<static_cast<unsigned>((nq + 255) / 256), 256, 0, st>>>(
+            reinterpret_cast<const float4*>(in), reinterpret_cast<uint4*>(rgba), nq);
+        done = nq * 4;
+    }
+    if (done < npix)
+        float_to_rgba_kernel<<<static_cast<unsigned>((npix - done + 255) / 256), 256, 0, st>>>(in, rgba, done, npix);
     return cudaGetLastError();
 }
 
@@ -405,48 +357,6 @@ cudaError_t launch_resize_nearest(const float* in, int iw, int ih, float* out, i
 {
     const dim3 b(32, 8);
     resize_nearest_kernel<<<grid2d(ow, oh, b), b, 0, st>>>(in, iw, ih, out, ow, oh);
-    return cudaGetLastError();
-}
-
-size_t solver_workspace_floats(int w, int h) { return static_cast<size_t>(w) * h * 3 * 3; }
-
-cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,
-    float step, float mom, float* workspace, cudaStream_t st, int* launches, uint8_t* rgba_out)
-{
-    const size_t n = static_cast<size_t>(w) * h * 3;
-    float* U = workspace;
-    float* L = workspace + n;
-    float* O2 = workspace + 2 * n;
-    const dim3 b(32, 8);
-    const dim3 g = grid2d(w, h, b);
-    int nl = 0;
-    if (num_iter <= 0) {
-        if (rgba_out) {
-            cudaError_t e = launch_float_to_rgba(O, rgba_out, static_cast<int64_t>(w) * h, st);
-            if (launches)
-                *launches += 1;
-            return e;
-        }
-        return cudaSuccess;
-    }
-    lap_pr_kernel<<<g, b, 0, st>>>(P, L, w, h);
-    ++nl;
-    // Ping-pong so that the last iteration writes O itself.
-    float* cur = (num_iter % 2 == 0) ? O : O2;
-    if (cur != O) {
-        cudaError_t e = cudaMemcpyAsync(O2, O, n * sizeof(float), cudaMemcpyDeviceToDevice, st);
-        if (e != cudaSuccess)
-            return e;
-    }
-    for (int k = 0; k < num_iter; ++k) {
-        float* nxt = (cur == O) ? O2 : O;
-        solver_iter_kernel<<<g, b, 0, st>>>(
-            cur, nxt, U, L, A, Wt, w, h, step, mom, k > 0 ? 1 : 0, (k == num_iter - 1) ? rgba_out : nullptr);
-        ++nl;
-        cur = nxt;
-    }
-    if (launches)
-        *launches += nl;
     return cudaGetLastError();
 }
 
