@@ -175,6 +175,87 @@ def cpu_baseline_sample(frames, threads: int, n_frames: int = 10):
             "seconds": dt}
 
 
+def reference_gpu_timing(frames, reps: int = 5):
+    """The reference's own CUDA kernels (compiled in place for sm_103a with
+    nvcc's default flags, launched with the reference's geometry and host
+    schedule by oracle/ref_gpu) timed on this GPU at 1920x1080: one
+    stabilization pass (videostabilizer.cpp:178-247, synchronising after every
+    launcher and allocating inside get_consist_out and copyToQImage as the
+    reference does) and its Correlation / Warp op calls over the five flow
+    levels of one direction.  Host wall time, since the reference schedule
+    synchronises inside.  None when no GPU or no cubin is present."""
+    try:
+        import torch
+    except ImportError:
+        return None
+    if not torch.cuda.is_available():
+        return None
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    import ref_gpu as RG
+
+    O.build(ref=False)
+    if not RG.available("default"):
+        return None
+    L = RG.load("default")
+    dev = torch.device("cuda", 0)
+    f = lambda a: torch.from_numpy(O.rgba_to_float(a)).to(dev)  # noqa: E731
+    orig = [f(o) for o, _ in frames[:3]]
+    proc = [f(p) for _, p in frames[:3]]
+    g = torch.Generator(device=dev).manual_seed(2)
+    flows = [torch.randn((H, W, 3), device=dev, generator=g) * 2 for _ in range(2)]
+    for fl in flows:
+        fl[..., 2] = 0
+    last = proc[2].clone()
+    e = lambda c=3, w=W, h=H: torch.empty((h, w, c), dtype=torch.float32, device=dev)  # noqa: E731
+    ins = [*orig, *proc, flows[0], flows[1], last]
+    scratch = [e() for _ in range(11)]
+    lvl0 = [e() for _ in range(4)]
+    lvl1 = [e(3, W // 2, H // 2) for _ in range(4)]
+    host = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory()
+    arr = lambda ts: (RG.Img * len(ts))(*[RG.img(t) for t in ts])  # noqa: E731
+    a_in, a_s, a_0, a_1 = arr(ins), arr(scratch), arr(lvl0), arr(lvl1)
+
+    def stab():
+        RG.check(L, L.rg_stab_pass(a_in, a_s, a_0, a_1, 2, 150, 6800.0, 6800.0, 2.0, 0.15, 0.15, host.data_ptr()))
+
+    stab()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        stab()
+    torch.cuda.synchronize()
+    stab_ms = 1000 * (time.perf_counter() - t0) / reps
+    # the ops of one flow direction over the PWC pyramid of a 1920x1088 frame
+    levels = [(480, 272, 32), (240, 136, 64), (120, 68, 96), (60, 34, 128), (30, 17, 196)]
+    bufs = []
+    for lw, lh, lc in levels:
+        a = torch.randn((1, lc, lh, lw), device=dev, generator=g)
+        b = torch.randn((1, lc, lh, lw), device=dev, generator=g)
+        fl = torch.randn((1, 2, lh, lw), device=dev, generator=g)
+        bufs.append((a, b, fl, torch.empty((1, 81, lh, lw), device=dev), torch.empty_like(a), lw, lh, lc))
+
+    def ops(kind):
+        for a, b, fl, cv, wo, lw, lh, lc in bufs:
+            if kind == "corr":
+                RG.check(L, L.rg_correlation(a.data_ptr(), b.data_ptr(), cv.data_ptr(), 1, lc, lh, lw, 4, None))
+            else:
+                RG.check(L, L.rg_warp_op(b.data_ptr(), fl.data_ptr(), wo.data_ptr(), 1, lc, lh, lw, None))
+        torch.cuda.synchronize()
+
+    res = {"stab_pass_ms": stab_ms}
+    for kind in ("corr", "warp"):
+        ops(kind)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            ops(kind)
+        res[f"{kind}_pyramid_one_direction_ms"] = 1000 * (time.perf_counter() - t0) / reps
+    res["source"] = ("the reference's CUDA kernels (flowconsistency.cu, gpuimage.cu, correlation_cuda.cu, "
+                     "warp_cuda.cu) compiled in place for sm_103a with nvcc defaults, launched with the "
+                     "reference's geometry and host schedule; 1920x1080, host wall time")
+    return res
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -206,6 +287,7 @@ def run_reference(args):
         step(args.warmup + t)
     dt = time.perf_counter() - t0
     v = args.steps / dt
+    ref_gpu = reference_gpu_timing(frames)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": 0, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,
@@ -218,6 +300,8 @@ def run_reference(args):
                                    "reference has no CPU stabilization pass"},
         "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if ref_gpu:
+        line["reference_gpu"] = ref_gpu
     print(json.dumps(line))
 
 

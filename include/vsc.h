@@ -184,7 +184,8 @@ typedef struct vsc_stabilizer_config {
     int32_t use_graphs;     /* 1: after the first step, each step replays a CUDA graph
                                captured on first use (needs a non-default stream);
                                the graph is re-captured when the hyper-parameters or
-                               the device output pointer change */
+                               the device output pointer change; steps run without
+                               a graph while stage timing is on */
 } vsc_stabilizer_config;
 
 /* Replaces the VideoStabilizer constructor (videostabilizer.cpp:46-102).

@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import shutil
 import subprocess
 from pathlib import Path
 
@@ -43,10 +44,13 @@ class Hyper(C.Structure):
 def build(ref: bool = True) -> None:
     """Compile the restatement (and the in-place reference ops when the
     reference tree is present)."""
-    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    targets = ["_build/liboracle.so"]
+    if shutil.which("nvcc") or Path("/usr/local/cuda/bin/nvcc").exists():
+        targets.append("_build/librefgpu.so")
+    subprocess.run(["make", "-s", "-C", str(HERE), *targets], check=True)
     refdir = os.environ.get("VSC_REFERENCE_ROOT", "/root/reference")
     if ref and Path(refdir, "src", "ort_custom_ops").is_dir():
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={refdir}"], check=True)
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", "refgpu", f"REF={refdir}"], check=True)
 
 
 _lib = None

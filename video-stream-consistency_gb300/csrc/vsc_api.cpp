@@ -821,7 +821,8 @@ VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int
     cudaError_t e = cudaSuccess;
     // The first step (which seeds the feedback frame) runs directly; later
     // steps replay a captured graph when the stream allows capture.
-    const bool graphed = s->use_graphs && s->started && s->st != nullptr &&
+    // (stage timing records plain events, so timed steps are not captured)
+    const bool graphed = s->use_graphs && !s->timing && s->started && s->st != nullptr &&
                          launch_step_graph(s, hp, rgba_dev, &nl, &e);
     if (!graphed)
         e = enqueue_step(s, hp, rgba_dev, &nl);

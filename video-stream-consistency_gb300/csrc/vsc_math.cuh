@@ -59,40 +59,4 @@ __device__ __forceinline__ uint32_t pack_rgba(float r, float g, float b)
            (static_cast<uint32_t>(quantize(b)) << 16) | (1u << 24);
 }
 
-// VSC_PACKED_MATH selects the packed f32x2 instruction paths of the
-// correlation and solver kernels (1) or their scalar forms (0).
-#ifndef VSC_PACKED_MATH
-#define VSC_PACKED_MATH 0
-#endif
-
-// Packed single precision: two fp32 lanes in one 64-bit register, operated
-// on by the .rn.f32x2 instructions (each lane rounded exactly as the scalar
-// instruction would round it, no contraction).
-typedef unsigned long long f2;  // two fp32 lanes (lo = left pixel, hi = right pixel)
-
-__device__ __forceinline__ f2 pk(float lo, float hi)
-{
-    return (static_cast<f2>(__float_as_uint(hi)) << 32) | __float_as_uint(lo);
-}
-__device__ __forceinline__ float lo_of(f2 v) { return __uint_as_float(static_cast<unsigned>(v)); }
-__device__ __forceinline__ float hi_of(f2 v) { return __uint_as_float(static_cast<unsigned>(v >> 32)); }
-__device__ __forceinline__ f2 add2(f2 a, f2 b)
-{
-    f2 r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 sub2(f2 a, f2 b)
-{
-    f2 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 mul2(f2 a, f2 b)
-{
-    f2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-
 }  // namespace vsc

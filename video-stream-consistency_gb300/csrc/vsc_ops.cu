@@ -11,10 +11,12 @@
 // inputs (no temporaries), and every thread keeps 4 adjacent pixels x
 // (2md+1) horizontal displacements of one vertical displacement in
 // registers.  Per channel a thread reads 1 + ceil((4+2md)/4) 128-bit words
-// of shared memory for 4*(2md+1) multiply-adds, issued as packed f32x2
-// multiplies and adds on pixel pairs.  Sums run in channel order with
-// separately rounded products and sums, which is the reference CPU op's
-// arithmetic, so results match it bit for bit.
+// of shared memory for 4*(2md+1) multiply-adds.  Sums run in channel order
+// with separately rounded products and sums (-fmad=false), which is the
+// reference CPU op's arithmetic, so results match it bit for bit.  (The
+// packed f32x2 instructions would halve the issue count, but ptxas fuses a
+// packed multiply followed by a packed add into an FMA even under
+// -fmad=false, which changes the rounding; they are not used.)
 //
 // Warp (warp.cc:71-133, warp_cuda.cu:28-98): one thread per pixel and group
 // of 8 channels; the flow, the four bilinear weights and the 0.999 edge mask
@@ -63,11 +65,12 @@ __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
     const float* a_n = in1 + n * sa;  // batch strides in elements (may be negative)
     const float* b_n = in2 + n * sb;
 
-    // acc[j][0] = pixels (0, 1), acc[j][1] = pixels (2, 3) of displacement j
-    f2 acc[P][2];
+    float acc[P][4];
 #pragma unroll
     for (int j = 0; j < P; ++j)
-        acc[j][0] = acc[j][1] = pk(0.0f, 0.0f);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            acc[j][i] = 0.0f;
 
     for (int c0 = 0; c0 < C; c0 += kCorrCC) {
         const int cc = min(kCorrCC, C - c0);
@@ -97,7 +100,7 @@ __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
         __syncthreads();
         for (int c = 0; c < cc; ++c) {
             const float4 av = *reinterpret_cast<const float4*>(&s1[(c * kCorrTH + ty) * kCorrTW + 4 * tx]);
-            const f2 a01 = pk(av.x, av.y), a23 = pk(av.z, av.w);
+            const float a[4] = {av.x, av.y, av.z, av.w};
             float b[4 * G::NB];
             const float* brow = &s2[(c * G::RH + ty + tz) * G::S2W + 4 * tx];
 #pragma unroll
@@ -108,19 +111,11 @@ __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
                 b[4 * q + 2] = bv.z;
                 b[4 * q + 3] = bv.w;
             }
-#if VSC_PACKED_MATH
 #pragma unroll
-            for (int j = 0; j < P; ++j) {
-                acc[j][0] = add2(acc[j][0], mul2(a01, pk(b[j], b[j + 1])));
-                acc[j][1] = add2(acc[j][1], mul2(a23, pk(b[j + 2], b[j + 3])));
-            }
-#else
+            for (int j = 0; j < P; ++j)
 #pragma unroll
-            for (int j = 0; j < P; ++j) {
-                acc[j][0] = pk(lo_of(acc[j][0]) + av.x * b[j], hi_of(acc[j][0]) + av.y * b[j + 1]);
-                acc[j][1] = pk(lo_of(acc[j][1]) + av.z * b[j + 2], hi_of(acc[j][1]) + av.w * b[j + 3]);
-            }
-#endif
+                for (int i = 0; i < 4; ++i)
+                    acc[j][i] = acc[j][i] + a[i] * b[i + j];
         }
         __syncthreads();
     }
@@ -136,11 +131,10 @@ __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
     for (int j = 0; j < P; ++j) {
         const int dx = j - MD;
         float r[4];
-        const float sums[4] = {lo_of(acc[j][0]), hi_of(acc[j][0]), lo_of(acc[j][1]), hi_of(acc[j][1])};
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const int xs = x0 + i + dx;
-            float v = (yok && xs >= 0 && xs < W) ? sums[i] : 0.0f;
+            float v = (yok && xs >= 0 && xs < W) ? acc[j][i] : 0.0f;
             if (legacy)
                 v = __fdiv_rn(v, fc);
             r[i] = v;

@@ -64,14 +64,11 @@ __global__ void lap_pr_kernel(const float* __restrict__ P, float* __restrict__ L
 // interior (the tile minus a kTbT-wide ring) is exact after kTbT iterations
 // and is written back.  Each of the 512 threads owns a 2x2 pixel block and
 // keeps its state (O, U) and the per-pixel constants (lap P, A, consWt) in
-// registers as horizontal pixel pairs; O is published to shared memory
-// (double-buffered) for the rows of the neighbouring warps, and horizontal
-// neighbours travel by warp shuffle (one warp spans the full tile width).
-// Tiles away from the image border run the update on pixel pairs with the
-// packed single-precision instructions (add/sub/mul .rn.f32x2: two IEEE
-// operations, each rounded as the scalar one would be); border tiles apply
-// the reference's neighbour-validity rule per pixel.  Either way the result
-// equals the one-iteration-per-launch Jacobi bit for bit.
+// registers; O is published to shared memory (double-buffered) for the rows
+// of the neighbouring warps, and horizontal neighbours travel by warp
+// shuffle (one warp spans the full tile width).  Tiles away from the image
+// border skip the reference's neighbour-validity selects.  The result equals
+// the one-iteration-per-launch Jacobi bit for bit.
 #ifndef VSC_SOLVER_T
 #define VSC_SOLVER_T 8
 #endif
@@ -83,34 +80,24 @@ constexpr int kTbPlane = kTbPX * (kTbEY + 2);  // one colour plane with a 1-row 
 constexpr int kTbSmem = 2 * 3 * kTbPlane * static_cast<int>(sizeof(float));
 static_assert(2 * kTbT < kTbEY, "tile too small for the iteration count");
 
-// One Jacobi step of a pixel pair with all four neighbours valid (cnt = 4).
-__device__ __forceinline__ f2 jacobi_pair(f2 o, f2& u, f2 a, f2 wt, f2 lp, f2 right, f2 left, f2 down, f2 up,
-    f2 four, f2 step2, f2 mom2, bool mom_on)
-{
-    f2 lap = add2(pk(0.0f, 0.0f), right);
-    lap = add2(lap, left);
-    lap = add2(lap, down);
-    lap = add2(lap, up);
-    lap = sub2(lap, mul2(four, o));
-    const f2 tmp_1 = mul2(wt, sub2(o, a));
-    const f2 tmp_2 = sub2(lap, lp);
-    const f2 sg = mul2(step2, sub2(tmp_2, tmp_1));
-    f2 out = add2(o, sg);
-    if (mom_on)
-        out = add2(out, mul2(mom2, u));
-    u = sg;
-    return out;
-}
-
-// One Jacobi step of one pixel with the reference's validity rule.
+// One Jacobi step of one pixel (kernel_consist_out's expression).  With kAll
+// every neighbour is valid (cnt = 4) and the validity selects are skipped.
+template <bool kAll>
 __device__ __forceinline__ float jacobi_px(float o, float& u, float a, float wt, float lp, float right, float left,
     float down, float up, bool vr, bool vl, bool vd, bool vu, float cnt, float step, float mom, bool mom_on)
 {
     float lap = 0.0f;
-    lap += vr ? right : 0.0f;
-    lap += vl ? left : 0.0f;
-    lap += vd ? down : 0.0f;
-    lap += vu ? up : 0.0f;
+    if (kAll) {
+        lap += right;
+        lap += left;
+        lap += down;
+        lap += up;
+    } else {
+        lap += vr ? right : 0.0f;
+        lap += vl ? left : 0.0f;
+        lap += vd ? down : 0.0f;
+        lap += vu ? up : 0.0f;
+    }
     lap -= cnt * o;
     const float tmp_1 = wt * (o - a);
     const float tmp_2 = lap - lp;
@@ -123,55 +110,42 @@ __device__ __forceinline__ float jacobi_px(float o, float& u, float a, float wt,
 }
 
 struct TbState {
-    f2 o[2][3], u[2][3], a[2][3], wt[2][3], lp[2][3];  // [row][channel], pair = (left, right) pixel
+    float o[4][3], u[4][3], a[4][3], wt[4][3], lp[4][3];  // [pixel q = 2*row + col][channel]
 };
 
-template <bool kBorder>
+template <bool kAll>
 __device__ __forceinline__ void tb_iterate(TbState& s, const bool (&vr)[4], const bool (&vl)[4],
     const bool (&vd)[4], const bool (&vu)[4], const float (&cnt)[4], float* smem, int T, int k0, float step,
     float mom, int px0, int py0)
 {
-    const f2 four = pk(4.0f, 4.0f), step2 = pk(step, step), mom2 = pk(mom, mom);
     for (int k = 0; k < T; ++k) {
         const int cur = k & 1;
         const bool mom_on = (k0 + k) > 0;
 #pragma unroll
         for (int ch = 0; ch < 3; ++ch) {
             const float* S = smem + (cur * 3 + ch) * kTbPlane;
-            const f2 up = *reinterpret_cast<const f2*>(&S[py0 * kTbPX + px0 + 2]);
-            const f2 dn = *reinterpret_cast<const f2*>(&S[(py0 + 3) * kTbPX + px0 + 2]);
-            const f2 r0p = s.o[0][ch], r1p = s.o[1][ch];
-            const float o0 = lo_of(r0p), o1 = hi_of(r0p), o2 = lo_of(r1p), o3 = hi_of(r1p);
+            const float2 up = *reinterpret_cast<const float2*>(&S[py0 * kTbPX + px0 + 2]);
+            const float2 dn = *reinterpret_cast<const float2*>(&S[(py0 + 3) * kTbPX + px0 + 2]);
+            const float o0 = s.o[0][ch], o1 = s.o[1][ch], o2 = s.o[2][ch], o3 = s.o[3][ch];
             const float l0 = __shfl_up_sync(0xffffffffu, o1, 1);
             const float l1 = __shfl_up_sync(0xffffffffu, o3, 1);
             const float r0 = __shfl_down_sync(0xffffffffu, o0, 1);
             const float r1 = __shfl_down_sync(0xffffffffu, o2, 1);
-            f2 n0, n1;
-            if (!kBorder) {
-                n0 = jacobi_pair(r0p, s.u[0][ch], s.a[0][ch], s.wt[0][ch], s.lp[0][ch], pk(o1, r0), pk(l0, o0), r1p,
-                    up, four, step2, mom2, mom_on);
-                n1 = jacobi_pair(r1p, s.u[1][ch], s.a[1][ch], s.wt[1][ch], s.lp[1][ch], pk(o3, r1), pk(l1, o2), dn,
-                    r0p, four, step2, mom2, mom_on);
-            } else {
-                float u0 = lo_of(s.u[0][ch]), u1 = hi_of(s.u[0][ch]), u2 = lo_of(s.u[1][ch]), u3 = hi_of(s.u[1][ch]);
-                const float m0 = jacobi_px(o0, u0, lo_of(s.a[0][ch]), lo_of(s.wt[0][ch]), lo_of(s.lp[0][ch]), o1, l0,
-                    o2, lo_of(up), vr[0], vl[0], vd[0], vu[0], cnt[0], step, mom, mom_on);
-                const float m1 = jacobi_px(o1, u1, hi_of(s.a[0][ch]), hi_of(s.wt[0][ch]), hi_of(s.lp[0][ch]), r0, o0,
-                    o3, hi_of(up), vr[1], vl[1], vd[1], vu[1], cnt[1], step, mom, mom_on);
-                const float m2 = jacobi_px(o2, u2, lo_of(s.a[1][ch]), lo_of(s.wt[1][ch]), lo_of(s.lp[1][ch]), o3, l1,
-                    lo_of(dn), o0, vr[2], vl[2], vd[2], vu[2], cnt[2], step, mom, mom_on);
-                const float m3 = jacobi_px(o3, u3, hi_of(s.a[1][ch]), hi_of(s.wt[1][ch]), hi_of(s.lp[1][ch]), r1, o2,
-                    hi_of(dn), o1, vr[3], vl[3], vd[3], vu[3], cnt[3], step, mom, mom_on);
-                s.u[0][ch] = pk(u0, u1);
-                s.u[1][ch] = pk(u2, u3);
-                n0 = pk(m0, m1);
-                n1 = pk(m2, m3);
-            }
+            const float n0 = jacobi_px<kAll>(o0, s.u[0][ch], s.a[0][ch], s.wt[0][ch], s.lp[0][ch], o1, l0, o2, up.x,
+                vr[0], vl[0], vd[0], vu[0], cnt[0], step, mom, mom_on);
+            const float n1 = jacobi_px<kAll>(o1, s.u[1][ch], s.a[1][ch], s.wt[1][ch], s.lp[1][ch], r0, o0, o3, up.y,
+                vr[1], vl[1], vd[1], vu[1], cnt[1], step, mom, mom_on);
+            const float n2 = jacobi_px<kAll>(o2, s.u[2][ch], s.a[2][ch], s.wt[2][ch], s.lp[2][ch], o3, l1, dn.x, o0,
+                vr[2], vl[2], vd[2], vu[2], cnt[2], step, mom, mom_on);
+            const float n3 = jacobi_px<kAll>(o3, s.u[3][ch], s.a[3][ch], s.wt[3][ch], s.lp[3][ch], r1, o2, dn.y, o1,
+                vr[3], vl[3], vd[3], vu[3], cnt[3], step, mom, mom_on);
             s.o[0][ch] = n0;
             s.o[1][ch] = n1;
+            s.o[2][ch] = n2;
+            s.o[3][ch] = n3;
             float* D = smem + ((cur ^ 1) * 3 + ch) * kTbPlane;
-            *reinterpret_cast<f2*>(&D[(py0 + 1) * kTbPX + px0 + 2]) = n0;
-            *reinterpret_cast<f2*>(&D[(py0 + 2) * kTbPX + px0 + 2]) = n1;
+            *reinterpret_cast<float2*>(&D[(py0 + 1) * kTbPX + px0 + 2]) = make_float2(n0, n1);
+            *reinterpret_cast<float2*>(&D[(py0 + 2) * kTbPX + px0 + 2]) = make_float2(n2, n3);
         }
         __syncthreads();
     }
@@ -199,49 +173,41 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
     float cnt[4];
     bool vr[4], vl[4], vd[4], vu[4], inimg[4];
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        float v[5][3][2];
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-            const int q = 2 * r + c;
-            const int gx = ox + px0 + c;
-            const int gy = oy + py0 + r;
-            inimg[q] = gx >= 0 && gx < w && gy >= 0 && gy < h;
-            vr[q] = (gx + 1) < (w - 1);
-            vl[q] = (gx - 1) >= 0;
-            vd[q] = (gy + 1) < (h - 1);
-            vu[q] = (gy - 1) >= 0;
-            cnt[q] = static_cast<float>(static_cast<int>(vr[q]) + static_cast<int>(vl[q]) +
-                                        static_cast<int>(vd[q]) + static_cast<int>(vu[q]));
-            const int64_t idx = inimg[q] ? pix_index(gx, gy, w) * 3 : 0;
-#pragma unroll
-            for (int ch = 0; ch < 3; ++ch) {
-                v[0][ch][c] = inimg[q] ? Oin[idx + ch] : 0.0f;
-                v[1][ch][c] = inimg[q] ? Uin[idx + ch] : 0.0f;
-                v[2][ch][c] = inimg[q] ? A[idx + ch] : 0.0f;
-                v[3][ch][c] = inimg[q] ? Wt[idx + ch] : 0.0f;
-                v[4][ch][c] = inimg[q] ? L[idx + ch] : 0.0f;
-            }
-        }
+    for (int q = 0; q < 4; ++q) {
+        const int gx = ox + px0 + (q & 1);
+        const int gy = oy + py0 + (q >> 1);
+        inimg[q] = gx >= 0 && gx < w && gy >= 0 && gy < h;
+        vr[q] = (gx + 1) < (w - 1);
+        vl[q] = (gx - 1) >= 0;
+        vd[q] = (gy + 1) < (h - 1);
+        vu[q] = (gy - 1) >= 0;
+        cnt[q] = static_cast<float>(static_cast<int>(vr[q]) + static_cast<int>(vl[q]) + static_cast<int>(vd[q]) +
+                                    static_cast<int>(vu[q]));
+        const int64_t idx = inimg[q] ? pix_index(gx, gy, w) * 3 : 0;
 #pragma unroll
         for (int ch = 0; ch < 3; ++ch) {
-            s.o[r][ch] = pk(v[0][ch][0], v[0][ch][1]);
-            s.u[r][ch] = pk(v[1][ch][0], v[1][ch][1]);
-            s.a[r][ch] = pk(v[2][ch][0], v[2][ch][1]);
-            s.wt[r][ch] = pk(v[3][ch][0], v[3][ch][1]);
-            s.lp[r][ch] = pk(v[4][ch][0], v[4][ch][1]);
-            float* S = smem + ch * kTbPlane;
-            *reinterpret_cast<f2*>(&S[(py0 + 1 + r) * kTbPX + px0 + 2]) = s.o[r][ch];
+            s.o[q][ch] = inimg[q] ? Oin[idx + ch] : 0.0f;
+            s.u[q][ch] = inimg[q] ? Uin[idx + ch] : 0.0f;
+            s.a[q][ch] = inimg[q] ? A[idx + ch] : 0.0f;
+            s.wt[q][ch] = inimg[q] ? Wt[idx + ch] : 0.0f;
+            s.lp[q][ch] = inimg[q] ? L[idx + ch] : 0.0f;
         }
+    }
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        float* S = smem + ch * kTbPlane;
+        *reinterpret_cast<float2*>(&S[(py0 + 1) * kTbPX + px0 + 2]) = make_float2(s.o[0][ch], s.o[1][ch]);
+        *reinterpret_cast<float2*>(&S[(py0 + 2) * kTbPX + px0 + 2]) = make_float2(s.o[2][ch], s.o[3][ch]);
     }
     __syncthreads();
 
     // tiles whose every pixel has all four neighbours take the packed path
-    const bool interior = VSC_PACKED_MATH && ox >= 1 && oy >= 1 && ox + kTbEX - 1 <= w - 3 && oy + kTbEY - 1 <= h - 3;
+    // tiles whose every pixel has all four neighbours skip the validity selects
+    const bool interior = ox >= 1 && oy >= 1 && ox + kTbEX - 1 <= w - 3 && oy + kTbEY - 1 <= h - 3;
     if (interior)
-        tb_iterate<false>(s, vr, vl, vd, vu, cnt, smem, T, k0, step, mom, px0, py0);
-    else
         tb_iterate<true>(s, vr, vl, vd, vu, cnt, smem, T, k0, step, mom, px0, py0);
+    else
+        tb_iterate<false>(s, vr, vl, vd, vu, cnt, smem, T, k0, step, mom, px0, py0);
 
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -253,9 +219,9 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
         float ov[3];
 #pragma unroll
         for (int ch = 0; ch < 3; ++ch) {
-            ov[ch] = c ? hi_of(s.o[r][ch]) : lo_of(s.o[r][ch]);
+            ov[ch] = s.o[q][ch];
             Oout[p * 3 + ch] = ov[ch];
-            Uout[p * 3 + ch] = c ? hi_of(s.u[r][ch]) : lo_of(s.u[r][ch]);
+            Uout[p * 3 + ch] = s.u[q][ch];
         }
         if (rgba)
             reinterpret_cast<uint32_t*>(rgba)[p] = pack_rgba(ov[0], ov[1], ov[2]);
@@ -400,20 +366,26 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
                                             static_cast<int>(vd[q]) + static_cast<int>(vu[q]));
             }
             // six consecutive floats: both pixels' RGB (TMA zero-fills outside the image)
-            f2 (*dst[5])[3] = {s.o, s.u, s.a, s.wt, s.lp};
+            float(*dst[5])[3] = {s.o, s.u, s.a, s.wt, s.lp};
 #pragma unroll
             for (int arr = 0; arr < 5; ++arr) {
                 const float* src = stage + arr * kStageFloats + row * (3 * kTbEX) + 3 * px0;
                 const float2 v01 = *reinterpret_cast<const float2*>(src);
                 const float2 v23 = *reinterpret_cast<const float2*>(src + 2);
                 const float2 v45 = *reinterpret_cast<const float2*>(src + 4);
-                dst[arr][r][0] = pk(v01.x, v23.y);
-                dst[arr][r][1] = pk(v01.y, v45.x);
-                dst[arr][r][2] = pk(v23.x, v45.y);
+                float* p0 = dst[arr][2 * r];
+                float* p1 = dst[arr][2 * r + 1];
+                p0[0] = v01.x;
+                p0[1] = v01.y;
+                p0[2] = v23.x;
+                p1[0] = v23.y;
+                p1[1] = v45.x;
+                p1[2] = v45.y;
             }
 #pragma unroll
             for (int ch = 0; ch < 3; ++ch)
-                *reinterpret_cast<f2*>(&obuf[ch * kTbPlane + (row + 1) * kTbPX + px0 + 2]) = s.o[r][ch];
+                *reinterpret_cast<float2*>(&obuf[ch * kTbPlane + (row + 1) * kTbPX + px0 + 2]) =
+                    make_float2(s.o[2 * r][ch], s.o[2 * r + 1][ch]);
         }
         __syncthreads();  // staging consumed, O published
         if (tid == 0 && tile + static_cast<int>(gridDim.x) < ntiles) {
@@ -421,12 +393,11 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
             issue_tile(stage, &mO, &mU, &mA, &mW, &mL, tile + gridDim.x, tiles_x, bar);
         }
 
-        const bool interior =
-            VSC_PACKED_MATH && ox >= 1 && oy >= 1 && ox + kTbEX - 1 <= w - 3 && oy + kTbEY - 1 <= h - 3;
+        const bool interior = ox >= 1 && oy >= 1 && ox + kTbEX - 1 <= w - 3 && oy + kTbEY - 1 <= h - 3;
         if (interior)
-            tb_iterate<false>(s, vr, vl, vd, vu, cnt, obuf, T, k0, step, mom, px0, py0);
-        else
             tb_iterate<true>(s, vr, vl, vd, vu, cnt, obuf, T, k0, step, mom, px0, py0);
+        else
+            tb_iterate<false>(s, vr, vl, vd, vu, cnt, obuf, T, k0, step, mom, px0, py0);
 
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -438,9 +409,9 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
             float ov[3];
 #pragma unroll
             for (int ch = 0; ch < 3; ++ch) {
-                ov[ch] = c ? hi_of(s.o[r][ch]) : lo_of(s.o[r][ch]);
+                ov[ch] = s.o[q][ch];
                 Oout[p * 3 + ch] = ov[ch];
-                Uout[p * 3 + ch] = c ? hi_of(s.u[r][ch]) : lo_of(s.u[r][ch]);
+                Uout[p * 3 + ch] = s.u[q][ch];
             }
             if (rgba)
                 reinterpret_cast<uint32_t*>(rgba)[p] = pack_rgba(ov[0], ov[1], ov[2]);
