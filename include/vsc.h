@@ -152,6 +152,30 @@ VSC_API vsc_status vsc_get_consist_out(const vsc_image* crnt_pr, const vsc_image
     const vsc_image* cons_wt, int32_t num_iter, float step_size, float mom_fac, const vsc_image* consis_out,
     void* workspace, size_t workspace_bytes, vsc_stream_t stream);
 
+/* Largest image (width * height) vsc_get_consist_out_noalloc accepts. */
+#define VSC_NOALLOC_MAX_PIXELS 349525u
+
+/* vsc_get_consist_out for callers that must not allocate device memory:
+ * code recording a CUDA graph by stream capture, where allocation calls
+ * cannot be captured; real-time frame loops, where cudaMalloc or cudaFree
+ * can stall on a device-wide synchronisation; and plugins whose host
+ * application owns all device memory.  No counterpart in the reference (its
+ * get_consist_out allocates two images on every call,
+ * flowconsistency.cu:363-365).
+ * Same arguments, arithmetic and results as vsc_get_consist_out.  The
+ * workspace is a 16 MiB array inside the library (each GPU that loads the
+ * library holds it until the process exits), so images are limited to
+ * VSC_NOALLOC_MAX_PIXELS pixels (720 x 480 fits); larger ones get VSC_EINVAL.
+ * Every call shares that array and leaves its contents behind (nothing in
+ * it needs to start at zero), so calls that overlap on the GPU — on two
+ * streams, or from two threads — race and must be serialised by the caller.
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any
+ * stream capture. */
+VSC_API vsc_status vsc_get_consist_out_noalloc(const vsc_image* crnt_pr, const vsc_image* prev_stab_warp,
+    const vsc_image* cons_wt, int32_t num_iter, float step_size, float mom_fac, const vsc_image* consis_out,
+    vsc_stream_t stream);
+
 /* ========================================================================
  * Per-frame orchestrator (src/stabilization/videostabilizer.{h,cpp})
  * ======================================================================== */

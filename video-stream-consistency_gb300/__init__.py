@@ -34,7 +34,9 @@ EXPORTED = [
     "vsc_stabilizer_create", "vsc_stabilizer_destroy", "vsc_stabilizer_hyper_params", "vsc_stabilizer_load_frame",
     "vsc_stabilizer_set_flows", "vsc_stabilizer_step", "vsc_stabilizer_buffer", "vsc_stabilizer_last_launches",
     "vsc_stabilizer_enable_timing", "vsc_stabilizer_stage_ms", "vsc_check_device", "vsc_selftest_bounded_wait",
+    "vsc_get_consist_out_noalloc",
 ]
+NOALLOC_MAX_PIXELS = 349525  # VSC_NOALLOC_MAX_PIXELS
 
 
 class VscError(RuntimeError):
@@ -102,6 +104,7 @@ def load():
         "vsc_get_consist_wt": [IP, IP, IP, f32, f32, vp],
         "vsc_get_bilinear": [IP, IP, vp],
         "vsc_get_consist_out": [IP, IP, IP, i32, f32, f32, IP, vp, C.c_size_t, vp],
+        "vsc_get_consist_out_noalloc": [IP, IP, IP, i32, f32, f32, IP, vp],
         "vsc_stabilizer_create": [C.POINTER(StabilizerConfig), vp, C.POINTER(vp)],
         "vsc_stabilizer_destroy": [vp],
         "vsc_stabilizer_load_frame": [vp, vp, vp, i32],
@@ -260,6 +263,17 @@ def get_consist_out(crnt_pr, prev_stab_warp, cons_wt, num_iter, step_size, mom_f
 def check_device() -> None:
     """Raises VscError(VSC_ETIMEOUT) if a kernel's bounded wait gave up."""
     _check(load().vsc_check_device())
+
+
+def get_consist_out_noalloc(crnt_pr, prev_stab_warp, cons_wt, num_iter, step_size, mom_fac, consis_out,
+                            stream=None):
+    """get_consist_out with the library's built-in workspace: no device memory
+    is allocated (images up to NOALLOC_MAX_PIXELS pixels; calls must not
+    overlap on the GPU)."""
+    _check(load().vsc_get_consist_out_noalloc(C.byref(image(crnt_pr)), C.byref(image(prev_stab_warp)),
+                                              C.byref(image(cons_wt)), int(num_iter), float(step_size),
+                                              float(mom_fac), C.byref(image(consis_out)), _stream(stream)))
+    return consis_out
 
 
 def default_hyper_params() -> HyperParams:

@@ -22,6 +22,8 @@
 
 #include "vsc_internal.h"
 
+static_assert(VSC_NOALLOC_MAX_PIXELS == vsc::kNoAllocMaxPixels, "header limit out of date");
+
 namespace vsc {
 
 namespace {
@@ -309,6 +311,33 @@ VSC_API vsc_status vsc_selftest_bounded_wait(int32_t spins, vsc_stream_t stream)
     if (spins < 1 || spins > (1 << 20))
         return set_error(VSC_EINVAL, "selftest_bounded_wait: spins outside [1, 2^20]");
     return check_cuda(launch_bounded_wait_selftest(spins, cs(stream)), "selftest launch");
+}
+
+VSC_API vsc_status vsc_get_consist_out_noalloc(const vsc_image* crnt_pr, const vsc_image* prev_stab_warp,
+    const vsc_image* cons_wt, int32_t num_iter, float step_size, float mom_fac, const vsc_image* consis_out,
+    vsc_stream_t stream)
+{
+    clear_error();
+    vsc_status s;
+    if ((s = check_image(crnt_pr, "crntPr", 3, 3)) || (s = check_image(prev_stab_warp, "prevStabWarp", 3, 3)) ||
+        (s = check_image(cons_wt, "consWt", 3, 3)) || (s = check_image(consis_out, "consisOut", 3, 3)) ||
+        (s = same_size(consis_out, crnt_pr, "crntPr")) || (s = same_size(consis_out, prev_stab_warp, "prevStabWarp")) ||
+        (s = same_size(consis_out, cons_wt, "consWt")))
+        return s;
+    if (num_iter < 0)
+        return set_error(VSC_EINVAL, "consist_out_noalloc: negative iteration count");
+    const int w = consis_out->width, h = consis_out->height;
+    const size_t pixels = static_cast<size_t>(w) * h;
+    if (pixels > VSC_NOALLOC_MAX_PIXELS)
+        return set_error(VSC_EINVAL,
+            "consist_out_noalloc: %dx%d image (%zu pixels) exceeds the %zu-pixel limit of the built-in workspace; "
+            "use vsc_get_consist_out",
+            w, h, pixels, static_cast<size_t>(VSC_NOALLOC_MAX_PIXELS));
+    if (num_iter == 0)
+        return VSC_OK;
+    return check_cuda(run_solver_noalloc(crnt_pr->data, prev_stab_warp->data, cons_wt->data, consis_out->data, w, h,
+                          num_iter, step_size, mom_fac, cs(stream)),
+        "consist_out_noalloc launch");
 }
 
 VSC_API void vsc_default_hyper_params(vsc_hyper_params* hp)

@@ -58,6 +58,13 @@ cudaError_t check_device_timeout(int* flagged);
 // after `spins` polls (the timeout path, without any fault).
 cudaError_t launch_bounded_wait_selftest(int spins, cudaStream_t st);
 
+// Solver with its workspace in a file-scope device array instead of caller
+// or pool memory (no allocation).  Images up to kNoAllocMaxPixels pixels.
+constexpr size_t kNoAllocWorkspaceFloats = size_t(1) << 22;  // 16 MiB
+constexpr size_t kNoAllocMaxPixels = kNoAllocWorkspaceFloats / 12;
+cudaError_t run_solver_noalloc(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,
+    float step, float mom, cudaStream_t st);
+
 // Fused five-warp + adaptive combination + consistency weights for the
 // orchestrator: writes adapCmbPr and consWt only.
 cudaError_t launch_fused_front(const float* o0, const float* o1, const float* o2, const float* p0, const float* p1,

@@ -571,6 +571,47 @@ cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O
     return cudaGetLastError();
 }
 
+// ---- solver workspace for callers that cannot allocate ------------------------
+// A file-scope device array (every GPU that loads the library holds it until
+// the process exits).  In host code g_noalloc_ws is only a stand-in symbol,
+// not a device address: its device address is looked up once per device with
+// cudaGetSymbolAddress, with that device current, and handed to the kernels.
+static __device__ __align__(256) float g_noalloc_ws[kNoAllocWorkspaceFloats];
+
+cudaError_t noalloc_workspace(float** out)
+{
+    static std::mutex mu;
+    static float* addr[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    if (dev < 0 || dev >= 64)
+        return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        float* p = nullptr;
+        e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_noalloc_ws);
+        if (e != cudaSuccess)
+            return e;
+        addr[dev] = p;
+    }
+    *out = addr[dev];
+    return cudaSuccess;
+}
+
+cudaError_t run_solver_noalloc(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,
+    float step, float mom, cudaStream_t st)
+{
+    float* ws = nullptr;
+    cudaError_t e = noalloc_workspace(&ws);
+    if (e != cudaSuccess)
+        return e;
+    // Every workspace element (lap P, both momentum images, the second Jacobi
+    // buffer) is written before it is read, so nothing is cleared.
+    return run_solver(P, A, Wt, O, w, h, num_iter, step, mom, ws, st, nullptr, nullptr);
+}
+
 cudaError_t check_device_timeout(int* flagged)
 {
     int v = 0;
