@@ -1,18 +1,28 @@
-"""Benchmark: 1080p stabilized frames/s of the plain FP32 GPU path.
+"""Benchmark: 1080p stabilized frames/s, the chosen form against the plain
+FP32 GPU path (and the PSNR between their outputs).
 
 Workload (one step = one frame): the 1920x1080 synthetic stream (seeded
 Gaussian blobs advected by a smooth flow re-drawn every 30 frames, processed
 frames with colour shift and flicker; RGBA8 in and out).  Per frame: load the
 next frame (RGBA8 -> float, flow features), compute the forward and backward
-flow at full resolution through the Correlation (81 displacements) and Warp
-kernels, then the stabilization pass (five warps, adaptive combination,
-consistency weights, 2-level pyramid solve with 75 + 150 iterations) and the
-RGBA8 output — VideoStabilizer::doOneStep with its defaults.
+flow through the Correlation (81 displacements) and Warp kernels, then the
+stabilization pass (five warps, adaptive combination, consistency weights,
+2-level pyramid solve with 75 + 150 iterations) and the RGBA8 output —
+VideoStabilizer::doOneStep with its defaults.
 
-value : frames/s with every input frame already resident in HBM (RGBA8).
-e2e   : the same through the public C ABI with host buffers: each step copies
-        the next frame pair from pinned host memory and reads the stabilized
-        frame back, inside the timed region.
+Forms (--form, default bf16): "plain" computes the flow with FP32
+correlations at full resolution, as the reference does; "bf16" / "fp16" run
+the flow estimator's correlations on the tensor cores; "bf16_ds2" also
+computes the flow at half resolution (FLOWDOWNSCALE=2, bilinear upsampling).
+Warps, mask and blend are FP32 in every form.
+
+value : frames/s of the chosen form with every input frame already resident
+        in HBM (RGBA8); "plain" holds the plain path's figure, timed the same
+        way, and "psnr_vs_plain" the PSNR of the chosen form's output frames
+        against the plain path's.
+e2e   : the chosen form through the public C ABI with host buffers: each
+        step copies the next frame pair from pinned host memory and reads the
+        stabilized frame back, inside the timed region.
 The per-step working set (~0.6 GB) is far larger than L2, so no flush is
 needed between steps.
 
@@ -30,6 +40,7 @@ from __future__ import annotations
 import argparse
 import importlib.util
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -41,13 +52,12 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 PKG = ROOT / "video-stream-consistency_gb300"
 W, H = 1920, 1080
-METRIC = "1080p stabilized frames/s (plain FP32 GPU path: correlation + warp + mask + blend)"
+METRIC = "1080p stabilized frames/s, chosen form vs plain GPU at PSNR>=40 dB; HBM GB/s"
 # Solver Jacobi step, per pixel: reads O, U, lap(P), A, consWt (5 x 12 B),
-# writes O, U (2 x 12 B); the kernel performs SOLVER_ITERS_PER_LAUNCH steps
-# per launch (temporal blocking), so its algorithmic bytes per launch are that
-# many steps' worth ("effective" bandwidth can exceed the HBM peak).
+# writes O, U (2 x 12 B); the kernel performs vsc_solver_steps_per_launch()
+# steps per launch (temporal blocking), so its algorithmic bytes per launch
+# are that many steps' worth ("effective" bandwidth can exceed the HBM peak).
 SOLVER_BYTES_PER_PX = 84
-SOLVER_ITERS_PER_LAUNCH = 8
 
 
 def import_pkg():
@@ -70,29 +80,85 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """SM clocks and clock-event (throttle) reasons sampled every 20 ms during
+    the timed region, through NVML (libnvidia-ml, the library nvidia-smi
+    reads), on a background thread.  The device is found by UUID so the
+    sample is of the GPU the benchmark runs on whatever CUDA_VISIBLE_DEVICES
+    says.  Falls back to `nvidia-smi -lms 20` when NVML cannot be loaded.
+    Reading clocks changes nothing on the GPU."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason* bits (nvml.h)
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40,
+            "hw_power_brake_slowdown": 0x80}
+    PERIOD_S = 0.02
 
-    def __init__(self, gpu_index: int):
-        self.gpu = gpu_index
+    def __init__(self, device_index: int):
+        import torch
+
+        self.uuid = None
+        try:
+            self.uuid = "GPU-" + str(torch.cuda.get_device_properties(device_index).uuid)
+        except Exception:  # noqa: BLE001 - older torch without .uuid
+            pass
+        self.samples = []  # (sm_mhz, max_mhz, reasons bitmask, source)
+        self.thread = None
+        self.stop_flag = False
         self.proc = None
         self.file = None
 
+    # ---- NVML -----------------------------------------------------------------
+    def _nvml(self):
+        import ctypes as C
+
+        lib = C.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        h = C.c_void_p()
+        if self.uuid is None or lib.nvmlDeviceGetHandleByUUID(self.uuid.encode(), C.byref(h)) != 0:
+            raise OSError("device not found by UUID")
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        return lib, h, reasons
+
+    def _loop(self, lib, h, reasons_fn):
+        import ctypes as C
+
+        clk, mx, rs = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        while not self.stop_flag:
+            if (lib.nvmlDeviceGetClockInfo(h, 1, C.byref(clk)) == 0 and  # NVML_CLOCK_SM
+                    lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0 and reasons_fn(h, C.byref(rs)) == 0):
+                self.samples.append((float(clk.value), float(mx.value), int(rs.value)))
+            time.sleep(self.PERIOD_S)
+
     def start(self):
+        import threading
+
+        try:
+            lib, h, fn = self._nvml()
+        except (OSError, AttributeError):
+            return self._start_smi()
+        self.stop_flag = False
+        self.thread = threading.Thread(target=self._loop, args=(lib, h, fn), daemon=True)
+        self.thread.start()
+        t0 = time.perf_counter()
+        while not self.samples and time.perf_counter() - t0 < 2.0:  # first sample before the region opens
+            time.sleep(0.001)
+
+    # ---- nvidia-smi fallback -------------------------------------------------------
+    def _start_smi(self):
         try:
             self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
-            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.uuid or 0}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=self.file, stderr=subprocess.DEVNULL)
+            time.sleep(0.5)
         except (OSError, FileNotFoundError):
             self.proc = None
 
-    def stop(self):
-        if self.proc is None:
-            return None
+    def _stop_smi(self):
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -101,21 +167,30 @@ class ClockSampler:
         self.file.flush()
         rows = [r.split(",") for r in Path(self.file.name).read_text().strip().splitlines() if r.strip()]
         os.unlink(self.file.name)
-        sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in rows:
             try:
-                sm.append(float(r[1]))
-                smax.append(float(r[2]))
-                for n, v in zip(names, r[5:9]):
-                    if v.strip().lower() == "active":
-                        reasons.add(n)
+                bits = sum(self.BITS[n] for n, v in zip(names, r[5:9]) if v.strip().lower() == "active")
+                self.samples.append((float(r[1]), float(r[2]), bits))
             except (ValueError, IndexError):
                 continue
-        if not sm:
+
+    def stop(self):
+        source = "nvml"
+        if self.thread is not None:
+            self.stop_flag = True
+            self.thread.join(timeout=5)
+        elif self.proc is not None:
+            self._stop_smi()
+            source = "nvidia-smi"
+        else:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
-                "reasons": sorted(reasons)}
+        if not self.samples:
+            return None
+        sm = [s[0] for s in self.samples]
+        reasons = sorted({n for s in self.samples for n, b in self.BITS.items() if s[2] & b})
+        return {"sm_mhz": statistics.median(sm), "sm_min_mhz": min(sm), "sm_max_mhz": max(s[1] for s in self.samples),
+                "samples": len(sm), "period_ms": int(self.PERIOD_S * 1000), "source": source, "reasons": reasons}
 
 
 def dist_env():
@@ -307,8 +382,9 @@ def run_reference(args):
 
 def solver_roofline(vsc, dev, stream, iters: int = 144):
     """Times the dominant kernel — the full-resolution solver — with CUDA
-    events on its stream: per-launch time from a 1-launch and a
-    (1 + n)-launch solve of the same size."""
+    events on its stream: the time of one Jacobi step from an 8-step and an
+    (8 + iters)-step solve of the same size (both whole numbers of launches
+    for 4 or 8 steps per launch)."""
     import torch
 
     peak, peak_src = peaks()
@@ -318,27 +394,28 @@ def solver_roofline(vsc, dev, stream, iters: int = 144):
     Wt = torch.rand((H, W, 3), device=dev, generator=g) * 2
     O = P.clone()
     wsp = torch.empty(vsc.consist_out_workspace_size(W, H) // 4, dtype=torch.float32, device=dev)
-    T = SOLVER_ITERS_PER_LAUNCH
+    T = int(vsc.load().vsc_solver_steps_per_launch())
     torch.cuda.synchronize()
     for _ in range(2):
         vsc.get_consist_out(P, A, Wt, iters, 0.15, 0.15, O, workspace=wsp, stream=stream)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     ev[0].record(stream)
-    vsc.get_consist_out(P, A, Wt, T, 0.15, 0.15, O, workspace=wsp, stream=stream)
+    vsc.get_consist_out(P, A, Wt, 8, 0.15, 0.15, O, workspace=wsp, stream=stream)
     ev[1].record(stream)
     ev[2].record(stream)
-    vsc.get_consist_out(P, A, Wt, T + iters, 0.15, 0.15, O, workspace=wsp, stream=stream)
+    vsc.get_consist_out(P, A, Wt, 8 + iters, 0.15, 0.15, O, workspace=wsp, stream=stream)
     ev[3].record(stream)
     ev[3].synchronize()
-    n_launch = iters // T
-    per_launch_ms = (ev[2].elapsed_time(ev[3]) - ev[0].elapsed_time(ev[1])) / n_launch
+    step_ms = (ev[2].elapsed_time(ev[3]) - ev[0].elapsed_time(ev[1])) / iters
     alg_bytes = SOLVER_BYTES_PER_PX * W * H * T  # T Jacobi steps per launch
+    per_launch_ms = step_ms * T
     achieved = alg_bytes / (per_launch_ms / 1000.0) / 1e9
-    return {"bound": "hbm", "kernel": f"solver_tb_kernel ({T} Jacobi steps of kernel_consist_out per launch at "
-                                      f"1920x1080; effective bytes = {SOLVER_BYTES_PER_PX} B/px per step)",
+    traffic = SOLVER_TRAFFIC_BYTES.get(T)
+    return {"bound": "hbm", "kernel": f"solver_persistent_kernel ({T} Jacobi steps of kernel_consist_out per "
+                                      f"launch at 1920x1080; effective bytes = {SOLVER_BYTES_PER_PX} B/px per step)",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": SOLVER_TRAFFIC_BYTES, "algorithmic_bytes_per_launch": alg_bytes,
-            "launch_ms": per_launch_ms, "ms_per_jacobi_step": per_launch_ms / T, "peak_source": peak_src}
+            "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes, "steps_per_launch": T,
+            "launch_ms": per_launch_ms, "ms_per_jacobi_step": step_ms, "peak_source": peak_src}
 
 
 def run_solver_only(args):
@@ -350,10 +427,125 @@ def run_solver_only(args):
     vsc.load()
     dev = torch.device("cuda", 0)
     stream = torch.cuda.Stream(device=dev)
-    print(json.dumps(solver_roofline(vsc, dev, stream, iters=args.steps * SOLVER_ITERS_PER_LAUNCH)))
+    print(json.dumps(solver_roofline(vsc, dev, stream, iters=args.steps * 8)))
 
 
 # ---------------------------------------------------------------------------
+# Forms of the per-frame path.  "plain" is the method as the reference runs
+# it (FP32 correlations, flow at full resolution); the others change only the
+# flow estimator's arithmetic or resolution, never the warps, mask and blend.
+FORMS = {
+    "plain": ({"corr_dtype": "f32", "flow_downscale": 1},
+              "plain FP32 path: flow at full resolution (Correlation md=4 + Warp, FP32)"),
+    "bf16": ({"corr_dtype": "bf16", "flow_downscale": 1},
+             "flow at full resolution with the Correlations on the tensor cores (BF16 operands, FP32 "
+             "accumulation); warps, mask and blend FP32"),
+    "fp16": ({"corr_dtype": "fp16", "flow_downscale": 1},
+             "flow at full resolution with the Correlations on the tensor cores (FP16 operands with a per-level "
+             "scale, FP32 accumulation); warps, mask and blend FP32"),
+    "bf16_ds2": ({"corr_dtype": "bf16", "flow_downscale": 2},
+                 "FLOWDOWNSCALE=2 (flow at 960x540, bilinear upsampling) with BF16 tensor-core Correlations"),
+}
+
+
+def time_form(vsc, kw, dev_frames, stream, steps, warmup, ws, dev, clocks=None):
+    """K device-resident steps of one form, CUDA events on the stabilizer's
+    stream; returns (ms over ranks, launches per step, stabilizer)."""
+    import torch
+
+    n_frames = len(dev_frames)
+    out_dev = torch.empty((H, W, 4), dtype=torch.uint8, device=dev)
+    st = vsc.Stabilizer(W, H, stream=stream, **kw)
+    for i in range(3):
+        st.load_frame(*dev_frames[i])
+    state = {"nxt": 3, "launches": 0}
+
+    def step():
+        st.step(out_dev)
+        n = st.last_launches
+        st.load_frame(*dev_frames[state["nxt"] % n_frames])
+        state["launches"] = n + st.last_launches
+        state["nxt"] += 1
+
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            step()
+    stream.synchronize()
+    if clocks:
+        clocks.start()
+    barrier(ws)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    barrier(ws)
+    ms = reduce_max(e0.elapsed_time(e1), ws, dev)
+    st.step_fn = step
+    return ms, state["launches"], st
+
+
+def e2e_form(vsc, kw, pinned, stream, steps, warmup, ws, dev):
+    """The same metric through the public API with pinned host frames: each
+    step uploads the next frame pair and reads the stabilized frame back."""
+    import torch
+
+    n_frames = len(pinned)
+    out_host = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory()
+    st = vsc.Stabilizer(W, H, stream=stream, **kw)
+    for i in range(3):
+        st.load_frame(pinned[i][0].numpy(), pinned[i][1].numpy())
+    nxt = [3]
+
+    def step():
+        st.step(out_host)  # reads the result back (synchronises the stream)
+        o, p = pinned[nxt[0] % n_frames]
+        st.load_frame(o.numpy(), p.numpy())
+        nxt[0] += 1
+
+    for _ in range(warmup):
+        step()
+    stream.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    stream.synchronize()
+    t = reduce_max(time.perf_counter() - t0, ws, dev)
+    st.close()
+    return {"value": ws * steps / t, "unit": "frames/s", "h2d_bytes_per_step": 2 * W * H * 4,
+            "d2h_bytes_per_step": W * H * 4}
+
+
+def psnr_vs_plain(vsc, kw, dev_frames, stream, n_steps: int = 12):
+    """Stabilized RGB of the form against the plain path, frame by frame."""
+    import torch
+
+    sts = [vsc.Stabilizer(W, H, stream=stream, **FORMS["plain"][0]), vsc.Stabilizer(W, H, stream=stream, **kw)]
+    for st in sts:
+        for i in range(3):
+            st.load_frame(*dev_frames[i])
+    vals = []
+    for t in range(n_steps):
+        outs = []
+        for st in sts:
+            with torch.cuda.stream(stream):
+                outs.append(st.step()[..., :3].float())
+        stream.synchronize()
+        mse = float(torch.mean((outs[0] - outs[1]) ** 2)) / 255.0 ** 2
+        vals.append(99.0 if mse == 0 else 10 * math.log10(1.0 / mse))
+        for st in sts:
+            st.load_frame(*dev_frames[(t + 3) % len(dev_frames)])
+    for st in sts:
+        st.close()
+    return {"min_db": min(vals), "mean_db": statistics.mean(vals), "frames": n_steps,
+            "note": "99 = identical frames"}
+
+
 def run_gpu(args):
     import torch
 
@@ -372,105 +564,61 @@ def run_gpu(args):
     n_frames = min(args.steps + args.warmup + 3, 120)
     frames = make_frames(n_frames, seed=rank, device=str(dev))
     stream = torch.cuda.Stream(device=dev)
-
-    # ---- device-resident run -------------------------------------------------
     dev_frames = [(torch.from_numpy(o).to(dev), torch.from_numpy(p).to(dev)) for o, p in frames]
-    out_dev = torch.empty((H, W, 4), dtype=torch.uint8, device=dev)
     torch.cuda.synchronize()
-    st = vsc.Stabilizer(W, H, stream=stream)
-    for i in range(3):
-        st.load_frame(*dev_frames[i])
-    nxt = 3
-    launches_per_step = 0
+    form = args.form
+    kw, form_desc = FORMS[form]
 
-    def step_dev():
-        nonlocal nxt, launches_per_step
-        st.step(out_dev)
-        n = st.last_launches
-        st.load_frame(*dev_frames[nxt % n_frames])
-        launches_per_step = n + st.last_launches
-        nxt += 1
-
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            step_dev()
-    stream.synchronize()
+    # ---- device-resident: the chosen form (clocks sampled), then plain ----------
     clocks = ClockSampler(local)
-    clocks.start()
-    barrier(ws)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step_dev()
-    e1.record(stream)
-    e1.synchronize()
-    torch.cuda.synchronize()
-    barrier(ws)
+    ms_max, launches_per_step, st = time_form(vsc, kw, dev_frames, stream, args.steps, args.warmup, ws, dev, clocks)
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    ms_max = reduce_max(ms, ws, dev)
     value = ws * args.steps / (ms_max / 1000.0)
+    plain = None
+    if form != "plain":
+        pms, pl, pst = time_form(vsc, FORMS["plain"][0], dev_frames, stream, args.steps, args.warmup, ws, dev)
+        pst.close()
+        plain = {"value": ws * args.steps / (pms / 1000.0), "unit": "frames/s", "ms_per_step": pms / args.steps,
+                 "gpu_launches_per_step": pl}
 
     # ---- per-stage device time (separate pass; stage events synchronise) -------
     st.enable_timing(True)
     stages = []
     for _ in range(5):
-        step_dev()
+        st.step_fn()
         stages.append(st.stage_ms())
     st.enable_timing(False)
     stages_ms = {k: statistics.median(d[k] for d in stages) for k in stages[0]}
+    st.close()
 
     # ---- end to end through the public API with pinned host buffers ------------
     pinned = [(torch.from_numpy(o).pin_memory(), torch.from_numpy(p).pin_memory()) for o, p in frames]
-    out_host = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory()
-    st2 = vsc.Stabilizer(W, H, stream=stream)
-    for i in range(3):
-        st2.load_frame(pinned[i][0].numpy(), pinned[i][1].numpy())
-    nxt2 = 3
-
-    def step_e2e():
-        nonlocal nxt2
-        st2.step(out_host)  # reads the result back (synchronises the stream)
-        o, p = pinned[nxt2 % n_frames]
-        st2.load_frame(o.numpy(), p.numpy())
-        nxt2 += 1
-
-    for _ in range(args.warmup):
-        step_e2e()
-    stream.synchronize()
-    barrier(ws)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        step_e2e()
-    stream.synchronize()
-    t_e2e = time.perf_counter() - t0
-    barrier(ws)
-    t_e2e = reduce_max(t_e2e, ws, dev)
-    e2e = {"value": ws * args.steps / t_e2e, "unit": "frames/s", "h2d_bytes_per_step": 2 * W * H * 4,
-           "d2h_bytes_per_step": W * H * 4}
+    e2e = e2e_form(vsc, kw, pinned, stream, args.steps, args.warmup, ws, dev)
+    quality = psnr_vs_plain(vsc, kw, dev_frames, stream) if form != "plain" else None
 
     roofline = solver_roofline(vsc, dev, stream)
 
     line = {
         "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "1920x1080 synthetic stream (plain method: flow at full resolution via "
-                               "Correlation md=4 + Warp, 2-level pyramid, 75+150 solver iterations), RGBA8 in/out",
-                   "width": W, "height": H, "frames_generated": n_frames,
+        "vs_baseline": None, "dtype": "f32" if kw["corr_dtype"] == "f32" else f"f32 ({kw['corr_dtype']} correlation)",
+        "data": "synthetic",
+        "config": {"workload": f"1920x1080 synthetic stream, form '{form}': {form_desc}; 2-level pyramid, "
+                               "75+150 solver iterations, RGBA8 in/out",
+                   "form": form, "width": W, "height": H, "frames_generated": n_frames,
                    "l2": "per-step working set ~0.6 GB > 129 MB L2; no flush",
                    "parallelism": f"replicas x{ws}"},
         "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "roofline": roofline, "clocks": clk,
         "stages_ms": stages_ms,
     }
+    if plain:
+        line["plain"] = plain
+        line["speedup_vs_plain"] = value / plain["value"]
+        line["psnr_vs_plain"] = quality
     if rank == 0 and ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_sample(frames, os.cpu_count() or 1)
     if rank == 0:
         print(json.dumps(line))
-    st.close()
-    st2.close()
     if ws > 1:
         import torch.distributed as dist
 
@@ -478,8 +626,9 @@ def run_gpu(args):
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one solver launch at
-# 1920x1080, from the ncu capture summarised in profiles/ (None until captured).
-SOLVER_TRAFFIC_BYTES = None
+# 1920x1080, by Jacobi steps per launch, from the ncu captures summarised in
+# profiles/ (8 steps: 124,483,584 + 26,466,304 bytes).
+SOLVER_TRAFFIC_BYTES = {8: 150_949_888}
 
 
 def main():
@@ -489,6 +638,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--form", choices=sorted(FORMS), default="bf16",
+                    help="the chosen form reported as value (the plain path is timed beside it)")
     ap.add_argument("--kernel", choices=["step", "solver"], default="step",
                     help="solver: time only the 1920x1080 solver (profiler target)")
     args = ap.parse_args()

@@ -62,6 +62,10 @@ VSC_API vsc_status vsc_check_device(void);
  * returns VSC_ETIMEOUT.  No fault, trap or hang is involved. */
 VSC_API vsc_status vsc_selftest_bounded_wait(int32_t spins, vsc_stream_t stream);
 
+/* Jacobi steps of the blend solver per kernel launch (temporal blocking);
+ * a property of the build, for profiling tools. */
+VSC_API int32_t vsc_solver_steps_per_launch(void);
+
 /* ========================================================================
  * ONNX Runtime custom ops (domain "custom")
  * ======================================================================== */
@@ -93,6 +97,35 @@ VSC_API vsc_status vsc_correlation_fwd(const float* f1, const float* f2, float* 
  * weights: within 2^-21 * max|input| of the reference's double-weight CPU op. */
 VSC_API vsc_status vsc_warp_fwd(const float* input, const float* flow, float* out, int64_t N, int64_t C, int64_t H,
     int64_t W, vsc_stream_t stream);
+
+/* Operand types of the reduced-precision correlation. */
+typedef enum vsc_dtype { VSC_DTYPE_F32 = 0, VSC_DTYPE_BF16 = 1, VSC_DTYPE_F16 = 2 } vsc_dtype;
+
+/* custom::Correlation (legacy = 0 layout) on the tensor cores: f1 and f2 are
+ * each scaled by a power of two chosen from their largest magnitude (per
+ * call, i.e. per pyramid level), rounded to BF16 or FP16, multiplied with FP32
+ * accumulation, and the sums scaled back exactly.  Error against the exact
+ * sum S = sum_c f1 f2: |out - S| <= (2u + u^2) sum_c |f1 f2| with u = 2^-8
+ * (BF16) or 2^-11 (FP16), plus the FP32 rounding of the sum.  No counterpart
+ * in the reference (whose op is FP32 only); max_displacement <= 8 and at most
+ * 208 channels.  workspace: device memory of
+ * vsc_correlation_lowp_workspace_size bytes, 256-byte aligned, or NULL to
+ * let the library take it from its stream-ordered pool. */
+VSC_API size_t vsc_correlation_lowp_workspace_size(int64_t N, int64_t C, int64_t H, int64_t W);
+VSC_API vsc_status vsc_correlation_fwd_lowp(const float* f1, const float* f2, float* out, int64_t N, int64_t C,
+    int64_t H, int64_t W, int64_t max_displacement, int32_t dtype, void* workspace, size_t workspace_bytes,
+    vsc_stream_t stream);
+
+/* The DOUBLE branches of the reference's CPU ops (correlation.cc:115-139,
+ * warp.cc:48-58; the op schemas declare FLOAT, the kernels also take
+ * double).  Same layouts and semantics as vsc_correlation_fwd (legacy = 0;
+ * the CPU op has no legacy form) and vsc_warp_fwd, computed in double with
+ * the reference's operation order: bit-exact to correlation.cc / warp.cc
+ * on double tensors. */
+VSC_API vsc_status vsc_correlation_fwd_f64(const double* f1, const double* f2, double* out, int64_t N, int64_t C,
+    int64_t H, int64_t W, int64_t max_displacement, vsc_stream_t stream);
+VSC_API vsc_status vsc_warp_fwd_f64(const double* input, const double* flow, double* out, int64_t N, int64_t C,
+    int64_t H, int64_t W, vsc_stream_t stream);
 
 /* ========================================================================
  * Stabilization kernels (src/stabilization/flowconsistency.cuh:3-50)
@@ -129,6 +162,26 @@ VSC_API vsc_status vsc_get_adap_comb(const vsc_image* crnt_in, const vsc_image* 
     const vsc_image* prev_warp_pr, const vsc_image* next_warp_in, const vsc_image* next_warp_pr,
     const vsc_image* adap_cmb_in, const vsc_image* adap_cmb_pr, const vsc_image* last_stab_warp, float alpha,
     vsc_stream_t stream);
+
+/* Opt-in extension, no counterpart in the reference (the reference weights
+ * the previous and next frames by colour similarity only,
+ * flowconsistency.cu:146-154).  Forward-backward flow consistency: for a
+ * flow a at a pixel, the opposite flow b is sampled bilinearly where a carries
+ * the pixel, p; the pixel is consistent when
+ * |a + b(p)|^2 <= 0.01 (|a|^2 + |b(p)|^2) + 0.5 and p lies in the frame.
+ * occ_mask (2 channels, same size): ch0 = 1 where flow_bwd is confirmed by
+ * flow_fwd (the previous frame's warp), ch1 = 1 where flow_fwd is confirmed
+ * by flow_bwd (the next frame's warp), else 0.  Flows: 2 or 3 channels. */
+VSC_API vsc_status vsc_get_flow_consistency_mask(const vsc_image* flow_fwd, const vsc_image* flow_bwd,
+    const vsc_image* occ_mask, vsc_stream_t stream);
+
+/* vsc_get_adap_comb with the previous/next frame weights multiplied by
+ * occ_mask ch0/ch1 after their clamps (a mask of ones gives
+ * vsc_get_adap_comb's bits).  Opt-in extension, no counterpart in the reference. */
+VSC_API vsc_status vsc_get_adap_comb_masked(const vsc_image* crnt_in, const vsc_image* crnt_pr,
+    const vsc_image* prev_warp_in, const vsc_image* prev_warp_pr, const vsc_image* next_warp_in,
+    const vsc_image* next_warp_pr, const vsc_image* adap_cmb_in, const vsc_image* adap_cmb_pr,
+    const vsc_image* last_stab_warp, const vsc_image* occ_mask, float alpha, vsc_stream_t stream);
 
 /* Consistency weights gamma*exp(-beta*(I - adapCmbIn)^2), < 0.001 -> 0.
  * Replaces get_consist_wt / kernel_consist_wt (flowconsistency.cu:168-191, :335-348). */
@@ -210,6 +263,10 @@ typedef struct vsc_stabilizer_config {
                                the graph is re-captured when the hyper-parameters or
                                the device output pointer change; steps run without
                                a graph while stage timing is on */
+    int32_t corr_dtype;     /* operand type of the flow estimator's correlations:
+                               VSC_DTYPE_F32 (0, the plain method), VSC_DTYPE_BF16 or
+                               VSC_DTYPE_F16 (tensor cores, FP32 accumulation); the
+                               warps, mask and blend stay FP32 */
 } vsc_stabilizer_config;
 
 /* Replaces the VideoStabilizer constructor (videostabilizer.cpp:46-102).
@@ -251,12 +308,53 @@ VSC_API int32_t vsc_stabilizer_last_launches(vsc_stabilizer* s);
 /* Per-stage device timing, the counterpart of the reference's load / optflow /
  * stabilize accumulators (videostabilizer.h:72-76, stabilizefiles.cpp:121-128).
  * Off by default; when on, CUDA events are recorded between the stages. */
+/* Opt-in (off by default; no counterpart in the reference): apply the
+ * forward-backward flow consistency mask of vsc_get_flow_consistency_mask to
+ * the temporal weights of every following step. */
+VSC_API vsc_status vsc_stabilizer_set_occlusion_mask(vsc_stabilizer* s, int32_t on);
+
 VSC_API vsc_status vsc_stabilizer_enable_timing(vsc_stabilizer* s, int32_t on);
 /* ms[0] last load_frame (upload, conversion, flow features), ms[1] flow
  * (forward + backward), ms[2] warps + adaptive combination + consistency
  * weights + pyramid, ms[3] coarse pyramid levels of the solve, ms[4]
  * full-resolution solve and RGBA8 output; n >= 5.  Synchronises the stream. */
 VSC_API vsc_status vsc_stabilizer_stage_ms(vsc_stabilizer* s, float* ms, int32_t n);
+
+/* ---- frame directories (FileStabilizer, stabilizefiles.cpp:37-149) ----------
+ * Image files: PNG (8-bit gray, gray+alpha, RGB or RGBA, not interlaced) and
+ * binary PPM (P6, maxval 255), read into RGBA8 host buffers (alpha 255 where
+ * the file has none).  JPEG, which the reference also reads through Qt, is
+ * reported as VSC_EUNSUPPORTED.  Flow files: Middlebury .flo (flowIO.cpp). */
+VSC_API vsc_status vsc_image_file_info(const char* path, int32_t* width, int32_t* height);
+VSC_API vsc_status vsc_read_image_file(const char* path, uint8_t* rgba, int32_t width, int32_t height);
+/* Writes an 8-bit RGB PNG (the alpha of rgba is dropped). */
+VSC_API vsc_status vsc_write_png(const char* path, const uint8_t* rgba, int32_t width, int32_t height);
+VSC_API vsc_status vsc_flo_info(const char* path, int32_t* width, int32_t* height);
+/* flow: width x height x 2 floats (u, v); the file must have exactly that
+ * size (initializeFlowImage, imagehelpers.cpp:42-50). */
+VSC_API vsc_status vsc_read_flo(const char* path, float* flow, int32_t width, int32_t height);
+VSC_API vsc_status vsc_write_flo(const char* path, const float* flow, int32_t width, int32_t height);
+
+typedef struct vsc_files_config {
+    const char* original_dir;  /* original frames, *.png / *.ppm in name order */
+    const char* processed_dir; /* per-frame processed frames, same count */
+    const char* output_dir;    /* created if missing; receives 000000.png ... */
+    const char* flow_dir;      /* NULL: flows computed by the library; else
+                                  frame_<i+1>.flo (i -> i+1) and frame_<i>_bwd.flo
+                                  (i -> i-1) per frame i, six-digit indices (-f) */
+    int32_t width, height;     /* frames are resized (nearest) to this size;
+                                  0: the first original frame's size */
+    int32_t flow_downscale;    /* FLOWDOWNSCALE, computed flows only; 0 or 1 = none */
+    int32_t corr_dtype;        /* vsc_stabilizer_config.corr_dtype */
+    const vsc_hyper_params* hyper; /* NULL: the defaults */
+} vsc_files_config;
+
+/* Stabilizes every frame of the directories: frame 0 is the processed frame,
+ * frames 1 .. n-2 the stabilized ones, frame n-1 the processed frame again
+ * (preloadProcessedFrames / outputFinalFrames), all written through the
+ * float conversion and back as the reference's gpuToImage does.  Needs at
+ * least three frames.  frames_written (optional) receives the count. */
+VSC_API vsc_status vsc_stabilize_files(const vsc_files_config* cfg, int32_t* frames_written);
 
 #ifdef __cplusplus
 }

@@ -77,6 +77,8 @@ def lib():
         L.vo_float_to_rgba.argtypes = [_f32p, _u8p, _i64]
         L.vo_stab_warp.argtypes = [_f32p, _f32p, _i, _f32p, _i, _i]
         L.vo_adap_comb.argtypes = [_f32p] * 9 + [C.c_float, _i64]
+        L.vo_adap_comb_masked.argtypes = [_f32p] * 9 + [C.c_void_p, C.c_float, _i64]
+        L.vo_flow_consistency_mask.argtypes = [_f32p, _f32p, _i, _f32p, _i, _i]
         L.vo_consist_wt.argtypes = [_f32p, _f32p, _f32p, C.c_float, C.c_float, _i64]
         L.vo_bilinear.argtypes = [_f32p, _i, _i, _f32p, _i, _i, _i]
         L.vo_consist_out.argtypes = [_f32p, _f32p, _f32p, _i, C.c_float, C.c_float, _f32p, _i, _i]
@@ -85,6 +87,11 @@ def lib():
         L.vo_stab_pass.argtypes = [
             _i, _i, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _f32p, _f32p, _i, _f32p,
             C.POINTER(Hyper), _f32p, C.c_void_p,
+        ]
+        L.vo_stab_pass_ex.restype = _i
+        L.vo_stab_pass_ex.argtypes = [
+            _i, _i, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _f32p, _f32p, _i, _f32p,
+            C.POINTER(Hyper), _i, _f32p, C.c_void_p,
         ]
         L.vo_flow_level_dims.argtypes = [_i, _i, _i, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)]
         L.vo_flow_feature_floats.restype = C.c_size_t
@@ -224,6 +231,27 @@ def adap_comb(crnt_in, crnt_pr, prev_in, prev_pr, next_in, next_pr, last_stab_wa
     return ain, apr
 
 
+def adap_comb_masked(crnt_in, crnt_pr, prev_in, prev_pr, next_in, next_pr, last_stab_warp, occ_mask, alpha):
+    """adap_comb with the temporal weights multiplied by occ_mask (HWC2: previous, next)."""
+    args = [_c(a, np.float32) for a in (crnt_in, crnt_pr, prev_in, prev_pr, next_in, next_pr)]
+    ain = np.empty_like(args[0])
+    apr = np.empty_like(args[0])
+    npix = args[0].shape[0] * args[0].shape[1]
+    m = _c(occ_mask, np.float32)
+    lib().vo_adap_comb_masked(*args, ain, apr, _c(last_stab_warp, np.float32), m.ctypes.data, float(alpha), npix)
+    return ain, apr
+
+
+def flow_consistency_mask(flow_fwd, flow_bwd):
+    """Forward-backward consistency mask, HWC2 of 0/1 (ch0 previous, ch1 next)."""
+    ff = _c(flow_fwd, np.float32)
+    fb = _c(flow_bwd, np.float32)
+    h, w, fc = ff.shape
+    out = np.empty((h, w, 2), np.float32)
+    lib().vo_flow_consistency_mask(ff, fb, fc, out, w, h)
+    return out
+
+
 def consist_wt(crnt_in, adap_in, beta, gamma):
     ci = _c(crnt_in, np.float32)
     out = np.empty_like(ci)
@@ -253,8 +281,9 @@ def default_hyper() -> Hyper:
     return hp
 
 
-def stab_pass(orig3, proc3, flow_fwd, flow_bwd, last_stab, hp: Hyper | None = None):
-    """One stabilization pass over frames (t-1, t, t+1); returns (float HWC3, RGBA8)."""
+def stab_pass(orig3, proc3, flow_fwd, flow_bwd, last_stab, hp: Hyper | None = None, occlusion_mask: bool = False):
+    """One stabilization pass over frames (t-1, t, t+1); returns (float HWC3, RGBA8).
+    occlusion_mask applies the opt-in forward-backward consistency mask."""
     hp = hp or default_hyper()
     orig3 = [_c(a, np.float32) for a in orig3]
     proc3 = [_c(a, np.float32) for a in proc3]
@@ -266,7 +295,8 @@ def stab_pass(orig3, proc3, flow_fwd, flow_bwd, last_stab, hp: Hyper | None = No
     pp = (C.c_void_p * 3)(*[a.ctypes.data for a in proc3])
     out = np.empty((h, w, 3), np.float32)
     rgba = np.empty((h, w, 4), np.uint8)
-    rc = lib().vo_stab_pass(w, h, po, pp, ff, fb, ff.shape[2], ls, C.byref(hp), out, rgba.ctypes.data)
+    rc = lib().vo_stab_pass_ex(w, h, po, pp, ff, fb, ff.shape[2], ls, C.byref(hp), int(bool(occlusion_mask)), out,
+                               rgba.ctypes.data)
     if rc != 0:
         raise ValueError("vo_stab_pass: invalid sizes")
     return out, rgba

@@ -19,6 +19,10 @@ class Img(C.Structure):
     _fields_ = [("data", C.c_void_p), ("width", C.c_int), ("height", C.c_int), ("channels", C.c_int)]
 
 
+# entry points of ref_gpu/ref_gpu_harness.cu (besides rg_last_error)
+FUNCS = ("rg_init", "rg_warp", "rg_adap_comb", "rg_consist_wt", "rg_bilinear", "rg_consist_out", "rg_to_float",
+         "rg_to_char", "rg_correlation", "rg_warp_op", "rg_stab_pass")
+
 _libs: dict = {}
 
 
@@ -38,8 +42,7 @@ def load(kind: str = "exact"):
     shutil.copy(LIB, tmp)
     L = C.CDLL(str(tmp))
     L.rg_last_error.restype = C.c_char_p
-    for fn in ("rg_init", "rg_warp", "rg_adap_comb", "rg_consist_wt", "rg_bilinear", "rg_consist_out", "rg_to_float",
-               "rg_to_char", "rg_correlation", "rg_warp_op", "rg_stab_pass"):
+    for fn in FUNCS:
         getattr(L, fn).restype = C.c_int
     L.rg_init.argtypes = [C.c_char_p]
     L.rg_warp.argtypes = [Img, Img, Img]

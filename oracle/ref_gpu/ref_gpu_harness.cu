@@ -26,20 +26,31 @@
 #include <string>
 #include <vector>
 
-namespace {
-
+// Outside the unnamed namespace: the exported functions take it by value,
+// and a parameter type with internal linkage would make them internal too.
 struct Img {  // layout of GPUImageWrapper (gpuimagewrapper.h:8-24)
     float* data;
     int width, height, channels;
 };
 
+namespace {
+
 CUmodule g_mod = nullptr;
 std::string g_err;
 enum K { kWarp, kAdap, kWt, kOut, kBil, kToF, kToC, kCorr, kRearr, kWarpOp, kCount };
 CUfunction g_fn[kCount] = {};
-const char* const kNames[kCount] = {"11kernel_warp", "16kernel_adap_comb", "17kernel_consist_wt",
-    "18kernel_consist_out", "15kernel_bilinear", "20kernel_to_float_image", "19kernel_to_char_image",
-    "31correlation_cuda_forward_kernelIf", "21blob_rearrange_kernelIf", "19warp_forward_kernelIf"};
+// Kernels are found by their source name inside the mangled name: the
+// Itanium ABI writes <length><name> (then "If" for the float instantiation
+// of the templated op kernels).
+const char* const kNames[kCount] = {"kernel_warp", "kernel_adap_comb", "kernel_consist_wt", "kernel_consist_out",
+    "kernel_bilinear", "kernel_to_float_image", "kernel_to_char_image", "correlation_cuda_forward_kernel",
+    "blob_rearrange_kernel", "warp_forward_kernel"};
+const bool kTemplated[kCount] = {false, false, false, false, false, false, false, true, true, true};
+
+std::string mangled_key(int k)
+{
+    return std::to_string(std::strlen(kNames[k])) + kNames[k] + (kTemplated[k] ? "If" : "");
+}
 
 int fail(const char* what, CUresult r)
 {
@@ -82,12 +93,12 @@ int rg_init(const char* cubin)
         if (cuFuncGetName(&name, f) != CUDA_SUCCESS || !name)
             continue;
         for (int k = 0; k < kCount; ++k)
-            if (std::strstr(name, kNames[k]))
+            if (std::strstr(name, mangled_key(k).c_str()))
                 g_fn[k] = f;
     }
     for (int k = 0; k < kCount; ++k)
         if (!g_fn[k]) {
-            g_err = std::string("kernel not found: ") + kNames[k];
+            g_err = std::string("kernel not found: ") + mangled_key(k);
             return -1;
         }
     return 0;

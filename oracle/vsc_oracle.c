@@ -353,6 +353,67 @@ void vo_adap_comb(const float* crnt_in, const float* crnt_pr, const float* prev_
     const float* next_warp_in, const float* next_warp_pr, float* adap_in, float* adap_pr, const float* last_stab_warp,
     float alpha, int64_t npix)
 {
+    vo_adap_comb_masked(crnt_in, crnt_pr, prev_warp_in, prev_warp_pr, next_warp_in, next_warp_pr, adap_in, adap_pr,
+        last_stab_warp, NULL, alpha, npix);
+}
+
+/* Forward-backward flow consistency (not in the reference; an opt-in
+ * extension).  For flow a at pixel (x, y), sample the opposite flow b at the
+ * point a carries the pixel to, p = (x + a.x, y + a.y) (bilinear, right and
+ * bottom taps clamped to the last column/row); the pixel is consistent if
+ * |a + b(p)|^2 <= 0.01 (|a|^2 + |b(p)|^2) + 0.5, the usual occlusion test
+ * of forward-backward checks.  Pixels carried outside the frame, and NaN
+ * flows, are inconsistent.  Returns 1 or 0. */
+static float occl_check(const float* a, const float* b, int fc, int x, int y, int w, int h)
+{
+    const int64_t i = ((int64_t)y * w + x) * fc;
+    const float ax = a[i], ay = a[i + 1];
+    const float px = (float)x + ax;
+    const float py = (float)y + ay;
+    if (!(px >= 0.0f && px <= (float)(w - 1) && py >= 0.0f && py <= (float)(h - 1)))
+        return 0.0f;
+    const int ix = (int)floorf(px);
+    const int iy = (int)floorf(py);
+    const float fx = px - (float)ix;
+    const float fy = py - (float)iy;
+    const int ix1 = ix + 1 < w - 1 ? ix + 1 : w - 1;
+    const int iy1 = iy + 1 < h - 1 ? iy + 1 : h - 1;
+    float bv[2];
+    for (int k = 0; k < 2; ++k) {
+        const float b00 = b[((int64_t)iy * w + ix) * fc + k];
+        const float b10 = b[((int64_t)iy * w + ix1) * fc + k];
+        const float b01 = b[((int64_t)iy1 * w + ix) * fc + k];
+        const float b11 = b[((int64_t)iy1 * w + ix1) * fc + k];
+        const float t0 = b00 * (1.0f - fx) + b10 * fx;
+        const float t1 = b01 * (1.0f - fx) + b11 * fx;
+        bv[k] = t0 * (1.0f - fy) + t1 * fy;
+    }
+    const float dx = ax + bv[0];
+    const float dy = ay + bv[1];
+    const float lhs = dx * dx + dy * dy;
+    const float rhs = 0.01f * ((ax * ax + ay * ay) + (bv[0] * bv[0] + bv[1] * bv[1])) + 0.5f;
+    return lhs <= rhs ? 1.0f : 0.0f;
+}
+
+void vo_flow_consistency_mask(const float* flow_fwd, const float* flow_bwd, int fc, float* mask, int w, int h)
+{
+    _Pragma("omp parallel for schedule(static)") for (int y = 0; y < h; ++y)
+    {
+        for (int x = 0; x < w; ++x) {
+            float* m = mask + ((int64_t)y * w + x) * 2;
+            m[0] = occl_check(flow_bwd, flow_fwd, fc, x, y, w, h);
+            m[1] = occl_check(flow_fwd, flow_bwd, fc, x, y, w, h);
+        }
+    }
+}
+
+/* kernel_adap_comb with the two temporal weights multiplied by a per-pixel
+ * mask after their clamps (mask ch0 -> previous frame, ch1 -> next frame);
+ * a NULL mask, or a mask of ones, gives kernel_adap_comb's bits. */
+void vo_adap_comb_masked(const float* crnt_in, const float* crnt_pr, const float* prev_warp_in,
+    const float* prev_warp_pr, const float* next_warp_in, const float* next_warp_pr, float* adap_in, float* adap_pr,
+    const float* last_stab_warp, const float* occ_mask, float alpha, int64_t npix)
+{
     _Pragma("omp parallel for schedule(static)") for (int64_t i = 0; i < npix * 3; ++i)
     {
         const float ci = crnt_in[i], pi = prev_warp_in[i], ni = next_warp_in[i];
@@ -368,6 +429,10 @@ void vo_adap_comb(const float* crnt_in, const float* crnt_pr, const float* prev_
             wt_prv = 0.0f;
         if (wt_nxt < 0.001f)
             wt_nxt = 0.0f;
+        if (occ_mask) {
+            wt_prv = wt_prv * occ_mask[(i / 3) * 2];
+            wt_nxt = wt_nxt * occ_mask[(i / 3) * 2 + 1];
+        }
         const float ain = wt_prv * pi + wt_nxt * ni + (1.0f - (wt_prv + wt_nxt)) * ci;
         float apr = wt_prv * pp + wt_nxt * np + (1.0f - (wt_prv + wt_nxt)) * cp;
         apr = wt_prv * ls + (1.0f - wt_prv) * apr;
@@ -508,6 +573,13 @@ void vo_default_hyper(vo_hyper* hp)
 int vo_stab_pass(int w, int h, const float* const orig[3], const float* const proc[3], const float* flow_fwd,
     const float* flow_bwd, int fc, const float* last_stab, const vo_hyper* hp, float* out_f32, uint8_t* out_rgba)
 {
+    return vo_stab_pass_ex(w, h, orig, proc, flow_fwd, flow_bwd, fc, last_stab, hp, 0, out_f32, out_rgba);
+}
+
+int vo_stab_pass_ex(int w, int h, const float* const orig[3], const float* const proc[3], const float* flow_fwd,
+    const float* flow_bwd, int fc, const float* last_stab, const vo_hyper* hp, int occlusion_mask, float* out_f32,
+    uint8_t* out_rgba)
+{
     const int L = hp->pyramid_levels;
     if (L < 1 || L > 8 || (w >> (L - 1)) < 2 || (h >> (L - 1)) < 2)
         return -1;
@@ -526,7 +598,14 @@ int vo_stab_pass(int w, int h, const float* const orig[3], const float* const pr
     vo_stab_warp(orig[2], flow_fwd, fc, next_in, w, h);
     vo_stab_warp(proc[2], flow_fwd, fc, next_pr, w, h);
     vo_stab_warp(last_stab, flow_bwd, fc, last_w, w, h);
-    vo_adap_comb(orig[1], proc[1], prev_in, prev_pr, next_in, next_pr, adap_in, adap_pr, last_w, hp->alpha, npix);
+    float* occ = NULL;
+    if (occlusion_mask) {
+        occ = (float*)malloc((size_t)npix * 2 * sizeof(float));
+        vo_flow_consistency_mask(flow_fwd, flow_bwd, fc, occ, w, h);
+    }
+    vo_adap_comb_masked(orig[1], proc[1], prev_in, prev_pr, next_in, next_pr, adap_in, adap_pr, last_w, occ, hp->alpha,
+        npix);
+    free(occ);
     vo_consist_wt(orig[1], adap_in, cons_wt, hp->beta, hp->gamma, npix);
 
     float* pP[8];

@@ -58,6 +58,16 @@ void vo_stab_warp(const float* in, const float* flow, int fc, float* out, int w,
 void vo_adap_comb(const float* crnt_in, const float* crnt_pr, const float* prev_warp_in, const float* prev_warp_pr,
     const float* next_warp_in, const float* next_warp_pr, float* adap_in, float* adap_pr, const float* last_stab_warp,
     float alpha, int64_t npix); /* :116-166 */
+/* Opt-in extension (no counterpart in the reference): forward-backward flow
+ * consistency.  mask is HWC2: ch0 = 1 where the backward flow is confirmed by
+ * the forward flow (the previous frame's warp), ch1 = 1 where the forward
+ * flow is confirmed by the backward flow (the next frame's warp), else 0. */
+void vo_flow_consistency_mask(const float* flow_fwd, const float* flow_bwd, int fc, float* mask, int w, int h);
+/* vo_adap_comb with wt_prv, wt_nxt multiplied by occ_mask ch0, ch1 after the
+ * clamps; occ_mask == NULL is vo_adap_comb. */
+void vo_adap_comb_masked(const float* crnt_in, const float* crnt_pr, const float* prev_warp_in,
+    const float* prev_warp_pr, const float* next_warp_in, const float* next_warp_pr, float* adap_in, float* adap_pr,
+    const float* last_stab_warp, const float* occ_mask, float alpha, int64_t npix);
 void vo_consist_wt(const float* crnt_in, const float* adap_in, float* cons_wt, float beta, float gamma,
     int64_t npix); /* :168-191 */
 void vo_bilinear(const float* in, int iw, int ih, float* out, int ow, int oh, int c); /* :50-75 */
@@ -78,6 +88,11 @@ void vo_default_hyper(vo_hyper* hp); /* videostabilizer.cpp:104-112 */
  * out_rgba != NULL, its RGBA8 quantisation.  Returns 0, or -1 on bad sizes. */
 int vo_stab_pass(int w, int h, const float* const orig[3], const float* const proc[3], const float* flow_fwd,
     const float* flow_bwd, int fc, const float* last_stab, const vo_hyper* hp, float* out_f32, uint8_t* out_rgba);
+/* vo_stab_pass with the opt-in forward-backward consistency mask applied to
+ * the temporal weights when occlusion_mask != 0. */
+int vo_stab_pass_ex(int w, int h, const float* const orig[3], const float* const proc[3], const float* flow_fwd,
+    const float* flow_bwd, int fc, const float* last_stab, const vo_hyper* hp, int occlusion_mask, float* out_f32,
+    uint8_t* out_rgba);
 
 /* ---- weight-free flow estimator built from the two ops ---------------------
  * A coarse-to-fine stand-in for the missing PWC-Net weights: random-projection

@@ -103,6 +103,7 @@ def test_stabilizer_rejects_bad_config(vsc):
         (vsc.StabilizerConfig(64, 64, 2, 1, 1, 3, 1), vsc.VSC_EUNSUPPORTED, "batch"),
         (vsc.StabilizerConfig(64, 64, 1, 1, 0, 3, 1), vsc.VSC_EINVAL, "downscale"),
         (vsc.StabilizerConfig(64, 64, 1, 0, 1, 4, 1), vsc.VSC_EINVAL, "flow_channels"),
+        (vsc.StabilizerConfig(64, 64, 1, 1, 1, 3, 1, 7), vsc.VSC_EINVAL, "corr_dtype"),
     ]:
         rc, msg = _status(vsc, L.vsc_stabilizer_create(C.byref(cfg), None, C.byref(h)))
         assert rc == code and word in msg, (rc, msg)

@@ -4,7 +4,8 @@ the CPU restatement and the reference's own CPU ops (golden fixtures).
 Tolerances: Correlation is bit-exact (channel-order sum with separately
 rounded products, as correlation.cc computes).  Warp is bit-exact against the
 single-precision restatement and within 2^-21 * max|input| of the reference's
-double-weight CPU op."""
+double-weight CPU op.  The double-precision entry points are bit-exact to the
+reference's DOUBLE outputs."""
 from __future__ import annotations
 
 import numpy as np
@@ -99,6 +100,40 @@ def test_warp_reference_fixture(vsc, cuda, golden, i):
     x = g[f"warp{i}_x"]
     out = vsc.warp(_t(x, cuda), _t(g[f"warp{i}_flow"], cuda)).cpu().numpy()
     assert np.max(np.abs(out - g[f"warp{i}_out"])) <= 2.0 ** -21 * np.max(np.abs(x))
+
+
+@pytest.mark.parametrize("i", range(5))
+def test_correlation_f64_reference_fixture(vsc, cuda, golden, i):
+    """The DOUBLE branch of correlation.cc: bit-exact to the reference's output."""
+    g = golden["ref_ops"]
+    f1 = g[f"corr{i}_f1"].astype(np.float64)
+    f2 = g[f"corr{i}_f2"].astype(np.float64)
+    out = vsc.correlation(_t(f1, cuda), _t(f2, cuda), int(g[f"corr{i}_md"]))
+    assert np.array_equal(out.cpu().numpy(), g[f"corr{i}_out64"])
+
+
+@pytest.mark.parametrize("i", range(3))
+def test_warp_f64_reference_fixture(vsc, cuda, golden, i):
+    """The DOUBLE branch of warp.cc: bit-exact to the reference's output."""
+    g = golden["ref_ops"]
+    x = g[f"warp{i}_x"].astype(np.float64)
+    fl = g[f"warp{i}_flow"].astype(np.float64)
+    out = vsc.warp(_t(x, cuda), _t(fl, cuda)).cpu().numpy()
+    assert np.array_equal(out, g[f"warp{i}_out64"])
+
+
+@pytest.mark.parametrize("shape,md", [((2, 37, 19, 45), 4), ((1, 196, 17, 30), 4), ((1, 5, 8, 8), 0)])
+def test_ops_f64_vs_restatement(vsc, oracle, cuda, shape, md):
+    f1 = RNG.standard_normal(shape)
+    f2 = RNG.standard_normal(shape)
+    out = vsc.correlation(_t(f1, cuda), _t(f2, cuda), md).cpu().numpy()
+    assert out.dtype == np.float64 and np.array_equal(out, oracle.correlation(f1, f2, md))
+    fl = RNG.normal(0, 4, (shape[0], 2) + shape[2:])
+    fl[0, 0, 0, :3] = [np.nan, 1e9, -0.0]
+    w = vsc.warp(_t(f1, cuda), _t(fl, cuda)).cpu().numpy()
+    assert np.array_equal(w, oracle.warp_op(f1, fl, "f64"), equal_nan=True)
+    with pytest.raises(ValueError, match="legacy"):
+        vsc.correlation(_t(f1, cuda), _t(f2, cuda), md, legacy=1)
 
 
 def test_ops_on_a_side_stream(vsc, oracle, cuda):

@@ -6,7 +6,8 @@ Bars, stated per test:
   * kernels without transcendental functions, built without FMA contraction
     ("exact" cubin): bit-exact to the restatement;
   * adaptive combination / consistency weights: the reference calls CUDA's
-    expf, the restatement its own exp (< 1 ulp); weights within 4e-7 absolute,
+    expf, the restatement its own exp (< 1 ulp); combinations within 4e-7
+    absolute, weights (computed from the same adapCmbIn) within 4e-7 * gamma,
     clamp decisions flipping on at most 1e-4 of the values;
   * the solver: the reference updates in place (a data race); after the full
     pyramid solve the result is within 40 dB PSNR of the Jacobi restatement;
@@ -51,7 +52,8 @@ def test_frame_io_exact(rg, oracle, cuda):
     L = rg.load("exact")
     rgba = RNG.integers(0, 256, (21, 37, 4), dtype=np.uint8)
     out = _empty((21, 37, 3), cuda)
-    rg.check(L, L.rg_to_float(_t(rgba, cuda).data_ptr(), rg.img(out)))
+    d_rgba = _t(rgba, cuda)
+    rg.check(L, L.rg_to_float(d_rgba.data_ptr(), rg.img(out)))
     assert np.array_equal(out.cpu().numpy(), oracle.rgba_to_float(rgba))
     vals = np.concatenate([RNG.uniform(-1.2, 1.2, 21 * 37 * 3 - 3), [np.nan, 1.0, 256 / 255]]).astype(np.float32)
     f = _t(vals.reshape(21, 37, 3), cuda)
@@ -66,7 +68,8 @@ def test_kernel_warp_exact(rg, oracle, vsc, cuda, fc):
     img = RNG.random((45, 70, 3)).astype(np.float32)
     flow = RNG.normal(0, 6, (45, 70, fc)).astype(np.float32)
     out = _empty((45, 70, 3), cuda)
-    rg.check(L, L.rg_warp(rg.img(_t(img, cuda)), rg.img(_t(flow, cuda)), rg.img(out)))
+    d_img, d_flow = _t(img, cuda), _t(flow, cuda)  # held: the harness takes raw pointers
+    rg.check(L, L.rg_warp(rg.img(d_img), rg.img(d_flow), rg.img(out)))
     ref = out.cpu().numpy()
     assert np.array_equal(ref, oracle.stab_warp(img, flow))
     assert np.array_equal(ref, vsc.get_warp_result(_t(img, cuda), _t(flow, cuda)).cpu().numpy())
@@ -77,7 +80,8 @@ def test_kernel_bilinear_exact(rg, oracle, cuda, src, dst):
     L = rg.load("exact")
     img = RNG.random((src[1], src[0], 3)).astype(np.float32)
     out = _empty((dst[1], dst[0], 3), cuda)
-    rg.check(L, L.rg_bilinear(rg.img(_t(img, cuda)), rg.img(out)))
+    d_img = _t(img, cuda)
+    rg.check(L, L.rg_bilinear(rg.img(d_img), rg.img(out)))
     assert np.array_equal(out.cpu().numpy(), oracle.bilinear(img, dst[0], dst[1]))
 
 
@@ -92,11 +96,14 @@ def test_adap_comb_and_weights_vs_cuda_expf(rg, oracle, cuda):
     wt = _empty(base.shape, cuda)
     rg.check(L, L.rg_consist_wt(rg.img(ain), rg.img(dev[0]), rg.img(wt), 6800.0, 2.0))
     oin, opr = oracle.adap_comb(*ims, 6800.0)
-    owt = oracle.consist_wt(ims[0], oin, 6800.0, 2.0)
-    for got, ref in ((ain, oin), (apr, opr), (wt, owt)):
+    for got, ref in ((ain, oin), (apr, opr)):
         got = got.cpu().numpy()
         assert np.max(np.abs(got - ref)) <= 4e-7 * max(1.0, float(np.abs(ref).max()))
+    # the weights from the reference's own adapCmbIn: with beta = 6800 an
+    # ulp of adapCmbIn moves a weight by ~100 ulp, so only the exp differs here
+    owt = oracle.consist_wt(ims[0], ain.cpu().numpy(), 6800.0, 2.0)
     g = wt.cpu().numpy()
+    assert np.max(np.abs(g - owt)) <= 4e-7 * 2.0
     flips = np.mean((g == 0) != (owt == 0))
     assert flips <= 1e-4, flips
 
@@ -113,8 +120,8 @@ def test_in_place_solver_vs_jacobi(rg, oracle, cuda):
     A = np.clip(P + RNG.normal(0, 0.05, P.shape), 0, 1).astype(np.float32)
     Wt = RNG.uniform(0, 2, P.shape).astype(np.float32)
     out = _t(P, cuda)
-    rg.check(L, L.rg_consist_out(rg.img(_t(P, cuda)), rg.img(_t(A, cuda)), rg.img(_t(Wt, cuda)), 150, 0.15, 0.15,
-                                 rg.img(out)))
+    d_p, d_a, d_w = _t(P, cuda), _t(A, cuda), _t(Wt, cuda)
+    rg.check(L, L.rg_consist_out(rg.img(d_p), rg.img(d_a), rg.img(d_w), 150, 0.15, 0.15, rg.img(out)))
     jac = oracle.consist_out(P, A, Wt, 150, 0.15, 0.15, P)
     assert _psnr(out.cpu().numpy(), jac) >= 40.0
 
@@ -126,8 +133,8 @@ def test_reference_correlation_op(rg, oracle, cuda):
     f1 = RNG.standard_normal((2, 64, 17, 23)).astype(np.float32)
     f2 = RNG.standard_normal((2, 64, 17, 23)).astype(np.float32)
     out = torch.empty((2, 9, 9, 17, 23), dtype=torch.float32, device=cuda)
-    rg.check(L, L.rg_correlation(_t(f1, cuda).data_ptr(), _t(f2, cuda).data_ptr(), out.data_ptr(), 2, 64, 17, 23, 4,
-                                 None))
+    d1, d2 = _t(f1, cuda), _t(f2, cuda)
+    rg.check(L, L.rg_correlation(d1.data_ptr(), d2.data_ptr(), out.data_ptr(), 2, 64, 17, 23, 4, None))
     torch.cuda.synchronize()
     ref = oracle.correlation(f1, f2, 4)
     np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=1e-5, atol=1e-5)
@@ -142,7 +149,8 @@ def test_reference_warp_op_exact(rg, oracle, cuda):
     x = (RNG.random((2, 6, 19, 13)) * 10).astype(np.float32)
     fl = (RNG.random((2, 2, 19, 13)) * 8 - 4).astype(np.float32)
     out = torch.empty(x.shape, dtype=torch.float32, device=cuda)
-    rg.check(L, L.rg_warp_op(_t(x, cuda).data_ptr(), _t(fl, cuda).data_ptr(), out.data_ptr(), 2, 6, 19, 13, None))
+    dx, dfl = _t(x, cuda), _t(fl, cuda)
+    rg.check(L, L.rg_warp_op(dx.data_ptr(), dfl.data_ptr(), out.data_ptr(), 2, 6, 19, 13, None))
     torch.cuda.synchronize()
     assert np.array_equal(out.cpu().numpy(), oracle.warp_op(x, fl, "refsem"))
 

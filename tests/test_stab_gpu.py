@@ -133,7 +133,7 @@ def _frames(w, h, n, seed):
     return [s.frame(i) for i in range(n)]
 
 
-def _run_oracle_stream(oracle, frames, flows=None, hp=None, downscale=1):
+def _run_oracle_stream(oracle, frames, flows=None, hp=None, downscale=1, occlusion=False):
     """The reference's driver loop (stabilizefiles.cpp:108-131 with
     videostabilizer.cpp:136-265) over the restatement."""
     orig = [oracle.rgba_to_float(o) for o, _ in frames]
@@ -152,7 +152,7 @@ def _run_oracle_stream(oracle, frames, flows=None, hp=None, downscale=1):
         else:
             ff = oracle.flow_estimate(orig[t], orig[t + 1])
             fb = oracle.flow_estimate(orig[t + 1], orig[t])
-        out, rgba = oracle.stab_pass(orig[t - 1:t + 2], proc[t - 1:t + 2], ff, fb, last, hp)
+        out, rgba = oracle.stab_pass(orig[t - 1:t + 2], proc[t - 1:t + 2], ff, fb, last, hp, occlusion_mask=occlusion)
         outs.append((out, rgba, ff, fb))
         last = out
     return outs
@@ -245,6 +245,75 @@ def test_stabilizer_external_flows_host_io(vsc, oracle, cuda):
             st.load_frame(*frames[t + 2])
     with pytest.raises(vsc.VscError, match="ESTATE"):
         st.step()
+    st.close()
+
+
+@pytest.mark.parametrize("fc", [2, 3])
+def test_flow_consistency_mask(vsc, oracle, cuda, fc):
+    """Opt-in forward-backward consistency mask: the 0/1 decisions equal the
+    restatement's, including pixels carried out of the frame and NaN flows."""
+    h, w = 57, 83
+    # a near-constant motion and its inverse are consistent (but for noise)
+    ff = (np.array([2.3, -1.1, 0.0][:fc], np.float32) + RNG.normal(0, 0.1, (h, w, fc))).astype(np.float32)
+    fb = (np.array([-2.3, 1.1, 0.0][:fc], np.float32) + RNG.normal(0, 0.3, (h, w, fc))).astype(np.float32)
+    fb[5:15, 10:30] = RNG.normal(0, 6, (10, 20, fc))              # an inconsistent patch
+    ff[0, :5, 0] = -10.0                                           # carried out of the frame
+    ff[3, 3, 1] = np.nan
+    ref = oracle.flow_consistency_mask(ff, fb)
+    got = vsc.get_flow_consistency_mask(_t(ff, cuda), _t(fb, cuda)).cpu().numpy()
+    assert np.array_equal(got, ref)
+    assert 0.2 < ref.mean() < 0.98  # both outcomes occur
+    assert ref[0, :5, 1].max() == 0.0 and ref[3, 3, 1] == 0.0
+
+
+def test_adap_comb_masked(vsc, oracle, cuda):
+    h, w = 40, 64
+    base = _img(h, w)
+    ims = [np.clip(base + RNG.normal(0, s, base.shape), 0, 1).astype(np.float32)
+           for s in (0.0, 0.05, 0.02, 0.03, 0.02, 0.04, 0.01)]
+    mask = (RNG.random((h, w, 2)) < 0.6).astype(np.float32)
+    mask[:4] = RNG.random((4, w, 2)).astype(np.float32)  # soft factors multiply too
+    dev = [_t(a, cuda) for a in ims]
+    ain, apr = vsc.get_adap_comb_masked(*dev[:6], dev[6], _t(mask, cuda), 20.0)
+    oin, opr = oracle.adap_comb_masked(*ims[:6], ims[6], mask, 20.0)
+    assert np.array_equal(ain.cpu().numpy(), oin) and np.array_equal(apr.cpu().numpy(), opr)
+    ones = np.ones((h, w, 2), np.float32)
+    ain1, apr1 = vsc.get_adap_comb_masked(*dev[:6], dev[6], _t(ones, cuda), 20.0)
+    bin_, bpr = vsc.get_adap_comb(*dev[:6], dev[6], 20.0)
+    assert np.array_equal(ain1.cpu().numpy(), bin_.cpu().numpy())
+    assert np.array_equal(apr1.cpu().numpy(), bpr.cpu().numpy())
+    assert not np.array_equal(apr.cpu().numpy(), bpr.cpu().numpy())
+
+
+@pytest.mark.parametrize("use_graphs", [False, True])
+def test_stabilizer_occlusion_mask(vsc, oracle, cuda, use_graphs):
+    """The opt-in mask inside the fused front end equals the restatement's
+    pass with the mask; switching it off again restores the default bits."""
+    import torch
+
+    w, h = 80, 48
+    frames = _frames(w, h, 6, seed=21)
+    flows = {}
+    for t in range(1, 5):
+        ff = RNG.normal(0, 2, (h, w, 2)).astype(np.float32)
+        fb = (-ff + RNG.normal(0, 0.5, ff.shape)).astype(np.float32)
+        flows[t] = (ff, fb)
+    ref_on = _run_oracle_stream(oracle, frames, flows=flows, occlusion=True)
+    ref_off = _run_oracle_stream(oracle, frames, flows=flows)
+    assert not np.array_equal(ref_on[0][0], ref_off[0][0])
+    stream = torch.cuda.Stream()
+    st = vsc.Stabilizer(w, h, compute_flow=False, flow_channels=2, stream=stream, use_graphs=use_graphs)
+    st.set_occlusion_mask(True)
+    for i in range(3):
+        st.load_frame(*frames[i])
+    for k, t in enumerate(range(1, 5)):
+        st.set_flows(torch.from_numpy(flows[t][0]), torch.from_numpy(flows[t][1]))
+        with torch.cuda.stream(stream):
+            out = st.step()
+        stream.synchronize()
+        assert np.array_equal(out.cpu().numpy(), ref_on[k][1]), k
+        if t + 2 < len(frames):
+            st.load_frame(*frames[t + 2])
     st.close()
 
 

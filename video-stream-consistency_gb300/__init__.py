@@ -34,8 +34,13 @@ EXPORTED = [
     "vsc_stabilizer_create", "vsc_stabilizer_destroy", "vsc_stabilizer_hyper_params", "vsc_stabilizer_load_frame",
     "vsc_stabilizer_set_flows", "vsc_stabilizer_step", "vsc_stabilizer_buffer", "vsc_stabilizer_last_launches",
     "vsc_stabilizer_enable_timing", "vsc_stabilizer_stage_ms", "vsc_check_device", "vsc_selftest_bounded_wait",
-    "vsc_get_consist_out_noalloc",
+    "vsc_get_consist_out_noalloc", "vsc_get_flow_consistency_mask", "vsc_get_adap_comb_masked",
+    "vsc_stabilizer_set_occlusion_mask", "vsc_correlation_fwd_f64", "vsc_warp_fwd_f64",
+    "vsc_correlation_lowp_workspace_size", "vsc_correlation_fwd_lowp",
+    "vsc_image_file_info", "vsc_read_image_file", "vsc_write_png", "vsc_flo_info", "vsc_read_flo", "vsc_write_flo",
+    "vsc_stabilize_files", "vsc_solver_steps_per_launch",
 ]
+VSC_DTYPE_F32, VSC_DTYPE_BF16, VSC_DTYPE_F16 = 0, 1, 2
 NOALLOC_MAX_PIXELS = 349525  # VSC_NOALLOC_MAX_PIXELS
 
 
@@ -61,10 +66,19 @@ class HyperParams(C.Structure):
     ]
 
 
+class FilesConfig(C.Structure):
+    _fields_ = [
+        ("original_dir", C.c_char_p), ("processed_dir", C.c_char_p), ("output_dir", C.c_char_p),
+        ("flow_dir", C.c_char_p), ("width", C.c_int32), ("height", C.c_int32), ("flow_downscale", C.c_int32),
+        ("corr_dtype", C.c_int32), ("hyper", C.c_void_p),
+    ]
+
+
 class StabilizerConfig(C.Structure):
     _fields_ = [
         ("width", C.c_int32), ("height", C.c_int32), ("batch_size", C.c_int32), ("compute_flow", C.c_int32),
         ("flow_downscale", C.c_int32), ("flow_channels", C.c_int32), ("use_graphs", C.c_int32),
+        ("corr_dtype", C.c_int32),
     ]
 
 
@@ -97,6 +111,9 @@ def load():
     for fn, args in {
         "vsc_correlation_fwd": [vp, vp, vp, i64, i64, i64, i64, i64, i64, vp],
         "vsc_warp_fwd": [vp, vp, vp, i64, i64, i64, i64, vp],
+        "vsc_correlation_fwd_f64": [vp, vp, vp, i64, i64, i64, i64, i64, vp],
+        "vsc_correlation_fwd_lowp": [vp, vp, vp, i64, i64, i64, i64, i64, i32, vp, C.c_size_t, vp],
+        "vsc_warp_fwd_f64": [vp, vp, vp, i64, i64, i64, i64, vp],
         "vsc_char_to_float_image": [vp, IP, vp],
         "vsc_float_to_char_image": [IP, vp, vp],
         "vsc_get_warp_result": [IP, IP, IP, vp],
@@ -112,6 +129,16 @@ def load():
         "vsc_stabilizer_step": [vp, vp, i32],
         "vsc_stabilizer_buffer": [vp, i32, C.POINTER(vp)],
         "vsc_stabilizer_enable_timing": [vp, i32],
+        "vsc_get_flow_consistency_mask": [IP, IP, IP, vp],
+        "vsc_image_file_info": [C.c_char_p, C.POINTER(i32), C.POINTER(i32)],
+        "vsc_read_image_file": [C.c_char_p, vp, i32, i32],
+        "vsc_write_png": [C.c_char_p, vp, i32, i32],
+        "vsc_flo_info": [C.c_char_p, C.POINTER(i32), C.POINTER(i32)],
+        "vsc_read_flo": [C.c_char_p, vp, i32, i32],
+        "vsc_write_flo": [C.c_char_p, vp, i32, i32],
+        "vsc_stabilize_files": [C.POINTER(FilesConfig), C.POINTER(i32)],
+        "vsc_get_adap_comb_masked": [IP] * 10 + [f32, vp],
+        "vsc_stabilizer_set_occlusion_mask": [vp, i32],
         "vsc_check_device": [],
         "vsc_selftest_bounded_wait": [i32, vp],
         "vsc_stabilizer_stage_ms": [vp, C.POINTER(C.c_float), i32],
@@ -119,6 +146,10 @@ def load():
         f = getattr(L, fn)
         f.argtypes = args
         f.restype = C.c_int
+    L.vsc_solver_steps_per_launch.restype = i32
+    L.vsc_solver_steps_per_launch.argtypes = []
+    L.vsc_correlation_lowp_workspace_size.restype = C.c_size_t
+    L.vsc_correlation_lowp_workspace_size.argtypes = [i64, i64, i64, i64]
     L.vsc_consist_out_workspace_size.restype = C.c_size_t
     L.vsc_consist_out_workspace_size.argtypes = [i32, i32]
     L.vsc_default_hyper_params.restype = None
@@ -160,14 +191,32 @@ def image(t) -> Image:
 
 # ---- custom ops ---------------------------------------------------------------
 
-def correlation(f1, f2, max_displacement: int = 4, legacy: int = 0, out=None, stream=None):
-    """custom::Correlation on N x C x H x W float tensors."""
+def _f64(t, name):
     import torch
 
-    _f32(f1, "f1")
-    _f32(f2, "f2")
+    if not (t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+        raise ValueError(f"{name}: expected a contiguous float64 CUDA tensor")
+
+
+def correlation(f1, f2, max_displacement: int = 4, legacy: int = 0, out=None, stream=None):
+    """custom::Correlation on N x C x H x W float (or, like the reference's
+    CPU kernel, double) tensors."""
+    import torch
+
     N, Cc, H, W = f1.shape
     P = 2 * max_displacement + 1
+    if f1.dtype == torch.float64:
+        if legacy:
+            raise ValueError("correlation: the legacy form has no double version (correlation.h:45-46)")
+        _f64(f1, "f1")
+        _f64(f2, "f2")
+        if out is None:
+            out = torch.empty((N, P, P, H, W), dtype=torch.float64, device=f1.device)
+        _check(load().vsc_correlation_fwd_f64(f1.data_ptr(), f2.data_ptr(), out.data_ptr(), N, Cc, H, W,
+                                              max_displacement, _stream(stream)))
+        return out
+    _f32(f1, "f1")
+    _f32(f2, "f2")
     shape = (N, P * P, H, W) if legacy else (N, P, P, H, W)
     if out is None:
         out = torch.empty(shape, dtype=torch.float32, device=f1.device)
@@ -176,15 +225,41 @@ def correlation(f1, f2, max_displacement: int = 4, legacy: int = 0, out=None, st
     return out
 
 
-def warp(x, flow, out=None, stream=None):
-    """custom::Warp: x N x C x H x W, flow N x 2 x H x W."""
+def correlation_lowp(f1, f2, max_displacement: int = 4, dtype: str = "bf16", out=None, workspace=None,
+                     stream=None):
+    """custom::Correlation (legacy 0 layout) on the tensor cores with BF16 or
+    FP16 operands and FP32 accumulation; f1, f2 float32 N x C x H x W."""
     import torch
 
-    _f32(x, "input")
-    _f32(flow, "flow")
+    _f32(f1, "f1")
+    _f32(f2, "f2")
+    N, Cc, H, W = f1.shape
+    P = 2 * max_displacement + 1
+    if out is None:
+        out = torch.empty((N, P, P, H, W), dtype=torch.float32, device=f1.device)
+    code = {"bf16": VSC_DTYPE_BF16, "fp16": VSC_DTYPE_F16, "f16": VSC_DTYPE_F16}[dtype]
+    ws_ptr, ws_bytes = (None, 0) if workspace is None else (workspace.data_ptr(),
+                                                           workspace.numel() * workspace.element_size())
+    _check(load().vsc_correlation_fwd_lowp(f1.data_ptr(), f2.data_ptr(), out.data_ptr(), N, Cc, H, W,
+                                           max_displacement, code, ws_ptr, ws_bytes, _stream(stream)))
+    return out
+
+
+def warp(x, flow, out=None, stream=None):
+    """custom::Warp: x N x C x H x W, flow N x 2 x H x W (float, or double)."""
+    import torch
+
     N, Cc, H, W = x.shape
     if out is None:
         out = torch.empty_like(x)
+    if x.dtype == torch.float64:
+        _f64(x, "input")
+        _f64(flow, "flow")
+        _check(load().vsc_warp_fwd_f64(x.data_ptr(), flow.data_ptr(), out.data_ptr(), N, Cc, H, W,
+                                       _stream(stream)))
+        return out
+    _f32(x, "input")
+    _f32(flow, "flow")
     _check(load().vsc_warp_fwd(x.data_ptr(), flow.data_ptr(), out.data_ptr(), N, Cc, H, W, _stream(stream)))
     return out
 
@@ -225,6 +300,31 @@ def get_adap_comb(crnt_in, crnt_pr, prev_in, prev_pr, next_in, next_pr, last_sta
     apr = torch.empty_like(crnt_in)
     ims = [image(t) for t in (crnt_in, crnt_pr, prev_in, prev_pr, next_in, next_pr, ain, apr, last_stab_warp)]
     _check(load().vsc_get_adap_comb(*[C.byref(i) for i in ims], float(alpha), _stream(stream)))
+    return ain, apr
+
+
+def get_flow_consistency_mask(flow_fwd, flow_bwd, stream=None):
+    """Forward-backward flow consistency mask (opt-in extension): HWC2 of 0/1,
+    ch0 for the previous frame's warp, ch1 for the next frame's."""
+    import torch
+
+    h, w = flow_fwd.shape[:2]
+    mask = torch.empty((h, w, 2), dtype=torch.float32, device=flow_fwd.device)
+    _check(load().vsc_get_flow_consistency_mask(C.byref(image(flow_fwd)), C.byref(image(flow_bwd)),
+                                                C.byref(image(mask)), _stream(stream)))
+    return mask
+
+
+def get_adap_comb_masked(crnt_in, crnt_pr, prev_in, prev_pr, next_in, next_pr, last_stab_warp, occ_mask, alpha,
+                         stream=None):
+    """get_adap_comb with the temporal weights multiplied by occ_mask (HWC2)."""
+    import torch
+
+    ain = torch.empty_like(crnt_in)
+    apr = torch.empty_like(crnt_in)
+    ims = [image(t) for t in (crnt_in, crnt_pr, prev_in, prev_pr, next_in, next_pr, ain, apr, last_stab_warp,
+                              occ_mask)]
+    _check(load().vsc_get_adap_comb_masked(*[C.byref(i) for i in ims], float(alpha), _stream(stream)))
     return ain, apr
 
 
@@ -276,6 +376,55 @@ def get_consist_out_noalloc(crnt_pr, prev_stab_warp, cons_wt, num_iter, step_siz
     return consis_out
 
 
+# ---- files ----------------------------------------------------------------------
+
+def read_image(path):
+    """RGBA8 numpy array of a PNG / PPM file."""
+    import numpy as np
+
+    w, h = C.c_int32(), C.c_int32()
+    _check(load().vsc_image_file_info(str(path).encode(), C.byref(w), C.byref(h)))
+    out = np.empty((h.value, w.value, 4), np.uint8)
+    _check(load().vsc_read_image_file(str(path).encode(), out.ctypes.data, w.value, h.value))
+    return out
+
+
+def write_png(path, rgba):
+    import numpy as np
+
+    a = np.ascontiguousarray(rgba, dtype=np.uint8)
+    _check(load().vsc_write_png(str(path).encode(), a.ctypes.data, a.shape[1], a.shape[0]))
+
+
+def read_flo(path):
+    import numpy as np
+
+    w, h = C.c_int32(), C.c_int32()
+    _check(load().vsc_flo_info(str(path).encode(), C.byref(w), C.byref(h)))
+    out = np.empty((h.value, w.value, 2), np.float32)
+    _check(load().vsc_read_flo(str(path).encode(), out.ctypes.data, w.value, h.value))
+    return out
+
+
+def write_flo(path, flow):
+    import numpy as np
+
+    a = np.ascontiguousarray(flow, dtype=np.float32)
+    _check(load().vsc_write_flo(str(path).encode(), a.ctypes.data, a.shape[1], a.shape[0]))
+
+
+def stabilize_files(original_dir, processed_dir, output_dir, flow_dir=None, width=0, height=0, flow_downscale=1,
+                    corr_dtype: str = "f32", hyper: "HyperParams | None" = None) -> int:
+    """Headless FileStabilizer: stabilizes a frame directory; returns the number of frames written."""
+    code = {"f32": VSC_DTYPE_F32, "bf16": VSC_DTYPE_BF16, "fp16": VSC_DTYPE_F16}[corr_dtype]
+    cfg = FilesConfig(str(original_dir).encode(), str(processed_dir).encode(), str(output_dir).encode(),
+                      str(flow_dir).encode() if flow_dir else None, width, height, flow_downscale, code,
+                      C.cast(C.pointer(hyper), C.c_void_p) if hyper is not None else None)
+    n = C.c_int32()
+    _check(load().vsc_stabilize_files(C.byref(cfg), C.byref(n)))
+    return n.value
+
+
 def default_hyper_params() -> HyperParams:
     hp = HyperParams()
     load().vsc_default_hyper_params(C.byref(hp))
@@ -299,13 +448,16 @@ class Stabilizer:
     """
 
     def __init__(self, width, height, compute_flow=True, flow_downscale=1, flow_channels=3, stream=None,
-                 use_graphs=True):
+                 use_graphs=True, corr_dtype: str = "f32"):
+        """corr_dtype: "f32" (the plain method), "bf16" or "fp16" (the flow
+        estimator's correlations on the tensor cores)."""
         import torch
 
         self.width, self.height = width, height
         self._stream_obj = stream if stream is not None else torch.cuda.current_stream()
+        code = {"f32": VSC_DTYPE_F32, "bf16": VSC_DTYPE_BF16, "fp16": VSC_DTYPE_F16, "f16": VSC_DTYPE_F16}[corr_dtype]
         cfg = StabilizerConfig(width, height, 1, 1 if compute_flow else 0, flow_downscale, flow_channels,
-                               1 if use_graphs else 0)
+                               1 if use_graphs else 0, code)
         h = C.c_void_p()
         _check(load().vsc_stabilizer_create(C.byref(cfg), _stream(self._stream_obj), C.byref(h)))
         self._h = h
@@ -351,6 +503,10 @@ class Stabilizer:
         return torch.as_tensor(view, device="cuda").clone()
 
     STAGES = ("load", "flow", "front", "coarse_solve", "full_solve")
+
+    def set_occlusion_mask(self, on: bool = True):
+        """Opt-in forward-backward flow consistency mask on the temporal weights."""
+        _check(load().vsc_stabilizer_set_occlusion_mask(self._h, 1 if on else 0))
 
     def enable_timing(self, on: bool = True):
         _check(load().vsc_stabilizer_enable_timing(self._h, 1 if on else 0))

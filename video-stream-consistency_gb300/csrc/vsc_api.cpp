@@ -163,6 +163,88 @@ VSC_API vsc_status vsc_warp_fwd(const float* input, const float* flow, float* ou
     return check_cuda(launch_warp_op(input, flow, out, (int)N, (int)C, (int)H, (int)W, cs(stream)), "warp launch");
 }
 
+VSC_API size_t vsc_correlation_lowp_workspace_size(int64_t N, int64_t C, int64_t H, int64_t W)
+{
+    if (!dims_ok(N) || !dims_ok(C) || !dims_ok(H) || !dims_ok(W))
+        return 0;
+    return corr_tc_workspace_bytes(static_cast<int>(N), static_cast<int>(C), static_cast<int>(H), static_cast<int>(W));
+}
+
+VSC_API vsc_status vsc_correlation_fwd_lowp(const float* f1, const float* f2, float* out, int64_t N, int64_t C,
+    int64_t H, int64_t W, int64_t max_displacement, int32_t dtype, void* workspace, size_t workspace_bytes,
+    vsc_stream_t stream)
+{
+    clear_error();
+    if (!f1 || !f2 || !out)
+        return set_error(VSC_EINVAL, "correlation_lowp: null pointer");
+    if (!dims_ok(N) || !dims_ok(C) || !dims_ok(H) || !dims_ok(W))
+        return set_error(VSC_EINVAL, "correlation_lowp: invalid shape %lldx%lldx%lldx%lld", (long long)N, (long long)C,
+            (long long)H, (long long)W);
+    if (dtype != VSC_DTYPE_BF16 && dtype != VSC_DTYPE_F16)
+        return set_error(VSC_EINVAL, "correlation_lowp: dtype must be VSC_DTYPE_BF16 or VSC_DTYPE_F16");
+    if (max_displacement < 0 || max_displacement > kTcMaxMd)
+        return set_error(VSC_EUNSUPPORTED, "correlation_lowp: max_displacement %lld outside [0, %d]",
+            (long long)max_displacement, kTcMaxMd);
+    if (tc_padded_channels(static_cast<int>(C)) > kTcMaxChannelsPadded)
+        return set_error(VSC_EUNSUPPORTED, "correlation_lowp: %lld channels, at most %d", (long long)C,
+            kTcMaxChannelsPadded);
+    if (N > 65535 || H > 65535 || H * W > (int64_t(1) << 31) / 4)
+        return set_error(VSC_EINVAL, "correlation_lowp: shape too large");
+    const size_t need = corr_tc_workspace_bytes((int)N, (int)C, (int)H, (int)W);
+    void* ws = workspace;
+    bool pooled = false;
+    vsc_status s;
+    if (ws) {
+        if (workspace_bytes < need)
+            return set_error(VSC_ENOMEM, "correlation_lowp: workspace of %zu bytes, need %zu", workspace_bytes, need);
+        if (reinterpret_cast<uintptr_t>(ws) & 255)
+            return set_error(VSC_EINVAL, "correlation_lowp: workspace not 256-byte aligned");
+    } else {
+        if ((s = check_cuda(pool_alloc(&ws, need, cs(stream)), "correlation_lowp workspace")))
+            return s;
+        pooled = true;
+    }
+    cudaError_t e = launch_corr_tc(f1, f2, out, (int)N, (int)C, (int)H, (int)W, (int)max_displacement,
+        dtype == VSC_DTYPE_BF16, ws, cs(stream));
+    if (pooled)
+        cudaFreeAsync(ws, cs(stream));
+    return check_cuda(e, "correlation_lowp launch");
+}
+
+VSC_API vsc_status vsc_correlation_fwd_f64(const double* f1, const double* f2, double* out, int64_t N, int64_t C,
+    int64_t H, int64_t W, int64_t max_displacement, vsc_stream_t stream)
+{
+    clear_error();
+    if (!f1 || !f2 || !out)
+        return set_error(VSC_EINVAL, "correlation_f64: null pointer");
+    if (!dims_ok(N) || !dims_ok(C) || !dims_ok(H) || !dims_ok(W))
+        return set_error(VSC_EINVAL, "correlation_f64: invalid shape %lldx%lldx%lldx%lld", (long long)N, (long long)C,
+            (long long)H, (long long)W);
+    if (max_displacement < 0 || max_displacement > 32)
+        return set_error(VSC_EINVAL, "correlation_f64: max_displacement %lld outside [0, 32]",
+            (long long)max_displacement);
+    if (N > 65535 || H * W > (int64_t(1) << 31))
+        return set_error(VSC_EINVAL, "correlation_f64: shape too large");
+    return check_cuda(launch_correlation_f64(f1, f2, out, (int)N, (int)C, (int)H, (int)W, (int)max_displacement,
+                          cs(stream)),
+        "correlation_f64 launch");
+}
+
+VSC_API vsc_status vsc_warp_fwd_f64(const double* input, const double* flow, double* out, int64_t N, int64_t C,
+    int64_t H, int64_t W, vsc_stream_t stream)
+{
+    clear_error();
+    if (!input || !flow || !out)
+        return set_error(VSC_EINVAL, "warp_f64: null pointer");
+    if (!dims_ok(N) || !dims_ok(C) || !dims_ok(H) || !dims_ok(W))
+        return set_error(VSC_EINVAL, "warp_f64: invalid shape %lldx%lldx%lldx%lld", (long long)N, (long long)C,
+            (long long)H, (long long)W);
+    if (N > 65535 || H * W > (int64_t(1) << 31))
+        return set_error(VSC_EINVAL, "warp_f64: shape too large");
+    return check_cuda(launch_warp_op_f64(input, flow, out, (int)N, (int)C, (int)H, (int)W, cs(stream)),
+        "warp_f64 launch");
+}
+
 // ---- stabilization kernels -------------------------------------------------
 
 VSC_API vsc_status vsc_char_to_float_image(const uint8_t* rgba, const vsc_image* out, vsc_stream_t stream)
@@ -203,12 +285,19 @@ VSC_API vsc_status vsc_get_warp_result(const vsc_image* input, const vsc_image* 
     return check_cuda(launch_stab_warp(img(input), img(flow), img(input_warp), cs(stream)), "warp_result launch");
 }
 
-VSC_API vsc_status vsc_get_adap_comb(const vsc_image* crnt_in, const vsc_image* crnt_pr, const vsc_image* prev_warp_in,
+namespace {
+vsc_status adap_comb_impl(const vsc_image* crnt_in, const vsc_image* crnt_pr, const vsc_image* prev_warp_in,
     const vsc_image* prev_warp_pr, const vsc_image* next_warp_in, const vsc_image* next_warp_pr,
-    const vsc_image* adap_cmb_in, const vsc_image* adap_cmb_pr, const vsc_image* last_stab_warp, float alpha,
-    vsc_stream_t stream)
+    const vsc_image* adap_cmb_in, const vsc_image* adap_cmb_pr, const vsc_image* last_stab_warp,
+    const vsc_image* occ_mask, float alpha, vsc_stream_t stream)
 {
     clear_error();
+    if (occ_mask) {
+        vsc_status s;
+        if ((s = check_image(occ_mask, "occMask", 2, 2)) || (s = check_image(crnt_in, "crntIn", 3, 3)) ||
+            (s = same_size(crnt_in, occ_mask, "occMask")))
+            return s;
+    }
     const vsc_image* all[9] = {crnt_in, crnt_pr, prev_warp_in, prev_warp_pr, next_warp_in, next_warp_pr, adap_cmb_in,
         adap_cmb_pr, last_stab_warp};
     static const char* names[9] = {"crntIn", "crntPr", "prevWarpIn", "prevWarpPr", "nextWarpIn", "nextWarpPr",
@@ -222,8 +311,47 @@ VSC_API vsc_status vsc_get_adap_comb(const vsc_image* crnt_in, const vsc_image* 
     }
     return check_cuda(launch_adap_comb(img(crnt_in), img(crnt_pr), img(prev_warp_in), img(prev_warp_pr),
                           img(next_warp_in), img(next_warp_pr), img(adap_cmb_in), img(adap_cmb_pr),
-                          img(last_stab_warp), alpha, cs(stream)),
+                          img(last_stab_warp), alpha, cs(stream), occ_mask ? occ_mask->data : nullptr),
         "adap_comb launch");
+}
+}  // namespace
+
+VSC_API vsc_status vsc_get_adap_comb(const vsc_image* crnt_in, const vsc_image* crnt_pr, const vsc_image* prev_warp_in,
+    const vsc_image* prev_warp_pr, const vsc_image* next_warp_in, const vsc_image* next_warp_pr,
+    const vsc_image* adap_cmb_in, const vsc_image* adap_cmb_pr, const vsc_image* last_stab_warp, float alpha,
+    vsc_stream_t stream)
+{
+    return adap_comb_impl(crnt_in, crnt_pr, prev_warp_in, prev_warp_pr, next_warp_in, next_warp_pr, adap_cmb_in,
+        adap_cmb_pr, last_stab_warp, nullptr, alpha, stream);
+}
+
+VSC_API vsc_status vsc_get_adap_comb_masked(const vsc_image* crnt_in, const vsc_image* crnt_pr,
+    const vsc_image* prev_warp_in, const vsc_image* prev_warp_pr, const vsc_image* next_warp_in,
+    const vsc_image* next_warp_pr, const vsc_image* adap_cmb_in, const vsc_image* adap_cmb_pr,
+    const vsc_image* last_stab_warp, const vsc_image* occ_mask, float alpha, vsc_stream_t stream)
+{
+    if (!occ_mask) {
+        clear_error();
+        return set_error(VSC_EINVAL, "adap_comb_masked: null occMask descriptor");
+    }
+    return adap_comb_impl(crnt_in, crnt_pr, prev_warp_in, prev_warp_pr, next_warp_in, next_warp_pr, adap_cmb_in,
+        adap_cmb_pr, last_stab_warp, occ_mask, alpha, stream);
+}
+
+VSC_API vsc_status vsc_get_flow_consistency_mask(const vsc_image* flow_fwd, const vsc_image* flow_bwd,
+    const vsc_image* occ_mask, vsc_stream_t stream)
+{
+    clear_error();
+    vsc_status s;
+    if ((s = check_image(flow_fwd, "flowFwd", 2, 3)) || (s = check_image(flow_bwd, "flowBwd", 2, 3)) ||
+        (s = check_image(occ_mask, "occMask", 2, 2)) || (s = same_size(flow_fwd, flow_bwd, "flowBwd")) ||
+        (s = same_size(flow_fwd, occ_mask, "occMask")))
+        return s;
+    if (flow_fwd->channels != flow_bwd->channels)
+        return set_error(VSC_EINVAL, "flow_consistency_mask: flows have %d and %d channels", flow_fwd->channels,
+            flow_bwd->channels);
+    return check_cuda(launch_flow_consistency(img(flow_fwd), img(flow_bwd), img(occ_mask), cs(stream)),
+        "flow_consistency_mask launch");
 }
 
 VSC_API vsc_status vsc_get_consist_wt(const vsc_image* adap_cmb_in, const vsc_image* crnt_in,
@@ -292,6 +420,8 @@ VSC_API vsc_status vsc_get_consist_out(const vsc_image* crnt_pr, const vsc_image
         cudaFreeAsync(ws, cs(stream));
     return check_cuda(e, "consist_out launch");
 }
+
+VSC_API int32_t vsc_solver_steps_per_launch(void) { return solver_steps_per_launch(); }
 
 VSC_API vsc_status vsc_check_device(void)
 {
@@ -391,8 +521,15 @@ struct vsc_stabilizer {
     float* solver_ws = nullptr;
     float* feat_scratch = nullptr;
     float* flow_scratch = nullptr;
+    // tensor-core correlations (corr_dtype BF16 / F16): chunked 16-bit
+    // features of the three frames, the warped operand, the operand scales
+    int corr_dtype = VSC_DTYPE_F32;
+    unsigned char* feat_tc[3] = {};
+    unsigned char* warped_tc = nullptr;
+    float* tc_scales = nullptr;
     FlowDims fd{};
     int last_launches = 0;
+    bool occlusion = false;  // opt-in forward-backward consistency mask
     // stage timing (off by default): events around load_frame and the stages of a step
     bool timing = false;
     cudaEvent_t ev[7] = {};
@@ -404,7 +541,7 @@ struct vsc_stabilizer {
         int head = 0, ls_cur = 0, nl = 0;
         uint8_t* rgba = nullptr;
         vsc_hyper_params hp{};
-        bool timing = false;
+        bool timing = false, occlusion = false;
         cudaGraphExec_t exec = nullptr;
         uint64_t used = 0;
     } graphs[8];
@@ -473,6 +610,9 @@ void free_all(vsc_stabilizer* s)
     f(s->solver_ws);
     f(s->feat_scratch);
     f(s->flow_scratch);
+    f(s->feat_tc[0]);
+    f(s->warped_tc);
+    f(s->tc_scales);
     for (cudaEvent_t& e : s->ev)
         if (e) {
             cudaEventDestroy(e);
@@ -539,6 +679,21 @@ vsc_status alloc_all(vsc_stabilizer* s)
         }
         A(dalloc(&s->feat_scratch, flow_feature_scratch_floats(s->fd)));
         A(dalloc(&s->flow_scratch, 2 * flow_estimate_scratch_floats(s->fd)));
+        if (s->corr_dtype != VSC_DTYPE_F32) {
+            const size_t fb = tc_frame_bytes(s->fd);
+            A(dalloc(&s->feat_tc[0], 3 * fb));
+            if (e == cudaSuccess) {
+                s->feat_tc[1] = s->feat_tc[0] + fb;
+                s->feat_tc[2] = s->feat_tc[1] + fb;
+            }
+            A(dalloc(&s->warped_tc, 2 * tc_warped_bytes(s->fd)));
+            A(dalloc(&s->tc_scales, 2));
+            // |feature| <= 1 (L2-normalised): 2^14 keeps FP16 below its
+            // maximum with every level's values in its normal range
+            const float sc[2] = {16384.0f, 16384.0f};
+            if (e == cudaSuccess)
+                A(cudaMemcpy(s->tc_scales, sc, sizeof(sc), cudaMemcpyHostToDevice));
+        }
         if (s->downscale > 1) {
             A(dalloc(&s->small, static_cast<size_t>(s->fw) * s->fh * 3));
             A(dalloc(&s->flow_small, 2 * static_cast<size_t>(s->fw) * s->fh * 3));
@@ -566,6 +721,8 @@ VSC_API vsc_status vsc_stabilizer_create(const vsc_stabilizer_config* cfg, vsc_s
         return set_error(VSC_EINVAL, "stabilizer_create: flow_downscale %d outside [1, 8]", cfg->flow_downscale);
     if (!cfg->compute_flow && cfg->flow_channels != 2 && cfg->flow_channels != 3)
         return set_error(VSC_EINVAL, "stabilizer_create: flow_channels must be 2 or 3");
+    if (cfg->corr_dtype != VSC_DTYPE_F32 && cfg->corr_dtype != VSC_DTYPE_BF16 && cfg->corr_dtype != VSC_DTYPE_F16)
+        return set_error(VSC_EINVAL, "stabilizer_create: corr_dtype %d unknown", cfg->corr_dtype);
     vsc_stabilizer* s = new (std::nothrow) vsc_stabilizer();
     if (!s)
         return set_error(VSC_ENOMEM, "stabilizer_create: out of host memory");
@@ -579,6 +736,7 @@ VSC_API vsc_status vsc_stabilizer_create(const vsc_stabilizer_config* cfg, vsc_s
     s->fh = static_cast<int>(std::lround(static_cast<float>(s->h) / static_cast<float>(s->downscale)));
     s->st = cs(stream);
     s->use_graphs = cfg->use_graphs != 0;
+    s->corr_dtype = cfg->corr_dtype;
     cudaGetDevice(&s->device);
     vsc_default_hyper_params(&s->hp);
     vsc_status st = alloc_all(s);
@@ -652,6 +810,11 @@ VSC_API vsc_status vsc_stabilizer_load_frame(vsc_stabilizer* s, const uint8_t* o
             "load_frame features");
         if (st)
             return st;
+        if (s->corr_dtype != VSC_DTYPE_F32 &&
+            (st = check_cuda(launch_flow_features_chunked(s->feat[slot], s->fd, s->feat_tc[slot], s->tc_scales,
+                                 s->corr_dtype == VSC_DTYPE_BF16, s->st, &nl),
+                 "load_frame features (16-bit)")))
+            return st;
     }
     mark(s, kEvLoad1);
     s->count += 1;
@@ -708,9 +871,19 @@ cudaError_t enqueue_step(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t*
     if (s->compute_flow) {
         const bool small = s->downscale > 1;
         const int64_t fs = static_cast<int64_t>(s->fw) * s->fh * 3;
+        FlowTc tc{};
+        if (s->corr_dtype != VSC_DTYPE_F32) {
+            tc.a[0] = s->feat_tc[s1];
+            tc.a[1] = s->feat_tc[s2];
+            tc.b[0] = s->feat_tc[s2];
+            tc.b[1] = s->feat_tc[s1];
+            tc.warped = s->warped_tc;
+            tc.scales = s->tc_scales;
+            tc.bf16 = s->corr_dtype == VSC_DTYPE_BF16;
+        }
         run(launch_flow_pair(s->feat[s1], s->feat[s2] - s->feat[s1], s->feat[s2], s->feat[s1] - s->feat[s2], s->fw,
             s->fh, s->fd, small ? s->flow_small : s->flow_fwd, small ? fs : s->flow_bwd - s->flow_fwd,
-            s->flow_scratch, st, &nl));
+            s->flow_scratch, st, &nl, s->corr_dtype != VSC_DTYPE_F32 ? &tc : nullptr));
         if (small) {
             // flowmodel.cpp:158-161: bilinear upsampling, vectors not rescaled
             run(launch_bilinear(Img{s->flow_small, s->fw, s->fh, 3}, Img{s->flow_fwd, s->w, s->h, 3}, st));
@@ -723,7 +896,8 @@ cudaError_t enqueue_step(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t*
     float* ls_in = s->last_stab[s->ls_cur];
     float* ls_out = s->last_stab[s->ls_cur ^ 1];
     run(launch_fused_front(s->orig[s0], s->orig[s1], s->orig[s2], s->proc[s0], s->proc[s1], s->proc[s2], ls_in,
-        s->flow_fwd, s->flow_bwd, s->fc, s->adap_pr, s->cons_wt, s->w, s->h, hp.alpha, hp.beta, hp.gamma, st));
+        s->flow_fwd, s->flow_bwd, s->fc, s->adap_pr, s->cons_wt, s->w, s->h, hp.alpha, hp.beta, hp.gamma, st,
+        s->occlusion));
     ++nl;
 
     // pyramid (videostabilizer.cpp:203-217)
@@ -775,7 +949,7 @@ bool launch_step_graph(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t* r
     auto* hit = static_cast<vsc_stabilizer::GraphEntry*>(nullptr);
     for (auto& g : s->graphs)
         if (g.valid && g.head == s->head && g.ls_cur == s->ls_cur && g.rgba == rgba_dev && g.timing == s->timing &&
-            same_hp(g.hp, hp))
+            g.occlusion == s->occlusion && same_hp(g.hp, hp))
             hit = &g;
     if (!hit) {
         auto* slot = &s->graphs[0];
@@ -813,6 +987,7 @@ bool launch_step_graph(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t* r
         slot->ls_cur = s->ls_cur;
         slot->rgba = rgba_dev;
         slot->timing = s->timing;
+        slot->occlusion = s->occlusion;
         slot->hp = hp;
         slot->nl = nl;
         hit = slot;
@@ -902,6 +1077,15 @@ VSC_API vsc_status vsc_stabilizer_buffer(vsc_stabilizer* s, int32_t which, const
 }
 
 VSC_API int32_t vsc_stabilizer_last_launches(vsc_stabilizer* s) { return s ? s->last_launches : 0; }
+
+VSC_API vsc_status vsc_stabilizer_set_occlusion_mask(vsc_stabilizer* s, int32_t on)
+{
+    clear_error();
+    if (!s)
+        return set_error(VSC_EINVAL, "set_occlusion_mask: null stabilizer");
+    s->occlusion = on != 0;
+    return VSC_OK;
+}
 
 VSC_API vsc_status vsc_stabilizer_enable_timing(vsc_stabilizer* s, int32_t on)
 {

@@ -444,8 +444,41 @@ size_t flow_estimate_scratch_floats(const FlowDims& d)
     return 9 * d.max_plane + maxcl + 81 * d.max_plane;
 }
 
+size_t tc_level_offset(const FlowDims& d, int level)
+{
+    size_t off = 0;
+    for (int l = 0; l < level; ++l)
+        off += (static_cast<size_t>(d.lw[l]) * d.lh[l] * tc_padded_channels(d.lc[l]) * 2 + 255) / 256 * 256;
+    return off;
+}
+
+size_t tc_frame_bytes(const FlowDims& d) { return tc_level_offset(d, kFlowLevels); }
+
+size_t tc_warped_bytes(const FlowDims& d)
+{
+    size_t m = 0;
+    for (int l = 0; l < kFlowLevels; ++l)
+        m = std::max(m, (static_cast<size_t>(d.lw[l]) * d.lh[l] * tc_padded_channels(d.lc[l]) * 2 + 255) / 256 * 256);
+    return m;
+}
+
+cudaError_t launch_flow_features_chunked(const float* feats, const FlowDims& d, void* chunked, const float* scale,
+    bool bf16, cudaStream_t st, int* launches)
+{
+    for (int l = 0; l < kFlowLevels; ++l) {
+        cudaError_t e = launch_to_chunked(feats + d.off[l], static_cast<unsigned char*>(chunked) + tc_level_offset(d, l),
+            scale, 1, d.lc[l], d.lh[l], d.lw[l], bf16, st);
+        if (e != cudaSuccess)
+            return e;
+    }
+    if (launches)
+        *launches += kFlowLevels;
+    return cudaSuccess;
+}
+
 cudaError_t launch_flow_pair(const float* featA, int64_t sA, const float* featB, int64_t sB, int w, int h,
-    const FlowDims& d, float* flow_out, int64_t s_out, float* scratch, cudaStream_t st, int* launches)
+    const FlowDims& d, float* flow_out, int64_t s_out, float* scratch, cudaStream_t st, int* launches,
+    const FlowTc* tc)
 {
     const dim3 b(32, 8);
     const int64_t bs = static_cast<int64_t>(flow_estimate_scratch_floats(d));  // per-direction scratch
@@ -473,18 +506,41 @@ cudaError_t launch_flow_pair(const float* featA, int64_t sA, const float* featB,
             g.z = 2;
             up2_kernel<<<g, b, 0, st>>>(sm[cur], d.lw[l + 1], d.lh[l + 1], up, lw, lh, bs);
             ++nl;
-            e = launch_warp_op(fb, up, warped, 2, lc, lh, lw, st, sB, bs, bs);
+            upp = up;
+            if (tc) {
+                e = launch_warp_to_chunked(fb, up, tc->warped, tc->scales, 2, lc, lh, lw, sB, bs,
+                    static_cast<int64_t>(tc_warped_bytes(d)), tc->bf16, st);
+            } else {
+                e = launch_warp_op(fb, up, warped, 2, lc, lh, lw, st, sB, bs, bs);
+                fb_use = warped;
+                sb_use = bs;
+            }
             if (e != cudaSuccess)
                 return e;
             ++nl;
-            upp = up;
-            fb_use = warped;
-            sb_use = bs;
         }
-        e = launch_correlation(fa, fb_use, cv, 2, lc, lh, lw, 4, 0, st, sA, sb_use, bs);
-        if (e != cudaSuccess)
-            return e;
-        ++nl;
+        if (tc) {
+            // the tensor-core correlation, one launch per direction (each
+            // direction's operands are separate tensors)
+            const size_t lo = tc_level_offset(d, l);
+            for (int dir = 0; dir < 2; ++dir) {
+                const void* ac = static_cast<const unsigned char*>(tc->a[dir]) + lo;
+                const void* bc = l < kFlowLevels - 1
+                                     ? static_cast<const void*>(static_cast<const unsigned char*>(tc->warped) +
+                                                                dir * tc_warped_bytes(d))
+                                     : static_cast<const void*>(static_cast<const unsigned char*>(tc->b[dir]) + lo);
+                e = launch_corr_tc_chunked(ac, bc, cv + dir * bs, tc->scales, 1, tc_padded_channels(lc), lh, lw, 4,
+                    tc->bf16, st);
+                if (e != cudaSuccess)
+                    return e;
+                ++nl;
+            }
+        } else {
+            e = launch_correlation(fa, fb_use, cv, 2, lc, lh, lw, 4, 0, st, sA, sb_use, bs);
+            if (e != cudaSuccess)
+                return e;
+            ++nl;
+        }
         decode_kernel<<<dim3(static_cast<unsigned>((plane + 255) / 256), 1, 2), 256, 0, st>>>(cv, raw, raw + 2 * plane,
             plane, kLevelPrior[l], bs);
         ++nl;

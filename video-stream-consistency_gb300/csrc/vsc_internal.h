@@ -25,6 +25,37 @@ cudaError_t launch_correlation(const float* f1, const float* f2, float* out, int
     int legacy, cudaStream_t st, int64_t s1 = -1, int64_t s2 = -1, int64_t so = -1);
 cudaError_t launch_warp_op(const float* in, const float* flow, float* out, int N, int C, int H, int W,
     cudaStream_t st, int64_t sin = -1, int64_t sfl = -1, int64_t sout = -1);
+// Double-precision ops (the DOUBLE branches of correlation.cc / warp.cc;
+// the CPU op has no legacy form).
+cudaError_t launch_correlation_f64(const double* f1, const double* f2, double* out, int N, int C, int H, int W, int md,
+    cudaStream_t st);
+cudaError_t launch_warp_op_f64(const double* in, const double* flow, double* out, int N, int C, int H, int W,
+    cudaStream_t st);
+
+// ---- tensor-core correlation (vsc_corr_tc.cu) --------------------------------
+// BF16 / FP16 operands on tcgen05 with FP32 accumulation, legacy = 0 layout.
+constexpr int kTcMaxMd = 8;                 // max_displacement limit of the tile
+constexpr int kTcMaxChannelsPadded = 208;   // channels, padded to a multiple of 16
+int tc_padded_channels(int C);
+size_t corr_tc_workspace_bytes(int N, int C, int H, int W);
+// From float NCHW (scaled per tensor, converted in the workspace).
+cudaError_t launch_corr_tc(const float* f1, const float* f2, float* out, int N, int C, int H, int W, int md,
+    bool bf16, void* workspace, cudaStream_t st);
+// From operands already in the chunked 16-bit layout [n][y][c / 8][x][c % 8]
+// (Cp channels) with their scales (2 floats: f1, f2) on the device.
+cudaError_t launch_corr_tc_chunked(const void* f1c, const void* f2c, float* out, const float* scales, int N, int Cp,
+    int H, int W, int md, bool bf16, cudaStream_t st);
+
+// float NCHW -> chunked 16-bit operand layout, multiplied by *scale.
+cudaError_t launch_to_chunked(const float* in, void* out, const float* scale, int N, int C, int H, int W, bool bf16,
+    cudaStream_t st);
+// custom::Warp (single precision) with the chunked 16-bit layout as output;
+// batch n reads in + n * sin, flow + n * sfl (floats), writes out + n * sout_bytes.
+cudaError_t launch_warp_to_chunked(const float* in, const float* flow, void* out, const float* scale, int N, int C,
+    int H, int W, int64_t sin, int64_t sfl, int64_t sout_bytes, bool bf16, cudaStream_t st);
+
+// Device address of the flag a kernel sets when one of its bounded waits gave up.
+cudaError_t device_timeout_flag(int** flag);
 
 // ---- stabilization (vsc_stab.cu) -------------------------------------------
 struct Img {
@@ -34,8 +65,13 @@ struct Img {
 cudaError_t launch_rgba_to_float(const uint8_t* rgba, float* out, int64_t npix, cudaStream_t st);
 cudaError_t launch_float_to_rgba(const float* in, uint8_t* rgba, int64_t npix, cudaStream_t st);
 cudaError_t launch_stab_warp(Img in, Img flow, Img out, cudaStream_t st);
+// occ_mask: optional HWC2 forward-backward consistency mask multiplied into
+// the previous/next frame weights after their clamps (nullptr: none).
 cudaError_t launch_adap_comb(Img ci, Img cp, Img pwi, Img pwp, Img nwi, Img nwp, Img ai, Img ap, Img lsw, float alpha,
-    cudaStream_t st);
+    cudaStream_t st, const float* occ_mask = nullptr);
+// Forward-backward flow consistency mask (HWC2 of 0/1: ch0 previous frame,
+// ch1 next frame); an opt-in extension with no counterpart in the reference.
+cudaError_t launch_flow_consistency(Img ffwd, Img fbwd, Img mask, cudaStream_t st);
 cudaError_t launch_consist_wt(Img ai, Img ci, Img wt, float beta, float gamma, cudaStream_t st);
 cudaError_t launch_bilinear(Img in, Img out, cudaStream_t st);
 // Nearest-neighbour resize of a float HWC3 image for the FLOWDOWNSCALE mode
@@ -46,6 +82,7 @@ cudaError_t launch_resize_nearest(const float* in, int iw, int ih, float* out, i
 // Solver.  The workspace holds the Laplacian of the processed image, two
 // momentum images and the second Jacobi buffer: 4 * w*h*3 floats.
 size_t solver_workspace_floats(int w, int h);
+int solver_steps_per_launch();  // Jacobi steps one solver launch performs (temporal blocking)
 // Runs num_iter iterations; O holds the initial solution and receives the
 // result.  Returns the number of kernels launched through *launches.
 cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,
@@ -69,7 +106,7 @@ cudaError_t run_solver_noalloc(const float* P, const float* A, const float* Wt, 
 // orchestrator: writes adapCmbPr and consWt only.
 cudaError_t launch_fused_front(const float* o0, const float* o1, const float* o2, const float* p0, const float* p1,
     const float* p2, const float* last_stab, const float* flow_fwd, const float* flow_bwd, int fc, float* adap_pr,
-    float* cons_wt, int w, int h, float alpha, float beta, float gamma, cudaStream_t st);
+    float* cons_wt, int w, int h, float alpha, float beta, float gamma, cudaStream_t st, bool occlusion_mask = false);
 // P, A, Wt of the next coarser pyramid level, one launch.
 cudaError_t launch_pyr_down3(const float* P, const float* A, const float* Wt, int iw, int ih, float* Pd, float* Ad,
     float* Wd, int ow, int oh, cudaStream_t st);
@@ -89,12 +126,29 @@ cudaError_t flow_upload_weights();
 size_t flow_feature_scratch_floats(const FlowDims& d);
 cudaError_t launch_flow_features(const float* img, int w, int h, const FlowDims& d, float* feats, float* scratch,
     cudaStream_t st, int* launches);
+// The tensor-core form of the estimator's correlations: each frame's
+// features also kept in the chunked 16-bit layout (level l at byte offset
+// tc_level_offset(d, l)), scaled by scales[0] (|f| <= 1 after the features'
+// L2 normalisation, so a fixed power of two serves every level).
+size_t tc_level_offset(const FlowDims& d, int level);
+size_t tc_frame_bytes(const FlowDims& d);
+size_t tc_warped_bytes(const FlowDims& d);  // one direction's warped operand at the largest level
+cudaError_t launch_flow_features_chunked(const float* feats, const FlowDims& d, void* chunked, const float* scale,
+    bool bf16, cudaStream_t st, int* launches);
+struct FlowTc {
+    const void* a[2];  // chunked features of the first frame of direction 0 / 1
+    const void* b[2];  // chunked features of the second frame (used at the coarsest level)
+    void* warped;      // 2 x tc_warped_bytes of scratch
+    const float* scales;
+    bool bf16;
+};
 // scratch for one flow direction: up/raw/smooth flows, warped features, cost volume
 size_t flow_estimate_scratch_floats(const FlowDims& d);
 // Two flows in the same launches (batch index z): direction n runs A_n =
 // featA + n*sA against B_n = featB + n*sB and writes flow_out + n*s_out
 // (w x h x 3).  scratch holds 2 * flow_estimate_scratch_floats(d).
 cudaError_t launch_flow_pair(const float* featA, int64_t sA, const float* featB, int64_t sB, int w, int h,
-    const FlowDims& d, float* flow_out, int64_t s_out, float* scratch, cudaStream_t st, int* launches);
+    const FlowDims& d, float* flow_out, int64_t s_out, float* scratch, cudaStream_t st, int* launches,
+    const FlowTc* tc = nullptr);
 
 }  // namespace vsc

@@ -8,7 +8,9 @@
 // 81-step shared-memory reduction.  Here a CTA owns a TH x 32 pixel tile and
 // all (2md+1)^2 displacements: channel chunks of f1 (tile) and f2 (tile plus
 // an md-pixel halo) are staged in shared memory straight from the NCHW
-// inputs (no temporaries), and every thread keeps 4 adjacent pixels x
+// inputs (no temporaries) by cp.async, double-buffered so the next channel
+// chunk streams in while the current one is consumed, and every thread keeps
+// 4 adjacent pixels x
 // (2md+1) horizontal displacements of one vertical displacement in
 // registers.  Per channel a thread reads 1 + ceil((4+2md)/4) 128-bit words
 // of shared memory for 4*(2md+1) multiply-adds.  Sums run in channel order
@@ -23,6 +25,8 @@
 // are computed once per pixel instead of once per (pixel, channel).
 #include "vsc_internal.h"
 #include "vsc_math.cuh"
+
+#include <mutex>
 
 namespace vsc {
 namespace {
@@ -41,22 +45,92 @@ struct CorrGeom {
     static constexpr int S2 = kCorrCC * RH * S2W;
 };
 
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Asynchronous global -> shared copies; when `valid` is false nothing is read
+// and the destination is zero-filled (src-size 0).
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_addr(dst)), "l"(src), "r"(valid ? 4 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16(float* dst, const float* src, bool valid)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst)), "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Stages one chunk of kCorrCC channels: the f1 tile and the f2 tile with its
+// md halo, zero outside the map.  vec: 16-byte copies (rows and tile origins
+// on the 16-byte grid, so a 4-float vector is entirely inside or outside).
+template <int MD>
+__device__ __forceinline__ void corr_stage(float* s1, float* s2, const float* a_n, const float* b_n, int c0, int cc,
+    int X0, int Y0, int H, int W, int64_t HW, int tid, int nthreads, bool vec)
+{
+    using G = CorrGeom<MD>;
+    if (vec) {
+        constexpr int V1 = kCorrCC * kCorrTH * (kCorrTW / 4);
+        for (int v = tid; v < V1; v += nthreads) {
+            const int c = v / (kCorrTH * (kCorrTW / 4)), rem = v % (kCorrTH * (kCorrTW / 4));
+            const int row = rem / (kCorrTW / 4), q = rem % (kCorrTW / 4);
+            const int gy = Y0 + row, gx = X0 + 4 * q;
+            const bool ok = c < cc && gy < H && gx < W;
+            const float* src = ok ? a_n + static_cast<int64_t>(c0 + c) * HW + static_cast<int64_t>(gy) * W + gx : a_n;
+            cp_async16(s1 + (c * kCorrTH + row) * kCorrTW + 4 * q, src, ok);
+        }
+        constexpr int Q2 = G::S2W / 4;
+        constexpr int V2 = kCorrCC * G::RH * Q2;
+        for (int v = tid; v < V2; v += nthreads) {
+            const int c = v / (G::RH * Q2), rem = v % (G::RH * Q2);
+            const int row = rem / Q2, q = rem % Q2;
+            const int gy = Y0 - MD + row, gx = X0 - MD + 4 * q;
+            const bool ok = c < cc && gy >= 0 && gy < H && gx >= 0 && gx < W && 4 * q < kCorrTW + 2 * MD;
+            const float* src = ok ? b_n + static_cast<int64_t>(c0 + c) * HW + static_cast<int64_t>(gy) * W + gx : b_n;
+            cp_async16(s2 + (c * G::RH + row) * G::S2W + 4 * q, src, ok);
+        }
+    } else {
+        constexpr int E1 = kCorrCC * kCorrTH * kCorrTW;
+        for (int v = tid; v < E1; v += nthreads) {
+            const int c = v / (kCorrTH * kCorrTW), rem = v % (kCorrTH * kCorrTW);
+            const int row = rem / kCorrTW, col = rem % kCorrTW;
+            const int gy = Y0 + row, gx = X0 + col;
+            const bool ok = c < cc && gy < H && gx < W;
+            const float* src = ok ? a_n + static_cast<int64_t>(c0 + c) * HW + static_cast<int64_t>(gy) * W + gx : a_n;
+            cp_async4(s1 + v, src, ok);
+        }
+        constexpr int E2 = kCorrCC * G::RH * G::S2W;
+        for (int v = tid; v < E2; v += nthreads) {
+            const int c = v / (G::RH * G::S2W), rem = v % (G::RH * G::S2W);
+            const int row = rem / G::S2W, col = rem % G::S2W;
+            const int gy = Y0 - MD + row, gx = X0 - MD + col;
+            const bool ok = c < cc && gy >= 0 && gy < H && gx >= 0 && gx < W && col < kCorrTW + 2 * MD;
+            const float* src = ok ? b_n + static_cast<int64_t>(c0 + c) * HW + static_cast<int64_t>(gy) * W + gx : b_n;
+            cp_async4(s2 + v, src, ok);
+        }
+    }
+}
+
 template <int MD>
 __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
     corr_tile_kernel(const float* __restrict__ in1, const float* __restrict__ in2, float* __restrict__ out, int C,
-        int H, int W, int legacy, int vec_store, int64_t sa, int64_t sb, int64_t so)
+        int H, int W, int legacy, int vec_store, int vec_load, int64_t sa, int64_t sb, int64_t so)
 {
     using G = CorrGeom<MD>;
     constexpr int P = G::P;
-    __shared__ __align__(16) float s1[G::S1];
-    __shared__ __align__(16) float s2[G::S2];
+    // two stages of (f1 tile, f2 tile): the next channel chunk streams in
+    // while the current one is consumed
+    extern __shared__ __align__(16) float corr_smem[];
 
     const int tx = threadIdx.x;  // x quad
     const int ty = threadIdx.y;  // row in tile
     const int tz = threadIdx.z;  // vertical displacement index
     const int tid = (tz * kCorrTH + ty) * 8 + tx;
     const int nthreads = 8 * kCorrTH * P;
-    const int lane = tid & 31, warp = tid >> 5, nwarps = (nthreads + 31) >> 5;
 
     const int n = blockIdx.z;
     const int X0 = blockIdx.x * kCorrTW;
@@ -72,32 +146,22 @@ __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
         for (int i = 0; i < 4; ++i)
             acc[j][i] = 0.0f;
 
+    int cur = 0;
+    corr_stage<MD>(corr_smem, corr_smem + G::S1, a_n, b_n, 0, min(kCorrCC, C), X0, Y0, H, W, HW, tid, nthreads,
+        vec_load != 0);
+    cp_async_commit();
     for (int c0 = 0; c0 < C; c0 += kCorrCC) {
         const int cc = min(kCorrCC, C - c0);
-        // stage f1 tile: cc x TH x TW
-        for (int r = warp; r < kCorrCC * kCorrTH; r += nwarps) {
-            const int c = r / kCorrTH, row = r % kCorrTH;
-            const int gy = Y0 + row, gx = X0 + lane;
-            float v = 0.0f;
-            if (c < cc && gy < H && gx < W)
-                v = __ldg(a_n + static_cast<int64_t>(c0 + c) * HW + static_cast<int64_t>(gy) * W + gx);
-            s1[(c * kCorrTH + row) * kCorrTW + lane] = v;
+        if (c0 + kCorrCC < C) {
+            float* nb = corr_smem + (cur ^ 1) * (G::S1 + G::S2);
+            corr_stage<MD>(nb, nb + G::S1, a_n, b_n, c0 + kCorrCC, min(kCorrCC, C - c0 - kCorrCC), X0, Y0, H, W, HW,
+                tid, nthreads, vec_load != 0);
         }
-        // stage f2 tile with halo: cc x (TH + 2md) x (TW + 2md), zero outside the map
-        for (int r = warp; r < kCorrCC * G::RH; r += nwarps) {
-            const int c = r / G::RH, row = r % G::RH;
-            const int gy = Y0 - MD + row;
-            const bool rowok = (c < cc) && gy >= 0 && gy < H;
-            const float* src = b_n + static_cast<int64_t>(c0 + c) * HW + static_cast<int64_t>(gy) * W;
-            for (int col = lane; col < G::S2W; col += 32) {
-                const int gx = X0 - MD + col;
-                float v = 0.0f;
-                if (rowok && col < kCorrTW + 2 * MD && gx >= 0 && gx < W)
-                    v = __ldg(src + gx);
-                s2[(c * G::RH + row) * G::S2W + col] = v;
-            }
-        }
+        cp_async_commit();
+        cp_async_wait_prev();  // the chunk of this iteration has landed
         __syncthreads();
+        const float* s1 = corr_smem + cur * (G::S1 + G::S2);
+        const float* s2 = s1 + G::S1;
         for (int c = 0; c < cc; ++c) {
             const float4 av = *reinterpret_cast<const float4*>(&s1[(c * kCorrTH + ty) * kCorrTW + 4 * tx]);
             const float a[4] = {av.x, av.y, av.z, av.w};
@@ -117,7 +181,8 @@ __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
                 for (int i = 0; i < 4; ++i)
                     acc[j][i] = acc[j][i] + a[i] * b[i + j];
         }
-        __syncthreads();
+        __syncthreads();  // the next iteration refills this stage
+        cur ^= 1;
     }
 
     const int y = Y0 + ty;
@@ -183,11 +248,34 @@ template <int MD>
 cudaError_t launch_corr_tile(const float* f1, const float* f2, float* out, int N, int C, int H, int W, int legacy,
     int64_t s1, int64_t s2, int64_t so, cudaStream_t st)
 {
+    using G = CorrGeom<MD>;
+    constexpr int smem = 2 * (G::S1 + G::S2) * static_cast<int>(sizeof(float));
+    // > 48 KB of dynamic shared memory: opt in once per device
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (dev < 0 || dev >= 64)
+            return cudaErrorInvalidDevice;
+        if (!done[dev]) {
+            if ((e = cudaFuncSetAttribute(corr_tile_kernel<MD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
+                cudaSuccess)
+                return e;
+            done[dev] = true;
+        }
+    }
+    auto a16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
     dim3 block(8, kCorrTH, 2 * MD + 1);
     dim3 grid((W + kCorrTW - 1) / kCorrTW, (H + kCorrTH - 1) / kCorrTH, N);
     // 128-bit stores need rows that start on 16 bytes: W % 4 == 0 and aligned outputs
-    const int vec = ((W & 3) == 0) && ((reinterpret_cast<uintptr_t>(out) & 15) == 0) && ((so & 3) == 0);
-    corr_tile_kernel<MD><<<grid, block, 0, st>>>(f1, f2, out, C, H, W, legacy, vec, s1, s2, so);
+    const int vec = ((W & 3) == 0) && a16(out) && ((so & 3) == 0);
+    // 128-bit loads additionally need the f2 halo origin X0 - md on the grid
+    const int vec_load = ((W & 3) == 0) && (MD % 4 == 0) && a16(f1) && a16(f2) && ((s1 & 3) == 0) && ((s2 & 3) == 0);
+    corr_tile_kernel<MD><<<grid, block, smem, st>>>(f1, f2, out, C, H, W, legacy, vec, vec_load, s1, s2, so);
     return cudaGetLastError();
 }
 
@@ -239,6 +327,78 @@ __global__ void warp_op_kernel(const float* __restrict__ in, const float* __rest
     }
 }
 
+// ---- double-precision ops (correlation.cc:115-139, warp.cc:48-58) ----------
+// The reference's CPU kernels also accept DOUBLE tensors.  These are the
+// same loops on the device: one thread per output element, the channel sum
+// in channel order, every product and sum rounded separately (the library is
+// built without contraction), so they equal correlation.cc / warp.cc's
+// double instantiations bit for bit.  Correctness paths, not hot paths.
+__global__ void corr_f64_kernel(const double* __restrict__ f1, const double* __restrict__ f2, double* __restrict__ out,
+    int C, int H, int W, int md)
+{
+    const int64_t HW = static_cast<int64_t>(H) * W;
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= HW)
+        return;
+    const int P = 2 * md + 1;
+    const int pp = blockIdx.y;
+    const int n = blockIdx.z;
+    const int h = static_cast<int>(i / W), w = static_cast<int>(i % W);
+    const int h2 = h + pp / P - md, w2 = w + pp % P - md;
+    const double* a = f1 + static_cast<int64_t>(n) * C * HW + i;
+    double acc = 0.0;
+    if (h2 >= 0 && h2 < H && w2 >= 0 && w2 < W) {
+        const double* b = f2 + static_cast<int64_t>(n) * C * HW + static_cast<int64_t>(h2) * W + w2;
+        for (int c = 0; c < C; ++c)
+            acc += a[c * HW] * b[c * HW];
+    }
+    out[(static_cast<int64_t>(n) * P * P + pp) * HW + i] = acc;
+}
+
+__global__ void warp_f64_kernel(const double* __restrict__ in, const double* __restrict__ flow,
+    double* __restrict__ out, int C, int H, int W)
+{
+    const int64_t HW = static_cast<int64_t>(H) * W;
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= HW)
+        return;
+    const int n = blockIdx.z;
+    const int y = static_cast<int>(i / W), x = static_cast<int>(i % W);
+    const double xf = static_cast<double>(x) + flow[static_cast<int64_t>(n) * 2 * HW + i];
+    const double yf = static_cast<double>(y) + flow[(static_cast<int64_t>(n) * 2 + 1) * HW + i];
+    const double alpha = xf - floor(xf);
+    const double beta = yf - floor(yf);
+    const double xL = floor(xf), xR = floor(xf) + 1.0;
+    const double yT = floor(yf), yB = floor(yf) + 1.0;
+    const bool mL = 0 <= xL && xL <= static_cast<double>(W - 1);
+    const bool mR = 0 <= xR && xR <= static_cast<double>(W - 1);
+    const bool mT = 0 <= yT && yT <= static_cast<double>(H - 1);
+    const bool mB = 0 <= yB && yB <= static_cast<double>(H - 1);
+    const bool tl = mT && mL, tr = mT && mR, bl = mB && mL, br = mB && mR;
+    double mask = 0.0;
+    mask += (1.0 - alpha) * (1.0 - beta) * (tl ? 1.0 : 0.0);
+    mask += (alpha) * (1.0 - beta) * (tr ? 1.0 : 0.0);
+    mask += (1.0 - alpha) * (beta) * (bl ? 1.0 : 0.0);
+    mask += (alpha) * (beta) * (br ? 1.0 : 0.0);
+    const bool keep = mask > 0.999;
+    // tap offsets only where the tap is inside the map
+    const int64_t oTL = tl ? static_cast<int64_t>(yT) * W + static_cast<int64_t>(xL) : 0;
+    const int64_t oTR = tr ? static_cast<int64_t>(yT) * W + static_cast<int64_t>(xR) : 0;
+    const int64_t oBL = bl ? static_cast<int64_t>(yB) * W + static_cast<int64_t>(xL) : 0;
+    const int64_t oBR = br ? static_cast<int64_t>(yB) * W + static_cast<int64_t>(xR) : 0;
+    for (int c = 0; c < C; ++c) {
+        const double* src = in + (static_cast<int64_t>(n) * C + c) * HW;
+        double val = 0.0;
+        if (keep) {
+            val += (1.0 - alpha) * (1.0 - beta) * (tl ? src[oTL] : 0.0);
+            val += (alpha) * (1.0 - beta) * (tr ? src[oTR] : 0.0);
+            val += (1.0 - alpha) * (beta) * (bl ? src[oBL] : 0.0);
+            val += (alpha) * (beta) * (br ? src[oBR] : 0.0);
+        }
+        out[(static_cast<int64_t>(n) * C + c) * HW + i] = val;
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_correlation(const float* f1, const float* f2, float* out, int N, int C, int H, int W, int md,
@@ -281,6 +441,25 @@ cudaError_t launch_warp_op(const float* in, const float* flow, float* out, int N
     }
     dim3 grid(static_cast<unsigned>((HW + 255) / 256), (C + kWarpCG - 1) / kWarpCG, N);
     warp_op_kernel<<<grid, 256, 0, st>>>(in, flow, out, C, H, W, sin, sfl, sout);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_correlation_f64(const double* f1, const double* f2, double* out, int N, int C, int H, int W, int md,
+    cudaStream_t st)
+{
+    const int64_t HW = static_cast<int64_t>(H) * W;
+    const int P = 2 * md + 1;
+    dim3 grid(static_cast<unsigned>((HW + 255) / 256), P * P, N);
+    corr_f64_kernel<<<grid, 256, 0, st>>>(f1, f2, out, C, H, W, md);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_warp_op_f64(const double* in, const double* flow, double* out, int N, int C, int H, int W,
+    cudaStream_t st)
+{
+    const int64_t HW = static_cast<int64_t>(H) * W;
+    dim3 grid(static_cast<unsigned>((HW + 255) / 256), 1, N);
+    warp_f64_kernel<<<grid, 256, 0, st>>>(in, flow, out, C, H, W);
     return cudaGetLastError();
 }
 

@@ -98,7 +98,12 @@ __device__ __forceinline__ float jacobi_px(float o, float& u, float a, float wt,
         lap += vd ? down : 0.0f;
         lap += vu ? up : 0.0f;
     }
-    lap -= cnt * o;
+    // with every neighbour valid cnt is 4 and 4 * o is exact (|o| < 2^125),
+    // so one fused multiply-add rounds as the reference's multiply, subtract
+    if (kAll)
+        lap = __fmaf_rn(-4.0f, o, lap);
+    else
+        lap -= cnt * o;
     const float tmp_1 = wt * (o - a);
     const float tmp_2 = lap - lp;
     const float sg = step * (tmp_2 - tmp_1);
@@ -113,14 +118,25 @@ struct TbState {
     float o[4][3], u[4][3], a[4][3], wt[4][3], lp[4][3];  // [pixel q = 2*row + col][channel]
 };
 
+// `ring` is the width of the ring around the rows written back (the rows
+// [ring, kTbEY - ring) are exact after the T iterations).  Iteration k only
+// has to be right on rows [ring - T + k + 1, kTbEY - ring + T - k - 1), one
+// row fewer on each side per iteration, so a warp (two rows) whose rows all
+// lie outside skips it: the rows it would have published are read only by
+// rows that are themselves outside the next iteration's range.
 template <bool kAll>
 __device__ __forceinline__ void tb_iterate(TbState& s, const bool (&vr)[4], const bool (&vl)[4],
-    const bool (&vd)[4], const bool (&vu)[4], const float (&cnt)[4], float* smem, int T, int k0, float step,
-    float mom, int px0, int py0)
+    const bool (&vd)[4], const bool (&vu)[4], const float (&cnt)[4], float* smem, int T, int ring, int k0,
+    float step, float mom, int px0, int py0)
 {
     for (int k = 0; k < T; ++k) {
         const int cur = k & 1;
         const bool mom_on = (k0 + k) > 0;
+        const int lo = ring - T + k + 1, hi = kTbEY - ring + T - k - 1;
+        if (py0 + 1 < lo || py0 >= hi) {  // warp-uniform: py0 = 2 * threadIdx.y
+            __syncthreads();
+            continue;
+        }
 #pragma unroll
         for (int ch = 0; ch < 3; ++ch) {
             const float* S = smem + (cur * 3 + ch) * kTbPlane;
@@ -205,9 +221,9 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
     // tiles whose every pixel has all four neighbours skip the validity selects
     const bool interior = ox >= 1 && oy >= 1 && ox + kTbEX - 1 <= w - 3 && oy + kTbEY - 1 <= h - 3;
     if (interior)
-        tb_iterate<true>(s, vr, vl, vd, vu, cnt, smem, T, k0, step, mom, px0, py0);
+        tb_iterate<true>(s, vr, vl, vd, vu, cnt, smem, T, T, k0, step, mom, px0, py0);
     else
-        tb_iterate<false>(s, vr, vl, vd, vu, cnt, smem, T, k0, step, mom, px0, py0);
+        tb_iterate<false>(s, vr, vl, vd, vu, cnt, smem, T, T, k0, step, mom, px0, py0);
 
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -395,9 +411,9 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
 
         const bool interior = ox >= 1 && oy >= 1 && ox + kTbEX - 1 <= w - 3 && oy + kTbEY - 1 <= h - 3;
         if (interior)
-            tb_iterate<true>(s, vr, vl, vd, vu, cnt, obuf, T, k0, step, mom, px0, py0);
+            tb_iterate<true>(s, vr, vl, vd, vu, cnt, obuf, T, kTbT, k0, step, mom, px0, py0);
         else
-            tb_iterate<false>(s, vr, vl, vd, vu, cnt, obuf, T, k0, step, mom, px0, py0);
+            tb_iterate<false>(s, vr, vl, vd, vu, cnt, obuf, T, kTbT, k0, step, mom, px0, py0);
 
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -505,6 +521,8 @@ bool aligned16p(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) ==
 
 size_t solver_workspace_floats(int w, int h) { return static_cast<size_t>(w) * h * 3 * 4; }
 
+int solver_steps_per_launch() { return kTbT; }
+
 cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,
     float step, float mom, float* workspace, cudaStream_t st, int* launches, uint8_t* rgba_out)
 {
@@ -610,6 +628,23 @@ cudaError_t run_solver_noalloc(const float* P, const float* A, const float* Wt, 
     // Every workspace element (lap P, both momentum images, the second Jacobi
     // buffer) is written before it is read, so nothing is cleared.
     return run_solver(P, A, Wt, O, w, h, num_iter, step, mom, ws, st, nullptr, nullptr);
+}
+
+cudaError_t device_timeout_flag(int** flag)
+{
+    static std::mutex mu;
+    static int* addr[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    if (dev < 0 || dev >= 64)
+        return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev] && (e = cudaGetSymbolAddress(reinterpret_cast<void**>(&addr[dev]), g_device_timeout)) != cudaSuccess)
+        return e;
+    *flag = addr[dev];
+    return cudaSuccess;
 }
 
 cudaError_t check_device_timeout(int* flagged)

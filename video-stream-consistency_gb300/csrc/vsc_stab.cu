@@ -131,8 +131,10 @@ struct Comb {
     float ain, apr;
 };
 
+// mp, mn: the opt-in occlusion mask's factors for the previous and the next
+// frame's weight, applied after the clamps (1, 1 = kernel_adap_comb's bits).
 __device__ __forceinline__ Comb adap_comb_px(float ci, float cp, float pi, float pp, float ni, float np, float ls,
-    float alpha)
+    float alpha, float mp = 1.0f, float mn = 1.0f, bool masked = false)
 {
     float wt_prv = expf_cw(-alpha * (ci - pi) * (ci - pi));
     float wt_nxt = expf_cw(-alpha * (ci - ni) * (ci - ni));
@@ -144,6 +146,10 @@ __device__ __forceinline__ Comb adap_comb_px(float ci, float cp, float pi, float
         wt_prv = 0.0f;
     if (wt_nxt < 0.001f)
         wt_nxt = 0.0f;
+    if (masked) {
+        wt_prv = wt_prv * mp;
+        wt_nxt = wt_nxt * mn;
+    }
     Comb r;
     r.ain = wt_prv * pi + wt_nxt * ni + (1.0f - (wt_prv + wt_nxt)) * ci;
     float apr = wt_prv * pp + wt_nxt * np + (1.0f - (wt_prv + wt_nxt)) * cp;
@@ -162,14 +168,70 @@ __device__ __forceinline__ float consist_wt_px(float c, float a, float beta, flo
 __global__ void adap_comb_kernel(const float* __restrict__ ci, const float* __restrict__ cp,
     const float* __restrict__ pwi, const float* __restrict__ pwp, const float* __restrict__ nwi,
     const float* __restrict__ nwp, float* __restrict__ ai, float* __restrict__ ap, const float* __restrict__ lsw,
-    float alpha, int64_t n)
+    const float* __restrict__ occ, float alpha, int64_t n)
 {
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (i >= n)
         return;
-    const Comb r = adap_comb_px(ci[i], cp[i], pwi[i], pwp[i], nwi[i], nwp[i], lsw[i], alpha);
+    Comb r;
+    if (occ)
+        r = adap_comb_px(ci[i], cp[i], pwi[i], pwp[i], nwi[i], nwp[i], lsw[i], alpha, occ[(i / 3) * 2],
+            occ[(i / 3) * 2 + 1], true);
+    else
+        r = adap_comb_px(ci[i], cp[i], pwi[i], pwp[i], nwi[i], nwp[i], lsw[i], alpha);
     ai[i] = r.ain;
     ap[i] = r.apr;
+}
+
+// ---- forward-backward flow consistency (opt-in; no counterpart in the reference)
+// Flow a at (x, y) carries the pixel to p = (x + a.x, y + a.y); the opposite
+// flow b is sampled there bilinearly (right/bottom taps clamped) and the
+// pixel is consistent if |a + b(p)|^2 <= 0.01 (|a|^2 + |b(p)|^2) + 0.5.
+// Outside the frame, or NaN: inconsistent.  Operation order as the CPU
+// restatement's, so the 0/1 decisions agree bit for bit.
+__device__ __forceinline__ float occl_check(const float* __restrict__ a, const float* __restrict__ b, int fc, int x,
+    int y, int w, int h)
+{
+    const int64_t i = pix_index(x, y, w) * fc;
+    const float ax = a[i], ay = a[i + 1];
+    const float px = static_cast<float>(x) + ax;
+    const float py = static_cast<float>(y) + ay;
+    if (!(px >= 0.0f && px <= static_cast<float>(w - 1) && py >= 0.0f && py <= static_cast<float>(h - 1)))
+        return 0.0f;
+    const int ix = static_cast<int>(floorf(px));
+    const int iy = static_cast<int>(floorf(py));
+    const float fx = px - static_cast<float>(ix);
+    const float fy = py - static_cast<float>(iy);
+    const int ix1 = min(ix + 1, w - 1);
+    const int iy1 = min(iy + 1, h - 1);
+    float bv[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const float b00 = b[pix_index(ix, iy, w) * fc + k];
+        const float b10 = b[pix_index(ix1, iy, w) * fc + k];
+        const float b01 = b[pix_index(ix, iy1, w) * fc + k];
+        const float b11 = b[pix_index(ix1, iy1, w) * fc + k];
+        const float t0 = b00 * (1.0f - fx) + b10 * fx;
+        const float t1 = b01 * (1.0f - fx) + b11 * fx;
+        bv[k] = t0 * (1.0f - fy) + t1 * fy;
+    }
+    const float dx = ax + bv[0];
+    const float dy = ay + bv[1];
+    const float lhs = dx * dx + dy * dy;
+    const float rhs = 0.01f * ((ax * ax + ay * ay) + (bv[0] * bv[0] + bv[1] * bv[1])) + 0.5f;
+    return lhs <= rhs ? 1.0f : 0.0f;
+}
+
+__global__ void flow_consistency_kernel(const float* __restrict__ ffwd, const float* __restrict__ fbwd, int fc,
+    float* __restrict__ mask, int w, int h)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h)
+        return;
+    const int64_t o = pix_index(x, y, w) * 2;
+    mask[o] = occl_check(fbwd, ffwd, fc, x, y, w, h);
+    mask[o + 1] = occl_check(ffwd, fbwd, fc, x, y, w, h);
 }
 
 __global__ void consist_wt_kernel(const float* __restrict__ ci, const float* __restrict__ ai, float* __restrict__ wt,
@@ -228,6 +290,8 @@ __global__ void pyr_down3_kernel(const float* __restrict__ P, const float* __res
 }
 
 // ---- fused front end of doOneStep (videostabilizer.cpp:182-198) --------------
+// kOcc: the opt-in forward-backward consistency mask, evaluated in place.
+template <bool kOcc>
 __global__ void fused_front_kernel(const float* __restrict__ o0, const float* __restrict__ o1,
     const float* __restrict__ o2, const float* __restrict__ p0, const float* __restrict__ p1,
     const float* __restrict__ p2, const float* __restrict__ ls, const float* __restrict__ ffwd,
@@ -240,6 +304,11 @@ __global__ void fused_front_kernel(const float* __restrict__ o0, const float* __
         return;
     const WarpTap tb = warp_tap(fbwd, fc, x, y, w, h);
     const WarpTap tf = warp_tap(ffwd, fc, x, y, w, h);
+    float mp = 1.0f, mn = 1.0f;
+    if (kOcc) {
+        mp = occl_check(fbwd, ffwd, fc, x, y, w, h);
+        mn = occl_check(ffwd, fbwd, fc, x, y, w, h);
+    }
     const int64_t o = pix_index(x, y, w) * 3;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -249,7 +318,7 @@ __global__ void fused_front_kernel(const float* __restrict__ o0, const float* __
         const float nwp = warp_sample(p2, tf, c);
         const float lsw = warp_sample(ls, tb, c);
         const float ci = o1[o + c];
-        const Comb r = adap_comb_px(ci, p1[o + c], pwi, pwp, nwi, nwp, lsw, alpha);
+        const Comb r = adap_comb_px(ci, p1[o + c], pwi, pwp, nwi, nwp, lsw, alpha, mp, mn, kOcc);
         adap_pr[o + c] = r.apr;
         cons_wt[o + c] = consist_wt_px(ci, r.ain, beta, gamma);
     }
@@ -313,11 +382,19 @@ cudaError_t launch_stab_warp(Img in, Img flow, Img out, cudaStream_t st)
 }
 
 cudaError_t launch_adap_comb(Img ci, Img cp, Img pwi, Img pwp, Img nwi, Img nwp, Img ai, Img ap, Img lsw, float alpha,
-    cudaStream_t st)
+    cudaStream_t st, const float* occ_mask)
 {
     const int64_t n = static_cast<int64_t>(ci.w) * ci.h * 3;
     adap_comb_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(
-        ci.d, cp.d, pwi.d, pwp.d, nwi.d, nwp.d, ai.d, ap.d, lsw.d, alpha, n);
+        ci.d, cp.d, pwi.d, pwp.d, nwi.d, nwp.d, ai.d, ap.d, lsw.d, occ_mask, alpha, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flow_consistency(Img ffwd, Img fbwd, Img mask, cudaStream_t st)
+{
+    const dim3 b(32, 8);
+    flow_consistency_kernel<<<grid2d(mask.w, mask.h, b), b, 0, st>>>(
+        ffwd.d, fbwd.d, ffwd.c, mask.d, mask.w, mask.h);
     return cudaGetLastError();
 }
 
@@ -345,11 +422,15 @@ cudaError_t launch_pyr_down3(const float* P, const float* A, const float* Wt, in
 
 cudaError_t launch_fused_front(const float* o0, const float* o1, const float* o2, const float* p0, const float* p1,
     const float* p2, const float* last_stab, const float* flow_fwd, const float* flow_bwd, int fc, float* adap_pr,
-    float* cons_wt, int w, int h, float alpha, float beta, float gamma, cudaStream_t st)
+    float* cons_wt, int w, int h, float alpha, float beta, float gamma, cudaStream_t st, bool occlusion_mask)
 {
     const dim3 b(32, 8);
-    fused_front_kernel<<<grid2d(w, h, b), b, 0, st>>>(
-        o0, o1, o2, p0, p1, p2, last_stab, flow_fwd, flow_bwd, fc, adap_pr, cons_wt, w, h, alpha, beta, gamma);
+    if (occlusion_mask)
+        fused_front_kernel<true><<<grid2d(w, h, b), b, 0, st>>>(
+            o0, o1, o2, p0, p1, p2, last_stab, flow_fwd, flow_bwd, fc, adap_pr, cons_wt, w, h, alpha, beta, gamma);
+    else
+        fused_front_kernel<false><<<grid2d(w, h, b), b, 0, st>>>(
+            o0, o1, o2, p0, p1, p2, last_stab, flow_fwd, flow_bwd, fc, adap_pr, cons_wt, w, h, alpha, beta, gamma);
     return cudaGetLastError();
 }
 
