@@ -418,6 +418,53 @@ def solver_roofline(vsc, dev, stream, iters: int = 144):
             "launch_ms": per_launch_ms, "ms_per_jacobi_step": step_ms, "peak_source": peak_src}
 
 
+PWC_LEVELS_1080P = [(480, 272, 32), (240, 136, 64), (120, 68, 96), (60, 34, 128), (30, 17, 196)]
+
+
+def run_corr_only(args):
+    """--kernel corr: the Correlation op over the five PWC levels of a
+    1920x1088 frame (one direction), FP32 CUDA-core kernel against the BF16 /
+    FP16 tensor-core one (the latter including its per-level scaling and
+    16-bit conversion launches); CUDA events on the launching stream.
+    Algorithmic bytes of the FP32 contract: 4 (2 C H W + 81 H W)."""
+    import torch
+
+    vsc = import_pkg()
+    vsc.build()
+    vsc.load()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    g = torch.Generator(device=dev).manual_seed(3)
+    peak, peak_src = peaks()
+    res = {}
+    for lw, lh, lc in PWC_LEVELS_1080P:
+        f1 = torch.randn((1, lc, lh, lw), device=dev, generator=g)
+        f2 = torch.randn((1, lc, lh, lw), device=dev, generator=g)
+        out = torch.empty((1, 9, 9, lh, lw), device=dev)
+        ws = torch.empty(vsc.load().vsc_correlation_lowp_workspace_size(1, lc, lh, lw), dtype=torch.uint8,
+                         device=dev)
+        calls = {"f32": lambda: vsc.correlation(f1, f2, 4, out=out, stream=stream),
+                 "bf16": lambda: vsc.correlation_lowp(f1, f2, 4, "bf16", out=out, workspace=ws, stream=stream),
+                 "fp16": lambda: vsc.correlation_lowp(f1, f2, 4, "fp16", out=out, workspace=ws, stream=stream)}
+        alg = 4 * (2 * lc * lh * lw + 81 * lh * lw)
+        lev = {"shape": [lc, lh, lw], "algorithmic_bytes": alg}
+        for name, fn in calls.items():
+            for _ in range(max(args.warmup, 3)):
+                fn()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                fn()
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            lev[name] = {"ms": ms, "gbs": alg / (ms / 1000) / 1e9}
+        res[f"{lw}x{lh}"] = lev
+    tot = {k: sum(v[k]["ms"] for v in res.values()) for k in ("f32", "bf16", "fp16")}
+    print(json.dumps({"kernel": "correlation, PWC pyramid of one 1920x1088 direction", "levels": res,
+                      "total_ms": tot, "peak_gbs": peak, "peak_source": peak_src}))
+
+
 def run_solver_only(args):
     """--kernel solver: only the 1920x1080 solver (for profiler captures)."""
     import torch
@@ -640,8 +687,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--form", choices=sorted(FORMS), default="bf16",
                     help="the chosen form reported as value (the plain path is timed beside it)")
-    ap.add_argument("--kernel", choices=["step", "solver"], default="step",
-                    help="solver: time only the 1920x1080 solver (profiler target)")
+    ap.add_argument("--kernel", choices=["step", "solver", "corr"], default="step",
+                    help="solver / corr: time only the 1920x1080 solver or the correlation pyramid "
+                         "(profiler targets)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -649,6 +697,8 @@ def main():
         run_reference(args)
     elif args.kernel == "solver":
         run_solver_only(args)
+    elif args.kernel == "corr":
+        run_corr_only(args)
     else:
         run_gpu(args)
 

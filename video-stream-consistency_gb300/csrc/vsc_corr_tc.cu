@@ -39,168 +39,268 @@ constexpr int kTcM = 128;        // pixels per tile (MMA M, TMEM lanes)
 constexpr int kTcN = 144;        // f2 window per displacement row (MMA N)
 constexpr int kTcCols = 48;      // TMEM columns one warp reads per row: 32 + 2 md
 constexpr int kTcPitch = 52;     // staging row pitch (floats): 53 * lane spreads the diagonal over all banks
-constexpr int kTcThreads = 128;  // 4 warps, one per 32 TMEM lanes
-constexpr uint32_t kTmemCols = 256;
+constexpr int kTcWarps = 6;      // 0: TMA producer, 1: MMA issuer + TMEM owner, 2..5: epilogue
+constexpr int kTcThreads = kTcWarps * 32;
+constexpr int kMaxStagesA = 2, kMaxStagesB = 4, kStagesD = 3;
+constexpr uint32_t kTmemCols = 512;    // three accumulators
+constexpr uint32_t kDStride = 160;     // TMEM columns between accumulators (>= kTcN, multiple of 32)
 constexpr int kTcWaitSpins = 1 << 22;  // bounded mbarrier waits (about a second)
 constexpr int kTcStageBytes = 4 * 32 * kTcPitch * 4;
-// At least this much dynamic shared memory per CTA, so that at most two CTAs
-// share an SM and their Tensor Memory (2 x 256 of 512 columns) never waits.
-constexpr int kTcMinSmem = 100 * 1024;
+constexpr int kTcBarBytes = 256;
+constexpr int kTcSmemLimit = 232448;   // dynamic shared memory per CTA on sm_103
+// at least this much dynamic shared memory, so that one CTA (and one
+// 512-column Tensor Memory allocation) occupies an SM
+constexpr int kTcMinSmem = 120 * 1024;
 static_assert(kTcN >= kTcM + 2 * kTcMaxMd && kTcN % 16 == 0 && kTcN <= 256, "MMA N");
 static_assert(32 * 3 + kTcCols <= kTcN, "epilogue columns inside the accumulator");
 static_assert(kTcCols >= 32 + 2 * kTcMaxMd, "epilogue columns cover the band");
+static_assert((kStagesD - 1) * kDStride + kTcN <= kTmemCols, "accumulators inside the allocation");
 
 __host__ __device__ constexpr uint32_t align1k(uint32_t v) { return (v + 1023u) & ~1023u; }
 
-__host__ __device__ constexpr uint32_t tc_smem_bytes(int cp)
+struct TcPlan {
+    int stages_a, stages_b;
+    uint32_t smem;
+};
+
+// Operand buffers that fit in shared memory for Cp channels: two A tiles and
+// four B rows when they fit, down to one A tile and two B rows (208 channels).
+__host__ TcPlan tc_plan(int cp)
 {
-    return 1024 + align1k(kTcM * cp * 2) + 2 * align1k(kTcN * cp * 2) + kTcStageBytes + 64;
+    const uint32_t a = align1k(kTcM * cp * 2), b = align1k(kTcN * cp * 2);
+    const uint32_t fixed = 1024 + kTcStageBytes + kTcBarBytes;
+    TcPlan p{2, 4, 0};
+    while (fixed + p.stages_a * a + p.stages_b * b > static_cast<uint32_t>(kTcSmemLimit)) {
+        if (p.stages_b > 2)
+            --p.stages_b;
+        else if (p.stages_a > 1)
+            --p.stages_a;
+        else
+            break;
+    }
+    p.smem = std::max<uint32_t>(fixed + p.stages_a * a + p.stages_b * b, kTcMinSmem);
+    return p;
 }
 
+struct TcShared {
+    unsigned char* a[kMaxStagesA];
+    unsigned char* b[kMaxStagesB];
+    float* stage;
+    uint64_t *full_a, *empty_a, *full_b, *empty_b, *full_d, *empty_d;
+    uint32_t* tmem_slot;
+    volatile int* abort;
+};
+
+// Bounded wait that also gives up when another role has aborted; a wait that
+// runs out raises the abort for everyone.
+__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, volatile int* abort)
+{
+    for (int i = 0; i < kTcWaitSpins; ++i) {
+        if (ptx::mbar_try_wait(bar, parity))
+            return true;
+        if ((i & 63) == 63 && *abort)
+            return false;
+        if (i > 32)
+            __nanosleep(128);
+    }
+    *abort = 1;
+    return false;
+}
+
+// Persistent, warp-specialised: work item = (batch n, row y, 128-pixel
+// segment); every CTA walks items blockIdx.x, +gridDim.x, ...  Rings:
+// A tiles (producer -> MMA, freed by the MMA's commit after the item's last
+// row), B rows (freed by the commit of the MMA that read them), accumulators
+// in Tensor Memory (MMA -> epilogue, freed by the four epilogue warps as soon
+// as their columns are in registers, before the shared-memory and global
+// part of the epilogue).
 __global__ void __launch_bounds__(kTcThreads, 1)
     corr_tc_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB,
-        float* __restrict__ out, const float* __restrict__ scales, int H, int W, int Cp, int md, uint32_t idesc,
-        int* __restrict__ timeout_flag)
+        float* __restrict__ out, const float* __restrict__ scales, int N, int H, int W, int Cp, int md,
+        uint32_t idesc, int stages_a, int stages_b, int* __restrict__ timeout_flag)
 {
     extern __shared__ unsigned char smem_raw[];
-    unsigned char* sA = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
-                                                         ~static_cast<uintptr_t>(1023));
     const uint32_t bytesA = kTcM * Cp * 2;
     const uint32_t bytesB = kTcN * Cp * 2;
-    unsigned char* sB[2];
-    sB[0] = sA + align1k(bytesA);
-    sB[1] = sB[0] + align1k(bytesB);
-    float* stage = reinterpret_cast<float*>(sB[1] + align1k(bytesB));
-    uint64_t* bars = reinterpret_cast<uint64_t*>(stage + 4 * 32 * kTcPitch);  // A, B0, B1, MMA
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 4);
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int x0 = blockIdx.x * kTcM, y = blockIdx.y, n = blockIdx.z;
+    TcShared sh;
+    {
+        unsigned char* p = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                            ~static_cast<uintptr_t>(1023));
+        for (int i = 0; i < stages_a; ++i, p += align1k(bytesA))
+            sh.a[i] = p;
+        for (int i = 0; i < stages_b; ++i, p += align1k(bytesB))
+            sh.b[i] = p;
+        sh.stage = reinterpret_cast<float*>(p);
+        uint64_t* bars = reinterpret_cast<uint64_t*>(p + kTcStageBytes);
+        sh.full_a = bars;
+        sh.empty_a = bars + 2;
+        sh.full_b = bars + 4;
+        sh.empty_b = bars + 8;
+        sh.full_d = bars + 12;
+        sh.empty_d = bars + 15;
+        sh.tmem_slot = reinterpret_cast<uint32_t*>(bars + 18);
+        sh.abort = reinterpret_cast<volatile int*>(bars + 19);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int P = 2 * md + 1;
+    const int nseg = (W + kTcM - 1) / kTcM;
+    const int items = N * H * nseg;
 
-    if (warp == 0) {
-        ptx::tmem_alloc(tmem_slot, kTmemCols);
+    if (warp == 1) {
+        ptx::tmem_alloc(sh.tmem_slot, kTmemCols);
         ptx::tmem_relinquish();
     }
-    if (tid == 0) {
-        *abort_flag = 0;
-        for (int i = 0; i < 4; ++i)
-            ptx::mbar_init(&bars[i], 1);
+    if (threadIdx.x == 0) {
+        *sh.abort = 0;
+        for (int i = 0; i < 2; ++i) {
+            ptx::mbar_init(&sh.full_a[i], 1);
+            ptx::mbar_init(&sh.empty_a[i], 1);
+        }
+        for (int i = 0; i < 4; ++i) {
+            ptx::mbar_init(&sh.full_b[i], 1);
+            ptx::mbar_init(&sh.empty_b[i], 1);
+        }
+        for (int i = 0; i < kStagesD; ++i) {
+            ptx::mbar_init(&sh.full_d[i], 1);
+            ptx::mbar_init(&sh.empty_d[i], 4);  // one arrival per epilogue warp
+        }
     }
     ptx::tc_fence_before();
     __syncthreads();
     ptx::tc_fence_after();
-    const uint32_t tmem = *tmem_slot;
+    const uint32_t tmem = *sh.tmem_slot;
 
-    // thread 0 owns the pipeline: loads in flight per B buffer and phase parities
-    bool a_pending = false;
-    bool b_pending[2] = {false, false};
-    uint32_t b_par[2] = {0, 0};
-    bool mma_pending = false;
-    uint32_t mma_par = 0;
-    if (tid == 0) {
-        ptx::mbar_expect_tx(&bars[0], bytesA);
-        ptx::tma_load_5d(sA, &mA, 0, x0, 0, y, n, &bars[0]);
-        a_pending = true;
-        for (int d = 0; d < 2 && d < P; ++d) {
-            ptx::mbar_expect_tx(&bars[1 + d], bytesB);
-            ptx::tma_load_5d(sB[d], &mB, 0, x0 - md, 0, y + d - md, n, &bars[1 + d]);
-            b_pending[d] = true;
-        }
-    }
-    const float inv_scale = 1.0f / (scales[0] * scales[1]);  // powers of two: exact
-    float* st = stage + warp * 32 * kTcPitch;
-    const int64_t HW = static_cast<int64_t>(H) * W;
-    const int x = x0 + warp * 32 + lane;
-    float* obase = out + static_cast<int64_t>(n) * P * P * HW + static_cast<int64_t>(y) * W + x;
-    const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
-
-    for (int d = 0; d < P; ++d) {
-        const int buf = d & 1;
-        if (tid == 0) {
+    if (warp == 0) {
+        // ---- TMA producer ------------------------------------------------------
+        if (lane == 0) {
+            int ua = 0, ub = 0;
             bool ok = true;
-            if (a_pending) {
-                ok = ptx::mbar_wait_bounded(&bars[0], 0, kTcWaitSpins);
-                a_pending = !ok;
-            }
-            if (ok) {
-                ok = ptx::mbar_wait_bounded(&bars[1 + buf], b_par[buf], kTcWaitSpins);
-                if (ok) {
-                    b_pending[buf] = false;
-                    b_par[buf] ^= 1u;
+            for (int it = blockIdx.x; ok && it < items; it += gridDim.x) {
+                const int y = it % H, seg = (it / H) % nseg, n = it / (H * nseg);
+                const int x0 = seg * kTcM;
+                const int sa = ua % stages_a;
+                if (!(ok = tc_wait(&sh.empty_a[sa], ((ua / stages_a) & 1) ^ 1, sh.abort)))
+                    break;
+                ptx::mbar_expect_tx(&sh.full_a[sa], bytesA);
+                ptx::tma_load_5d(sh.a[sa], &mA, 0, x0, 0, y, n, &sh.full_a[sa]);
+                ++ua;
+                for (int d = 0; d < P; ++d) {
+                    const int sb = ub % stages_b;
+                    if (!(ok = tc_wait(&sh.empty_b[sb], ((ub / stages_b) & 1) ^ 1, sh.abort)))
+                        break;
+                    ptx::mbar_expect_tx(&sh.full_b[sb], bytesB);
+                    ptx::tma_load_5d(sh.b[sb], &mB, 0, x0 - md, 0, y + d - md, n, &sh.full_b[sb]);
+                    ++ub;
                 }
             }
-            if (ok) {
-                ptx::tc_fence_after();
-                const uint32_t a0 = ptx::smem_u32(sA), b0 = ptx::smem_u32(sB[buf]);
-                for (int kk = 0; kk < Cp / 16; ++kk) {
-                    const uint64_t ad = ptx::umma_desc_kmajor(a0 + kk * 2 * kTcM * 16, kTcM * 16, 128);
-                    const uint64_t bd = ptx::umma_desc_kmajor(b0 + kk * 2 * kTcN * 16, kTcN * 16, 128);
-                    ptx::umma_f16(tmem, ad, bd, idesc, kk > 0);
+            if (*sh.abort) {  // let every copy issued land before the CTA exits
+                for (int i = 0; i < stages_a && i < ua; ++i) {
+                    const int u = ua - 1 - i;
+                    ptx::mbar_wait_bounded(&sh.full_a[u % stages_a], (u / stages_a) & 1, kTcWaitSpins);
                 }
-                ptx::umma_commit(&bars[3]);
-                mma_pending = true;
-                mma_par = static_cast<uint32_t>(d & 1);
-                ok = ptx::mbar_wait_bounded(&bars[3], d & 1, kTcWaitSpins);
-                if (ok) {
-                    mma_pending = false;
-                    if (d + 2 < P) {  // the MMA has read this buffer: refill it
-                        ptx::mbar_expect_tx(&bars[1 + buf], bytesB);
-                        ptx::tma_load_5d(sB[buf], &mB, 0, x0 - md, 0, y + d + 2 - md, n, &bars[1 + buf]);
-                        b_pending[buf] = true;
+                for (int i = 0; i < stages_b && i < ub; ++i) {
+                    const int u = ub - 1 - i;
+                    ptx::mbar_wait_bounded(&sh.full_b[u % stages_b], (u / stages_b) & 1, kTcWaitSpins);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        // ---- MMA issuer ----------------------------------------------------------
+        if (lane == 0) {
+            int ua = 0, ub = 0, ud = 0;
+            bool ok = true;
+            for (int it = blockIdx.x; ok && it < items; it += gridDim.x) {
+                const int sa = ua % stages_a;
+                if (!(ok = tc_wait(&sh.full_a[sa], (ua / stages_a) & 1, sh.abort)))
+                    break;
+                for (int d = 0; d < P; ++d) {
+                    const int sb = ub % stages_b, sd = ud % kStagesD;
+                    if (!(ok = tc_wait(&sh.full_b[sb], (ub / stages_b) & 1, sh.abort)))
+                        break;
+                    if (!(ok = tc_wait(&sh.empty_d[sd], ((ud / kStagesD) & 1) ^ 1, sh.abort)))
+                        break;
+                    ptx::tc_fence_after();
+                    const uint32_t a0 = ptx::smem_u32(sh.a[sa]), b0 = ptx::smem_u32(sh.b[sb]);
+                    const uint32_t dcol = tmem + sd * kDStride;
+                    for (int kk = 0; kk < Cp / 16; ++kk) {
+                        const uint64_t ad = ptx::umma_desc_kmajor(a0 + kk * 2 * kTcM * 16, kTcM * 16, 128);
+                        const uint64_t bd = ptx::umma_desc_kmajor(b0 + kk * 2 * kTcN * 16, kTcN * 16, 128);
+                        ptx::umma_f16(dcol, ad, bd, idesc, kk > 0);
                     }
+                    ptx::umma_commit(&sh.full_d[sd]);   // accumulator ready
+                    ptx::umma_commit(&sh.empty_b[sb]);  // B row read
+                    ++ub;
+                    ++ud;
                 }
+                if (!ok)
+                    break;
+                ptx::umma_commit(&sh.empty_a[sa]);  // A tile read by every row of the item
+                ++ua;
             }
-            if (!ok)
-                *abort_flag = 1;
+            if (*sh.abort && ud > 0) {  // the MMAs still in flight finish before Tensor Memory is freed
+                const int u = ud - 1;
+                ptx::mbar_wait_bounded(&sh.full_d[u % kStagesD], (u / kStagesD) & 1, kTcWaitSpins);
+            }
         }
-        __syncthreads();
-        if (*abort_flag)
-            break;
-        ptx::tc_fence_after();
-        uint32_t v0[32], v1[16];
-        ptx::tmem_ld32(tmem + lane_base + warp * 32, v0);
-        ptx::tmem_ld16(tmem + lane_base + warp * 32 + 32, v1);
-        ptx::tmem_ld_wait();
-        float4* row = reinterpret_cast<float4*>(st + lane * kTcPitch);
+    } else {
+        // ---- epilogue: TMEM -> registers -> shared (diagonal) -> global -----------
+        const int q = warp & 3;  // this warp's 32 TMEM lanes (warps 2, 3, 4, 5 -> 2, 3, 0, 1)
+        const uint32_t lane_base = static_cast<uint32_t>(q * 32) << 16;
+        float* st = sh.stage + (warp - 2) * 32 * kTcPitch;
+        const float inv_scale = 1.0f / (scales[0] * scales[1]);  // powers of two: exact
+        const int64_t HW = static_cast<int64_t>(H) * W;
+        int ud = 0;
+        bool ok = true;
+        for (int it = blockIdx.x; ok && it < items; it += gridDim.x) {
+            const int y = it % H, seg = (it / H) % nseg, n = it / (H * nseg);
+            const int x = seg * kTcM + q * 32 + lane;
+            float* obase = out + static_cast<int64_t>(n) * P * P * HW + static_cast<int64_t>(y) * W + x;
+            for (int d = 0; d < P; ++d) {
+                const int sd = ud % kStagesD;
+                // warp-uniform outcome: the Tensor Memory loads below are warp-collective
+                ok = __all_sync(0xffffffffu, tc_wait(&sh.full_d[sd], (ud / kStagesD) & 1, sh.abort));
+                if (!ok)
+                    break;
+                ptx::tc_fence_after();
+                uint32_t v0[32], v1[16];
+                const uint32_t ta = tmem + lane_base + sd * kDStride + q * 32;
+                ptx::tmem_ld32(ta, v0);
+                ptx::tmem_ld16(ta + 32, v1);
+                ptx::tmem_ld_wait();
+                ptx::tc_fence_before();
+                __syncwarp();
+                if (lane == 0)
+                    ptx::mbar_arrive(&sh.empty_d[sd]);  // the accumulator may be overwritten
+                ++ud;
+                float4* row = reinterpret_cast<float4*>(st + lane * kTcPitch);
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-            row[j] = make_float4(__uint_as_float(v0[4 * j]), __uint_as_float(v0[4 * j + 1]),
-                __uint_as_float(v0[4 * j + 2]), __uint_as_float(v0[4 * j + 3]));
+                for (int j = 0; j < 8; ++j)
+                    row[j] = make_float4(__uint_as_float(v0[4 * j]), __uint_as_float(v0[4 * j + 1]),
+                        __uint_as_float(v0[4 * j + 2]), __uint_as_float(v0[4 * j + 3]));
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
-            row[8 + j] = make_float4(__uint_as_float(v1[4 * j]), __uint_as_float(v1[4 * j + 1]),
-                __uint_as_float(v1[4 * j + 2]), __uint_as_float(v1[4 * j + 3]));
-        __syncwarp();
-        if (x < W) {
-            float* o = obase + static_cast<int64_t>(d) * P * HW;
-            const float* srow = st + lane * kTcPitch + lane;
-            for (int k = 0; k < P; ++k)
-                o[k * HW] = srow[k] * inv_scale;
+                for (int j = 0; j < 4; ++j)
+                    row[8 + j] = make_float4(__uint_as_float(v1[4 * j]), __uint_as_float(v1[4 * j + 1]),
+                        __uint_as_float(v1[4 * j + 2]), __uint_as_float(v1[4 * j + 3]));
+                __syncwarp();
+                if (x < W) {
+                    float* o = obase + static_cast<int64_t>(d) * P * HW;
+                    const float* srow = st + lane * kTcPitch + lane;
+                    for (int k = 0; k < P; ++k)
+                        o[k * HW] = srow[k] * inv_scale;
+                }
+                __syncwarp();
+            }
         }
-        __syncwarp();
-        ptx::tc_fence_before();
-        __syncthreads();
     }
 
-    if (tid == 0 && *abort_flag) {
-        atomicExch(timeout_flag, 1);
-        // let the copies and the MMA still in flight land before the CTA exits
-        if (a_pending)
-            ptx::mbar_wait_bounded(&bars[0], 0, kTcWaitSpins);
-        for (int b = 0; b < 2; ++b)
-            if (b_pending[b])
-                ptx::mbar_wait_bounded(&bars[1 + b], b_par[b], kTcWaitSpins);
-        if (mma_pending)
-            ptx::mbar_wait_bounded(&bars[3], mma_par, kTcWaitSpins);
-    }
     ptx::tc_fence_before();
     __syncthreads();
-    if (warp == 0) {
+    if (warp == 1) {
         ptx::tc_fence_after();
         ptx::tmem_dealloc(tmem, kTmemCols);
     }
+    if (threadIdx.x == 0 && *sh.abort)
+        atomicExch(timeout_flag, 1);
 }
 
 // ---- operand preparation ---------------------------------------------------------
@@ -345,11 +445,12 @@ bool encode_chunked_map(CUtensorMap* m, const void* base, int N, int H, int W, i
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// The dynamic shared memory opt-in is a per-device function attribute.
-cudaError_t tc_prepare_device()
+// The dynamic shared memory opt-in is a per-device function attribute; the
+// persistent grid is sized by the device's SM count.
+cudaError_t tc_prepare_device(int* sms)
 {
     static std::mutex mu;
-    static bool done[64] = {};
+    static int count[64] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess)
@@ -357,13 +458,14 @@ cudaError_t tc_prepare_device()
     if (dev < 0 || dev >= 64)
         return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(mu);
-    if (!done[dev]) {
-        e = cudaFuncSetAttribute(corr_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-            static_cast<int>(tc_smem_bytes(kTcMaxChannelsPadded)));
-        if (e != cudaSuccess)
+    if (!count[dev]) {
+        if ((e = cudaFuncSetAttribute(corr_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemLimit)) !=
+            cudaSuccess)
             return e;
-        done[dev] = true;
+        if ((e = cudaDeviceGetAttribute(&count[dev], cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+            return e;
     }
+    *sms = count[dev];
     return cudaSuccess;
 }
 
@@ -382,7 +484,8 @@ cudaError_t launch_corr_tc_chunked(const void* f1c, const void* f2c, float* out,
 {
     if (Cp % 16 != 0 || Cp > kTcMaxChannelsPadded || md < 0 || md > kTcMaxMd)
         return cudaErrorInvalidValue;
-    cudaError_t e = tc_prepare_device();
+    int sms = 0;
+    cudaError_t e = tc_prepare_device(&sms);
     if (e != cudaSuccess)
         return e;
     int* flag = nullptr;
@@ -391,10 +494,10 @@ cudaError_t launch_corr_tc_chunked(const void* f1c, const void* f2c, float* out,
     CUtensorMap mA, mB;
     if (!encode_chunked_map(&mA, f1c, N, H, W, Cp, kTcM) || !encode_chunked_map(&mB, f2c, N, H, W, Cp, kTcN))
         return cudaErrorInvalidValue;
-    const uint32_t smem = std::max<uint32_t>(tc_smem_bytes(Cp), kTcMinSmem);
-    const dim3 grid((W + kTcM - 1) / kTcM, H, N);
-    corr_tc_kernel<<<grid, kTcThreads, smem, st>>>(mA, mB, out, scales, H, W, Cp, md,
-        ptx::umma_idesc_f16(bf16, kTcM, kTcN), flag);
+    const TcPlan plan = tc_plan(Cp);
+    const int items = N * H * ((W + kTcM - 1) / kTcM);
+    corr_tc_kernel<<<std::min(items, sms), kTcThreads, plan.smem, st>>>(mA, mB, out, scales, N, H, W, Cp, md,
+        ptx::umma_idesc_f16(bf16, kTcM, kTcN), plan.stages_a, plan.stages_b, flag);
     return cudaGetLastError();
 }
 

@@ -216,9 +216,11 @@ __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
     }
 }
 
-// Any max_displacement: one thread per output element, channel-order sum.
+// Any max_displacement, and the small pyramid levels (where the tile kernel
+// would run on a handful of CTAs): one thread per output element, the
+// channel sum in channel order; batch n at base + n * stride.
 __global__ void corr_generic_kernel(const float* __restrict__ in1, const float* __restrict__ in2,
-    float* __restrict__ out, int N, int C, int H, int W, int md, int legacy)
+    float* __restrict__ out, int N, int C, int H, int W, int md, int legacy, int64_t s1, int64_t s2, int64_t so)
 {
     const int P = 2 * md + 1;
     const int64_t HW = static_cast<int64_t>(H) * W;
@@ -233,15 +235,26 @@ __global__ void corr_generic_kernel(const float* __restrict__ in1, const float* 
         const int y2 = y + d / P - md, x2 = x + d % P - md;
         float acc = 0.0f;
         if (y2 >= 0 && y2 < H && x2 >= 0 && x2 < W) {
-            const float* a = in1 + static_cast<int64_t>(n) * C * HW + pix;
-            const float* b = in2 + static_cast<int64_t>(n) * C * HW + static_cast<int64_t>(y2) * W + x2;
+            const float* a = in1 + n * s1 + pix;
+            const float* b = in2 + n * s2 + static_cast<int64_t>(y2) * W + x2;
             for (int c = 0; c < C; ++c)
                 acc = acc + __ldg(a + c * HW) * __ldg(b + c * HW);
         }
         if (legacy)
             acc = __fdiv_rn(acc, static_cast<float>(C));
-        out[idx] = acc;
+        out[n * so + static_cast<int64_t>(d) * HW + pix] = acc;
     }
+}
+
+cudaError_t launch_corr_generic(const float* f1, const float* f2, float* out, int N, int C, int H, int W, int md,
+    int legacy, int64_t s1, int64_t s2, int64_t so, cudaStream_t st)
+{
+    const int64_t P = 2 * md + 1;
+    const int64_t total = static_cast<int64_t>(N) * P * P * H * W;
+    const int64_t blocks = (total + 255) / 256;
+    corr_generic_kernel<<<static_cast<unsigned>(blocks < 152 * 64 ? blocks : 152 * 64), 256, 0, st>>>(
+        f1, f2, out, N, C, H, W, md, legacy, s1, s2, so);
+    return cudaGetLastError();
 }
 
 template <int MD>
@@ -410,6 +423,11 @@ cudaError_t launch_correlation(const float* f1, const float* f2, float* out, int
         s1 = s2 = C * HW;
         so = P * P * HW;
     }
+    // the tile kernel's CTAs: 32 x 4 pixels each; below 64 of them the
+    // per-output kernel has far more parallelism (same sums, same bits)
+    const int64_t tile_ctas = static_cast<int64_t>((W + 31) / 32) * ((H + 3) / 4) * N;
+    if (md >= 1 && md <= 4 && tile_ctas < 64)
+        return launch_corr_generic(f1, f2, out, N, C, H, W, md, legacy, s1, s2, so, st);
     switch (md) {
         case 1:
             return launch_corr_tile<1>(f1, f2, out, N, C, H, W, legacy, s1, s2, so, st);
@@ -419,15 +437,8 @@ cudaError_t launch_correlation(const float* f1, const float* f2, float* out, int
             return launch_corr_tile<3>(f1, f2, out, N, C, H, W, legacy, s1, s2, so, st);
         case 4:
             return launch_corr_tile<4>(f1, f2, out, N, C, H, W, legacy, s1, s2, so, st);
-        default: {
-            if (s1 != C * HW || s2 != C * HW || so != P * P * HW)
-                return cudaErrorInvalidValue;  // the generic kernel takes contiguous batches only
-            const int64_t total = static_cast<int64_t>(N) * P * P * HW;
-            const int64_t blocks = (total + 255) / 256;
-            corr_generic_kernel<<<static_cast<unsigned>(blocks < 152 * 64 ? blocks : 152 * 64), 256, 0, st>>>(
-                f1, f2, out, N, C, H, W, md, legacy);
-            return cudaGetLastError();
-        }
+        default:
+            return launch_corr_generic(f1, f2, out, N, C, H, W, md, legacy, s1, s2, so, st);
     }
 }
 
