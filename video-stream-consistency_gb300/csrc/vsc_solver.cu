@@ -118,51 +118,69 @@ struct TbState {
     float o[4][3], u[4][3], a[4][3], wt[4][3], lp[4][3];  // [pixel q = 2*row + col][channel]
 };
 
+// One Jacobi step of a thread's 2x2 block, all three channels: reads the
+// previous iterate from shared buffer `cur` (vertical neighbours) and the
+// neighbouring lanes (horizontal ones), publishes the new one to `cur ^ 1`.
+template <bool kAll>
+__device__ __forceinline__ void tb_step(TbState& s, const bool (&vr)[4], const bool (&vl)[4], const bool (&vd)[4],
+    const bool (&vu)[4], const float (&cnt)[4], float* smem, int cur, bool mom_on, float step, float mom, int px0,
+    int py0)
+{
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        const float* S = smem + (cur * 3 + ch) * kTbPlane;
+        const float2 up = *reinterpret_cast<const float2*>(&S[py0 * kTbPX + px0 + 2]);
+        const float2 dn = *reinterpret_cast<const float2*>(&S[(py0 + 3) * kTbPX + px0 + 2]);
+        const float o0 = s.o[0][ch], o1 = s.o[1][ch], o2 = s.o[2][ch], o3 = s.o[3][ch];
+        const float l0 = __shfl_up_sync(0xffffffffu, o1, 1);
+        const float l1 = __shfl_up_sync(0xffffffffu, o3, 1);
+        const float r0 = __shfl_down_sync(0xffffffffu, o0, 1);
+        const float r1 = __shfl_down_sync(0xffffffffu, o2, 1);
+        const float n0 = jacobi_px<kAll>(o0, s.u[0][ch], s.a[0][ch], s.wt[0][ch], s.lp[0][ch], o1, l0, o2, up.x,
+            vr[0], vl[0], vd[0], vu[0], cnt[0], step, mom, mom_on);
+        const float n1 = jacobi_px<kAll>(o1, s.u[1][ch], s.a[1][ch], s.wt[1][ch], s.lp[1][ch], r0, o0, o3, up.y,
+            vr[1], vl[1], vd[1], vu[1], cnt[1], step, mom, mom_on);
+        const float n2 = jacobi_px<kAll>(o2, s.u[2][ch], s.a[2][ch], s.wt[2][ch], s.lp[2][ch], o3, l1, dn.x, o0,
+            vr[2], vl[2], vd[2], vu[2], cnt[2], step, mom, mom_on);
+        const float n3 = jacobi_px<kAll>(o3, s.u[3][ch], s.a[3][ch], s.wt[3][ch], s.lp[3][ch], r1, o2, dn.y, o1,
+            vr[3], vl[3], vd[3], vu[3], cnt[3], step, mom, mom_on);
+        s.o[0][ch] = n0;
+        s.o[1][ch] = n1;
+        s.o[2][ch] = n2;
+        s.o[3][ch] = n3;
+        float* D = smem + ((cur ^ 1) * 3 + ch) * kTbPlane;
+        *reinterpret_cast<float2*>(&D[(py0 + 1) * kTbPX + px0 + 2]) = make_float2(n0, n1);
+        *reinterpret_cast<float2*>(&D[(py0 + 2) * kTbPX + px0 + 2]) = make_float2(n2, n3);
+    }
+}
+
 // `ring` is the width of the ring around the rows written back (the rows
 // [ring, kTbEY - ring) are exact after the T iterations).  Iteration k only
 // has to be right on rows [ring - T + k + 1, kTbEY - ring + T - k - 1), one
 // row fewer on each side per iteration, so a warp (two rows) whose rows all
 // lie outside skips it: the rows it would have published are read only by
-// rows that are themselves outside the next iteration's range.
+// rows that are themselves outside the next iteration's range.  A launch of
+// the full kTbT iterations after the first step of the solve (momentum on
+// throughout) runs fully unrolled; others take the general loop.
 template <bool kAll>
 __device__ __forceinline__ void tb_iterate(TbState& s, const bool (&vr)[4], const bool (&vl)[4],
     const bool (&vd)[4], const bool (&vu)[4], const float (&cnt)[4], float* smem, int T, int ring, int k0,
     float step, float mom, int px0, int py0)
 {
-    for (int k = 0; k < T; ++k) {
-        const int cur = k & 1;
-        const bool mom_on = (k0 + k) > 0;
-        const int lo = ring - T + k + 1, hi = kTbEY - ring + T - k - 1;
-        if (py0 + 1 < lo || py0 >= hi) {  // warp-uniform: py0 = 2 * threadIdx.y
-            __syncthreads();
-            continue;
-        }
+    if (T == kTbT && ring == kTbT && k0 > 0) {
 #pragma unroll
-        for (int ch = 0; ch < 3; ++ch) {
-            const float* S = smem + (cur * 3 + ch) * kTbPlane;
-            const float2 up = *reinterpret_cast<const float2*>(&S[py0 * kTbPX + px0 + 2]);
-            const float2 dn = *reinterpret_cast<const float2*>(&S[(py0 + 3) * kTbPX + px0 + 2]);
-            const float o0 = s.o[0][ch], o1 = s.o[1][ch], o2 = s.o[2][ch], o3 = s.o[3][ch];
-            const float l0 = __shfl_up_sync(0xffffffffu, o1, 1);
-            const float l1 = __shfl_up_sync(0xffffffffu, o3, 1);
-            const float r0 = __shfl_down_sync(0xffffffffu, o0, 1);
-            const float r1 = __shfl_down_sync(0xffffffffu, o2, 1);
-            const float n0 = jacobi_px<kAll>(o0, s.u[0][ch], s.a[0][ch], s.wt[0][ch], s.lp[0][ch], o1, l0, o2, up.x,
-                vr[0], vl[0], vd[0], vu[0], cnt[0], step, mom, mom_on);
-            const float n1 = jacobi_px<kAll>(o1, s.u[1][ch], s.a[1][ch], s.wt[1][ch], s.lp[1][ch], r0, o0, o3, up.y,
-                vr[1], vl[1], vd[1], vu[1], cnt[1], step, mom, mom_on);
-            const float n2 = jacobi_px<kAll>(o2, s.u[2][ch], s.a[2][ch], s.wt[2][ch], s.lp[2][ch], o3, l1, dn.x, o0,
-                vr[2], vl[2], vd[2], vu[2], cnt[2], step, mom, mom_on);
-            const float n3 = jacobi_px<kAll>(o3, s.u[3][ch], s.a[3][ch], s.wt[3][ch], s.lp[3][ch], r1, o2, dn.y, o1,
-                vr[3], vl[3], vd[3], vu[3], cnt[3], step, mom, mom_on);
-            s.o[0][ch] = n0;
-            s.o[1][ch] = n1;
-            s.o[2][ch] = n2;
-            s.o[3][ch] = n3;
-            float* D = smem + ((cur ^ 1) * 3 + ch) * kTbPlane;
-            *reinterpret_cast<float2*>(&D[(py0 + 1) * kTbPX + px0 + 2]) = make_float2(n0, n1);
-            *reinterpret_cast<float2*>(&D[(py0 + 2) * kTbPX + px0 + 2]) = make_float2(n2, n3);
+        for (int k = 0; k < kTbT; ++k) {
+            const int lo = k + 1, hi = kTbEY - k - 1;  // the general bounds with ring == T == kTbT
+            if (!(py0 + 1 < lo || py0 >= hi))  // warp-uniform: py0 = 2 * threadIdx.y
+                tb_step<kAll>(s, vr, vl, vd, vu, cnt, smem, k & 1, true, step, mom, px0, py0);
+            __syncthreads();
         }
+        return;
+    }
+    for (int k = 0; k < T; ++k) {
+        const int lo = ring - T + k + 1, hi = kTbEY - ring + T - k - 1;
+        if (!(py0 + 1 < lo || py0 >= hi))
+            tb_step<kAll>(s, vr, vl, vd, vu, cnt, smem, k & 1, (k0 + k) > 0, step, mom, px0, py0);
         __syncthreads();
     }
 }
