@@ -54,6 +54,7 @@ struct ConstValue {
     {
         return static_cast<const T*>(t_->data);
     }
+    const void* GetTensorRawData() const { return t_->data; }
 
 private:
     const OrtStubTensor* t_;
@@ -67,6 +68,7 @@ struct UnownedValue {
     {
         return static_cast<T*>(t_->data);
     }
+    void* GetTensorMutableRawData() { return t_->data; }
 
 private:
     OrtStubTensor* t_;

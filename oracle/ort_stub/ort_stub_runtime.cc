@@ -118,6 +118,10 @@ int stub_op_info(int i, const char** name, const char** provider, int* n_in, int
 /* Runs op i once.  attrs: n_attr (name, value) pairs.  Tensors: two float
  * inputs of rank 4 with the given shapes and one output buffer of capacity
  * out_bytes; the output shape the op requested comes back in out_shape. */
+// element type of the tensors stub_run hands to Compute (FLOAT by default)
+static ONNXTensorElementDataType g_run_type = ONNX_TENSOR_ELEMENT_DATA_TYPE_FLOAT;
+void stub_set_tensor_type(int type) { g_run_type = static_cast<ONNXTensorElementDataType>(type); }
+
 int stub_run(int i, int n_attr, const char** attr_names, const int64_t* attr_values, const void* in0,
     const int64_t* shape0, const void* in1, const int64_t* shape1, void* out, size_t out_bytes, int64_t* out_shape,
     int* out_rank, void* stream)
@@ -140,7 +144,7 @@ int stub_run(int i, int n_attr, const char** attr_names, const int64_t* attr_val
         const void* data[2] = {in0, in1};
         const int64_t* shapes[2] = {shape0, shape1};
         for (int k = 0; k < 2; ++k) {
-            ins[k].type = ONNX_TENSOR_ELEMENT_DATA_TYPE_FLOAT;
+            ins[k].type = g_run_type;
             ins[k].rank = 4;
             for (int r = 0; r < 4; ++r)
                 ins[k].shape[r] = shapes[k][r];
@@ -148,7 +152,7 @@ int stub_run(int i, int n_attr, const char** attr_names, const int64_t* attr_val
         }
         OrtStubTensor o;
         std::memset(&o, 0, sizeof(o));
-        o.type = ONNX_TENSOR_ELEMENT_DATA_TYPE_FLOAT;
+        o.type = g_run_type;
         o.data = out;
         o.capacity = out_bytes;
         OrtKernelContext ctx = {ins, 2, &o, 1, stream, 0};

@@ -30,6 +30,7 @@ def ort_lib(vsc, tmp_path_factory):
     cp = C.POINTER(C.c_char_p)
     ip = C.POINTER(C.c_int)
     L.stub_op_info.argtypes = [C.c_int, cp, cp, ip, ip, ip, ip]
+    L.stub_set_tensor_type.argtypes = [C.c_int]
     L.stub_run.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_int64), C.c_void_p,
                            C.POINTER(C.c_int64), C.c_void_p, C.POINTER(C.c_int64), C.c_void_p, C.c_size_t,
                            C.POINTER(C.c_int64), ip, C.c_void_p]
@@ -118,3 +119,38 @@ def test_compute_cuda_and_cpu_providers(ort_lib, vsc, oracle, cuda):
     rc, _ = _run(ort_lib, 1, {}, dx.data_ptr(), x.shape, dfl.data_ptr(), fl.shape, (dw.data_ptr(), dw.numel() * 4),
                  C.c_void_p(s.cuda_stream))
     assert rc == 0 and np.array_equal(dw.cpu().numpy(), wref)
+
+
+@pytest.mark.gpu
+def test_double_tensors(ort_lib, vsc, cuda, golden):
+    """DOUBLE inputs: the CPU provider computes them as correlation.cc / warp.cc
+    do (bit-exact to the reference's double outputs); the CUDA provider
+    accepts FLOAT only, like the reference's CUDA kernels."""
+    g = golden["ref_ops"]
+    ort_lib.stub_register(1)
+    ort_lib.stub_set_tensor_type(11)  # ONNX_TENSOR_ELEMENT_DATA_TYPE_DOUBLE
+    try:
+        f1 = g["corr0_f1"].astype(np.float64)
+        f2 = g["corr0_f2"].astype(np.float64)
+        ref = g["corr0_out64"]
+        hout = np.empty(ref.shape, np.float64)
+        rc, shp = _run(ort_lib, 2, {"legacy": 0, "max_displacement": int(g["corr0_md"])}, f1.ctypes.data, f1.shape,
+                       f2.ctypes.data, f2.shape, (hout.ctypes.data, hout.nbytes))
+        assert rc == 0, ort_lib.stub_last_error()
+        assert np.array_equal(hout, ref)
+        x = g["warp0_x"].astype(np.float64)
+        fl = g["warp0_flow"].astype(np.float64)
+        wout = np.empty_like(x)
+        rc, _ = _run(ort_lib, 3, {}, x.ctypes.data, x.shape, fl.ctypes.data, fl.shape, (wout.ctypes.data, wout.nbytes))
+        assert rc == 0 and np.array_equal(wout, g["warp0_out64"])
+        # the CUDA provider refuses doubles
+        import torch
+
+        s = torch.cuda.current_stream()
+        d1 = torch.from_numpy(f1).to(cuda)
+        dout = torch.empty(ref.shape, dtype=torch.float64, device=cuda)
+        rc, _ = _run(ort_lib, 0, {"legacy": 0, "max_displacement": 4}, d1.data_ptr(), f1.shape, d1.data_ptr(),
+                     f1.shape, (dout.data_ptr(), dout.numel() * 8), C.c_void_p(s.cuda_stream))
+        assert rc == -1 and b"float" in ort_lib.stub_last_error()
+    finally:
+        ort_lib.stub_set_tensor_type(1)  # FLOAT

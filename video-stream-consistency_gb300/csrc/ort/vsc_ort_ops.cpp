@@ -73,10 +73,23 @@ struct KernelBase {
 
 std::vector<int64_t> shape_of(const Ort::ConstValue& v) { return v.GetTensorTypeAndShapeInfo().GetShape(); }
 
+ONNXTensorElementDataType elem_type(const Ort::ConstValue& v) { return v.GetTensorTypeAndShapeInfo().GetElementType(); }
+
+// CUDA provider: FLOAT only, as the reference's CUDA kernels (correlation_cuda.cc, warp_cuda.cc).
 void require_float(const Ort::ConstValue& v)
 {
-    if (v.GetTensorTypeAndShapeInfo().GetElementType() != ONNX_TENSOR_ELEMENT_DATA_TYPE_FLOAT)
+    if (elem_type(v) != ONNX_TENSOR_ELEMENT_DATA_TYPE_FLOAT)
         throw std::runtime_error("Unsupported input type. Must be float.");
+}
+
+// CPU provider: FLOAT or DOUBLE, as the reference's CPU kernels dispatch
+// (correlation.cc:115-141, warp.cc:48-64); returns the element size.
+size_t require_float_or_double(const Ort::ConstValue& a, const Ort::ConstValue& b)
+{
+    const auto t = elem_type(a);
+    if ((t != ONNX_TENSOR_ELEMENT_DATA_TYPE_FLOAT && t != ONNX_TENSOR_ELEMENT_DATA_TYPE_DOUBLE) || elem_type(b) != t)
+        throw std::runtime_error("Unsupported input type. Must be float or double.");
+    return t == ONNX_TENSOR_ELEMENT_DATA_TYPE_DOUBLE ? sizeof(double) : sizeof(float);
 }
 
 struct CorrelationKernel : KernelBase {
@@ -100,8 +113,12 @@ struct CorrelationKernel : KernelBase {
         Ort::KernelContext ctx{context};
         Ort::ConstValue in1 = ctx.GetInput(0);
         Ort::ConstValue in2 = ctx.GetInput(1);
-        require_float(in1);
-        require_float(in2);
+        const bool cuda = is_cuda(provider_);
+        if (cuda) {
+            require_float(in1);
+            require_float(in2);
+        }
+        const size_t es = cuda ? sizeof(float) : require_float_or_double(in1, in2);
         const std::vector<int64_t> d = shape_of(in1);
         if (d.size() != 4 || shape_of(in2) != d)
             throw std::runtime_error("Correlation: inputs must be two N x C x H x W tensors of the same shape");
@@ -109,9 +126,9 @@ struct CorrelationKernel : KernelBase {
         const std::vector<int64_t> od =
             legacy_ ? std::vector<int64_t>{N, P * P, H, W} : std::vector<int64_t>{N, P, P, H, W};
         auto out = ctx.GetOutput(0, od.data(), od.size());
-        const size_t in_bytes = static_cast<size_t>(N * C * H * W) * sizeof(float);
-        const size_t out_bytes = static_cast<size_t>(N * P * P * H * W) * sizeof(float);
-        if (is_cuda(provider_)) {
+        const size_t in_bytes = static_cast<size_t>(N * C * H * W) * es;
+        const size_t out_bytes = static_cast<size_t>(N * P * P * H * W) * es;
+        if (cuda) {
             auto st = static_cast<vsc_stream_t>(ctx.GetGPUComputeStream());
             check(vsc_correlation_fwd(in1.GetTensorData<float>(), in2.GetTensorData<float>(),
                       out.GetTensorMutableData<float>(), N, C, H, W, md_, legacy_, st),
@@ -122,12 +139,17 @@ struct CorrelationKernel : KernelBase {
             throw std::runtime_error("Legacy correlation not supported in CPU mode (only cuda)");
         cudaStream_t st = cudaStreamPerThread;
         Staged a(in_bytes, st), b(in_bytes, st), o(out_bytes, st);
-        check_cuda(cudaMemcpyAsync(a.p, in1.GetTensorData<float>(), in_bytes, cudaMemcpyHostToDevice, st), "upload");
-        check_cuda(cudaMemcpyAsync(b.p, in2.GetTensorData<float>(), in_bytes, cudaMemcpyHostToDevice, st), "upload");
-        check(vsc_correlation_fwd(static_cast<float*>(a.p), static_cast<float*>(b.p), static_cast<float*>(o.p), N, C,
-                  H, W, md_, 0, st),
-            "Correlation");
-        check_cuda(cudaMemcpyAsync(out.GetTensorMutableData<float>(), o.p, out_bytes, cudaMemcpyDeviceToHost, st),
+        check_cuda(cudaMemcpyAsync(a.p, in1.GetTensorRawData(), in_bytes, cudaMemcpyHostToDevice, st), "upload");
+        check_cuda(cudaMemcpyAsync(b.p, in2.GetTensorRawData(), in_bytes, cudaMemcpyHostToDevice, st), "upload");
+        if (es == sizeof(double))
+            check(vsc_correlation_fwd_f64(static_cast<double*>(a.p), static_cast<double*>(b.p),
+                      static_cast<double*>(o.p), N, C, H, W, md_, st),
+                "Correlation");
+        else
+            check(vsc_correlation_fwd(static_cast<float*>(a.p), static_cast<float*>(b.p), static_cast<float*>(o.p), N,
+                      C, H, W, md_, 0, st),
+                "Correlation");
+        check_cuda(cudaMemcpyAsync(out.GetTensorMutableRawData(), o.p, out_bytes, cudaMemcpyDeviceToHost, st),
             "download");
         check_cuda(cudaStreamSynchronize(st), "synchronize");
     }
@@ -144,8 +166,12 @@ struct WarpKernel : KernelBase {
         Ort::KernelContext ctx{context};
         Ort::ConstValue x = ctx.GetInput(0);
         Ort::ConstValue flow = ctx.GetInput(1);
-        require_float(x);
-        require_float(flow);
+        const bool cuda = is_cuda(provider_);
+        if (cuda) {
+            require_float(x);
+            require_float(flow);
+        }
+        const size_t es = cuda ? sizeof(float) : require_float_or_double(x, flow);
         const std::vector<int64_t> d = shape_of(x);
         const std::vector<int64_t> fd = shape_of(flow);
         // warp.cc reads the flow as N x 2 x H x W without checking; we do check
@@ -153,7 +179,7 @@ struct WarpKernel : KernelBase {
             throw std::runtime_error("Warp: input N x C x H x W and flow N x 2 x H x W expected");
         const int64_t N = d[0], C = d[1], H = d[2], W = d[3];
         auto out = ctx.GetOutput(0, d.data(), d.size());
-        if (is_cuda(provider_)) {
+        if (cuda) {
             auto st = static_cast<vsc_stream_t>(ctx.GetGPUComputeStream());
             check(vsc_warp_fwd(x.GetTensorData<float>(), flow.GetTensorData<float>(), out.GetTensorMutableData<float>(),
                       N, C, H, W, st),
@@ -161,14 +187,20 @@ struct WarpKernel : KernelBase {
             return;
         }
         cudaStream_t st = cudaStreamPerThread;
-        const size_t xb = static_cast<size_t>(N * C * H * W) * sizeof(float);
-        const size_t fb = static_cast<size_t>(N * 2 * H * W) * sizeof(float);
+        const size_t xb = static_cast<size_t>(N * C * H * W) * es;
+        const size_t fb = static_cast<size_t>(N * 2 * H * W) * es;
         Staged a(xb, st), f(fb, st), o(xb, st);
-        check_cuda(cudaMemcpyAsync(a.p, x.GetTensorData<float>(), xb, cudaMemcpyHostToDevice, st), "upload");
-        check_cuda(cudaMemcpyAsync(f.p, flow.GetTensorData<float>(), fb, cudaMemcpyHostToDevice, st), "upload");
-        check(vsc_warp_fwd(static_cast<float*>(a.p), static_cast<float*>(f.p), static_cast<float*>(o.p), N, C, H, W, st),
-            "Warp");
-        check_cuda(cudaMemcpyAsync(out.GetTensorMutableData<float>(), o.p, xb, cudaMemcpyDeviceToHost, st), "download");
+        check_cuda(cudaMemcpyAsync(a.p, x.GetTensorRawData(), xb, cudaMemcpyHostToDevice, st), "upload");
+        check_cuda(cudaMemcpyAsync(f.p, flow.GetTensorRawData(), fb, cudaMemcpyHostToDevice, st), "upload");
+        if (es == sizeof(double))
+            check(vsc_warp_fwd_f64(static_cast<double*>(a.p), static_cast<double*>(f.p), static_cast<double*>(o.p), N,
+                      C, H, W, st),
+                "Warp");
+        else
+            check(vsc_warp_fwd(static_cast<float*>(a.p), static_cast<float*>(f.p), static_cast<float*>(o.p), N, C, H,
+                      W, st),
+                "Warp");
+        check_cuda(cudaMemcpyAsync(out.GetTensorMutableRawData(), o.p, xb, cudaMemcpyDeviceToHost, st), "download");
         check_cuda(cudaStreamSynchronize(st), "synchronize");
     }
 };

@@ -39,13 +39,15 @@ constexpr int kTcM = 128;        // pixels per tile (MMA M, TMEM lanes)
 constexpr int kTcN = 144;        // f2 window per displacement row (MMA N)
 constexpr int kTcCols = 48;      // TMEM columns one warp reads per row: 32 + 2 md
 constexpr int kTcPitch = 52;     // staging row pitch (floats): 53 * lane spreads the diagonal over all banks
-constexpr int kTcWarps = 6;      // 0: TMA producer, 1: MMA issuer + TMEM owner, 2..5: epilogue
-constexpr int kTcThreads = kTcWarps * 32;
+// warps: 0 TMA producer, 1 MMA issuer + Tensor Memory owner, then 1..3
+// epilogue groups of four warps (one per 32 TMEM lanes); group g drains the
+// accumulators of rows u with u % groups == g
+constexpr int kMaxEpiGroups = 3;
 constexpr int kMaxStagesA = 2, kMaxStagesB = 4, kStagesD = 3;
 constexpr uint32_t kTmemCols = 512;    // three accumulators
 constexpr uint32_t kDStride = 160;     // TMEM columns between accumulators (>= kTcN, multiple of 32)
 constexpr int kTcWaitSpins = 1 << 22;  // bounded mbarrier waits (about a second)
-constexpr int kTcStageBytes = 4 * 32 * kTcPitch * 4;
+constexpr int kTcGroupStageBytes = 4 * 32 * kTcPitch * 4;  // one epilogue group's staging
 constexpr int kTcBarBytes = 256;
 constexpr int kTcSmemLimit = 232448;   // dynamic shared memory per CTA on sm_103
 // at least this much dynamic shared memory, so that one CTA (and one
@@ -59,26 +61,32 @@ static_assert((kStagesD - 1) * kDStride + kTcN <= kTmemCols, "accumulators insid
 __host__ __device__ constexpr uint32_t align1k(uint32_t v) { return (v + 1023u) & ~1023u; }
 
 struct TcPlan {
-    int stages_a, stages_b;
+    int stages_a, stages_b, groups;
     uint32_t smem;
 };
 
-// Operand buffers that fit in shared memory for Cp channels: two A tiles and
-// four B rows when they fit, down to one A tile and two B rows (208 channels).
+__host__ uint32_t tc_smem_need(int cp, int sa, int sb, int g)
+{
+    return 1024 + sa * align1k(kTcM * cp * 2) + sb * align1k(kTcN * cp * 2) + g * kTcGroupStageBytes + kTcBarBytes;
+}
+
+// Buffers that fit in shared memory for Cp channels: three epilogue groups,
+// two A tiles and four B rows when they fit; B rows, then A tiles, then
+// epilogue groups are given up in that order (208 channels: 1, 2, 2).
 __host__ TcPlan tc_plan(int cp)
 {
-    const uint32_t a = align1k(kTcM * cp * 2), b = align1k(kTcN * cp * 2);
-    const uint32_t fixed = 1024 + kTcStageBytes + kTcBarBytes;
-    TcPlan p{2, 4, 0};
-    while (fixed + p.stages_a * a + p.stages_b * b > static_cast<uint32_t>(kTcSmemLimit)) {
+    TcPlan p{2, 4, kMaxEpiGroups, 0};
+    while (tc_smem_need(cp, p.stages_a, p.stages_b, p.groups) > static_cast<uint32_t>(kTcSmemLimit)) {
         if (p.stages_b > 2)
             --p.stages_b;
         else if (p.stages_a > 1)
             --p.stages_a;
+        else if (p.groups > 1)
+            --p.groups;
         else
             break;
     }
-    p.smem = std::max<uint32_t>(fixed + p.stages_a * a + p.stages_b * b, kTcMinSmem);
+    p.smem = std::max<uint32_t>(tc_smem_need(cp, p.stages_a, p.stages_b, p.groups), kTcMinSmem);
     return p;
 }
 
@@ -114,10 +122,10 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, volatile
 // in Tensor Memory (MMA -> epilogue, freed by the four epilogue warps as soon
 // as their columns are in registers, before the shared-memory and global
 // part of the epilogue).
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__((2 + 4 * kMaxEpiGroups) * 32, 1)
     corr_tc_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB,
         float* __restrict__ out, const float* __restrict__ scales, int N, int H, int W, int Cp, int md,
-        uint32_t idesc, int stages_a, int stages_b, int* __restrict__ timeout_flag)
+        uint32_t idesc, int stages_a, int stages_b, int groups, int ndyg, int* __restrict__ timeout_flag)
 {
     extern __shared__ unsigned char smem_raw[];
     const uint32_t bytesA = kTcM * Cp * 2;
@@ -131,7 +139,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         for (int i = 0; i < stages_b; ++i, p += align1k(bytesB))
             sh.b[i] = p;
         sh.stage = reinterpret_cast<float*>(p);
-        uint64_t* bars = reinterpret_cast<uint64_t*>(p + kTcStageBytes);
+        uint64_t* bars = reinterpret_cast<uint64_t*>(p + groups * kTcGroupStageBytes);
         sh.full_a = bars;
         sh.empty_a = bars + 2;
         sh.full_b = bars + 4;
@@ -144,7 +152,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int P = 2 * md + 1;
     const int nseg = (W + kTcM - 1) / kTcM;
-    const int items = N * H * nseg;
+    // work item: (n, segment, row y, group of displacement rows); small maps
+    // split the 2 md + 1 displacement rows over ndyg items to fill the GPU
+    const int rpg = (P + ndyg - 1) / ndyg;
+    const int items = N * H * nseg * ndyg;
 
     if (warp == 1) {
         ptx::tmem_alloc(sh.tmem_slot, kTmemCols);
@@ -176,7 +187,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             int ua = 0, ub = 0;
             bool ok = true;
             for (int it = blockIdx.x; ok && it < items; it += gridDim.x) {
-                const int y = it % H, seg = (it / H) % nseg, n = it / (H * nseg);
+                const int dyg = it % ndyg, r = it / ndyg;
+                const int y = r % H, seg = (r / H) % nseg, n = r / (H * nseg);
+                const int d0 = dyg * rpg, d1 = min(P, d0 + rpg);
                 const int x0 = seg * kTcM;
                 const int sa = ua % stages_a;
                 if (!(ok = tc_wait(&sh.empty_a[sa], ((ua / stages_a) & 1) ^ 1, sh.abort)))
@@ -184,7 +197,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 ptx::mbar_expect_tx(&sh.full_a[sa], bytesA);
                 ptx::tma_load_5d(sh.a[sa], &mA, 0, x0, 0, y, n, &sh.full_a[sa]);
                 ++ua;
-                for (int d = 0; d < P; ++d) {
+                for (int d = d0; d < d1; ++d) {
                     const int sb = ub % stages_b;
                     if (!(ok = tc_wait(&sh.empty_b[sb], ((ub / stages_b) & 1) ^ 1, sh.abort)))
                         break;
@@ -210,10 +223,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             int ua = 0, ub = 0, ud = 0;
             bool ok = true;
             for (int it = blockIdx.x; ok && it < items; it += gridDim.x) {
+                const int dyg = it % ndyg;
+                const int d0 = dyg * rpg, d1 = min(P, d0 + rpg);
                 const int sa = ua % stages_a;
                 if (!(ok = tc_wait(&sh.full_a[sa], (ua / stages_a) & 1, sh.abort)))
                     break;
-                for (int d = 0; d < P; ++d) {
+                for (int d = d0; d < d1; ++d) {
                     const int sb = ub % stages_b, sd = ud % kStagesD;
                     if (!(ok = tc_wait(&sh.full_b[sb], (ub / stages_b) & 1, sh.abort)))
                         break;
@@ -244,18 +259,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
     } else {
         // ---- epilogue: TMEM -> registers -> shared (diagonal) -> global -----------
-        const int q = warp & 3;  // this warp's 32 TMEM lanes (warps 2, 3, 4, 5 -> 2, 3, 0, 1)
+        const int q = warp & 3;          // this warp's 32 TMEM lanes (the warp's rank in its warpgroup)
+        const int grp = (warp - 2) >> 2;  // epilogue group
         const uint32_t lane_base = static_cast<uint32_t>(q * 32) << 16;
         float* st = sh.stage + (warp - 2) * 32 * kTcPitch;
         const float inv_scale = 1.0f / (scales[0] * scales[1]);  // powers of two: exact
         const int64_t HW = static_cast<int64_t>(H) * W;
-        int ud = 0;
+        int ud = 0;  // accumulator use index, counted over every row of the CTA
         bool ok = true;
         for (int it = blockIdx.x; ok && it < items; it += gridDim.x) {
-            const int y = it % H, seg = (it / H) % nseg, n = it / (H * nseg);
+            const int dyg = it % ndyg, r = it / ndyg;
+            const int y = r % H, seg = (r / H) % nseg, n = r / (H * nseg);
+            const int d0 = dyg * rpg, d1 = min(P, d0 + rpg);
             const int x = seg * kTcM + q * 32 + lane;
             float* obase = out + static_cast<int64_t>(n) * P * P * HW + static_cast<int64_t>(y) * W + x;
-            for (int d = 0; d < P; ++d) {
+            for (int d = d0; d < d1; ++d, ++ud) {
+                if (ud % groups != grp)
+                    continue;
                 const int sd = ud % kStagesD;
                 // warp-uniform outcome: the Tensor Memory loads below are warp-collective
                 ok = __all_sync(0xffffffffu, tc_wait(&sh.full_d[sd], (ud / kStagesD) & 1, sh.abort));
@@ -271,7 +291,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 __syncwarp();
                 if (lane == 0)
                     ptx::mbar_arrive(&sh.empty_d[sd]);  // the accumulator may be overwritten
-                ++ud;
                 float4* row = reinterpret_cast<float4*>(st + lane * kTcPitch);
 #pragma unroll
                 for (int j = 0; j < 8; ++j)
@@ -495,9 +514,14 @@ cudaError_t launch_corr_tc_chunked(const void* f1c, const void* f2c, float* out,
     if (!encode_chunked_map(&mA, f1c, N, H, W, Cp, kTcM) || !encode_chunked_map(&mB, f2c, N, H, W, Cp, kTcN))
         return cudaErrorInvalidValue;
     const TcPlan plan = tc_plan(Cp);
-    const int items = N * H * ((W + kTcM - 1) / kTcM);
-    corr_tc_kernel<<<std::min(items, sms), kTcThreads, plan.smem, st>>>(mA, mB, out, scales, N, H, W, Cp, md,
-        ptx::umma_idesc_f16(bf16, kTcM, kTcN), plan.stages_a, plan.stages_b, flag);
+    const int P = 2 * md + 1;
+    const int base = N * H * ((W + kTcM - 1) / kTcM);
+    int ndyg = 1;  // split the displacement rows until there are two items per SM
+    while (ndyg < P && base * ndyg < 2 * sms)
+        ++ndyg;
+    const int items = base * ndyg;
+    corr_tc_kernel<<<std::min(items, sms), (2 + 4 * plan.groups) * 32, plan.smem, st>>>(mA, mB, out, scales, N, H,
+        W, Cp, md, ptx::umma_idesc_f16(bf16, kTcM, kTcN), plan.stages_a, plan.stages_b, plan.groups, ndyg, flag);
     return cudaGetLastError();
 }
 
