@@ -320,6 +320,31 @@ VSC_API vsc_status vsc_stabilizer_enable_timing(vsc_stabilizer* s, int32_t on);
  * full-resolution solve and RGBA8 output; n >= 5.  Synchronises the stream. */
 VSC_API vsc_status vsc_stabilizer_stage_ms(vsc_stabilizer* s, float* ms, int32_t n);
 
+/* ---- several streams per frame step (no counterpart in the reference) -------
+ * Stabilizes n independent videos of any sizes in lockstep: each step runs
+ * every stream's doOneStep, forked from `stream` onto one CUDA stream per
+ * video and joined back, and from the second step on the whole fork/join is
+ * replayed as one CUDA graph (captured once per window position).  Flows are
+ * computed by the library (compute_flow = 1); every stream shares the
+ * hyper-parameters of vsc_multistream_hyper_params. */
+typedef struct vsc_stream_desc {
+    int32_t width, height;
+    int32_t flow_downscale; /* 0 or 1: none */
+    int32_t corr_dtype;     /* as vsc_stabilizer_config.corr_dtype */
+} vsc_stream_desc;
+typedef struct vsc_multistream vsc_multistream;
+
+VSC_API vsc_status vsc_multistream_create(const vsc_stream_desc* streams, int32_t n, vsc_stream_t stream,
+    vsc_multistream** out);
+VSC_API vsc_status vsc_multistream_destroy(vsc_multistream* m);
+VSC_API vsc_hyper_params* vsc_multistream_hyper_params(vsc_multistream* m);
+/* One frame per stream: orig[i], proc[i] RGBA8 of stream i's size. */
+VSC_API vsc_status vsc_multistream_load_frames(vsc_multistream* m, const uint8_t* const* orig,
+    const uint8_t* const* proc, int32_t on_device);
+/* out[i]: stream i's stabilized RGBA8 frame (NULL entries skip the copy). */
+VSC_API vsc_status vsc_multistream_step(vsc_multistream* m, uint8_t* const* out, int32_t out_on_device);
+VSC_API int32_t vsc_multistream_last_launches(vsc_multistream* m);
+
 /* ---- frame directories (FileStabilizer, stabilizefiles.cpp:37-149) ----------
  * Image files: PNG (8-bit gray, gray+alpha, RGB or RGBA, not interlaced) and
  * binary PPM (P6, maxval 255), read into RGBA8 host buffers (alpha 255 where

@@ -369,3 +369,47 @@ def test_full_hd_step_deterministic(vsc, cuda):
     for a, b in zip(outs[0], outs[1]):
         assert np.array_equal(a, b)
     assert outs[0][1][..., 3].max() == 1
+
+
+def test_multistream_equals_independent_stabilizers(vsc, cuda):
+    """Three videos of different sizes in one multistream object: every
+    stream's output equals its own stabilizer's, bit for bit, on the direct
+    first step and on the graph replays that follow."""
+    import torch
+
+    sizes = [(96, 64), (128, 72), (80, 48)]
+    streams = [_frames(w, h, 7, seed=50 + i) for i, (w, h) in enumerate(sizes)]
+    side = torch.cuda.Stream()
+    ms = vsc.MultiStream(sizes, stream=side)
+    ms.hyper_params.num_iter = 60
+    singles = []
+    for (w, h), fr in zip(sizes, streams):
+        st = vsc.Stabilizer(w, h)
+        st.hyper_params.num_iter = 60
+        singles.append(st)
+    for i in range(3):  # host frames: each stream uploads on its own CUDA stream
+        ms.load_frames([fr[i][0] for fr in streams], [fr[i][1] for fr in streams])
+        for st, fr in zip(singles, streams):
+            st.load_frame(*fr[i])
+    side.synchronize()
+    for t in range(1, 6):
+        with torch.cuda.stream(side):
+            outs = ms.step()
+        side.synchronize()
+        for k, (st, out) in enumerate(zip(singles, outs)):
+            ref = st.step().cpu().numpy()
+            assert np.array_equal(out.cpu().numpy(), ref), (t, k)
+        if t + 2 < 7:
+            if t % 2:  # device frames, made ready before the call
+                o = [torch.from_numpy(fr[t + 2][0]).cuda() for fr in streams]
+                p = [torch.from_numpy(fr[t + 2][1]).cuda() for fr in streams]
+                torch.cuda.synchronize()
+                ms.load_frames(o, p)
+            else:
+                ms.load_frames([fr[t + 2][0] for fr in streams], [fr[t + 2][1] for fr in streams])
+            for st, fr in zip(singles, streams):
+                st.load_frame(*fr[t + 2])
+    assert ms.last_launches > 3 * 20
+    ms.close()
+    for st in singles:
+        st.close()

@@ -39,6 +39,8 @@ EXPORTED = [
     "vsc_correlation_lowp_workspace_size", "vsc_correlation_fwd_lowp",
     "vsc_image_file_info", "vsc_read_image_file", "vsc_write_png", "vsc_flo_info", "vsc_read_flo", "vsc_write_flo",
     "vsc_stabilize_files", "vsc_solver_steps_per_launch",
+    "vsc_multistream_create", "vsc_multistream_destroy", "vsc_multistream_hyper_params", "vsc_multistream_load_frames",
+    "vsc_multistream_step", "vsc_multistream_last_launches",
 ]
 VSC_DTYPE_F32, VSC_DTYPE_BF16, VSC_DTYPE_F16 = 0, 1, 2
 NOALLOC_MAX_PIXELS = 349525  # VSC_NOALLOC_MAX_PIXELS
@@ -72,6 +74,10 @@ class FilesConfig(C.Structure):
         ("flow_dir", C.c_char_p), ("width", C.c_int32), ("height", C.c_int32), ("flow_downscale", C.c_int32),
         ("corr_dtype", C.c_int32), ("hyper", C.c_void_p),
     ]
+
+
+class StreamDesc(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("flow_downscale", C.c_int32), ("corr_dtype", C.c_int32)]
 
 
 class StabilizerConfig(C.Structure):
@@ -137,6 +143,10 @@ def load():
         "vsc_read_flo": [C.c_char_p, vp, i32, i32],
         "vsc_write_flo": [C.c_char_p, vp, i32, i32],
         "vsc_stabilize_files": [C.POINTER(FilesConfig), C.POINTER(i32)],
+        "vsc_multistream_create": [C.POINTER(StreamDesc), i32, vp, C.POINTER(vp)],
+        "vsc_multistream_destroy": [vp],
+        "vsc_multistream_load_frames": [vp, C.POINTER(vp), C.POINTER(vp), i32],
+        "vsc_multistream_step": [vp, C.POINTER(vp), i32],
         "vsc_get_adap_comb_masked": [IP] * 10 + [f32, vp],
         "vsc_stabilizer_set_occlusion_mask": [vp, i32],
         "vsc_check_device": [],
@@ -146,6 +156,10 @@ def load():
         f = getattr(L, fn)
         f.argtypes = args
         f.restype = C.c_int
+    L.vsc_multistream_hyper_params.restype = C.POINTER(HyperParams)
+    L.vsc_multistream_hyper_params.argtypes = [vp]
+    L.vsc_multistream_last_launches.restype = i32
+    L.vsc_multistream_last_launches.argtypes = [vp]
     L.vsc_solver_steps_per_launch.restype = i32
     L.vsc_solver_steps_per_launch.argtypes = []
     L.vsc_correlation_lowp_workspace_size.restype = C.c_size_t
@@ -531,3 +545,69 @@ class Stabilizer:
             self.close()
         except Exception:
             pass
+
+
+class MultiStream:
+    """Several independent videos stabilized in lockstep, one graph launch per
+    frame step (vsc_multistream_*).  sizes: [(width, height), ...]."""
+
+    def __init__(self, sizes, flow_downscale=1, corr_dtype: str = "f32", stream=None):
+        import torch
+
+        code = {"f32": VSC_DTYPE_F32, "bf16": VSC_DTYPE_BF16, "fp16": VSC_DTYPE_F16}[corr_dtype]
+        self.sizes = [tuple(x) for x in sizes]
+        descs = (StreamDesc * len(sizes))(*[StreamDesc(w, h, flow_downscale, code) for w, h in sizes])
+        self._stream_obj = stream if stream is not None else torch.cuda.current_stream()
+        h = C.c_void_p()
+        _check(load().vsc_multistream_create(descs, len(sizes), _stream(self._stream_obj), C.byref(h)))
+        self._h = h
+
+    @property
+    def hyper_params(self) -> HyperParams:
+        return load().vsc_multistream_hyper_params(self._h).contents
+
+    @property
+    def last_launches(self) -> int:
+        return int(load().vsc_multistream_last_launches(self._h))
+
+    def load_frames(self, origs, procs):
+        """One RGBA8 (H, W, 4) frame pair per stream: all numpy (host) or all CUDA tensors."""
+        import numpy as np
+
+        on_dev = hasattr(origs[0], "is_cuda") and origs[0].is_cuda
+        keep = []
+
+        def ptr(a):
+            if on_dev:
+                return a.data_ptr()
+            a = np.ascontiguousarray(a)
+            keep.append(a)
+            return a.ctypes.data
+
+        o = (C.c_void_p * len(origs))(*[ptr(a) for a in origs])
+        p = (C.c_void_p * len(procs))(*[ptr(a) for a in procs])
+        _check(load().vsc_multistream_load_frames(self._h, o, p, 1 if on_dev else 0))
+
+    def step(self, outs=None):
+        """Stabilizes every stream's middle frame; returns the RGBA8 results
+        (device tensors unless host arrays are given)."""
+        import torch
+
+        if outs is None:
+            outs = [torch.empty((h, w, 4), dtype=torch.uint8, device="cuda") for w, h in self.sizes]
+        on_dev = hasattr(outs[0], "is_cuda") and outs[0].is_cuda
+        ptrs = (C.c_void_p * len(outs))(*[(o.data_ptr() if on_dev else o.ctypes.data) for o in outs])
+        _check(load().vsc_multistream_step(self._h, ptrs, 1 if on_dev else 0))
+        return outs
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().vsc_multistream_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
+

@@ -19,6 +19,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "vsc_internal.h"
 
@@ -998,6 +999,31 @@ bool launch_step_graph(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t* r
     return true;
 }
 
+// The window advances after a step: the feedback frame flips, the oldest
+// frame leaves the ring (doOneStep's pop_front, videostabilizer.cpp:247-252).
+void finish_step(vsc_stabilizer* s, int launches)
+{
+    s->ls_cur ^= 1;
+    s->started = true;
+    s->flows_set = false;
+    s->head = (s->head + 1) % 3;
+    s->count -= 1;
+    s->last_launches = launches;
+}
+
+vsc_status step_preconditions(vsc_stabilizer* s, const vsc_hyper_params& hp)
+{
+    if (s->count < 3)
+        return set_error(VSC_ESTATE, "step: window holds %d of 3 frames", s->count);
+    if (!s->compute_flow && !s->flows_set)
+        return set_error(VSC_ESTATE, "step: flows not set for this step");
+    if (hp.pyramid_levels < 1 || hp.pyramid_levels > s->levels_alloc)
+        return set_error(VSC_EINVAL, "step: pyramid_levels %d outside [1, %d]", hp.pyramid_levels, s->levels_alloc);
+    if (hp.num_iter < 0)
+        return set_error(VSC_EINVAL, "step: negative num_iter");
+    return VSC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1033,12 +1059,7 @@ VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int
     vsc_status stt = check_cuda(e, "step");
     if (stt)
         return stt;
-    s->ls_cur ^= 1;
-    s->started = true;
-    s->flows_set = false;
-    s->head = (s->head + 1) % 3;
-    s->count -= 1;
-    s->last_launches = nl;
+    finish_step(s, nl);
     if (out_rgba && !out_on_device) {
         stt = check_cuda(cudaMemcpyAsync(out_rgba, s->out_rgba, static_cast<size_t>(s->w) * s->h * 4,
                              cudaMemcpyDeviceToHost, s->st),
@@ -1123,3 +1144,274 @@ VSC_API vsc_status vsc_stabilizer_stage_ms(vsc_stabilizer* s, float* ms, int32_t
 }
 
 }  // extern "C"
+
+// ---- several streams in one graph launch per frame step -------------------------
+// Each stream is a stabilizer on its own CUDA stream; a frame step forks from
+// the caller's stream into every stabilizer's stream, enqueues its step there,
+// and joins back, so the steps of small and large frames overlap on the
+// device.  After the first step the whole fork/join is captured once per
+// window position as one CUDA graph (all streams advance in lockstep).
+struct vsc_multistream {
+    std::vector<vsc_stabilizer*> st;
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> loaded, joined;
+    cudaEvent_t fork = nullptr, done = nullptr;
+    cudaStream_t main = nullptr;
+    bool own_main = false;
+    int device = 0;
+    vsc_hyper_params hp{};
+    int last_launches = 0;
+    struct Graph {
+        bool valid = false;
+        int head = 0, ls_cur = 0, nl = 0;
+        std::vector<uint8_t*> outs;
+        vsc_hyper_params hp{};
+        cudaGraphExec_t exec = nullptr;
+        uint64_t used = 0;
+    } graphs[6];
+    uint64_t clock = 0;
+};
+
+namespace {
+
+void ms_free(vsc_multistream* m)
+{
+    for (auto& g : m->graphs)
+        if (g.exec)
+            cudaGraphExecDestroy(g.exec);
+    for (vsc_stabilizer* s : m->st)
+        vsc_stabilizer_destroy(s);
+    for (cudaStream_t x : m->side)
+        if (x)
+            cudaStreamDestroy(x);
+    for (cudaEvent_t e : m->loaded)
+        if (e)
+            cudaEventDestroy(e);
+    for (cudaEvent_t e : m->joined)
+        if (e)
+            cudaEventDestroy(e);
+    if (m->fork)
+        cudaEventDestroy(m->fork);
+    if (m->done)
+        cudaEventDestroy(m->done);
+    if (m->own_main && m->main)
+        cudaStreamDestroy(m->main);
+}
+
+// fork -> every stream's step -> join, on m->main; counts launches
+cudaError_t ms_enqueue(vsc_multistream* m, const std::vector<uint8_t*>& outs, int* launches)
+{
+    cudaError_t e = cudaEventRecord(m->fork, m->main);
+    int nl = 0;
+    for (size_t i = 0; i < m->st.size() && e == cudaSuccess; ++i) {
+        if ((e = cudaStreamWaitEvent(m->side[i], m->fork, 0)) != cudaSuccess)
+            break;
+        int n = 0;
+        if ((e = enqueue_step(m->st[i], m->hp, outs[i], &n)) != cudaSuccess)
+            break;
+        nl += n;
+        if ((e = cudaEventRecord(m->joined[i], m->side[i])) == cudaSuccess)
+            e = cudaStreamWaitEvent(m->main, m->joined[i], 0);
+    }
+    *launches = nl;
+    return e;
+}
+
+bool ms_launch_graph(vsc_multistream* m, const std::vector<uint8_t*>& outs, int* launches, cudaError_t* err)
+{
+    *err = cudaSuccess;
+    vsc_stabilizer* s0 = m->st[0];
+    vsc_multistream::Graph* hit = nullptr;
+    for (auto& g : m->graphs)
+        if (g.valid && g.head == s0->head && g.ls_cur == s0->ls_cur && g.outs == outs && same_hp(g.hp, m->hp))
+            hit = &g;
+    if (!hit) {
+        auto* slot = &m->graphs[0];
+        for (auto& g : m->graphs)
+            if (!g.valid || g.used < slot->used)
+                slot = &g;
+        if (slot->exec) {
+            cudaGraphExecDestroy(slot->exec);
+            slot->exec = nullptr;
+        }
+        slot->valid = false;
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(m->main, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        int nl = 0;
+        const cudaError_t ee = ms_enqueue(m, outs, &nl);
+        const cudaError_t ec = cudaStreamEndCapture(m->main, &graph);
+        if (ee != cudaSuccess || ec != cudaSuccess || !graph) {
+            if (graph)
+                cudaGraphDestroy(graph);
+            cudaGetLastError();
+            return false;
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&slot->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) {
+            cudaGetLastError();
+            slot->exec = nullptr;
+            return false;
+        }
+        slot->valid = true;
+        slot->head = s0->head;
+        slot->ls_cur = s0->ls_cur;
+        slot->outs = outs;
+        slot->hp = m->hp;
+        slot->nl = nl;
+        hit = slot;
+    }
+    hit->used = ++m->clock;
+    *launches = hit->nl;
+    *err = cudaGraphLaunch(hit->exec, m->main);
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+VSC_API vsc_status vsc_multistream_create(const vsc_stream_desc* desc, int32_t n, vsc_stream_t stream,
+    vsc_multistream** out)
+{
+    clear_error();
+    if (!desc || !out || n < 1 || n > 256)
+        return set_error(VSC_EINVAL, "multistream_create: bad arguments (1..256 streams)");
+    *out = nullptr;
+    vsc_multistream* m = new (std::nothrow) vsc_multistream();
+    if (!m)
+        return set_error(VSC_ENOMEM, "multistream_create: out of host memory");
+    cudaGetDevice(&m->device);
+    vsc_default_hyper_params(&m->hp);
+    vsc_status s = VSC_OK;
+    cudaError_t e = cudaSuccess;
+    m->main = cs(stream);
+    if (!m->main) {  // capture needs a stream other than the legacy default one
+        e = cudaStreamCreateWithFlags(&m->main, cudaStreamNonBlocking);
+        m->own_main = e == cudaSuccess;
+    }
+    if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(&m->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(&m->done, cudaEventDisableTiming);
+    for (int i = 0; i < n && e == cudaSuccess && !s; ++i) {
+        cudaStream_t x = nullptr;
+        cudaEvent_t a = nullptr, b = nullptr;
+        e = cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking);
+        if (e == cudaSuccess)
+            m->side.push_back(x);
+        if (e == cudaSuccess && (e = cudaEventCreateWithFlags(&a, cudaEventDisableTiming)) == cudaSuccess)
+            m->loaded.push_back(a);
+        if (e == cudaSuccess && (e = cudaEventCreateWithFlags(&b, cudaEventDisableTiming)) == cudaSuccess)
+            m->joined.push_back(b);
+        if (e != cudaSuccess)
+            break;
+        vsc_stabilizer_config cfg{};
+        cfg.width = desc[i].width;
+        cfg.height = desc[i].height;
+        cfg.batch_size = 1;
+        cfg.compute_flow = 1;
+        cfg.flow_downscale = desc[i].flow_downscale > 0 ? desc[i].flow_downscale : 1;
+        cfg.flow_channels = 3;
+        cfg.use_graphs = 0;  // the multistream object captures the whole step itself
+        cfg.corr_dtype = desc[i].corr_dtype;
+        vsc_stabilizer* st = nullptr;
+        if ((s = vsc_stabilizer_create(&cfg, x, &st)) == VSC_OK)
+            m->st.push_back(st);
+    }
+    if (!s && e != cudaSuccess)
+        s = check_cuda(e, "multistream_create");
+    if (s) {
+        const std::string msg = vsc_last_error();
+        ms_free(m);
+        delete m;
+        return set_error(s, "%s", msg.c_str());
+    }
+    *out = m;
+    return VSC_OK;
+}
+
+VSC_API vsc_status vsc_multistream_destroy(vsc_multistream* m)
+{
+    clear_error();
+    if (!m)
+        return VSC_OK;
+    DeviceGuard g(m->device);
+    cudaStreamSynchronize(m->main);
+    ms_free(m);
+    delete m;
+    return VSC_OK;
+}
+
+VSC_API vsc_hyper_params* vsc_multistream_hyper_params(vsc_multistream* m) { return m ? &m->hp : nullptr; }
+
+VSC_API int32_t vsc_multistream_last_launches(vsc_multistream* m) { return m ? m->last_launches : 0; }
+
+VSC_API vsc_status vsc_multistream_load_frames(vsc_multistream* m, const uint8_t* const* orig,
+    const uint8_t* const* proc, int32_t on_device)
+{
+    clear_error();
+    if (!m || !orig || !proc)
+        return set_error(VSC_EINVAL, "multistream_load_frames: null argument");
+    DeviceGuard g(m->device);
+    vsc_status s = check_cuda(cudaEventRecord(m->done, m->main), "multistream_load_frames");
+    for (size_t i = 0; i < m->st.size() && !s; ++i) {
+        // the previous step, which reads the window, completes first
+        if ((s = check_cuda(cudaStreamWaitEvent(m->side[i], m->done, 0), "multistream_load_frames")))
+            break;
+        if ((s = vsc_stabilizer_load_frame(m->st[i], orig[i], proc[i], on_device)))
+            break;
+        s = check_cuda(cudaEventRecord(m->loaded[i], m->side[i]), "multistream_load_frames");
+    }
+    return s;
+}
+
+VSC_API vsc_status vsc_multistream_step(vsc_multistream* m, uint8_t* const* out, int32_t out_on_device)
+{
+    clear_error();
+    if (!m)
+        return set_error(VSC_EINVAL, "multistream_step: null argument");
+    DeviceGuard g(m->device);
+    vsc_status s;
+    for (vsc_stabilizer* st : m->st)
+        if ((s = step_preconditions(st, m->hp)))
+            return s;
+    const size_t n = m->st.size();
+    std::vector<uint8_t*> outs(n);
+    for (size_t i = 0; i < n; ++i) {
+        outs[i] = (out && out[i] && out_on_device) ? out[i] : m->st[i]->out_rgba;
+        if (reinterpret_cast<uintptr_t>(outs[i]) & 3)
+            return set_error(VSC_EINVAL, "multistream_step: device output %zu not 4-byte aligned", i);
+    }
+    for (size_t i = 0; i < n; ++i)  // the frames just loaded are in place
+        if ((s = check_cuda(cudaStreamWaitEvent(m->main, m->loaded[i], 0), "multistream_step")))
+            return s;
+    int nl = 0;
+    cudaError_t e = cudaSuccess;
+    bool started = true;
+    for (vsc_stabilizer* st : m->st)
+        started = started && st->started;
+    if (!(started && ms_launch_graph(m, outs, &nl, &e)))
+        e = ms_enqueue(m, outs, &nl);
+    if ((s = check_cuda(e, "multistream_step")))
+        return s;
+    for (vsc_stabilizer* st : m->st)
+        finish_step(st, 0);
+    m->last_launches = nl;
+    if (out && !out_on_device) {
+        for (size_t i = 0; i < n; ++i)
+            if (out[i] &&
+                (s = check_cuda(cudaMemcpyAsync(out[i], outs[i], static_cast<size_t>(m->st[i]->w) * m->st[i]->h * 4,
+                                    cudaMemcpyDeviceToHost, m->main),
+                     "multistream_step download")))
+                return s;
+        return check_cuda(cudaStreamSynchronize(m->main), "multistream_step synchronize");
+    }
+    return VSC_OK;
+}
+
+}  // extern "C"
+

@@ -90,9 +90,12 @@ __host__ TcPlan tc_plan(int cp)
     return p;
 }
 
+// Base + stride, not arrays of pointers: indexed by run-time stage numbers,
+// arrays would live in local memory and every access would wait on it.
 struct TcShared {
-    unsigned char* a[kMaxStagesA];
-    unsigned char* b[kMaxStagesB];
+    unsigned char* a;  // stage i at a + i * a_stride
+    unsigned char* b;
+    uint32_t a_stride, b_stride;
     float* stage;
     uint64_t *full_a, *empty_a, *full_b, *empty_b, *full_d, *empty_d;
     uint32_t* tmem_slot;
@@ -108,8 +111,8 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, volatile
             return true;
         if ((i & 63) == 63 && *abort)
             return false;
-        if (i > 32)
-            __nanosleep(128);
+        if (i > 256)  // hand-offs are short: poll first, then back off
+            __nanosleep(64);
     }
     *abort = 1;
     return false;
@@ -134,10 +137,12 @@ __global__ void __launch_bounds__((2 + 4 * kMaxEpiGroups) * 32, 1)
     {
         unsigned char* p = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                             ~static_cast<uintptr_t>(1023));
-        for (int i = 0; i < stages_a; ++i, p += align1k(bytesA))
-            sh.a[i] = p;
-        for (int i = 0; i < stages_b; ++i, p += align1k(bytesB))
-            sh.b[i] = p;
+        sh.a_stride = align1k(bytesA);
+        sh.b_stride = align1k(bytesB);
+        sh.a = p;
+        p += stages_a * sh.a_stride;
+        sh.b = p;
+        p += stages_b * sh.b_stride;
         sh.stage = reinterpret_cast<float*>(p);
         uint64_t* bars = reinterpret_cast<uint64_t*>(p + groups * kTcGroupStageBytes);
         sh.full_a = bars;
@@ -195,14 +200,14 @@ __global__ void __launch_bounds__((2 + 4 * kMaxEpiGroups) * 32, 1)
                 if (!(ok = tc_wait(&sh.empty_a[sa], ((ua / stages_a) & 1) ^ 1, sh.abort)))
                     break;
                 ptx::mbar_expect_tx(&sh.full_a[sa], bytesA);
-                ptx::tma_load_5d(sh.a[sa], &mA, 0, x0, 0, y, n, &sh.full_a[sa]);
+                ptx::tma_load_5d(sh.a + sa * sh.a_stride, &mA, 0, x0, 0, y, n, &sh.full_a[sa]);
                 ++ua;
                 for (int d = d0; d < d1; ++d) {
                     const int sb = ub % stages_b;
                     if (!(ok = tc_wait(&sh.empty_b[sb], ((ub / stages_b) & 1) ^ 1, sh.abort)))
                         break;
                     ptx::mbar_expect_tx(&sh.full_b[sb], bytesB);
-                    ptx::tma_load_5d(sh.b[sb], &mB, 0, x0 - md, 0, y + d - md, n, &sh.full_b[sb]);
+                    ptx::tma_load_5d(sh.b + sb * sh.b_stride, &mB, 0, x0 - md, 0, y + d - md, n, &sh.full_b[sb]);
                     ++ub;
                 }
             }
@@ -235,7 +240,7 @@ __global__ void __launch_bounds__((2 + 4 * kMaxEpiGroups) * 32, 1)
                     if (!(ok = tc_wait(&sh.empty_d[sd], ((ud / kStagesD) & 1) ^ 1, sh.abort)))
                         break;
                     ptx::tc_fence_after();
-                    const uint32_t a0 = ptx::smem_u32(sh.a[sa]), b0 = ptx::smem_u32(sh.b[sb]);
+                    const uint32_t a0 = ptx::smem_u32(sh.a + sa * sh.a_stride), b0 = ptx::smem_u32(sh.b + sb * sh.b_stride);
                     const uint32_t dcol = tmem + sd * kDStride;
                     for (int kk = 0; kk < Cp / 16; ++kk) {
                         const uint64_t ad = ptx::umma_desc_kmajor(a0 + kk * 2 * kTcM * 16, kTcM * 16, 128);
