@@ -445,6 +445,8 @@ def run_multistream(args):
         s_ = synth.SyntheticStream(w, h, seed=100 + i, device=str(dev))
         frames.append([tuple(torch.from_numpy(a).to(dev) for a in s_.frame(t)) for t in range(n_unique)])
     torch.cuda.synchronize()
+    if kw.get("upsampler"):
+        raise SystemExit("the multistream workload has no learned-upsampler form")
     ms = vsc.MultiStream(MULTI_STREAMS, flow_downscale=kw["flow_downscale"], corr_dtype=kw["corr_dtype"],
                          stream=stream)
     outs = [torch.empty((h, w, 4), dtype=torch.uint8, device=dev) for w, h in MULTI_STREAMS]
@@ -539,6 +541,44 @@ def run_corr_only(args):
                       "total_ms": tot, "peak_gbs": peak, "peak_source": peak_src}))
 
 
+def run_front_only(args):
+    """--kernel front: vsc_stab_front (five warps + adaptive combination +
+    consistency weights in one pass) at 1920x1080, CUDA events on its stream.
+    Algorithmic bytes 124 B/px: two 3-channel flows (24 B), five warped
+    sources (60 B), the current original and processed frames (24 B), two
+    outputs (24 B); the inputs (258 MB) exceed L2, so no flush is needed."""
+    import torch
+
+    vsc = import_pkg()
+    vsc.build()
+    vsc.load()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    g = torch.Generator(device=dev).manual_seed(5)
+    ims = [torch.rand((H, W, 3), device=dev, generator=g) for _ in range(7)]
+    yy, xx = torch.meshgrid(torch.arange(H, device=dev), torch.arange(W, device=dev), indexing="ij")
+    ff = torch.stack([3 * torch.sin(xx / 97.0), 2 * torch.cos(yy / 83.0), torch.zeros_like(xx, dtype=torch.float32)],
+                     -1).float().contiguous()
+    fb = (-ff).contiguous()
+    apr, wt = torch.empty_like(ims[0]), torch.empty_like(ims[0])
+    peak, peak_src = peaks()
+    call = lambda: vsc.stab_front(ims[0:3], ims[3:6], ims[6], ff, fb, 6800.0, 6800.0, 2.0, out=(apr, wt),  # noqa: E731
+                                  stream=stream)
+    for _ in range(max(args.warmup, 3)):
+        call()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        call()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    alg = 124 * W * H
+    print(json.dumps({"kernel": "fused_front_kernel (vsc_stab_front) 1920x1080", "ms": ms,
+                      "achieved_gbs": alg / (ms / 1000) / 1e9, "peak_gbs": peak,
+                      "frac": alg / (ms / 1000) / 1e9 / peak, "algorithmic_bytes": alg, "peak_source": peak_src}))
+
+
 def run_solver_only(args):
     """--kernel solver: only the 1920x1080 solver (for profiler captures)."""
     import torch
@@ -566,7 +606,20 @@ FORMS = {
              "scale, FP32 accumulation); warps, mask and blend FP32"),
     "bf16_ds2": ({"corr_dtype": "bf16", "flow_downscale": 2},
                  "FLOWDOWNSCALE=2 (flow at 960x540, bilinear upsampling) with BF16 tensor-core Correlations"),
+    "bf16_ds2_learned": ({"corr_dtype": "bf16", "flow_downscale": 2, "upsampler": "default"},
+                         "FLOWDOWNSCALE=2 with BF16 tensor-core Correlations and the learned 2x flow upsampler "
+                         "(weights shipped with the package; bilinear fallback where its residual exceeds 0.5 px)"),
 }
+
+
+def make_stabilizer(vsc, kw, stream):
+    """A Stabilizer for a form; the learned upsampler, when the form has one,
+    is attached (and kept alive by the stabilizer)."""
+    args = {k: v for k, v in kw.items() if k != "upsampler"}
+    st = vsc.Stabilizer(W, H, stream=stream, **args)
+    if kw.get("upsampler"):
+        st.set_upsampler(vsc.Upsampler(kw["upsampler"]))
+    return st
 
 
 def time_form(vsc, kw, dev_frames, stream, steps, warmup, ws, dev, clocks=None):
@@ -576,7 +629,7 @@ def time_form(vsc, kw, dev_frames, stream, steps, warmup, ws, dev, clocks=None):
 
     n_frames = len(dev_frames)
     out_dev = torch.empty((H, W, 4), dtype=torch.uint8, device=dev)
-    st = vsc.Stabilizer(W, H, stream=stream, **kw)
+    st = make_stabilizer(vsc, kw, stream)
     for i in range(3):
         st.load_frame(*dev_frames[i])
     state = {"nxt": 3, "launches": 0}
@@ -616,7 +669,7 @@ def e2e_form(vsc, kw, pinned, stream, steps, warmup, ws, dev):
 
     n_frames = len(pinned)
     out_host = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory()
-    st = vsc.Stabilizer(W, H, stream=stream, **kw)
+    st = make_stabilizer(vsc, kw, stream)
     for i in range(3):
         st.load_frame(pinned[i][0].numpy(), pinned[i][1].numpy())
     nxt = [3]
@@ -646,7 +699,7 @@ def psnr_vs_plain(vsc, kw, dev_frames, stream, n_steps: int = 12):
     """Stabilized RGB of the form against the plain path, frame by frame."""
     import torch
 
-    sts = [vsc.Stabilizer(W, H, stream=stream, **FORMS["plain"][0]), vsc.Stabilizer(W, H, stream=stream, **kw)]
+    sts = [make_stabilizer(vsc, FORMS["plain"][0], stream), make_stabilizer(vsc, kw, stream)]
     for st in sts:
         for i in range(3):
             st.load_frame(*dev_frames[i])
@@ -763,7 +816,7 @@ def main():
                     help="multistream: the 16-stream mixed-resolution workload (a separate line)")
     ap.add_argument("--form", choices=sorted(FORMS), default="bf16_ds2",
                     help="the chosen form reported as value (the plain path is timed beside it)")
-    ap.add_argument("--kernel", choices=["step", "solver", "corr"], default="step",
+    ap.add_argument("--kernel", choices=["step", "solver", "corr", "front"], default="step",
                     help="solver / corr: time only the 1920x1080 solver or the correlation pyramid "
                          "(profiler targets)")
     args = ap.parse_args()
@@ -777,6 +830,8 @@ def main():
         run_solver_only(args)
     elif args.kernel == "corr":
         run_corr_only(args)
+    elif args.kernel == "front":
+        run_front_only(args)
     else:
         run_gpu(args)
 

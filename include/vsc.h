@@ -183,6 +183,26 @@ VSC_API vsc_status vsc_get_adap_comb_masked(const vsc_image* crnt_in, const vsc_
     const vsc_image* next_warp_pr, const vsc_image* adap_cmb_in, const vsc_image* adap_cmb_pr,
     const vsc_image* last_stab_warp, const vsc_image* occ_mask, float alpha, vsc_stream_t stream);
 
+/* The library's flow estimator on one frame pair (what FlowModel::run
+ * provides in compute mode, flowmodel.cpp:121-168, here built from the two
+ * ops): img_a, img_b float HWC3 in [0, 1]; flow_ab (a -> b) and flow_ba
+ * (b -> a) HWC3 (u, v, 0) of the same size.  Workspace from the library's
+ * stream-ordered pool. */
+VSC_API vsc_status vsc_flow_estimate(const vsc_image* img_a, const vsc_image* img_b, const vsc_image* flow_ab,
+    const vsc_image* flow_ba, vsc_stream_t stream);
+
+/* The front half of doOneStep (videostabilizer.cpp:182-198) in one pass:
+ * the five get_warp_result calls (previous original and processed frames and
+ * the last stabilized frame along flow_bwd, next original and processed
+ * frames along flow_fwd), get_adap_comb and get_consist_wt, writing only
+ * adapCmbPr and consWt (the intermediates never reach memory).  Results
+ * equal the separate calls bit for bit; occlusion_mask != 0 applies the
+ * opt-in forward-backward mask.  No single counterpart in the reference. */
+VSC_API vsc_status vsc_stab_front(const vsc_image* orig_prev, const vsc_image* orig_cur, const vsc_image* orig_next,
+    const vsc_image* proc_prev, const vsc_image* proc_cur, const vsc_image* proc_next, const vsc_image* last_stab,
+    const vsc_image* flow_fwd, const vsc_image* flow_bwd, const vsc_image* adap_cmb_pr, const vsc_image* consis_wt,
+    float alpha, float beta, float gamma, int32_t occlusion_mask, vsc_stream_t stream);
+
 /* Consistency weights gamma*exp(-beta*(I - adapCmbIn)^2), < 0.001 -> 0.
  * Replaces get_consist_wt / kernel_consist_wt (flowconsistency.cu:168-191, :335-348). */
 VSC_API vsc_status vsc_get_consist_wt(const vsc_image* adap_cmb_in, const vsc_image* crnt_in,
@@ -319,6 +339,39 @@ VSC_API vsc_status vsc_stabilizer_enable_timing(vsc_stabilizer* s, int32_t on);
  * weights + pyramid, ms[3] coarse pyramid levels of the solve, ms[4]
  * full-resolution solve and RGBA8 output; n >= 5.  Synchronises the stream. */
 VSC_API vsc_status vsc_stabilizer_stage_ms(vsc_stabilizer* s, float* ms, int32_t n);
+
+/* ---- learned flow upsampler (no counterpart in the reference) ----------------
+ * For the FLOWDOWNSCALE = 2 fast mode: a 4-layer 3x3 convolutional net
+ * (3 -> 32 -> 32 -> 32 -> 2 channels, ReLU between, 19,970 parameters)
+ * predicts a residual r on top of the bilinearly upsampled coarse flow with
+ * its vectors scaled to the full-resolution grid ("base"), from the base
+ * flow and the frame's luma; output = base + r where max(|r_u|, |r_v|) <=
+ * the maximum residual (0.5 px by default), else base.  Trained by
+ * vsc_upsampler_train_step (L1 loss against the full-resolution flow, Adam);
+ * inference rounds the weights to FP16.  Parameter order: per layer the
+ * weights [out][ky][kx][in], then the biases. */
+typedef struct vsc_upsampler vsc_upsampler;
+VSC_API int32_t vsc_upsampler_param_count(void);
+/* params: host array of vsc_upsampler_param_count floats, or NULL for a
+ * seeded initialisation (the last layer near zero: output = base). */
+VSC_API vsc_status vsc_upsampler_create(const float* params, vsc_upsampler** out);
+VSC_API vsc_status vsc_upsampler_destroy(vsc_upsampler* u);
+VSC_API vsc_status vsc_upsampler_get_params(vsc_upsampler* u, float* host_params);
+VSC_API vsc_status vsc_upsampler_set_max_residual(vsc_upsampler* u, float px);
+/* input (frame size, 3 channels): base u, base v, luma. */
+VSC_API vsc_status vsc_upsampler_prepare(const vsc_image* coarse_flow, const vsc_image* frame, const vsc_image* input,
+    vsc_stream_t stream);
+/* One Adam step on a batch: input n x h x w x 3 (from vsc_upsampler_prepare),
+ * target n x h x w x 2 (the full-resolution flow), device pointers; the
+ * batch's mean L1 loss in *loss_out (synchronises) when non-null. */
+VSC_API vsc_status vsc_upsampler_train_step(vsc_upsampler* u, const float* input, const float* target, int32_t n,
+    int32_t h, int32_t w, float lr, float* loss_out, vsc_stream_t stream);
+/* flow_out (frame size, 3 channels (u, v, 0)) from a coarse flow and the frame. */
+VSC_API vsc_status vsc_upsampler_apply(vsc_upsampler* u, const vsc_image* coarse_flow, const vsc_image* frame,
+    const vsc_image* flow_out, vsc_stream_t stream);
+/* Use u instead of bilinear upsampling in a stabilizer with flow_downscale > 1
+ * (NULL: back to bilinear, the reference's fast mode). */
+VSC_API vsc_status vsc_stabilizer_set_upsampler(vsc_stabilizer* s, vsc_upsampler* u);
 
 /* ---- several streams per frame step (no counterpart in the reference) -------
  * Stabilizes n independent videos of any sizes in lockstep: each step runs

@@ -413,3 +413,39 @@ def test_multistream_equals_independent_stabilizers(vsc, cuda):
     ms.close()
     for st in singles:
         st.close()
+
+
+@pytest.mark.parametrize("fc,occ", [(3, False), (2, False), (2, True)])
+def test_stab_front_equals_separate_calls(vsc, oracle, cuda, fc, occ):
+    """vsc_stab_front (five warps + combination + weights in one pass) equals
+    the separate entry points bit for bit; with the occlusion mask, the
+    restatement's masked combination."""
+    h, w = 53, 77
+    base = _img(h, w)
+    ims = [np.clip(base + RNG.normal(0, s_, base.shape), 0, 1).astype(np.float32)
+           for s_ in (0.03, 0.0, 0.02, 0.02, 0.01, 0.03, 0.01)]
+    o3, p3, ls = ims[0:3], ims[3:6], ims[6]
+    ff = (RNG.normal(0, 2, (h, w, fc))).astype(np.float32)
+    fb = (-ff + RNG.normal(0, 0.4, ff.shape)).astype(np.float32)
+    d = lambda a: _t(a, cuda)  # noqa: E731
+    apr, wt = vsc.stab_front([d(a) for a in o3], [d(a) for a in p3], d(ls), d(ff), d(fb), 20.0, 30.0, 2.0,
+                             occlusion_mask=occ)
+    warps = [oracle.stab_warp(src, fl) for src, fl in ((o3[0], fb), (p3[0], fb), (o3[2], ff), (p3[2], ff),
+                                                       (ls, fb))]
+    if occ:
+        m = oracle.flow_consistency_mask(ff, fb)
+        ain, rpr = oracle.adap_comb_masked(o3[1], p3[1], warps[0], warps[1], warps[2], warps[3], warps[4], m, 20.0)
+    else:
+        ain, rpr = oracle.adap_comb(o3[1], p3[1], warps[0], warps[1], warps[2], warps[3], warps[4], 20.0)
+    rwt = oracle.consist_wt(o3[1], ain, 30.0, 2.0)
+    assert np.array_equal(apr.cpu().numpy(), rpr)
+    assert np.array_equal(wt.cpu().numpy(), rwt)
+
+
+def test_flow_estimate_equals_restatement(vsc, oracle, cuda):
+    w, h = 112, 80
+    fr = _frames(w, h, 2, seed=61)
+    a, b = [oracle.rgba_to_float(o) for o, _ in fr]
+    ab, ba = vsc.flow_estimate(_t(a, cuda), _t(b, cuda))
+    assert np.array_equal(ab.cpu().numpy(), oracle.flow_estimate(a, b))
+    assert np.array_equal(ba.cpu().numpy(), oracle.flow_estimate(b, a))

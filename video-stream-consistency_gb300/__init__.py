@@ -40,7 +40,10 @@ EXPORTED = [
     "vsc_image_file_info", "vsc_read_image_file", "vsc_write_png", "vsc_flo_info", "vsc_read_flo", "vsc_write_flo",
     "vsc_stabilize_files", "vsc_solver_steps_per_launch",
     "vsc_multistream_create", "vsc_multistream_destroy", "vsc_multistream_hyper_params", "vsc_multistream_load_frames",
-    "vsc_multistream_step", "vsc_multistream_last_launches",
+    "vsc_multistream_step", "vsc_multistream_last_launches", "vsc_stab_front", "vsc_flow_estimate",
+    "vsc_upsampler_param_count", "vsc_upsampler_create", "vsc_upsampler_destroy", "vsc_upsampler_get_params",
+    "vsc_upsampler_set_max_residual", "vsc_upsampler_prepare", "vsc_upsampler_train_step", "vsc_upsampler_apply",
+    "vsc_stabilizer_set_upsampler",
 ]
 VSC_DTYPE_F32, VSC_DTYPE_BF16, VSC_DTYPE_F16 = 0, 1, 2
 NOALLOC_MAX_PIXELS = 349525  # VSC_NOALLOC_MAX_PIXELS
@@ -136,6 +139,16 @@ def load():
         "vsc_stabilizer_buffer": [vp, i32, C.POINTER(vp)],
         "vsc_stabilizer_enable_timing": [vp, i32],
         "vsc_get_flow_consistency_mask": [IP, IP, IP, vp],
+        "vsc_stab_front": [IP] * 11 + [f32, f32, f32, i32, vp],
+        "vsc_flow_estimate": [IP, IP, IP, IP, vp],
+        "vsc_upsampler_create": [vp, C.POINTER(vp)],
+        "vsc_upsampler_destroy": [vp],
+        "vsc_upsampler_get_params": [vp, vp],
+        "vsc_upsampler_set_max_residual": [vp, f32],
+        "vsc_upsampler_prepare": [IP, IP, IP, vp],
+        "vsc_upsampler_train_step": [vp, vp, vp, i32, i32, i32, f32, C.POINTER(f32), vp],
+        "vsc_upsampler_apply": [vp, IP, IP, IP, vp],
+        "vsc_stabilizer_set_upsampler": [vp, vp],
         "vsc_image_file_info": [C.c_char_p, C.POINTER(i32), C.POINTER(i32)],
         "vsc_read_image_file": [C.c_char_p, vp, i32, i32],
         "vsc_write_png": [C.c_char_p, vp, i32, i32],
@@ -156,6 +169,8 @@ def load():
         f = getattr(L, fn)
         f.argtypes = args
         f.restype = C.c_int
+    L.vsc_upsampler_param_count.restype = i32
+    L.vsc_upsampler_param_count.argtypes = []
     L.vsc_multistream_hyper_params.restype = C.POINTER(HyperParams)
     L.vsc_multistream_hyper_params.argtypes = [vp]
     L.vsc_multistream_last_launches.restype = i32
@@ -342,6 +357,29 @@ def get_adap_comb_masked(crnt_in, crnt_pr, prev_in, prev_pr, next_in, next_pr, l
     return ain, apr
 
 
+def flow_estimate(img_a, img_b, stream=None):
+    """Forward and backward flow (HWC3 (u, v, 0)) of two float HWC3 frames."""
+    import torch
+
+    ab, ba = torch.empty_like(img_a), torch.empty_like(img_a)
+    _check(load().vsc_flow_estimate(C.byref(image(img_a)), C.byref(image(img_b)), C.byref(image(ab)),
+                                    C.byref(image(ba)), _stream(stream)))
+    return ab, ba
+
+
+def stab_front(orig3, proc3, last_stab, flow_fwd, flow_bwd, alpha, beta, gamma, occlusion_mask=False, out=None,
+               stream=None):
+    """Five warps + adaptive combination + consistency weights in one pass;
+    returns (adapCmbPr, consWt)."""
+    import torch
+
+    apr, wt = out if out is not None else (torch.empty_like(orig3[1]), torch.empty_like(orig3[1]))
+    ims = [image(t) for t in (*orig3, *proc3, last_stab, flow_fwd, flow_bwd, apr, wt)]
+    _check(load().vsc_stab_front(*[C.byref(i) for i in ims], float(alpha), float(beta), float(gamma),
+                                 1 if occlusion_mask else 0, _stream(stream)))
+    return apr, wt
+
+
 def get_consist_wt(adap_in, crnt_in, beta, gamma, stream=None):
     import torch
 
@@ -522,6 +560,12 @@ class Stabilizer:
         """Opt-in forward-backward flow consistency mask on the temporal weights."""
         _check(load().vsc_stabilizer_set_occlusion_mask(self._h, 1 if on else 0))
 
+    def set_upsampler(self, upsampler: "Upsampler | None"):
+        """Learned flow upsampling (flow_downscale > 1); None: bilinear.  The
+        stabilizer keeps a reference for as long as it uses it."""
+        self._upsampler = upsampler
+        _check(load().vsc_stabilizer_set_upsampler(self._h, upsampler._h if upsampler is not None else None))
+
     def enable_timing(self, on: bool = True):
         _check(load().vsc_stabilizer_enable_timing(self._h, 1 if on else 0))
 
@@ -603,6 +647,78 @@ class MultiStream:
     def close(self):
         if getattr(self, "_h", None):
             load().vsc_multistream_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
+
+
+UPSAMPLER_WEIGHTS = PKG_DIR / "upsampler_weights.npz"
+
+
+class Upsampler:
+    """Learned 2x flow upsampler (vsc_upsampler_*): params None for the
+    seeded initialisation, "default" for the weights shipped with the
+    package, or an array of vsc_upsampler_param_count floats."""
+
+    def __init__(self, params=None):
+        import numpy as np
+
+        if isinstance(params, str) and params == "default":
+            params = np.load(UPSAMPLER_WEIGHTS)["params"]
+        arr = None if params is None else np.ascontiguousarray(params, dtype=np.float32)
+        if arr is not None and arr.size != self.param_count():
+            raise ValueError(f"expected {self.param_count()} parameters, got {arr.size}")
+        h = C.c_void_p()
+        _check(load().vsc_upsampler_create(None if arr is None else arr.ctypes.data, C.byref(h)))
+        self._h = h
+
+    @staticmethod
+    def param_count() -> int:
+        return int(load().vsc_upsampler_param_count())
+
+    def params(self):
+        import numpy as np
+
+        out = np.empty(self.param_count(), np.float32)
+        _check(load().vsc_upsampler_get_params(self._h, out.ctypes.data))
+        return out
+
+    def set_max_residual(self, px: float):
+        _check(load().vsc_upsampler_set_max_residual(self._h, float(px)))
+
+    @staticmethod
+    def prepare(coarse_flow, frame, stream=None):
+        """(h, w, 3) input: base flow (bilinear, vectors scaled) and luma."""
+        import torch
+
+        out = torch.empty_like(frame)
+        _check(load().vsc_upsampler_prepare(C.byref(image(coarse_flow)), C.byref(image(frame)), C.byref(image(out)),
+                                            _stream(stream)))
+        return out
+
+    def train_step(self, inputs, targets, lr: float, stream=None) -> float:
+        """inputs (n, h, w, 3), targets (n, h, w, 2): CUDA float32; returns the batch loss."""
+        n, h, w, _ = inputs.shape
+        loss = C.c_float()
+        _check(load().vsc_upsampler_train_step(self._h, inputs.data_ptr(), targets.data_ptr(), n, h, w, float(lr),
+                                               C.byref(loss), _stream(stream)))
+        return loss.value
+
+    def apply(self, coarse_flow, frame, stream=None):
+        import torch
+
+        out = torch.empty_like(frame)
+        _check(load().vsc_upsampler_apply(self._h, C.byref(image(coarse_flow)), C.byref(image(frame)),
+                                          C.byref(image(out)), _stream(stream)))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().vsc_upsampler_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -355,6 +355,77 @@ VSC_API vsc_status vsc_get_flow_consistency_mask(const vsc_image* flow_fwd, cons
         "flow_consistency_mask launch");
 }
 
+VSC_API vsc_status vsc_flow_estimate(const vsc_image* img_a, const vsc_image* img_b, const vsc_image* flow_ab,
+    const vsc_image* flow_ba, vsc_stream_t stream)
+{
+    clear_error();
+    vsc_status s;
+    if ((s = check_image(img_a, "imgA", 3, 3)) || (s = check_image(img_b, "imgB", 3, 3)) ||
+        (s = check_image(flow_ab, "flowAB", 3, 3)) || (s = check_image(flow_ba, "flowBA", 3, 3)) ||
+        (s = same_size(img_a, img_b, "imgB")) || (s = same_size(img_a, flow_ab, "flowAB")) ||
+        (s = same_size(img_a, flow_ba, "flowBA")))
+        return s;
+    const int w = img_a->width, h = img_a->height;
+    if (w < 8 || h < 8)
+        return set_error(VSC_EINVAL, "flow_estimate: image must be at least 8x8");
+    cudaStream_t st = cs(stream);
+    const FlowDims d = flow_dims(w, h);
+    if ((s = check_cuda(flow_upload_weights(), "flow_estimate weights")))
+        return s;
+    // two feature pyramids (contiguous: the pair addresses them as a strided
+    // batch), the feature scratch, the pair's scratch and the two flows
+    const size_t nf = d.feat_floats, nfs = flow_feature_scratch_floats(d), nps = 2 * flow_estimate_scratch_floats(d);
+    const size_t n3 = static_cast<size_t>(w) * h * 3;
+    void* ws = nullptr;
+    if ((s = check_cuda(pool_alloc(&ws, (2 * nf + nfs + nps + 2 * n3) * sizeof(float), st), "flow_estimate workspace")))
+        return s;
+    float* fa = static_cast<float*>(ws);
+    float* fb = fa + nf;
+    float* fsc = fb + nf;
+    float* psc = fsc + nfs;
+    float* flows = psc + nps;
+    cudaError_t e = launch_flow_features(img_a->data, w, h, d, fa, fsc, st, nullptr);
+    if (e == cudaSuccess)
+        e = launch_flow_features(img_b->data, w, h, d, fb, fsc, st, nullptr);
+    if (e == cudaSuccess)
+        e = launch_flow_pair(fa, fb - fa, fb, fa - fb, w, h, d, flows, static_cast<int64_t>(n3), psc, st, nullptr);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(flow_ab->data, flows, n3 * sizeof(float), cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(flow_ba->data, flows + n3, n3 * sizeof(float), cudaMemcpyDeviceToDevice, st);
+    cudaFreeAsync(ws, st);
+    return check_cuda(e, "flow_estimate");
+}
+
+VSC_API vsc_status vsc_stab_front(const vsc_image* orig_prev, const vsc_image* orig_cur, const vsc_image* orig_next,
+    const vsc_image* proc_prev, const vsc_image* proc_cur, const vsc_image* proc_next, const vsc_image* last_stab,
+    const vsc_image* flow_fwd, const vsc_image* flow_bwd, const vsc_image* adap_cmb_pr, const vsc_image* consis_wt,
+    float alpha, float beta, float gamma, int32_t occlusion_mask, vsc_stream_t stream)
+{
+    clear_error();
+    const vsc_image* im[9] = {orig_prev, orig_cur, orig_next, proc_prev, proc_cur, proc_next, last_stab, adap_cmb_pr,
+        consis_wt};
+    static const char* names[9] = {"origPrev", "origCur", "origNext", "procPrev", "procCur", "procNext", "lastStab",
+        "adapCmbPr", "consisWt"};
+    vsc_status s;
+    for (int i = 0; i < 9; ++i)
+        if ((s = check_image(im[i], names[i], 3, 3)) || (s = same_size(orig_cur, im[i], names[i])))
+            return s;
+    if ((s = check_image(flow_fwd, "flowFwd", 2, 3)) || (s = check_image(flow_bwd, "flowBwd", 2, 3)) ||
+        (s = same_size(orig_cur, flow_fwd, "flowFwd")) || (s = same_size(orig_cur, flow_bwd, "flowBwd")))
+        return s;
+    if (flow_fwd->channels != flow_bwd->channels)
+        return set_error(VSC_EINVAL, "stab_front: flows have %d and %d channels", flow_fwd->channels,
+            flow_bwd->channels);
+    if (orig_cur->width < 3 || orig_cur->height < 3)
+        return set_error(VSC_EINVAL, "stab_front: image must be at least 3x3");
+    return check_cuda(launch_fused_front(orig_prev->data, orig_cur->data, orig_next->data, proc_prev->data,
+                          proc_cur->data, proc_next->data, last_stab->data, flow_fwd->data, flow_bwd->data,
+                          flow_fwd->channels, adap_cmb_pr->data, consis_wt->data, orig_cur->width, orig_cur->height,
+                          alpha, beta, gamma, cs(stream), occlusion_mask != 0),
+        "stab_front launch");
+}
+
 VSC_API vsc_status vsc_get_consist_wt(const vsc_image* adap_cmb_in, const vsc_image* crnt_in,
     const vsc_image* consis_wt, float beta, float gamma, vsc_stream_t stream)
 {
@@ -531,6 +602,9 @@ struct vsc_stabilizer {
     FlowDims fd{};
     int last_launches = 0;
     bool occlusion = false;  // opt-in forward-backward consistency mask
+    // learned flow upsampling (flow_downscale > 1); null: bilinear
+    vsc_upsampler* upsampler = nullptr;
+    float* up_work = nullptr;  // input (2 x w x h x 3), activations, residual
     // stage timing (off by default): events around load_frame and the stages of a step
     bool timing = false;
     cudaEvent_t ev[7] = {};
@@ -543,6 +617,7 @@ struct vsc_stabilizer {
         uint8_t* rgba = nullptr;
         vsc_hyper_params hp{};
         bool timing = false, occlusion = false;
+        const vsc_upsampler* upsampler = nullptr;
         cudaGraphExec_t exec = nullptr;
         uint64_t used = 0;
     } graphs[8];
@@ -614,6 +689,7 @@ void free_all(vsc_stabilizer* s)
     f(s->feat_tc[0]);
     f(s->warped_tc);
     f(s->tc_scales);
+    f(s->up_work);
     for (cudaEvent_t& e : s->ev)
         if (e) {
             cudaEventDestroy(e);
@@ -848,6 +924,54 @@ VSC_API vsc_status vsc_stabilizer_set_flows(vsc_stabilizer* s, const float* fwd,
 namespace {
 
 // All device work of one doOneStep, enqueued on the stabilizer's stream.
+// ---- learned flow upsampler state -----------------------------------------------------
+}  // namespace
+struct vsc_upsampler {
+    int device = 0;
+    float* prm = nullptr;  // FP32 master parameters
+    float* grad = nullptr;
+    float* m = nullptr;
+    float* v = nullptr;
+    __half* w16 = nullptr;  // FP16 copy used by inference
+    bool w16_valid = false;
+    int step = 0;
+    float* work = nullptr;
+    size_t work_floats = 0;
+    float* loss = nullptr;
+    float max_residual = 0.5f;
+};
+namespace {
+
+cudaError_t upsampler_sync_half(vsc_upsampler* u, cudaStream_t st)
+{
+    if (u->w16_valid)
+        return cudaSuccess;
+    cudaError_t e = launch_to_half(u->prm, u->w16, upsampler_param_count(), st);
+    u->w16_valid = e == cudaSuccess;
+    return e;
+}
+
+// both flows of a step: coarse flows (fw x fh) -> full-size flows
+cudaError_t upsampler_apply_pair(vsc_stabilizer* s, cudaStream_t st, int* nl)
+{
+    const int64_t npx = static_cast<int64_t>(s->w) * s->h;
+    const int64_t fs = static_cast<int64_t>(s->fw) * s->fh * 3;
+    float* input = s->up_work;
+    float* act = input + 2 * npx * 3;
+    float* r = act + upsampler_act_floats(2, s->h, s->w) - 2 * npx * 2;
+    cudaError_t e = upsampler_sync_half(s->upsampler, st);
+    if (e == cudaSuccess)
+        e = launch_upsampler_prepare(s->flow_small, s->fw, s->fh, 3, s->orig[(s->head + 1) % 3], input, s->w, s->h, 2,
+            fs, s->orig[(s->head + 2) % 3] - s->orig[(s->head + 1) % 3], npx * 3, st);
+    if (e == cudaSuccess)
+        e = launch_upsampler_forward_half(s->upsampler->w16, s->upsampler->prm, input, act, r, 2, s->h, s->w, st);
+    if (e == cudaSuccess)
+        e = launch_upsampler_finish(input, r, s->flow_fwd, 2, npx, s->upsampler->max_residual, npx * 3, npx * 2,
+            s->flow_bwd - s->flow_fwd, st);
+    *nl += 6;
+    return e;
+}
+
 cudaError_t enqueue_step(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t* rgba_dev, int* launches)
 {
     const int L = hp.pyramid_levels;
@@ -885,7 +1009,11 @@ cudaError_t enqueue_step(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t*
         run(launch_flow_pair(s->feat[s1], s->feat[s2] - s->feat[s1], s->feat[s2], s->feat[s1] - s->feat[s2], s->fw,
             s->fh, s->fd, small ? s->flow_small : s->flow_fwd, small ? fs : s->flow_bwd - s->flow_fwd,
             s->flow_scratch, st, &nl, s->corr_dtype != VSC_DTYPE_F32 ? &tc : nullptr));
-        if (small) {
+        if (small && s->upsampler) {
+            // learned upsampling of both flows in one batch (the luma of
+            // frame t for the forward flow, of frame t+1 for the backward one)
+            run(upsampler_apply_pair(s, st, &nl));
+        } else if (small) {
             // flowmodel.cpp:158-161: bilinear upsampling, vectors not rescaled
             run(launch_bilinear(Img{s->flow_small, s->fw, s->fh, 3}, Img{s->flow_fwd, s->w, s->h, 3}, st));
             run(launch_bilinear(Img{s->flow_small + fs, s->fw, s->fh, 3}, Img{s->flow_bwd, s->w, s->h, 3}, st));
@@ -950,7 +1078,7 @@ bool launch_step_graph(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t* r
     auto* hit = static_cast<vsc_stabilizer::GraphEntry*>(nullptr);
     for (auto& g : s->graphs)
         if (g.valid && g.head == s->head && g.ls_cur == s->ls_cur && g.rgba == rgba_dev && g.timing == s->timing &&
-            g.occlusion == s->occlusion && same_hp(g.hp, hp))
+            g.occlusion == s->occlusion && g.upsampler == s->upsampler && same_hp(g.hp, hp))
             hit = &g;
     if (!hit) {
         auto* slot = &s->graphs[0];
@@ -989,6 +1117,7 @@ bool launch_step_graph(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t* r
         slot->rgba = rgba_dev;
         slot->timing = s->timing;
         slot->occlusion = s->occlusion;
+        slot->upsampler = s->upsampler;
         slot->hp = hp;
         slot->nl = nl;
         hit = slot;
@@ -1098,6 +1227,179 @@ VSC_API vsc_status vsc_stabilizer_buffer(vsc_stabilizer* s, int32_t which, const
 }
 
 VSC_API int32_t vsc_stabilizer_last_launches(vsc_stabilizer* s) { return s ? s->last_launches : 0; }
+
+VSC_API int32_t vsc_upsampler_param_count(void) { return upsampler_param_count(); }
+
+VSC_API vsc_status vsc_upsampler_create(const float* params, vsc_upsampler** out)
+{
+    clear_error();
+    if (!out)
+        return set_error(VSC_EINVAL, "upsampler_create: null argument");
+    *out = nullptr;
+    vsc_upsampler* u = new (std::nothrow) vsc_upsampler();
+    if (!u)
+        return set_error(VSC_ENOMEM, "upsampler_create: out of host memory");
+    cudaGetDevice(&u->device);
+    const int n = upsampler_param_count();
+    std::vector<float> host(n);
+    if (params)
+        std::memcpy(host.data(), params, n * sizeof(float));
+    else
+        upsampler_init_params(host.data(), 0x55505341'4D504C45ULL);  // seeded He-uniform
+    cudaError_t e = dalloc(&u->prm, n);
+    if (e == cudaSuccess)
+        e = dalloc(&u->grad, n);
+    if (e == cudaSuccess)
+        e = dalloc(&u->m, n);
+    if (e == cudaSuccess)
+        e = dalloc(&u->v, n);
+    if (e == cudaSuccess)
+        e = dalloc(&u->w16, n);
+    if (e == cudaSuccess)
+        e = dalloc(&u->loss, 1);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(u->prm, host.data(), n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemset(u->m, 0, n * sizeof(float));
+    if (e == cudaSuccess)
+        e = cudaMemset(u->v, 0, n * sizeof(float));
+    if (e != cudaSuccess) {
+        vsc_upsampler_destroy(u);
+        return check_cuda(e, "upsampler_create");
+    }
+    *out = u;
+    return VSC_OK;
+}
+
+VSC_API vsc_status vsc_upsampler_destroy(vsc_upsampler* u)
+{
+    if (!u)
+        return VSC_OK;
+    DeviceGuard g(u->device);
+    cudaDeviceSynchronize();
+    for (void* p : {static_cast<void*>(u->prm), static_cast<void*>(u->grad), static_cast<void*>(u->m),
+             static_cast<void*>(u->v), static_cast<void*>(u->w16), static_cast<void*>(u->work),
+             static_cast<void*>(u->loss)})
+        if (p)
+            cudaFree(p);
+    delete u;
+    return VSC_OK;
+}
+
+VSC_API vsc_status vsc_upsampler_get_params(vsc_upsampler* u, float* host_params)
+{
+    clear_error();
+    if (!u || !host_params)
+        return set_error(VSC_EINVAL, "upsampler_get_params: null argument");
+    DeviceGuard g(u->device);
+    return check_cuda(cudaMemcpy(host_params, u->prm, upsampler_param_count() * sizeof(float), cudaMemcpyDeviceToHost),
+        "upsampler_get_params");
+}
+
+VSC_API vsc_status vsc_upsampler_set_max_residual(vsc_upsampler* u, float px)
+{
+    clear_error();
+    if (!u || !(px >= 0.0f))
+        return set_error(VSC_EINVAL, "upsampler_set_max_residual: bad argument");
+    u->max_residual = px;
+    return VSC_OK;
+}
+
+VSC_API vsc_status vsc_upsampler_prepare(const vsc_image* coarse_flow, const vsc_image* frame, const vsc_image* input,
+    vsc_stream_t stream)
+{
+    clear_error();
+    vsc_status s;
+    if ((s = check_image(coarse_flow, "coarseFlow", 2, 3)) || (s = check_image(frame, "frame", 3, 3)) ||
+        (s = check_image(input, "input", 3, 3)) || (s = same_size(frame, input, "input")))
+        return s;
+    return check_cuda(launch_upsampler_prepare(coarse_flow->data, coarse_flow->width, coarse_flow->height,
+                          coarse_flow->channels, frame->data, input->data, frame->width, frame->height, 1, 0, 0, 0,
+                          cs(stream)),
+        "upsampler_prepare");
+}
+
+VSC_API vsc_status vsc_upsampler_train_step(vsc_upsampler* u, const float* input, const float* target, int32_t n,
+    int32_t h, int32_t w, float lr, float* loss_out, vsc_stream_t stream)
+{
+    clear_error();
+    if (!u || !input || !target || n < 1 || h < 1 || w < 1 || n > 65535 || static_cast<int64_t>(n) * h * w > (1 << 26))
+        return set_error(VSC_EINVAL, "upsampler_train_step: bad arguments");
+    DeviceGuard g(u->device);
+    cudaStream_t st = cs(stream);
+    const size_t need = upsampler_train_work_floats(n, h, w);
+    if (need > u->work_floats) {
+        cudaStreamSynchronize(st);
+        if (u->work)
+            cudaFree(u->work);
+        u->work = nullptr;
+        u->work_floats = 0;
+        vsc_status s = check_cuda(dalloc(&u->work, need), "upsampler_train_step workspace");
+        if (s)
+            return s;
+        u->work_floats = need;
+    }
+    u->w16_valid = false;
+    vsc_status s = check_cuda(upsampler_train_step(u->prm, u->grad, u->m, u->v, ++u->step, input, target, n, h, w, lr,
+                                  u->work, u->loss, st),
+        "upsampler_train_step");
+    if (s || !loss_out)
+        return s;
+    s = check_cuda(cudaMemcpyAsync(loss_out, u->loss, sizeof(float), cudaMemcpyDeviceToHost, st), "upsampler loss");
+    return s ? s : check_cuda(cudaStreamSynchronize(st), "upsampler loss");
+}
+
+VSC_API vsc_status vsc_upsampler_apply(vsc_upsampler* u, const vsc_image* coarse_flow, const vsc_image* frame,
+    const vsc_image* flow_out, vsc_stream_t stream)
+{
+    clear_error();
+    vsc_status s;
+    if (!u)
+        return set_error(VSC_EINVAL, "upsampler_apply: null upsampler");
+    if ((s = check_image(coarse_flow, "coarseFlow", 2, 3)) || (s = check_image(frame, "frame", 3, 3)) ||
+        (s = check_image(flow_out, "flowOut", 3, 3)) || (s = same_size(frame, flow_out, "flowOut")))
+        return s;
+    DeviceGuard g(u->device);
+    cudaStream_t st = cs(stream);
+    const int w = frame->width, h = frame->height;
+    const int64_t npx = static_cast<int64_t>(w) * h;
+    void* ws = nullptr;
+    if ((s = check_cuda(pool_alloc(&ws, (npx * 3 + upsampler_act_floats(1, h, w)) * sizeof(float), st),
+             "upsampler_apply workspace")))
+        return s;
+    float* input = static_cast<float*>(ws);
+    float* act = input + npx * 3;
+    float* r = act + npx * 96;
+    cudaError_t e = upsampler_sync_half(u, st);
+    if (e == cudaSuccess)
+        e = launch_upsampler_prepare(coarse_flow->data, coarse_flow->width, coarse_flow->height, coarse_flow->channels,
+            frame->data, input, w, h, 1, 0, 0, 0, st);
+    if (e == cudaSuccess)
+        e = launch_upsampler_forward_half(u->w16, u->prm, input, act, r, 1, h, w, st);
+    if (e == cudaSuccess)
+        e = launch_upsampler_finish(input, r, flow_out->data, 1, npx, u->max_residual, 0, 0, 0, st);
+    cudaFreeAsync(ws, st);
+    return check_cuda(e, "upsampler_apply");
+}
+
+VSC_API vsc_status vsc_stabilizer_set_upsampler(vsc_stabilizer* s, vsc_upsampler* u)
+{
+    clear_error();
+    if (!s)
+        return set_error(VSC_EINVAL, "set_upsampler: null stabilizer");
+    if (u && !(s->compute_flow && s->downscale > 1))
+        return set_error(VSC_ESTATE, "set_upsampler: the stabilizer computes no downscaled flow");
+    DeviceGuard g(s->device);
+    if (u && !s->up_work) {
+        const size_t npx = static_cast<size_t>(s->w) * s->h;
+        vsc_status st = check_cuda(dalloc(&s->up_work, 2 * npx * 3 + upsampler_act_floats(2, s->h, s->w)),
+            "set_upsampler workspace");
+        if (st)
+            return st;
+    }
+    s->upsampler = u;
+    return VSC_OK;
+}
 
 VSC_API vsc_status vsc_stabilizer_set_occlusion_mask(vsc_stabilizer* s, int32_t on)
 {

@@ -5,6 +5,7 @@
 // given stream, returning the launch error.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
@@ -53,6 +54,24 @@ cudaError_t launch_to_chunked(const float* in, void* out, const float* scale, in
 // batch n reads in + n * sin, flow + n * sfl (floats), writes out + n * sout_bytes.
 cudaError_t launch_warp_to_chunked(const float* in, const float* flow, void* out, const float* scale, int N, int C,
     int H, int W, int64_t sin, int64_t sfl, int64_t sout_bytes, bool bf16, cudaStream_t st);
+
+// ---- learned flow upsampler (vsc_upsampler.cu) ------------------------------------
+int upsampler_param_count();
+void upsampler_init_params(float* host, uint64_t seed);
+size_t upsampler_act_floats(int N, int H, int W);          // inference activations + residual
+size_t upsampler_train_work_floats(int N, int H, int W);   // activations and gradients of a batch
+// input (N x h x w x 3): the coarse flows bilinearly upsampled with their vectors
+// scaled to the full grid, and the frames' luma; batch n at base + n * stride
+cudaError_t launch_upsampler_prepare(const float* coarse, int cw, int ch, int cfc, const float* img, float* input,
+    int w, int h, int N, int64_t s_coarse, int64_t s_img, int64_t s_in, cudaStream_t st);
+// the net with FP16 weights: act holds upsampler_act_floats - 2 px floats, r the residual (N x H x W x 2)
+cudaError_t launch_upsampler_forward_half(const __half* w16, const float* prm, const float* input, float* act,
+    float* r, int N, int H, int W, cudaStream_t st);
+cudaError_t launch_upsampler_finish(const float* input, const float* r, float* flow, int N, int64_t npx,
+    float max_residual, int64_t s_in, int64_t s_r, int64_t s_out, cudaStream_t st);
+cudaError_t launch_to_half(const float* a, __half* b, int n, cudaStream_t st);
+cudaError_t upsampler_train_step(float* prm, float* grad, float* m, float* v, int step, const float* input,
+    const float* target, int N, int H, int W, float lr, float* work, float* loss_dev, cudaStream_t st);
 
 // Device address of the flag a kernel sets when one of its bounded waits gave up.
 cudaError_t device_timeout_flag(int** flag);
