@@ -411,7 +411,7 @@ def solver_roofline(vsc, dev, stream, iters: int = 144):
     per_launch_ms = step_ms * T
     achieved = alg_bytes / (per_launch_ms / 1000.0) / 1e9
     traffic = SOLVER_TRAFFIC_BYTES.get(T)
-    return {"bound": "hbm", "kernel": f"solver_persistent_kernel ({T} Jacobi steps of kernel_consist_out per "
+    return {"bound": "hbm", "kernel": f"solver_tall_kernel (64x48 tiles; {T} Jacobi steps of kernel_consist_out per "
                                       f"launch at 1920x1080; effective bytes = {SOLVER_BYTES_PER_PX} B/px per step)",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes, "steps_per_launch": T,

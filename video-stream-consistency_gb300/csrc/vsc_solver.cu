@@ -453,6 +453,223 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
     }
 }
 
+// ---- persistent, TMA-fed solver on 64 x 48 tiles of 2 x 4 pixel blocks -------------
+// Same per-pixel arithmetic as the kernels above, on a taller tile: 12 warps,
+// each thread a 2-column x 4-row block (its vertical neighbours inside the
+// block are its own registers), so 48 rows fit in the register budget of
+// 384 threads and the interior after the 8-pixel ring is 48 x 32 (50 % of
+// the tile instead of 37.5 %).  Only the top and bottom row of each warp
+// are read by other warps; they are published to a compact double-buffered
+// array of "slots" (slot w + 1 holds warp w's two edge rows, slots 0 and 13
+// are zero aprons).  Half the shared-memory traffic per pixel of the 2 x 2
+// blocking, the same shuffles per pixel.
+constexpr int kPWarps = 12;
+constexpr int kPThreads = 32 * kPWarps;
+constexpr int kPEY = 4 * kPWarps;            // 48 tile rows
+constexpr int kPIH = kPEY - 2 * kTbT;        // 32 interior rows
+constexpr int kPStageFloats = kPEY * kTbEX * 3;
+constexpr int kPStageBytes = kPStageFloats * static_cast<int>(sizeof(float));
+constexpr int kPSlots = kPWarps + 2;
+constexpr int kPPlane = kPSlots * 2 * kTbPX;  // one channel of one buffer
+constexpr int kPObuf = 2 * 3 * kPPlane;
+constexpr int kPSmem = 5 * kPStageBytes + kPObuf * static_cast<int>(sizeof(float)) + 16;
+static_assert(kPSmem <= 232448, "dynamic shared memory per CTA");
+static_assert(2 * kTbT < kPEY, "tile too small for the iteration count");
+
+struct P8State {
+    float o[8][3], u[8][3], a[8][3], wt[8][3], lp[8][3];  // [pixel q = 2 * row + col][channel]
+};
+
+// validity of a pixel's four neighbours in the reference's rule (border tiles only)
+struct Nb {
+    bool vr, vl, vd, vu;
+    float cnt;
+};
+__device__ __forceinline__ Nb nb_of(int gx, int gy, int w, int h)
+{
+    Nb n;
+    n.vr = (gx + 1) < (w - 1);
+    n.vl = (gx - 1) >= 0;
+    n.vd = (gy + 1) < (h - 1);
+    n.vu = (gy - 1) >= 0;
+    n.cnt = static_cast<float>(static_cast<int>(n.vr) + static_cast<int>(n.vl) + static_cast<int>(n.vd) +
+                               static_cast<int>(n.vu));
+    return n;
+}
+
+template <bool kAll>
+__device__ __forceinline__ void p8_step(P8State& s, float* obuf, int cur, bool mom_on, float step, float mom, int px0,
+    int warp, int gx0, int gy0, int w, int h)
+{
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        const float* S = obuf + (cur * 3 + ch) * kPPlane;
+        const float2 up = *reinterpret_cast<const float2*>(&S[(warp * 2 + 1) * kTbPX + px0 + 2]);   // slot w, row 1
+        const float2 dn = *reinterpret_cast<const float2*>(&S[((warp + 2) * 2) * kTbPX + px0 + 2]);  // slot w+2, row 0
+        float ol[4], orr[4], L[4], R[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            ol[r] = s.o[2 * r][ch];
+            orr[r] = s.o[2 * r + 1][ch];
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            L[r] = __shfl_up_sync(0xffffffffu, orr[r], 1);
+            R[r] = __shfl_down_sync(0xffffffffu, ol[r], 1);
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const float ul = r == 0 ? up.x : ol[r - 1], ur = r == 0 ? up.y : orr[r - 1];
+            const float dl = r == 3 ? dn.x : ol[r + 1], dr = r == 3 ? dn.y : orr[r + 1];
+            Nb a{true, true, true, true, 4.0f}, b{true, true, true, true, 4.0f};
+            if (!kAll) {
+                a = nb_of(gx0, gy0 + r, w, h);
+                b = nb_of(gx0 + 1, gy0 + r, w, h);
+            }
+            const int ql = 2 * r, qr = 2 * r + 1;
+            s.o[ql][ch] = jacobi_px<kAll>(ol[r], s.u[ql][ch], s.a[ql][ch], s.wt[ql][ch], s.lp[ql][ch], orr[r], L[r], dl,
+                ul, a.vr, a.vl, a.vd, a.vu, a.cnt, step, mom, mom_on);
+            s.o[qr][ch] = jacobi_px<kAll>(orr[r], s.u[qr][ch], s.a[qr][ch], s.wt[qr][ch], s.lp[qr][ch], R[r], ol[r],
+                dr, ur, b.vr, b.vl, b.vd, b.vu, b.cnt, step, mom, mom_on);
+        }
+        float* D = obuf + ((cur ^ 1) * 3 + ch) * kPPlane + ((warp + 1) * 2) * kTbPX + px0 + 2;
+        *reinterpret_cast<float2*>(D) = make_float2(s.o[0][ch], s.o[1][ch]);            // top row
+        *reinterpret_cast<float2*>(D + kTbPX) = make_float2(s.o[6][ch], s.o[7][ch]);    // bottom row
+    }
+}
+
+// Iteration k is needed on rows [ring - T + k + 1, kPEY - ring + T - k - 1);
+// a warp (four rows) outside that range skips it (the argument of tb_iterate).
+template <bool kAll>
+__device__ __forceinline__ void p8_iterate(P8State& s, float* obuf, int T, int k0, float step, float mom, int px0,
+    int warp, int gx0, int gy0, int w, int h)
+{
+    const int r0 = 4 * warp;
+    if (T == kTbT && k0 > 0) {
+#pragma unroll
+        for (int k = 0; k < kTbT; ++k) {
+            if (!(r0 + 3 < k + 1 || r0 >= kPEY - k - 1))
+                p8_step<kAll>(s, obuf, k & 1, true, step, mom, px0, warp, gx0, gy0, w, h);
+            __syncthreads();
+        }
+        return;
+    }
+    for (int k = 0; k < T; ++k) {
+        const int lo = kTbT - T + k + 1, hi = kPEY - kTbT + T - k - 1;
+        if (!(r0 + 3 < lo || r0 >= hi))
+            p8_step<kAll>(s, obuf, k & 1, (k0 + k) > 0, step, mom, px0, warp, gx0, gy0, w, h);
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ void issue_tall_tile(float* stage, const CUtensorMap* m0, const CUtensorMap* m1,
+    const CUtensorMap* m2, const CUtensorMap* m3, const CUtensorMap* m4, int tile, int tiles_x, uint64_t* bar)
+{
+    const int ox = (tile % tiles_x) * kIW - kTbT;
+    const int oy = (tile / tiles_x) * kPIH - kTbT;
+    mbar_expect_tx(bar, 5 * kPStageBytes);
+    tma_load_2d(stage + 0 * kPStageFloats, m0, 3 * ox, oy, bar);
+    tma_load_2d(stage + 1 * kPStageFloats, m1, 3 * ox, oy, bar);
+    tma_load_2d(stage + 2 * kPStageFloats, m2, 3 * ox, oy, bar);
+    tma_load_2d(stage + 3 * kPStageFloats, m3, 3 * ox, oy, bar);
+    tma_load_2d(stage + 4 * kPStageFloats, m4, 3 * ox, oy, bar);
+}
+
+__global__ void __launch_bounds__(kPThreads, 1)
+    solver_tall_kernel(const __grid_constant__ CUtensorMap mO, const __grid_constant__ CUtensorMap mU,
+        const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mW,
+        const __grid_constant__ CUtensorMap mL, float* __restrict__ Oout, float* __restrict__ Uout, int w, int h,
+        int T, int k0, float step, float mom, uint8_t* __restrict__ rgba, int tiles_x, int ntiles)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* stage = reinterpret_cast<float*>(smem_raw);
+    float* obuf = stage + 5 * kPStageFloats;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(obuf + kPObuf);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int px0 = 2 * lane, py0 = 4 * warp;
+
+    for (int i = threadIdx.x; i < kPObuf; i += kPThreads)
+        obuf[i] = 0.0f;  // the apron slots stay zero
+    if (threadIdx.x == 0)
+        mbar_init(bar, 1);
+    __syncthreads();
+    int tile = blockIdx.x;
+    if (threadIdx.x == 0 && tile < ntiles)
+        issue_tall_tile(stage, &mO, &mU, &mA, &mW, &mL, tile, tiles_x, bar);
+    uint32_t parity = 0;
+    for (; tile < ntiles; tile += gridDim.x) {
+        const int ox = (tile % tiles_x) * kIW - kTbT;
+        const int oy = (tile / tiles_x) * kPIH - kTbT;
+        if (!mbar_wait_bounded(bar, parity, kWaitSpins)) {
+            if (threadIdx.x == 0)
+                atomicExch(&g_device_timeout, 1);
+            mbar_wait_bounded(bar, parity, kWaitSpins);  // let copies still in flight land
+            return;
+        }
+        parity ^= 1;
+
+        P8State s;
+        float(*dst[5])[3] = {s.o, s.u, s.a, s.wt, s.lp};
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            // six consecutive floats: both pixels' RGB (TMA zero-fills outside the image)
+#pragma unroll
+            for (int arr = 0; arr < 5; ++arr) {
+                const float* src = stage + arr * kPStageFloats + (py0 + r) * (3 * kTbEX) + 3 * px0;
+                const float2 v01 = *reinterpret_cast<const float2*>(src);
+                const float2 v23 = *reinterpret_cast<const float2*>(src + 2);
+                const float2 v45 = *reinterpret_cast<const float2*>(src + 4);
+                float* p0 = dst[arr][2 * r];
+                float* p1 = dst[arr][2 * r + 1];
+                p0[0] = v01.x;
+                p0[1] = v01.y;
+                p0[2] = v23.x;
+                p1[0] = v23.y;
+                p1[1] = v45.x;
+                p1[2] = v45.y;
+            }
+        }
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            float* D = obuf + ch * kPPlane + ((warp + 1) * 2) * kTbPX + px0 + 2;  // buffer 0
+            *reinterpret_cast<float2*>(D) = make_float2(s.o[0][ch], s.o[1][ch]);
+            *reinterpret_cast<float2*>(D + kTbPX) = make_float2(s.o[6][ch], s.o[7][ch]);
+        }
+        __syncthreads();  // staging consumed, edge rows published
+        if (threadIdx.x == 0 && tile + static_cast<int>(gridDim.x) < ntiles) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue_tall_tile(stage, &mO, &mU, &mA, &mW, &mL, tile + gridDim.x, tiles_x, bar);
+        }
+
+        const int gx0 = ox + px0, gy0 = oy + py0;
+        const bool interior = ox >= 1 && oy >= 1 && ox + kTbEX - 1 <= w - 3 && oy + kPEY - 1 <= h - 3;
+        if (interior)
+            p8_iterate<true>(s, obuf, T, k0, step, mom, px0, warp, gx0, gy0, w, h);
+        else
+            p8_iterate<false>(s, obuf, T, k0, step, mom, px0, warp, gx0, gy0, w, h);
+
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int r = q >> 1, c = q & 1;
+            const int px = px0 + c, py = py0 + r;
+            const int gx = ox + px, gy = oy + py;
+            if (gx < 0 || gx >= w || gy < 0 || gy >= h || px < kTbT || px >= kTbEX - kTbT || py < kTbT ||
+                py >= kPEY - kTbT)
+                continue;
+            const int64_t p = pix_index(gx, gy, w);
+            float ov[3];
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+                ov[ch] = s.o[q][ch];
+                Oout[p * 3 + ch] = ov[ch];
+                Uout[p * 3 + ch] = s.u[q][ch];
+            }
+            if (rgba)
+                reinterpret_cast<uint32_t*>(rgba)[p] = pack_rgba(ov[0], ov[1], ov[2]);
+        }
+    }
+}
+
 // An mbarrier nobody arrives on, waited for with a bounded spin: exercises
 // the timeout path of the bounded waits (sets g_device_timeout, returns).
 __global__ void bounded_wait_selftest_kernel(int spins)
@@ -485,14 +702,14 @@ EncodeTiledFn encode_fn()
 }
 
 // 2D map over an interleaved w x h x 3 float image: x = float index in a row.
-bool encode_image_map(CUtensorMap* m, const float* base, int w, int h)
+bool encode_image_map(CUtensorMap* m, const float* base, int w, int h, int box_rows)
 {
     EncodeTiledFn fn = encode_fn();
     if (!fn)
         return false;
     const cuuint64_t dims[2] = {static_cast<cuuint64_t>(w) * 3, static_cast<cuuint64_t>(h)};
     const cuuint64_t strides[1] = {static_cast<cuuint64_t>(w) * 3 * sizeof(float)};
-    const cuuint32_t box[2] = {3 * kTbEX, kTbEY};
+    const cuuint32_t box[2] = {3 * kTbEX, static_cast<cuuint32_t>(box_rows)};
     const cuuint32_t estr[2] = {1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -526,7 +743,9 @@ cudaError_t device_info(DeviceInfo** out)
             cudaSuccess)
             return e;
         d.ps_smem = cudaFuncSetAttribute(solver_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                        kPsSmem) == cudaSuccess;
+                        kPsSmem) == cudaSuccess &&
+                    cudaFuncSetAttribute(solver_tall_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmem) ==
+                        cudaSuccess;
         cudaGetLastError();
     }
     *out = &d;
@@ -577,22 +796,33 @@ cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O
     // TMA path: 16-byte row pitch and aligned images
     bool tma = di->ps_smem && (w % 4) == 0 && aligned16p(O) && aligned16p(O2) && aligned16p(U[0]) &&
                aligned16p(U[1]) && aligned16p(A) && aligned16p(Wt) && aligned16p(L);
+    // Tile shape: the persistent kernels walk their tiles in waves of one
+    // tile per SM, so a launch costs about ceil(tiles / SMs) tile times; a
+    // 64 x 48 tile costs 1.91 times a 64 x 32 one (measured on GB300,
+    // 1920x1080 and 960x540), and the shape with the cheaper waves is used.
+    const int tiles_x = (w + kIW - 1) / kIW;
+    const int n_short = tiles_x * ((h + kIH - 1) / kIH), n_tall = tiles_x * ((h + kPIH - 1) / kPIH);
+    const bool tall = 1.91 * ((n_tall + di->sms - 1) / di->sms) < 1.0 * ((n_short + di->sms - 1) / di->sms);
+    const int rows = tall ? kPEY : kTbEY;
+    const int ntiles = tall ? n_tall : n_short;
     CUtensorMap mO[2], mU[2], mA, mW, mL;
     if (tma)
-        tma = encode_image_map(&mO[0], O, w, h) && encode_image_map(&mO[1], O2, w, h) &&
-              encode_image_map(&mU[0], U[0], w, h) && encode_image_map(&mU[1], U[1], w, h) &&
-              encode_image_map(&mA, A, w, h) && encode_image_map(&mW, Wt, w, h) && encode_image_map(&mL, L, w, h);
-    const int tiles_x = (w + kIW - 1) / kIW, tiles_y = (h + kIH - 1) / kIH;
-    const int ntiles = tiles_x * tiles_y;
+        tma = encode_image_map(&mO[0], O, w, h, rows) && encode_image_map(&mO[1], O2, w, h, rows) &&
+              encode_image_map(&mU[0], U[0], w, h, rows) && encode_image_map(&mU[1], U[1], w, h, rows) &&
+              encode_image_map(&mA, A, w, h, rows) && encode_image_map(&mW, Wt, w, h, rows) &&
+              encode_image_map(&mL, L, w, h, rows);
     int k0 = 0;
     for (int li = 0; li < nlaunch; ++li) {
         const int T = std::min(kTbT, num_iter - k0);
         float* nxt = (cur == O) ? O2 : O;
         uint8_t* rg = (li == nlaunch - 1) ? rgba_out : nullptr;
-        if (tma) {
-            const int grid = std::min(ntiles, di->sms);
-            solver_persistent_kernel<<<grid, dim3(32, kTbEY / 2), kPsSmem, st>>>(mO[cur == O ? 0 : 1], mU[li & 1], mA,
-                mW, mL, nxt, U[(li + 1) & 1], w, h, T, k0, step, mom, rg, tiles_x, ntiles);
+        if (tma && tall) {
+            solver_tall_kernel<<<std::min(ntiles, di->sms), kPThreads, kPSmem, st>>>(mO[cur == O ? 0 : 1],
+                mU[li & 1], mA, mW, mL, nxt, U[(li + 1) & 1], w, h, T, k0, step, mom, rg, tiles_x, ntiles);
+        } else if (tma) {
+            solver_persistent_kernel<<<std::min(ntiles, di->sms), dim3(32, kTbEY / 2), kPsSmem, st>>>(
+                mO[cur == O ? 0 : 1], mU[li & 1], mA, mW, mL, nxt, U[(li + 1) & 1], w, h, T, k0, step, mom, rg,
+                tiles_x, ntiles);
         } else {
             const dim3 grid((w + (kTbEX - 2 * T) - 1) / (kTbEX - 2 * T), (h + (kTbEY - 2 * T) - 1) / (kTbEY - 2 * T));
             solver_tb_kernel<<<grid, dim3(32, kTbEY / 2), kTbSmem, st>>>(cur, nxt, U[li & 1], U[(li + 1) & 1], L, A,
