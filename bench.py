@@ -542,11 +542,15 @@ def run_corr_only(args):
 
 
 def run_front_only(args):
-    """--kernel front: vsc_stab_front (five warps + adaptive combination +
-    consistency weights in one pass) at 1920x1080, CUDA events on its stream.
-    Algorithmic bytes 124 B/px: two 3-channel flows (24 B), five warped
-    sources (60 B), the current original and processed frames (24 B), two
-    outputs (24 B); the inputs (258 MB) exceed L2, so no flush is needed."""
+    """--kernel front: the fused front pass (five warps + adaptive combination
+    + consistency weights in one pass) at 1920x1080, CUDA events on its
+    stream, in both forms: vsc_stab_front on float frames (124 B/px: two
+    3-channel flows 24 B, five warped sources 60 B, the current original and
+    processed frames 24 B, two outputs 24 B; the stabilizer's form) and
+    vsc_stab_front_rgba on RGBA8 frames (84 B/px: flows 24 B, four warped
+    RGBA8 sources 16 B, the warped last stabilized frame 12 B, the current
+    RGBA8 frames 8 B, outputs 24 B).  The inputs exceed L2 (258 / 174 MB),
+    so no flush is needed."""
     import torch
 
     vsc = import_pkg()
@@ -555,28 +559,40 @@ def run_front_only(args):
     dev = torch.device("cuda", 0)
     stream = torch.cuda.Stream(device=dev)
     g = torch.Generator(device=dev).manual_seed(5)
-    ims = [torch.rand((H, W, 3), device=dev, generator=g) for _ in range(7)]
+    rgba = [torch.randint(0, 256, (H, W, 4), device=dev, generator=g, dtype=torch.uint8) for _ in range(6)]
+    with torch.cuda.stream(stream):
+        ims = [vsc.char_to_float_image(r, stream=stream) for r in rgba]
+    stream.synchronize()
+    ims.append(torch.rand((H, W, 3), device=dev, generator=g))
     yy, xx = torch.meshgrid(torch.arange(H, device=dev), torch.arange(W, device=dev), indexing="ij")
     ff = torch.stack([3 * torch.sin(xx / 97.0), 2 * torch.cos(yy / 83.0), torch.zeros_like(xx, dtype=torch.float32)],
                      -1).float().contiguous()
     fb = (-ff).contiguous()
     apr, wt = torch.empty_like(ims[0]), torch.empty_like(ims[0])
     peak, peak_src = peaks()
-    call = lambda: vsc.stab_front(ims[0:3], ims[3:6], ims[6], ff, fb, 6800.0, 6800.0, 2.0, out=(apr, wt),  # noqa: E731
-                                  stream=stream)
-    for _ in range(max(args.warmup, 3)):
-        call()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        call()
-    e1.record(stream)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
-    alg = 124 * W * H
-    print(json.dumps({"kernel": "fused_front_kernel (vsc_stab_front) 1920x1080", "ms": ms,
-                      "achieved_gbs": alg / (ms / 1000) / 1e9, "peak_gbs": peak,
-                      "frac": alg / (ms / 1000) / 1e9 / peak, "algorithmic_bytes": alg, "peak_source": peak_src}))
+    forms = {
+        "fused_front_kernel (vsc_stab_front, float frames)": (124, lambda: vsc.stab_front(
+            ims[0:3], ims[3:6], ims[6], ff, fb, 6800.0, 6800.0, 2.0, out=(apr, wt), stream=stream)),
+        "fused_front_rgba_kernel (vsc_stab_front_rgba, RGBA8 frames)": (84, lambda: (
+            vsc.stab_front_rgba(rgba[0:3], rgba[3:6], ims[6], ff, fb, 6800.0, 6800.0, 2.0, out=(apr, wt),
+                                stream=stream))),
+    }
+    res = []
+    for name, (bpp, call) in forms.items():
+        for _ in range(max(args.warmup, 3)):
+            call()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            call()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        alg = bpp * W * H
+        res.append({"kernel": name + " 1920x1080", "ms": ms, "bytes_per_px": bpp,
+                    "achieved_gbs": alg / (ms / 1000) / 1e9, "frac": alg / (ms / 1000) / 1e9 / peak,
+                    "algorithmic_bytes": alg})
+    print(json.dumps({"forms": res, "peak_gbs": peak, "peak_source": peak_src}))
 
 
 def run_solver_only(args):

@@ -203,6 +203,18 @@ VSC_API vsc_status vsc_stab_front(const vsc_image* orig_prev, const vsc_image* o
     const vsc_image* flow_fwd, const vsc_image* flow_bwd, const vsc_image* adap_cmb_pr, const vsc_image* consis_wt,
     float alpha, float beta, float gamma, int32_t occlusion_mask, vsc_stream_t stream);
 
+/* vsc_stab_front with the six original / processed frames given as the
+ * RGBA8 device frames they are converted from (w x h 32-bit words each,
+ * 4-byte aligned; alpha ignored): the bilinear taps are gathered as 4-byte
+ * words and converted with vsc_char_to_float_image's exact conversion, so
+ * the outputs equal vsc_stab_front's on the converted frames bit for bit
+ * with 84 instead of 124 bytes of traffic per pixel.  No single counterpart in the
+ * reference (videostabilizer.cpp:182-198 on the frames of gpuimage.cu:39-51). */
+VSC_API vsc_status vsc_stab_front_rgba(const uint8_t* orig_prev, const uint8_t* orig_cur, const uint8_t* orig_next,
+    const uint8_t* proc_prev, const uint8_t* proc_cur, const uint8_t* proc_next, const vsc_image* last_stab,
+    const vsc_image* flow_fwd, const vsc_image* flow_bwd, const vsc_image* adap_cmb_pr, const vsc_image* consis_wt,
+    float alpha, float beta, float gamma, int32_t occlusion_mask, vsc_stream_t stream);
+
 /* Consistency weights gamma*exp(-beta*(I - adapCmbIn)^2), < 0.001 -> 0.
  * Replaces get_consist_wt / kernel_consist_wt (flowconsistency.cu:168-191, :335-348). */
 VSC_API vsc_status vsc_get_consist_wt(const vsc_image* adap_cmb_in, const vsc_image* crnt_in,

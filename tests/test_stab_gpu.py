@@ -442,6 +442,42 @@ def test_stab_front_equals_separate_calls(vsc, oracle, cuda, fc, occ):
     assert np.array_equal(wt.cpu().numpy(), rwt)
 
 
+@pytest.mark.parametrize("fc,occ", [(3, False), (2, True), (3, True)])
+def test_stab_front_rgba_equals_restatement(vsc, oracle, cuda, fc, occ):
+    """vsc_stab_front_rgba (taps gathered as RGBA8 words) equals the
+    restatement on the converted frames bit for bit, and vsc_stab_front on
+    the same converted frames; flows large enough to reach the clamped
+    border taps."""
+    import torch
+
+    h, w = 61, 83
+    fr = _frames(w, h, 3, seed=71)
+    rgba = [o for o, _ in fr] + [p for _, p in fr]
+    f = [oracle.rgba_to_float(a) for a in rgba]
+    ls = np.clip(f[4] + RNG.normal(0, 0.02, f[4].shape), 0, 1).astype(np.float32)
+    ff = RNG.normal(0, 6, (h, w, fc)).astype(np.float32)
+    fb = (-ff + RNG.normal(0, 0.5, ff.shape)).astype(np.float32)
+    d = lambda a: _t(a, cuda)  # noqa: E731
+    r8 = [torch.from_numpy(np.ascontiguousarray(a)).to(cuda) for a in rgba]
+    apr, wt = vsc.stab_front_rgba(r8[0:3], r8[3:6], d(ls), d(ff), d(fb), 20.0, 30.0, 2.0, occlusion_mask=occ)
+    fapr, fwt = vsc.stab_front([d(a) for a in f[0:3]], [d(a) for a in f[3:6]], d(ls), d(ff), d(fb), 20.0, 30.0,
+                               2.0, occlusion_mask=occ)
+    assert np.array_equal(apr.cpu().numpy(), fapr.cpu().numpy())
+    assert np.array_equal(wt.cpu().numpy(), fwt.cpu().numpy())
+    warps = [oracle.stab_warp(src, fl) for src, fl in ((f[0], fb), (f[3], fb), (f[2], ff), (f[5], ff), (ls, fb))]
+    if occ:
+        m = oracle.flow_consistency_mask(ff, fb)
+        ain, rpr = oracle.adap_comb_masked(f[1], f[4], warps[0], warps[1], warps[2], warps[3], warps[4], m, 20.0)
+    else:
+        ain, rpr = oracle.adap_comb(f[1], f[4], warps[0], warps[1], warps[2], warps[3], warps[4], 20.0)
+    assert np.array_equal(apr.cpu().numpy(), rpr)
+    assert np.array_equal(wt.cpu().numpy(), oracle.consist_wt(f[1], ain, 30.0, 2.0))
+    # misaligned frame pointer: an error, nothing launched
+    bad = torch.empty(w * h * 4 + 1, dtype=torch.uint8, device=cuda)[1:].view(h, w, 4)
+    with pytest.raises(vsc.VscError, match="aligned"):
+        vsc.stab_front_rgba([bad, r8[1], r8[2]], r8[3:6], d(ls), d(ff), d(fb), 20.0, 30.0, 2.0)
+
+
 def test_flow_estimate_equals_restatement(vsc, oracle, cuda):
     w, h = 112, 80
     fr = _frames(w, h, 2, seed=61)

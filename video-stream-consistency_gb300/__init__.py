@@ -40,7 +40,8 @@ EXPORTED = [
     "vsc_image_file_info", "vsc_read_image_file", "vsc_write_png", "vsc_flo_info", "vsc_read_flo", "vsc_write_flo",
     "vsc_stabilize_files", "vsc_solver_steps_per_launch",
     "vsc_multistream_create", "vsc_multistream_destroy", "vsc_multistream_hyper_params", "vsc_multistream_load_frames",
-    "vsc_multistream_step", "vsc_multistream_last_launches", "vsc_stab_front", "vsc_flow_estimate",
+    "vsc_multistream_step", "vsc_multistream_last_launches", "vsc_stab_front", "vsc_stab_front_rgba",
+    "vsc_flow_estimate",
     "vsc_upsampler_param_count", "vsc_upsampler_create", "vsc_upsampler_destroy", "vsc_upsampler_get_params",
     "vsc_upsampler_set_max_residual", "vsc_upsampler_prepare", "vsc_upsampler_train_step", "vsc_upsampler_apply",
     "vsc_stabilizer_set_upsampler",
@@ -140,6 +141,7 @@ def load():
         "vsc_stabilizer_enable_timing": [vp, i32],
         "vsc_get_flow_consistency_mask": [IP, IP, IP, vp],
         "vsc_stab_front": [IP] * 11 + [f32, f32, f32, i32, vp],
+        "vsc_stab_front_rgba": [vp] * 6 + [IP] * 5 + [f32, f32, f32, i32, vp],
         "vsc_flow_estimate": [IP, IP, IP, IP, vp],
         "vsc_upsampler_create": [vp, C.POINTER(vp)],
         "vsc_upsampler_destroy": [vp],
@@ -377,6 +379,29 @@ def stab_front(orig3, proc3, last_stab, flow_fwd, flow_bwd, alpha, beta, gamma, 
     ims = [image(t) for t in (*orig3, *proc3, last_stab, flow_fwd, flow_bwd, apr, wt)]
     _check(load().vsc_stab_front(*[C.byref(i) for i in ims], float(alpha), float(beta), float(gamma),
                                  1 if occlusion_mask else 0, _stream(stream)))
+    return apr, wt
+
+
+def stab_front_rgba(orig3, proc3, last_stab, flow_fwd, flow_bwd, alpha, beta, gamma, occlusion_mask=False,
+                    out=None, stream=None):
+    """stab_front with the six frames as (h, w, 4) uint8 RGBA device tensors;
+    returns (adapCmbPr, consWt), equal bit for bit to stab_front on the
+    frames converted by char_to_float_image."""
+    import torch
+
+    frames = [*orig3, *proc3]
+    for f in frames:
+        if f.dtype != torch.uint8 or f.dim() != 3 or f.shape[2] != 4 or not f.is_contiguous() or not f.is_cuda:
+            raise ValueError("stab_front_rgba: frames must be contiguous (h, w, 4) uint8 CUDA tensors")
+    if out is None:
+        h, w = last_stab.shape[:2]
+        out = (torch.empty((h, w, 3), dtype=torch.float32, device=last_stab.device),
+               torch.empty((h, w, 3), dtype=torch.float32, device=last_stab.device))
+    apr, wt = out
+    ims = [image(t) for t in (last_stab, flow_fwd, flow_bwd, apr, wt)]
+    _check(load().vsc_stab_front_rgba(*[C.c_void_p(f.data_ptr()) for f in frames], *[C.byref(i) for i in ims],
+                                      float(alpha), float(beta), float(gamma), 1 if occlusion_mask else 0,
+                                      _stream(stream)))
     return apr, wt
 
 

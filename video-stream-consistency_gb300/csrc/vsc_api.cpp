@@ -426,6 +426,40 @@ VSC_API vsc_status vsc_stab_front(const vsc_image* orig_prev, const vsc_image* o
         "stab_front launch");
 }
 
+VSC_API vsc_status vsc_stab_front_rgba(const uint8_t* orig_prev, const uint8_t* orig_cur, const uint8_t* orig_next,
+    const uint8_t* proc_prev, const uint8_t* proc_cur, const uint8_t* proc_next, const vsc_image* last_stab,
+    const vsc_image* flow_fwd, const vsc_image* flow_bwd, const vsc_image* adap_cmb_pr, const vsc_image* consis_wt,
+    float alpha, float beta, float gamma, int32_t occlusion_mask, vsc_stream_t stream)
+{
+    clear_error();
+    const uint8_t* fr[6] = {orig_prev, orig_cur, orig_next, proc_prev, proc_cur, proc_next};
+    for (int i = 0; i < 6; ++i) {
+        if (!fr[i])
+            return set_error(VSC_EINVAL, "stab_front_rgba: frame %d is null", i);
+        if (reinterpret_cast<uintptr_t>(fr[i]) & 3)
+            return set_error(VSC_EINVAL, "stab_front_rgba: frame %d is not 4-byte aligned", i);
+    }
+    const vsc_image* im[3] = {last_stab, adap_cmb_pr, consis_wt};
+    static const char* names[3] = {"lastStab", "adapCmbPr", "consisWt"};
+    vsc_status s;
+    for (int i = 0; i < 3; ++i)
+        if ((s = check_image(im[i], names[i], 3, 3)) || (s = same_size(last_stab, im[i], names[i])))
+            return s;
+    if ((s = check_image(flow_fwd, "flowFwd", 2, 3)) || (s = check_image(flow_bwd, "flowBwd", 2, 3)) ||
+        (s = same_size(last_stab, flow_fwd, "flowFwd")) || (s = same_size(last_stab, flow_bwd, "flowBwd")))
+        return s;
+    if (flow_fwd->channels != flow_bwd->channels)
+        return set_error(VSC_EINVAL, "stab_front_rgba: flows have %d and %d channels", flow_fwd->channels,
+            flow_bwd->channels);
+    if (last_stab->width < 3 || last_stab->height < 3)
+        return set_error(VSC_EINVAL, "stab_front_rgba: image must be at least 3x3");
+    return check_cuda(launch_fused_front_rgba(orig_prev, orig_cur, orig_next, proc_prev, proc_cur, proc_next,
+                          last_stab->data, flow_fwd->data, flow_bwd->data, flow_fwd->channels, adap_cmb_pr->data,
+                          consis_wt->data, last_stab->width, last_stab->height, alpha, beta, gamma, cs(stream),
+                          occlusion_mask != 0),
+        "stab_front_rgba launch");
+}
+
 VSC_API vsc_status vsc_get_consist_wt(const vsc_image* adap_cmb_in, const vsc_image* crnt_in,
     const vsc_image* consis_wt, float beta, float gamma, vsc_stream_t stream)
 {

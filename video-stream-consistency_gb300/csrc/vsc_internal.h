@@ -126,6 +126,12 @@ cudaError_t run_solver_noalloc(const float* P, const float* A, const float* Wt, 
 cudaError_t launch_fused_front(const float* o0, const float* o1, const float* o2, const float* p0, const float* p1,
     const float* p2, const float* last_stab, const float* flow_fwd, const float* flow_bwd, int fc, float* adap_pr,
     float* cons_wt, int w, int h, float alpha, float beta, float gamma, cudaStream_t st, bool occlusion_mask = false);
+// fused_front on the RGBA8 words of the six frames (4-byte aligned, w x h
+// words each); same outputs bit for bit
+cudaError_t launch_fused_front_rgba(const uint8_t* o0, const uint8_t* o1, const uint8_t* o2, const uint8_t* p0,
+    const uint8_t* p1, const uint8_t* p2, const float* last_stab, const float* flow_fwd, const float* flow_bwd, int fc,
+    float* adap_pr, float* cons_wt, int w, int h, float alpha, float beta, float gamma, cudaStream_t st,
+    bool occlusion_mask);
 // P, A, Wt of the next coarser pyramid level, one launch.
 cudaError_t launch_pyr_down3(const float* P, const float* A, const float* Wt, int iw, int ih, float* Pd, float* Ad,
     float* Wd, int ow, int oh, cudaStream_t st);

@@ -84,7 +84,8 @@ __global__ void float_to_rgba_kernel(const float* __restrict__ in, uint8_t* __re
 
 // ---- kernel_warp (flowconsistency.cu:77-114) --------------------------------
 struct WarpTap {
-    int64_t o0, o1;  // element offsets of the top-left tap of rows map_iy and map_iy+1
+    int64_t q0, q1;  // pixel indices of the top-left tap of rows map_iy and map_iy+1
+    int64_t o0, o1;  // their element offsets in a 3-channel image
     float fx, fy;
 };
 
@@ -100,16 +101,24 @@ __device__ __forceinline__ WarpTap warp_tap(const float* __restrict__ flow, int 
     WarpTap t;
     t.fx = map_fx - static_cast<float>(map_ix);
     t.fy = map_fy - static_cast<float>(map_iy);
-    t.o0 = pix_index(map_ix, map_iy, w) * 3;
-    t.o1 = pix_index(map_ix, map_iy + 1, w) * 3;
+    t.q0 = pix_index(map_ix, map_iy, w);
+    t.q1 = pix_index(map_ix, map_iy + 1, w);
+    t.o0 = t.q0 * 3;
+    t.o1 = t.q1 * 3;
     return t;
+}
+
+// the bilinear blend of the four taps, in kernel_warp's operation order
+__device__ __forceinline__ float bilerp(float t00, float t01, float t10, float t11, float fx, float fy)
+{
+    const float tmp_1 = t00 * (1.0f - fx) + t01 * fx;
+    const float tmp_2 = t10 * (1.0f - fx) + t11 * fx;
+    return tmp_1 * (1.0f - fy) + tmp_2 * fy;
 }
 
 __device__ __forceinline__ float warp_sample(const float* __restrict__ in, const WarpTap& t, int c)
 {
-    const float tmp_1 = in[t.o0 + c] * (1.0f - t.fx) + in[t.o0 + 3 + c] * t.fx;
-    const float tmp_2 = in[t.o1 + c] * (1.0f - t.fx) + in[t.o1 + 3 + c] * t.fx;
-    return tmp_1 * (1.0f - t.fy) + tmp_2 * t.fy;
+    return bilerp(in[t.o0 + c], in[t.o0 + 3 + c], in[t.o1 + c], in[t.o1 + 3 + c], t.fx, t.fy);
 }
 
 __global__ void stab_warp_kernel(const float* __restrict__ in, const float* __restrict__ flow, int fc,
@@ -324,6 +333,71 @@ __global__ void fused_front_kernel(const float* __restrict__ o0, const float* __
     }
 }
 
+// ---- the fused front pass on RGBA8 frames ------------------------------------------
+// For callers that hold the original and processed frames as RGBA8.  Every
+// value of a converted frame is lut[byte] (the float(double(v)/255.0)
+// conversion), so gathering the four bilinear taps of a frame as four
+// 32-bit words and converting the bytes through the same table gives the
+// same tap values, and therefore the same outputs bit for bit, as
+// fused_front_kernel on the converted frames: 4 bytes per tap instead of 12
+// (84 instead of 124 algorithmic bytes per pixel).  The last stabilized
+// frame is a float image and is gathered as such.
+struct RgbaTaps {
+    uint32_t t00, t01, t10, t11;
+};
+
+__device__ __forceinline__ RgbaTaps rgba_taps(const uint32_t* __restrict__ img, const WarpTap& t)
+{
+    return RgbaTaps{img[t.q0], img[t.q0 + 1], img[t.q1], img[t.q1 + 1]};
+}
+
+__device__ __forceinline__ float rgba_sample(const float* lut, const RgbaTaps& q, const WarpTap& t, int c)
+{
+    const int sh = 8 * c;
+    return bilerp(lut[(q.t00 >> sh) & 0xff], lut[(q.t01 >> sh) & 0xff], lut[(q.t10 >> sh) & 0xff],
+        lut[(q.t11 >> sh) & 0xff], t.fx, t.fy);
+}
+
+template <bool kOcc>
+__global__ void __launch_bounds__(256) fused_front_rgba_kernel(const uint32_t* __restrict__ o0,
+    const uint32_t* __restrict__ o1, const uint32_t* __restrict__ o2, const uint32_t* __restrict__ p0,
+    const uint32_t* __restrict__ p1, const uint32_t* __restrict__ p2, const float* __restrict__ ls,
+    const float* __restrict__ ffwd, const float* __restrict__ fbwd, int fc, float* __restrict__ adap_pr,
+    float* __restrict__ cons_wt, int w, int h, float alpha, float beta, float gamma)
+{
+    __shared__ float lut[256];
+    build_lut(lut);
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h)
+        return;
+    const WarpTap tb = warp_tap(fbwd, fc, x, y, w, h);
+    const WarpTap tf = warp_tap(ffwd, fc, x, y, w, h);
+    float mp = 1.0f, mn = 1.0f;
+    if (kOcc) {
+        mp = occl_check(fbwd, ffwd, fc, x, y, w, h);
+        mn = occl_check(ffwd, fbwd, fc, x, y, w, h);
+    }
+    const RgbaTaps qoi = rgba_taps(o0, tb), qop = rgba_taps(p0, tb);
+    const RgbaTaps qni = rgba_taps(o2, tf), qnp = rgba_taps(p2, tf);
+    const int64_t px = pix_index(x, y, w);
+    const uint32_t ci8 = o1[px], cp8 = p1[px];
+    const int64_t o = px * 3;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float pwi = rgba_sample(lut, qoi, tb, c);
+        const float pwp = rgba_sample(lut, qop, tb, c);
+        const float nwi = rgba_sample(lut, qni, tf, c);
+        const float nwp = rgba_sample(lut, qnp, tf, c);
+        const float lsw = warp_sample(ls, tb, c);
+        const float ci = lut[(ci8 >> (8 * c)) & 0xff];
+        const float cp = lut[(cp8 >> (8 * c)) & 0xff];
+        const Comb r = adap_comb_px(ci, cp, pwi, pwp, nwi, nwp, lsw, alpha, mp, mn, kOcc);
+        adap_pr[o + c] = r.apr;
+        cons_wt[o + c] = consist_wt_px(ci, r.ain, beta, gamma);
+    }
+}
+
 __global__ void resize_nearest_kernel(const float* __restrict__ in, int iw, int ih, float* __restrict__ out, int ow,
     int oh)
 {
@@ -431,6 +505,22 @@ cudaError_t launch_fused_front(const float* o0, const float* o1, const float* o2
     else
         fused_front_kernel<false><<<grid2d(w, h, b), b, 0, st>>>(
             o0, o1, o2, p0, p1, p2, last_stab, flow_fwd, flow_bwd, fc, adap_pr, cons_wt, w, h, alpha, beta, gamma);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fused_front_rgba(const uint8_t* o0, const uint8_t* o1, const uint8_t* o2, const uint8_t* p0,
+    const uint8_t* p1, const uint8_t* p2, const float* last_stab, const float* flow_fwd, const float* flow_bwd, int fc,
+    float* adap_pr, float* cons_wt, int w, int h, float alpha, float beta, float gamma, cudaStream_t st,
+    bool occlusion_mask)
+{
+    const dim3 b(32, 8);
+    auto u = [](const uint8_t* p) { return reinterpret_cast<const uint32_t*>(p); };
+    if (occlusion_mask)
+        fused_front_rgba_kernel<true><<<grid2d(w, h, b), b, 0, st>>>(u(o0), u(o1), u(o2), u(p0), u(p1), u(p2),
+            last_stab, flow_fwd, flow_bwd, fc, adap_pr, cons_wt, w, h, alpha, beta, gamma);
+    else
+        fused_front_rgba_kernel<false><<<grid2d(w, h, b), b, 0, st>>>(u(o0), u(o1), u(o2), u(p0), u(p1), u(p2),
+            last_stab, flow_fwd, flow_bwd, fc, adap_pr, cons_wt, w, h, alpha, beta, gamma);
     return cudaGetLastError();
 }
 
