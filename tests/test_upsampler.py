@@ -1,7 +1,9 @@
-"""Learned flow upsampler (vsc_upsampler_*): the FP16-weight inference
-against a numpy restatement of the net (tolerance from the FP16 weights),
-the bilinear fallback, training that overfits a small batch, and the
-stabilizer's fast mode with the net attached."""
+"""Learned flow upsampler (vsc_upsampler_*): the tensor-core inference (FP16
+weights and activations, FP32 accumulation) against a float64 numpy
+restatement of the net that rounds the same operands to FP16, and against
+the same net in FP32 (the error FP16 costs); the bilinear fallback; training
+that overfits a small batch; the stabilizer's fast mode with the net
+attached, whose two flows (one batched launch) equal single-image calls."""
 from __future__ import annotations
 
 import numpy as np
@@ -16,9 +18,12 @@ def test_param_count(vsc):
     assert vsc.Upsampler.param_count() == n == 19970
 
 
-def _np_forward(params, inp):
-    """The net in float64: 3x3 zero-padded convolutions, ReLU between."""
-    x = inp.astype(np.float64)
+def _np_forward(params, inp, half_acts=False):
+    """The net in float64: 3x3 zero-padded convolutions, ReLU between; with
+    half_acts the input and every inner activation are rounded to FP16 (the
+    tensor-core path's operands)."""
+    rnd = (lambda a: a.astype(np.float16).astype(np.float64)) if half_acts else (lambda a: a)  # noqa: E731
+    x = rnd(inp.astype(np.float64))
     off = 0
     for li, (ci, co) in enumerate(LAYERS):
         w = params[off:off + co * 9 * ci].reshape(co, 3, 3, ci).astype(np.float64)
@@ -31,7 +36,7 @@ def _np_forward(params, inp):
         for ky in range(3):
             for kx in range(3):
                 y += xp[ky:ky + h, kx:kx + wd] @ w[:, ky, kx, :].T
-        x = np.maximum(y, 0) if li < 3 else y
+        x = rnd(np.maximum(y, 0)) if li < 3 else y
     return x
 
 
@@ -52,10 +57,12 @@ def _base(coarse, w, h):
 
 
 @pytest.mark.gpu
-def test_inference_matches_numpy_and_fallback(vsc, cuda):
+@pytest.mark.parametrize("h,w", [(24, 36), (45, 261)])
+def test_inference_matches_numpy_and_fallback(vsc, cuda, h, w):
+    """(45, 261): three 128-pixel segments, the last one partial, and a
+    partial band of rows."""
     import torch
 
-    h, w = 24, 36
     coarse = RNG.normal(0, 1.5, (h // 2, w // 2, 3)).astype(np.float32)
     frame = RNG.random((h, w, 3)).astype(np.float32)
     params = (RNG.normal(0, 0.08, vsc.Upsampler.param_count())).astype(np.float32)
@@ -70,11 +77,16 @@ def test_inference_matches_numpy_and_fallback(vsc, cuda):
     for i, (ci, co) in enumerate(LAYERS):  # biases stay FP32
         start = sum(c * 9 * a + c for a, c in LAYERS[:i]) + co * 9 * ci
         p16[start:start + co] = params[start:start + co]
-    r = _np_forward(p16, inp)
+    r = _np_forward(p16, inp, half_acts=True)
     up.set_max_residual(1e9)
     got = up.apply(dc, df).cpu().numpy()
-    assert np.allclose(got[..., :2], inp[..., :2] + r, atol=2e-4 * (1 + np.abs(r).max()))
+    # same FP16 operands, FP32 vs float64 accumulation (an activation's FP16
+    # rounding may flip one unit where the two sums straddle a rounding point)
+    assert np.allclose(got[..., :2], inp[..., :2] + r, atol=1e-3 * (1 + np.abs(r).max()))
     assert np.all(got[..., 2] == 0)
+    # the cost of FP16 activations against the net in FP32 (FP16 weights in both)
+    r32 = _np_forward(p16, inp)
+    assert np.abs(got[..., :2] - (inp[..., :2] + r32)).max() <= 2e-2 * (1 + np.abs(r32).max())
     up.set_max_residual(0.0)  # every residual is refused: the bilinear base
     got0 = up.apply(dc, df).cpu().numpy()
     keep = np.max(np.abs(r), -1) > 1e-3
@@ -120,6 +132,16 @@ def test_stabilizer_with_learned_upsampler(vsc, cuda):
         st.step()
     fa, fb = a.buffer(1).cpu().numpy(), b.buffer(1).cpu().numpy()
     assert not np.allclose(fa, fb)
+    # both flows come from one batched launch; each equals the single-image call
+    # on the same coarse flow and frame (flow(I1 -> I2) with I1, flow(I2 -> I1) with I2)
+    import torch
+
+    from vsc_gb300.train_upsampler import nearest
+
+    f1, f2 = (vsc.char_to_float_image(torch.from_numpy(frames[i][0]).to(cuda)) for i in (1, 2))
+    ab, ba = vsc.flow_estimate(nearest(f1, w // 2, h // 2), nearest(f2, w // 2, h // 2))
+    assert np.allclose(up.apply(ab, f1).cpu().numpy(), fb, atol=1e-5)
+    assert np.allclose(up.apply(ba, f2).cpu().numpy(), b.buffer(2).cpu().numpy(), atol=1e-5)
     with pytest.raises(vsc.VscError, match="ESTATE"):
         vsc.Stabilizer(w, h).set_upsampler(up)
     a.close()

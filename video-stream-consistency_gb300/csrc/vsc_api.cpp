@@ -966,8 +966,8 @@ struct vsc_upsampler {
     float* grad = nullptr;
     float* m = nullptr;
     float* v = nullptr;
-    __half* w16 = nullptr;  // FP16 copy used by inference
-    bool w16_valid = false;
+    void* wtc = nullptr;  // FP16 weights packed for the tensor-core inference
+    bool wtc_valid = false;
     int step = 0;
     float* work = nullptr;
     size_t work_floats = 0;
@@ -976,13 +976,20 @@ struct vsc_upsampler {
 };
 namespace {
 
-cudaError_t upsampler_sync_half(vsc_upsampler* u, cudaStream_t st)
+cudaError_t upsampler_sync_weights(vsc_upsampler* u, cudaStream_t st)
 {
-    if (u->w16_valid)
+    if (u->wtc_valid)
         return cudaSuccess;
-    cudaError_t e = launch_to_half(u->prm, u->w16, upsampler_param_count(), st);
-    u->w16_valid = e == cudaSuccess;
+    cudaError_t e = launch_upsampler_tc_pack(u->prm, u->wtc, st);
+    u->wtc_valid = e == cudaSuccess;
     return e;
+}
+
+// the tensor-core work area follows the prepared input, on the 16-byte grid
+unsigned char* up_tc_work(float* input, int64_t input_floats)
+{
+    return reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(input + input_floats) + 15) &
+                                            ~static_cast<uintptr_t>(15));
 }
 
 // both flows of a step: coarse flows (fw x fh) -> full-size flows
@@ -991,18 +998,14 @@ cudaError_t upsampler_apply_pair(vsc_stabilizer* s, cudaStream_t st, int* nl)
     const int64_t npx = static_cast<int64_t>(s->w) * s->h;
     const int64_t fs = static_cast<int64_t>(s->fw) * s->fh * 3;
     float* input = s->up_work;
-    float* act = input + 2 * npx * 3;
-    float* r = act + upsampler_act_floats(2, s->h, s->w) - 2 * npx * 2;
-    cudaError_t e = upsampler_sync_half(s->upsampler, st);
+    cudaError_t e = upsampler_sync_weights(s->upsampler, st);
     if (e == cudaSuccess)
         e = launch_upsampler_prepare(s->flow_small, s->fw, s->fh, 3, s->orig[(s->head + 1) % 3], input, s->w, s->h, 2,
             fs, s->orig[(s->head + 2) % 3] - s->orig[(s->head + 1) % 3], npx * 3, st);
+    *nl += 1;
     if (e == cudaSuccess)
-        e = launch_upsampler_forward_half(s->upsampler->w16, s->upsampler->prm, input, act, r, 2, s->h, s->w, st);
-    if (e == cudaSuccess)
-        e = launch_upsampler_finish(input, r, s->flow_fwd, 2, npx, s->upsampler->max_residual, npx * 3, npx * 2,
-            s->flow_bwd - s->flow_fwd, st);
-    *nl += 6;
+        e = launch_upsampler_tc(s->upsampler->wtc, s->upsampler->prm, input, up_tc_work(input, 2 * npx * 3),
+            s->flow_fwd, 2, s->h, s->w, s->upsampler->max_residual, s->flow_bwd - s->flow_fwd, st, nl);
     return e;
 }
 
@@ -1288,7 +1291,7 @@ VSC_API vsc_status vsc_upsampler_create(const float* params, vsc_upsampler** out
     if (e == cudaSuccess)
         e = dalloc(&u->v, n);
     if (e == cudaSuccess)
-        e = dalloc(&u->w16, n);
+        e = cudaMalloc(&u->wtc, upsampler_tc_weight_bytes());
     if (e == cudaSuccess)
         e = dalloc(&u->loss, 1);
     if (e == cudaSuccess)
@@ -1312,7 +1315,7 @@ VSC_API vsc_status vsc_upsampler_destroy(vsc_upsampler* u)
     DeviceGuard g(u->device);
     cudaDeviceSynchronize();
     for (void* p : {static_cast<void*>(u->prm), static_cast<void*>(u->grad), static_cast<void*>(u->m),
-             static_cast<void*>(u->v), static_cast<void*>(u->w16), static_cast<void*>(u->work),
+             static_cast<void*>(u->v), u->wtc, static_cast<void*>(u->work),
              static_cast<void*>(u->loss)})
         if (p)
             cudaFree(p);
@@ -1373,7 +1376,7 @@ VSC_API vsc_status vsc_upsampler_train_step(vsc_upsampler* u, const float* input
             return s;
         u->work_floats = need;
     }
-    u->w16_valid = false;
+    u->wtc_valid = false;
     vsc_status s = check_cuda(upsampler_train_step(u->prm, u->grad, u->m, u->v, ++u->step, input, target, n, h, w, lr,
                                   u->work, u->loss, st),
         "upsampler_train_step");
@@ -1398,20 +1401,17 @@ VSC_API vsc_status vsc_upsampler_apply(vsc_upsampler* u, const vsc_image* coarse
     const int w = frame->width, h = frame->height;
     const int64_t npx = static_cast<int64_t>(w) * h;
     void* ws = nullptr;
-    if ((s = check_cuda(pool_alloc(&ws, (npx * 3 + upsampler_act_floats(1, h, w)) * sizeof(float), st),
+    if ((s = check_cuda(pool_alloc(&ws, npx * 3 * sizeof(float) + 16 + upsampler_tc_work_bytes(1, h, w), st),
              "upsampler_apply workspace")))
         return s;
     float* input = static_cast<float*>(ws);
-    float* act = input + npx * 3;
-    float* r = act + npx * 96;
-    cudaError_t e = upsampler_sync_half(u, st);
+    cudaError_t e = upsampler_sync_weights(u, st);
     if (e == cudaSuccess)
         e = launch_upsampler_prepare(coarse_flow->data, coarse_flow->width, coarse_flow->height, coarse_flow->channels,
             frame->data, input, w, h, 1, 0, 0, 0, st);
     if (e == cudaSuccess)
-        e = launch_upsampler_forward_half(u->w16, u->prm, input, act, r, 1, h, w, st);
-    if (e == cudaSuccess)
-        e = launch_upsampler_finish(input, r, flow_out->data, 1, npx, u->max_residual, 0, 0, 0, st);
+        e = launch_upsampler_tc(u->wtc, u->prm, input, up_tc_work(input, npx * 3), flow_out->data, 1, h, w,
+            u->max_residual, 0, st, nullptr);
     cudaFreeAsync(ws, st);
     return check_cuda(e, "upsampler_apply");
 }
@@ -1426,7 +1426,8 @@ VSC_API vsc_status vsc_stabilizer_set_upsampler(vsc_stabilizer* s, vsc_upsampler
     DeviceGuard g(s->device);
     if (u && !s->up_work) {
         const size_t npx = static_cast<size_t>(s->w) * s->h;
-        vsc_status st = check_cuda(dalloc(&s->up_work, 2 * npx * 3 + upsampler_act_floats(2, s->h, s->w)),
+        vsc_status st = check_cuda(
+            dalloc(&s->up_work, 2 * npx * 3 + 4 + upsampler_tc_work_bytes(2, s->h, s->w) / sizeof(float)),
             "set_upsampler workspace");
         if (st)
             return st;

@@ -55,21 +55,33 @@ cudaError_t launch_to_chunked(const float* in, void* out, const float* scale, in
 cudaError_t launch_warp_to_chunked(const float* in, const float* flow, void* out, const float* scale, int N, int C,
     int H, int W, int64_t sin, int64_t sfl, int64_t sout_bytes, bool bf16, cudaStream_t st);
 
-// ---- learned flow upsampler (vsc_upsampler.cu) ------------------------------------
+// ---- learned flow upsampler (vsc_upsampler.cu, vsc_upsampler_tc.cu) ----------------
+// Layer table: input / output channels, offsets of the weights (laid out
+// [out][tap][in], tap = 3 (dy + 1) + dx + 1) and of the biases in the
+// parameter vector.
+struct UpLayer {
+    int ci, co, w_off, b_off;
+};
+constexpr UpLayer kUpLayers[4] = {{3, 32, 0, 864}, {32, 32, 896, 896 + 9216}, {32, 32, 10144, 10144 + 9216},
+    {32, 2, 19392, 19392 + 576}};
 int upsampler_param_count();
 void upsampler_init_params(float* host, uint64_t seed);
-size_t upsampler_act_floats(int N, int H, int W);          // inference activations + residual
 size_t upsampler_train_work_floats(int N, int H, int W);   // activations and gradients of a batch
 // input (N x h x w x 3): the coarse flows bilinearly upsampled with their vectors
 // scaled to the full grid, and the frames' luma; batch n at base + n * stride
 cudaError_t launch_upsampler_prepare(const float* coarse, int cw, int ch, int cfc, const float* img, float* input,
     int w, int h, int N, int64_t s_coarse, int64_t s_img, int64_t s_in, cudaStream_t st);
-// the net with FP16 weights: act holds upsampler_act_floats - 2 px floats, r the residual (N x H x W x 2)
-cudaError_t launch_upsampler_forward_half(const __half* w16, const float* prm, const float* input, float* act,
-    float* r, int N, int H, int W, cudaStream_t st);
-cudaError_t launch_upsampler_finish(const float* input, const float* r, float* flow, int N, int64_t npx,
-    float max_residual, int64_t s_in, int64_t s_r, int64_t s_out, cudaStream_t st);
-cudaError_t launch_to_half(const float* a, __half* b, int n, cudaStream_t st);
+// Tensor-core inference (tcgen05 implicit-GEMM convolutions, FP16 operands,
+// FP32 accumulation).  Packed weights: upsampler_tc_weight_bytes() bytes,
+// written from the FP32 parameters by launch_upsampler_tc_pack.  Work:
+// upsampler_tc_work_bytes(N, H, W) bytes, 16-byte aligned.  Writes the
+// finished flows (u, v, 0) of every batch image (flow + n * s_out floats)
+// from the prepared input (launch_upsampler_prepare's layout).
+size_t upsampler_tc_weight_bytes();
+size_t upsampler_tc_work_bytes(int N, int H, int W);
+cudaError_t launch_upsampler_tc_pack(const float* prm, void* wtc, cudaStream_t st);
+cudaError_t launch_upsampler_tc(const void* wtc, const float* prm, const float* input, void* work, float* flow, int N,
+    int H, int W, float max_residual, int64_t s_out, cudaStream_t st, int* launches);
 cudaError_t upsampler_train_step(float* prm, float* grad, float* m, float* v, int step, const float* input,
     const float* target, int N, int H, int W, float lr, float* work, float* loss_dev, cudaStream_t st);
 

@@ -10,12 +10,14 @@
 // base flow (the bilinear fallback).  19,970 parameters, kept in FP32 for
 // training and rounded to FP16 for inference.
 //
-// Training and inference kernels are written here: direct convolutions on
-// the CUDA cores over NHWC activations (one thread per pixel, the layer's
-// weights in shared memory, fused multiply-adds), a backward pass for the
-// data and the weights, an L1 loss against the full-resolution flow and
-// Adam.  Nothing here has a bit-exact contract (contraction is spelled out
-// with __fmaf_rn, the library being built without automatic contraction).
+// The training kernels are written here, in FP32: direct convolutions on the
+// CUDA cores over NHWC activations (one thread per pixel, the layer's weights
+// in shared memory, fused multiply-adds), a backward pass for the data and
+// the weights, an L1 loss against the full-resolution flow and Adam.  The
+// input preparation is shared with the inference, which runs on the tensor
+// cores (vsc_upsampler_tc.cu).  Nothing here has a bit-exact contract
+// (contraction is spelled out with __fmaf_rn, the library being built
+// without automatic contraction).
 #include "vsc_internal.h"
 #include "vsc_math.cuh"
 
@@ -27,13 +29,8 @@
 namespace vsc {
 namespace {
 
-struct Layer {
-    int ci, co, w_off, b_off;
-};
-constexpr Layer kLayers[4] = {{3, 32, 0, 864}, {32, 32, 896, 896 + 9216}, {32, 32, 10144, 10144 + 9216},
-    {32, 2, 19392, 19392 + 576}};
 constexpr int kParams = 19970;
-static_assert(kLayers[3].b_off + 2 == kParams, "parameter layout");
+static_assert(kUpLayers[3].b_off + 2 == kParams, "parameter layout");
 constexpr int kThreads = 128;
 
 __device__ __forceinline__ float luma(const float* p) { return 0.299f * p[0] + 0.587f * p[1] + 0.114f * p[2]; }
@@ -226,30 +223,6 @@ __global__ void adam_kernel(float* __restrict__ prm, const float* __restrict__ g
     prm[i] -= lr * (m[i] / c1) / (sqrtf(v[i] / c2) + eps);
 }
 
-// flow = base + r where the residual is small, else base; (u, v, 0)
-__global__ void finish_kernel(const float* __restrict__ input, const float* __restrict__ r, float* __restrict__ flow,
-    int64_t npx, float max_residual, int64_t s_in, int64_t s_r, int64_t s_out)
-{
-    const int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-    if (p >= npx)
-        return;
-    const int n = blockIdx.y;
-    const float* in = input + n * s_in + p * 3;
-    const float* rr = r + n * s_r + p * 2;
-    const bool take = fmaxf(fabsf(rr[0]), fabsf(rr[1])) <= max_residual;
-    float* o = flow + n * s_out + p * 3;
-    o[0] = take ? in[0] + rr[0] : in[0];
-    o[1] = take ? in[1] + rr[1] : in[1];
-    o[2] = 0.0f;
-}
-
-__global__ void to_half_kernel(const float* __restrict__ a, __half* __restrict__ b, int n)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n)
-        b[i] = __float2half_rn(a[i]);
-}
-
 uint64_t splitmix(uint64_t* s)
 {
     uint64_t z = (*s += 0x9E3779B97F4A7C15ULL);
@@ -265,14 +238,14 @@ cudaError_t forward(const WT* wts, const float* prm, const float* input, float* 
 {
     const int64_t HW = static_cast<int64_t>(H) * W;
     const dim3 g(static_cast<unsigned>((HW + kThreads - 1) / kThreads), N);
-    const WT* w0 = wts + kLayers[0].w_off;
-    const WT* w1 = wts + kLayers[1].w_off;
-    const WT* w2 = wts + kLayers[2].w_off;
-    const WT* w3 = wts + kLayers[3].w_off;
-    conv_fwd_kernel<3, 32, true, WT><<<g, kThreads, 0, st>>>(input, w0, prm + kLayers[0].b_off, a1, H, W);
-    conv_fwd_kernel<32, 32, true, WT><<<g, kThreads, 0, st>>>(a1, w1, prm + kLayers[1].b_off, a2, H, W);
-    conv_fwd_kernel<32, 32, true, WT><<<g, kThreads, 0, st>>>(a2, w2, prm + kLayers[2].b_off, a3, H, W);
-    conv_fwd_kernel<32, 2, false, WT><<<g, kThreads, 0, st>>>(a3, w3, prm + kLayers[3].b_off, r, H, W);
+    const WT* w0 = wts + kUpLayers[0].w_off;
+    const WT* w1 = wts + kUpLayers[1].w_off;
+    const WT* w2 = wts + kUpLayers[2].w_off;
+    const WT* w3 = wts + kUpLayers[3].w_off;
+    conv_fwd_kernel<3, 32, true, WT><<<g, kThreads, 0, st>>>(input, w0, prm + kUpLayers[0].b_off, a1, H, W);
+    conv_fwd_kernel<32, 32, true, WT><<<g, kThreads, 0, st>>>(a1, w1, prm + kUpLayers[1].b_off, a2, H, W);
+    conv_fwd_kernel<32, 32, true, WT><<<g, kThreads, 0, st>>>(a2, w2, prm + kUpLayers[2].b_off, a3, H, W);
+    conv_fwd_kernel<32, 2, false, WT><<<g, kThreads, 0, st>>>(a3, w3, prm + kUpLayers[3].b_off, r, H, W);
     return cudaGetLastError();
 }
 
@@ -283,7 +256,7 @@ int upsampler_param_count() { return kParams; }
 void upsampler_init_params(float* host, uint64_t seed)
 {
     uint64_t s = seed;
-    for (const Layer& l : kLayers) {
+    for (const UpLayer& l : kUpLayers) {
         const float bound = std::sqrt(6.0f / static_cast<float>(9 * l.ci));  // He-uniform
         for (int i = 0; i < l.co * 9 * l.ci; ++i)
             host[l.w_off + i] = (static_cast<float>(splitmix(&s) >> 40) * (1.0f / 16777216.0f) * 2.0f - 1.0f) * bound;
@@ -291,11 +264,9 @@ void upsampler_init_params(float* host, uint64_t seed)
             host[l.b_off + i] = 0.0f;
     }
     // the last layer starts near zero: the initial prediction is the base flow
-    for (int i = 0; i < kLayers[3].co * 9 * kLayers[3].ci; ++i)
-        host[kLayers[3].w_off + i] *= 0.01f;
+    for (int i = 0; i < kUpLayers[3].co * 9 * kUpLayers[3].ci; ++i)
+        host[kUpLayers[3].w_off + i] *= 0.01f;
 }
-
-size_t upsampler_act_floats(int N, int H, int W) { return static_cast<size_t>(N) * H * W * (32 * 3 + 2); }
 
 cudaError_t launch_upsampler_prepare(const float* coarse, int cw, int ch, int cfc, const float* img, float* input, int w,
     int h, int N, int64_t s_coarse, int64_t s_img, int64_t s_in, cudaStream_t st)
@@ -303,27 +274,6 @@ cudaError_t launch_upsampler_prepare(const float* coarse, int cw, int ch, int cf
     const dim3 b(32, 8);
     const dim3 g((w + 31) / 32, (h + 7) / 8, N);
     prepare_kernel<<<g, b, 0, st>>>(coarse, cw, ch, cfc, img, input, w, h, s_coarse, s_img, s_in);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_upsampler_forward_half(const __half* w16, const float* prm, const float* input, float* act, float* r,
-    int N, int H, int W, cudaStream_t st)
-{
-    const size_t px = static_cast<size_t>(N) * H * W;
-    return forward<__half>(w16, prm, input, act, act + px * 32, act + px * 64, r, N, H, W, st);
-}
-
-cudaError_t launch_upsampler_finish(const float* input, const float* r, float* flow, int N, int64_t npx,
-    float max_residual, int64_t s_in, int64_t s_r, int64_t s_out, cudaStream_t st)
-{
-    const dim3 g(static_cast<unsigned>((npx + 255) / 256), N);
-    finish_kernel<<<g, 256, 0, st>>>(input, r, flow, npx, max_residual, s_in, s_r, s_out);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_to_half(const float* a, __half* b, int n, cudaStream_t st)
-{
-    to_half_kernel<<<(n + 255) / 256, 256, 0, st>>>(a, b, n);
     return cudaGetLastError();
 }
 
@@ -354,20 +304,20 @@ cudaError_t upsampler_train_step(float* prm, float* grad, float* m, float* v, in
     const dim3 g(static_cast<unsigned>((HW + kThreads - 1) / kThreads), N);
     const unsigned slices = static_cast<unsigned>(std::min<int64_t>(64, (px + 4095) / 4096));
     // layer 4 (32 -> 2)
-    conv_wgrad_kernel<32, 2><<<dim3(2, 9, slices), kThreads, 0, st>>>(a3, dr, grad + kLayers[3].w_off,
-        grad + kLayers[3].b_off, N, H, W);
-    conv_bwd_data_kernel<32, 2, true><<<g, kThreads, 0, st>>>(dr, prm + kLayers[3].w_off, a3, dz3, H, W);
+    conv_wgrad_kernel<32, 2><<<dim3(2, 9, slices), kThreads, 0, st>>>(a3, dr, grad + kUpLayers[3].w_off,
+        grad + kUpLayers[3].b_off, N, H, W);
+    conv_bwd_data_kernel<32, 2, true><<<g, kThreads, 0, st>>>(dr, prm + kUpLayers[3].w_off, a3, dz3, H, W);
     // layer 3
-    conv_wgrad_kernel<32, 32><<<dim3(32, 9, slices), kThreads, 0, st>>>(a2, dz3, grad + kLayers[2].w_off,
-        grad + kLayers[2].b_off, N, H, W);
-    conv_bwd_data_kernel<32, 32, true><<<g, kThreads, 0, st>>>(dz3, prm + kLayers[2].w_off, a2, dz2, H, W);
+    conv_wgrad_kernel<32, 32><<<dim3(32, 9, slices), kThreads, 0, st>>>(a2, dz3, grad + kUpLayers[2].w_off,
+        grad + kUpLayers[2].b_off, N, H, W);
+    conv_bwd_data_kernel<32, 32, true><<<g, kThreads, 0, st>>>(dz3, prm + kUpLayers[2].w_off, a2, dz2, H, W);
     // layer 2
-    conv_wgrad_kernel<32, 32><<<dim3(32, 9, slices), kThreads, 0, st>>>(a1, dz2, grad + kLayers[1].w_off,
-        grad + kLayers[1].b_off, N, H, W);
-    conv_bwd_data_kernel<32, 32, true><<<g, kThreads, 0, st>>>(dz2, prm + kLayers[1].w_off, a1, dz1, H, W);
+    conv_wgrad_kernel<32, 32><<<dim3(32, 9, slices), kThreads, 0, st>>>(a1, dz2, grad + kUpLayers[1].w_off,
+        grad + kUpLayers[1].b_off, N, H, W);
+    conv_bwd_data_kernel<32, 32, true><<<g, kThreads, 0, st>>>(dz2, prm + kUpLayers[1].w_off, a1, dz1, H, W);
     // layer 1 (3 -> 32): weights only
-    conv_wgrad_kernel<3, 32><<<dim3(32, 9, slices), kThreads, 0, st>>>(input, dz1, grad + kLayers[0].w_off,
-        grad + kLayers[0].b_off, N, H, W);
+    conv_wgrad_kernel<3, 32><<<dim3(32, 9, slices), kThreads, 0, st>>>(input, dz1, grad + kUpLayers[0].w_off,
+        grad + kUpLayers[0].b_off, N, H, W);
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.0f - std::pow(b1, static_cast<float>(step)), c2 = 1.0f - std::pow(b2, static_cast<float>(step));
     adam_kernel<<<(kParams + 255) / 256, 256, 0, st>>>(prm, grad, m, v, kParams, lr, b1, b2, c1, c2, 1e-8f);
