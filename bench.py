@@ -607,6 +607,49 @@ def run_solver_only(args):
     print(json.dumps(solver_roofline(vsc, dev, stream, iters=args.steps * 8)))
 
 
+def run_upsampler_only(args):
+    """--kernel upsampler: the learned 2x upsampler's inference on one
+    1920x1080 flow (vsc_upsampler_apply: input preparation, FP16 conversion,
+    the four tensor-core convolutions with the fallback test fused into the
+    last), CUDA events on its stream.  Algorithmic bytes per pixel: prepare
+    12 in (frame; the coarse flow is a quarter of the pixels, 3 B) + 12 out,
+    conversion 12 in + 16 out, layer 1 16 in + 64 out, layers 2-3 64 in + 64
+    out each, layer 4 64 + 12 in + 12 out: 423 B/px.  Tensor work: 2 x 9 x
+    (16 x 32 + 32 x 32 + 32 x 32 + 32 x 16) FLOP per pixel as issued
+    (channels padded to the MMA shape; 39,744 FLOP/px useful)."""
+    import torch
+
+    vsc = import_pkg()
+    vsc.build()
+    vsc.load()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    g = torch.Generator(device=dev).manual_seed(9)
+    coarse = (torch.randn((H // 2, W // 2, 3), device=dev, generator=g) * 2).contiguous()
+    frame = torch.rand((H, W, 3), device=dev, generator=g)
+    up = vsc.Upsampler("default")
+    out = torch.empty_like(frame)
+    for _ in range(max(args.warmup, 3)):
+        vsc.load().vsc_upsampler_apply(up._h, *(vsc.C.byref(vsc.image(t)) for t in (coarse, frame, out)),
+                                      vsc._stream(stream))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        vsc._check(vsc.load().vsc_upsampler_apply(up._h, *(vsc.C.byref(vsc.image(t)) for t in (coarse, frame, out)),
+                                                  vsc._stream(stream)))
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    peak, peak_src = peaks()
+    alg = 423 * W * H
+    flops = 2 * 9 * (16 * 32 + 32 * 32 + 32 * 32 + 32 * 16) * W * H
+    print(json.dumps({"kernel": "learned upsampler inference (vsc_upsampler_apply) 1920x1080", "ms": ms,
+                      "algorithmic_bytes": alg, "achieved_gbs": alg / (ms / 1000) / 1e9,
+                      "frac_hbm": alg / (ms / 1000) / 1e9 / peak, "tensor_tflops_issued": flops / (ms / 1000) / 1e12,
+                      "peak_gbs": peak, "peak_source": peak_src}))
+    up.close()
+
+
 # ---------------------------------------------------------------------------
 # Forms of the per-frame path.  "plain" is the method as the reference runs
 # it (FP32 correlations, flow at full resolution); the others change only the
@@ -832,7 +875,7 @@ def main():
                     help="multistream: the 16-stream mixed-resolution workload (a separate line)")
     ap.add_argument("--form", choices=sorted(FORMS), default="bf16_ds2",
                     help="the chosen form reported as value (the plain path is timed beside it)")
-    ap.add_argument("--kernel", choices=["step", "solver", "corr", "front"], default="step",
+    ap.add_argument("--kernel", choices=["step", "solver", "corr", "front", "upsampler"], default="step",
                     help="solver / corr: time only the 1920x1080 solver or the correlation pyramid "
                          "(profiler targets)")
     args = ap.parse_args()
@@ -848,6 +891,8 @@ def main():
         run_corr_only(args)
     elif args.kernel == "front":
         run_front_only(args)
+    elif args.kernel == "upsampler":
+        run_upsampler_only(args)
     else:
         run_gpu(args)
 

@@ -1,33 +1,38 @@
 // Inference of the learned flow upsampler on the tensor cores (tcgen05).
 //
-// Each 3x3 convolution (zero padding) is an implicit GEMM.  For one output
-// row y and a segment of kUpM = 128 pixels starting at x0,
-//     D[m][o] = sum over taps t = (ty, tx) and input channels c of
-//               act[c][y + ty - 1][x0 + m + tx - 1] * w[o][t][c],
-// which is nine MMA chains (one per tap, K = input channels in steps of 16)
-// into one accumulator of M = 128 pixels x N output channels in Tensor
-// Memory.  Activations are FP16 in a chunked planar layout
-//     [n][c / 8][y][x][c % 8],
-// so one TMA box {8, 130, kUpR + 2, chunks} brings a band of kUpR + 2 rows x
-// 130 pixels (the segment with its one-pixel halo; zero-filled outside the
-// image, which is the convolution's zero padding) into shared memory as
-// [chunk][row][pixel][8].  The A operand of tap (ty, tx) for output row r is
-// that buffer seen from (row r + ty, pixel tx): 8 consecutive pixels x 16
-// bytes are one core matrix, M-adjacent core matrices 128 bytes apart,
-// K-adjacent ones one chunk plane apart.  Weights [tap][chunk][out][8] (FP16,
-// out padded to the MMA's N, in to the K chunks) stay in shared memory for the
-// whole launch.  The first layer's three input channels (base flow u, v and
-// luma) occupy one chunk; its second K chunk is a zero plane that is never
-// loaded.
+// Each 3x3 convolution (zero padding) is an implicit GEMM.  Activations are
+// FP16 in a chunked planar layout [n][c / 8][y][x][c % 8].  For a segment of
+// kUpM = 128 output positions x0 ... x0 + 127 and one input row j,
+//     D_j[x][ty][o] = sum over tx and input channels c of
+//                     act[c][j][x + tx - 1] * w[o][ty][tx][c],
+// three MMA chains (one per horizontal tap tx, K = input channels in steps of
+// 16) of M = 128 positions x N = 3 x (output channels), accumulated in one
+// Tensor Memory slot per input row.  Output row y is then
+//     out[o][y][x] = D_{y-1}[x][0][o] + D_y[x][1][o] + D_{y+1}[x][2][o] + bias,
+// three slots read by the same Tensor Memory lane: no exchange between lanes.
+// A tcgen05.mma of M = 128, K = 16 costs about max(45, N / 2) cycles on
+// GB300, so folding the three vertical taps into N (96 columns) issues 2.7x
+// fewer MMAs than one chain per tap with N = 32, at a third of the cycles.
+// A work item is a segment of kUpRC output rows; its kUpRC + 2 input rows
+// stream through a ring of row buffers (one TMA box {8, 130, 1, chunks} per
+// row: the segment with its one-pixel halo, zero-filled outside the image,
+// which is the convolution's zero padding) and a ring of Tensor Memory slots.
+// The A operand is a row buffer seen from position tx (8 positions x 16 bytes
+// per core matrix, M-adjacent core matrices 128 bytes apart, K-adjacent ones
+// a chunk plane apart).  Weights [tx][chunk][ty * NO + o][8] (FP16, output
+// channels padded to NO, input channels to the K chunks) stay in shared
+// memory for the launch.  The first layer's three input channels (base flow
+// u, v and luma) occupy one chunk; its second K chunk is a zero plane that is
+// never loaded.
 //
-// Persistent and warp-specialised: warp 0 issues the TMA loads (a ring of
-// band buffers), warp 1 the MMAs (and owns Tensor Memory; two accumulator
-// sets of kUpR rows), warps 2-5 the epilogue, one per 32 Tensor Memory lanes:
-// bias, ReLU, FP16 and the chunked store for the inner layers; for the last
-// layer the residual test and the finished flow (base + r where
-// max(|r_u|, |r_v|) <= max_residual, else base).  Every mbarrier wait is
-// bounded; a wait that runs out stops all roles and sets the device timeout
-// flag.
+// Persistent and warp-specialised: warp 0 issues the TMA loads, warp 1 the
+// MMAs (and owns Tensor Memory), then kUpGroups epilogue groups taking
+// alternate output rows, each of eight warps: two per 32 Tensor Memory lanes,
+// splitting the output channels.  Epilogue: bias, ReLU, FP16 and the chunked
+// store for the inner layers; for the last layer the residual test and the
+// finished flow (base + r where max(|r_u|, |r_v|) <= max_residual, else
+// base).  Every mbarrier wait is bounded; a wait that runs out stops all
+// roles and sets the device timeout flag.
 #include "vsc_internal.h"
 #include "vsc_math.cuh"
 #include "vsc_ptx.cuh"
@@ -39,23 +44,28 @@
 namespace vsc {
 namespace {
 
-constexpr int kUpM = 128;               // pixels per segment (MMA M, Tensor Memory lanes)
-constexpr int kUpR = 4;                 // output rows per band
-constexpr int kUpTW = kUpM + 2;         // band width with the halo
-constexpr int kUpStages = 3;            // band buffers
-constexpr uint32_t kUpTmemCols = 256;   // two accumulator sets of kUpR x 32 columns
-constexpr int kUpWaitSpins = 1 << 22;   // bounded mbarrier waits (about a second)
-constexpr int kUpThreads = 6 * 32;
-constexpr int kUpPlaneBytes = (kUpR + 2) * kUpTW * 16;  // one chunk plane of a band
+constexpr int kUpM = 128;                // output positions per segment (MMA M, Tensor Memory lanes)
+constexpr int kUpRC = 16;                // output rows per work item
+constexpr int kUpRows = kUpRC + 2;       // input rows per work item
+constexpr int kUpTW = kUpM + 2;          // positions loaded per row (one-pixel halo)
+constexpr int kUpRowBufs = 16;           // row buffers in shared memory (TMA loads in flight)
+constexpr int kUpSlots = 5;              // input-row accumulators in Tensor Memory
+constexpr int kUpSlotCols = 96;          // columns per accumulator (3 x 32)
+constexpr uint32_t kUpTmemCols = 512;
+constexpr int kUpGroups = 2;             // epilogue groups (output rows alternate between them)
+constexpr int kUpEpiWarps = 8;           // warps per group: 4 lane quarters x 2 channel halves
+constexpr int kUpWaitSpins = 1 << 22;    // bounded mbarrier waits (about a second)
+constexpr int kUpThreads = (2 + kUpEpiWarps * kUpGroups) * 32;
+constexpr int kUpPlaneBytes = kUpTW * 16;  // one chunk plane of a row buffer
 constexpr int kUpSmemLimit = 232448;
 constexpr uint32_t kUpMinSmem = 120 * 1024;
-static_assert(kUpPlaneBytes % 16 == 0, "chunk planes on the 16-byte grid");
-static_assert(2 * kUpR * 32 <= static_cast<int>(kUpTmemCols), "accumulators inside the allocation");
+static_assert(kUpSlots >= kUpGroups + 2 && kUpSlots * kUpSlotCols <= static_cast<int>(kUpTmemCols),
+    "accumulator ring");
 
 __host__ __device__ constexpr uint32_t up_align1k(uint32_t v) { return (v + 1023u) & ~1023u; }
 
 // Per-layer shape: kch K chunks of 8 channels (lch of them loaded, the rest
-// zero), no output columns of the MMA.
+// zero), no output channels per vertical tap in the MMA (N = 3 no).
 struct TcLayer {
     int kch, lch, no, ci, co;
     size_t wt_off;  // byte offset of the layer's packed weights
@@ -63,13 +73,17 @@ struct TcLayer {
 constexpr TcLayer kTcLayers[4] = {{2, 1, 32, 3, 32, 0}, {4, 4, 32, 32, 32, 9216}, {4, 4, 32, 32, 32, 27648},
     {4, 4, 16, 32, 2, 46080}};
 constexpr size_t kTcWeightBytes = 55296;
-static_assert(kTcLayers[3].wt_off + 9 * 4 * 16 * 16 == kTcWeightBytes, "packed weight layout");
 
-__host__ __device__ constexpr uint32_t up_weight_bytes(int kch, int no) { return 9u * kch * no * 16u; }
+__host__ __device__ constexpr uint32_t up_weight_bytes(int kch, int no) { return 3u * kch * 3u * no * 16u; }
+static_assert(kTcLayers[3].wt_off + up_weight_bytes(4, 16) == kTcWeightBytes, "packed weight layout");
 
+// row buffers, weights, bias, barriers (full / empty per row buffer, full / empty per
+// slot, the drain barrier, the Tensor Memory address and the abort flag)
+constexpr uint32_t kBarBytes = (2 * kUpRowBufs + 2 * kUpSlots + 3) * 8;
 __host__ __device__ constexpr uint32_t up_smem_bytes(int kch, int no)
 {
-    return 1024 + kUpStages * up_align1k(kch * kUpPlaneBytes) + up_align1k(up_weight_bytes(kch, no)) + 32 * 4 + 256;
+    return 1024 + kUpRowBufs * up_align1k(kch * kUpPlaneBytes) + up_align1k(up_weight_bytes(kch, no)) + 32 * 4 +
+           kBarBytes;
 }
 
 // Bounded wait that also gives up when another role has aborted; a wait that
@@ -97,35 +111,39 @@ __global__ void __launch_bounds__(kUpThreads, 1)
         float* __restrict__ flow, int64_t s_out, float max_residual, int N, int H, int W,
         int* __restrict__ timeout_flag)
 {
-    constexpr uint32_t kStageBytes = up_align1k(KCH * kUpPlaneBytes);
+    constexpr int N3 = 3 * NO;                    // MMA N: the three vertical taps
+    constexpr int KH = 16;                        // output channels per epilogue warp (half of 32)
+    constexpr uint32_t kRowBytes = up_align1k(KCH * kUpPlaneBytes);
     constexpr uint32_t kWBytes = up_weight_bytes(KCH, NO);
-    constexpr uint32_t idesc = ptx::umma_idesc_f16(false, kUpM, NO);
+    constexpr uint32_t idesc = ptx::umma_idesc_f16(false, kUpM, N3);
+    static_assert(N3 <= kUpSlotCols && N3 % 16 == 0, "MMA N");
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base =
         reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-    unsigned char* stages = base;
-    unsigned char* wts = stages + kUpStages * kStageBytes;
+    unsigned char* rows = base;
+    unsigned char* wts = rows + kUpRowBufs * kRowBytes;
     float* sbias = reinterpret_cast<float*>(wts + up_align1k(kWBytes));
     uint64_t* bars = reinterpret_cast<uint64_t*>(sbias + 32);
-    uint64_t* full = bars;            // [kUpStages]
-    uint64_t* empty = bars + 3;       // [kUpStages]
-    uint64_t* dfull = bars + 6;       // [2]
-    uint64_t* dempty = bars + 8;      // [2]
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 10);
-    volatile int* abort = reinterpret_cast<volatile int*>(bars + 11);
+    uint64_t* full = bars;                        // [kUpRowBufs]
+    uint64_t* empty = full + kUpRowBufs;          // [kUpRowBufs]
+    uint64_t* sfull = empty + kUpRowBufs;         // [kUpSlots]
+    uint64_t* sempty = sfull + kUpSlots;          // [kUpSlots]
+    uint64_t* drain = sempty + kUpSlots;          // the MMA issuer's last commit on abort
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+    volatile int* abort = reinterpret_cast<volatile int*>(drain + 2);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nseg = (W + kUpM - 1) / kUpM, nband = (H + kUpR - 1) / kUpR;
-    const int items = N * nband * nseg;
+    const int nseg = (W + kUpM - 1) / kUpM, nchunk = (H + kUpRC - 1) / kUpRC;
+    const int items = N * nchunk * nseg;
 
     // weights and bias into shared memory; the K chunks that are never loaded are zero
     for (uint32_t i = threadIdx.x; i < kWBytes / 16; i += blockDim.x)
         reinterpret_cast<uint4*>(wts)[i] = wpk[i];
-    for (int i = threadIdx.x; i < NO; i += blockDim.x)
+    for (int i = threadIdx.x; i < 32; i += blockDim.x)
         sbias[i] = i < co ? bias[i] : 0.0f;
     if (LCH < KCH) {
-        for (int s = 0; s < kUpStages; ++s) {
-            uint4* z = reinterpret_cast<uint4*>(stages + s * kStageBytes + LCH * kUpPlaneBytes);
+        for (int b = 0; b < kUpRowBufs; ++b) {
+            uint4* z = reinterpret_cast<uint4*>(rows + b * kRowBytes + LCH * kUpPlaneBytes);
             for (int i = threadIdx.x; i < (KCH - LCH) * kUpPlaneBytes / 16; i += blockDim.x)
                 z[i] = make_uint4(0u, 0u, 0u, 0u);
         }
@@ -137,124 +155,159 @@ __global__ void __launch_bounds__(kUpThreads, 1)
     }
     if (threadIdx.x == 0) {
         *abort = 0;
-        for (int i = 0; i < kUpStages; ++i) {
+        for (int i = 0; i < kUpRowBufs; ++i) {
             ptx::mbar_init(&full[i], 1);
             ptx::mbar_init(&empty[i], 1);
         }
-        for (int i = 0; i < 2; ++i) {
-            ptx::mbar_init(&dfull[i], 1);
-            ptx::mbar_init(&dempty[i], 4);  // one arrival per epilogue warp
+        for (int i = 0; i < kUpSlots; ++i) {
+            ptx::mbar_init(&sfull[i], 1);
+            // every input row is released by three output rows' eight warps (rows at an
+            // item's edge, read fewer times, are topped up by one of their readers)
+            ptx::mbar_init(&sempty[i], 3 * kUpEpiWarps);
         }
+        ptx::mbar_init(drain, 1);
     }
     ptx::tc_fence_before();
     __syncthreads();
     ptx::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
+    // input rows are counted over the whole CTA (u): row buffer u % kUpRowBufs,
+    // Tensor Memory slot u % kUpSlots; item k of the CTA owns rows k * kUpRows ...
     if (warp == 0) {
         // ---- TMA producer -------------------------------------------------------------
         if (lane == 0) {
             int u = 0;
-            for (int it = blockIdx.x; it < items; it += gridDim.x) {
+            bool ok = true;
+            for (int it = blockIdx.x; ok && it < items; it += gridDim.x) {
                 const int seg = it % nseg, rest = it / nseg;
-                const int band = rest % nband, n = rest / nband;
-                const int s = u % kUpStages;
-                if (!up_wait(&empty[s], ((u / kUpStages) & 1) ^ 1, abort))
-                    break;
-                ptx::mbar_expect_tx(&full[s], LCH * kUpPlaneBytes);
-                ptx::tma_load_5d(stages + s * kStageBytes, &mIn, 0, seg * kUpM - 1, band * kUpR - 1, 0, n, &full[s]);
-                ++u;
+                const int chunk = rest % nchunk, n = rest / nchunk;
+                for (int i = 0; i < kUpRows; ++i, ++u) {
+                    const int b = u % kUpRowBufs;
+                    if (!(ok = up_wait(&empty[b], ((u / kUpRowBufs) & 1) ^ 1, abort)))
+                        break;
+                    ptx::mbar_expect_tx(&full[b], LCH * kUpPlaneBytes);
+                    ptx::tma_load_5d(rows + b * kRowBytes, &mIn, 0, seg * kUpM - 1, chunk * kUpRC - 1 + i, 0, n,
+                        &full[b]);
+                }
             }
             if (*abort)  // let every copy issued land before the CTA exits
-                for (int i = 0; i < kUpStages && i < u; ++i) {
+                for (int i = 0; i < kUpRowBufs && i < u; ++i) {
                     const int v = u - 1 - i;
-                    ptx::mbar_wait_bounded(&full[v % kUpStages], (v / kUpStages) & 1, kUpWaitSpins);
+                    ptx::mbar_wait_bounded(&full[v % kUpRowBufs], (v / kUpRowBufs) & 1, kUpWaitSpins);
                 }
         }
     } else if (warp == 1) {
         // ---- MMA issuer ---------------------------------------------------------------
         if (lane == 0) {
-            int u = 0, ud = 0;
-            const uint32_t w0 = ptx::smem_u32(wts);
-            for (int it = blockIdx.x; it < items; it += gridDim.x) {
-                const int s = u % kUpStages, b = ud & 1;
-                if (!up_wait(&full[s], (u / kUpStages) & 1, abort))
-                    break;
-                if (!up_wait(&dempty[b], ((ud >> 1) & 1) ^ 1, abort))
-                    break;
-                ptx::tc_fence_after();
-                const uint32_t a0 = ptx::smem_u32(stages + s * kStageBytes);
-                for (int r = 0; r < kUpR; ++r) {
-                    const uint32_t dcol = tmem + b * (kUpR * NO) + r * NO;
+            int u = 0;
+            bool ok = true;
+            // Descriptors are built once; an operand at byte offset d from its base is
+            // the base descriptor + d / 16 (the start-address field, which cannot carry:
+            // shared memory stays below 256 KB).  The offsets below are compile-time
+            // constants, so an MMA costs two 64-bit adds to issue.
+            const uint64_t adesc0 = ptx::umma_desc_kmajor(ptx::smem_u32(rows), kUpPlaneBytes, 128);
+            const uint64_t bdesc0 = ptx::umma_desc_kmajor(ptx::smem_u32(wts), N3 * 16, 128);
+            for (int it = blockIdx.x; ok && it < items; it += gridDim.x) {
+                for (int i = 0; i < kUpRows; ++i, ++u) {
+                    const int b = u % kUpRowBufs, sl = u % kUpSlots;
+                    if (!(ok = up_wait(&full[b], (u / kUpRowBufs) & 1, abort)))
+                        break;
+                    if (!(ok = up_wait(&sempty[sl], ((u / kUpSlots) & 1) ^ 1, abort)))
+                        break;
+                    ptx::tc_fence_after();
+                    const uint64_t ab = adesc0 + ((b * kRowBytes) >> 4);
+                    const uint32_t dcol = tmem + sl * kUpSlotCols;
 #pragma unroll
-                    for (int t = 0; t < 9; ++t) {
-                        const int ty = t / 3, tx = t % 3;
+                    for (int tx = 0; tx < 3; ++tx) {
 #pragma unroll
                         for (int k = 0; k < KCH / 2; ++k) {
-                            const uint64_t ad = ptx::umma_desc_kmajor(
-                                a0 + 2 * k * kUpPlaneBytes + ((r + ty) * kUpTW + tx) * 16, kUpPlaneBytes, 128);
-                            const uint64_t bd = ptx::umma_desc_kmajor(w0 + (t * KCH + 2 * k) * NO * 16, NO * 16, 128);
-                            ptx::umma_f16(dcol, ad, bd, idesc, t > 0 || k > 0);
+                            const uint64_t ad = ab + ((2 * k * kUpPlaneBytes + tx * 16) >> 4);
+                            const uint64_t bd = bdesc0 + (((tx * KCH + 2 * k) * N3 * 16) >> 4);
+                            ptx::umma_f16(dcol, ad, bd, idesc, tx > 0 || k > 0);
                         }
                     }
+                    ptx::umma_commit(&sfull[sl]);  // row accumulator ready
+                    ptx::umma_commit(&empty[b]);   // row buffer read
                 }
-                ptx::umma_commit(&dfull[b]);   // accumulators ready
-                ptx::umma_commit(&empty[s]);   // band buffer read
-                ++u;
-                ++ud;
             }
-            if (*abort && ud > 0) {  // the MMAs in flight finish before Tensor Memory is freed
-                const int v = ud - 1;
-                ptx::mbar_wait_bounded(&dfull[v & 1], (v >> 1) & 1, kUpWaitSpins);
+            if (*abort) {  // the MMAs in flight finish before Tensor Memory is freed
+                ptx::umma_commit(drain);
+                ptx::mbar_wait_bounded(drain, 0, kUpWaitSpins);
             }
         }
     } else {
-        // ---- epilogue: Tensor Memory -> registers -> global ------------------------------
-        const int q = warp & 3;  // this warp's 32 Tensor Memory lanes
+        // ---- epilogue: three row accumulators -> registers -> global ----------------------
+        const int e = warp - 2;
+        const int q = warp & 3;                   // this warp's 32 Tensor Memory lanes
+        const int half = (e >> 2) & 1;            // output channels half * 16 ... + 15
+        const int grp = e >> 3;                   // output rows i with i % kUpGroups == grp
+        const bool active = !kFinish || half == 0;  // the last layer has two output channels
         const uint32_t lane_base = static_cast<uint32_t>(q * 32) << 16;
         const int64_t HW = static_cast<int64_t>(H) * W;
-        int ud = 0;
-        for (int it = blockIdx.x; it < items; it += gridDim.x, ++ud) {
+        int u0 = 0;  // the item's first input row
+        bool ok = true;
+        for (int it = blockIdx.x; ok && it < items; it += gridDim.x, u0 += kUpRows) {
             const int seg = it % nseg, rest = it / nseg;
-            const int band = rest % nband, n = rest / nband;
-            const int b = ud & 1;
-            // warp-uniform outcome: the Tensor Memory loads below are warp-collective
-            if (!__all_sync(0xffffffffu, up_wait(&dfull[b], (ud >> 1) & 1, abort)))
-                break;
-            ptx::tc_fence_after();
+            const int chunk = rest % nchunk, n = rest / nchunk;
             const int x = seg * kUpM + q * 32 + lane;
-            for (int r = 0; r < kUpR; ++r) {
-                const int y = band * kUpR + r;
-                const uint32_t ta = tmem + lane_base + b * (kUpR * NO) + r * NO;
-                const bool inside = x < W && y < H;
-                const int64_t p = static_cast<int64_t>(y) * W + x;
-                if (!kFinish) {
-                    uint32_t v[32];
-                    ptx::tmem_ld32(ta, v);
+            for (int i = grp; i < kUpRC; i += kUpGroups) {
+                // output row y = chunk * kUpRC + i reads input rows u0 + i + ty, ty = 0, 1, 2
+                for (int ty = 0; ty < 3 && ok; ++ty) {
+                    const int v = u0 + i + ty;
+                    // warp-uniform outcome: the Tensor Memory loads below are warp-collective
+                    ok = __all_sync(0xffffffffu, up_wait(&sfull[v % kUpSlots], (v / kUpSlots) & 1, abort));
+                }
+                if (!ok)
+                    break;
+                ptx::tc_fence_after();
+                float acc[KH];
+                if (active) {
+                    const uint32_t c0 = half * KH;
+                    const uint32_t ta0 = tmem + lane_base + ((u0 + i) % kUpSlots) * kUpSlotCols + c0;
+                    const uint32_t ta1 = tmem + lane_base + ((u0 + i + 1) % kUpSlots) * kUpSlotCols + NO + c0;
+                    const uint32_t ta2 = tmem + lane_base + ((u0 + i + 2) % kUpSlots) * kUpSlotCols + 2 * NO + c0;
+                    uint32_t r0[16], r1[16], r2[16];
+                    ptx::tmem_ld16(ta0, r0);
+                    ptx::tmem_ld16(ta1, r1);
+                    ptx::tmem_ld16(ta2, r2);
                     ptx::tmem_ld_wait();
-                    if (inside) {
 #pragma unroll
-                        for (int c8 = 0; c8 < 4; ++c8) {
+                    for (int o = 0; o < KH; ++o)
+                        acc[o] = (__uint_as_float(r0[o]) + __uint_as_float(r1[o])) + __uint_as_float(r2[o]);
+                }
+                ptx::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) {
+                    // item row k = i + ty is read by outputs k - 2 ... k inside [0, kUpRC); its
+                    // reader i = min(k, kUpRC - 1) adds the arrivals of the readers it lacks
+#pragma unroll
+                    for (int ty = 0; ty < 3; ++ty) {
+                        const int k = i + ty;
+                        const int readers = min(k, kUpRC - 1) - max(k - 2, 0) + 1;
+                        const uint32_t cnt = 1u + (i == min(k, kUpRC - 1) ? static_cast<uint32_t>(3 - readers) : 0u);
+                        ptx::mbar_arrive_n(&sempty[(u0 + k) % kUpSlots], cnt);
+                    }
+                }
+                const int y = chunk * kUpRC + i;
+                if (active && x < W && y < H) {
+                    const int64_t p = static_cast<int64_t>(y) * W + x;
+                    if (!kFinish) {
+#pragma unroll
+                        for (int c = 0; c < KH / 8; ++c) {
                             uint32_t h[4];
 #pragma unroll
                             for (int j = 0; j < 4; ++j) {
-                                const int o = c8 * 8 + 2 * j;
-                                const float lo = fmaxf(__uint_as_float(v[o]) + sbias[o], 0.0f);
-                                const float hi = fmaxf(__uint_as_float(v[o + 1]) + sbias[o + 1], 0.0f);
-                                const __half2 hv = __floats2half2_rn(lo, hi);
+                                const int o = c * 8 + 2 * j, og = half * KH + o;
+                                const __half2 hv = __floats2half2_rn(fmaxf(acc[o] + sbias[og], 0.0f),
+                                    fmaxf(acc[o + 1] + sbias[og + 1], 0.0f));
                                 h[j] = *reinterpret_cast<const uint32_t*>(&hv);
                             }
-                            reinterpret_cast<uint4*>(out)[(static_cast<int64_t>(n) * 4 + c8) * HW + p] =
+                            reinterpret_cast<uint4*>(out)[(static_cast<int64_t>(n) * 4 + half * 2 + c) * HW + p] =
                                 make_uint4(h[0], h[1], h[2], h[3]);
                         }
-                    }
-                } else {
-                    uint32_t v[16];
-                    ptx::tmem_ld16(ta, v);
-                    ptx::tmem_ld_wait();
-                    if (inside) {
-                        const float ru = __uint_as_float(v[0]) + sbias[0];
-                        const float rv = __uint_as_float(v[1]) + sbias[1];
+                    } else {
+                        const float ru = acc[0] + sbias[0], rv = acc[1] + sbias[1];
                         const float* in = input + (static_cast<int64_t>(n) * HW + p) * 3;
                         const bool take = fmaxf(fabsf(ru), fabsf(rv)) <= max_residual;
                         float* o = flow + n * s_out + p * 3;
@@ -264,10 +317,6 @@ __global__ void __launch_bounds__(kUpThreads, 1)
                     }
                 }
             }
-            ptx::tc_fence_before();
-            __syncwarp();
-            if (lane == 0)
-                ptx::mbar_arrive(&dempty[b]);  // the accumulators may be overwritten
         }
     }
 
@@ -282,16 +331,17 @@ __global__ void __launch_bounds__(kUpThreads, 1)
 }
 
 // ---- operand preparation ------------------------------------------------------------
-// One layer's FP32 weights [out][tap][in] -> [tap][chunk][out][8] in FP16,
-// zero for padded input and output channels.
+// One layer's FP32 weights [out][tap][in] -> [tx][chunk][ty * no + out][8] in
+// FP16, zero for padded input and output channels.
 __global__ void up_pack_weights_kernel(const float* __restrict__ w, int ci, int co, int kch, int no,
     __half* __restrict__ wtc)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= 9 * kch * no * 8)
+    const int n3 = 3 * no;
+    if (i >= 3 * kch * n3 * 8)
         return;
-    const int j = i % 8, o = (i / 8) % no, c8 = (i / (8 * no)) % kch, t = i / (8 * no * kch);
-    const int c = c8 * 8 + j;
+    const int j = i % 8, nr = (i / 8) % n3, c8 = (i / (8 * n3)) % kch, tx = i / (8 * n3 * kch);
+    const int ty = nr / no, o = nr % no, t = ty * 3 + tx, c = c8 * 8 + j;
     wtc[i] = __float2half_rn(o < co && c < ci ? w[(o * 9 + t) * ci + c] : 0.0f);
 }
 
@@ -315,7 +365,7 @@ bool encode_act_map(CUtensorMap* m, const void* base, int N, int H, int W, int c
         static_cast<cuuint64_t>(chunks), static_cast<cuuint64_t>(N)};
     const cuuint64_t plane = static_cast<cuuint64_t>(H) * W * 16;
     const cuuint64_t strides[4] = {16, static_cast<cuuint64_t>(W) * 16, plane, plane * chunks};
-    const cuuint32_t box[5] = {8, kUpTW, kUpR + 2, static_cast<cuuint32_t>(chunks), 1};
+    const cuuint32_t box[5] = {8, kUpTW, 1, static_cast<cuuint32_t>(chunks), 1};
     const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 5, const_cast<void*>(base), dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -340,7 +390,7 @@ cudaError_t run_layer(int l, const void* wtc, const float* prm, const void* in, 
     CUtensorMap m;
     if (!encode_act_map(&m, in, N, H, W, LCH))
         return cudaErrorInvalidValue;
-    const int items = N * ((H + kUpR - 1) / kUpR) * ((W + kUpM - 1) / kUpM);
+    const int items = N * ((H + kUpRC - 1) / kUpRC) * ((W + kUpM - 1) / kUpM);
     up_conv_tc_kernel<KCH, LCH, NO, kFinish><<<std::min(items, sms), kUpThreads, smem, st>>>(m,
         reinterpret_cast<const uint4*>(static_cast<const unsigned char*>(wtc) + kTcLayers[l].wt_off),
         prm + kUpLayers[l].b_off, kUpLayers[l].co, out, input, flow, s_out, max_residual, N, H, W, flag);
@@ -358,7 +408,7 @@ cudaError_t launch_upsampler_tc_pack(const float* prm, void* wtc, cudaStream_t s
 {
     for (int l = 0; l < 4; ++l) {
         const TcLayer& L = kTcLayers[l];
-        const int n = 9 * L.kch * L.no * 8;
+        const int n = static_cast<int>(up_weight_bytes(L.kch, L.no) / 2);
         up_pack_weights_kernel<<<(n + 255) / 256, 256, 0, st>>>(prm + kUpLayers[l].w_off, L.ci, L.co, L.kch, L.no,
             reinterpret_cast<__half*>(static_cast<unsigned char*>(wtc) + L.wt_off));
     }
