@@ -66,6 +66,21 @@ VSC_API vsc_status vsc_selftest_bounded_wait(int32_t spins, vsc_stream_t stream)
  * a property of the build, for profiling tools. */
 VSC_API int32_t vsc_solver_steps_per_launch(void);
 
+/* Tile-shape autotuner of the blend solver (vsc_get_consist_out and the
+ * stabilizer).  Its two persistent kernels, on 64 x 32 and 64 x 48 pixel
+ * tiles, give the same results bit for bit; which is faster at a size
+ * depends on how the tiles fill the GPU's waves.  vsc_solver_autotune times
+ * both at width x height on scratch images and keeps the faster for the
+ * current device (it synchronises the stream and is refused while the stream
+ * is being captured); vsc_stabilizer_create tunes its pyramid's sizes.
+ * vsc_solver_tile_rows returns the tile rows (32 or 48) a solve at that size
+ * uses, with *tuned = 1 when they were measured (else the wave model's
+ * choice).  vsc_solver_set_autotune(0) forgets the measurements and stops
+ * tuning; (1) resumes.  No counterpart in the reference. */
+VSC_API vsc_status vsc_solver_autotune(int32_t width, int32_t height, vsc_stream_t stream, int32_t* tile_rows);
+VSC_API int32_t vsc_solver_tile_rows(int32_t width, int32_t height, int32_t* tuned);
+VSC_API void vsc_solver_set_autotune(int32_t on);
+
 /* ========================================================================
  * ONNX Runtime custom ops (domain "custom")
  * ======================================================================== */

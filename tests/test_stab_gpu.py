@@ -478,6 +478,33 @@ def test_stab_front_rgba_equals_restatement(vsc, oracle, cuda, fc, occ):
         vsc.stab_front_rgba([bad, r8[1], r8[2]], r8[3:6], d(ls), d(ff), d(fb), 20.0, 30.0, 2.0)
 
 
+def test_solver_autotune(vsc, oracle, cuda):
+    """The tile-shape autotuner measures both persistent kernels at a size and
+    keeps one; the solve at that size still equals the restatement bit for
+    bit; switched off, sizes fall back to the wave model."""
+    rows = vsc.solver_autotune(960, 544)
+    assert rows in (32, 48)
+    assert vsc.solver_tile_rows(960, 544) == (rows, True)
+    assert vsc.solver_autotune(960, 544) == rows  # cached
+    h, w = 544, 960
+    P, A, Wt, O0 = _img(h, w), _img(h, w), _img(h, w, hi=2.0), _img(h, w)
+    O = _t(O0, cuda)
+    vsc.get_consist_out(_t(P, cuda), _t(A, cuda), _t(Wt, cuda), 17, 0.15, 0.15, O)
+    assert np.array_equal(O.cpu().numpy(), oracle.consist_out(P, A, Wt, 17, 0.15, 0.15, O0))
+    vsc.solver_set_autotune(False)
+    try:
+        r, tuned = vsc.solver_tile_rows(960, 544)
+        assert r in (32, 48) and not tuned
+        assert vsc.solver_autotune(960, 544) == r  # refused quietly: the model's choice
+        assert vsc.solver_tile_rows(960, 544) == (r, False)
+    finally:
+        vsc.solver_set_autotune(True)
+    # the stabilizer tunes its pyramid's sizes when it is created
+    st = vsc.Stabilizer(200, 120)
+    assert vsc.solver_tile_rows(200, 120)[1] and vsc.solver_tile_rows(100, 60)[1]
+    st.close()
+
+
 def test_flow_estimate_equals_restatement(vsc, oracle, cuda):
     w, h = 112, 80
     fr = _frames(w, h, 2, seed=61)

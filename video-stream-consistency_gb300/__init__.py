@@ -44,7 +44,7 @@ EXPORTED = [
     "vsc_flow_estimate",
     "vsc_upsampler_param_count", "vsc_upsampler_create", "vsc_upsampler_destroy", "vsc_upsampler_get_params",
     "vsc_upsampler_set_max_residual", "vsc_upsampler_prepare", "vsc_upsampler_train_step", "vsc_upsampler_apply",
-    "vsc_stabilizer_set_upsampler",
+    "vsc_stabilizer_set_upsampler", "vsc_solver_autotune", "vsc_solver_tile_rows", "vsc_solver_set_autotune",
 ]
 VSC_DTYPE_F32, VSC_DTYPE_BF16, VSC_DTYPE_F16 = 0, 1, 2
 NOALLOC_MAX_PIXELS = 349525  # VSC_NOALLOC_MAX_PIXELS
@@ -142,6 +142,8 @@ def load():
         "vsc_get_flow_consistency_mask": [IP, IP, IP, vp],
         "vsc_stab_front": [IP] * 11 + [f32, f32, f32, i32, vp],
         "vsc_stab_front_rgba": [vp] * 6 + [IP] * 5 + [f32, f32, f32, i32, vp],
+        "vsc_solver_autotune": [i32, i32, vp, C.POINTER(i32)],
+
         "vsc_flow_estimate": [IP, IP, IP, IP, vp],
         "vsc_upsampler_create": [vp, C.POINTER(vp)],
         "vsc_upsampler_destroy": [vp],
@@ -179,6 +181,10 @@ def load():
     L.vsc_multistream_last_launches.argtypes = [vp]
     L.vsc_solver_steps_per_launch.restype = i32
     L.vsc_solver_steps_per_launch.argtypes = []
+    L.vsc_solver_tile_rows.restype = i32
+    L.vsc_solver_tile_rows.argtypes = [i32, i32, C.POINTER(i32)]
+    L.vsc_solver_set_autotune.restype = None
+    L.vsc_solver_set_autotune.argtypes = [i32]
     L.vsc_correlation_lowp_workspace_size.restype = C.c_size_t
     L.vsc_correlation_lowp_workspace_size.argtypes = [i64, i64, i64, i64]
     L.vsc_consist_out_workspace_size.restype = C.c_size_t
@@ -420,6 +426,24 @@ def get_bilinear(inp, ow: int, oh: int, stream=None):
     out = torch.empty((oh, ow, inp.shape[2]), dtype=torch.float32, device=inp.device)
     _check(load().vsc_get_bilinear(C.byref(image(inp)), C.byref(image(out)), _stream(stream)))
     return out
+
+
+def solver_autotune(w: int, h: int, stream=None) -> int:
+    """Time both solver tile shapes at w x h and keep the faster; returns its rows (32 or 48)."""
+    rows = C.c_int32()
+    _check(load().vsc_solver_autotune(int(w), int(h), _stream(stream), C.byref(rows)))
+    return rows.value
+
+
+def solver_tile_rows(w: int, h: int):
+    """(rows, tuned): the tile rows a solve at w x h uses, and whether they were measured."""
+    tuned = C.c_int32()
+    rows = load().vsc_solver_tile_rows(int(w), int(h), C.byref(tuned))
+    return rows, bool(tuned.value)
+
+
+def solver_set_autotune(on: bool) -> None:
+    load().vsc_solver_set_autotune(1 if on else 0)
 
 
 def consist_out_workspace_size(w: int, h: int) -> int:

@@ -529,6 +529,35 @@ VSC_API vsc_status vsc_get_consist_out(const vsc_image* crnt_pr, const vsc_image
 
 VSC_API int32_t vsc_solver_steps_per_launch(void) { return solver_steps_per_launch(); }
 
+VSC_API vsc_status vsc_solver_autotune(int32_t width, int32_t height, vsc_stream_t stream, int32_t* tile_rows)
+{
+    clear_error();
+    if (width < 1 || height < 1)
+        return set_error(VSC_EINVAL, "solver_autotune: size %dx%d", width, height);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    vsc_status s = check_cuda(cudaStreamIsCapturing(cs(stream), &cap), "solver_autotune");
+    if (s)
+        return s;
+    if (cap != cudaStreamCaptureStatusNone)
+        return set_error(VSC_ESTATE, "solver_autotune: the stream is being captured");
+    int rows = 0;
+    s = check_cuda(solver_autotune(width, height, cs(stream), &rows), "solver_autotune");
+    if (!s && tile_rows)
+        *tile_rows = rows;
+    return s;
+}
+
+VSC_API int32_t vsc_solver_tile_rows(int32_t width, int32_t height, int32_t* tuned)
+{
+    bool t = false;
+    const int rows = width > 0 && height > 0 ? solver_tile_rows(width, height, &t) : 0;
+    if (tuned)
+        *tuned = t ? 1 : 0;
+    return rows;
+}
+
+VSC_API void vsc_solver_set_autotune(int32_t on) { solver_set_autotune(on != 0); }
+
 VSC_API vsc_status vsc_check_device(void)
 {
     clear_error();
@@ -856,6 +885,14 @@ VSC_API vsc_status vsc_stabilizer_create(const vsc_stabilizer_config* cfg, vsc_s
         delete s;
         return st;
     }
+    // the solver's tile shape for the pyramid's sizes (a stream being captured keeps the model)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s->st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone)
+        for (int j = 0; j < std::min(s->levels_alloc, 4); ++j)
+            if (solver_autotune(s->lw[j], s->lh[j], s->st, nullptr) != cudaSuccess) {
+                cudaGetLastError();  // a failed measurement leaves the model's choice
+                break;
+            }
     *out = s;
     return VSC_OK;
 }

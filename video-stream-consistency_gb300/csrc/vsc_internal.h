@@ -114,6 +114,14 @@ cudaError_t launch_resize_nearest(const float* in, int iw, int ih, float* out, i
 // momentum images and the second Jacobi buffer: 4 * w*h*3 floats.
 size_t solver_workspace_floats(int w, int h);
 int solver_steps_per_launch();  // Jacobi steps one solver launch performs (temporal blocking)
+// Tile-shape autotuner of the persistent solver kernels (same results either
+// way): solver_autotune times both shapes at (w, h) on scratch images and
+// keeps the faster for the current device (synchronises `st`; not during
+// stream capture); solver_tile_rows reports the rows of the tile a solve at
+// (w, h) uses (tuned, or the wave model's choice).
+cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out);
+int solver_tile_rows(int w, int h, bool* tuned);
+void solver_set_autotune(bool on);
 // Runs num_iter iterations; O holds the initial solution and receives the
 // result.  Returns the number of kernels launched through *launches.
 cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,

@@ -16,7 +16,9 @@
 #include <cuda.h>  // CUtensorMap (the encoder is fetched from the driver at run time)
 
 #include <algorithm>
+#include <map>
 #include <mutex>
+#include <tuple>
 
 namespace vsc {
 namespace {
@@ -754,7 +756,157 @@ cudaError_t device_info(DeviceInfo** out)
 
 bool aligned16p(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
+// ---- tile-shape autotuner ------------------------------------------------------------
+// The two persistent kernels (64 x 32 and 64 x 48 tiles) give the same results
+// bit for bit; which is faster at a size depends on how their tiles fill the
+// waves of one tile per SM.  solver_autotune times both on scratch images of
+// the size and keeps the faster per (device, width, height); sizes never
+// tuned use the wave model: a 64 x 48 tile costs about 1.91 times a 64 x 32
+// one (GB300, 1920x1080 and 960x540).
+struct ShapeTable {
+    std::mutex mu;
+    std::map<std::tuple<int, int, int>, int> rows;  // (device, w, h) -> kPEY or kTbEY
+    bool enabled = true;
+};
+ShapeTable& shape_table()
+{
+    static ShapeTable t;
+    return t;
+}
+
+int model_rows(int w, int h, int sms)
+{
+    const int tiles_x = (w + kIW - 1) / kIW;
+    const int n_short = tiles_x * ((h + kIH - 1) / kIH), n_tall = tiles_x * ((h + kPIH - 1) / kPIH);
+    return 1.91 * ((n_tall + sms - 1) / sms) < 1.0 * ((n_short + sms - 1) / sms) ? kPEY : kTbEY;
+}
+
+// the tile rows a solve at (w, h) on the current device uses: tuned, else the model
+int chosen_rows(int dev, int w, int h, int sms)
+{
+    ShapeTable& t = shape_table();
+    std::lock_guard<std::mutex> lock(t.mu);
+    auto it = t.rows.find(std::make_tuple(dev, w, h));
+    return it != t.rows.end() ? it->second : model_rows(w, h, sms);
+}
+
+// One 8-step launch of the persistent kernel with `rows`-row tiles.
+void launch_persistent(int rows, const CUtensorMap& mO, const CUtensorMap& mU, const CUtensorMap& mA,
+    const CUtensorMap& mW, const CUtensorMap& mL, float* Oout, float* Uout, int w, int h, int T, int k0, float step,
+    float mom, uint8_t* rgba, int sms, cudaStream_t st)
+{
+    const int tiles_x = (w + kIW - 1) / kIW;
+    if (rows == kPEY) {
+        const int ntiles = tiles_x * ((h + kPIH - 1) / kPIH);
+        solver_tall_kernel<<<std::min(ntiles, sms), kPThreads, kPSmem, st>>>(mO, mU, mA, mW, mL, Oout, Uout, w, h,
+            T, k0, step, mom, rgba, tiles_x, ntiles);
+    } else {
+        const int ntiles = tiles_x * ((h + kIH - 1) / kIH);
+        solver_persistent_kernel<<<std::min(ntiles, sms), dim3(32, kTbEY / 2), kPsSmem, st>>>(mO, mU, mA, mW, mL,
+            Oout, Uout, w, h, T, k0, step, mom, rgba, tiles_x, ntiles);
+    }
+}
+
 }  // namespace
+
+void solver_set_autotune(bool on)
+{
+    ShapeTable& t = shape_table();
+    std::lock_guard<std::mutex> lock(t.mu);
+    t.enabled = on;
+    if (!on)
+        t.rows.clear();
+}
+
+int solver_tile_rows(int w, int h, bool* tuned)
+{
+    int dev = 0;
+    DeviceInfo* di = nullptr;
+    if (cudaGetDevice(&dev) != cudaSuccess || device_info(&di) != cudaSuccess)
+        return 0;
+    ShapeTable& t = shape_table();
+    std::lock_guard<std::mutex> lock(t.mu);
+    auto it = t.rows.find(std::make_tuple(dev, w, h));
+    if (tuned)
+        *tuned = it != t.rows.end();
+    return it != t.rows.end() ? it->second : model_rows(w, h, di->sms);
+}
+
+cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out)
+{
+    DeviceInfo* di = nullptr;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+        e = device_info(&di);
+    if (e != cudaSuccess)
+        return e;
+    ShapeTable& t = shape_table();
+    {
+        std::lock_guard<std::mutex> lock(t.mu);
+        auto it = t.rows.find(std::make_tuple(dev, w, h));
+        if (it != t.rows.end() || !t.enabled || !di->ps_smem || (w % 4) != 0 || w < 1 || h < 1) {
+            if (rows_out)
+                *rows_out = it != t.rows.end() ? it->second : model_rows(w, h, di->sms);
+            return cudaSuccess;
+        }
+    }
+    // scratch images (zeros; the kernels have no data-dependent control flow):
+    // O, O2, U0, U1, A, Wt, lap P
+    const size_t n = static_cast<size_t>(w) * h * 3;
+    float* buf = nullptr;
+    if ((e = cudaMalloc(&buf, 7 * n * sizeof(float))) != cudaSuccess)
+        return e;
+    float* im[7];
+    for (int i = 0; i < 7; ++i)
+        im[i] = buf + i * n;
+    cudaEvent_t ev[3] = {};
+    float ms[2] = {0.0f, 0.0f};
+    const int shapes[2] = {kTbEY, kPEY};
+    e = cudaMemsetAsync(buf, 0, 7 * n * sizeof(float), st);
+    for (int i = 0; i < 3 && e == cudaSuccess; ++i)
+        e = cudaEventCreate(&ev[i]);
+    for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
+        const int rows = shapes[s];
+        CUtensorMap mO[2], mU, mA, mW, mL;
+        if (!(encode_image_map(&mO[0], im[0], w, h, rows) && encode_image_map(&mO[1], im[1], w, h, rows) &&
+                encode_image_map(&mU, im[2], w, h, rows) && encode_image_map(&mA, im[4], w, h, rows) &&
+                encode_image_map(&mW, im[5], w, h, rows) && encode_image_map(&mL, im[6], w, h, rows))) {
+            e = cudaErrorInvalidValue;
+            break;
+        }
+        // one launch to warm up, then three timed (O ping-pongs, momentum on)
+        for (int r = 0; r < 4 && e == cudaSuccess; ++r) {
+            if (r == 1)
+                e = cudaEventRecord(ev[0], st);
+            launch_persistent(rows, mO[r & 1], mU, mA, mW, mL, im[(r + 1) & 1], im[3], w, h, kTbT, kTbT, 0.15f,
+                0.15f, nullptr, di->sms, st);
+            if (e == cudaSuccess)
+                e = cudaGetLastError();
+        }
+        if (e == cudaSuccess)
+            e = cudaEventRecord(ev[1], st);
+        if (e == cudaSuccess)
+            e = cudaEventSynchronize(ev[1]);
+        if (e == cudaSuccess)
+            e = cudaEventElapsedTime(&ms[s], ev[0], ev[1]);
+    }
+    for (cudaEvent_t x : ev)
+        if (x)
+            cudaEventDestroy(x);
+    cudaFree(buf);
+    if (e != cudaSuccess)
+        return e;
+    const int best = ms[1] < ms[0] ? kPEY : kTbEY;
+    {
+        std::lock_guard<std::mutex> lock(t.mu);
+        if (t.enabled)
+            t.rows[std::make_tuple(dev, w, h)] = best;
+    }
+    if (rows_out)
+        *rows_out = best;
+    return cudaSuccess;
+}
 
 size_t solver_workspace_floats(int w, int h) { return static_cast<size_t>(w) * h * 3 * 4; }
 
@@ -796,15 +948,11 @@ cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O
     // TMA path: 16-byte row pitch and aligned images
     bool tma = di->ps_smem && (w % 4) == 0 && aligned16p(O) && aligned16p(O2) && aligned16p(U[0]) &&
                aligned16p(U[1]) && aligned16p(A) && aligned16p(Wt) && aligned16p(L);
-    // Tile shape: the persistent kernels walk their tiles in waves of one
-    // tile per SM, so a launch costs about ceil(tiles / SMs) tile times; a
-    // 64 x 48 tile costs 1.91 times a 64 x 32 one (measured on GB300,
-    // 1920x1080 and 960x540), and the shape with the cheaper waves is used.
-    const int tiles_x = (w + kIW - 1) / kIW;
-    const int n_short = tiles_x * ((h + kIH - 1) / kIH), n_tall = tiles_x * ((h + kPIH - 1) / kPIH);
-    const bool tall = 1.91 * ((n_tall + di->sms - 1) / di->sms) < 1.0 * ((n_short + di->sms - 1) / di->sms);
-    const int rows = tall ? kPEY : kTbEY;
-    const int ntiles = tall ? n_tall : n_short;
+    // tile shape: the autotuned one for this size, else the wave model
+    int dev = 0;
+    if ((e0 = cudaGetDevice(&dev)) != cudaSuccess)
+        return e0;
+    const int rows = chosen_rows(dev, w, h, di->sms);
     CUtensorMap mO[2], mU[2], mA, mW, mL;
     if (tma)
         tma = encode_image_map(&mO[0], O, w, h, rows) && encode_image_map(&mO[1], O2, w, h, rows) &&
@@ -816,13 +964,9 @@ cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O
         const int T = std::min(kTbT, num_iter - k0);
         float* nxt = (cur == O) ? O2 : O;
         uint8_t* rg = (li == nlaunch - 1) ? rgba_out : nullptr;
-        if (tma && tall) {
-            solver_tall_kernel<<<std::min(ntiles, di->sms), kPThreads, kPSmem, st>>>(mO[cur == O ? 0 : 1],
-                mU[li & 1], mA, mW, mL, nxt, U[(li + 1) & 1], w, h, T, k0, step, mom, rg, tiles_x, ntiles);
-        } else if (tma) {
-            solver_persistent_kernel<<<std::min(ntiles, di->sms), dim3(32, kTbEY / 2), kPsSmem, st>>>(
-                mO[cur == O ? 0 : 1], mU[li & 1], mA, mW, mL, nxt, U[(li + 1) & 1], w, h, T, k0, step, mom, rg,
-                tiles_x, ntiles);
+        if (tma) {
+            launch_persistent(rows, mO[cur == O ? 0 : 1], mU[li & 1], mA, mW, mL, nxt, U[(li + 1) & 1], w, h, T, k0,
+                step, mom, rg, di->sms, st);
         } else {
             const dim3 grid((w + (kTbEX - 2 * T) - 1) / (kTbEX - 2 * T), (h + (kTbEY - 2 * T) - 1) / (kTbEY - 2 * T));
             solver_tb_kernel<<<grid, dim3(32, kTbEY / 2), kTbSmem, st>>>(cur, nxt, U[li & 1], U[(li + 1) & 1], L, A,
