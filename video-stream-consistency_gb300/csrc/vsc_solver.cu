@@ -336,6 +336,33 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
         : "memory");
 }
 
+// TMA tensor store (shared -> global) of one box; elements outside the image are clipped
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, const void* src)
+{
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+        "r"(x), "r"(y), "r"(smem_u32(src))
+        : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// this thread's bulk stores have read their shared-memory source
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// this thread's bulk stores are complete
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+// The interior of a tile (after the T-pixel ring) leaves through shared memory
+// and two TMA stores, one per image, instead of scalar stores of 12-byte
+// pixels: `so` / `su` hold rows of 3 * kIW floats, filled by every thread,
+// then one thread issues the stores; the staging is reusable after
+// bulk_wait_read and a barrier.
+__device__ __forceinline__ void store_interior(const CUtensorMap* mOo, const CUtensorMap* mUo, int ox, int oy,
+    const float* so, const float* su)
+{
+    tma_store_2d(mOo, 3 * (ox + kTbT), oy + kTbT, so);
+    tma_store_2d(mUo, 3 * (ox + kTbT), oy + kTbT, su);
+    bulk_commit();
+}
+
 __device__ __forceinline__ void issue_tile(float* stage, const CUtensorMap* m0, const CUtensorMap* m1,
     const CUtensorMap* m2, const CUtensorMap* m3, const CUtensorMap* m4, int tile, int tiles_x, uint64_t* bar)
 {
@@ -352,8 +379,9 @@ __device__ __forceinline__ void issue_tile(float* stage, const CUtensorMap* m0, 
 __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
     solver_persistent_kernel(const __grid_constant__ CUtensorMap mO, const __grid_constant__ CUtensorMap mU,
         const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mW,
-        const __grid_constant__ CUtensorMap mL, float* __restrict__ Oout, float* __restrict__ Uout, int w, int h,
-        int T, int k0, float step, float mom, uint8_t* __restrict__ rgba, int tiles_x, int ntiles)
+        const __grid_constant__ CUtensorMap mL, const __grid_constant__ CUtensorMap mOo,
+        const __grid_constant__ CUtensorMap mUo, int w, int h, int T, int k0, float step, float mom,
+        uint8_t* __restrict__ rgba, int tiles_x, int ntiles)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* stage = reinterpret_cast<float*>(smem_raw);
@@ -376,8 +404,10 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
         const int ox = (tile % tiles_x) * kIW - kTbT;
         const int oy = (tile / tiles_x) * kIH - kTbT;
         if (!mbar_wait_bounded(bar, parity, kWaitSpins)) {
-            if (tid == 0)
+            if (tid == 0) {
                 atomicExch(&g_device_timeout, 1);
+                bulk_wait_all();
+            }
             mbar_wait_bounded(bar, parity, kWaitSpins);  // let copies still in flight land
             return;
         }
@@ -435,24 +465,40 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
         else
             tb_iterate<false>(s, vr, vl, vd, vu, cnt, obuf, T, kTbT, k0, step, mom, px0, py0);
 
+        // interior out: the edge-row buffers are idle until the next tile's publish
+        float* so = obuf;
+        float* su = obuf + kIH * 3 * kIW;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            const int r = q >> 1, c = q & 1;
-            const int px = px0 + c, py = py0 + r;
-            if (!inimg[q] || px < kTbT || px >= kTbEX - kTbT || py < kTbT || py >= kTbEY - kTbT)
+            const int ix = px0 + (q & 1) - kTbT, iy = py0 + (q >> 1) - kTbT;
+            if (ix < 0 || ix >= kIW || iy < 0 || iy >= kIH)
                 continue;
-            const int64_t p = pix_index(ox + px, oy + py, w);
-            float ov[3];
 #pragma unroll
             for (int ch = 0; ch < 3; ++ch) {
-                ov[ch] = s.o[q][ch];
-                Oout[p * 3 + ch] = ov[ch];
-                Uout[p * 3 + ch] = s.u[q][ch];
+                so[iy * 3 * kIW + 3 * ix + ch] = s.o[q][ch];
+                su[iy * 3 * kIW + 3 * ix + ch] = s.u[q][ch];
             }
-            if (rgba)
-                reinterpret_cast<uint32_t*>(rgba)[p] = pack_rgba(ov[0], ov[1], ov[2]);
         }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0)
+            store_interior(&mOo, &mUo, ox, oy, so, su);
+        if (rgba) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int px = px0 + (q & 1), py = py0 + (q >> 1);
+                if (!inimg[q] || px < kTbT || px >= kTbEX - kTbT || py < kTbT || py >= kTbEY - kTbT)
+                    continue;
+                reinterpret_cast<uint32_t*>(rgba)[pix_index(ox + px, oy + py, w)] =
+                    pack_rgba(s.o[q][0], s.o[q][1], s.o[q][2]);
+            }
+        }
+        if (tid == 0)
+            bulk_wait_read();
+        __syncthreads();  // the staging may be overwritten
     }
+    if (tid == 0)
+        bulk_wait_all();
 }
 
 // ---- persistent, TMA-fed solver on 64 x 48 tiles of 2 x 4 pixel blocks -------------
@@ -476,6 +522,10 @@ constexpr int kPPlane = kPSlots * 2 * kTbPX;  // one channel of one buffer
 constexpr int kPObuf = 2 * 3 * kPPlane;
 constexpr int kPSmem = 5 * kPStageBytes + kPObuf * static_cast<int>(sizeof(float)) + 16;
 static_assert(kPSmem <= 232448, "dynamic shared memory per CTA");
+static_assert(kPObuf >= 2 * kPIH * 3 * kIW && 2 * 3 * kTbPlane >= 2 * kIH * 3 * kIW,
+    "the edge-row buffers hold a tile's interior O and U");
+static_assert((kPIH * 3 * kIW * 4) % 128 == 0 && (kIH * 3 * kIW * 4) % 128 == 0 &&
+    (5 * kPStageBytes) % 128 == 0 && (5 * kStageBytes) % 128 == 0, "TMA store sources on the 128-byte grid");
 static_assert(2 * kTbT < kPEY, "tile too small for the iteration count");
 
 struct P8State {
@@ -580,8 +630,9 @@ __device__ __forceinline__ void issue_tall_tile(float* stage, const CUtensorMap*
 __global__ void __launch_bounds__(kPThreads, 1)
     solver_tall_kernel(const __grid_constant__ CUtensorMap mO, const __grid_constant__ CUtensorMap mU,
         const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mW,
-        const __grid_constant__ CUtensorMap mL, float* __restrict__ Oout, float* __restrict__ Uout, int w, int h,
-        int T, int k0, float step, float mom, uint8_t* __restrict__ rgba, int tiles_x, int ntiles)
+        const __grid_constant__ CUtensorMap mL, const __grid_constant__ CUtensorMap mOo,
+        const __grid_constant__ CUtensorMap mUo, int w, int h, int T, int k0, float step, float mom,
+        uint8_t* __restrict__ rgba, int tiles_x, int ntiles)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* stage = reinterpret_cast<float*>(smem_raw);
@@ -603,8 +654,10 @@ __global__ void __launch_bounds__(kPThreads, 1)
         const int ox = (tile % tiles_x) * kIW - kTbT;
         const int oy = (tile / tiles_x) * kPIH - kTbT;
         if (!mbar_wait_bounded(bar, parity, kWaitSpins)) {
-            if (threadIdx.x == 0)
+            if (threadIdx.x == 0) {
                 atomicExch(&g_device_timeout, 1);
+                bulk_wait_all();
+            }
             mbar_wait_bounded(bar, parity, kWaitSpins);  // let copies still in flight land
             return;
         }
@@ -650,26 +703,41 @@ __global__ void __launch_bounds__(kPThreads, 1)
         else
             p8_iterate<false>(s, obuf, T, k0, step, mom, px0, warp, gx0, gy0, w, h);
 
+        // interior out: the edge-row slots are idle until the next tile's publish
+        float* so = obuf;
+        float* su = obuf + kPIH * 3 * kIW;
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            const int r = q >> 1, c = q & 1;
-            const int px = px0 + c, py = py0 + r;
-            const int gx = ox + px, gy = oy + py;
-            if (gx < 0 || gx >= w || gy < 0 || gy >= h || px < kTbT || px >= kTbEX - kTbT || py < kTbT ||
-                py >= kPEY - kTbT)
+            const int ix = px0 + (q & 1) - kTbT, iy = py0 + (q >> 1) - kTbT;
+            if (ix < 0 || ix >= kIW || iy < 0 || iy >= kPIH)
                 continue;
-            const int64_t p = pix_index(gx, gy, w);
-            float ov[3];
 #pragma unroll
             for (int ch = 0; ch < 3; ++ch) {
-                ov[ch] = s.o[q][ch];
-                Oout[p * 3 + ch] = ov[ch];
-                Uout[p * 3 + ch] = s.u[q][ch];
+                so[iy * 3 * kIW + 3 * ix + ch] = s.o[q][ch];
+                su[iy * 3 * kIW + 3 * ix + ch] = s.u[q][ch];
             }
-            if (rgba)
-                reinterpret_cast<uint32_t*>(rgba)[p] = pack_rgba(ov[0], ov[1], ov[2]);
         }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0)
+            store_interior(&mOo, &mUo, ox, oy, so, su);
+        if (rgba) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int px = px0 + (q & 1), py = py0 + (q >> 1);
+                const int gx = ox + px, gy = oy + py;
+                if (gx < 0 || gx >= w || gy < 0 || gy >= h || px < kTbT || px >= kTbEX - kTbT || py < kTbT ||
+                    py >= kPEY - kTbT)
+                    continue;
+                reinterpret_cast<uint32_t*>(rgba)[pix_index(gx, gy, w)] = pack_rgba(s.o[q][0], s.o[q][1], s.o[q][2]);
+            }
+        }
+        if (threadIdx.x == 0)
+            bulk_wait_read();
+        __syncthreads();  // the staging may be overwritten
     }
+    if (threadIdx.x == 0)
+        bulk_wait_all();
 }
 
 // An mbarrier nobody arrives on, waited for with a bounded spin: exercises
@@ -704,14 +772,14 @@ EncodeTiledFn encode_fn()
 }
 
 // 2D map over an interleaved w x h x 3 float image: x = float index in a row.
-bool encode_image_map(CUtensorMap* m, const float* base, int w, int h, int box_rows)
+bool encode_image_map(CUtensorMap* m, const float* base, int w, int h, int box_rows, int box_cols = 3 * kTbEX)
 {
     EncodeTiledFn fn = encode_fn();
     if (!fn)
         return false;
     const cuuint64_t dims[2] = {static_cast<cuuint64_t>(w) * 3, static_cast<cuuint64_t>(h)};
     const cuuint64_t strides[1] = {static_cast<cuuint64_t>(w) * 3 * sizeof(float)};
-    const cuuint32_t box[2] = {3 * kTbEX, static_cast<cuuint32_t>(box_rows)};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(box_cols), static_cast<cuuint32_t>(box_rows)};
     const cuuint32_t estr[2] = {1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -790,20 +858,23 @@ int chosen_rows(int dev, int w, int h, int sms)
     return it != t.rows.end() ? it->second : model_rows(w, h, sms);
 }
 
-// One 8-step launch of the persistent kernel with `rows`-row tiles.
+// One launch of the persistent kernel with `rows`-row tiles; mOo / mUo are the
+// output images' maps with the interior box (interior_rows(rows) rows).
+int interior_rows(int rows) { return rows == kPEY ? kPIH : kIH; }
+
 void launch_persistent(int rows, const CUtensorMap& mO, const CUtensorMap& mU, const CUtensorMap& mA,
-    const CUtensorMap& mW, const CUtensorMap& mL, float* Oout, float* Uout, int w, int h, int T, int k0, float step,
-    float mom, uint8_t* rgba, int sms, cudaStream_t st)
+    const CUtensorMap& mW, const CUtensorMap& mL, const CUtensorMap& mOo, const CUtensorMap& mUo, int w, int h,
+    int T, int k0, float step, float mom, uint8_t* rgba, int sms, cudaStream_t st)
 {
     const int tiles_x = (w + kIW - 1) / kIW;
     if (rows == kPEY) {
         const int ntiles = tiles_x * ((h + kPIH - 1) / kPIH);
-        solver_tall_kernel<<<std::min(ntiles, sms), kPThreads, kPSmem, st>>>(mO, mU, mA, mW, mL, Oout, Uout, w, h,
+        solver_tall_kernel<<<std::min(ntiles, sms), kPThreads, kPSmem, st>>>(mO, mU, mA, mW, mL, mOo, mUo, w, h,
             T, k0, step, mom, rgba, tiles_x, ntiles);
     } else {
         const int ntiles = tiles_x * ((h + kIH - 1) / kIH);
         solver_persistent_kernel<<<std::min(ntiles, sms), dim3(32, kTbEY / 2), kPsSmem, st>>>(mO, mU, mA, mW, mL,
-            Oout, Uout, w, h, T, k0, step, mom, rgba, tiles_x, ntiles);
+            mOo, mUo, w, h, T, k0, step, mom, rgba, tiles_x, ntiles);
     }
 }
 
@@ -868,10 +939,14 @@ cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out)
         e = cudaEventCreate(&ev[i]);
     for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
         const int rows = shapes[s];
-        CUtensorMap mO[2], mU, mA, mW, mL;
+        CUtensorMap mO[2], mU, mA, mW, mL, mOo[2], mUo;
+        const int ir = interior_rows(rows);
         if (!(encode_image_map(&mO[0], im[0], w, h, rows) && encode_image_map(&mO[1], im[1], w, h, rows) &&
                 encode_image_map(&mU, im[2], w, h, rows) && encode_image_map(&mA, im[4], w, h, rows) &&
-                encode_image_map(&mW, im[5], w, h, rows) && encode_image_map(&mL, im[6], w, h, rows))) {
+                encode_image_map(&mW, im[5], w, h, rows) && encode_image_map(&mL, im[6], w, h, rows) &&
+                encode_image_map(&mOo[0], im[0], w, h, ir, 3 * kIW) &&
+                encode_image_map(&mOo[1], im[1], w, h, ir, 3 * kIW) &&
+                encode_image_map(&mUo, im[3], w, h, ir, 3 * kIW))) {
             e = cudaErrorInvalidValue;
             break;
         }
@@ -879,7 +954,7 @@ cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out)
         for (int r = 0; r < 4 && e == cudaSuccess; ++r) {
             if (r == 1)
                 e = cudaEventRecord(ev[0], st);
-            launch_persistent(rows, mO[r & 1], mU, mA, mW, mL, im[(r + 1) & 1], im[3], w, h, kTbT, kTbT, 0.15f,
+            launch_persistent(rows, mO[r & 1], mU, mA, mW, mL, mOo[(r + 1) & 1], mUo, w, h, kTbT, kTbT, 0.15f,
                 0.15f, nullptr, di->sms, st);
             if (e == cudaSuccess)
                 e = cudaGetLastError();
@@ -953,20 +1028,23 @@ cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O
     if ((e0 = cudaGetDevice(&dev)) != cudaSuccess)
         return e0;
     const int rows = chosen_rows(dev, w, h, di->sms);
-    CUtensorMap mO[2], mU[2], mA, mW, mL;
+    CUtensorMap mO[2], mU[2], mA, mW, mL, mOo[2], mUo[2];
+    const int ir = interior_rows(rows);
     if (tma)
         tma = encode_image_map(&mO[0], O, w, h, rows) && encode_image_map(&mO[1], O2, w, h, rows) &&
               encode_image_map(&mU[0], U[0], w, h, rows) && encode_image_map(&mU[1], U[1], w, h, rows) &&
               encode_image_map(&mA, A, w, h, rows) && encode_image_map(&mW, Wt, w, h, rows) &&
-              encode_image_map(&mL, L, w, h, rows);
+              encode_image_map(&mL, L, w, h, rows) && encode_image_map(&mOo[0], O, w, h, ir, 3 * kIW) &&
+              encode_image_map(&mOo[1], O2, w, h, ir, 3 * kIW) && encode_image_map(&mUo[0], U[0], w, h, ir, 3 * kIW) &&
+              encode_image_map(&mUo[1], U[1], w, h, ir, 3 * kIW);
     int k0 = 0;
     for (int li = 0; li < nlaunch; ++li) {
         const int T = std::min(kTbT, num_iter - k0);
         float* nxt = (cur == O) ? O2 : O;
         uint8_t* rg = (li == nlaunch - 1) ? rgba_out : nullptr;
         if (tma) {
-            launch_persistent(rows, mO[cur == O ? 0 : 1], mU[li & 1], mA, mW, mL, nxt, U[(li + 1) & 1], w, h, T, k0,
-                step, mom, rg, di->sms, st);
+            launch_persistent(rows, mO[cur == O ? 0 : 1], mU[li & 1], mA, mW, mL, mOo[nxt == O ? 0 : 1],
+                mUo[(li + 1) & 1], w, h, T, k0, step, mom, rg, di->sms, st);
         } else {
             const dim3 grid((w + (kTbEX - 2 * T) - 1) / (kTbEX - 2 * T), (h + (kTbEY - 2 * T) - 1) / (kTbEY - 2 * T));
             solver_tb_kernel<<<grid, dim3(32, kTbEY / 2), kTbSmem, st>>>(cur, nxt, U[li & 1], U[(li + 1) & 1], L, A,
