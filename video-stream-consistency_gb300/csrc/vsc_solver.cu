@@ -448,11 +448,16 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
                 p1[1] = v45.x;
                 p1[2] = v45.y;
             }
+        }
+        if (tid == 0)
+            bulk_wait_read();  // the previous tile's TMA stores have read the staging
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
 #pragma unroll
             for (int ch = 0; ch < 3; ++ch)
-                *reinterpret_cast<float2*>(&obuf[ch * kTbPlane + (row + 1) * kTbPX + px0 + 2]) =
+                *reinterpret_cast<float2*>(&obuf[ch * kTbPlane + (py0 + r + 1) * kTbPX + px0 + 2]) =
                     make_float2(s.o[2 * r][ch], s.o[2 * r + 1][ch]);
-        }
         __syncthreads();  // staging consumed, O published
         if (tid == 0 && tile + static_cast<int>(gridDim.x) < ntiles) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -465,18 +470,29 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
         else
             tb_iterate<false>(s, vr, vl, vd, vu, cnt, obuf, T, kTbT, k0, step, mom, px0, py0);
 
-        // interior out: the edge-row buffers are idle until the next tile's publish
+        // interior out: the edge-row buffers are idle until the next tile's publish;
+        // a thread's two pixels of a row are six consecutive floats
         float* so = obuf;
         float* su = obuf + kIH * 3 * kIW;
+        {
+            const int ix = px0 - kTbT;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int ix = px0 + (q & 1) - kTbT, iy = py0 + (q >> 1) - kTbT;
-            if (ix < 0 || ix >= kIW || iy < 0 || iy >= kIH)
-                continue;
-#pragma unroll
-            for (int ch = 0; ch < 3; ++ch) {
-                so[iy * 3 * kIW + 3 * ix + ch] = s.o[q][ch];
-                su[iy * 3 * kIW + 3 * ix + ch] = s.u[q][ch];
+            for (int r = 0; r < 2; ++r) {
+                const int iy = py0 + r - kTbT;
+                if (ix < 0 || ix >= kIW || iy < 0 || iy >= kIH)
+                    continue;
+                float2* o2 = reinterpret_cast<float2*>(so + iy * 3 * kIW + 3 * ix);
+                float2* u2 = reinterpret_cast<float2*>(su + iy * 3 * kIW + 3 * ix);
+                const float* a = s.o[2 * r];
+                const float* b = s.o[2 * r + 1];
+                o2[0] = make_float2(a[0], a[1]);
+                o2[1] = make_float2(a[2], b[0]);
+                o2[2] = make_float2(b[1], b[2]);
+                const float* c = s.u[2 * r];
+                const float* d = s.u[2 * r + 1];
+                u2[0] = make_float2(c[0], c[1]);
+                u2[1] = make_float2(c[2], d[0]);
+                u2[2] = make_float2(d[1], d[2]);
             }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -493,9 +509,7 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
                     pack_rgba(s.o[q][0], s.o[q][1], s.o[q][2]);
             }
         }
-        if (tid == 0)
-            bulk_wait_read();
-        __syncthreads();  // the staging may be overwritten
+        // the TMA stores read the staging while the next tile's copies land
     }
     if (tid == 0)
         bulk_wait_all();
@@ -684,6 +698,9 @@ __global__ void __launch_bounds__(kPThreads, 1)
                 p1[2] = v45.y;
             }
         }
+        if (threadIdx.x == 0)
+            bulk_wait_read();  // the previous tile's TMA stores have read the staging
+        __syncthreads();
 #pragma unroll
         for (int ch = 0; ch < 3; ++ch) {
             float* D = obuf + ch * kPPlane + ((warp + 1) * 2) * kTbPX + px0 + 2;  // buffer 0
@@ -703,18 +720,30 @@ __global__ void __launch_bounds__(kPThreads, 1)
         else
             p8_iterate<false>(s, obuf, T, k0, step, mom, px0, warp, gx0, gy0, w, h);
 
-        // interior out: the edge-row slots are idle until the next tile's publish
+        // interior out: the edge-row slots are idle until the next tile's publish;
+        // a thread's two pixels of a row are six consecutive floats (the
+        // interior starts at an even column, so both or neither are inside)
         float* so = obuf;
         float* su = obuf + kPIH * 3 * kIW;
+        {
+            const int ix = px0 - kTbT;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int ix = px0 + (q & 1) - kTbT, iy = py0 + (q >> 1) - kTbT;
-            if (ix < 0 || ix >= kIW || iy < 0 || iy >= kPIH)
-                continue;
-#pragma unroll
-            for (int ch = 0; ch < 3; ++ch) {
-                so[iy * 3 * kIW + 3 * ix + ch] = s.o[q][ch];
-                su[iy * 3 * kIW + 3 * ix + ch] = s.u[q][ch];
+            for (int r = 0; r < 4; ++r) {
+                const int iy = py0 + r - kTbT;
+                if (ix < 0 || ix >= kIW || iy < 0 || iy >= kPIH)
+                    continue;
+                float2* o2 = reinterpret_cast<float2*>(so + iy * 3 * kIW + 3 * ix);
+                float2* u2 = reinterpret_cast<float2*>(su + iy * 3 * kIW + 3 * ix);
+                const float* a = s.o[2 * r];
+                const float* b = s.o[2 * r + 1];
+                o2[0] = make_float2(a[0], a[1]);
+                o2[1] = make_float2(a[2], b[0]);
+                o2[2] = make_float2(b[1], b[2]);
+                const float* c = s.u[2 * r];
+                const float* d = s.u[2 * r + 1];
+                u2[0] = make_float2(c[0], c[1]);
+                u2[1] = make_float2(c[2], d[0]);
+                u2[2] = make_float2(d[1], d[2]);
             }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -732,9 +761,8 @@ __global__ void __launch_bounds__(kPThreads, 1)
                 reinterpret_cast<uint32_t*>(rgba)[pix_index(gx, gy, w)] = pack_rgba(s.o[q][0], s.o[q][1], s.o[q][2]);
             }
         }
-        if (threadIdx.x == 0)
-            bulk_wait_read();
-        __syncthreads();  // the staging may be overwritten
+        // the TMA stores read the staging while the next tile's copies land; the
+        // next tile waits for those reads before it publishes its edge rows
     }
     if (threadIdx.x == 0)
         bulk_wait_all();
