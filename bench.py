@@ -860,8 +860,8 @@ def run_gpu(args):
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one solver launch at
 # 1920x1080, by Jacobi steps per launch, from the ncu captures summarised in
-# profiles/ (solver_tall_kernel, 8 steps: 124,536,832 + 20,745,728 bytes).
-SOLVER_TRAFFIC_BYTES = {8: 145_282_560}
+# profiles/ (solver_tall_kernel, 8 steps: 124,875,264 + 23,028,736 bytes).
+SOLVER_TRAFFIC_BYTES = {8: 147_904_000}
 
 
 def main():
