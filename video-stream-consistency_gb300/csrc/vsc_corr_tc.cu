@@ -370,30 +370,29 @@ __device__ __forceinline__ uint32_t pack2(float a, float b)
 }
 
 // NCHW float -> chunked 16-bit [n][y][c / 8][x][c % 8], scaled, zero-padded
-// to chunks * 8 channels.  One thread per pixel; reads coalesced along x
-// for every channel, one 16-byte store per chunk.
+// to chunks * 8 channels.  One thread per pixel and chunk of 8 channels
+// (the small pyramid levels have few pixels and up to 25 chunks); reads
+// coalesced along x for every channel, one 16-byte store.
 template <bool kBf16>
 __global__ void to_chunked_kernel(const float* __restrict__ in, uint4* __restrict__ out, const float* __restrict__ scale,
     int C, int H, int W, int chunks)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= W)
-        return;
-    const int y = blockIdx.y, n = blockIdx.z;
-    const float s = *scale;
     const int64_t HW = static_cast<int64_t>(H) * W;
-    const float* src = in + static_cast<int64_t>(n) * C * HW + static_cast<int64_t>(y) * W + x;
-    uint4* dst = out + (static_cast<int64_t>(n) * H + y) * chunks * W + x;
-    for (int q = 0; q < chunks; ++q) {
-        float v[8];
+    const int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (p >= HW)
+        return;
+    const int q = blockIdx.y, n = blockIdx.z;
+    const int y = static_cast<int>(p / W), x = static_cast<int>(p % W);
+    const float s = *scale;
+    const float* src = in + static_cast<int64_t>(n) * C * HW + p;
+    float v[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int c = q * 8 + j;
-            v[j] = c < C ? src[c * HW] * s : 0.0f;
-        }
-        dst[static_cast<int64_t>(q) * W] = make_uint4(pack2<kBf16>(v[0], v[1]), pack2<kBf16>(v[2], v[3]),
-            pack2<kBf16>(v[4], v[5]), pack2<kBf16>(v[6], v[7]));
+    for (int j = 0; j < 8; ++j) {
+        const int c = q * 8 + j;
+        v[j] = c < C ? src[c * HW] * s : 0.0f;
     }
+    out[((static_cast<int64_t>(n) * H + y) * chunks + q) * W + x] = make_uint4(pack2<kBf16>(v[0], v[1]),
+        pack2<kBf16>(v[2], v[3]), pack2<kBf16>(v[4], v[5]), pack2<kBf16>(v[6], v[7]));
 }
 
 // custom::Warp (the single-precision arithmetic of warp_op_kernel) writing
@@ -534,7 +533,8 @@ cudaError_t launch_to_chunked(const float* in, void* out, const float* scale, in
     cudaStream_t st)
 {
     const int chunks = tc_padded_channels(C) / 8;
-    const dim3 g((W + 127) / 128, H, N);
+    const int64_t HW = static_cast<int64_t>(H) * W;
+    const dim3 g(static_cast<unsigned>((HW + 127) / 128), chunks, N);
     if (bf16)
         to_chunked_kernel<true><<<g, 128, 0, st>>>(in, static_cast<uint4*>(out), scale, C, H, W, chunks);
     else
@@ -578,7 +578,7 @@ cudaError_t launch_corr_tc(const float* f1, const float* f2, float* out, int N, 
     absmax_kernel<<<blocks, 256, 0, st>>>(f2, total, maxbits + 1);
     scales_kernel<<<1, 32, 0, st>>>(maxbits, scales);
     const int chunks = cp / 8;
-    const dim3 g((W + 127) / 128, H, N);
+    const dim3 g(static_cast<unsigned>((static_cast<int64_t>(H) * W + 127) / 128), chunks, N);
     if (bf16) {
         to_chunked_kernel<true><<<g, 128, 0, st>>>(f1, c1, scales, C, H, W, chunks);
         to_chunked_kernel<true><<<g, 128, 0, st>>>(f2, c2, scales + 1, C, H, W, chunks);

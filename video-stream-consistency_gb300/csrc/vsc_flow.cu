@@ -37,7 +37,10 @@ constexpr float kTemp = 20.0f;
 constexpr float kEps = 0.1f;
 constexpr float kLevelPrior[kFlowLevels] = {0.01f, 0.01f * 4.0f, 0.01f * 16.0f, 0.01f * 64.0f, 0.01f * 256.0f};
 
-__constant__ float c_flow_w[kWeightTotal];
+// the feature weights, in global memory: each features_kernel block stages its
+// level's weights in shared memory (the small levels' 196 x 27 weights exceed
+// what the constant cache keeps, and every warp would stream them from it)
+__device__ float g_flow_w[kWeightTotal];
 
 uint64_t splitmix64(uint64_t* s)
 {
@@ -134,7 +137,11 @@ __global__ void __launch_bounds__(32 * kFeatGroups) features_kernel(const float*
 {
     __shared__ float sf[kFeatMaxC][32];
     __shared__ float snrm[32];
+    __shared__ float sw[kFeatMaxC * 27];
     const int tx = threadIdx.x, g = threadIdx.y;
+    for (int i = g * 32 + tx; i < lc * 27; i += 32 * kFeatGroups)
+        sw[i] = g_flow_w[woff + i];
+    __syncthreads();
     const int x = blockIdx.x * 32 + tx;
     const int y = blockIdx.y;
     const bool ok = x < lw;
@@ -167,7 +174,7 @@ __global__ void __launch_bounds__(32 * kFeatGroups) features_kernel(const float*
         float f = 0.0f;
 #pragma unroll
         for (int k = 0; k < 27; ++k)
-            f += c_flow_w[woff + c * 27 + k] * p[k];
+            f += sw[c * 27 + k] * p[k];
         sf[c][tx] = f;
     }
     __syncthreads();
@@ -391,7 +398,7 @@ cudaError_t flow_upload_weights()
             host_w[kWeightOff[l] + i] = static_cast<float>(static_cast<uint32_t>(z >> 40)) * (1.0f / 8388608.0f) - 1.0f;
         }
     }
-    e = cudaMemcpyToSymbol(c_flow_w, host_w, sizeof(host_w));
+    e = cudaMemcpyToSymbol(g_flow_w, host_w, sizeof(host_w));
     if (e == cudaSuccess && dev >= 0 && dev < 64)
         done[dev] = true;
     return e;

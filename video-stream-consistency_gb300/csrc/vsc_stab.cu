@@ -284,6 +284,50 @@ __global__ void bilinear_kernel(const float* __restrict__ in, int iw, int ih, fl
     bilinear_px(in, iw, ih, ow, oh, c, ox, oy, out + pix_index(ox, oy, ow) * c);
 }
 
+// bilinear_px for four consecutive output pixels of C channels per thread:
+// the row terms are computed once, the 4 C outputs leave as 16-byte stores
+// when the row is 16-byte aligned (same arithmetic, same bits).
+template <int C>
+__global__ void bilinear4_kernel(const float* __restrict__ in, int iw, int ih, float* __restrict__ out, int ow, int oh)
+{
+    const int ox0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    const int oy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ox0 >= ow || oy >= oh)
+        return;
+    const float yy = static_cast<float>(oy) * static_cast<float>(ih) / static_cast<float>(oh);
+    const int iy = min(static_cast<int>(floorf(yy)), ih - 1);
+    const float fy = yy - static_cast<float>(iy);
+    const int iy1 = min(iy + 1, ih - 1);
+    float v[4 * C];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int ox = min(ox0 + j, ow - 1);
+        const float xx = static_cast<float>(ox) * static_cast<float>(iw) / static_cast<float>(ow);
+        const int ix = min(static_cast<int>(floorf(xx)), iw - 1);
+        const float fx = xx - static_cast<float>(ix);
+        const int ix1 = min(ix + 1, iw - 1);
+#pragma unroll
+        for (int k = 0; k < C; ++k) {
+            const float v00 = in[pix_index(ix, iy, iw) * C + k];
+            const float v10 = in[pix_index(ix1, iy, iw) * C + k];
+            const float v01 = in[pix_index(ix, iy1, iw) * C + k];
+            const float v11 = in[pix_index(ix1, iy1, iw) * C + k];
+            v[j * C + k] = v00 * (1 - fx) * (1 - fy) + v10 * fx * (1 - fy) + v01 * (1 - fx) * fy + v11 * fx * fy;
+        }
+    }
+    float* dst = out + pix_index(ox0, oy, ow) * C;
+    if (ox0 + 3 < ow && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+#pragma unroll
+        for (int q = 0; q < C; ++q)
+            reinterpret_cast<float4*>(dst)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    } else {
+        for (int j = 0; j < 4 && ox0 + j < ow; ++j)
+#pragma unroll
+            for (int k = 0; k < C; ++k)
+                dst[j * C + k] = v[j * C + k];
+    }
+}
+
 __global__ void pyr_down3_kernel(const float* __restrict__ P, const float* __restrict__ A,
     const float* __restrict__ Wt, int iw, int ih, float* __restrict__ Pd, float* __restrict__ Ad,
     float* __restrict__ Wd, int ow, int oh)
@@ -482,7 +526,15 @@ cudaError_t launch_consist_wt(Img ai, Img ci, Img wt, float beta, float gamma, c
 cudaError_t launch_bilinear(Img in, Img out, cudaStream_t st)
 {
     const dim3 b(32, 8);
-    bilinear_kernel<<<grid2d(out.w, out.h, b), b, 0, st>>>(in.d, in.w, in.h, out.d, out.w, out.h, out.c);
+    if (out.c == 2 || out.c == 3) {
+        const dim3 g((out.w + 4 * b.x - 1) / (4 * b.x), (out.h + b.y - 1) / b.y);
+        if (out.c == 3)
+            bilinear4_kernel<3><<<g, b, 0, st>>>(in.d, in.w, in.h, out.d, out.w, out.h);
+        else
+            bilinear4_kernel<2><<<g, b, 0, st>>>(in.d, in.w, in.h, out.d, out.w, out.h);
+    } else {
+        bilinear_kernel<<<grid2d(out.w, out.h, b), b, 0, st>>>(in.d, in.w, in.h, out.d, out.w, out.h, out.c);
+    }
     return cudaGetLastError();
 }
 
