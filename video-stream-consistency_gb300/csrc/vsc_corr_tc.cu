@@ -127,7 +127,8 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, volatile
 // part of the epilogue).
 __global__ void __launch_bounds__((2 + 4 * kMaxEpiGroups) * 32, 1)
     corr_tc_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB,
-        float* __restrict__ out, const float* __restrict__ scales, int N, int H, int W, int Cp, int md,
+        float* __restrict__ out, const __grid_constant__ CUtensorMap mA2, const __grid_constant__ CUtensorMap mB2,
+        float* __restrict__ out2, int nprob, const float* __restrict__ scales, int N, int H, int W, int Cp, int md,
         uint32_t idesc, int stages_a, int stages_b, int groups, int ndyg, int* __restrict__ timeout_flag)
 {
     extern __shared__ unsigned char smem_raw[];
@@ -160,7 +161,10 @@ __global__ void __launch_bounds__((2 + 4 * kMaxEpiGroups) * 32, 1)
     // work item: (n, segment, row y, group of displacement rows); small maps
     // split the 2 md + 1 displacement rows over ndyg items to fill the GPU
     const int rpg = (P + ndyg - 1) / ndyg;
-    const int items = N * H * nseg * ndyg;
+    // nprob independent correlations of the same shape (the flow's two
+    // directions) share the launch: item it belongs to problem it / items_per
+    const int items_per = N * H * nseg * ndyg;
+    const int items = items_per * nprob;
 
     if (warp == 1) {
         ptx::tmem_alloc(sh.tmem_slot, kTmemCols);
@@ -192,7 +196,10 @@ __global__ void __launch_bounds__((2 + 4 * kMaxEpiGroups) * 32, 1)
             int ua = 0, ub = 0;
             bool ok = true;
             for (int it = blockIdx.x; ok && it < items; it += gridDim.x) {
-                const int dyg = it % ndyg, r = it / ndyg;
+                const int prob = it / items_per, il = it - prob * items_per;
+                const CUtensorMap* ma = prob ? &mA2 : &mA;
+                const CUtensorMap* mb = prob ? &mB2 : &mB;
+                const int dyg = il % ndyg, r = il / ndyg;
                 const int y = r % H, seg = (r / H) % nseg, n = r / (H * nseg);
                 const int d0 = dyg * rpg, d1 = min(P, d0 + rpg);
                 const int x0 = seg * kTcM;
@@ -200,14 +207,14 @@ __global__ void __launch_bounds__((2 + 4 * kMaxEpiGroups) * 32, 1)
                 if (!(ok = tc_wait(&sh.empty_a[sa], ((ua / stages_a) & 1) ^ 1, sh.abort)))
                     break;
                 ptx::mbar_expect_tx(&sh.full_a[sa], bytesA);
-                ptx::tma_load_5d(sh.a + sa * sh.a_stride, &mA, 0, x0, 0, y, n, &sh.full_a[sa]);
+                ptx::tma_load_5d(sh.a + sa * sh.a_stride, ma, 0, x0, 0, y, n, &sh.full_a[sa]);
                 ++ua;
                 for (int d = d0; d < d1; ++d) {
                     const int sb = ub % stages_b;
                     if (!(ok = tc_wait(&sh.empty_b[sb], ((ub / stages_b) & 1) ^ 1, sh.abort)))
                         break;
                     ptx::mbar_expect_tx(&sh.full_b[sb], bytesB);
-                    ptx::tma_load_5d(sh.b + sb * sh.b_stride, &mB, 0, x0 - md, 0, y + d - md, n, &sh.full_b[sb]);
+                    ptx::tma_load_5d(sh.b + sb * sh.b_stride, mb, 0, x0 - md, 0, y + d - md, n, &sh.full_b[sb]);
                     ++ub;
                 }
             }
@@ -228,7 +235,7 @@ __global__ void __launch_bounds__((2 + 4 * kMaxEpiGroups) * 32, 1)
             int ua = 0, ub = 0, ud = 0;
             bool ok = true;
             for (int it = blockIdx.x; ok && it < items; it += gridDim.x) {
-                const int dyg = it % ndyg;
+                const int dyg = (it % items_per) % ndyg;
                 const int d0 = dyg * rpg, d1 = min(P, d0 + rpg);
                 const int sa = ua % stages_a;
                 if (!(ok = tc_wait(&sh.full_a[sa], (ua / stages_a) & 1, sh.abort)))
@@ -273,11 +280,12 @@ __global__ void __launch_bounds__((2 + 4 * kMaxEpiGroups) * 32, 1)
         int ud = 0;  // accumulator use index, counted over every row of the CTA
         bool ok = true;
         for (int it = blockIdx.x; ok && it < items; it += gridDim.x) {
-            const int dyg = it % ndyg, r = it / ndyg;
+            const int prob = it / items_per, il = it - prob * items_per;
+            const int dyg = il % ndyg, r = il / ndyg;
             const int y = r % H, seg = (r / H) % nseg, n = r / (H * nseg);
             const int d0 = dyg * rpg, d1 = min(P, d0 + rpg);
             const int x = seg * kTcM + q * 32 + lane;
-            float* obase = out + static_cast<int64_t>(n) * P * P * HW + static_cast<int64_t>(y) * W + x;
+            float* obase = (prob ? out2 : out) + static_cast<int64_t>(n) * P * P * HW + static_cast<int64_t>(y) * W + x;
             for (int d = d0; d < d1; ++d, ++ud) {
                 if (ud % groups != grp)
                     continue;
@@ -505,6 +513,13 @@ size_t corr_tc_workspace_bytes(int N, int C, int H, int W)
 cudaError_t launch_corr_tc_chunked(const void* f1c, const void* f2c, float* out, const float* scales, int N, int Cp,
     int H, int W, int md, bool bf16, cudaStream_t st)
 {
+    return launch_corr_tc_chunked2(f1c, f2c, out, nullptr, nullptr, nullptr, scales, N, Cp, H, W, md, bf16, st);
+}
+
+cudaError_t launch_corr_tc_chunked2(const void* f1c, const void* f2c, float* out, const void* g1c, const void* g2c,
+    float* out2, const float* scales, int N, int Cp, int H, int W, int md, bool bf16, cudaStream_t st)
+{
+    const int nprob = g1c ? 2 : 1;
     if (Cp % 16 != 0 || Cp > kTcMaxChannelsPadded || md < 0 || md > kTcMaxMd)
         return cudaErrorInvalidValue;
     int sms = 0;
@@ -514,18 +529,26 @@ cudaError_t launch_corr_tc_chunked(const void* f1c, const void* f2c, float* out,
     int* flag = nullptr;
     if ((e = device_timeout_flag(&flag)) != cudaSuccess)
         return e;
-    CUtensorMap mA, mB;
+    CUtensorMap mA, mB, mA2, mB2;
     if (!encode_chunked_map(&mA, f1c, N, H, W, Cp, kTcM) || !encode_chunked_map(&mB, f2c, N, H, W, Cp, kTcN))
         return cudaErrorInvalidValue;
+    if (nprob == 2 &&
+        (!encode_chunked_map(&mA2, g1c, N, H, W, Cp, kTcM) || !encode_chunked_map(&mB2, g2c, N, H, W, Cp, kTcN)))
+        return cudaErrorInvalidValue;
+    if (nprob == 1) {
+        mA2 = mA;
+        mB2 = mB;
+    }
     const TcPlan plan = tc_plan(Cp);
     const int P = 2 * md + 1;
-    const int base = N * H * ((W + kTcM - 1) / kTcM);
+    const int base = nprob * N * H * ((W + kTcM - 1) / kTcM);
     int ndyg = 1;  // split the displacement rows until there are two items per SM
     while (ndyg < P && base * ndyg < 2 * sms)
         ++ndyg;
     const int items = base * ndyg;
-    corr_tc_kernel<<<std::min(items, sms), (2 + 4 * plan.groups) * 32, plan.smem, st>>>(mA, mB, out, scales, N, H,
-        W, Cp, md, ptx::umma_idesc_f16(bf16, kTcM, kTcN), plan.stages_a, plan.stages_b, plan.groups, ndyg, flag);
+    corr_tc_kernel<<<std::min(items, sms), (2 + 4 * plan.groups) * 32, plan.smem, st>>>(mA, mB, out, mA2, mB2,
+        nprob == 2 ? out2 : out, nprob, scales, N, H, W, Cp, md, ptx::umma_idesc_f16(bf16, kTcM, kTcN), plan.stages_a,
+        plan.stages_b, plan.groups, ndyg, flag);
     return cudaGetLastError();
 }
 

@@ -527,21 +527,23 @@ cudaError_t launch_flow_pair(const float* featA, int64_t sA, const float* featB,
             ++nl;
         }
         if (tc) {
-            // the tensor-core correlation, one launch per direction (each
-            // direction's operands are separate tensors)
+            // the tensor-core correlations of both directions in one launch
+            // (each direction's operands are separate tensors)
             const size_t lo = tc_level_offset(d, l);
+            const void* ac[2];
+            const void* bc[2];
             for (int dir = 0; dir < 2; ++dir) {
-                const void* ac = static_cast<const unsigned char*>(tc->a[dir]) + lo;
-                const void* bc = l < kFlowLevels - 1
-                                     ? static_cast<const void*>(static_cast<const unsigned char*>(tc->warped) +
-                                                                dir * tc_warped_bytes(d))
-                                     : static_cast<const void*>(static_cast<const unsigned char*>(tc->b[dir]) + lo);
-                e = launch_corr_tc_chunked(ac, bc, cv + dir * bs, tc->scales, 1, tc_padded_channels(lc), lh, lw, 4,
-                    tc->bf16, st);
-                if (e != cudaSuccess)
-                    return e;
-                ++nl;
+                ac[dir] = static_cast<const unsigned char*>(tc->a[dir]) + lo;
+                bc[dir] = l < kFlowLevels - 1
+                              ? static_cast<const void*>(static_cast<const unsigned char*>(tc->warped) +
+                                                         dir * tc_warped_bytes(d))
+                              : static_cast<const void*>(static_cast<const unsigned char*>(tc->b[dir]) + lo);
             }
+            e = launch_corr_tc_chunked2(ac[0], bc[0], cv, ac[1], bc[1], cv + bs, tc->scales, 1,
+                tc_padded_channels(lc), lh, lw, 4, tc->bf16, st);
+            if (e != cudaSuccess)
+                return e;
+            ++nl;
         } else {
             e = launch_correlation(fa, fb_use, cv, 2, lc, lh, lw, 4, 0, st, sA, sb_use, bs);
             if (e != cudaSuccess)

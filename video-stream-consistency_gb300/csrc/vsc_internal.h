@@ -46,6 +46,9 @@ cudaError_t launch_corr_tc(const float* f1, const float* f2, float* out, int N, 
 // (Cp channels) with their scales (2 floats: f1, f2) on the device.
 cudaError_t launch_corr_tc_chunked(const void* f1c, const void* f2c, float* out, const float* scales, int N, int Cp,
     int H, int W, int md, bool bf16, cudaStream_t st);
+// two correlations of the same shape in one launch (f1c / f2c -> out and g1c / g2c -> out2)
+cudaError_t launch_corr_tc_chunked2(const void* f1c, const void* f2c, float* out, const void* g1c, const void* g2c,
+    float* out2, const float* scales, int N, int Cp, int H, int W, int md, bool bf16, cudaStream_t st);
 
 // float NCHW -> chunked 16-bit operand layout, multiplied by *scale.
 cudaError_t launch_to_chunked(const float* in, void* out, const float* scale, int N, int C, int H, int W, bool bf16,
