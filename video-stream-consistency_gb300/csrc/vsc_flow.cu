@@ -228,21 +228,33 @@ __global__ void up2_kernel(const float* __restrict__ in, int sw, int sh, float* 
     }
 }
 
-__global__ void decode_kernel(const float* __restrict__ cv, float* __restrict__ res, float* __restrict__ conf,
-    int64_t plane, float prior, int64_t bs)
+// One thread per pixel, 64 per block: the pixel's 81 cost values are first
+// copied to its own column of shared memory (independent loads, issued
+// nine at a time), then the arg-max, the soft centroid and the confidence
+// read them from there -- the same operations in the same order as a direct
+// walk over the cost volume, without a chain of dependent global loads.
+constexpr int kDecodeThreads = 64;
+
+__global__ void __launch_bounds__(kDecodeThreads) decode_kernel(const float* __restrict__ cv, float* __restrict__ res,
+    float* __restrict__ conf, int64_t plane, float prior, int64_t bs)
 {
-    const int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    __shared__ float sv[81][kDecodeThreads];
+    const int t = threadIdx.x;
+    const int64_t p = blockIdx.x * static_cast<int64_t>(kDecodeThreads) + t;
     if (p >= plane)
         return;
     cv += blockIdx.z * bs;
     res += blockIdx.z * bs;
     conf += blockIdx.z * bs;
+#pragma unroll 9
+    for (int d = 0; d < 81; ++d)
+        sv[d][t] = cv[d * plane + p];
     int best = 0;
-    float cmax = cv[p] - prior * 32.0f;
-    float csum = cv[p];
+    float cmax = sv[0][t] - prior * 32.0f;
+    float csum = sv[0][t];
     for (int d = 1; d < 81; ++d) {
         const int ddx = d % 9 - 4, ddy = d / 9 - 4;
-        const float raw = cv[d * plane + p];
+        const float raw = sv[d][t];
         csum += raw;
         const float v = raw - prior * static_cast<float>(ddx * ddx + ddy * ddy);
         if (v > cmax) {
@@ -259,7 +271,7 @@ __global__ void decode_kernel(const float* __restrict__ cv, float* __restrict__ 
             if (nx < 0 || nx > 8)
                 continue;
             const float sc =
-                cv[(ny * 9 + nx) * plane + p] - prior * static_cast<float>((nx - 4) * (nx - 4) + (ny - 4) * (ny - 4));
+                sv[ny * 9 + nx][t] - prior * static_cast<float>((nx - 4) * (nx - 4) + (ny - 4) * (ny - 4));
             const float e = expf_cw((sc - cmax) * kTemp);
             sw += e;
             sx += e * static_cast<float>(nx - 4);
@@ -268,7 +280,7 @@ __global__ void decode_kernel(const float* __restrict__ cv, float* __restrict__ 
     }
     res[p] = __fdiv_rn(sx, sw);
     res[plane + p] = __fdiv_rn(sy, sw);
-    const float k = cv[best * plane + p] - __fdiv_rn(csum, 81.0f);
+    const float k = sv[best][t] - __fdiv_rn(csum, 81.0f);
     conf[p] = k > 0.0f ? k : 0.0f;
 }
 
@@ -550,8 +562,8 @@ cudaError_t launch_flow_pair(const float* featA, int64_t sA, const float* featB,
                 return e;
             ++nl;
         }
-        decode_kernel<<<dim3(static_cast<unsigned>((plane + 255) / 256), 1, 2), 256, 0, st>>>(cv, raw, raw + 2 * plane,
-            plane, kLevelPrior[l], bs);
+        decode_kernel<<<dim3(static_cast<unsigned>((plane + kDecodeThreads - 1) / kDecodeThreads), 1, 2),
+            kDecodeThreads, 0, st>>>(cv, raw, raw + 2 * plane, plane, kLevelPrior[l], bs);
         ++nl;
         cur ^= 1;
         dim3 g = g2(lw, lh, b);
