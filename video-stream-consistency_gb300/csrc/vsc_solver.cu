@@ -336,6 +336,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
         : "memory");
 }
 
+// Programmatic dependent launch: a solver launch may start while the previous
+// one drains (its CTAs set up shared memory and barriers meanwhile); before
+// the first read of the previous launch's O and U, and before any write to
+// the images it was reading, every thread waits for that launch to complete.
+// The previous launch lets the next one start once each of its CTAs is on
+// its last tile.  Without the launch attribute both are no-ops.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void allow_dependent_launch() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+
 // TMA tensor store (shared -> global) of one box; elements outside the image are clipped
 __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, const void* src)
 {
@@ -397,10 +406,13 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
         mbar_init(bar, 1);
     __syncthreads();
     int tile = blockIdx.x;
+    grid_dependency_wait();
     if (tid == 0 && tile < ntiles)
         issue_tile(stage, &mO, &mU, &mA, &mW, &mL, tile, tiles_x, bar);
     uint32_t parity = 0;
     for (; tile < ntiles; tile += gridDim.x) {
+        if (tile + static_cast<int>(gridDim.x) >= ntiles)
+            allow_dependent_launch();
         const int ox = (tile % tiles_x) * kIW - kTbT;
         const int oy = (tile / tiles_x) * kIH - kTbT;
         if (!mbar_wait_bounded(bar, parity, kWaitSpins)) {
@@ -661,10 +673,13 @@ __global__ void __launch_bounds__(kPThreads, 1)
         mbar_init(bar, 1);
     __syncthreads();
     int tile = blockIdx.x;
+    grid_dependency_wait();
     if (threadIdx.x == 0 && tile < ntiles)
         issue_tall_tile(stage, &mO, &mU, &mA, &mW, &mL, tile, tiles_x, bar);
     uint32_t parity = 0;
     for (; tile < ntiles; tile += gridDim.x) {
+        if (tile + static_cast<int>(gridDim.x) >= ntiles)
+            allow_dependent_launch();
         const int ox = (tile % tiles_x) * kIW - kTbT;
         const int oy = (tile / tiles_x) * kPIH - kTbT;
         if (!mbar_wait_bounded(bar, parity, kWaitSpins)) {
@@ -895,14 +910,27 @@ void launch_persistent(int rows, const CUtensorMap& mO, const CUtensorMap& mU, c
     int T, int k0, float step, float mom, uint8_t* rgba, int sms, cudaStream_t st)
 {
     const int tiles_x = (w + kIW - 1) / kIW;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
     if (rows == kPEY) {
         const int ntiles = tiles_x * ((h + kPIH - 1) / kPIH);
-        solver_tall_kernel<<<std::min(ntiles, sms), kPThreads, kPSmem, st>>>(mO, mU, mA, mW, mL, mOo, mUo, w, h,
-            T, k0, step, mom, rgba, tiles_x, ntiles);
+        cfg.gridDim = dim3(std::min(ntiles, sms));
+        cfg.blockDim = dim3(kPThreads);
+        cfg.dynamicSmemBytes = kPSmem;
+        cudaLaunchKernelEx(&cfg, solver_tall_kernel, mO, mU, mA, mW, mL, mOo, mUo, w, h, T, k0, step, mom, rgba,
+            tiles_x, ntiles);
     } else {
         const int ntiles = tiles_x * ((h + kIH - 1) / kIH);
-        solver_persistent_kernel<<<std::min(ntiles, sms), dim3(32, kTbEY / 2), kPsSmem, st>>>(mO, mU, mA, mW, mL,
-            mOo, mUo, w, h, T, k0, step, mom, rgba, tiles_x, ntiles);
+        cfg.gridDim = dim3(std::min(ntiles, sms));
+        cfg.blockDim = dim3(32, kTbEY / 2);
+        cfg.dynamicSmemBytes = kPsSmem;
+        cudaLaunchKernelEx(&cfg, solver_persistent_kernel, mO, mU, mA, mW, mL, mOo, mUo, w, h, T, k0, step, mom, rgba,
+            tiles_x, ntiles);
     }
 }
 
