@@ -328,7 +328,11 @@ VSC_API vsc_hyper_params* vsc_stabilizer_hyper_params(vsc_stabilizer* s);
 
 /* Append frame i to the window (loadFrame + imageToGPU, stabilizefiles.cpp:72-96):
  * RGBA8 original and per-frame processed images, width x height x 4, on the
- * host (on_device = 0; pinned memory gives asynchronous copies) or device. */
+ * host (on_device = 0) or device.  Pageable host frames are copied before the
+ * call returns; pinned host frames and device frames are read asynchronously
+ * on the stabilizer's stream, so keep them unchanged until that stream has
+ * passed the load (a later vsc_stabilizer_step with a host output, or a
+ * stream synchronisation). */
 VSC_API vsc_status vsc_stabilizer_load_frame(vsc_stabilizer* s, const uint8_t* orig_rgba, const uint8_t* proc_rgba,
     int32_t on_device);
 
