@@ -406,11 +406,17 @@ VSC_API vsc_status vsc_stabilizer_set_upsampler(vsc_stabilizer* s, vsc_upsampler
 
 /* ---- several streams per frame step (no counterpart in the reference) -------
  * Stabilizes n independent videos of any sizes in lockstep: each step runs
- * every stream's doOneStep, forked from `stream` onto one CUDA stream per
- * video and joined back, and from the second step on the whole fork/join is
- * replayed as one CUDA graph (captured once per window position).  Flows are
- * computed by the library (compute_flow = 1); every stream shares the
- * hyper-parameters of vsc_multistream_hyper_params. */
+ * every stream's doOneStep.  Each video's flows, warps, combination and
+ * pyramid run on a CUDA stream of its own, forked from `stream`; the solves
+ * are grouped: per pyramid level, each launch of the persistent solver
+ * kernel (8 Jacobi steps) walks the tiles of every video's image, so one
+ * launch sequence on `stream` solves all videos (up to 16 per launch), with
+ * the tile shape autotuned at creation for the list of sizes.  From the
+ * second step on the whole step is replayed as one CUDA graph (captured once
+ * per window position).  Flows are computed by the library (compute_flow =
+ * 1); every stream shares the hyper-parameters of
+ * vsc_multistream_hyper_params.  Results equal those of independent
+ * stabilizers bit for bit, grouped or not. */
 typedef struct vsc_stream_desc {
     int32_t width, height;
     int32_t flow_downscale; /* 0 or 1: none */
@@ -428,6 +434,17 @@ VSC_API vsc_status vsc_multistream_load_frames(vsc_multistream* m, const uint8_t
 /* out[i]: stream i's stabilized RGBA8 frame (NULL entries skip the copy). */
 VSC_API vsc_status vsc_multistream_step(vsc_multistream* m, uint8_t* const* out, int32_t out_on_device);
 VSC_API int32_t vsc_multistream_last_launches(vsc_multistream* m);
+/* Grouped solves on (default) or off (each video's solve on its own CUDA
+ * stream, as a lone stabilizer runs it).  Grouping needs every pyramid
+ * level's width to be a multiple of 4; otherwise the step runs ungrouped.
+ * vsc_multistream_fused: 1 if a step with the current hyper-parameters runs
+ * grouped. */
+VSC_API vsc_status vsc_multistream_set_fused(vsc_multistream* m, int32_t on);
+VSC_API int32_t vsc_multistream_fused(vsc_multistream* m);
+/* The learned flow upsampler for stream `index` (-1: every stream created
+ * with flow_downscale > 1), as vsc_stabilizer_set_upsampler; NULL: bilinear.
+ * Synchronises `stream`. */
+VSC_API vsc_status vsc_multistream_set_upsampler(vsc_multistream* m, int32_t index, vsc_upsampler* u);
 
 /* ---- frame directories (FileStabilizer, stabilizefiles.cpp:37-149) ----------
  * Image files: PNG (8-bit gray, gray+alpha, RGB or RGBA, not interlaced) and

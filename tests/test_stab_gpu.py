@@ -90,6 +90,17 @@ def test_bilinear(vsc, oracle, cuda, src, dst):
     assert np.array_equal(got, oracle.bilinear(img, dst[0], dst[1]))
 
 
+def _equal_up_to_zero_sign(a, b):
+    """Equal as IEEE values, and where the bits differ both are zeros: the
+    solver sums a pixel's neighbours from the first term, the oracle (as the
+    reference) onto 0.0f, which can change only the sign of a zero."""
+    a, b = np.ascontiguousarray(a, np.float32), np.ascontiguousarray(b, np.float32)
+    if not np.array_equal(a, b):
+        return False
+    differ = a.view(np.uint32) != b.view(np.uint32)
+    return bool(np.all(a[differ] == 0))
+
+
 # widths divisible by 4 take the persistent TMA-fed kernel, others the
 # per-tile kernel; iteration counts not divisible by 8 end in a short launch
 @pytest.mark.parametrize("h,w,iters", [(9, 11, 0), (9, 11, 1), (9, 11, 2), (40, 56, 75), (3, 3, 5), (2, 2, 4),
@@ -102,12 +113,31 @@ def test_consist_out(vsc, oracle, cuda, h, w, iters):
     O = _t(O0, cuda)
     vsc.get_consist_out(_t(P, cuda), _t(A, cuda), _t(Wt, cuda), iters, 0.15, 0.15, O)
     ref = oracle.consist_out(P, A, Wt, iters, 0.15, 0.15, O0)
-    assert np.array_equal(O.cpu().numpy(), ref)
+    assert _equal_up_to_zero_sign(O.cpu().numpy(), ref)
     # caller-provided workspace gives the same bits
     ws = torch.empty(vsc.consist_out_workspace_size(w, h) // 4, dtype=torch.float32, device=cuda)
     O2 = _t(O0, cuda)
     vsc.get_consist_out(_t(P, cuda), _t(A, cuda), _t(Wt, cuda), iters, 0.15, 0.15, O2, workspace=ws)
-    assert np.array_equal(O2.cpu().numpy(), ref)
+    assert np.array_equal(O2.cpu().numpy().view(np.uint32), O.cpu().numpy().view(np.uint32))
+
+
+def test_consist_out_zero_regions(vsc, oracle, cuda):
+    """All-zero regions (black borders, zero weights) where the sign of a
+    zero can differ from the oracle's: the values and the RGBA8 bytes are
+    the oracle's."""
+    h, w = 40, 56
+    P, A, Wt, O0 = _img(h, w), _img(h, w), _img(h, w, hi=2.0), _img(h, w)
+    for X in (P, A, O0):
+        X[:, :9] = 0.0
+        X[:12] = 0.0
+    Wt[:, :20] = 0.0
+    O0[:6, :6] = -0.0
+    O = _t(O0, cuda)
+    vsc.get_consist_out(_t(P, cuda), _t(A, cuda), _t(Wt, cuda), 37, 0.15, 0.15, O)
+    ref = oracle.consist_out(P, A, Wt, 37, 0.15, 0.15, O0)
+    got = O.cpu().numpy()
+    assert _equal_up_to_zero_sign(got, ref)
+    assert np.array_equal(oracle.float_to_rgba(got), oracle.float_to_rgba(ref))
 
 
 def test_bounded_wait_timeout_is_reported(vsc, oracle, cuda):
@@ -371,35 +401,42 @@ def test_full_hd_step_deterministic(vsc, cuda):
     assert outs[0][1][..., 3].max() == 1
 
 
-def test_multistream_equals_independent_stabilizers(vsc, cuda):
-    """Three videos of different sizes in one multistream object: every
-    stream's output equals its own stabilizer's, bit for bit, on the direct
-    first step and on the graph replays that follow."""
+def _multistream_vs_singles(vsc, sizes, forms, fused, num_iter, upsampler=None, steps=5, levels=2):
+    """Runs a MultiStream and one Stabilizer per stream (each with the
+    stream's (flow_downscale, corr_dtype) form) on the same frames and
+    asserts equal outputs, bit for bit, on the direct first step and on the
+    graph replays that follow.  Returns the multistream's launch count."""
     import torch
 
-    sizes = [(96, 64), (128, 72), (80, 48)]
-    streams = [_frames(w, h, 7, seed=50 + i) for i, (w, h) in enumerate(sizes)]
+    streams = [_frames(w, h, steps + 2, seed=50 + i) for i, (w, h) in enumerate(sizes)]
     side = torch.cuda.Stream()
-    ms = vsc.MultiStream(sizes, stream=side)
-    ms.hyper_params.num_iter = 60
+    ms = vsc.MultiStream(sizes, flow_downscale=[f[0] for f in forms], corr_dtype=[f[1] for f in forms], stream=side)
+    ms.set_fused(fused)
+    ms.hyper_params.num_iter = num_iter
+    ms.hyper_params.pyramid_levels = levels
     singles = []
-    for (w, h), fr in zip(sizes, streams):
-        st = vsc.Stabilizer(w, h)
-        st.hyper_params.num_iter = 60
+    for (w, h), (ds, dt) in zip(sizes, forms):
+        st = vsc.Stabilizer(w, h, flow_downscale=ds, corr_dtype=dt)
+        st.hyper_params.num_iter = num_iter
+        st.hyper_params.pyramid_levels = levels
+        if upsampler is not None and ds > 1:
+            st.set_upsampler(upsampler)
         singles.append(st)
+    if upsampler is not None:
+        ms.set_upsampler(upsampler)
     for i in range(3):  # host frames: each stream uploads on its own CUDA stream
         ms.load_frames([fr[i][0] for fr in streams], [fr[i][1] for fr in streams])
         for st, fr in zip(singles, streams):
             st.load_frame(*fr[i])
     side.synchronize()
-    for t in range(1, 6):
+    for t in range(1, steps + 1):
         with torch.cuda.stream(side):
             outs = ms.step()
         side.synchronize()
         for k, (st, out) in enumerate(zip(singles, outs)):
             ref = st.step().cpu().numpy()
             assert np.array_equal(out.cpu().numpy(), ref), (t, k)
-        if t + 2 < 7:
+        if t + 2 < steps + 2:
             if t % 2:  # device frames, made ready before the call
                 o = [torch.from_numpy(fr[t + 2][0]).cuda() for fr in streams]
                 p = [torch.from_numpy(fr[t + 2][1]).cuda() for fr in streams]
@@ -409,10 +446,53 @@ def test_multistream_equals_independent_stabilizers(vsc, cuda):
                 ms.load_frames([fr[t + 2][0] for fr in streams], [fr[t + 2][1] for fr in streams])
             for st, fr in zip(singles, streams):
                 st.load_frame(*fr[t + 2])
-    assert ms.last_launches > 3 * 20
+    n = ms.last_launches
+    grouped = ms.fused
     ms.close()
     for st in singles:
         st.close()
+    return n, grouped
+
+
+@pytest.mark.parametrize("fused,levels", [(True, 2), (False, 2), (True, 1)])
+def test_multistream_equals_independent_stabilizers(vsc, cuda, fused, levels):
+    """Three videos of different sizes in one multistream object, solves
+    grouped into shared persistent-kernel launches or each on its own CUDA
+    stream: every stream's output equals its own stabilizer's, bit for bit."""
+    sizes = [(96, 64), (128, 72), (80, 48)]
+    n, grouped = _multistream_vs_singles(vsc, sizes, [(1, "f32")] * 3, fused, 60, levels=levels)
+    assert grouped == fused
+    assert n > (3 * 20 if not fused else 8)
+
+
+def test_multistream_mixed_forms_with_upsampler(vsc, cuda):
+    """Per-stream forms in one grouped step: full-size FP32 and BF16 flows,
+    and half-size flows upsampled by the learned network (odd iteration
+    count, so each level's solve starts in the second buffer; three
+    pyramid levels)."""
+    up = vsc.Upsampler("default")
+    sizes = [(96, 64), (128, 80), (160, 96), (112, 64)]
+    forms = [(1, "f32"), (2, "bf16"), (2, "f32"), (1, "bf16")]
+    _, grouped = _multistream_vs_singles(vsc, sizes, forms, True, 45, upsampler=up, steps=4, levels=3)
+    assert grouped
+    up.close()
+
+
+def test_multistream_more_than_one_group(vsc, cuda):
+    """18 streams: each solver launch of the grouped form covers at most 16
+    images, so every level takes two launches per 8 steps; results equal the
+    independent stabilizers'."""
+    sizes = [(64 + 8 * (i % 5), 40 + 4 * (i % 3)) for i in range(18)]
+    n, grouped = _multistream_vs_singles(vsc, sizes, [(1, "f32")] * 18, True, 40, steps=3)
+    assert grouped
+
+
+def test_multistream_ungroupable_size_runs_ungrouped(vsc, cuda):
+    """A level width that is not a multiple of 4 (70 -> 35) keeps the step
+    ungrouped, with the same results."""
+    sizes = [(96, 64), (70, 45)]
+    _, grouped = _multistream_vs_singles(vsc, sizes, [(1, "f32")] * 2, True, 24, steps=3)
+    assert not grouped
 
 
 @pytest.mark.parametrize("fc,occ", [(3, False), (2, False), (2, True)])

@@ -45,6 +45,7 @@ EXPORTED = [
     "vsc_upsampler_param_count", "vsc_upsampler_create", "vsc_upsampler_destroy", "vsc_upsampler_get_params",
     "vsc_upsampler_set_max_residual", "vsc_upsampler_prepare", "vsc_upsampler_train_step", "vsc_upsampler_apply",
     "vsc_stabilizer_set_upsampler", "vsc_solver_autotune", "vsc_solver_tile_rows", "vsc_solver_set_autotune",
+    "vsc_multistream_set_fused", "vsc_multistream_fused", "vsc_multistream_set_upsampler",
 ]
 VSC_DTYPE_F32, VSC_DTYPE_BF16, VSC_DTYPE_F16 = 0, 1, 2
 NOALLOC_MAX_PIXELS = 349525  # VSC_NOALLOC_MAX_PIXELS
@@ -164,6 +165,8 @@ def load():
         "vsc_multistream_destroy": [vp],
         "vsc_multistream_load_frames": [vp, C.POINTER(vp), C.POINTER(vp), i32],
         "vsc_multistream_step": [vp, C.POINTER(vp), i32],
+        "vsc_multistream_set_fused": [vp, i32],
+        "vsc_multistream_set_upsampler": [vp, i32, vp],
         "vsc_get_adap_comb_masked": [IP] * 10 + [f32, vp],
         "vsc_stabilizer_set_occlusion_mask": [vp, i32],
         "vsc_check_device": [],
@@ -179,6 +182,8 @@ def load():
     L.vsc_multistream_hyper_params.argtypes = [vp]
     L.vsc_multistream_last_launches.restype = i32
     L.vsc_multistream_last_launches.argtypes = [vp]
+    L.vsc_multistream_fused.restype = i32
+    L.vsc_multistream_fused.argtypes = [vp]
     L.vsc_solver_steps_per_launch.restype = i32
     L.vsc_solver_steps_per_launch.argtypes = []
     L.vsc_solver_tile_rows.restype = i32
@@ -642,18 +647,27 @@ class Stabilizer:
 
 class MultiStream:
     """Several independent videos stabilized in lockstep, one graph launch per
-    frame step (vsc_multistream_*).  sizes: [(width, height), ...]."""
+    frame step, the solves of all videos grouped into shared launches of the
+    persistent solver kernel (vsc_multistream_*).  sizes: [(width, height),
+    ...]; flow_downscale and corr_dtype: one value for every stream or a
+    list with one per stream."""
 
-    def __init__(self, sizes, flow_downscale=1, corr_dtype: str = "f32", stream=None):
+    def __init__(self, sizes, flow_downscale=1, corr_dtype="f32", stream=None):
         import torch
 
-        code = {"f32": VSC_DTYPE_F32, "bf16": VSC_DTYPE_BF16, "fp16": VSC_DTYPE_F16}[corr_dtype]
+        codes = {"f32": VSC_DTYPE_F32, "bf16": VSC_DTYPE_BF16, "fp16": VSC_DTYPE_F16}
         self.sizes = [tuple(x) for x in sizes]
-        descs = (StreamDesc * len(sizes))(*[StreamDesc(w, h, flow_downscale, code) for w, h in sizes])
+        n = len(self.sizes)
+        ds = list(flow_downscale) if isinstance(flow_downscale, (list, tuple)) else [flow_downscale] * n
+        dt = list(corr_dtype) if isinstance(corr_dtype, (list, tuple)) else [corr_dtype] * n
+        if len(ds) != n or len(dt) != n:
+            raise ValueError("one flow_downscale and corr_dtype per stream")
+        descs = (StreamDesc * n)(*[StreamDesc(w, h, d, codes[c]) for (w, h), d, c in zip(self.sizes, ds, dt)])
         self._stream_obj = stream if stream is not None else torch.cuda.current_stream()
         h = C.c_void_p()
-        _check(load().vsc_multistream_create(descs, len(sizes), _stream(self._stream_obj), C.byref(h)))
+        _check(load().vsc_multistream_create(descs, n, _stream(self._stream_obj), C.byref(h)))
         self._h = h
+        self._upsamplers = {}
 
     @property
     def hyper_params(self) -> HyperParams:
@@ -662,6 +676,20 @@ class MultiStream:
     @property
     def last_launches(self) -> int:
         return int(load().vsc_multistream_last_launches(self._h))
+
+    @property
+    def fused(self) -> bool:
+        """True when a step with the current hyper-parameters groups the solves."""
+        return bool(load().vsc_multistream_fused(self._h))
+
+    def set_fused(self, on: bool):
+        _check(load().vsc_multistream_set_fused(self._h, 1 if on else 0))
+
+    def set_upsampler(self, upsampler, index: int = -1):
+        """The learned upsampler for stream `index` (-1: every stream with
+        flow_downscale > 1); None: bilinear."""
+        _check(load().vsc_multistream_set_upsampler(self._h, index, upsampler._h if upsampler else None))
+        self._upsamplers[index] = upsampler  # kept alive while the streams use it
 
     def load_frames(self, origs, procs):
         """One RGBA8 (H, W, 4) frame pair per stream: all numpy (host) or all CUDA tensors."""

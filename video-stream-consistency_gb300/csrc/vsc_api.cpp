@@ -1046,7 +1046,17 @@ cudaError_t upsampler_apply_pair(vsc_stabilizer* s, cudaStream_t st, int* nl)
     return e;
 }
 
-cudaError_t enqueue_step(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t* rgba_dev, int* launches)
+// The images of the solve at each pyramid level of a step.
+struct LevelImages {
+    float* P[8];
+    float* A[8];
+    float* W[8];
+    float* O[8];
+};
+
+// A step up to the solves: flows, the fused front pass (warps, adaptive
+// combination, consistency weights) and the pyramid of the solve's inputs.
+cudaError_t enqueue_pre_solve(vsc_stabilizer* s, const vsc_hyper_params& hp, LevelImages* lv, int* launches)
 {
     const int L = hp.pyramid_levels;
     const int s0 = s->head, s1 = (s->head + 1) % 3, s2 = (s->head + 2) % 3;
@@ -1104,10 +1114,10 @@ cudaError_t enqueue_step(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t*
     ++nl;
 
     // pyramid (videostabilizer.cpp:203-217)
-    float* P[8];
-    float* A[8];
-    float* W[8];
-    float* O[8];
+    float** P = lv->P;
+    float** A = lv->A;
+    float** W = lv->W;
+    float** O = lv->O;
     P[0] = s->proc[s1];
     A[0] = s->adap_pr;
     W[0] = s->cons_wt;
@@ -1121,6 +1131,25 @@ cudaError_t enqueue_step(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t*
             s->lh[j], st));
         ++nl;
     }
+    *launches += nl;
+    return e;
+}
+
+cudaError_t enqueue_step(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t* rgba_dev, int* launches)
+{
+    const int L = hp.pyramid_levels;
+    cudaStream_t st = s->st;
+    int nl = 0;
+    LevelImages lv;
+    cudaError_t e = enqueue_pre_solve(s, hp, &lv, &nl);
+    auto run = [&](cudaError_t r) {
+        if (e == cudaSuccess)
+            e = r;
+    };
+    float** P = lv.P;
+    float** A = lv.A;
+    float** W = lv.W;
+    float** O = lv.O;
     // The solution is initialised with the processed frame and carried down
     // with the same bilinear chain, so at the coarsest level it equals P.
     run(cudaMemcpyAsync(O[L - 1], P[L - 1], static_cast<size_t>(s->lw[L - 1]) * s->lh[L - 1] * 3 * sizeof(float),
@@ -1527,6 +1556,12 @@ VSC_API vsc_status vsc_stabilizer_stage_ms(vsc_stabilizer* s, float* ms, int32_t
 // window position as one CUDA graph (all streams advance in lockstep).
 struct vsc_multistream {
     std::vector<vsc_stabilizer*> st;
+    // grouped solves: one persistent-kernel launch per 8 Jacobi steps walks
+    // the tiles of every stream's image at a pyramid level
+    bool fused = true;      // requested (vsc_multistream_set_fused)
+    bool fused_ok = false;  // every stream's level sizes take the TMA path
+    std::vector<float*> lvl_ws;  // per stream: solver workspaces of levels 1 ..
+    int tuned_levels = 0;        // levels whose group tile shape was autotuned
     std::vector<cudaStream_t> side;
     std::vector<cudaEvent_t> loaded, joined;
     cudaEvent_t fork = nullptr, done = nullptr;
@@ -1550,6 +1585,10 @@ namespace {
 
 void ms_free(vsc_multistream* m)
 {
+    for (float* p : m->lvl_ws)
+        if (p)
+            cudaFree(p);
+    m->lvl_ws.clear();
     for (auto& g : m->graphs)
         if (g.exec)
             cudaGraphExecDestroy(g.exec);
@@ -1591,6 +1630,107 @@ cudaError_t ms_enqueue(vsc_multistream* m, const std::vector<uint8_t*>& outs, in
     return e;
 }
 
+// Level j's solver workspace of stream i: the stabilizer's own at level 0,
+// the multistream's per-level ones above (every level's Laplacian is
+// computed before the first grouped solve).
+float* ms_level_ws(vsc_multistream* m, size_t i, int j)
+{
+    vsc_stabilizer* s = m->st[i];
+    if (j == 0)
+        return s->solver_ws;
+    float* p = m->lvl_ws[i];
+    for (int k = 1; k < j; ++k)
+        p += solver_workspace_floats(s->lw[k], s->lh[k]);
+    return p;
+}
+
+// The step with grouped solves: each stream's flows, front pass, pyramid and
+// Laplacians on its own CUDA stream; then, on the multistream's stream, per
+// pyramid level one bilinear launch over all streams and the level's solve
+// as launches of the persistent kernel over every stream's tiles.
+cudaError_t ms_enqueue_fused(vsc_multistream* m, const std::vector<uint8_t*>& outs, int* launches)
+{
+    const vsc_hyper_params& hp = m->hp;
+    const int L = hp.pyramid_levels;
+    const size_t n = m->st.size();
+    std::vector<LevelImages> lv(n);
+    cudaError_t e = cudaEventRecord(m->fork, m->main);
+    int nl = 0;
+    for (size_t i = 0; i < n && e == cudaSuccess; ++i) {
+        vsc_stabilizer* s = m->st[i];
+        if ((e = cudaStreamWaitEvent(m->side[i], m->fork, 0)) != cudaSuccess)
+            break;
+        e = enqueue_pre_solve(s, hp, &lv[i], &nl);
+        for (int j = 0; j < L && e == cudaSuccess; ++j) {
+            e = solver_lap(lv[i].P[j], s->lw[j], s->lh[j], ms_level_ws(m, i, j), s->st);
+            ++nl;
+        }
+        // videostabilizer.cpp:212-217: the coarsest level starts from P
+        const int it = hp.num_iter / L;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(solver_start_buffer(lv[i].O[L - 1], s->lw[L - 1], s->lh[L - 1], it,
+                                    ms_level_ws(m, i, L - 1)),
+                lv[i].P[L - 1], static_cast<size_t>(s->lw[L - 1]) * s->lh[L - 1] * 3 * sizeof(float),
+                cudaMemcpyDeviceToDevice, s->st);
+        if (e == cudaSuccess && (e = cudaEventRecord(m->joined[i], m->side[i])) == cudaSuccess)
+            e = cudaStreamWaitEvent(m->main, m->joined[i], 0);
+    }
+    std::vector<SolverImage> im(n);
+    std::vector<Img> up_in(n), up_out(n);
+    for (int j = L - 1; j >= 0 && e == cudaSuccess; --j) {
+        const int it = hp.num_iter / (j + 1);
+        for (size_t i = 0; i < n; ++i) {
+            vsc_stabilizer* s = m->st[i];
+            float* ws = ms_level_ws(m, i, j);
+            im[i] = SolverImage{lv[i].P[j], lv[i].A[j], lv[i].W[j], lv[i].O[j], s->lw[j], s->lh[j], ws,
+                j == 0 ? outs[i] : nullptr};
+            if (j != L - 1) {
+                up_in[i] = Img{lv[i].O[j + 1], s->lw[j + 1], s->lh[j + 1], 3};
+                up_out[i] = Img{solver_start_buffer(lv[i].O[j], s->lw[j], s->lh[j], it, ws), s->lw[j], s->lh[j], 3};
+            }
+        }
+        if (j != L - 1) {
+            e = launch_bilinear_group(up_in.data(), up_out.data(), static_cast<int>(n), m->main);
+            nl += static_cast<int>((n + 15) / 16);
+        }
+        if (e == cudaSuccess)
+            e = run_solver_group(im.data(), static_cast<int>(n), it, hp.step_size, hp.mom_fac, m->main, &nl);
+    }
+    *launches = nl;
+    return e;
+}
+
+// the grouped form when requested and possible for the current
+// hyper-parameters: every level width a multiple of 4 (the TMA path)
+bool ms_use_fused(vsc_multistream* m)
+{
+    if (!m->fused || !m->fused_ok)
+        return false;
+    for (vsc_stabilizer* s : m->st) {
+        if (m->hp.pyramid_levels > s->levels_alloc)
+            return false;
+        for (int j = 0; j < m->hp.pyramid_levels; ++j)
+            if (s->lw[j] % 4 != 0)
+                return false;
+    }
+    return true;
+}
+
+void ms_drop_graphs(vsc_multistream* m)
+{
+    for (auto& g : m->graphs) {
+        if (g.exec)
+            cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+        g.valid = false;
+    }
+}
+
+cudaError_t ms_step_enqueue(vsc_multistream* m, const std::vector<uint8_t*>& outs, int* launches)
+{
+    return ms_use_fused(m) ? ms_enqueue_fused(m, outs, launches) : ms_enqueue(m, outs, launches);
+}
+
 bool ms_launch_graph(vsc_multistream* m, const std::vector<uint8_t*>& outs, int* launches, cudaError_t* err)
 {
     *err = cudaSuccess;
@@ -1615,7 +1755,7 @@ bool ms_launch_graph(vsc_multistream* m, const std::vector<uint8_t*>& outs, int*
             return false;
         }
         int nl = 0;
-        const cudaError_t ee = ms_enqueue(m, outs, &nl);
+        const cudaError_t ee = ms_step_enqueue(m, outs, &nl);
         const cudaError_t ec = cudaStreamEndCapture(m->main, &graph);
         if (ee != cudaSuccess || ec != cudaSuccess || !graph) {
             if (graph)
@@ -1698,6 +1838,41 @@ VSC_API vsc_status vsc_multistream_create(const vsc_stream_desc* desc, int32_t n
     }
     if (!s && e != cudaSuccess)
         s = check_cuda(e, "multistream_create");
+    // grouped solves: per-level workspaces above level 0, and the tile shape
+    // of each level's group (a stream being captured keeps the wave model)
+    m->fused_ok = !s;
+    for (size_t i = 0; i < m->st.size() && !s; ++i) {
+        vsc_stabilizer* st = m->st[i];
+        size_t floats = 0;
+        for (int j = 1; j < st->levels_alloc; ++j)
+            floats += solver_workspace_floats(st->lw[j], st->lh[j]);
+        float* p = nullptr;
+        if (floats && (s = check_cuda(dalloc(&p, floats), "multistream_create level workspaces")))
+            break;
+        m->lvl_ws.push_back(p);
+    }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (!s && cudaStreamIsCapturing(m->main, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone) {
+        int levels = 4;
+        for (vsc_stabilizer* st : m->st)
+            levels = std::min(levels, st->levels_alloc);
+        std::vector<int> ws(m->st.size()), hs(m->st.size());
+        for (int j = 0; j < levels; ++j) {
+            bool eligible = true;
+            for (size_t i = 0; i < m->st.size(); ++i) {
+                ws[i] = m->st[i]->lw[j];
+                hs[i] = m->st[i]->lh[j];
+                eligible = eligible && ws[i] % 4 == 0;
+            }
+            if (!eligible)
+                break;
+            if (solver_group_autotune(ws.data(), hs.data(), static_cast<int>(ws.size()), m->main, nullptr) !=
+                cudaSuccess) {
+                cudaGetLastError();  // a failed measurement leaves the model's choice
+                break;
+            }
+        }
+    }
     if (s) {
         const std::string msg = vsc_last_error();
         ms_free(m);
@@ -1723,6 +1898,47 @@ VSC_API vsc_status vsc_multistream_destroy(vsc_multistream* m)
 VSC_API vsc_hyper_params* vsc_multistream_hyper_params(vsc_multistream* m) { return m ? &m->hp : nullptr; }
 
 VSC_API int32_t vsc_multistream_last_launches(vsc_multistream* m) { return m ? m->last_launches : 0; }
+
+VSC_API vsc_status vsc_multistream_set_fused(vsc_multistream* m, int32_t on)
+{
+    clear_error();
+    if (!m)
+        return set_error(VSC_EINVAL, "multistream_set_fused: null argument");
+    DeviceGuard g(m->device);
+    if (m->fused != (on != 0)) {
+        cudaStreamSynchronize(m->main);  // a graph being replayed is not destroyed under it
+        ms_drop_graphs(m);
+    }
+    m->fused = on != 0;
+    return VSC_OK;
+}
+
+VSC_API int32_t vsc_multistream_fused(vsc_multistream* m) { return m && ms_use_fused(m) ? 1 : 0; }
+
+VSC_API vsc_status vsc_multistream_set_upsampler(vsc_multistream* m, int32_t index, vsc_upsampler* u)
+{
+    clear_error();
+    if (!m)
+        return set_error(VSC_EINVAL, "multistream_set_upsampler: null argument");
+    if (index < -1 || index >= static_cast<int32_t>(m->st.size()))
+        return set_error(VSC_EINVAL, "multistream_set_upsampler: stream %d outside [-1, %zu)", index, m->st.size());
+    DeviceGuard g(m->device);
+    vsc_status s = check_cuda(cudaStreamSynchronize(m->main), "multistream_set_upsampler");
+    if (s)
+        return s;
+    // the FP16 weights are packed here, once, not inside a captured step
+    if (u && (s = check_cuda(upsampler_sync_weights(u, m->main), "multistream_set_upsampler weights")))
+        return s;
+    if ((s = check_cuda(cudaStreamSynchronize(m->main), "multistream_set_upsampler")))
+        return s;
+    for (size_t i = 0; i < m->st.size() && !s; ++i) {
+        vsc_stabilizer* st = m->st[i];
+        if (index >= 0 ? static_cast<int32_t>(i) == index : (st->compute_flow && st->downscale > 1))
+            s = vsc_stabilizer_set_upsampler(st, u);
+    }
+    ms_drop_graphs(m);
+    return s;
+}
 
 VSC_API vsc_status vsc_multistream_load_frames(vsc_multistream* m, const uint8_t* const* orig,
     const uint8_t* const* proc, int32_t on_device)
@@ -1769,7 +1985,7 @@ VSC_API vsc_status vsc_multistream_step(vsc_multistream* m, uint8_t* const* out,
     for (vsc_stabilizer* st : m->st)
         started = started && st->started;
     if (!(started && ms_launch_graph(m, outs, &nl, &e)))
-        e = ms_enqueue(m, outs, &nl);
+        e = ms_step_enqueue(m, outs, &nl);
     if ((s = check_cuda(e, "multistream_step")))
         return s;
     for (vsc_stabilizer* st : m->st)

@@ -108,6 +108,8 @@ cudaError_t launch_adap_comb(Img ci, Img cp, Img pwi, Img pwp, Img nwi, Img nwp,
 cudaError_t launch_flow_consistency(Img ffwd, Img fbwd, Img mask, cudaStream_t st);
 cudaError_t launch_consist_wt(Img ai, Img ci, Img wt, float beta, float gamma, cudaStream_t st);
 cudaError_t launch_bilinear(Img in, Img out, cudaStream_t st);
+// launch_bilinear for n 3-channel images in one launch per 16 (same bits)
+cudaError_t launch_bilinear_group(const Img* in, const Img* out, int n, cudaStream_t st);
 // Nearest-neighbour resize of a float HWC3 image for the FLOWDOWNSCALE mode
 // (the reference scales the QImage with Qt::FastTransformation,
 // flowmodel.cpp:126-133): source = min(iw-1, ((2x+1)*iw) / (2*ow)).
@@ -125,10 +127,36 @@ int solver_steps_per_launch();  // Jacobi steps one solver launch performs (temp
 cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out);
 int solver_tile_rows(int w, int h, bool* tuned);
 void solver_set_autotune(bool on);
+// The same for the sizes one grouped launch solves together (one image per
+// stream of a multi-stream step), keyed by the whole list.
+cudaError_t solver_group_autotune(const int* w, const int* h, int n, cudaStream_t st, int* rows_out);
+int solver_group_tile_rows(const int* w, const int* h, int n, bool* tuned);
 // Runs num_iter iterations; O holds the initial solution and receives the
 // result.  Returns the number of kernels launched through *launches.
 cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,
     float step, float mom, float* workspace, cudaStream_t st, int* launches, uint8_t* rgba_out = nullptr);
+
+// Grouped solve: n images of any sizes, the same iterations, each launch of
+// the persistent kernel walking the tiles of all of them (up to 16 images
+// per launch).  Per image, before run_solver_group on the same stream:
+// solver_lap(P) into its workspace, and the initial solution written to
+// solver_start_buffer(O, ...) (O itself or the workspace's second buffer,
+// whichever makes the last launch write O).  Needs solver_group_eligible
+// (width % 4 == 0 and 16-byte aligned images, the TMA path).
+struct SolverImage {
+    const float* P;
+    const float* A;
+    const float* Wt;
+    float* O;
+    int w, h;
+    float* workspace;  // solver_workspace_floats(w, h)
+    uint8_t* rgba;     // RGBA8 copy of the result, or null
+};
+float* solver_start_buffer(float* O, int w, int h, int num_iter, float* workspace);
+cudaError_t solver_lap(const float* P, int w, int h, float* workspace, cudaStream_t st);
+bool solver_group_eligible(const SolverImage* im, int n);
+cudaError_t run_solver_group(const SolverImage* im, int n, int num_iter, float step, float mom, cudaStream_t st,
+    int* launches);
 
 // Device-side bounded waits record a timeout in a device flag instead of
 // hanging; this reads and clears it for the current device.

@@ -2,7 +2,8 @@
 // and get_consist_out, src/stabilization/flowconsistency.cu:193-258, :350-374).
 //
 // Differences from the reference's schedule (results are the CPU
-// restatement's, bit for bit):
+// restatement's, bit for bit except that a zero may carry the other sign,
+// see jacobi_px):
 //   - Jacobi iteration: the reference updates consisOut in place
 //     (flowconsistency.cu:370), so neighbours read a timing-dependent mix of
 //     old and new values; here every pixel reads the previous iterate;
@@ -19,6 +20,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <vector>
 
 namespace vsc {
 namespace {
@@ -88,14 +90,19 @@ template <bool kAll>
 __device__ __forceinline__ float jacobi_px(float o, float& u, float a, float wt, float lp, float right, float left,
     float down, float up, bool vr, bool vl, bool vd, bool vu, float cnt, float step, float mom, bool mom_on)
 {
-    float lap = 0.0f;
+    // The reference sums the neighbours onto 0.0f; starting from the first
+    // term drops one addition per pixel and channel.  0 + x equals x except
+    // for x = -0 (0 + -0 = +0), so the two sums differ at most in the sign of
+    // a zero, and no later operation of the pass (sums, products, squares,
+    // fabs, comparisons) turns a zero's sign into a different non-zero value
+    // or output byte.
+    float lap;
     if (kAll) {
-        lap += right;
-        lap += left;
+        lap = right + left;
         lap += down;
         lap += up;
     } else {
-        lap += vr ? right : 0.0f;
+        lap = vr ? right : 0.0f;
         lap += vl ? left : 0.0f;
         lap += vd ? down : 0.0f;
         lap += vu ? up : 0.0f;
@@ -372,25 +379,91 @@ __device__ __forceinline__ void store_interior(const CUtensorMap* mOo, const CUt
     bulk_commit();
 }
 
-__device__ __forceinline__ void issue_tile(float* stage, const CUtensorMap* m0, const CUtensorMap* m1,
-    const CUtensorMap* m2, const CUtensorMap* m3, const CUtensorMap* m4, int tile, int tiles_x, uint64_t* bar)
+// The images of one solve, in the order of a problem's tensor maps: the five
+// loaded per tile (O, U, A, consWt, lap P; tile box) and the two stored
+// (O, U; interior box).
+enum { kMapO, kMapU, kMapA, kMapW, kMapL, kMapOo, kMapUo, kMaps };
+
+// The problems of one launch of a persistent solver kernel: kN images of any
+// sizes (one per video stream at one pyramid level), each with its tensor
+// maps, its size and its first tile in the launch's tile list.  Every problem
+// runs the same iterations (T, k0, step, mom).  Passed by value as a
+// __grid_constant__ parameter, so the maps stay in parameter memory, where
+// TMA reads them.
+template <int kN>
+struct SolverGroup {
+    CUtensorMap map[kN][kMaps];
+    int w[kN], h[kN], tiles_x[kN];
+    int tile0[kN + 1];  // first tile of problem p; tile0[count] = tiles in all
+    uint8_t* rgba[kN];  // RGBA8 output of the last launch, or null
+    int count;
+};
+constexpr int kGroupMax = 16;
+
+struct TileLoc {
+    int p;       // problem
+    int ox, oy;  // tile origin (ring included)
+    int w, h;
+};
+
+// tile -> problem by a scan of the first-tile table (kN <= kGroupMax)
+template <int kN, int kRows>
+__device__ __forceinline__ TileLoc locate(const SolverGroup<kN>& g, int tile)
 {
-    const int ox = (tile % tiles_x) * kIW - kTbT;
-    const int oy = (tile / tiles_x) * kIH - kTbT;
-    mbar_expect_tx(bar, 5 * kStageBytes);
-    tma_load_2d(stage + 0 * kStageFloats, m0, 3 * ox, oy, bar);
-    tma_load_2d(stage + 1 * kStageFloats, m1, 3 * ox, oy, bar);
-    tma_load_2d(stage + 2 * kStageFloats, m2, 3 * ox, oy, bar);
-    tma_load_2d(stage + 3 * kStageFloats, m3, 3 * ox, oy, bar);
-    tma_load_2d(stage + 4 * kStageFloats, m4, 3 * ox, oy, bar);
+    int p = 0;
+    if (kN > 1) {
+#pragma unroll 1
+        while (p + 1 < g.count && tile >= g.tile0[p + 1])
+            ++p;
+    }
+    const int t = tile - g.tile0[p];
+    TileLoc l;
+    l.p = p;
+    l.ox = (t % g.tiles_x[p]) * kIW - kTbT;
+    l.oy = (t / g.tiles_x[p]) * kRows - kTbT;
+    l.w = g.w[p];
+    l.h = g.h[p];
+    return l;
 }
 
+// input tiles first .. last - 1 (map order) of a tile at (ox, oy), into consecutive stages
+__device__ __forceinline__ void issue_tile_loads(float* stage, const CUtensorMap* m, int ox, int oy, int stage_floats,
+    int first, int last, uint64_t* bar)
+{
+    for (int i = first; i < last; ++i)
+        tma_load_2d(stage + i * stage_floats, m + i, 3 * ox, oy, bar);
+}
+
+// the five input tiles of a tile at (ox, oy), `bytes` each, into consecutive stages
+__device__ __forceinline__ void issue_loads(float* stage, const CUtensorMap* m, int ox, int oy, int stage_floats,
+    uint32_t bytes, uint64_t* bar)
+{
+    mbar_expect_tx(bar, 5 * bytes);
+    issue_tile_loads(stage, m, ox, oy, stage_floats, kMapO, kMapL + 1, bar);
+}
+
+// The first tile of a launch.  A, consWt and lap P are not written by solver
+// launches, so a launch after the first of a solve (k0 > 0: its predecessor
+// is the previous solver launch, which itself waited for the kernels that
+// wrote them) fetches them before waiting for the predecessor to complete;
+// O and U, which the predecessor writes, after.
+__device__ __forceinline__ void issue_first_loads(float* stage, const CUtensorMap* m, int ox, int oy,
+    int stage_floats, uint32_t bytes, uint64_t* bar, bool early)
+{
+    if (early) {
+        mbar_expect_tx(bar, 5 * bytes);
+        issue_tile_loads(stage, m, ox, oy, stage_floats, kMapA, kMapL + 1, bar);
+    }
+    grid_dependency_wait();
+    if (early)
+        issue_tile_loads(stage, m, ox, oy, stage_floats, kMapO, kMapU + 1, bar);
+    else
+        issue_loads(stage, m, ox, oy, stage_floats, bytes, bar);
+}
+
+template <int kN>
 __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
-    solver_persistent_kernel(const __grid_constant__ CUtensorMap mO, const __grid_constant__ CUtensorMap mU,
-        const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mW,
-        const __grid_constant__ CUtensorMap mL, const __grid_constant__ CUtensorMap mOo,
-        const __grid_constant__ CUtensorMap mUo, int w, int h, int T, int k0, float step, float mom,
-        uint8_t* __restrict__ rgba, int tiles_x, int ntiles)
+    solver_persistent_kernel(const __grid_constant__ SolverGroup<kN> g, int T, int k0, float step, float mom)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* stage = reinterpret_cast<float*>(smem_raw);
@@ -405,16 +478,19 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
     if (tid == 0)
         mbar_init(bar, 1);
     __syncthreads();
+    const int ntiles = g.tile0[g.count];
     int tile = blockIdx.x;
+    if (tid == 0 && tile < ntiles) {
+        const TileLoc n = locate<kN, kIH>(g, tile);
+        issue_first_loads(stage, g.map[n.p], n.ox, n.oy, kStageFloats, kStageBytes, bar, k0 > 0);
+    }
     grid_dependency_wait();
-    if (tid == 0 && tile < ntiles)
-        issue_tile(stage, &mO, &mU, &mA, &mW, &mL, tile, tiles_x, bar);
     uint32_t parity = 0;
     for (; tile < ntiles; tile += gridDim.x) {
         if (tile + static_cast<int>(gridDim.x) >= ntiles)
             allow_dependent_launch();
-        const int ox = (tile % tiles_x) * kIW - kTbT;
-        const int oy = (tile / tiles_x) * kIH - kTbT;
+        const TileLoc c = locate<kN, kIH>(g, tile);
+        const int ox = c.ox, oy = c.oy, w = c.w, h = c.h;
         if (!mbar_wait_bounded(bar, parity, kWaitSpins)) {
             if (tid == 0) {
                 atomicExch(&g_device_timeout, 1);
@@ -473,7 +549,8 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
         __syncthreads();  // staging consumed, O published
         if (tid == 0 && tile + static_cast<int>(gridDim.x) < ntiles) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue_tile(stage, &mO, &mU, &mA, &mW, &mL, tile + gridDim.x, tiles_x, bar);
+            const TileLoc n = locate<kN, kIH>(g, tile + gridDim.x);
+            issue_loads(stage, g.map[n.p], n.ox, n.oy, kStageFloats, kStageBytes, bar);
         }
 
         const bool interior = ox >= 1 && oy >= 1 && ox + kTbEX - 1 <= w - 3 && oy + kTbEY - 1 <= h - 3;
@@ -510,8 +587,8 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (tid == 0)
-            store_interior(&mOo, &mUo, ox, oy, so, su);
-        if (rgba) {
+            store_interior(g.map[c.p] + kMapOo, g.map[c.p] + kMapUo, ox, oy, so, su);
+        if (uint8_t* rgba = g.rgba[c.p]) {
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int px = px0 + (q & 1), py = py0 + (q >> 1);
@@ -640,25 +717,9 @@ __device__ __forceinline__ void p8_iterate(P8State& s, float* obuf, int T, int k
     }
 }
 
-__device__ __forceinline__ void issue_tall_tile(float* stage, const CUtensorMap* m0, const CUtensorMap* m1,
-    const CUtensorMap* m2, const CUtensorMap* m3, const CUtensorMap* m4, int tile, int tiles_x, uint64_t* bar)
-{
-    const int ox = (tile % tiles_x) * kIW - kTbT;
-    const int oy = (tile / tiles_x) * kPIH - kTbT;
-    mbar_expect_tx(bar, 5 * kPStageBytes);
-    tma_load_2d(stage + 0 * kPStageFloats, m0, 3 * ox, oy, bar);
-    tma_load_2d(stage + 1 * kPStageFloats, m1, 3 * ox, oy, bar);
-    tma_load_2d(stage + 2 * kPStageFloats, m2, 3 * ox, oy, bar);
-    tma_load_2d(stage + 3 * kPStageFloats, m3, 3 * ox, oy, bar);
-    tma_load_2d(stage + 4 * kPStageFloats, m4, 3 * ox, oy, bar);
-}
-
+template <int kN>
 __global__ void __launch_bounds__(kPThreads, 1)
-    solver_tall_kernel(const __grid_constant__ CUtensorMap mO, const __grid_constant__ CUtensorMap mU,
-        const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mW,
-        const __grid_constant__ CUtensorMap mL, const __grid_constant__ CUtensorMap mOo,
-        const __grid_constant__ CUtensorMap mUo, int w, int h, int T, int k0, float step, float mom,
-        uint8_t* __restrict__ rgba, int tiles_x, int ntiles)
+    solver_tall_kernel(const __grid_constant__ SolverGroup<kN> g, int T, int k0, float step, float mom)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* stage = reinterpret_cast<float*>(smem_raw);
@@ -672,16 +733,19 @@ __global__ void __launch_bounds__(kPThreads, 1)
     if (threadIdx.x == 0)
         mbar_init(bar, 1);
     __syncthreads();
+    const int ntiles = g.tile0[g.count];
     int tile = blockIdx.x;
+    if (threadIdx.x == 0 && tile < ntiles) {
+        const TileLoc n = locate<kN, kPIH>(g, tile);
+        issue_first_loads(stage, g.map[n.p], n.ox, n.oy, kPStageFloats, kPStageBytes, bar, k0 > 0);
+    }
     grid_dependency_wait();
-    if (threadIdx.x == 0 && tile < ntiles)
-        issue_tall_tile(stage, &mO, &mU, &mA, &mW, &mL, tile, tiles_x, bar);
     uint32_t parity = 0;
     for (; tile < ntiles; tile += gridDim.x) {
         if (tile + static_cast<int>(gridDim.x) >= ntiles)
             allow_dependent_launch();
-        const int ox = (tile % tiles_x) * kIW - kTbT;
-        const int oy = (tile / tiles_x) * kPIH - kTbT;
+        const TileLoc c = locate<kN, kPIH>(g, tile);
+        const int ox = c.ox, oy = c.oy, w = c.w, h = c.h;
         if (!mbar_wait_bounded(bar, parity, kWaitSpins)) {
             if (threadIdx.x == 0) {
                 atomicExch(&g_device_timeout, 1);
@@ -725,7 +789,8 @@ __global__ void __launch_bounds__(kPThreads, 1)
         __syncthreads();  // staging consumed, edge rows published
         if (threadIdx.x == 0 && tile + static_cast<int>(gridDim.x) < ntiles) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue_tall_tile(stage, &mO, &mU, &mA, &mW, &mL, tile + gridDim.x, tiles_x, bar);
+            const TileLoc n = locate<kN, kPIH>(g, tile + gridDim.x);
+            issue_loads(stage, g.map[n.p], n.ox, n.oy, kPStageFloats, kPStageBytes, bar);
         }
 
         const int gx0 = ox + px0, gy0 = oy + py0;
@@ -764,8 +829,8 @@ __global__ void __launch_bounds__(kPThreads, 1)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (threadIdx.x == 0)
-            store_interior(&mOo, &mUo, ox, oy, so, su);
-        if (rgba) {
+            store_interior(g.map[c.p] + kMapOo, g.map[c.p] + kMapUo, ox, oy, so, su);
+        if (uint8_t* rgba = g.rgba[c.p]) {
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
                 const int px = px0 + (q & 1), py = py0 + (q >> 1);
@@ -773,7 +838,8 @@ __global__ void __launch_bounds__(kPThreads, 1)
                 if (gx < 0 || gx >= w || gy < 0 || gy >= h || px < kTbT || px >= kTbEX - kTbT || py < kTbT ||
                     py >= kPEY - kTbT)
                     continue;
-                reinterpret_cast<uint32_t*>(rgba)[pix_index(gx, gy, w)] = pack_rgba(s.o[q][0], s.o[q][1], s.o[q][2]);
+                reinterpret_cast<uint32_t*>(rgba)[pix_index(gx, gy, w)] =
+                    pack_rgba(s.o[q][0], s.o[q][1], s.o[q][2]);
             }
         }
         // the TMA stores read the staging while the next tile's copies land; the
@@ -829,6 +895,15 @@ bool encode_image_map(CUtensorMap* m, const float* base, int w, int h, int box_r
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+template <int kN>
+bool set_group_smem()
+{
+    return cudaFuncSetAttribute(solver_persistent_kernel<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+               kPsSmem) == cudaSuccess &&
+           cudaFuncSetAttribute(solver_tall_kernel<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmem) ==
+               cudaSuccess;
+}
+
 struct DeviceInfo {
     int sms = 0;
     bool tb_smem = false, ps_smem = false;
@@ -855,10 +930,7 @@ cudaError_t device_info(DeviceInfo** out)
         if ((e = cudaFuncSetAttribute(solver_tb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTbSmem)) !=
             cudaSuccess)
             return e;
-        d.ps_smem = cudaFuncSetAttribute(solver_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                        kPsSmem) == cudaSuccess &&
-                    cudaFuncSetAttribute(solver_tall_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmem) ==
-                        cudaSuccess;
+        d.ps_smem = set_group_smem<1>() && set_group_smem<4>() && set_group_smem<kGroupMax>();
         cudaGetLastError();
     }
     *out = &d;
@@ -869,14 +941,15 @@ bool aligned16p(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) ==
 
 // ---- tile-shape autotuner ------------------------------------------------------------
 // The two persistent kernels (64 x 32 and 64 x 48 tiles) give the same results
-// bit for bit; which is faster at a size depends on how their tiles fill the
-// waves of one tile per SM.  solver_autotune times both on scratch images of
-// the size and keeps the faster per (device, width, height); sizes never
+// bit for bit; which is faster depends on how their tiles fill the waves of
+// one tile per SM.  solver_group_autotune times both on scratch images of the
+// sizes one launch solves (one image, or one image per stream of a
+// multi-stream step) and keeps the faster per (device, sizes); sizes never
 // tuned use the wave model: a 64 x 48 tile costs about 1.91 times a 64 x 32
 // one (GB300, 1920x1080 and 960x540).
 struct ShapeTable {
     std::mutex mu;
-    std::map<std::tuple<int, int, int>, int> rows;  // (device, w, h) -> kPEY or kTbEY
+    std::map<std::vector<int>, int> rows;  // {device, w0, h0, w1, h1, ...} -> kPEY or kTbEY
     bool enabled = true;
 };
 ShapeTable& shape_table()
@@ -885,31 +958,88 @@ ShapeTable& shape_table()
     return t;
 }
 
-int model_rows(int w, int h, int sms)
+std::vector<int> shape_key(int dev, const int* w, const int* h, int n)
 {
-    const int tiles_x = (w + kIW - 1) / kIW;
-    const int n_short = tiles_x * ((h + kIH - 1) / kIH), n_tall = tiles_x * ((h + kPIH - 1) / kPIH);
+    std::vector<int> k(1, dev);
+    for (int i = 0; i < n; ++i) {
+        k.push_back(w[i]);
+        k.push_back(h[i]);
+    }
+    return k;
+}
+
+int tiles_of(int w, int h, int ir) { return ((w + kIW - 1) / kIW) * ((h + ir - 1) / ir); }
+
+int model_rows(const int* w, const int* h, int n, int sms)
+{
+    int64_t n_short = 0, n_tall = 0;
+    for (int i = 0; i < n; ++i) {
+        n_short += tiles_of(w[i], h[i], kIH);
+        n_tall += tiles_of(w[i], h[i], kPIH);
+    }
     return 1.91 * ((n_tall + sms - 1) / sms) < 1.0 * ((n_short + sms - 1) / sms) ? kPEY : kTbEY;
 }
 
-// the tile rows a solve at (w, h) on the current device uses: tuned, else the model
-int chosen_rows(int dev, int w, int h, int sms)
+// the tile rows a launch over these sizes uses on the current device: tuned, else the model
+int chosen_rows(int dev, const int* w, const int* h, int n, int sms, bool* tuned = nullptr)
 {
     ShapeTable& t = shape_table();
     std::lock_guard<std::mutex> lock(t.mu);
-    auto it = t.rows.find(std::make_tuple(dev, w, h));
-    return it != t.rows.end() ? it->second : model_rows(w, h, sms);
+    auto it = t.rows.find(shape_key(dev, w, h, n));
+    if (tuned)
+        *tuned = it != t.rows.end();
+    return it != t.rows.end() ? it->second : model_rows(w, h, n, sms);
 }
 
-// One launch of the persistent kernel with `rows`-row tiles; mOo / mUo are the
-// output images' maps with the interior box (interior_rows(rows) rows).
 int interior_rows(int rows) { return rows == kPEY ? kPIH : kIH; }
 
-void launch_persistent(int rows, const CUtensorMap& mO, const CUtensorMap& mU, const CUtensorMap& mA,
-    const CUtensorMap& mW, const CUtensorMap& mL, const CUtensorMap& mOo, const CUtensorMap& mUo, int w, int h,
-    int T, int k0, float step, float mom, uint8_t* rgba, int sms, cudaStream_t st)
+// The tensor maps of one image's solve for both ping-pong phases: O[c] / U[c]
+// with the tile box (loads), Oo[c] / Uo[c] with the interior box (stores).
+struct SolveMaps {
+    CUtensorMap O[2], U[2], A, W, L, Oo[2], Uo[2];
+};
+
+bool encode_solve(SolveMaps* m, float* const O[2], float* const U[2], const float* A, const float* Wt,
+    const float* L, int w, int h, int rows)
 {
-    const int tiles_x = (w + kIW - 1) / kIW;
+    const int ir = interior_rows(rows);
+    bool ok = encode_image_map(&m->A, A, w, h, rows) && encode_image_map(&m->W, Wt, w, h, rows) &&
+              encode_image_map(&m->L, L, w, h, rows);
+    for (int c = 0; c < 2 && ok; ++c)
+        ok = encode_image_map(&m->O[c], O[c], w, h, rows) && encode_image_map(&m->U[c], U[c], w, h, rows) &&
+             encode_image_map(&m->Oo[c], O[c], w, h, ir, 3 * kIW) &&
+             encode_image_map(&m->Uo[c], U[c], w, h, ir, 3 * kIW);
+    return ok;
+}
+
+// problem p of a launch: launch li of the solve reads O[c] and U[li & 1] and
+// writes O[c ^ 1] and U[(li + 1) & 1]
+template <int kN>
+void group_set(SolverGroup<kN>& g, int p, const SolveMaps& m, int c, int li, int w, int h, int rows, uint8_t* rgba)
+{
+    g.map[p][kMapO] = m.O[c];
+    g.map[p][kMapU] = m.U[li & 1];
+    g.map[p][kMapA] = m.A;
+    g.map[p][kMapW] = m.W;
+    g.map[p][kMapL] = m.L;
+    g.map[p][kMapOo] = m.Oo[c ^ 1];
+    g.map[p][kMapUo] = m.Uo[(li + 1) & 1];
+    g.w[p] = w;
+    g.h[p] = h;
+    g.tiles_x[p] = (w + kIW - 1) / kIW;
+    g.rgba[p] = rgba;
+    if (p == 0)
+        g.tile0[0] = 0;
+    g.tile0[p + 1] = g.tile0[p] + tiles_of(w, h, interior_rows(rows));
+    g.count = p + 1;
+}
+
+// One launch of a persistent kernel (`rows`-row tiles) over a group's tiles,
+// with programmatic dependent launch on the previous launch of the stream.
+template <int kN>
+cudaError_t launch_group(int rows, const SolverGroup<kN>& g, int T, int k0, float step, float mom, int sms,
+    cudaStream_t st)
+{
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -917,21 +1047,48 @@ void launch_persistent(int rows, const CUtensorMap& mO, const CUtensorMap& mU, c
     cfg.stream = st;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    cfg.gridDim = dim3(std::min(g.tile0[g.count], sms));
     if (rows == kPEY) {
-        const int ntiles = tiles_x * ((h + kPIH - 1) / kPIH);
-        cfg.gridDim = dim3(std::min(ntiles, sms));
         cfg.blockDim = dim3(kPThreads);
         cfg.dynamicSmemBytes = kPSmem;
-        cudaLaunchKernelEx(&cfg, solver_tall_kernel, mO, mU, mA, mW, mL, mOo, mUo, w, h, T, k0, step, mom, rgba,
-            tiles_x, ntiles);
-    } else {
-        const int ntiles = tiles_x * ((h + kIH - 1) / kIH);
-        cfg.gridDim = dim3(std::min(ntiles, sms));
-        cfg.blockDim = dim3(32, kTbEY / 2);
-        cfg.dynamicSmemBytes = kPsSmem;
-        cudaLaunchKernelEx(&cfg, solver_persistent_kernel, mO, mU, mA, mW, mL, mOo, mUo, w, h, T, k0, step, mom, rgba,
-            tiles_x, ntiles);
+        return cudaLaunchKernelEx(&cfg, solver_tall_kernel<kN>, g, T, k0, step, mom);
     }
+    cfg.blockDim = dim3(32, kTbEY / 2);
+    cfg.dynamicSmemBytes = kPsSmem;
+    return cudaLaunchKernelEx(&cfg, solver_persistent_kernel<kN>, g, T, k0, step, mom);
+}
+
+// One image of a grouped solve: its maps and where its iterate starts.
+struct GroupMember {
+    SolveMaps maps;
+    int w, h, c0;  // c0: the ping-pong buffer the first launch reads
+    uint8_t* rgba;
+};
+
+// Steps k_first .. num_iter - 1 of a solve over all members, in launches of
+// T <= kTbT steps, kN problems per launch.
+template <int kN>
+cudaError_t launch_members(const std::vector<GroupMember>& mem, int rows, int num_iter, float step, float mom,
+    int sms, cudaStream_t st, int* nl, int k_first = 0)
+{
+    const int nlaunch = (num_iter - k_first + kTbT - 1) / kTbT;
+    SolverGroup<kN> g{};
+    cudaError_t e = cudaSuccess;
+    int k0 = k_first;
+    for (int li = 0; li < nlaunch && e == cudaSuccess; ++li) {
+        const int T = std::min(kTbT, num_iter - k0);
+        for (size_t b = 0; b < mem.size() && e == cudaSuccess; b += kN) {
+            const int cnt = static_cast<int>(std::min(mem.size() - b, static_cast<size_t>(kN)));
+            for (int p = 0; p < cnt; ++p) {
+                const GroupMember& m = mem[b + p];
+                group_set(g, p, m.maps, m.c0 ^ (li & 1), li, m.w, m.h, rows, li == nlaunch - 1 ? m.rgba : nullptr);
+            }
+            e = launch_group(rows, g, T, k0, step, mom, sms, st);
+            ++*nl;
+        }
+        k0 += T;
+    }
+    return e;
 }
 
 }  // namespace
@@ -945,21 +1102,18 @@ void solver_set_autotune(bool on)
         t.rows.clear();
 }
 
-int solver_tile_rows(int w, int h, bool* tuned)
+int solver_group_tile_rows(const int* w, const int* h, int n, bool* tuned)
 {
     int dev = 0;
     DeviceInfo* di = nullptr;
-    if (cudaGetDevice(&dev) != cudaSuccess || device_info(&di) != cudaSuccess)
+    if (n < 1 || cudaGetDevice(&dev) != cudaSuccess || device_info(&di) != cudaSuccess)
         return 0;
-    ShapeTable& t = shape_table();
-    std::lock_guard<std::mutex> lock(t.mu);
-    auto it = t.rows.find(std::make_tuple(dev, w, h));
-    if (tuned)
-        *tuned = it != t.rows.end();
-    return it != t.rows.end() ? it->second : model_rows(w, h, di->sms);
+    return chosen_rows(dev, w, h, n, di->sms, tuned);
 }
 
-cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out)
+int solver_tile_rows(int w, int h, bool* tuned) { return solver_group_tile_rows(&w, &h, 1, tuned); }
+
+cudaError_t solver_group_autotune(const int* w, const int* h, int n, cudaStream_t st, int* rows_out)
 {
     DeviceInfo* di = nullptr;
     int dev = 0;
@@ -968,25 +1122,30 @@ cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out)
         e = device_info(&di);
     if (e != cudaSuccess)
         return e;
+    if (n < 1)
+        return cudaErrorInvalidValue;
+    bool eligible = di->ps_smem;
+    size_t total = 0;  // floats of one image per member, 16-byte multiples
+    for (int i = 0; i < n; ++i) {
+        eligible = eligible && (w[i] % 4) == 0 && w[i] >= 1 && h[i] >= 1;
+        total += static_cast<size_t>(w[i]) * h[i] * 3;
+    }
     ShapeTable& t = shape_table();
+    const std::vector<int> key = shape_key(dev, w, h, n);
     {
         std::lock_guard<std::mutex> lock(t.mu);
-        auto it = t.rows.find(std::make_tuple(dev, w, h));
-        if (it != t.rows.end() || !t.enabled || !di->ps_smem || (w % 4) != 0 || w < 1 || h < 1) {
+        auto it = t.rows.find(key);
+        if (it != t.rows.end() || !t.enabled || !eligible) {
             if (rows_out)
-                *rows_out = it != t.rows.end() ? it->second : model_rows(w, h, di->sms);
+                *rows_out = it != t.rows.end() ? it->second : model_rows(w, h, n, di->sms);
             return cudaSuccess;
         }
     }
     // scratch images (zeros; the kernels have no data-dependent control flow):
-    // O, O2, U0, U1, A, Wt, lap P
-    const size_t n = static_cast<size_t>(w) * h * 3;
+    // per member O, O2, U0, U1, A, Wt, lap P
     float* buf = nullptr;
-    if ((e = cudaMalloc(&buf, 7 * n * sizeof(float))) != cudaSuccess)
+    if ((e = cudaMalloc(&buf, 7 * total * sizeof(float))) != cudaSuccess)
         return e;
-    float* im[7];
-    for (int i = 0; i < 7; ++i)
-        im[i] = buf + i * n;
     // Three rounds, the shapes alternating within each, one warm-up launch per
     // shape and two timed 8-step launches; each shape's best round counts (the
     // first launches after the allocation and a clock still ramping up would
@@ -994,30 +1153,36 @@ cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out)
     cudaEvent_t ev[2] = {};
     float best_ms[2] = {1e30f, 1e30f};
     const int shapes[2] = {kTbEY, kPEY};
-    CUtensorMap mO[2][2], mU[2], mA[2], mW[2], mL[2], mOo[2][2], mUo[2];
-    e = cudaMemsetAsync(buf, 0, 7 * n * sizeof(float), st);
+    std::vector<GroupMember> mem[2];
+    e = cudaMemsetAsync(buf, 0, 7 * total * sizeof(float), st);
     for (int i = 0; i < 2 && e == cudaSuccess; ++i)
         e = cudaEventCreate(&ev[i]);
     for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
-        const int rows = shapes[s], ir = interior_rows(rows);
-        if (!(encode_image_map(&mO[s][0], im[0], w, h, rows) && encode_image_map(&mO[s][1], im[1], w, h, rows) &&
-                encode_image_map(&mU[s], im[2], w, h, rows) && encode_image_map(&mA[s], im[4], w, h, rows) &&
-                encode_image_map(&mW[s], im[5], w, h, rows) && encode_image_map(&mL[s], im[6], w, h, rows) &&
-                encode_image_map(&mOo[s][0], im[0], w, h, ir, 3 * kIW) &&
-                encode_image_map(&mOo[s][1], im[1], w, h, ir, 3 * kIW) &&
-                encode_image_map(&mUo[s], im[3], w, h, ir, 3 * kIW)))
-            e = cudaErrorInvalidValue;
+        size_t off = 0;
+        for (int i = 0; i < n && e == cudaSuccess; ++i) {
+            float* im[7];
+            for (int k = 0; k < 7; ++k)
+                im[k] = buf + k * total + off;
+            off += static_cast<size_t>(w[i]) * h[i] * 3;
+            GroupMember m{};
+            float* const O[2] = {im[0], im[1]};
+            float* const U[2] = {im[2], im[3]};
+            if (!encode_solve(&m.maps, O, U, im[4], im[5], im[6], w[i], h[i], shapes[s]))
+                e = cudaErrorInvalidValue;
+            m.w = w[i];
+            m.h = h[i];
+            mem[s].push_back(m);
+        }
     }
     for (int round = 0; round < 3 && e == cudaSuccess; ++round) {
         for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
-            for (int r = 0; r < 3 && e == cudaSuccess; ++r) {
-                if (r == 1)
-                    e = cudaEventRecord(ev[0], st);
-                launch_persistent(shapes[s], mO[s][r & 1], mU[s], mA[s], mW[s], mL[s], mOo[s][(r + 1) & 1], mUo[s], w,
-                    h, kTbT, kTbT, 0.15f, 0.15f, nullptr, di->sms, st);
-                if (e == cudaSuccess)
-                    e = cudaGetLastError();
-            }
+            int nl = 0;
+            // a warm-up launch, then two timed ones, all of kTbT steps with momentum
+            e = launch_members<kGroupMax>(mem[s], shapes[s], 2 * kTbT, 0.15f, 0.15f, di->sms, st, &nl, kTbT);
+            if (e == cudaSuccess)
+                e = cudaEventRecord(ev[0], st);
+            if (e == cudaSuccess)
+                e = launch_members<kGroupMax>(mem[s], shapes[s], 3 * kTbT, 0.15f, 0.15f, di->sms, st, &nl, kTbT);
             float ms = 0.0f;
             if (e == cudaSuccess)
                 e = cudaEventRecord(ev[1], st);
@@ -1039,24 +1204,124 @@ cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out)
     {
         std::lock_guard<std::mutex> lock(t.mu);
         if (t.enabled)
-            t.rows[std::make_tuple(dev, w, h)] = best;
+            t.rows[key] = best;
     }
     if (rows_out)
         *rows_out = best;
     return cudaSuccess;
 }
 
+cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out)
+{
+    return solver_group_autotune(&w, &h, 1, st, rows_out);
+}
+
 size_t solver_workspace_floats(int w, int h) { return static_cast<size_t>(w) * h * 3 * 4; }
 
 int solver_steps_per_launch() { return kTbT; }
+
+namespace {
+
+// launches of a solve, and the buffer its iterate starts in so that the last
+// launch writes O: O itself for an even count, the second buffer otherwise
+int solve_launches(int num_iter) { return num_iter > 0 ? (num_iter + kTbT - 1) / kTbT : 0; }
+
+struct WsView {
+    float *L, *U0, *U1, *O2;
+};
+WsView ws_view(float* ws, int w, int h)
+{
+    const size_t n = static_cast<size_t>(w) * h * 3;
+    return WsView{ws, ws + n, ws + 2 * n, ws + 3 * n};
+}
+
+bool tma_eligible(const DeviceInfo* di, int w, const float* O, const WsView& v, const float* A, const float* Wt)
+{
+    return di->ps_smem && (w % 4) == 0 && aligned16p(O) && aligned16p(v.O2) && aligned16p(v.U0) &&
+           aligned16p(v.U1) && aligned16p(A) && aligned16p(Wt) && aligned16p(v.L);
+}
+
+}  // namespace
+
+float* solver_start_buffer(float* O, int w, int h, int num_iter, float* workspace)
+{
+    return solve_launches(num_iter) % 2 == 0 ? O : ws_view(workspace, w, h).O2;
+}
+
+cudaError_t solver_lap(const float* P, int w, int h, float* workspace, cudaStream_t st)
+{
+    const dim3 b(32, 8);
+    lap_pr_kernel<<<grid2d(w, h, b), b, 0, st>>>(P, workspace, w, h);
+    return cudaGetLastError();
+}
+
+bool solver_group_eligible(const SolverImage* im, int n)
+{
+    DeviceInfo* di = nullptr;
+    if (n < 1 || device_info(&di) != cudaSuccess)
+        return false;
+    for (int i = 0; i < n; ++i)
+        if (!tma_eligible(di, im[i].w, im[i].O, ws_view(im[i].workspace, im[i].w, im[i].h), im[i].A, im[i].Wt))
+            return false;
+    return true;
+}
+
+cudaError_t run_solver_group(const SolverImage* im, int n, int num_iter, float step, float mom, cudaStream_t st,
+    int* launches)
+{
+    DeviceInfo* di = nullptr;
+    cudaError_t e = device_info(&di);
+    if (e != cudaSuccess)
+        return e;
+    if (!solver_group_eligible(im, n))
+        return cudaErrorInvalidValue;
+    int nl = 0;
+    if (num_iter <= 0) {
+        for (int i = 0; i < n && e == cudaSuccess; ++i)
+            if (im[i].rgba) {
+                e = launch_float_to_rgba(im[i].O, im[i].rgba, static_cast<int64_t>(im[i].w) * im[i].h, st);
+                ++nl;
+            }
+        if (launches)
+            *launches += nl;
+        return e;
+    }
+    int dev = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess)
+        return e;
+    std::vector<int> ws(n), hs(n);
+    for (int i = 0; i < n; ++i) {
+        ws[i] = im[i].w;
+        hs[i] = im[i].h;
+    }
+    const int rows = chosen_rows(dev, ws.data(), hs.data(), n, di->sms);
+    const bool odd = solve_launches(num_iter) % 2 == 1;
+    std::vector<GroupMember> mem(n);
+    for (int i = 0; i < n; ++i) {
+        const WsView v = ws_view(im[i].workspace, im[i].w, im[i].h);
+        float* const O[2] = {im[i].O, v.O2};
+        float* const U[2] = {v.U0, v.U1};
+        if (!encode_solve(&mem[i].maps, O, U, im[i].A, im[i].Wt, v.L, im[i].w, im[i].h, rows))
+            return cudaErrorInvalidValue;
+        mem[i].w = im[i].w;
+        mem[i].h = im[i].h;
+        mem[i].c0 = odd ? 1 : 0;
+        mem[i].rgba = im[i].rgba;
+    }
+    e = n <= 4 ? launch_members<4>(mem, rows, num_iter, step, mom, di->sms, st, &nl)
+               : launch_members<kGroupMax>(mem, rows, num_iter, step, mom, di->sms, st, &nl);
+    if (launches)
+        *launches += nl;
+    if (e == cudaSuccess)
+        e = cudaGetLastError();
+    return e;
+}
 
 cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,
     float step, float mom, float* workspace, cudaStream_t st, int* launches, uint8_t* rgba_out)
 {
     const size_t n = static_cast<size_t>(w) * h * 3;
-    float* L = workspace;
-    float* U[2] = {workspace + n, workspace + 2 * n};
-    float* O2 = workspace + 3 * n;
+    const WsView v = ws_view(workspace, w, h);
     int nl = 0;
     if (num_iter <= 0) {
         if (rgba_out) {
@@ -1071,48 +1336,51 @@ cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O
     cudaError_t e0 = device_info(&di);
     if (e0 != cudaSuccess)
         return e0;
-    const dim3 b(32, 8);
-    lap_pr_kernel<<<grid2d(w, h, b), b, 0, st>>>(P, L, w, h);
+    if ((e0 = solver_lap(P, w, h, v.L, st)) != cudaSuccess)
+        return e0;
     ++nl;
     // Launches of up to kTbT iterations; ping-pong O between O and O2 and U
     // between its two buffers so that the last launch writes O.
-    const int nlaunch = (num_iter + kTbT - 1) / kTbT;
-    float* cur = (nlaunch % 2 == 0) ? O : O2;
+    const int nlaunch = solve_launches(num_iter);
+    float* cur = solver_start_buffer(O, w, h, num_iter, workspace);
     if (cur != O) {
-        cudaError_t e = cudaMemcpyAsync(O2, O, n * sizeof(float), cudaMemcpyDeviceToDevice, st);
+        cudaError_t e = cudaMemcpyAsync(v.O2, O, n * sizeof(float), cudaMemcpyDeviceToDevice, st);
         if (e != cudaSuccess)
             return e;
     }
-    // TMA path: 16-byte row pitch and aligned images
-    bool tma = di->ps_smem && (w % 4) == 0 && aligned16p(O) && aligned16p(O2) && aligned16p(U[0]) &&
-               aligned16p(U[1]) && aligned16p(A) && aligned16p(Wt) && aligned16p(L);
-    // tile shape: the autotuned one for this size, else the wave model
+    // TMA path: 16-byte row pitch and aligned images; the tile shape is the
+    // autotuned one for this size, else the wave model's
     int dev = 0;
     if ((e0 = cudaGetDevice(&dev)) != cudaSuccess)
         return e0;
-    const int rows = chosen_rows(dev, w, h, di->sms);
-    CUtensorMap mO[2], mU[2], mA, mW, mL, mOo[2], mUo[2];
-    const int ir = interior_rows(rows);
-    if (tma)
-        tma = encode_image_map(&mO[0], O, w, h, rows) && encode_image_map(&mO[1], O2, w, h, rows) &&
-              encode_image_map(&mU[0], U[0], w, h, rows) && encode_image_map(&mU[1], U[1], w, h, rows) &&
-              encode_image_map(&mA, A, w, h, rows) && encode_image_map(&mW, Wt, w, h, rows) &&
-              encode_image_map(&mL, L, w, h, rows) && encode_image_map(&mOo[0], O, w, h, ir, 3 * kIW) &&
-              encode_image_map(&mOo[1], O2, w, h, ir, 3 * kIW) && encode_image_map(&mUo[0], U[0], w, h, ir, 3 * kIW) &&
-              encode_image_map(&mUo[1], U[1], w, h, ir, 3 * kIW);
+    const int rows = chosen_rows(dev, &w, &h, 1, di->sms);
+    GroupMember m{};
+    bool tma = tma_eligible(di, w, O, v, A, Wt);
+    if (tma) {
+        float* const Ob[2] = {O, v.O2};
+        float* const Ub[2] = {v.U0, v.U1};
+        tma = encode_solve(&m.maps, Ob, Ub, A, Wt, v.L, w, h, rows);
+    }
+    if (tma) {
+        m.w = w;
+        m.h = h;
+        m.c0 = cur == O ? 0 : 1;
+        m.rgba = rgba_out;
+        const std::vector<GroupMember> one(1, m);
+        cudaError_t e = launch_members<1>(one, rows, num_iter, step, mom, di->sms, st, &nl);
+        if (launches)
+            *launches += nl;
+        return e != cudaSuccess ? e : cudaGetLastError();
+    }
+    float* U[2] = {v.U0, v.U1};
     int k0 = 0;
     for (int li = 0; li < nlaunch; ++li) {
         const int T = std::min(kTbT, num_iter - k0);
-        float* nxt = (cur == O) ? O2 : O;
+        float* nxt = (cur == O) ? v.O2 : O;
         uint8_t* rg = (li == nlaunch - 1) ? rgba_out : nullptr;
-        if (tma) {
-            launch_persistent(rows, mO[cur == O ? 0 : 1], mU[li & 1], mA, mW, mL, mOo[nxt == O ? 0 : 1],
-                mUo[(li + 1) & 1], w, h, T, k0, step, mom, rg, di->sms, st);
-        } else {
-            const dim3 grid((w + (kTbEX - 2 * T) - 1) / (kTbEX - 2 * T), (h + (kTbEY - 2 * T) - 1) / (kTbEY - 2 * T));
-            solver_tb_kernel<<<grid, dim3(32, kTbEY / 2), kTbSmem, st>>>(cur, nxt, U[li & 1], U[(li + 1) & 1], L, A,
-                Wt, w, h, T, k0, step, mom, rg);
-        }
+        const dim3 grid((w + (kTbEX - 2 * T) - 1) / (kTbEX - 2 * T), (h + (kTbEY - 2 * T) - 1) / (kTbEY - 2 * T));
+        solver_tb_kernel<<<grid, dim3(32, kTbEY / 2), kTbSmem, st>>>(cur, nxt, U[li & 1], U[(li + 1) & 1], v.L, A,
+            Wt, w, h, T, k0, step, mom, rg);
         ++nl;
         k0 += T;
         cur = nxt;

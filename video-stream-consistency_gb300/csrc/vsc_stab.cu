@@ -12,6 +12,7 @@
 #include "vsc_internal.h"
 #include "vsc_math.cuh"
 
+#include <algorithm>
 
 namespace vsc {
 namespace {
@@ -288,10 +289,9 @@ __global__ void bilinear_kernel(const float* __restrict__ in, int iw, int ih, fl
 // the row terms are computed once, the 4 C outputs leave as 16-byte stores
 // when the row is 16-byte aligned (same arithmetic, same bits).
 template <int C>
-__global__ void bilinear4_kernel(const float* __restrict__ in, int iw, int ih, float* __restrict__ out, int ow, int oh)
+__device__ __forceinline__ void bilinear4_px(const float* __restrict__ in, int iw, int ih, float* __restrict__ out,
+    int ow, int oh, int ox0, int oy)
 {
-    const int ox0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
-    const int oy = blockIdx.y * blockDim.y + threadIdx.y;
     if (ox0 >= ow || oy >= oh)
         return;
     const float yy = static_cast<float>(oy) * static_cast<float>(ih) / static_cast<float>(oh);
@@ -326,6 +326,37 @@ __global__ void bilinear4_kernel(const float* __restrict__ in, int iw, int ih, f
             for (int k = 0; k < C; ++k)
                 dst[j * C + k] = v[j * C + k];
     }
+}
+
+template <int C>
+__global__ void bilinear4_kernel(const float* __restrict__ in, int iw, int ih, float* __restrict__ out, int ow, int oh)
+{
+    bilinear4_px<C>(in, iw, ih, out, ow, oh, (blockIdx.x * blockDim.x + threadIdx.x) * 4,
+        blockIdx.y * blockDim.y + threadIdx.y);
+}
+
+// bilinear4_kernel<3> over up to kBilinearGroupMax images of any sizes in one
+// launch (one per stream of a multi-stream step): a flat list of 32 x 8
+// blocks, each image's blocks after the previous image's.
+constexpr int kBilinearGroupMax = 16;
+struct BilinearGroup {
+    const float* in[kBilinearGroupMax];
+    float* out[kBilinearGroupMax];
+    int iw[kBilinearGroupMax], ih[kBilinearGroupMax], ow[kBilinearGroupMax], oh[kBilinearGroupMax];
+    int bx[kBilinearGroupMax];              // blocks per output row band
+    int block0[kBilinearGroupMax + 1];      // first block of each image
+    int count;
+};
+
+__global__ void __launch_bounds__(256) bilinear4_group_kernel(const __grid_constant__ BilinearGroup g)
+{
+    int p = 0;
+    while (p + 1 < g.count && static_cast<int>(blockIdx.x) >= g.block0[p + 1])
+        ++p;
+    const int b = blockIdx.x - g.block0[p];
+    const int bx = b % g.bx[p], by = b / g.bx[p];
+    bilinear4_px<3>(g.in[p], g.iw[p], g.ih[p], g.out[p], g.ow[p], g.oh[p], (bx * 32 + threadIdx.x) * 4,
+        by * 8 + threadIdx.y);
 }
 
 __global__ void pyr_down3_kernel(const float* __restrict__ P, const float* __restrict__ A,
@@ -536,6 +567,35 @@ cudaError_t launch_bilinear(Img in, Img out, cudaStream_t st)
         bilinear_kernel<<<grid2d(out.w, out.h, b), b, 0, st>>>(in.d, in.w, in.h, out.d, out.w, out.h, out.c);
     }
     return cudaGetLastError();
+}
+
+cudaError_t launch_bilinear_group(const Img* in, const Img* out, int n, cudaStream_t st)
+{
+    for (int b0 = 0; b0 < n; b0 += kBilinearGroupMax) {
+        BilinearGroup g{};
+        g.count = std::min(n - b0, kBilinearGroupMax);
+        g.block0[0] = 0;
+        for (int p = 0; p < g.count; ++p) {
+            const Img& i = in[b0 + p];
+            const Img& o = out[b0 + p];
+            if (i.c != 3 || o.c != 3)
+                return cudaErrorInvalidValue;
+            g.in[p] = i.d;
+            g.out[p] = o.d;
+            g.iw[p] = i.w;
+            g.ih[p] = i.h;
+            g.ow[p] = o.w;
+            g.oh[p] = o.h;
+            g.bx[p] = (o.w + 127) / 128;
+            g.block0[p + 1] = g.block0[p] + g.bx[p] * ((o.h + 7) / 8);
+        }
+        if (g.block0[g.count] > 0)
+            bilinear4_group_kernel<<<g.block0[g.count], dim3(32, 8), 0, st>>>(g);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_pyr_down3(const float* P, const float* A, const float* Wt, int iw, int ih, float* Pd, float* Ad,
