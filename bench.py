@@ -605,6 +605,9 @@ def run_front_only(args):
     forms = {
         "fused_front_kernel (vsc_stab_front, float frames)": (124, lambda: vsc.stab_front(
             ims[0:3], ims[3:6], ims[6], ff, fb, 6800.0, 6800.0, 2.0, out=(apr, wt), stream=stream)),
+        # |gamma| > 1e30 selects the general form (64-bit taps, the full expf_cw)
+        "fused_front_kernel general form (vsc_stab_front, gamma 2e30)": (124, lambda: vsc.stab_front(
+            ims[0:3], ims[3:6], ims[6], ff, fb, 6800.0, 6800.0, 2e30, out=(apr, wt), stream=stream)),
         "fused_front_rgba_kernel (vsc_stab_front_rgba, RGBA8 frames)": (84, lambda: (
             vsc.stab_front_rgba(rgba[0:3], rgba[3:6], ims[6], ff, fb, 6800.0, 6800.0, 2.0, out=(apr, wt),
                                 stream=stream))),
@@ -637,6 +640,91 @@ def run_solver_only(args):
     dev = torch.device("cuda", 0)
     stream = torch.cuda.Stream(device=dev)
     print(json.dumps(solver_roofline(vsc, dev, stream, iters=args.steps * 8)))
+
+
+def run_warpblend(args):
+    """--kernel warpblend: the warp, mask and blend kernels one by one at
+    1920x1080 (float HWC3 images, 3-channel flows), each against its
+    algorithmic bytes (every input tensor read once, every output written
+    once, in the layout the kernel uses): kernel_warp 36 B/px (source 12,
+    flow 12, out 12), adap_comb 108 B/px (seven images in, two out),
+    consist_wt 36 B/px, the fused front pass 124 B/px, bilinear 12 B per
+    input and output pixel, the Warp op 4 (2 C + 2) B per pixel (a batch of
+    8 at the 480x272, 32-channel PWC level), RGBA8 <-> float 16 B/px.
+    K calls back to back between two CUDA events on the kernels' stream,
+    each call on the next of four input sets, so that consecutive calls
+    never find their inputs in L2 (every case's four sets exceed 129 MB)."""
+    import torch
+
+    vsc = import_pkg()
+    vsc.build()
+    vsc.load()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    g = torch.Generator(device=dev).manual_seed(6)
+    nsets = 4
+    yy, xx = torch.meshgrid(torch.arange(H, device=dev), torch.arange(W, device=dev), indexing="ij")
+
+    def img(h=H, w=W):
+        return torch.rand((h, w, 3), device=dev, generator=g)
+
+    def flow(k):
+        return torch.stack([3 * torch.sin(xx / (97.0 + k)), 2 * torch.cos(yy / (83.0 + k)),
+                            torch.zeros_like(xx, dtype=torch.float32)], -1).float().contiguous()
+
+    def smooth_flow(n, w, h, k):  # N x 2 x h x w, |v| <= 3 px, smooth like an upsampled estimate
+        yy2, xx2 = torch.meshgrid(torch.arange(h, device=dev), torch.arange(w, device=dev), indexing="ij")
+        f = torch.stack([3 * torch.sin(xx2 / (31.0 + k)), 3 * torch.cos(yy2 / (23.0 + k))], 0).float()
+        return f.unsqueeze(0).repeat(n, 1, 1, 1).contiguous()
+
+    sets = []
+    for k in range(nsets):
+        ims = [img() for _ in range(7)]
+        ff = flow(k)
+        outs = [torch.empty_like(ims[0]) for _ in range(2)]
+        sets.append({
+            "ims": ims, "ff": ff, "fb": (-ff).contiguous(), "outs": outs, "small": img(H // 2, W // 2),
+            "rgba": torch.randint(0, 256, (H, W, 4), device=dev, generator=g, dtype=torch.uint8),
+            "x32": torch.randn((8, 32, 272, 480), device=dev, generator=g),
+            "fl32": smooth_flow(8, 480, 272, k),
+            "x3": ims[0].permute(2, 0, 1).unsqueeze(0).contiguous(),
+            "fl3": ff[..., :2].permute(2, 0, 1).unsqueeze(0).contiguous(),
+        })
+    torch.cuda.synchronize()
+    peak, peak_src = peaks()
+    px, spx = W * H, (W // 2) * (H // 2)
+    cases = [
+        ("stab_warp_kernel (get_warp_result)", 36 * px, lambda d: vsc.get_warp_result(d["ims"][0], d["ff"], stream=stream)),
+        ("adap_comb_kernel (get_adap_comb)", 108 * px, lambda d: vsc.get_adap_comb(*d["ims"][0:7], 6800.0, stream=stream)),
+        ("consist_wt_kernel (get_consist_wt)", 36 * px,
+         lambda d: vsc.get_consist_wt(d["ims"][0], d["ims"][1], 6800.0, 2.0, stream=stream)),
+        ("fused_front_kernel (stab_front)", 124 * px, lambda d: vsc.stab_front(
+            d["ims"][0:3], d["ims"][3:6], d["ims"][6], d["ff"], d["fb"], 6800.0, 6800.0, 2.0, out=d["outs"],
+            stream=stream)),
+        ("bilinear 1920x1080 -> 960x540", 12 * (px + spx), lambda d: vsc.get_bilinear(d["ims"][0], W // 2, H // 2,
+                                                                                      stream=stream)),
+        ("bilinear 960x540 -> 1920x1080", 12 * (px + spx), lambda d: vsc.get_bilinear(d["small"], W, H, stream=stream)),
+        ("warp_op_kernel (Warp op, C=3, 1920x1080)", 4 * (2 * 3 + 2) * px,
+         lambda d: vsc.warp(d["x3"], d["fl3"], stream=stream)),
+        ("warp_op_kernel (Warp op, 8 x C=32, 480x272)", 8 * 4 * (2 * 32 + 2) * 480 * 272,
+         lambda d: vsc.warp(d["x32"], d["fl32"], stream=stream)),
+        ("rgba_to_float (char_to_float_image)", 16 * px, lambda d: vsc.char_to_float_image(d["rgba"], stream=stream)),
+        ("float_to_rgba (float_to_char_image)", 16 * px, lambda d: vsc.float_to_char_image(d["ims"][0], stream=stream)),
+    ]
+    res = []
+    for name, alg, call in cases:
+        for k in range(max(args.warmup, 3)):
+            call(sets[k % nsets])
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(args.steps):
+            call(sets[k % nsets])
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        res.append({"kernel": name, "ms": ms, "algorithmic_bytes": alg, "achieved_gbs": alg / (ms / 1000) / 1e9,
+                    "frac": alg / (ms / 1000) / 1e9 / peak})
+    print(json.dumps({"kernels": res, "peak_gbs": peak, "peak_source": peak_src}))
 
 
 def run_upsampler_only(args):
@@ -910,7 +998,7 @@ def main():
                          "bf16_ds2 (1080p) or bf16_ds2_learned (multistream)")
     ap.add_argument("--ms-grouped", choices=["on", "off"], default="on",
                     help="multistream: group every stream's solve into shared solver launches")
-    ap.add_argument("--kernel", choices=["step", "solver", "corr", "front", "upsampler"], default="step",
+    ap.add_argument("--kernel", choices=["step", "solver", "corr", "front", "upsampler", "warpblend"], default="step",
                     help="solver / corr: time only the 1920x1080 solver or the correlation pyramid "
                          "(profiler targets)")
     args = ap.parse_args()
@@ -934,6 +1022,8 @@ def main():
         run_front_only(args)
     elif args.kernel == "upsampler":
         run_upsampler_only(args)
+    elif args.kernel == "warpblend":
+        run_warpblend(args)
     else:
         run_gpu(args)
 

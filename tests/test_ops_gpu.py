@@ -94,6 +94,24 @@ def test_warp(vsc, oracle, cuda, shape, scale, offset):
     assert np.max(np.abs(out - ref)) <= 2.0 ** -21 * np.max(np.abs(x))
 
 
+@pytest.mark.parametrize("shape", [(2, 3, 37, 70), (1, 8, 33, 65), (1, 16, 9, 130), (3, 5, 12, 64)])
+def test_warp_signed_inputs_and_nonfinite_flows(vsc, oracle, cuda, shape):
+    """Negative inputs (signed zeros and cancellation in the blend) and flows
+    with NaN and infinite entries (no sample taken: 0), for the image-shaped
+    3-channel kernel (two pixels per thread, an odd number of rows) and the
+    8-channel groups (full and partial)."""
+    x = (RNG.random(shape) * 10 - 5).astype(np.float32)
+    x.flat[::7] = 0.0
+    x.flat[3::11] = -0.0
+    flow = (RNG.random((shape[0], 2) + shape[2:]) * 8 - 4).astype(np.float32)
+    flow.flat[::13] = np.nan
+    flow.flat[5::17] = np.inf
+    flow.flat[9::19] = -np.inf
+    out = vsc.warp(_t(x, cuda), _t(flow, cuda)).cpu().numpy()
+    ref = oracle.warp_op(x, flow, "f32")
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+
+
 @pytest.mark.parametrize("i", range(3))
 def test_warp_reference_fixture(vsc, cuda, golden, i):
     g = golden["ref_ops"]

@@ -495,8 +495,14 @@ def test_multistream_ungroupable_size_runs_ungrouped(vsc, cuda):
     assert not grouped
 
 
+# (alpha, beta, gamma): the kernel's fast form (32-bit taps, the exponential
+# for non-positive arguments) needs alpha, beta >= 0 and |gamma| <= 1e30;
+# 1e6 drives most exponents below -87.3 (the fast form's floor), gamma 2e30
+# and a negative alpha take the general form
+@pytest.mark.parametrize("hp", [(20.0, 30.0, 2.0), (1e6, 1e6, 2.0), (1e6, 1e6, -1e30), (20.0, 30.0, 2e30),
+                                (-5.0, 30.0, 2.0)])
 @pytest.mark.parametrize("fc,occ", [(3, False), (2, False), (2, True)])
-def test_stab_front_equals_separate_calls(vsc, oracle, cuda, fc, occ):
+def test_stab_front_equals_separate_calls(vsc, oracle, cuda, fc, occ, hp):
     """vsc_stab_front (five warps + combination + weights in one pass) equals
     the separate entry points bit for bit; with the occlusion mask, the
     restatement's masked combination."""
@@ -508,16 +514,17 @@ def test_stab_front_equals_separate_calls(vsc, oracle, cuda, fc, occ):
     ff = (RNG.normal(0, 2, (h, w, fc))).astype(np.float32)
     fb = (-ff + RNG.normal(0, 0.4, ff.shape)).astype(np.float32)
     d = lambda a: _t(a, cuda)  # noqa: E731
-    apr, wt = vsc.stab_front([d(a) for a in o3], [d(a) for a in p3], d(ls), d(ff), d(fb), 20.0, 30.0, 2.0,
+    alpha, beta, gamma = hp
+    apr, wt = vsc.stab_front([d(a) for a in o3], [d(a) for a in p3], d(ls), d(ff), d(fb), alpha, beta, gamma,
                              occlusion_mask=occ)
     warps = [oracle.stab_warp(src, fl) for src, fl in ((o3[0], fb), (p3[0], fb), (o3[2], ff), (p3[2], ff),
                                                        (ls, fb))]
     if occ:
         m = oracle.flow_consistency_mask(ff, fb)
-        ain, rpr = oracle.adap_comb_masked(o3[1], p3[1], warps[0], warps[1], warps[2], warps[3], warps[4], m, 20.0)
+        ain, rpr = oracle.adap_comb_masked(o3[1], p3[1], warps[0], warps[1], warps[2], warps[3], warps[4], m, alpha)
     else:
-        ain, rpr = oracle.adap_comb(o3[1], p3[1], warps[0], warps[1], warps[2], warps[3], warps[4], 20.0)
-    rwt = oracle.consist_wt(o3[1], ain, 30.0, 2.0)
+        ain, rpr = oracle.adap_comb(o3[1], p3[1], warps[0], warps[1], warps[2], warps[3], warps[4], alpha)
+    rwt = oracle.consist_wt(o3[1], ain, beta, gamma)
     assert np.array_equal(apr.cpu().numpy(), rpr)
     assert np.array_equal(wt.cpu().numpy(), rwt)
 

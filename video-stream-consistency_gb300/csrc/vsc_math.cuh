@@ -44,6 +44,28 @@ __device__ __forceinline__ float expf_cw(float x)
     return p * __int_as_float((k + 127) << 23);
 }
 
+// expf_cw for an argument known to be <= 0 and not NaN: the same value for
+// x >= -87.33654 (the NaN, overflow and k > 127 branches cannot apply);
+// below, expf_cw gives 0 and this expf_cw(-87.33654) = 2^-126, which every
+// caller's cut at 0.001 (also after a factor of magnitude <= 1e30) turns
+// into the same 0.
+__device__ __forceinline__ float expf_cw_nonpos(float x)
+{
+    x = fmaxf(x, -87.33654f);
+    const float kf = rintf(__fmul_rn(x, 1.44269502f));
+    float r = fmaf(kf, -0.693145751953125f, x);
+    r = fmaf(kf, -1.42860682e-6f, r);
+    float p = 1.98412701e-4f;
+    p = fmaf(p, r, 1.38888892e-3f);
+    p = fmaf(p, r, 8.33333377e-3f);
+    p = fmaf(p, r, 4.16666679e-2f);
+    p = fmaf(p, r, 1.66666672e-1f);
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
+    return p * __int_as_float((static_cast<int>(kf) + 127) << 23);
+}
+
 __device__ __forceinline__ int64_t pix_index(int x, int y, int w) { return static_cast<int64_t>(y) * w + x; }
 
 // RGBA8 quantisation of gpuimage.cu:64: (uint8)__float2uint_rd(|v| * 255),

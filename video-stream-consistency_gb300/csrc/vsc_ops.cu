@@ -294,6 +294,122 @@ cudaError_t launch_corr_tile(const float* f1, const float* f2, float* out, int N
 
 constexpr int kWarpCG = 8;  // channels per thread
 
+// The Warp op's per-pixel taps (warp.cc:71-133): bilinear weights, the
+// in-range mask and whether the sample is taken (mask > 0.999).
+struct OpTap {
+    float wTL, wTR, wBL, wBR;
+    bool tl, tr, bl, br, take;
+    int xl, yt;
+};
+
+__device__ __forceinline__ OpTap op_tap(float flx, float fly, int x, int y, int H, int W)
+{
+    const float xf = static_cast<float>(x) + flx;
+    const float yf = static_cast<float>(y) + fly;
+    const float fxl = floorf(xf), fyt = floorf(yf);
+    const float a = xf - fxl, b = yf - fyt;
+    const float xR = fxl + 1.0f, yB = fyt + 1.0f;
+    const bool mL = (0.0f <= fxl && fxl <= static_cast<float>(W - 1));
+    const bool mR = (0.0f <= xR && xR <= static_cast<float>(W - 1));
+    const bool mT = (0.0f <= fyt && fyt <= static_cast<float>(H - 1));
+    const bool mB = (0.0f <= yB && yB <= static_cast<float>(H - 1));
+    const float ia = 1.0f - a, ib = 1.0f - b;
+    OpTap t;
+    t.wTL = ia * ib;
+    t.wTR = a * ib;
+    t.wBL = ia * b;
+    t.wBR = a * b;
+    t.tl = mT && mL;
+    t.tr = mT && mR;
+    t.bl = mB && mL;
+    t.br = mB && mR;
+    float mask = 0.0f;
+    mask += t.tl ? t.wTL : 0.0f;
+    mask += t.tr ? t.wTR : 0.0f;
+    mask += t.bl ? t.wBL : 0.0f;
+    mask += t.br ? t.wBR : 0.0f;
+    t.take = mask > 0.999f;
+    t.xl = t.take ? static_cast<int>(fxl) : 0;
+    t.yt = t.take ? static_cast<int>(fyt) : 0;
+    return t;
+}
+
+// The Warp op for planes of fewer than 2^31 pixels: 64 x (4 PX) pixels per
+// block (a warp on 32 consecutive pixels of a row: coalesced flow reads and
+// output writes), PX pixels per thread (rows y, y + 4, ...), CG channels
+// each, every tap of the thread loaded before the first blend (one branch on
+// `take` per pixel, the in-range predicate per tap); blockIdx.z = batch *
+// groups + channel group.  kFull: C is a multiple of CG.  Where the sample
+// is taken every weight is finite and >= 0, so a tap that is not loaded
+// (held as 0) adds w * 0 = +0, the same +0 the reference's guarded sum adds
+// (warp.cc:116-126); where it is not taken the output is 0 (the weights may
+// then be NaN, from a NaN or infinite flow).
+template <int CG, bool kFull, int PX>
+__global__ void __launch_bounds__(256) warp_op2d_kernel(const float* __restrict__ in, const float* __restrict__ flow,
+    float* __restrict__ out, int C, int H, int W, int64_t sin, int64_t sfl, int64_t sout, int groups)
+{
+    const int x = blockIdx.x * 64 + (threadIdx.x & 63);
+    const int yb = blockIdx.y * (4 * PX) + (threadIdx.x >> 6);
+    if (x >= W || yb >= H)
+        return;
+    const int n = blockIdx.z / groups;
+    const int c0 = (blockIdx.z - n * groups) * CG;
+    const int HW = H * W;
+    const float* fl = flow + n * sfl;
+    const float* src = in + n * sin + static_cast<int64_t>(c0) * HW;
+    OpTap t[PX];
+    int oTL[PX];
+#pragma unroll
+    for (int k = 0; k < PX; ++k) {
+        const int y = min(yb + 4 * k, H - 1);  // a row past the end repeats the last (not stored)
+        const int p = y * W + x;
+        t[k] = op_tap(__ldg(fl + p), __ldg(fl + HW + p), x, y, H, W);
+        oTL[k] = t[k].yt * W + t[k].xl;
+    }
+    float q[PX][CG][4];
+#pragma unroll
+    for (int k = 0; k < PX; ++k) {
+#pragma unroll
+        for (int c = 0; c < CG; ++c)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                q[k][c][j] = 0.0f;
+        if (t[k].take) {
+#pragma unroll
+            for (int c = 0; c < CG; ++c) {
+                const float* sc = src + static_cast<int64_t>(c) * HW + oTL[k];
+                const bool ok = kFull || c0 + c < C;
+                if (ok && t[k].tl)
+                    q[k][c][0] = __ldg(sc);
+                if (ok && t[k].tr)
+                    q[k][c][1] = __ldg(sc + 1);
+                if (ok && t[k].bl)
+                    q[k][c][2] = __ldg(sc + W);
+                if (ok && t[k].br)
+                    q[k][c][3] = __ldg(sc + W + 1);
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < PX; ++k) {
+        const int y = yb + 4 * k;
+        if (y >= H)
+            continue;
+        float* dst = out + n * sout + static_cast<int64_t>(c0) * HW + (y * W + x);
+#pragma unroll
+        for (int c = 0; c < CG; ++c) {
+            if (!(kFull || c0 + c < C))
+                continue;
+            float val = 0.0f;
+            val += t[k].wTL * q[k][c][0];
+            val += t[k].wTR * q[k][c][1];
+            val += t[k].wBL * q[k][c][2];
+            val += t[k].wBR * q[k][c][3];
+            dst[static_cast<int64_t>(c) * HW] = t[k].take ? val : 0.0f;
+        }
+    }
+}
+
 __global__ void warp_op_kernel(const float* __restrict__ in, const float* __restrict__ flow, float* __restrict__ out,
     int C, int H, int W, int64_t sin, int64_t sfl, int64_t sout)
 {
@@ -449,6 +565,25 @@ cudaError_t launch_warp_op(const float* in, const float* flow, float* out, int N
     if (sin < 0 && sfl < 0 && sout < 0) {
         sin = sout = C * HW;
         sfl = 2 * HW;
+    }
+    if (HW < (int64_t(1) << 31)) {
+        // image-shaped inputs (C = 3) take one group of three; feature maps groups of eight
+        const int cg = C == 3 ? 3 : kWarpCG;
+        const int groups = (C + cg - 1) / cg;
+        const int px = C == 3 ? 2 : 1;  // pixels per thread
+        const int rows = 4 * px;
+        if (static_cast<int64_t>(N) * groups <= 65535 && (H + rows - 1) / rows <= 65535) {
+            dim3 grid(static_cast<unsigned>((W + 63) / 64), static_cast<unsigned>((H + rows - 1) / rows), N * groups);
+            if (C == 3)
+                warp_op2d_kernel<3, true, 2><<<grid, 256, 0, st>>>(in, flow, out, C, H, W, sin, sfl, sout, groups);
+            else if (C % kWarpCG == 0)
+                warp_op2d_kernel<kWarpCG, true, 1><<<grid, 256, 0, st>>>(in, flow, out, C, H, W, sin, sfl, sout,
+                    groups);
+            else
+                warp_op2d_kernel<kWarpCG, false, 1><<<grid, 256, 0, st>>>(in, flow, out, C, H, W, sin, sfl, sout,
+                    groups);
+            return cudaGetLastError();
+        }
     }
     dim3 grid(static_cast<unsigned>((HW + 255) / 256), (C + kWarpCG - 1) / kWarpCG, N);
     warp_op_kernel<<<grid, 256, 0, st>>>(in, flow, out, C, H, W, sin, sfl, sout);
