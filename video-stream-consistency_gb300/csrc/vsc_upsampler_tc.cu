@@ -2,37 +2,44 @@
 //
 // Each 3x3 convolution (zero padding) is an implicit GEMM.  Activations are
 // FP16 in a chunked planar layout [n][c / 8][y][x][c % 8].  For a segment of
-// kUpM = 128 output positions x0 ... x0 + 127 and one input row j,
-//     D_j[x][ty][o] = sum over tx and input channels c of
-//                     act[c][j][x + tx - 1] * w[o][ty][tx][c],
-// three MMA chains (one per horizontal tap tx, K = input channels in steps of
-// 16) of M = 128 positions x N = 3 x (output channels), accumulated in one
-// Tensor Memory slot per input row.  Output row y is then
-//     out[o][y][x] = D_{y-1}[x][0][o] + D_y[x][1][o] + D_{y+1}[x][2][o] + bias,
-// three slots read by the same Tensor Memory lane: no exchange between lanes.
-// A tcgen05.mma of M = 128, K = 16 costs about max(45, N / 2) cycles on
-// GB300, so folding the three vertical taps into N (96 columns) issues 2.7x
-// fewer MMAs than one chain per tap with N = 32, at a third of the cycles.
-// A work item is a segment of kUpRC output rows; its kUpRC + 2 input rows
-// stream through a ring of row buffers (one TMA box {8, 130, 1, chunks} per
-// row: the segment with its one-pixel halo, zero-filled outside the image,
-// which is the convolution's zero padding) and a ring of Tensor Memory slots.
-// The A operand is a row buffer seen from position tx (8 positions x 16 bytes
-// per core matrix, M-adjacent core matrices 128 bytes apart, K-adjacent ones
-// a chunk plane apart).  Weights [tx][chunk][ty * NO + o][8] (FP16, output
-// channels padded to NO, input channels to the K chunks) stay in shared
-// memory for the launch.  The first layer's three input channels (base flow
-// u, v and luma) occupy one chunk; its second K chunk is a zero plane that is
-// never loaded.
+// kUpM = 128 output positions x0 ... x0 + 127, output row y is
+//     out[o][y][x] = sum over ty, tx and input channels c of
+//                    act[c][y + ty - 1][x + tx - 1] * w[o][ty][tx][c] + bias.
+// Input row j contributes to output rows j + 1 (ty = 0), j (ty = 1) and
+// j - 1 (ty = 2).  Output rows are accumulated in groups of kUpGR = 8 in one
+// Tensor Memory slot of 8 NO columns, output row y0 + t at columns
+// NO (7 - t), so the three rows an input row feeds are adjacent columns in
+// ty order, which is the order of the packed weights: one MMA chain per
+// input row (M = 128 positions, N = NO times the number of its rows inside
+// the group, K = input channels x horizontal taps in steps of 16) writes
+// straight into its rows' columns.  A slot is cleared by one MMA of zero
+// operands and every later MMA accumulates; once its ten input rows are in,
+// the epilogue reads it once and frees it.  A tcgen05.mma of M = 128, K = 16
+// costs about max(45, N / 2) cycles on GB300, so a group of 8 rows costs
+// about 351 cycles per row, and with two slots the MMAs of one group overlap
+// the epilogue of the other: the layer is bound by HBM, not by the
+// accumulator ring.
+//
+// A work item is a segment of kUpRC = 16 output rows (two groups); its 18
+// input rows stream through a ring of row buffers (one TMA box {8, 130, 1,
+// chunks} per row: the segment with its one-pixel halo, zero-filled outside
+// the image, which is the convolution's zero padding).  The two rows the
+// groups share are released after the second group's MMAs.  The A operand is
+// a row buffer seen from position tx (8 positions x 16 bytes per core
+// matrix, M-adjacent core matrices 128 bytes apart, K-adjacent ones a chunk
+// plane apart).  Weights [tx][chunk][ty * NO + o][8] (FP16, output channels
+// padded to NO, input channels to the K chunks) stay in shared memory for the
+// launch.  The first layer's three input channels (base flow u, v and luma)
+// occupy one chunk; its second K chunk is a zero plane that is never loaded.
 //
 // Persistent and warp-specialised: warp 0 issues the TMA loads, warp 1 the
-// MMAs (and owns Tensor Memory), then kUpGroups epilogue groups taking
-// alternate output rows, each of eight warps: two per 32 Tensor Memory lanes,
-// splitting the output channels.  Epilogue: bias, ReLU, FP16 and the chunked
-// store for the inner layers; for the last layer the residual test and the
-// finished flow (base + r where max(|r_u|, |r_v|) <= max_residual, else
-// base).  Every mbarrier wait is bounded; a wait that runs out stops all
-// roles and sets the device timeout flag.
+// MMAs (and owns Tensor Memory), then sixteen epilogue warps: four per 32
+// Tensor Memory lanes, each taking two output rows of a group.  Epilogue:
+// bias, ReLU, FP16 and the chunked store for the inner layers; for the last
+// layer the residual test and the finished flow (base + r where
+// max(|r_u|, |r_v|) <= max_residual, else base).  Every mbarrier wait is
+// bounded; a wait that runs out stops all roles and sets the device timeout
+// flag.
 #include "vsc_internal.h"
 #include "vsc_math.cuh"
 #include "vsc_ptx.cuh"
@@ -45,24 +52,27 @@ namespace vsc {
 namespace {
 
 constexpr int kUpM = 128;                // output positions per segment (MMA M, Tensor Memory lanes)
+constexpr int kUpGR = 8;                 // output rows per accumulator group
 constexpr int kUpRC = 16;                // output rows per work item
+constexpr int kUpGPI = kUpRC / kUpGR;    // groups per work item
 constexpr int kUpRows = kUpRC + 2;       // input rows per work item
 constexpr int kUpTW = kUpM + 2;          // positions loaded per row (one-pixel halo)
-constexpr int kUpRowBufs = 16;           // row buffers in shared memory (TMA loads in flight)
-constexpr int kUpSlots = 5;              // input-row accumulators in Tensor Memory
-constexpr int kUpSlotCols = 96;          // columns per accumulator (3 x 32)
+constexpr int kUpRowBufs = 22;           // row buffers in shared memory (more than an item's 18 rows)
+constexpr int kUpSlots = 2;              // group accumulators in Tensor Memory
 constexpr uint32_t kUpTmemCols = 512;
-constexpr int kUpGroups = 2;             // epilogue groups (output rows alternate between them)
-constexpr int kUpEpiWarps = 8;           // warps per group: 4 lane quarters x 2 channel halves
+constexpr int kUpEpiWarps = 16;          // 4 lane quarters x 4 pairs of a group's rows
 constexpr int kUpWaitSpins = 1 << 22;    // bounded mbarrier waits (about a second)
-constexpr int kUpThreads = (2 + kUpEpiWarps * kUpGroups) * 32;
+constexpr int kUpThreads = (2 + kUpEpiWarps) * 32;
 constexpr int kUpPlaneBytes = kUpTW * 16;  // one chunk plane of a row buffer
+constexpr uint32_t kUpZeroBytes = 8192;  // zero operands of the slot-clearing MMA (A 4 KB, B 8 KB overlapped)
 constexpr int kUpSmemLimit = 232448;
 constexpr uint32_t kUpMinSmem = 120 * 1024;
-static_assert(kUpSlots >= kUpGroups + 2 && kUpSlots * kUpSlotCols <= static_cast<int>(kUpTmemCols),
-    "accumulator ring");
+static_assert(kUpRC % kUpGR == 0 && kUpEpiWarps == 4 * (kUpGR / 2), "epilogue rows");
+static_assert(kUpRowBufs >= kUpGR + 4, "row buffers for a group and the next loads");
 
 __host__ __device__ constexpr uint32_t up_align1k(uint32_t v) { return (v + 1023u) & ~1023u; }
+// a row buffer: the TMA destination and the MMA operands need 128-byte alignment
+__host__ __device__ constexpr uint32_t up_row_bytes(int kch) { return (kch * kUpPlaneBytes + 127u) & ~127u; }
 
 // Per-layer shape: kch K chunks of 8 channels (lch of them loaded, the rest
 // zero), no output channels per vertical tap in the MMA (N = 3 no).
@@ -77,13 +87,14 @@ constexpr size_t kTcWeightBytes = 55296;
 __host__ __device__ constexpr uint32_t up_weight_bytes(int kch, int no) { return 3u * kch * 3u * no * 16u; }
 static_assert(kTcLayers[3].wt_off + up_weight_bytes(4, 16) == kTcWeightBytes, "packed weight layout");
 
-// row buffers, weights, bias, barriers (full / empty per row buffer, full / empty per
-// slot, the drain barrier, the Tensor Memory address and the abort flag)
+// row buffers, weights, the zero operands, bias, barriers (full / empty per row
+// buffer, full / empty per slot, the drain barrier, the Tensor Memory address and
+// the abort flag)
 constexpr uint32_t kBarBytes = (2 * kUpRowBufs + 2 * kUpSlots + 3) * 8;
 __host__ __device__ constexpr uint32_t up_smem_bytes(int kch, int no)
 {
-    return 1024 + kUpRowBufs * up_align1k(kch * kUpPlaneBytes) + up_align1k(up_weight_bytes(kch, no)) + 32 * 4 +
-           kBarBytes;
+    return 1024 + up_align1k(kUpRowBufs * up_row_bytes(kch)) + up_align1k(up_weight_bytes(kch, no)) +
+           kUpZeroBytes + 32 * 4 + kBarBytes;
 }
 
 // Bounded wait that also gives up when another role has aborted; a wait that
@@ -111,18 +122,25 @@ __global__ void __launch_bounds__(kUpThreads, 1)
         float* __restrict__ flow, int64_t s_out, float max_residual, int N, int H, int W,
         int* __restrict__ timeout_flag)
 {
-    constexpr int N3 = 3 * NO;                    // MMA N: the three vertical taps
-    constexpr int KH = 16;                        // output channels per epilogue warp (half of 32)
-    constexpr uint32_t kRowBytes = up_align1k(KCH * kUpPlaneBytes);
+    constexpr int N3 = 3 * NO;                      // the weights' N rows: three vertical taps
+    constexpr int kSlotCols = kUpGR * NO;           // one group's accumulator
+    constexpr uint32_t kRowBytes = up_row_bytes(KCH);
     constexpr uint32_t kWBytes = up_weight_bytes(KCH, NO);
-    constexpr uint32_t idesc = ptx::umma_idesc_f16(false, kUpM, N3);
-    static_assert(N3 <= kUpSlotCols && N3 % 16 == 0, "MMA N");
+    constexpr uint32_t idesc1 = ptx::umma_idesc_f16(false, kUpM, NO);
+    constexpr uint32_t idesc2 = ptx::umma_idesc_f16(false, kUpM, 2 * NO);
+    constexpr uint32_t idesc3 = ptx::umma_idesc_f16(false, kUpM, N3);
+    constexpr uint32_t idesc0 = ptx::umma_idesc_f16(false, kUpM, kSlotCols);
+    static_assert(NO % 16 == 0 && kSlotCols <= 256 && kUpSlots * kSlotCols <= static_cast<int>(kUpTmemCols),
+        "MMA N and the accumulator ring");
+    static_assert(2 * 2048 <= kUpZeroBytes && 2 * kSlotCols * 16 <= static_cast<int>(kUpZeroBytes),
+        "zero operands (A: 128 x 16, B: kSlotCols x 16 halves)");
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base =
         reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
     unsigned char* rows = base;
-    unsigned char* wts = rows + kUpRowBufs * kRowBytes;
-    float* sbias = reinterpret_cast<float*>(wts + up_align1k(kWBytes));
+    unsigned char* wts = rows + up_align1k(kUpRowBufs * kRowBytes);
+    unsigned char* zero = wts + up_align1k(kWBytes);
+    float* sbias = reinterpret_cast<float*>(zero + kUpZeroBytes);
     uint64_t* bars = reinterpret_cast<uint64_t*>(sbias + 32);
     uint64_t* full = bars;                        // [kUpRowBufs]
     uint64_t* empty = full + kUpRowBufs;          // [kUpRowBufs]
@@ -136,9 +154,12 @@ __global__ void __launch_bounds__(kUpThreads, 1)
     const int nseg = (W + kUpM - 1) / kUpM, nchunk = (H + kUpRC - 1) / kUpRC;
     const int items = N * nchunk * nseg;
 
-    // weights and bias into shared memory; the K chunks that are never loaded are zero
+    // weights and bias into shared memory; the zero operands and the K chunks that
+    // are never loaded are zero
     for (uint32_t i = threadIdx.x; i < kWBytes / 16; i += blockDim.x)
         reinterpret_cast<uint4*>(wts)[i] = wpk[i];
+    for (uint32_t i = threadIdx.x; i < kUpZeroBytes / 16; i += blockDim.x)
+        reinterpret_cast<uint4*>(zero)[i] = make_uint4(0u, 0u, 0u, 0u);
     for (int i = threadIdx.x; i < 32; i += blockDim.x)
         sbias[i] = i < co ? bias[i] : 0.0f;
     if (LCH < KCH) {
@@ -161,9 +182,7 @@ __global__ void __launch_bounds__(kUpThreads, 1)
         }
         for (int i = 0; i < kUpSlots; ++i) {
             ptx::mbar_init(&sfull[i], 1);
-            // every input row is released by three output rows' eight warps (rows at an
-            // item's edge, read fewer times, are topped up by one of their readers)
-            ptx::mbar_init(&sempty[i], 3 * kUpEpiWarps);
+            ptx::mbar_init(&sempty[i], kUpEpiWarps);  // every epilogue warp reads each group once
         }
         ptx::mbar_init(drain, 1);
     }
@@ -172,8 +191,9 @@ __global__ void __launch_bounds__(kUpThreads, 1)
     ptx::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    // input rows are counted over the whole CTA (u): row buffer u % kUpRowBufs,
-    // Tensor Memory slot u % kUpSlots; item k of the CTA owns rows k * kUpRows ...
+    // input rows are counted over the whole CTA (u): row buffer u % kUpRowBufs; item
+    // k of the CTA owns rows k * kUpRows ...; groups are counted over the CTA (G):
+    // Tensor Memory slot G % kUpSlots
     if (warp == 0) {
         // ---- TMA producer -------------------------------------------------------------
         if (lane == 0) {
@@ -200,35 +220,55 @@ __global__ void __launch_bounds__(kUpThreads, 1)
     } else if (warp == 1) {
         // ---- MMA issuer ---------------------------------------------------------------
         if (lane == 0) {
-            int u = 0;
+            int u0 = 0, G = 0;
             bool ok = true;
             // Descriptors are built once; an operand at byte offset d from its base is
             // the base descriptor + d / 16 (the start-address field, which cannot carry:
-            // shared memory stays below 256 KB).  The offsets below are compile-time
-            // constants, so an MMA costs two 64-bit adds to issue.
+            // shared memory stays below 256 KB).
             const uint64_t adesc0 = ptx::umma_desc_kmajor(ptx::smem_u32(rows), kUpPlaneBytes, 128);
             const uint64_t bdesc0 = ptx::umma_desc_kmajor(ptx::smem_u32(wts), N3 * 16, 128);
-            for (int it = blockIdx.x; ok && it < items; it += gridDim.x) {
-                for (int i = 0; i < kUpRows; ++i, ++u) {
-                    const int b = u % kUpRowBufs, sl = u % kUpSlots;
-                    if (!(ok = up_wait(&full[b], (u / kUpRowBufs) & 1, abort)))
-                        break;
-                    if (!(ok = up_wait(&sempty[sl], ((u / kUpSlots) & 1) ^ 1, abort)))
+            const uint64_t zadesc = ptx::umma_desc_kmajor(ptx::smem_u32(zero), 2048, 128);
+            const uint64_t zbdesc = ptx::umma_desc_kmajor(ptx::smem_u32(zero), kSlotCols * 16, 128);
+            for (int it = blockIdx.x; ok && it < items; it += gridDim.x, u0 += kUpRows) {
+                for (int g = 0; ok && g < kUpGPI; ++g, ++G) {
+                    const int sl = G % kUpSlots, gb = g * kUpGR;
+                    if (!(ok = up_wait(&sempty[sl], ((G / kUpSlots) & 1) ^ 1, abort)))
                         break;
                     ptx::tc_fence_after();
-                    const uint64_t ab = adesc0 + ((b * kRowBytes) >> 4);
-                    const uint32_t dcol = tmem + sl * kUpSlotCols;
+                    const uint32_t dslot = tmem + sl * kSlotCols;
+                    ptx::umma_f16(dslot, zadesc, zbdesc, idesc0, false);  // clear the group's accumulator
+                    // the group's output rows gb ... gb + 7 read item input rows gb ... gb + 9
+                    for (int i = gb; i <= gb + kUpGR + 1; ++i) {
+                        const int u = u0 + i, b = u % kUpRowBufs;
+                        if (!(ok = up_wait(&full[b], (u / kUpRowBufs) & 1, abort)))
+                            break;
+                        ptx::tc_fence_after();
+                        // input row i feeds output row t = i - ty - gb for ty = 0, 1, 2 where
+                        // 0 <= t < kUpGR: ty_lo ... ty_hi, at columns NO (kUpGR - 1 - t)
+                        const int r = i - gb;
+                        const int ty_lo = r > kUpGR - 1 ? r - (kUpGR - 1) : 0;
+                        const int ty_hi = r < 2 ? r : 2;
+                        const int nt = ty_hi - ty_lo + 1;
+                        const uint32_t idesc = nt == 3 ? idesc3 : (nt == 2 ? idesc2 : idesc1);
+                        const uint32_t dcol = dslot + NO * (kUpGR - 1 - r + ty_lo);
+                        const uint64_t ab = adesc0 + ((b * kRowBytes) >> 4);
+                        const uint64_t bb = bdesc0 + ((ty_lo * NO * 16) >> 4);
 #pragma unroll
-                    for (int tx = 0; tx < 3; ++tx) {
+                        for (int tx = 0; tx < 3; ++tx) {
 #pragma unroll
-                        for (int k = 0; k < KCH / 2; ++k) {
-                            const uint64_t ad = ab + ((2 * k * kUpPlaneBytes + tx * 16) >> 4);
-                            const uint64_t bd = bdesc0 + (((tx * KCH + 2 * k) * N3 * 16) >> 4);
-                            ptx::umma_f16(dcol, ad, bd, idesc, tx > 0 || k > 0);
+                            for (int k = 0; k < KCH / 2; ++k) {
+                                const uint64_t ad = ab + ((2 * k * kUpPlaneBytes + tx * 16) >> 4);
+                                const uint64_t bd = bb + (((tx * KCH + 2 * k) * N3 * 16) >> 4);
+                                ptx::umma_f16(dcol, ad, bd, idesc, true);
+                            }
                         }
+                        // a row buffer is freed after its last group: the next group of
+                        // the item re-reads the two rows from gb + kUpGR on
+                        if (g == kUpGPI - 1 || i < gb + kUpGR)
+                            ptx::umma_commit(&empty[b]);
                     }
-                    ptx::umma_commit(&sfull[sl]);  // row accumulator ready
-                    ptx::umma_commit(&empty[b]);   // row buffer read
+                    if (ok)
+                        ptx::umma_commit(&sfull[sl]);  // the group's accumulator is complete
                 }
             }
             if (*abort) {  // the MMAs in flight finish before Tensor Memory is freed
@@ -237,77 +277,67 @@ __global__ void __launch_bounds__(kUpThreads, 1)
             }
         }
     } else {
-        // ---- epilogue: three row accumulators -> registers -> global ----------------------
+        // ---- epilogue: a group accumulator -> registers -> global -----------------------
         const int e = warp - 2;
         const int q = warp & 3;                   // this warp's 32 Tensor Memory lanes
-        const int half = (e >> 2) & 1;            // output channels half * 16 ... + 15
-        const int grp = e >> 3;                   // output rows i with i % kUpGroups == grp
-        const bool active = !kFinish || half == 0;  // the last layer has two output channels
+        const int rp = e >> 2;                    // its rows of a group: 2 rp, 2 rp + 1
         const uint32_t lane_base = static_cast<uint32_t>(q * 32) << 16;
         const int64_t HW = static_cast<int64_t>(H) * W;
-        int u0 = 0;  // the item's first input row
+        int G = 0;
         bool ok = true;
-        for (int it = blockIdx.x; ok && it < items; it += gridDim.x, u0 += kUpRows) {
+        for (int it = blockIdx.x; ok && it < items; it += gridDim.x) {
             const int seg = it % nseg, rest = it / nseg;
             const int chunk = rest % nchunk, n = rest / nchunk;
             const int x = seg * kUpM + q * 32 + lane;
-            for (int i = grp; i < kUpRC; i += kUpGroups) {
-                // output row y = chunk * kUpRC + i reads input rows u0 + i + ty, ty = 0, 1, 2
-                for (int ty = 0; ty < 3 && ok; ++ty) {
-                    const int v = u0 + i + ty;
-                    // warp-uniform outcome: the Tensor Memory loads below are warp-collective
-                    ok = __all_sync(0xffffffffu, up_wait(&sfull[v % kUpSlots], (v / kUpSlots) & 1, abort));
-                }
+            for (int g = 0; g < kUpGPI; ++g, ++G) {
+                const int sl = G % kUpSlots;
+                // warp-uniform outcome: the Tensor Memory loads below are warp-collective
+                ok = __all_sync(0xffffffffu, up_wait(&sfull[sl], (G / kUpSlots) & 1, abort));
                 if (!ok)
                     break;
                 ptx::tc_fence_after();
-                float acc[KH];
-                if (active) {
-                    const uint32_t c0 = half * KH;
-                    const uint32_t ta0 = tmem + lane_base + ((u0 + i) % kUpSlots) * kUpSlotCols + c0;
-                    const uint32_t ta1 = tmem + lane_base + ((u0 + i + 1) % kUpSlots) * kUpSlotCols + NO + c0;
-                    const uint32_t ta2 = tmem + lane_base + ((u0 + i + 2) % kUpSlots) * kUpSlotCols + 2 * NO + c0;
-                    uint32_t r0[16], r1[16], r2[16];
-                    ptx::tmem_ld16(ta0, r0);
-                    ptx::tmem_ld16(ta1, r1);
-                    ptx::tmem_ld16(ta2, r2);
+                constexpr int KC = kFinish ? 16 : 32;  // columns read per row (the last layer needs 2 of 16)
+                float acc[2][KC];
+#pragma unroll
+                for (int r = 0; r < 2; ++r) {
+                    const int t = 2 * rp + r;
+                    const uint32_t ta = tmem + lane_base + sl * kSlotCols + NO * (kUpGR - 1 - t);
+                    uint32_t v[KC];
+                    if constexpr (KC == 32)
+                        ptx::tmem_ld32(ta, v);
+                    else
+                        ptx::tmem_ld16(ta, v);
                     ptx::tmem_ld_wait();
 #pragma unroll
-                    for (int o = 0; o < KH; ++o)
-                        acc[o] = (__uint_as_float(r0[o]) + __uint_as_float(r1[o])) + __uint_as_float(r2[o]);
+                    for (int o = 0; o < KC; ++o)
+                        acc[r][o] = __uint_as_float(v[o]);
                 }
                 ptx::tc_fence_before();
                 __syncwarp();
-                if (lane == 0) {
-                    // item row k = i + ty is read by outputs k - 2 ... k inside [0, kUpRC); its
-                    // reader i = min(k, kUpRC - 1) adds the arrivals of the readers it lacks
+                if (lane == 0)
+                    ptx::mbar_arrive(&sempty[sl]);
 #pragma unroll
-                    for (int ty = 0; ty < 3; ++ty) {
-                        const int k = i + ty;
-                        const int readers = min(k, kUpRC - 1) - max(k - 2, 0) + 1;
-                        const uint32_t cnt = 1u + (i == min(k, kUpRC - 1) ? static_cast<uint32_t>(3 - readers) : 0u);
-                        ptx::mbar_arrive_n(&sempty[(u0 + k) % kUpSlots], cnt);
-                    }
-                }
-                const int y = chunk * kUpRC + i;
-                if (active && x < W && y < H) {
+                for (int r = 0; r < 2; ++r) {
+                    const int y = chunk * kUpRC + g * kUpGR + 2 * rp + r;
+                    if (x >= W || y >= H)
+                        continue;
                     const int64_t p = static_cast<int64_t>(y) * W + x;
                     if (!kFinish) {
 #pragma unroll
-                        for (int c = 0; c < KH / 8; ++c) {
+                        for (int c = 0; c < 4; ++c) {
                             uint32_t h[4];
 #pragma unroll
                             for (int j = 0; j < 4; ++j) {
-                                const int o = c * 8 + 2 * j, og = half * KH + o;
-                                const __half2 hv = __floats2half2_rn(fmaxf(acc[o] + sbias[og], 0.0f),
-                                    fmaxf(acc[o + 1] + sbias[og + 1], 0.0f));
+                                const int o = c * 8 + 2 * j;
+                                const __half2 hv = __floats2half2_rn(fmaxf(acc[r][o] + sbias[o], 0.0f),
+                                    fmaxf(acc[r][o + 1] + sbias[o + 1], 0.0f));
                                 h[j] = *reinterpret_cast<const uint32_t*>(&hv);
                             }
-                            reinterpret_cast<uint4*>(out)[(static_cast<int64_t>(n) * 4 + half * 2 + c) * HW + p] =
+                            reinterpret_cast<uint4*>(out)[(static_cast<int64_t>(n) * 4 + c) * HW + p] =
                                 make_uint4(h[0], h[1], h[2], h[3]);
                         }
                     } else {
-                        const float ru = acc[0] + sbias[0], rv = acc[1] + sbias[1];
+                        const float ru = acc[r][0] + sbias[0], rv = acc[r][1] + sbias[1];
                         const float* in = input + (static_cast<int64_t>(n) * HW + p) * 3;
                         const bool take = fmaxf(fabsf(ru), fabsf(rv)) <= max_residual;
                         float* o = flow + n * s_out + p * 3;
