@@ -330,9 +330,11 @@ VSC_API vsc_hyper_params* vsc_stabilizer_hyper_params(vsc_stabilizer* s);
  * RGBA8 original and per-frame processed images, width x height x 4, on the
  * host (on_device = 0) or device.  Pageable host frames are copied before the
  * call returns; pinned host frames and device frames are read asynchronously
- * on the stabilizer's stream, so keep them unchanged until that stream has
- * passed the load (a later vsc_stabilizer_step with a host output, or a
- * stream synchronisation). */
+ * (host frames on a copy stream of the stabilizer, so the upload overlaps the
+ * work already enqueued; the stabilizer's stream waits for it), so keep them
+ * unchanged until the stabilizer's stream has passed the load (a later
+ * vsc_stabilizer_step with a synchronous host output, or
+ * vsc_stabilizer_synchronize). */
 VSC_API vsc_status vsc_stabilizer_load_frame(vsc_stabilizer* s, const uint8_t* orig_rgba, const uint8_t* proc_rgba,
     int32_t on_device);
 
@@ -343,10 +345,18 @@ VSC_API vsc_status vsc_stabilizer_set_flows(vsc_stabilizer* s, const float* fwd,
     int32_t on_device);
 
 /* One frame: doOneStep (videostabilizer.cpp:167-265) for the middle frame of
- * the 3-frame window; writes its RGBA8 stabilized image to out_rgba (host or
- * device), keeps the FP32 result as the next step's previous stabilized
- * frame, and drops the oldest frame from the window. */
+ * the 3-frame window; writes its RGBA8 stabilized image to out_rgba, keeps
+ * the FP32 result as the next step's previous stabilized frame, and drops
+ * the oldest frame from the window.  out_on_device: 1 = device pointer
+ * (stream-ordered); 0 = host pointer, copied before the call returns (the
+ * stream is synchronised); VSC_OUT_HOST_ASYNC = host pointer, the copy is
+ * enqueued on the stabilizer's stream and the call returns at once: read
+ * out_rgba after vsc_stabilizer_synchronize (with page-locked memory the
+ * copy overlaps the caller's next load_frame and step). */
+#define VSC_OUT_HOST_ASYNC 2
 VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int32_t out_on_device);
+/* Waits until everything enqueued on the stabilizer's stream has finished. */
+VSC_API vsc_status vsc_stabilizer_synchronize(vsc_stabilizer* s);
 
 /* Device pointers to internal state, for inspection (valid until the next call):
  * which = 0: last stabilized frame (float HWC3), 1: forward flow, 2: backward flow

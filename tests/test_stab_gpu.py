@@ -254,6 +254,39 @@ def test_stabilizer_graph_replay_side_stream(vsc, oracle, cuda, use_graphs):
     st.close()
 
 
+def test_stabilizer_async_host_output_and_pinned_uploads(vsc, cuda):
+    """Results copied back with VSC_OUT_HOST_ASYNC into pinned memory while
+    the next frames upload from pinned memory on the copy stream (the host
+    two steps ahead) equal the synchronous host path's bytes; an unknown
+    output mode is rejected."""
+    import torch
+
+    w, h = 96, 64
+    fr = _frames(w, h, 9, seed=31)
+    pin = [(torch.from_numpy(o).pin_memory(), torch.from_numpy(p).pin_memory()) for o, p in fr]
+    ref_st, st = vsc.Stabilizer(w, h), vsc.Stabilizer(w, h)
+    for i in range(3):
+        ref_st.load_frame(*fr[i])
+        st.load_frame(pin[i][0].numpy(), pin[i][1].numpy())
+    refs = []
+    for t in range(6):
+        out = np.empty((h, w, 4), np.uint8)
+        ref_st.step(torch.from_numpy(out))
+        refs.append(out.copy())
+        ref_st.load_frame(*fr[t + 3])
+    outs = [torch.empty((h, w, 4), dtype=torch.uint8).pin_memory() for _ in range(6)]
+    for t in range(6):
+        st.step(outs[t], asynchronous=True)
+        st.load_frame(pin[t + 3][0].numpy(), pin[t + 3][1].numpy())
+    st.synchronize()
+    for t in range(6):
+        assert np.array_equal(outs[t].numpy(), refs[t]), t
+    with pytest.raises(vsc.VscError, match="out_on_device"):
+        vsc._check(vsc.load().vsc_stabilizer_step(st._h, outs[0].data_ptr(), 3))
+    st.close()
+    ref_st.close()
+
+
 def test_stabilizer_external_flows_host_io(vsc, oracle, cuda):
     """File mode (-f): 2-channel flows supplied per step, host frames in/out."""
     import torch

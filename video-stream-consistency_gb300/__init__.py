@@ -46,8 +46,10 @@ EXPORTED = [
     "vsc_upsampler_set_max_residual", "vsc_upsampler_prepare", "vsc_upsampler_train_step", "vsc_upsampler_apply",
     "vsc_stabilizer_set_upsampler", "vsc_solver_autotune", "vsc_solver_tile_rows", "vsc_solver_set_autotune",
     "vsc_multistream_set_fused", "vsc_multistream_fused", "vsc_multistream_set_upsampler",
+    "vsc_stabilizer_synchronize",
 ]
 VSC_DTYPE_F32, VSC_DTYPE_BF16, VSC_DTYPE_F16 = 0, 1, 2
+VSC_OUT_HOST_ASYNC = 2
 NOALLOC_MAX_PIXELS = 349525  # VSC_NOALLOC_MAX_PIXELS
 
 
@@ -166,6 +168,7 @@ def load():
         "vsc_multistream_load_frames": [vp, C.POINTER(vp), C.POINTER(vp), i32],
         "vsc_multistream_step": [vp, C.POINTER(vp), i32],
         "vsc_multistream_set_fused": [vp, i32],
+        "vsc_stabilizer_synchronize": [vp],
         "vsc_multistream_set_upsampler": [vp, i32, vp],
         "vsc_get_adap_comb_masked": [IP] * 10 + [f32, vp],
         "vsc_stabilizer_set_occlusion_mask": [vp, i32],
@@ -589,14 +592,20 @@ class Stabilizer:
     def set_flows(self, fwd, bwd):
         _check(load().vsc_stabilizer_set_flows(self._h, fwd.data_ptr(), bwd.data_ptr(), 1 if fwd.is_cuda else 0))
 
-    def step(self, out=None):
-        """Stabilize the window's middle frame; returns the RGBA result."""
+    def step(self, out=None, asynchronous: bool = False):
+        """Stabilize the window's middle frame; returns the RGBA result.  With
+        a host tensor and asynchronous=True the copy back is only enqueued
+        (VSC_OUT_HOST_ASYNC): read `out` after synchronize()."""
         import torch
 
         if out is None:
             out = torch.empty((self.height, self.width, 4), dtype=torch.uint8, device="cuda")
-        _check(load().vsc_stabilizer_step(self._h, out.data_ptr(), 1 if out.is_cuda else 0))
+        mode = 1 if out.is_cuda else (VSC_OUT_HOST_ASYNC if asynchronous else 0)
+        _check(load().vsc_stabilizer_step(self._h, out.data_ptr(), mode))
         return out
+
+    def synchronize(self):
+        _check(load().vsc_stabilizer_synchronize(self._h))
 
     def buffer(self, which: int, channels: int = 3):
         """Copy of internal state: 0 last stabilized, 1 fwd flow, 2 bwd flow, 3 adapCmbPr, 4 consWt."""

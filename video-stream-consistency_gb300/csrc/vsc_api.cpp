@@ -639,6 +639,10 @@ struct vsc_stabilizer {
     bool flows_set = false;
 
     uint8_t* stage[2] = {};  // device staging for host RGBA uploads
+    // host uploads run on a copy stream: staged[k] = stage[k] filled,
+    // consumed[k] = its conversion done (the next upload into it waits)
+    cudaStream_t cst = nullptr;
+    cudaEvent_t staged[2] = {}, consumed[2] = {};
     uint8_t* out_rgba = nullptr;
     float* small = nullptr;  // frame resized to the flow size (downscale mode)
     float* flow_fwd = nullptr;
@@ -758,6 +762,17 @@ void free_all(vsc_stabilizer* s)
             cudaEventDestroy(e);
             e = nullptr;
         }
+    for (int k = 0; k < 2; ++k) {
+        if (s->staged[k])
+            cudaEventDestroy(s->staged[k]);
+        if (s->consumed[k])
+            cudaEventDestroy(s->consumed[k]);
+        s->staged[k] = s->consumed[k] = nullptr;
+    }
+    if (s->cst) {
+        cudaStreamDestroy(s->cst);
+        s->cst = nullptr;
+    }
     for (auto& g : s->graphs)
         if (g.exec) {
             cudaGraphExecDestroy(g.exec);
@@ -780,6 +795,11 @@ vsc_status alloc_all(vsc_stabilizer* s)
     }
     A(dalloc(&s->stage[0], static_cast<size_t>(s->w) * s->h * 4));
     A(dalloc(&s->stage[1], static_cast<size_t>(s->w) * s->h * 4));
+    A(cudaStreamCreateWithFlags(&s->cst, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+        A(cudaEventCreateWithFlags(&s->staged[k], cudaEventDisableTiming));
+        A(cudaEventCreateWithFlags(&s->consumed[k], cudaEventDisableTiming));
+    }
     A(dalloc(&s->out_rgba, static_cast<size_t>(s->w) * s->h * 4));
     // forward and backward flow contiguous: the estimator writes both in one launch
     A(dalloc(&s->flow_fwd, 2 * static_cast<size_t>(s->w) * s->h * s->fc));
@@ -931,14 +951,24 @@ VSC_API vsc_status vsc_stabilizer_load_frame(vsc_stabilizer* s, const uint8_t* o
     for (int k = 0; k < 2; ++k) {
         const uint8_t* dsrc = src[k];
         if (!on_device) {
-            vsc_status st = check_cuda(cudaMemcpyAsync(s->stage[k], src[k], static_cast<size_t>(npix) * 4,
-                                           cudaMemcpyHostToDevice, s->st),
-                "load_frame upload");
+            // upload on the copy stream once the previous conversion has read
+            // the staging buffer; the stabilizer's stream waits for the upload
+            vsc_status st = check_cuda(cudaStreamWaitEvent(s->cst, s->consumed[k], 0), "load_frame upload");
+            if (!st)
+                st = check_cuda(cudaMemcpyAsync(s->stage[k], src[k], static_cast<size_t>(npix) * 4,
+                                    cudaMemcpyHostToDevice, s->cst),
+                    "load_frame upload");
+            if (!st)
+                st = check_cuda(cudaEventRecord(s->staged[k], s->cst), "load_frame upload");
+            if (!st)
+                st = check_cuda(cudaStreamWaitEvent(s->st, s->staged[k], 0), "load_frame upload");
             if (st)
                 return st;
             dsrc = s->stage[k];
         }
         vsc_status st = check_cuda(launch_rgba_to_float(dsrc, dst[k], npix, s->st), "load_frame convert");
+        if (!st && !on_device)
+            st = check_cuda(cudaEventRecord(s->consumed[k], s->st), "load_frame convert");
         if (st)
             return st;
         ++nl;
@@ -1275,10 +1305,12 @@ VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int
         return set_error(VSC_EINVAL, "step: pyramid_levels %d outside [1, %d]", L, s->levels_alloc);
     if (hp.num_iter < 0)
         return set_error(VSC_EINVAL, "step: negative num_iter");
-    if (out_rgba && out_on_device && (reinterpret_cast<uintptr_t>(out_rgba) & 3))
+    if (out_on_device < 0 || out_on_device > VSC_OUT_HOST_ASYNC)
+        return set_error(VSC_EINVAL, "step: out_on_device %d is not 0, 1 or VSC_OUT_HOST_ASYNC", out_on_device);
+    if (out_rgba && out_on_device == 1 && (reinterpret_cast<uintptr_t>(out_rgba) & 3))
         return set_error(VSC_EINVAL, "step: device output must be 4-byte aligned");
     DeviceGuard g(s->device);
-    uint8_t* rgba_dev = (out_rgba && out_on_device) ? out_rgba : s->out_rgba;
+    uint8_t* rgba_dev = (out_rgba && out_on_device == 1) ? out_rgba : s->out_rgba;
     int nl = 0;
     cudaError_t e = cudaSuccess;
     // The first step (which seeds the feedback frame) runs directly; later
@@ -1292,15 +1324,24 @@ VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int
     if (stt)
         return stt;
     finish_step(s, nl);
-    if (out_rgba && !out_on_device) {
+    if (out_rgba && out_on_device != 1) {
         stt = check_cuda(cudaMemcpyAsync(out_rgba, s->out_rgba, static_cast<size_t>(s->w) * s->h * 4,
                              cudaMemcpyDeviceToHost, s->st),
             "step download");
-        if (stt)
+        if (stt || out_on_device == VSC_OUT_HOST_ASYNC)
             return stt;
         return check_cuda(cudaStreamSynchronize(s->st), "step synchronize");
     }
     return VSC_OK;
+}
+
+VSC_API vsc_status vsc_stabilizer_synchronize(vsc_stabilizer* s)
+{
+    clear_error();
+    if (!s)
+        return set_error(VSC_EINVAL, "synchronize: null stabilizer");
+    DeviceGuard g(s->device);
+    return check_cuda(cudaStreamSynchronize(s->st), "synchronize");
 }
 
 VSC_API vsc_status vsc_stabilizer_buffer(vsc_stabilizer* s, int32_t which, const float** dev_ptr)

@@ -1174,15 +1174,21 @@ cudaError_t solver_group_autotune(const int* w, const int* h, int n, cudaStream_
             mem[s].push_back(m);
         }
     }
+    // the kernel instantiation the solves will use: one problem, up to 4, up to 16 per launch
+    auto launch = [&](const std::vector<GroupMember>& m, int rows, int num_iter, int* nl) {
+        return n == 1 ? launch_members<1>(m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT)
+             : n <= 4 ? launch_members<4>(m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT)
+                      : launch_members<kGroupMax>(m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT);
+    };
     for (int round = 0; round < 3 && e == cudaSuccess; ++round) {
         for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
             int nl = 0;
             // a warm-up launch, then two timed ones, all of kTbT steps with momentum
-            e = launch_members<kGroupMax>(mem[s], shapes[s], 2 * kTbT, 0.15f, 0.15f, di->sms, st, &nl, kTbT);
+            e = launch(mem[s], shapes[s], 2 * kTbT, &nl);
             if (e == cudaSuccess)
                 e = cudaEventRecord(ev[0], st);
             if (e == cudaSuccess)
-                e = launch_members<kGroupMax>(mem[s], shapes[s], 3 * kTbT, 0.15f, 0.15f, di->sms, st, &nl, kTbT);
+                e = launch(mem[s], shapes[s], 3 * kTbT, &nl);
             float ms = 0.0f;
             if (e == cudaSuccess)
                 e = cudaEventRecord(ev[1], st);
