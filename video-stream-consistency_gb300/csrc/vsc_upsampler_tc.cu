@@ -20,11 +20,12 @@
 // the epilogue of the other: the layer is bound by HBM, not by the
 // accumulator ring.
 //
-// A work item is a segment of kUpRC = 16 output rows (two groups); its 18
-// input rows stream through a ring of row buffers (one TMA box {8, 130, 1,
-// chunks} per row: the segment with its one-pixel halo, zero-filled outside
-// the image, which is the convolution's zero padding).  The two rows the
-// groups share are released after the second group's MMAs.  The A operand is
+// A work item is a segment of kUpRC = 16 output rows (two groups); each
+// group's ten input rows stream through a ring of row buffers (one TMA box
+// {8, 130, 1, chunks} per row: the segment with its one-pixel halo,
+// zero-filled outside the image, which is the convolution's zero padding);
+// the two rows the groups share are loaded for each, so that every buffer has
+// one reader.  The A operand is
 // a row buffer seen from position tx (8 positions x 16 bytes per core
 // matrix, M-adjacent core matrices 128 bytes apart, K-adjacent ones a chunk
 // plane apart).  Weights [tx][chunk][ty * NO + o][8] (FP16, output channels
@@ -32,9 +33,11 @@
 // launch.  The first layer's three input channels (base flow u, v and luma)
 // occupy one chunk; its second K chunk is a zero plane that is never loaded.
 //
-// Persistent and warp-specialised: warp 0 issues the TMA loads, warp 1 the
-// MMAs (and owns Tensor Memory), then sixteen epilogue warps: four per 32
-// Tensor Memory lanes, each taking two output rows of a group.  Epilogue:
+// Persistent and warp-specialised: warp 0 issues the TMA loads; warp 1 (which
+// owns Tensor Memory) issues the MMAs of every item's first group and warp 18
+// those of its second (one thread issues an MMA about every 90 cycles, twice
+// the tensor pipe's time for these shapes); warps 2-17 are the epilogue, four
+// per 32 Tensor Memory lanes, each taking two output rows of a group.  Epilogue:
 // bias, ReLU, FP16 and the chunked store for the inner layers; for the last
 // layer the residual test and the finished flow (base + r where
 // max(|r_u|, |r_v|) <= max_residual, else base).  Every mbarrier wait is
@@ -55,20 +58,22 @@ constexpr int kUpM = 128;                // output positions per segment (MMA M,
 constexpr int kUpGR = 8;                 // output rows per accumulator group
 constexpr int kUpRC = 16;                // output rows per work item
 constexpr int kUpGPI = kUpRC / kUpGR;    // groups per work item
-constexpr int kUpRows = kUpRC + 2;       // input rows per work item
+constexpr int kUpGRows = kUpGR + 2;      // input rows per group
+constexpr int kUpLoads = kUpGPI * kUpGRows;  // row loads per work item (each group has its own)
 constexpr int kUpTW = kUpM + 2;          // positions loaded per row (one-pixel halo)
 constexpr int kUpRowBufs = 22;           // row buffers in shared memory (more than an item's 18 rows)
 constexpr int kUpSlots = 2;              // group accumulators in Tensor Memory
 constexpr uint32_t kUpTmemCols = 512;
 constexpr int kUpEpiWarps = 16;          // 4 lane quarters x 4 pairs of a group's rows
 constexpr int kUpWaitSpins = 1 << 22;    // bounded mbarrier waits (about a second)
-constexpr int kUpThreads = (2 + kUpEpiWarps) * 32;
+constexpr int kUpIssuerWarp1 = 2 + kUpEpiWarps;  // the second group's MMA issuer (the first: warp 1)
+constexpr int kUpThreads = (3 + kUpEpiWarps) * 32;
 constexpr int kUpPlaneBytes = kUpTW * 16;  // one chunk plane of a row buffer
 constexpr uint32_t kUpZeroBytes = 8192;  // zero operands of the slot-clearing MMA (A 4 KB, B 8 KB overlapped)
 constexpr int kUpSmemLimit = 232448;
 constexpr uint32_t kUpMinSmem = 120 * 1024;
 static_assert(kUpRC % kUpGR == 0 && kUpEpiWarps == 4 * (kUpGR / 2), "epilogue rows");
-static_assert(kUpRowBufs >= kUpGR + 4, "row buffers for a group and the next loads");
+static_assert(kUpRowBufs >= kUpLoads + 2 && kUpGPI == kUpSlots, "row buffers; one slot and issuer per group");
 
 __host__ __device__ constexpr uint32_t up_align1k(uint32_t v) { return (v + 1023u) & ~1023u; }
 // a row buffer: the TMA destination and the MMA operands need 128-byte alignment
@@ -90,7 +95,7 @@ static_assert(kTcLayers[3].wt_off + up_weight_bytes(4, 16) == kTcWeightBytes, "p
 // row buffers, weights, the zero operands, bias, barriers (full / empty per row
 // buffer, full / empty per slot, the drain barrier, the Tensor Memory address and
 // the abort flag)
-constexpr uint32_t kBarBytes = (2 * kUpRowBufs + 2 * kUpSlots + 3) * 8;
+constexpr uint32_t kBarBytes = (2 * kUpRowBufs + 3 * kUpSlots + 2) * 8;
 __host__ __device__ constexpr uint32_t up_smem_bytes(int kch, int no)
 {
     return 1024 + up_align1k(kUpRowBufs * up_row_bytes(kch)) + up_align1k(up_weight_bytes(kch, no)) +
@@ -146,9 +151,9 @@ __global__ void __launch_bounds__(kUpThreads, 1)
     uint64_t* empty = full + kUpRowBufs;          // [kUpRowBufs]
     uint64_t* sfull = empty + kUpRowBufs;         // [kUpSlots]
     uint64_t* sempty = sfull + kUpSlots;          // [kUpSlots]
-    uint64_t* drain = sempty + kUpSlots;          // the MMA issuer's last commit on abort
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
-    volatile int* abort = reinterpret_cast<volatile int*>(drain + 2);
+    uint64_t* drain = sempty + kUpSlots;          // [kUpSlots] each MMA issuer's last commit on abort
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + kUpSlots);
+    volatile int* abort = reinterpret_cast<volatile int*>(drain + kUpSlots + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nseg = (W + kUpM - 1) / kUpM, nchunk = (H + kUpRC - 1) / kUpRC;
@@ -183,17 +188,20 @@ __global__ void __launch_bounds__(kUpThreads, 1)
         for (int i = 0; i < kUpSlots; ++i) {
             ptx::mbar_init(&sfull[i], 1);
             ptx::mbar_init(&sempty[i], kUpEpiWarps);  // every epilogue warp reads each group once
+            ptx::mbar_init(&drain[i], 1);
         }
-        ptx::mbar_init(drain, 1);
     }
     ptx::tc_fence_before();
     __syncthreads();
     ptx::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    // input rows are counted over the whole CTA (u): row buffer u % kUpRowBufs; item
-    // k of the CTA owns rows k * kUpRows ...; groups are counted over the CTA (G):
-    // Tensor Memory slot G % kUpSlots
+    // row loads are counted over the whole CTA (u): row buffer u % kUpRowBufs; item
+    // k of the CTA owns loads k * kUpLoads ..., group g's ten input rows from
+    // k * kUpLoads + g * kUpGRows (the two rows the groups share are loaded for
+    // each).  Group g of every item is issued by its own thread (warp 1 for g = 0,
+    // warp kUpIssuerWarp1 for g = 1) into Tensor Memory slot g; the epilogue
+    // counts groups over the CTA (G), slot G % kUpSlots = g.
     if (warp == 0) {
         // ---- TMA producer -------------------------------------------------------------
         if (lane == 0) {
@@ -202,13 +210,13 @@ __global__ void __launch_bounds__(kUpThreads, 1)
             for (int it = blockIdx.x; ok && it < items; it += gridDim.x) {
                 const int seg = it % nseg, rest = it / nseg;
                 const int chunk = rest % nchunk, n = rest / nchunk;
-                for (int i = 0; i < kUpRows; ++i, ++u) {
+                for (int j = 0; j < kUpLoads; ++j, ++u) {
                     const int b = u % kUpRowBufs;
                     if (!(ok = up_wait(&empty[b], ((u / kUpRowBufs) & 1) ^ 1, abort)))
                         break;
+                    const int y = chunk * kUpRC - 1 + (j / kUpGRows) * kUpGR + j % kUpGRows;
                     ptx::mbar_expect_tx(&full[b], LCH * kUpPlaneBytes);
-                    ptx::tma_load_5d(rows + b * kRowBytes, &mIn, 0, seg * kUpM - 1, chunk * kUpRC - 1 + i, 0, n,
-                        &full[b]);
+                    ptx::tma_load_5d(rows + b * kRowBytes, &mIn, 0, seg * kUpM - 1, y, 0, n, &full[b]);
                 }
             }
             if (*abort)  // let every copy issued land before the CTA exits
@@ -217,10 +225,11 @@ __global__ void __launch_bounds__(kUpThreads, 1)
                     ptx::mbar_wait_bounded(&full[v % kUpRowBufs], (v / kUpRowBufs) & 1, kUpWaitSpins);
                 }
         }
-    } else if (warp == 1) {
-        // ---- MMA issuer ---------------------------------------------------------------
+    } else if (warp == 1 || warp == kUpIssuerWarp1) {
+        // ---- MMA issuers: group g of every item ------------------------------------------
         if (lane == 0) {
-            int u0 = 0, G = 0;
+            const int g = warp == 1 ? 0 : 1;
+            int m = 0;  // items done by this issuer (slot g's uses)
             bool ok = true;
             // Descriptors are built once; an operand at byte offset d from its base is
             // the base descriptor + d / 16 (the start-address field, which cannot carry:
@@ -229,51 +238,44 @@ __global__ void __launch_bounds__(kUpThreads, 1)
             const uint64_t bdesc0 = ptx::umma_desc_kmajor(ptx::smem_u32(wts), N3 * 16, 128);
             const uint64_t zadesc = ptx::umma_desc_kmajor(ptx::smem_u32(zero), 2048, 128);
             const uint64_t zbdesc = ptx::umma_desc_kmajor(ptx::smem_u32(zero), kSlotCols * 16, 128);
-            for (int it = blockIdx.x; ok && it < items; it += gridDim.x, u0 += kUpRows) {
-                for (int g = 0; ok && g < kUpGPI; ++g, ++G) {
-                    const int sl = G % kUpSlots, gb = g * kUpGR;
-                    if (!(ok = up_wait(&sempty[sl], ((G / kUpSlots) & 1) ^ 1, abort)))
+            const uint32_t dslot = tmem + g * kSlotCols;
+            for (int it = blockIdx.x; ok && it < items; it += gridDim.x, ++m) {
+                if (!(ok = up_wait(&sempty[g], (m & 1) ^ 1, abort)))
+                    break;
+                ptx::tc_fence_after();
+                ptx::umma_f16(dslot, zadesc, zbdesc, idesc0, false);  // clear the group's accumulator
+                // the group's output rows 0 ... 7 read its input rows r = 0 ... 9
+                for (int r = 0; r < kUpGRows; ++r) {
+                    const int u = m * kUpLoads + g * kUpGRows + r, b = u % kUpRowBufs;
+                    if (!(ok = up_wait(&full[b], (u / kUpRowBufs) & 1, abort)))
                         break;
                     ptx::tc_fence_after();
-                    const uint32_t dslot = tmem + sl * kSlotCols;
-                    ptx::umma_f16(dslot, zadesc, zbdesc, idesc0, false);  // clear the group's accumulator
-                    // the group's output rows gb ... gb + 7 read item input rows gb ... gb + 9
-                    for (int i = gb; i <= gb + kUpGR + 1; ++i) {
-                        const int u = u0 + i, b = u % kUpRowBufs;
-                        if (!(ok = up_wait(&full[b], (u / kUpRowBufs) & 1, abort)))
-                            break;
-                        ptx::tc_fence_after();
-                        // input row i feeds output row t = i - ty - gb for ty = 0, 1, 2 where
-                        // 0 <= t < kUpGR: ty_lo ... ty_hi, at columns NO (kUpGR - 1 - t)
-                        const int r = i - gb;
-                        const int ty_lo = r > kUpGR - 1 ? r - (kUpGR - 1) : 0;
-                        const int ty_hi = r < 2 ? r : 2;
-                        const int nt = ty_hi - ty_lo + 1;
-                        const uint32_t idesc = nt == 3 ? idesc3 : (nt == 2 ? idesc2 : idesc1);
-                        const uint32_t dcol = dslot + NO * (kUpGR - 1 - r + ty_lo);
-                        const uint64_t ab = adesc0 + ((b * kRowBytes) >> 4);
-                        const uint64_t bb = bdesc0 + ((ty_lo * NO * 16) >> 4);
+                    // input row r feeds output row t = r - ty for ty = 0, 1, 2 where
+                    // 0 <= t < kUpGR: ty_lo ... ty_hi, at columns NO (kUpGR - 1 - t)
+                    const int ty_lo = r > kUpGR - 1 ? r - (kUpGR - 1) : 0;
+                    const int ty_hi = r < 2 ? r : 2;
+                    const int nt = ty_hi - ty_lo + 1;
+                    const uint32_t idesc = nt == 3 ? idesc3 : (nt == 2 ? idesc2 : idesc1);
+                    const uint32_t dcol = dslot + NO * (kUpGR - 1 - r + ty_lo);
+                    const uint64_t ab = adesc0 + ((b * kRowBytes) >> 4);
+                    const uint64_t bb = bdesc0 + ((ty_lo * NO * 16) >> 4);
 #pragma unroll
-                        for (int tx = 0; tx < 3; ++tx) {
+                    for (int tx = 0; tx < 3; ++tx) {
 #pragma unroll
-                            for (int k = 0; k < KCH / 2; ++k) {
-                                const uint64_t ad = ab + ((2 * k * kUpPlaneBytes + tx * 16) >> 4);
-                                const uint64_t bd = bb + (((tx * KCH + 2 * k) * N3 * 16) >> 4);
-                                ptx::umma_f16(dcol, ad, bd, idesc, true);
-                            }
+                        for (int k = 0; k < KCH / 2; ++k) {
+                            const uint64_t ad = ab + ((2 * k * kUpPlaneBytes + tx * 16) >> 4);
+                            const uint64_t bd = bb + (((tx * KCH + 2 * k) * N3 * 16) >> 4);
+                            ptx::umma_f16(dcol, ad, bd, idesc, true);
                         }
-                        // a row buffer is freed after its last group: the next group of
-                        // the item re-reads the two rows from gb + kUpGR on
-                        if (g == kUpGPI - 1 || i < gb + kUpGR)
-                            ptx::umma_commit(&empty[b]);
                     }
-                    if (ok)
-                        ptx::umma_commit(&sfull[sl]);  // the group's accumulator is complete
+                    ptx::umma_commit(&empty[b]);  // the row buffer is read once the MMAs finish
                 }
+                if (ok)
+                    ptx::umma_commit(&sfull[g]);  // the group's accumulator is complete
             }
             if (*abort) {  // the MMAs in flight finish before Tensor Memory is freed
-                ptx::umma_commit(drain);
-                ptx::mbar_wait_bounded(drain, 0, kUpWaitSpins);
+                ptx::umma_commit(&drain[g]);
+                ptx::mbar_wait_bounded(&drain[g], 0, kUpWaitSpins);
             }
         }
     } else {
