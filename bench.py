@@ -853,7 +853,6 @@ def e2e_form(vsc, kw, pinned, stream, steps, warmup, ws, dev):
 
     n_frames = len(pinned)
     outs = [torch.empty((H, W, 4), dtype=torch.uint8).pin_memory() for _ in range(2)]
-    done = [torch.cuda.Event(), torch.cuda.Event()]
     st = make_stabilizer(vsc, kw, stream)
     for i in range(3):
         st.load_frame(pinned[i][0].numpy(), pinned[i][1].numpy())
@@ -862,10 +861,9 @@ def e2e_form(vsc, kw, pinned, stream, steps, warmup, ws, dev):
     def step():
         k = state["k"]
         if k >= 2:
-            done[k % 2].synchronize()  # step k - 2's frame is on the host
+            st.wait_output(1)  # step k - 2's frame is on the host
             state["checksum"] += int(outs[k % 2][0, 0, 0])
         st.step(outs[k % 2], asynchronous=True)
-        done[k % 2].record(stream)
         o, p = pinned[state["nxt"] % n_frames]
         st.load_frame(o.numpy(), p.numpy())
         state["nxt"] += 1
@@ -879,13 +877,13 @@ def e2e_form(vsc, kw, pinned, stream, steps, warmup, ws, dev):
     t0 = time.perf_counter()
     for _ in range(steps):
         step()
-    stream.synchronize()  # the last two results
+    st.synchronize()  # the last two results
     t = reduce_max(time.perf_counter() - t0, ws, dev)
     st.close()
     return {"value": ws * steps / t, "unit": "frames/s", "h2d_bytes_per_step": 2 * W * H * 4,
             "d2h_bytes_per_step": W * H * 4,
-            "pipelining": "results read back asynchronously into pinned memory, the host at most two steps "
-                          "ahead; uploads on the stabilizer's copy stream"}
+            "pipelining": "results read back asynchronously into pinned memory on the stabilizer's download "
+                          "stream, the host at most two steps ahead; uploads on its copy stream"}
 
 
 def psnr_vs_plain(vsc, kw, dev_frames, stream, n_steps: int = 12):

@@ -348,14 +348,19 @@ VSC_API vsc_status vsc_stabilizer_set_flows(vsc_stabilizer* s, const float* fwd,
  * the 3-frame window; writes its RGBA8 stabilized image to out_rgba, keeps
  * the FP32 result as the next step's previous stabilized frame, and drops
  * the oldest frame from the window.  out_on_device: 1 = device pointer
- * (stream-ordered); 0 = host pointer, copied before the call returns (the
- * stream is synchronised); VSC_OUT_HOST_ASYNC = host pointer, the copy is
- * enqueued on the stabilizer's stream and the call returns at once: read
- * out_rgba after vsc_stabilizer_synchronize (with page-locked memory the
- * copy overlaps the caller's next load_frame and step). */
+ * (stream-ordered); 0 = host pointer, copied before the call returns;
+ * VSC_OUT_HOST_ASYNC = host pointer, the copy is enqueued and the call
+ * returns at once: read out_rgba after vsc_stabilizer_wait_output or
+ * vsc_stabilizer_synchronize.  Host copies run on a download stream of the
+ * stabilizer from one of two device buffers that alternate, so with
+ * page-locked memory a copy overlaps the caller's next load_frame and step. */
 #define VSC_OUT_HOST_ASYNC 2
 VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int32_t out_on_device);
-/* Waits until everything enqueued on the stabilizer's stream has finished. */
+/* Waits for the host copy of the last step with a host output (which = 0) or
+ * of the one before it (which = 1); no-op if there was none. */
+VSC_API vsc_status vsc_stabilizer_wait_output(vsc_stabilizer* s, int32_t which);
+/* Waits until everything enqueued by the stabilizer (steps, loads, host
+ * copies) has finished. */
 VSC_API vsc_status vsc_stabilizer_synchronize(vsc_stabilizer* s);
 
 /* Device pointers to internal state, for inspection (valid until the next call):

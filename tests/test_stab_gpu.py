@@ -255,10 +255,11 @@ def test_stabilizer_graph_replay_side_stream(vsc, oracle, cuda, use_graphs):
 
 
 def test_stabilizer_async_host_output_and_pinned_uploads(vsc, cuda):
-    """Results copied back with VSC_OUT_HOST_ASYNC into pinned memory while
-    the next frames upload from pinned memory on the copy stream (the host
-    two steps ahead) equal the synchronous host path's bytes; an unknown
-    output mode is rejected."""
+    """Results copied back with VSC_OUT_HOST_ASYNC into pinned memory (on the
+    download stream, from alternating device buffers) while the next frames
+    upload from pinned memory on the copy stream equal the synchronous host
+    path's bytes, each one readable after wait_output; an unknown output mode
+    is rejected."""
     import torch
 
     w, h = 96, 64
@@ -277,6 +278,9 @@ def test_stabilizer_async_host_output_and_pinned_uploads(vsc, cuda):
     outs = [torch.empty((h, w, 4), dtype=torch.uint8).pin_memory() for _ in range(6)]
     for t in range(6):
         st.step(outs[t], asynchronous=True)
+        if t >= 1:  # the previous step's copy, waited for alone
+            st.wait_output(1)
+            assert np.array_equal(outs[t - 1].numpy(), refs[t - 1]), t - 1
         st.load_frame(pin[t + 3][0].numpy(), pin[t + 3][1].numpy())
     st.synchronize()
     for t in range(6):

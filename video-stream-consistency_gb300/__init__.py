@@ -46,7 +46,7 @@ EXPORTED = [
     "vsc_upsampler_set_max_residual", "vsc_upsampler_prepare", "vsc_upsampler_train_step", "vsc_upsampler_apply",
     "vsc_stabilizer_set_upsampler", "vsc_solver_autotune", "vsc_solver_tile_rows", "vsc_solver_set_autotune",
     "vsc_multistream_set_fused", "vsc_multistream_fused", "vsc_multistream_set_upsampler",
-    "vsc_stabilizer_synchronize",
+    "vsc_stabilizer_synchronize", "vsc_stabilizer_wait_output",
 ]
 VSC_DTYPE_F32, VSC_DTYPE_BF16, VSC_DTYPE_F16 = 0, 1, 2
 VSC_OUT_HOST_ASYNC = 2
@@ -169,6 +169,7 @@ def load():
         "vsc_multistream_step": [vp, C.POINTER(vp), i32],
         "vsc_multistream_set_fused": [vp, i32],
         "vsc_stabilizer_synchronize": [vp],
+        "vsc_stabilizer_wait_output": [vp, i32],
         "vsc_multistream_set_upsampler": [vp, i32, vp],
         "vsc_get_adap_comb_masked": [IP] * 10 + [f32, vp],
         "vsc_stabilizer_set_occlusion_mask": [vp, i32],
@@ -595,7 +596,7 @@ class Stabilizer:
     def step(self, out=None, asynchronous: bool = False):
         """Stabilize the window's middle frame; returns the RGBA result.  With
         a host tensor and asynchronous=True the copy back is only enqueued
-        (VSC_OUT_HOST_ASYNC): read `out` after synchronize()."""
+        (VSC_OUT_HOST_ASYNC): read `out` after wait_output() or synchronize()."""
         import torch
 
         if out is None:
@@ -606,6 +607,10 @@ class Stabilizer:
 
     def synchronize(self):
         _check(load().vsc_stabilizer_synchronize(self._h))
+
+    def wait_output(self, which: int = 0):
+        """Waits for the host copy of the last asynchronous step (0) or the one before (1)."""
+        _check(load().vsc_stabilizer_wait_output(self._h, which))
 
     def buffer(self, which: int, channels: int = 3):
         """Copy of internal state: 0 last stabilized, 1 fwd flow, 2 bwd flow, 3 adapCmbPr, 4 consWt."""

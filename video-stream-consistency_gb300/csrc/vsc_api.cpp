@@ -643,7 +643,14 @@ struct vsc_stabilizer {
     // consumed[k] = its conversion done (the next upload into it waits)
     cudaStream_t cst = nullptr;
     cudaEvent_t staged[2] = {}, consumed[2] = {};
-    uint8_t* out_rgba = nullptr;
+    uint8_t* out_rgba = nullptr;    // device copy of a host-destined output (buffer 0 of two)
+    uint8_t* out_rgba_b = nullptr;  // buffer 1: a step writes one while the other is copied back
+    int out_par = 0;
+    // host outputs are copied back on a download stream: step_done orders the copy
+    // after its step, d2h_done[p] marks buffer p's copy finished
+    cudaStream_t dst = nullptr;
+    cudaEvent_t step_done = nullptr, d2h_done[2] = {};
+    int d2h_last = -1, d2h_prev = -1;  // buffers of the last two host copies
     float* small = nullptr;  // frame resized to the flow size (downscale mode)
     float* flow_fwd = nullptr;
     float* flow_bwd = nullptr;
@@ -687,7 +694,7 @@ struct vsc_stabilizer {
         const vsc_upsampler* upsampler = nullptr;
         cudaGraphExec_t exec = nullptr;
         uint64_t used = 0;
-    } graphs[8];
+    } graphs[12];  // 3 ring positions x 2 feedback buffers x 2 output buffers
     uint64_t graph_clock = 0;
 };
 
@@ -737,6 +744,7 @@ void free_all(vsc_stabilizer* s)
     f(s->stage[0]);
     f(s->stage[1]);
     f(s->out_rgba);
+    f(s->out_rgba_b);
     f(s->small);
     f(s->flow_fwd);
     f(s->flow_small);
@@ -773,6 +781,19 @@ void free_all(vsc_stabilizer* s)
         cudaStreamDestroy(s->cst);
         s->cst = nullptr;
     }
+    for (cudaEvent_t& e : s->d2h_done)
+        if (e) {
+            cudaEventDestroy(e);
+            e = nullptr;
+        }
+    if (s->step_done) {
+        cudaEventDestroy(s->step_done);
+        s->step_done = nullptr;
+    }
+    if (s->dst) {
+        cudaStreamDestroy(s->dst);
+        s->dst = nullptr;
+    }
     for (auto& g : s->graphs)
         if (g.exec) {
             cudaGraphExecDestroy(g.exec);
@@ -801,6 +822,11 @@ vsc_status alloc_all(vsc_stabilizer* s)
         A(cudaEventCreateWithFlags(&s->consumed[k], cudaEventDisableTiming));
     }
     A(dalloc(&s->out_rgba, static_cast<size_t>(s->w) * s->h * 4));
+    A(dalloc(&s->out_rgba_b, static_cast<size_t>(s->w) * s->h * 4));
+    A(cudaStreamCreateWithFlags(&s->dst, cudaStreamNonBlocking));
+    A(cudaEventCreateWithFlags(&s->step_done, cudaEventDisableTiming));
+    for (int k = 0; k < 2; ++k)
+        A(cudaEventCreateWithFlags(&s->d2h_done[k], cudaEventDisableTiming));
     // forward and backward flow contiguous: the estimator writes both in one launch
     A(dalloc(&s->flow_fwd, 2 * static_cast<size_t>(s->w) * s->h * s->fc));
     if (e == cudaSuccess)
@@ -1310,7 +1336,19 @@ VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int
     if (out_rgba && out_on_device == 1 && (reinterpret_cast<uintptr_t>(out_rgba) & 3))
         return set_error(VSC_EINVAL, "step: device output must be 4-byte aligned");
     DeviceGuard g(s->device);
+    const bool host_out = out_rgba && out_on_device != 1;
     uint8_t* rgba_dev = (out_rgba && out_on_device == 1) ? out_rgba : s->out_rgba;
+    int par = 0;
+    if (host_out) {
+        // alternate device buffers: this step writes one while the previous
+        // step's copy back reads the other; the copy from this buffer two host
+        // outputs ago must have finished
+        par = s->out_par;
+        rgba_dev = par ? s->out_rgba_b : s->out_rgba;
+        vsc_status w = check_cuda(cudaStreamWaitEvent(s->st, s->d2h_done[par], 0), "step");
+        if (w)
+            return w;
+    }
     int nl = 0;
     cudaError_t e = cudaSuccess;
     // The first step (which seeds the feedback frame) runs directly; later
@@ -1324,15 +1362,40 @@ VSC_API vsc_status vsc_stabilizer_step(vsc_stabilizer* s, uint8_t* out_rgba, int
     if (stt)
         return stt;
     finish_step(s, nl);
-    if (out_rgba && out_on_device != 1) {
-        stt = check_cuda(cudaMemcpyAsync(out_rgba, s->out_rgba, static_cast<size_t>(s->w) * s->h * 4,
-                             cudaMemcpyDeviceToHost, s->st),
-            "step download");
-        if (stt || out_on_device == VSC_OUT_HOST_ASYNC)
+    if (host_out) {
+        // the copy back runs on the download stream, after the step, beside the
+        // caller's next load_frame and step
+        s->out_par ^= 1;
+        stt = check_cuda(cudaEventRecord(s->step_done, s->st), "step download");
+        if (!stt)
+            stt = check_cuda(cudaStreamWaitEvent(s->dst, s->step_done, 0), "step download");
+        if (!stt)
+            stt = check_cuda(cudaMemcpyAsync(out_rgba, rgba_dev, static_cast<size_t>(s->w) * s->h * 4,
+                                 cudaMemcpyDeviceToHost, s->dst),
+                "step download");
+        if (!stt)
+            stt = check_cuda(cudaEventRecord(s->d2h_done[par], s->dst), "step download");
+        if (stt)
             return stt;
-        return check_cuda(cudaStreamSynchronize(s->st), "step synchronize");
+        s->d2h_prev = s->d2h_last;
+        s->d2h_last = par;
+        if (out_on_device == VSC_OUT_HOST_ASYNC)
+            return VSC_OK;
+        return check_cuda(cudaEventSynchronize(s->d2h_done[par]), "step synchronize");
     }
     return VSC_OK;
+}
+
+VSC_API vsc_status vsc_stabilizer_wait_output(vsc_stabilizer* s, int32_t which)
+{
+    clear_error();
+    if (!s || which < 0 || which > 1)
+        return set_error(VSC_EINVAL, "wait_output: null stabilizer or which not 0 or 1");
+    const int par = which == 0 ? s->d2h_last : s->d2h_prev;
+    if (par < 0)
+        return VSC_OK;
+    DeviceGuard g(s->device);
+    return check_cuda(cudaEventSynchronize(s->d2h_done[par]), "wait_output");
 }
 
 VSC_API vsc_status vsc_stabilizer_synchronize(vsc_stabilizer* s)
@@ -1341,7 +1404,10 @@ VSC_API vsc_status vsc_stabilizer_synchronize(vsc_stabilizer* s)
     if (!s)
         return set_error(VSC_EINVAL, "synchronize: null stabilizer");
     DeviceGuard g(s->device);
-    return check_cuda(cudaStreamSynchronize(s->st), "synchronize");
+    vsc_status st = check_cuda(cudaStreamSynchronize(s->st), "synchronize");
+    if (!st)
+        st = check_cuda(cudaStreamSynchronize(s->dst), "synchronize");
+    return st;
 }
 
 VSC_API vsc_status vsc_stabilizer_buffer(vsc_stabilizer* s, int32_t which, const float** dev_ptr)
