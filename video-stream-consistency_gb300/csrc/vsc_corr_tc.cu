@@ -131,6 +131,7 @@ __global__ void __launch_bounds__((2 + 4 * kMaxEpiGroups) * 32, 1)
         float* __restrict__ out2, int nprob, const float* __restrict__ scales, int N, int H, int W, int Cp, int md,
         uint32_t idesc, int stages_a, int stages_b, int groups, int ndyg, int* __restrict__ timeout_flag)
 {
+    pdl_enter();
     extern __shared__ unsigned char smem_raw[];
     const uint32_t bytesA = kTcM * Cp * 2;
     const uint32_t bytesB = kTcN * Cp * 2;
@@ -385,6 +386,7 @@ template <bool kBf16>
 __global__ void to_chunked_kernel(const float* __restrict__ in, uint4* __restrict__ out, const float* __restrict__ scale,
     int C, int H, int W, int chunks)
 {
+    pdl_enter();
     const int64_t HW = static_cast<int64_t>(H) * W;
     const int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (p >= HW)
@@ -412,6 +414,7 @@ __global__ void warp_to_chunked_kernel(const float* __restrict__ in, const float
     uint4* __restrict__ out, const float* __restrict__ scale, int C, int H, int W, int chunks, int64_t sin,
     int64_t sfl, int64_t sout)
 {
+    pdl_enter();
     const int64_t HW = static_cast<int64_t>(H) * W;
     const int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (p >= HW)
@@ -546,10 +549,10 @@ cudaError_t launch_corr_tc_chunked2(const void* f1c, const void* f2c, float* out
     while (ndyg < P && base * ndyg < 2 * sms)
         ++ndyg;
     const int items = base * ndyg;
-    corr_tc_kernel<<<std::min(items, sms), (2 + 4 * plan.groups) * 32, plan.smem, st>>>(mA, mB, out, mA2, mB2,
-        nprob == 2 ? out2 : out, nprob, scales, N, H, W, Cp, md, ptx::umma_idesc_f16(bf16, kTcM, kTcN), plan.stages_a,
-        plan.stages_b, plan.groups, ndyg, flag);
-    return cudaGetLastError();
+    const cudaError_t el = launch_pdl(corr_tc_kernel, dim3(std::min(items, sms)), dim3((2 + 4 * plan.groups) * 32),
+        plan.smem, st, mA, mB, out, mA2, mB2, nprob == 2 ? out2 : out, nprob, scales, N, H, W, Cp, md,
+        ptx::umma_idesc_f16(bf16, kTcM, kTcN), plan.stages_a, plan.stages_b, plan.groups, ndyg, flag);
+    return el != cudaSuccess ? el : cudaGetLastError();
 }
 
 cudaError_t launch_to_chunked(const float* in, void* out, const float* scale, int N, int C, int H, int W, bool bf16,
@@ -558,11 +561,9 @@ cudaError_t launch_to_chunked(const float* in, void* out, const float* scale, in
     const int chunks = tc_padded_channels(C) / 8;
     const int64_t HW = static_cast<int64_t>(H) * W;
     const dim3 g(static_cast<unsigned>((HW + 127) / 128), chunks, N);
-    if (bf16)
-        to_chunked_kernel<true><<<g, 128, 0, st>>>(in, static_cast<uint4*>(out), scale, C, H, W, chunks);
-    else
-        to_chunked_kernel<false><<<g, 128, 0, st>>>(in, static_cast<uint4*>(out), scale, C, H, W, chunks);
-    return cudaGetLastError();
+    const cudaError_t e = launch_pdl(bf16 ? to_chunked_kernel<true> : to_chunked_kernel<false>, g, dim3(128), 0, st, in,
+        static_cast<uint4*>(out), scale, C, H, W, chunks);
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_warp_to_chunked(const float* in, const float* flow, void* out, const float* scale, int N, int C,
@@ -572,13 +573,9 @@ cudaError_t launch_warp_to_chunked(const float* in, const float* flow, void* out
     const int64_t HW = static_cast<int64_t>(H) * W;
     const dim3 g(static_cast<unsigned>((HW + 255) / 256), chunks, N);
     const int64_t so = sout_bytes / 16;
-    if (bf16)
-        warp_to_chunked_kernel<true><<<g, 256, 0, st>>>(in, flow, static_cast<uint4*>(out), scale, C, H, W, chunks,
-            sin, sfl, so);
-    else
-        warp_to_chunked_kernel<false><<<g, 256, 0, st>>>(in, flow, static_cast<uint4*>(out), scale, C, H, W, chunks,
-            sin, sfl, so);
-    return cudaGetLastError();
+    const cudaError_t e = launch_pdl(bf16 ? warp_to_chunked_kernel<true> : warp_to_chunked_kernel<false>, g, dim3(256),
+        0, st, in, flow, static_cast<uint4*>(out), scale, C, H, W, chunks, sin, sfl, so);
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_corr_tc(const float* f1, const float* f2, float* out, int N, int C, int H, int W, int md,

@@ -83,6 +83,7 @@ __device__ __forceinline__ void sample_hp3(const float* __restrict__ src, int sw
 __global__ void level0_image_kernel(const float* __restrict__ img, int w, int h, float* __restrict__ lev, int lw,
     int lh)
 {
+    pdl_enter();
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= lw || y >= lh)
@@ -110,6 +111,7 @@ __global__ void level0_image_kernel(const float* __restrict__ img, int w, int h,
 
 __global__ void pool2_kernel(const float* __restrict__ s, float* __restrict__ d, int cw, int chh)
 {
+    pdl_enter();
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= cw || y >= chh)
@@ -135,6 +137,7 @@ constexpr int kFeatMaxC = 196;
 __global__ void __launch_bounds__(32 * kFeatGroups) features_kernel(const float* __restrict__ im, int lw, int lh,
     int lc, int woff, float* __restrict__ out)
 {
+    pdl_enter();
     __shared__ float sf[kFeatMaxC][32];
     __shared__ float snrm[32];
     __shared__ float sw[kFeatMaxC * 27];
@@ -198,6 +201,7 @@ __global__ void __launch_bounds__(32 * kFeatGroups) features_kernel(const float*
 __global__ void up2_kernel(const float* __restrict__ in, int sw, int sh, float* __restrict__ out, int dw, int dh,
     int64_t bs)
 {
+    pdl_enter();
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= dw || y >= dh)
@@ -238,6 +242,7 @@ constexpr int kDecodeThreads = 64;
 __global__ void __launch_bounds__(kDecodeThreads) decode_kernel(const float* __restrict__ cv, float* __restrict__ res,
     float* __restrict__ conf, int64_t plane, float prior, int64_t bs)
 {
+    pdl_enter();
     __shared__ float sv[81][kDecodeThreads];
     const int t = threadIdx.x;
     const int64_t p = blockIdx.x * static_cast<int64_t>(kDecodeThreads) + t;
@@ -289,6 +294,7 @@ __global__ void __launch_bounds__(kDecodeThreads) decode_kernel(const float* __r
 __global__ void smooth_kernel(const float* __restrict__ res, const float* __restrict__ conf,
     const float* __restrict__ up, float* __restrict__ out, int lw, int lh, int64_t bs)
 {
+    pdl_enter();
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= lw || y >= lh)
@@ -324,6 +330,7 @@ __global__ void smooth_kernel(const float* __restrict__ res, const float* __rest
 __global__ void final_flow_kernel(const float* __restrict__ S, int lw, int lh, float* __restrict__ out, int w, int h,
     int64_t bs, int64_t so)
 {
+    pdl_enter();
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h)
@@ -434,20 +441,23 @@ cudaError_t launch_flow_features(const float* img, int w, int h, const FlowDims&
         lev[l] = scratch + off;
         off += static_cast<size_t>(d.lw[l]) * d.lh[l] * 3;
     }
-    level0_image_kernel<<<g2(d.lw[0], d.lh[0], b), b, 0, st>>>(img, w, h, lev[0], d.lw[0], d.lh[0]);
+    cudaError_t e = launch_pdl(level0_image_kernel, g2(d.lw[0], d.lh[0], b), b, 0, st, img, w, h, lev[0], d.lw[0],
+        d.lh[0]);
     int nl = 1;
     for (int l = 1; l < kFlowLevels; ++l) {
-        pool2_kernel<<<g2(d.lw[l], d.lh[l], b), b, 0, st>>>(lev[l - 1], lev[l], d.lw[l], d.lh[l]);
+        if (e == cudaSuccess)
+            e = launch_pdl(pool2_kernel, g2(d.lw[l], d.lh[l], b), b, 0, st, lev[l - 1], lev[l], d.lw[l], d.lh[l]);
         ++nl;
     }
     for (int l = 0; l < kFlowLevels; ++l) {
-        features_kernel<<<dim3((d.lw[l] + 31) / 32, d.lh[l]), dim3(32, kFeatGroups), 0, st>>>(lev[l], d.lw[l], d.lh[l],
-            d.lc[l], kWeightOff[l], feats + d.off[l]);
+        if (e == cudaSuccess)
+            e = launch_pdl(features_kernel, dim3((d.lw[l] + 31) / 32, d.lh[l]), dim3(32, kFeatGroups), 0, st, lev[l],
+                d.lw[l], d.lh[l], d.lc[l], kWeightOff[l], feats + d.off[l]);
         ++nl;
     }
     if (launches)
         *launches += nl;
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 size_t flow_estimate_scratch_floats(const FlowDims& d)
@@ -523,7 +533,9 @@ cudaError_t launch_flow_pair(const float* featA, int64_t sA, const float* featB,
         if (l < kFlowLevels - 1) {
             dim3 g = g2(lw, lh, b);
             g.z = 2;
-            up2_kernel<<<g, b, 0, st>>>(sm[cur], d.lw[l + 1], d.lh[l + 1], up, lw, lh, bs);
+            if ((e = launch_pdl(up2_kernel, g, b, 0, st, sm[cur], d.lw[l + 1], d.lh[l + 1], up, lw, lh, bs)) !=
+                cudaSuccess)
+                return e;
             ++nl;
             upp = up;
             if (tc) {
@@ -562,18 +574,22 @@ cudaError_t launch_flow_pair(const float* featA, int64_t sA, const float* featB,
                 return e;
             ++nl;
         }
-        decode_kernel<<<dim3(static_cast<unsigned>((plane + kDecodeThreads - 1) / kDecodeThreads), 1, 2),
-            kDecodeThreads, 0, st>>>(cv, raw, raw + 2 * plane, plane, kLevelPrior[l], bs);
+        if ((e = launch_pdl(decode_kernel, dim3(static_cast<unsigned>((plane + kDecodeThreads - 1) / kDecodeThreads), 1, 2),
+                 dim3(kDecodeThreads), 0, st, cv, raw, raw + 2 * plane, plane, kLevelPrior[l], bs)) != cudaSuccess)
+            return e;
         ++nl;
         cur ^= 1;
         dim3 g = g2(lw, lh, b);
         g.z = 2;
-        smooth_kernel<<<g, b, 0, st>>>(raw, raw + 2 * plane, upp, sm[cur], lw, lh, bs);
+        if ((e = launch_pdl(smooth_kernel, g, b, 0, st, raw, raw + 2 * plane, upp, sm[cur], lw, lh, bs)) != cudaSuccess)
+            return e;
         ++nl;
     }
     dim3 g = g2(w, h, b);
     g.z = 2;
-    final_flow_kernel<<<g, b, 0, st>>>(sm[cur], d.lw[0], d.lh[0], flow_out, w, h, bs, s_out);
+    if ((e = launch_pdl(final_flow_kernel, g, b, 0, st, sm[cur], d.lw[0], d.lh[0], flow_out, w, h, bs, s_out)) !=
+        cudaSuccess)
+        return e;
     ++nl;
     if (launches)
         *launches += nl;

@@ -14,6 +14,26 @@
 
 namespace vsc {
 
+// A kernel launch with programmatic stream serialization: the kernel may be
+// scheduled while the stream's previous kernel drains; it must call
+// pdl_enter() (vsc_math.cuh) before touching memory.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+    Args&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
 // ---- error plumbing (vsc_api.cpp) ----------------------------------------
 vsc_status set_error(vsc_status st, const char* fmt, ...);
 vsc_status check_cuda(cudaError_t e, const char* what);

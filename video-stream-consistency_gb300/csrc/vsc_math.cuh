@@ -66,6 +66,18 @@ __device__ __forceinline__ float expf_cw_nonpos(float x)
     return p * __int_as_float((static_cast<int>(kf) + 127) << 23);
 }
 
+// Programmatic dependent launch: wait until the preceding kernel of the stream
+// has completed (its writes visible), then let the following kernel be
+// scheduled, so that its launch overlaps this kernel.  The following kernel
+// can start only once every block of this one has started, so a waiting grid
+// never holds resources this one still needs.  Without the launch attribute
+// both instructions do nothing.
+__device__ __forceinline__ void pdl_enter()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" :::);
+}
+
 __device__ __forceinline__ int64_t pix_index(int x, int y, int w) { return static_cast<int64_t>(y) * w + x; }
 
 // RGBA8 quantisation of gpuimage.cu:64: (uint8)__float2uint_rd(|v| * 255),

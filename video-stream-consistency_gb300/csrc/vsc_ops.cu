@@ -120,6 +120,7 @@ __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
     corr_tile_kernel(const float* __restrict__ in1, const float* __restrict__ in2, float* __restrict__ out, int C,
         int H, int W, int legacy, int vec_store, int vec_load, int64_t sa, int64_t sb, int64_t so)
 {
+    pdl_enter();
     using G = CorrGeom<MD>;
     constexpr int P = G::P;
     // two stages of (f1 tile, f2 tile): the next channel chunk streams in
@@ -222,6 +223,7 @@ __global__ void __launch_bounds__(8 * kCorrTH * (2 * MD + 1))
 __global__ void corr_generic_kernel(const float* __restrict__ in1, const float* __restrict__ in2,
     float* __restrict__ out, int N, int C, int H, int W, int md, int legacy, int64_t s1, int64_t s2, int64_t so)
 {
+    pdl_enter();
     const int P = 2 * md + 1;
     const int64_t HW = static_cast<int64_t>(H) * W;
     const int64_t total = static_cast<int64_t>(N) * P * P * HW;
@@ -252,9 +254,9 @@ cudaError_t launch_corr_generic(const float* f1, const float* f2, float* out, in
     const int64_t P = 2 * md + 1;
     const int64_t total = static_cast<int64_t>(N) * P * P * H * W;
     const int64_t blocks = (total + 255) / 256;
-    corr_generic_kernel<<<static_cast<unsigned>(blocks < 152 * 64 ? blocks : 152 * 64), 256, 0, st>>>(
-        f1, f2, out, N, C, H, W, md, legacy, s1, s2, so);
-    return cudaGetLastError();
+    const cudaError_t e = launch_pdl(corr_generic_kernel, dim3(static_cast<unsigned>(blocks < 152 * 64 ? blocks : 152 * 64)),
+        dim3(256), 0, st, f1, f2, out, N, C, H, W, md, legacy, s1, s2, so);
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template <int MD>
@@ -288,7 +290,10 @@ cudaError_t launch_corr_tile(const float* f1, const float* f2, float* out, int N
     const int vec = ((W & 3) == 0) && a16(out) && ((so & 3) == 0);
     // 128-bit loads additionally need the f2 halo origin X0 - md on the grid
     const int vec_load = ((W & 3) == 0) && (MD % 4 == 0) && a16(f1) && a16(f2) && ((s1 & 3) == 0) && ((s2 & 3) == 0);
-    corr_tile_kernel<MD><<<grid, block, smem, st>>>(f1, f2, out, C, H, W, legacy, vec, vec_load, s1, s2, so);
+    const cudaError_t el = launch_pdl(corr_tile_kernel<MD>, grid, block, smem, st, f1, f2, out, C, H, W, legacy, vec,
+        vec_load, s1, s2, so);
+    if (el != cudaSuccess)
+        return el;
     return cudaGetLastError();
 }
 
@@ -348,6 +353,7 @@ template <int CG, bool kFull, int PX>
 __global__ void __launch_bounds__(256) warp_op2d_kernel(const float* __restrict__ in, const float* __restrict__ flow,
     float* __restrict__ out, int C, int H, int W, int64_t sin, int64_t sfl, int64_t sout, int groups)
 {
+    pdl_enter();
     const int x = blockIdx.x * 64 + (threadIdx.x & 63);
     const int yb = blockIdx.y * (4 * PX) + (threadIdx.x >> 6);
     if (x >= W || yb >= H)
@@ -413,6 +419,7 @@ __global__ void __launch_bounds__(256) warp_op2d_kernel(const float* __restrict_
 __global__ void warp_op_kernel(const float* __restrict__ in, const float* __restrict__ flow, float* __restrict__ out,
     int C, int H, int W, int64_t sin, int64_t sfl, int64_t sout)
 {
+    pdl_enter();
     const int64_t HW = static_cast<int64_t>(H) * W;
     const int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (p >= HW)
@@ -574,19 +581,16 @@ cudaError_t launch_warp_op(const float* in, const float* flow, float* out, int N
         const int rows = 4 * px;
         if (static_cast<int64_t>(N) * groups <= 65535 && (H + rows - 1) / rows <= 65535) {
             dim3 grid(static_cast<unsigned>((W + 63) / 64), static_cast<unsigned>((H + rows - 1) / rows), N * groups);
-            if (C == 3)
-                warp_op2d_kernel<3, true, 2><<<grid, 256, 0, st>>>(in, flow, out, C, H, W, sin, sfl, sout, groups);
-            else if (C % kWarpCG == 0)
-                warp_op2d_kernel<kWarpCG, true, 1><<<grid, 256, 0, st>>>(in, flow, out, C, H, W, sin, sfl, sout,
-                    groups);
-            else
-                warp_op2d_kernel<kWarpCG, false, 1><<<grid, 256, 0, st>>>(in, flow, out, C, H, W, sin, sfl, sout,
-                    groups);
-            return cudaGetLastError();
+            auto k = C == 3 ? warp_op2d_kernel<3, true, 2>
+                   : (C % kWarpCG == 0 ? warp_op2d_kernel<kWarpCG, true, 1> : warp_op2d_kernel<kWarpCG, false, 1>);
+            const cudaError_t e = launch_pdl(k, grid, dim3(256), 0, st, in, flow, out, C, H, W, sin, sfl, sout, groups);
+            return e != cudaSuccess ? e : cudaGetLastError();
         }
     }
     dim3 grid(static_cast<unsigned>((HW + 255) / 256), (C + kWarpCG - 1) / kWarpCG, N);
-    warp_op_kernel<<<grid, 256, 0, st>>>(in, flow, out, C, H, W, sin, sfl, sout);
+    const cudaError_t e = launch_pdl(warp_op_kernel, grid, dim3(256), 0, st, in, flow, out, C, H, W, sin, sfl, sout);
+    if (e != cudaSuccess)
+        return e;
     return cudaGetLastError();
 }
 

@@ -32,6 +32,7 @@ inline dim3 grid2d(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h +
 // summation order (right, left, bottom, top, then - cnt * centre).
 __global__ void lap_pr_kernel(const float* __restrict__ P, float* __restrict__ L, int w, int h)
 {
+    pdl_enter();
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h)
@@ -1257,7 +1258,9 @@ float* solver_start_buffer(float* O, int w, int h, int num_iter, float* workspac
 cudaError_t solver_lap(const float* P, int w, int h, float* workspace, cudaStream_t st)
 {
     const dim3 b(32, 8);
-    lap_pr_kernel<<<grid2d(w, h, b), b, 0, st>>>(P, workspace, w, h);
+    const cudaError_t e = launch_pdl(lap_pr_kernel, grid2d(w, h, b), b, 0, st, P, workspace, w, h);
+    if (e != cudaSuccess)
+        return e;
     return cudaGetLastError();
 }
 

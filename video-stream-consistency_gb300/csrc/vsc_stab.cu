@@ -34,6 +34,7 @@ __device__ __forceinline__ void build_lut(float* lut)
 // 4 pixels per thread: one 16-byte RGBA load, three 16-byte float stores.
 __global__ void rgba_to_float4_kernel(const uint4* __restrict__ rgba, float4* __restrict__ out, int64_t nquad)
 {
+    pdl_enter();
     __shared__ float lut[256];
     build_lut(lut);
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
@@ -379,6 +380,7 @@ __device__ __forceinline__ void bilinear4_px(const float* __restrict__ in, int i
 template <int C>
 __global__ void bilinear4_kernel(const float* __restrict__ in, int iw, int ih, float* __restrict__ out, int ow, int oh)
 {
+    pdl_enter();
     bilinear4_px<C>(in, iw, ih, out, ow, oh, (blockIdx.x * blockDim.x + threadIdx.x) * 4,
         blockIdx.y * blockDim.y + threadIdx.y);
 }
@@ -411,6 +413,7 @@ __global__ void pyr_down3_kernel(const float* __restrict__ P, const float* __res
     const float* __restrict__ Wt, int iw, int ih, float* __restrict__ Pd, float* __restrict__ Ad,
     float* __restrict__ Wd, int ow, int oh)
 {
+    pdl_enter();
     const int ox = blockIdx.x * blockDim.x + threadIdx.x;
     const int oy = blockIdx.y * blockDim.y + threadIdx.y;
     if (ox >= ow || oy >= oh)
@@ -435,6 +438,7 @@ __global__ void __launch_bounds__(256) fused_front_kernel(const float* __restric
     const float* __restrict__ fbwd, int fc, float* __restrict__ adap_pr, float* __restrict__ cons_wt, int w, int h,
     float alpha, float beta, float gamma)
 {
+    pdl_enter();
     using I = typename std::conditional<kFast, int, int64_t>::type;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -530,6 +534,7 @@ __global__ void __launch_bounds__(256) fused_front_rgba_kernel(const uint32_t* _
 __global__ void resize_nearest_kernel(const float* __restrict__ in, int iw, int ih, float* __restrict__ out, int ow,
     int oh)
 {
+    pdl_enter();
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= ow || y >= oh)
@@ -554,8 +559,10 @@ cudaError_t launch_rgba_to_float(const uint8_t* rgba, float* out, int64_t npix, 
     int64_t done = 0;
     if (aligned16(rgba) && aligned16(out) && npix >= 4) {
         const int64_t nq = npix / 4;
-        rgba_to_float4_kernel<<<static_cast<unsigned>((nq + 255) / 256), 256, 0, st>>>(
-            reinterpret_cast<const uint4*>(rgba), reinterpret_cast<float4*>(out), nq);
+        const cudaError_t e = launch_pdl(rgba_to_float4_kernel, dim3(static_cast<unsigned>((nq + 255) / 256)),
+            dim3(256), 0, st, reinterpret_cast<const uint4*>(rgba), reinterpret_cast<float4*>(out), nq);
+        if (e != cudaSuccess)
+            return e;
         done = nq * 4;
     }
     if (done < npix)
@@ -645,9 +652,9 @@ cudaError_t launch_bilinear(Img in, Img out, cudaStream_t st)
     if (out.c == 2 || out.c == 3) {
         const dim3 g((out.w + 4 * b.x - 1) / (4 * b.x), (out.h + b.y - 1) / b.y);
         if (out.c == 3)
-            bilinear4_kernel<3><<<g, b, 0, st>>>(in.d, in.w, in.h, out.d, out.w, out.h);
+            return launch_pdl(bilinear4_kernel<3>, g, b, 0, st, in.d, in.w, in.h, out.d, out.w, out.h);
         else
-            bilinear4_kernel<2><<<g, b, 0, st>>>(in.d, in.w, in.h, out.d, out.w, out.h);
+            return launch_pdl(bilinear4_kernel<2>, g, b, 0, st, in.d, in.w, in.h, out.d, out.w, out.h);
     } else {
         bilinear_kernel<<<grid2d(out.w, out.h, b), b, 0, st>>>(in.d, in.w, in.h, out.d, out.w, out.h, out.c);
     }
@@ -687,7 +694,10 @@ cudaError_t launch_pyr_down3(const float* P, const float* A, const float* Wt, in
     float* Wd, int ow, int oh, cudaStream_t st)
 {
     const dim3 b(32, 8);
-    pyr_down3_kernel<<<grid2d(ow, oh, b), b, 0, st>>>(P, A, Wt, iw, ih, Pd, Ad, Wd, ow, oh);
+    const cudaError_t e = launch_pdl(pyr_down3_kernel, grid2d(ow, oh, b), b, 0, st, P, A, Wt, iw, ih, Pd, Ad, Wd, ow,
+        oh);
+    if (e != cudaSuccess)
+        return e;
     return cudaGetLastError();
 }
 
@@ -706,9 +716,9 @@ cudaError_t launch_fused_front(const float* o0, const float* o1, const float* o2
     const bool fast = front_fast_ok(w, h, fc, alpha, beta, gamma);
     auto k = occlusion_mask ? (fast ? fused_front_kernel<true, true> : fused_front_kernel<true, false>)
                             : (fast ? fused_front_kernel<false, true> : fused_front_kernel<false, false>);
-    k<<<grid2d(w, h, b), b, 0, st>>>(
+    const cudaError_t el = launch_pdl(k, grid2d(w, h, b), b, 0, st,
         o0, o1, o2, p0, p1, p2, last_stab, flow_fwd, flow_bwd, fc, adap_pr, cons_wt, w, h, alpha, beta, gamma);
-    return cudaGetLastError();
+    return el != cudaSuccess ? el : cudaGetLastError();
 }
 
 cudaError_t launch_fused_front_rgba(const uint8_t* o0, const uint8_t* o1, const uint8_t* o2, const uint8_t* p0,
@@ -730,7 +740,9 @@ cudaError_t launch_fused_front_rgba(const uint8_t* o0, const uint8_t* o1, const 
 cudaError_t launch_resize_nearest(const float* in, int iw, int ih, float* out, int ow, int oh, cudaStream_t st)
 {
     const dim3 b(32, 8);
-    resize_nearest_kernel<<<grid2d(ow, oh, b), b, 0, st>>>(in, iw, ih, out, ow, oh);
+    const cudaError_t e = launch_pdl(resize_nearest_kernel, grid2d(ow, oh, b), b, 0, st, in, iw, ih, out, ow, oh);
+    if (e != cudaSuccess)
+        return e;
     return cudaGetLastError();
 }
 
