@@ -405,6 +405,43 @@ __global__ void to_chunked_kernel(const float* __restrict__ in, uint4* __restric
         pack2<kBf16>(v[2], v[3]), pack2<kBf16>(v[4], v[5]), pack2<kBf16>(v[6], v[7]));
 }
 
+// to_chunked_kernel for the five levels of a feature pyramid (N = 1) in one
+// launch: a flat list of (128-pixel block, chunk) pairs, level after level.
+constexpr int kChunkLevelsMax = 5;
+struct ChunkLevels {
+    const float* in[kChunkLevelsMax];
+    uint4* out[kChunkLevelsMax];
+    int C[kChunkLevelsMax], H[kChunkLevelsMax], W[kChunkLevelsMax], chunks[kChunkLevelsMax];
+    int block0[kChunkLevelsMax + 1];
+    int count;
+};
+
+template <bool kBf16>
+__global__ void to_chunked_levels_kernel(const __grid_constant__ ChunkLevels cl, const float* __restrict__ scale)
+{
+    pdl_enter();
+    int l = 0;
+    while (l + 1 < cl.count && static_cast<int>(blockIdx.x) >= cl.block0[l + 1])
+        ++l;
+    const int W = cl.W[l], H = cl.H[l], C = cl.C[l], chunks = cl.chunks[l];
+    const int HW = H * W, nhw = (HW + 127) / 128;
+    const int b = blockIdx.x - cl.block0[l];
+    const int p = (b % nhw) * 128 + threadIdx.x, q = b / nhw;
+    if (p >= HW)
+        return;
+    const int y = p / W, x = p - y * W;
+    const float s = *scale;
+    const float* src = cl.in[l] + p;
+    float v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int c = q * 8 + j;
+        v[j] = c < C ? src[static_cast<int64_t>(c) * HW] * s : 0.0f;
+    }
+    cl.out[l][(static_cast<int64_t>(y) * chunks + q) * W + x] = make_uint4(pack2<kBf16>(v[0], v[1]),
+        pack2<kBf16>(v[2], v[3]), pack2<kBf16>(v[4], v[5]), pack2<kBf16>(v[6], v[7]));
+}
+
 // custom::Warp (the single-precision arithmetic of warp_op_kernel) writing
 // the chunked 16-bit operand layout directly, scaled by *scale: the warped
 // second-frame features of the flow estimator go straight to the tensor-core
@@ -563,6 +600,30 @@ cudaError_t launch_to_chunked(const float* in, void* out, const float* scale, in
     const dim3 g(static_cast<unsigned>((HW + 127) / 128), chunks, N);
     const cudaError_t e = launch_pdl(bf16 ? to_chunked_kernel<true> : to_chunked_kernel<false>, g, dim3(128), 0, st, in,
         static_cast<uint4*>(out), scale, C, H, W, chunks);
+    return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+cudaError_t launch_to_chunked_levels(const float* const* in, void* const* out, const int* C, const int* H,
+    const int* W, int n, const float* scale, bool bf16, cudaStream_t st)
+{
+    if (n < 1 || n > kChunkLevelsMax)
+        return cudaErrorInvalidValue;
+    ChunkLevels cl{};
+    cl.count = n;
+    cl.block0[0] = 0;
+    for (int l = 0; l < n; ++l) {
+        if (static_cast<int64_t>(H[l]) * W[l] >= (int64_t(1) << 31))
+            return cudaErrorInvalidValue;
+        cl.in[l] = in[l];
+        cl.out[l] = static_cast<uint4*>(out[l]);
+        cl.C[l] = C[l];
+        cl.H[l] = H[l];
+        cl.W[l] = W[l];
+        cl.chunks[l] = tc_padded_channels(C[l]) / 8;
+        cl.block0[l + 1] = cl.block0[l] + ((H[l] * W[l] + 127) / 128) * cl.chunks[l];
+    }
+    const cudaError_t e = launch_pdl(bf16 ? to_chunked_levels_kernel<true> : to_chunked_levels_kernel<false>,
+        dim3(cl.block0[n]), dim3(128), 0, st, cl, scale);
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 

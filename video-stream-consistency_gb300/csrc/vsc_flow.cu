@@ -134,19 +134,35 @@ __global__ void pool2_kernel(const float* __restrict__ s, float* __restrict__ d,
 constexpr int kFeatGroups = 8;
 constexpr int kFeatMaxC = 196;
 
-__global__ void __launch_bounds__(32 * kFeatGroups) features_kernel(const float* __restrict__ im, int lw, int lh,
-    int lc, int woff, float* __restrict__ out)
+// The five levels' features in one launch: a flat list of blocks, each
+// level's blocks (ceil(lw / 32) x lh) after the previous level's, coarsest
+// (fewest pixels, most channels) first.
+struct FeatLevels {
+    const float* im[kFlowLevels];
+    float* out[kFlowLevels];
+    int lw[kFlowLevels], lh[kFlowLevels], lc[kFlowLevels], woff[kFlowLevels];
+    int block0[kFlowLevels + 1];
+};
+
+__global__ void __launch_bounds__(32 * kFeatGroups) features_kernel(const __grid_constant__ FeatLevels fl)
 {
     pdl_enter();
     __shared__ float sf[kFeatMaxC][32];
     __shared__ float snrm[32];
     __shared__ float sw[kFeatMaxC * 27];
+    int l = 0;
+    while (l + 1 < kFlowLevels && static_cast<int>(blockIdx.x) >= fl.block0[l + 1])
+        ++l;
+    const float* __restrict__ im = fl.im[l];
+    float* __restrict__ out = fl.out[l];
+    const int lw = fl.lw[l], lh = fl.lh[l], lc = fl.lc[l], woff = fl.woff[l];
+    const int nbx = (lw + 31) / 32, b = blockIdx.x - fl.block0[l];
     const int tx = threadIdx.x, g = threadIdx.y;
     for (int i = g * 32 + tx; i < lc * 27; i += 32 * kFeatGroups)
         sw[i] = g_flow_w[woff + i];
     __syncthreads();
-    const int x = blockIdx.x * 32 + tx;
-    const int y = blockIdx.y;
+    const int x = (b % nbx) * 32 + tx;
+    const int y = b / nbx;
     const bool ok = x < lw;
     const int xc = ok ? x : lw - 1;
     const int64_t plane = static_cast<int64_t>(lw) * lh;
@@ -449,12 +465,21 @@ cudaError_t launch_flow_features(const float* img, int w, int h, const FlowDims&
             e = launch_pdl(pool2_kernel, g2(d.lw[l], d.lh[l], b), b, 0, st, lev[l - 1], lev[l], d.lw[l], d.lh[l]);
         ++nl;
     }
-    for (int l = 0; l < kFlowLevels; ++l) {
-        if (e == cudaSuccess)
-            e = launch_pdl(features_kernel, dim3((d.lw[l] + 31) / 32, d.lh[l]), dim3(32, kFeatGroups), 0, st, lev[l],
-                d.lw[l], d.lh[l], d.lc[l], kWeightOff[l], feats + d.off[l]);
-        ++nl;
+    FeatLevels fl{};
+    fl.block0[0] = 0;
+    for (int k = 0; k < kFlowLevels; ++k) {
+        const int l = kFlowLevels - 1 - k;  // coarsest first
+        fl.im[k] = lev[l];
+        fl.out[k] = feats + d.off[l];
+        fl.lw[k] = d.lw[l];
+        fl.lh[k] = d.lh[l];
+        fl.lc[k] = d.lc[l];
+        fl.woff[k] = kWeightOff[l];
+        fl.block0[k + 1] = fl.block0[k] + ((d.lw[l] + 31) / 32) * d.lh[l];
     }
+    if (e == cudaSuccess)
+        e = launch_pdl(features_kernel, dim3(fl.block0[kFlowLevels]), dim3(32, kFeatGroups), 0, st, fl);
+    ++nl;
     if (launches)
         *launches += nl;
     return e != cudaSuccess ? e : cudaGetLastError();
@@ -494,15 +519,20 @@ size_t tc_warped_bytes(const FlowDims& d)
 cudaError_t launch_flow_features_chunked(const float* feats, const FlowDims& d, void* chunked, const float* scale,
     bool bf16, cudaStream_t st, int* launches)
 {
+    const float* in[kFlowLevels];
+    void* out[kFlowLevels];
+    int C[kFlowLevels], H[kFlowLevels], W[kFlowLevels];
     for (int l = 0; l < kFlowLevels; ++l) {
-        cudaError_t e = launch_to_chunked(feats + d.off[l], static_cast<unsigned char*>(chunked) + tc_level_offset(d, l),
-            scale, 1, d.lc[l], d.lh[l], d.lw[l], bf16, st);
-        if (e != cudaSuccess)
-            return e;
+        in[l] = feats + d.off[l];
+        out[l] = static_cast<unsigned char*>(chunked) + tc_level_offset(d, l);
+        C[l] = d.lc[l];
+        H[l] = d.lh[l];
+        W[l] = d.lw[l];
     }
+    const cudaError_t e = launch_to_chunked_levels(in, out, C, H, W, kFlowLevels, scale, bf16, st);
     if (launches)
-        *launches += kFlowLevels;
-    return cudaSuccess;
+        *launches += 1;
+    return e;
 }
 
 cudaError_t launch_flow_pair(const float* featA, int64_t sA, const float* featB, int64_t sB, int w, int h,

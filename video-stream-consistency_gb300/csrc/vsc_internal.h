@@ -73,6 +73,9 @@ cudaError_t launch_corr_tc_chunked2(const void* f1c, const void* f2c, float* out
 // float NCHW -> chunked 16-bit operand layout, multiplied by *scale.
 cudaError_t launch_to_chunked(const float* in, void* out, const float* scale, int N, int C, int H, int W, bool bf16,
     cudaStream_t st);
+// the same for up to 5 tensors of one image each (a feature pyramid's levels) in one launch
+cudaError_t launch_to_chunked_levels(const float* const* in, void* const* out, const int* C, const int* H,
+    const int* W, int n, const float* scale, bool bf16, cudaStream_t st);
 // custom::Warp (single precision) with the chunked 16-bit layout as output;
 // batch n reads in + n * sin, flow + n * sfl (floats), writes out + n * sout_bytes.
 cudaError_t launch_warp_to_chunked(const float* in, const float* flow, void* out, const float* scale, int N, int C,
