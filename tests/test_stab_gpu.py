@@ -524,6 +524,15 @@ def test_multistream_more_than_one_group(vsc, cuda):
     assert grouped
 
 
+@pytest.mark.parametrize("num_iter", [0, 1, 9])
+def test_multistream_grouped_few_iterations(vsc, cuda, num_iter):
+    """Grouped solves with no iteration (the step writes the unsolved
+    pyramid result), one, and nine (a level with one launch of one step)."""
+    sizes = [(96, 64), (128, 72)]
+    _, grouped = _multistream_vs_singles(vsc, sizes, [(1, "f32")] * 2, True, num_iter, steps=3)
+    assert grouped
+
+
 def test_multistream_ungroupable_size_runs_ungrouped(vsc, cuda):
     """A level width that is not a multiple of 4 (70 -> 35) keeps the step
     ungrouped, with the same results."""
