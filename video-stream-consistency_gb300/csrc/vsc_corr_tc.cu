@@ -392,7 +392,8 @@ __global__ void to_chunked_kernel(const float* __restrict__ in, uint4* __restric
     if (p >= HW)
         return;
     const int q = blockIdx.y, n = blockIdx.z;
-    const int y = static_cast<int>(p / W), x = static_cast<int>(p % W);
+    const int y = HW < (int64_t(1) << 31) ? static_cast<int>(p) / W : static_cast<int>(p / W);
+    const int x = static_cast<int>(p - static_cast<int64_t>(y) * W);
     const float s = *scale;
     const float* src = in + static_cast<int64_t>(n) * C * HW + p;
     float v[8];
@@ -457,7 +458,9 @@ __global__ void warp_to_chunked_kernel(const float* __restrict__ in, const float
     if (p >= HW)
         return;
     const int q = blockIdx.y, n = blockIdx.z;
-    const int y = static_cast<int>(p / W), x = static_cast<int>(p % W);
+    // 32-bit division where the plane allows (a 64-bit one is a software routine)
+    const int y = HW < (int64_t(1) << 31) ? static_cast<int>(p) / W : static_cast<int>(p / W);
+    const int x = static_cast<int>(p - static_cast<int64_t>(y) * W);
     const float* fl = flow + n * sfl;
     const float xf = static_cast<float>(x) + __ldg(fl + p);
     const float yf = static_cast<float>(y) + __ldg(fl + HW + p);

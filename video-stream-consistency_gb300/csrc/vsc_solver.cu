@@ -1147,10 +1147,11 @@ cudaError_t solver_group_autotune(const int* w, const int* h, int n, cudaStream_
     float* buf = nullptr;
     if ((e = cudaMalloc(&buf, 7 * total * sizeof(float))) != cudaSuccess)
         return e;
-    // Three rounds, the shapes alternating within each, one warm-up launch per
-    // shape and two timed 8-step launches; each shape's best round counts (the
+    // Five rounds, the shapes alternating within each, one warm-up launch per
+    // shape and four timed 8-step launches; each shape's best round counts (the
     // first launches after the allocation and a clock still ramping up would
-    // otherwise favour whichever shape is timed last).
+    // otherwise favour whichever shape is timed last; where the shapes are
+    // close, more rounds keep the choice from flipping between runs).
     cudaEvent_t ev[2] = {};
     float best_ms[2] = {1e30f, 1e30f};
     const int shapes[2] = {kTbEY, kPEY};
@@ -1181,15 +1182,15 @@ cudaError_t solver_group_autotune(const int* w, const int* h, int n, cudaStream_
              : n <= 4 ? launch_members<4>(m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT)
                       : launch_members<kGroupMax>(m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT);
     };
-    for (int round = 0; round < 3 && e == cudaSuccess; ++round) {
+    for (int round = 0; round < 5 && e == cudaSuccess; ++round) {
         for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
             int nl = 0;
-            // a warm-up launch, then two timed ones, all of kTbT steps with momentum
+            // a warm-up launch, then four timed ones, all of kTbT steps with momentum
             e = launch(mem[s], shapes[s], 2 * kTbT, &nl);
             if (e == cudaSuccess)
                 e = cudaEventRecord(ev[0], st);
             if (e == cudaSuccess)
-                e = launch(mem[s], shapes[s], 3 * kTbT, &nl);
+                e = launch(mem[s], shapes[s], 5 * kTbT, &nl);
             float ms = 0.0f;
             if (e == cudaSuccess)
                 e = cudaEventRecord(ev[1], st);
