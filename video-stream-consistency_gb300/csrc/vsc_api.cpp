@@ -1808,10 +1808,12 @@ cudaError_t ms_enqueue_fused(vsc_multistream* m, const std::vector<uint8_t*>& ou
 }
 
 // the grouped form when requested and possible for the current
-// hyper-parameters: every level width a multiple of 4 (the TMA path)
+// hyper-parameters: the device runs the TMA kernels and every level width
+// is a multiple of 4 (buffers come from cudaMalloc, offsets are 16-byte
+// multiples then)
 bool ms_use_fused(vsc_multistream* m)
 {
-    if (!m->fused || !m->fused_ok)
+    if (!m->fused || !m->fused_ok || !solver_tma_supported())
         return false;
     for (vsc_stabilizer* s : m->st) {
         if (m->hp.pyramid_levels > s->levels_alloc)

@@ -176,6 +176,7 @@ struct SolverImage {
     uint8_t* rgba;     // RGBA8 copy of the result, or null
 };
 float* solver_start_buffer(float* O, int w, int h, int num_iter, float* workspace);
+bool solver_tma_supported();  // the persistent TMA kernels run on the current device
 cudaError_t solver_lap(const float* P, int w, int h, float* workspace, cudaStream_t st);
 bool solver_group_eligible(const SolverImage* im, int n);
 cudaError_t run_solver_group(const SolverImage* im, int n, int num_iter, float step, float mom, cudaStream_t st,

@@ -1251,6 +1251,12 @@ bool tma_eligible(const DeviceInfo* di, int w, const float* O, const WsView& v, 
 
 }  // namespace
 
+bool solver_tma_supported()
+{
+    DeviceInfo* di = nullptr;
+    return device_info(&di) == cudaSuccess && di->ps_smem;
+}
+
 float* solver_start_buffer(float* O, int w, int h, int num_iter, float* workspace)
 {
     return solve_launches(num_iter) % 2 == 0 ? O : ws_view(workspace, w, h).O2;
