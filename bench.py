@@ -991,9 +991,10 @@ def run_gpu(args):
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one solver launch at
-# 1920x1080, by Jacobi steps per launch, from the ncu captures summarised in
-# profiles/ (solver_tall_kernel, 8 steps: 124,875,264 + 23,028,736 bytes).
-SOLVER_TRAFFIC_BYTES = {8: 147_904_000}
+# 1920x1080, by Jacobi steps per launch, from the ncu capture summarised in
+# profiles/ (solver_tall_kernel, 8 steps, the mean of two launches:
+# 124,613,888 + 21,037,568 and 124,601,600 + 18,144,768 bytes).
+SOLVER_TRAFFIC_BYTES = {8: 144_198_912}
 
 
 def main():
