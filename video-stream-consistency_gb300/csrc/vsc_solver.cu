@@ -177,12 +177,14 @@ __device__ __forceinline__ void tb_iterate(TbState& s, const bool (&vr)[4], cons
     const bool (&vd)[4], const bool (&vu)[4], const float (&cnt)[4], float* smem, int T, int ring, int k0,
     float step, float mom, int px0, int py0)
 {
-    if (T == kTbT && ring == kTbT && k0 > 0) {
+    if (T == kTbT && ring == kTbT) {
+        // full launches, unrolled; momentum is off only in the first step of a solve
+        const bool later = k0 > 0;
 #pragma unroll
         for (int k = 0; k < kTbT; ++k) {
             const int lo = k + 1, hi = kTbEY - k - 1;  // the general bounds with ring == T == kTbT
             if (!(py0 + 1 < lo || py0 >= hi))  // warp-uniform: py0 = 2 * threadIdx.y
-                tb_step<kAll>(s, vr, vl, vd, vu, cnt, smem, k & 1, true, step, mom, px0, py0);
+                tb_step<kAll>(s, vr, vl, vd, vu, cnt, smem, k & 1, k > 0 || later, step, mom, px0, py0);
             __syncthreads();
         }
         return;
@@ -701,11 +703,13 @@ __device__ __forceinline__ void p8_iterate(P8State& s, float* obuf, int T, int k
     int warp, int gx0, int gy0, int w, int h)
 {
     const int r0 = 4 * warp;
-    if (T == kTbT && k0 > 0) {
+    if (T == kTbT) {
+        // full launches, unrolled; momentum is off only in the first step of a solve
+        const bool later = k0 > 0;
 #pragma unroll
         for (int k = 0; k < kTbT; ++k) {
             if (!(r0 + 3 < k + 1 || r0 >= kPEY - k - 1))
-                p8_step<kAll>(s, obuf, k & 1, true, step, mom, px0, warp, gx0, gy0, w, h);
+                p8_step<kAll>(s, obuf, k & 1, k > 0 || later, step, mom, px0, warp, gx0, gy0, w, h);
             __syncthreads();
         }
         return;
