@@ -949,7 +949,13 @@ VSC_API vsc_status vsc_stabilizer_destroy(vsc_stabilizer* s)
     if (!s)
         return VSC_OK;
     DeviceGuard g(s->device);
+    // the compute stream, then the upload and download streams (an
+    // asynchronous host read-back may still be running on the latter)
     cudaStreamSynchronize(s->st);
+    if (s->cst)
+        cudaStreamSynchronize(s->cst);
+    if (s->dst)
+        cudaStreamSynchronize(s->dst);
     free_all(s);
     delete s;
     return VSC_OK;
