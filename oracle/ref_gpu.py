@@ -21,7 +21,7 @@ class Img(C.Structure):
 
 # entry points of ref_gpu/ref_gpu_harness.cu (besides rg_last_error)
 FUNCS = ("rg_init", "rg_warp", "rg_adap_comb", "rg_consist_wt", "rg_bilinear", "rg_consist_out", "rg_to_float",
-         "rg_to_char", "rg_correlation", "rg_warp_op", "rg_stab_pass")
+         "rg_to_char", "rg_correlation", "rg_correlation_legacy", "rg_warp_op", "rg_stab_pass")
 
 _libs: dict = {}
 
@@ -53,6 +53,7 @@ def load(kind: str = "exact"):
     L.rg_to_float.argtypes = [C.c_void_p, Img]
     L.rg_to_char.argtypes = [Img, C.c_void_p]
     L.rg_correlation.argtypes = [C.c_void_p] * 3 + [C.c_int] * 5 + [C.c_void_p]
+    L.rg_correlation_legacy.argtypes = [C.c_void_p] * 3 + [C.c_int] * 5 + [C.c_void_p]
     L.rg_warp_op.argtypes = [C.c_void_p] * 3 + [C.c_int] * 4 + [C.c_void_p]
     L.rg_stab_pass.argtypes = [C.POINTER(Img), C.POINTER(Img), C.POINTER(Img), C.POINTER(Img), C.c_int, C.c_int,
                                C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_void_p]

@@ -12,6 +12,8 @@
  *                                updating consisOut in place, :363-372)
  *   gpuimage.cu:70-135           the RGBA8 conversions
  *   correlation_cuda.cu:333-442  rearrange to NHWC temporaries, 1 block per output pixel
+ *                                (legacy = 0); legacy = 1 (:182-331, :350-400): temporaries
+ *                                padded by 4, CorrelateData_old's geometry
  *   warp_cuda.cu:86-98           one 32-thread block row per channel
  *   videostabilizer.cpp:182-238  the order of one doOneStep pass
  * Used by the tests to pin the CPU restatement against the reference's GPU
@@ -37,15 +39,15 @@ namespace {
 
 CUmodule g_mod = nullptr;
 std::string g_err;
-enum K { kWarp, kAdap, kWt, kOut, kBil, kToF, kToC, kCorr, kRearr, kWarpOp, kCount };
+enum K { kWarp, kAdap, kWt, kOut, kBil, kToF, kToC, kCorr, kRearr, kWarpOp, kCorrOld, kCount };
 CUfunction g_fn[kCount] = {};
 // Kernels are found by their source name inside the mangled name: the
 // Itanium ABI writes <length><name> (then "If" for the float instantiation
 // of the templated op kernels).
 const char* const kNames[kCount] = {"kernel_warp", "kernel_adap_comb", "kernel_consist_wt", "kernel_consist_out",
     "kernel_bilinear", "kernel_to_float_image", "kernel_to_char_image", "correlation_cuda_forward_kernel",
-    "blob_rearrange_kernel", "warp_forward_kernel"};
-const bool kTemplated[kCount] = {false, false, false, false, false, false, false, true, true, true};
+    "blob_rearrange_kernel", "warp_forward_kernel", "correlation_old_kernel"};
+const bool kTemplated[kCount] = {false, false, false, false, false, false, false, true, true, true, true};
 
 std::string mangled_key(int k)
 {
@@ -60,9 +62,9 @@ int fail(const char* what, CUresult r)
     return -1;
 }
 
-int launch(K k, dim3 grid, dim3 block, void** args, CUstream st)
+int launch(K k, dim3 grid, dim3 block, void** args, CUstream st, unsigned smem = 0)
 {
-    CUresult r = cuLaunchKernel(g_fn[k], grid.x, grid.y, grid.z, block.x, block.y, block.z, 0, st, args, nullptr);
+    CUresult r = cuLaunchKernel(g_fn[k], grid.x, grid.y, grid.z, block.x, block.y, block.z, smem, st, args, nullptr);
     return r == CUDA_SUCCESS ? 0 : fail(kNames[k], r);
 }
 
@@ -197,6 +199,53 @@ int rg_correlation(const float* f1, const float* f2, float* out, int N, int C, i
             &one, &H, &W};
         rc = launch(kCorr, dim3(N, H, W), dim3(32), a, st);
     }
+    cudaFree(r1);
+    cudaFree(r2);
+    return rc;
+}
+
+// legacy = 1: correlation_cuda_forward with spatial_corr_sampler = false
+// (correlation_cuda.cu:350-400): both inputs rearranged to NHWC temporaries
+// padded by 4 pixels on every side, then CorrelateData_old (:267-331) with
+// kernel_size 1, strides 1, grid (W, H, N), 32 threads and C floats of
+// dynamic shared memory.  The reference leaves the padding of its
+// temporaries uninitialised (cudaMalloc, :366-370; the rearrange writes the
+// interior only), so a border output reads whatever the allocation held;
+// the harness clears the temporaries, which is the zero padding the op's
+// CPU semantics define.  The kernel places the window centre at padded
+// column x + max_displacement while the data sit at x + 4, so only
+// max_displacement = 4 (PWC-Net's) is meaningful.
+int rg_correlation_legacy(const float* f1, const float* f2, float* out, int N, int C, int H, int W, int md,
+    void* stream)
+{
+    CUstream st = static_cast<CUstream>(stream);
+    const int pad = 4;
+    const int HW = H * W;
+    int PW = W + 2 * pad, PH = H + 2 * pad;
+    int pHW = PW * PH;
+    float *r1 = nullptr, *r2 = nullptr;
+    const size_t bytes = static_cast<size_t>(pHW) * N * C * sizeof(float);
+    if (cudaMalloc(&r1, bytes) != cudaSuccess || cudaMalloc(&r2, bytes) != cudaSuccess)
+        return (g_err = "cudaMalloc", -1);
+    int rc = 0;
+    if (cudaMemsetAsync(r1, 0, bytes, st) != cudaSuccess || cudaMemsetAsync(r2, 0, bytes, st) != cudaSuccess)
+        rc = (g_err = "cudaMemset", -1);
+    const float* ins[2] = {f1, f2};
+    float* outs[2] = {r1, r2};
+    int padv = pad;
+    for (int i = 0; i < 2 && !rc; ++i) {
+        void* a[] = {&ins[i], &outs[i], &N, &C, &W, &H, const_cast<int*>(&HW), &padv, &pHW};
+        rc = launch(kRearr, dim3((HW - 1) / 16 + 1, C, N), dim3(16), a, st);
+    }
+    int P = 2 * md + 1;
+    int planes = P * P, count = H * W * planes, radius = md, kradius = 0, ksize = 1, one = 1;
+    if (!rc) {
+        void* a[] = {&count, &N, &W, &H, &planes, &count, &md, &radius, &P, &kradius, &ksize, &one, &one, &PW, &PH,
+            &C, &r1, &r2, &out};
+        rc = launch(kCorrOld, dim3(W, H, N), dim3(32), a, st, static_cast<unsigned>(C * sizeof(float)));
+    }
+    if (!rc && cudaStreamSynchronize(static_cast<cudaStream_t>(stream)) != cudaSuccess)
+        rc = (g_err = "sync", -1);
     cudaFree(r1);
     cudaFree(r2);
     return rc;

@@ -6,8 +6,8 @@ zlib (stored, fixed and dynamic Huffman blocks; every row filter), its PNG
 writer read back with Python's zlib, PPM, and .flo round trips with the
 reference's error cases (flowIO.cpp:31-80, imagehelpers.cpp:42-50).
 GPU tests: a whole directory stabilized through vsc_stabilize_files equals,
-frame for frame and bit for bit, the same stream run through the
-Stabilizer API (computed flows, and flows read from a flow directory)."""
+frame for frame and bit for bit, the reference's frame loop run over the CPU
+restatement (computed flows, and flows read from a flow directory)."""
 from __future__ import annotations
 
 import struct
@@ -157,7 +157,8 @@ def _write_stream(vsc, tmp_path, frames):
 
 
 @pytest.mark.gpu
-def test_stabilize_files_computed_flow(vsc, cuda, tmp_path):
+def test_stabilize_files_computed_flow(vsc, oracle, cuda, tmp_path):
+    from oracle_driver import run_oracle_stream
     from vsc_gb300 import synth
 
     w, h = 96, 64
@@ -172,32 +173,20 @@ def test_stabilize_files_computed_flow(vsc, cuda, tmp_path):
     assert vsc.stabilize_files(od, pd, out) == 6
     files = sorted(out.iterdir())
     assert [f.name for f in files] == [f"{i:06d}.png" for i in range(6)]
-    st = vsc.Stabilizer(w, h)
-    for i in range(3):
-        st.load_frame(*frames[i])
-    ref = {}
+    ref = run_oracle_stream(oracle, frames)
     for t in range(1, 5):
-        ref[t] = st.step().cpu().numpy()
-        if t + 2 < 6:
-            st.load_frame(*frames[t + 2])
-    st.close()
-    for t in range(1, 5):
-        assert np.array_equal(vsc.read_image(out / f"{t:06d}.png")[..., :3], ref[t][..., :3]), t
+        assert np.array_equal(vsc.read_image(out / f"{t:06d}.png")[..., :3], ref[t - 1][1][..., :3]), t
     # first and last frames: the processed frames through the float conversion and back
-    import torch
-
     for idx in (0, 5):
-        p = torch.from_numpy(frames[idx][1]).cuda()
-        back = vsc.float_to_char_image(vsc.char_to_float_image(p)).cpu().numpy()
+        back = oracle.float_to_rgba(oracle.rgba_to_float(frames[idx][1]))
         assert np.array_equal(vsc.read_image(out / f"{idx:06d}.png")[..., :3], back[..., :3])
 
 
 @pytest.mark.gpu
-def test_stabilize_files_flow_directory(vsc, cuda, tmp_path):
+def test_stabilize_files_flow_directory(vsc, oracle, cuda, tmp_path):
     """-f mode: frame_<i+1>.flo is the forward flow of frame i,
     frame_<i>_bwd.flo its backward flow."""
-    import torch
-
+    from oracle_driver import run_oracle_stream
     from vsc_gb300 import synth
 
     w, h = 80, 48
@@ -220,17 +209,11 @@ def test_stabilize_files_flow_directory(vsc, cuda, tmp_path):
     hp = vsc.default_hyper_params()
     hp.num_iter = 60
     assert vsc.stabilize_files(od, pd, out, flow_dir=fd, hyper=hp) == 5
-    st = vsc.Stabilizer(w, h, compute_flow=False, flow_channels=2)
-    st.hyper_params.num_iter = 60
-    for i in range(3):
-        st.load_frame(*frames[i])
+    ohp = oracle.default_hyper()
+    ohp.num_iter = 60
+    ref = run_oracle_stream(oracle, frames, flows=flows, hp=ohp)
     for t in range(1, 4):
-        st.set_flows(torch.from_numpy(flows[t][0]), torch.from_numpy(flows[t][1]))
-        ref = st.step().cpu().numpy()
-        assert np.array_equal(vsc.read_image(out / f"{t:06d}.png")[..., :3], ref[..., :3]), t
-        if t + 2 < 5:
-            st.load_frame(*frames[t + 2])
-    st.close()
+        assert np.array_equal(vsc.read_image(out / f"{t:06d}.png")[..., :3], ref[t - 1][1][..., :3]), t
     # a missing flow file is an error with its path
     (fd / "frame_000002_bwd.flo").unlink()
     with pytest.raises(vsc.VscError, match="frame_000002_bwd.flo"):

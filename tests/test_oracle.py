@@ -265,7 +265,7 @@ def test_reference_gpu_harness_finds_every_kernel_in_the_cubin():
     src = (root / "oracle" / "ref_gpu" / "ref_gpu_harness.cu").read_text()
     names = re.findall(r'"(\w+)"', re.search(r"kNames\[kCount\] = \{(.*?)\};", src, re.S).group(1))
     templated = re.findall(r"(true|false)", re.search(r"kTemplated\[kCount\] = \{(.*?)\};", src, re.S).group(1))
-    assert len(names) == len(templated) == 10
+    assert len(names) == len(templated) == 11
     out = subprocess.run(["readelf", "-sW", str(cubin)], capture_output=True, text=True, check=True).stdout
     syms = [ln.split()[-1] for ln in out.splitlines() if " FUNC " in ln]
     for n, t in zip(names, templated):

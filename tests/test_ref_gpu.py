@@ -12,7 +12,8 @@ Bars, stated per test:
   * the solver: the reference updates in place (a data race); after the full
     pyramid solve the result is within 40 dB PSNR of the Jacobi restatement;
   * Correlation: the reference GPU op sums 32 strided partial sums; within
-    1e-5 relative of the channel-order sum.
+    1e-5 relative of the channel-order sum (legacy = 0 and legacy = 1, the
+    latter divided by C).
 """
 from __future__ import annotations
 
@@ -138,6 +139,35 @@ def test_reference_correlation_op(rg, oracle, cuda):
     torch.cuda.synchronize()
     ref = oracle.correlation(f1, f2, 4)
     np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("n,c,h,w", [(2, 64, 17, 23), (1, 196, 9, 14), (1, 3, 5, 6)])
+def test_reference_legacy_correlation_op(rg, oracle, vsc, cuda, n, c, h, w):
+    """legacy = 1 (PWC-Net's original layer, correlation_cuda.cu:182-331):
+    N x 81 x H x W, each sum divided by C.  The reference kernel sums 32
+    strided partial sums per output and then divides; the restatement (and
+    this library, bit for bit) sums in channel order and divides, so the two
+    agree within 1e-5 relative.  Channel counts below, at and above one warp
+    of partial sums; borders included (the harness zero-fills the reference's
+    4-pixel padded temporaries, which it leaves uninitialised)."""
+    import torch
+
+    L = rg.load("exact")
+    f1 = RNG.standard_normal((n, c, h, w)).astype(np.float32)
+    f2 = RNG.standard_normal((n, c, h, w)).astype(np.float32)
+    out = torch.full((n, 81, h, w), float("nan"), dtype=torch.float32, device=cuda)
+    d1, d2 = _t(f1, cuda), _t(f2, cuda)
+    rg.check(L, L.rg_correlation_legacy(d1.data_ptr(), d2.data_ptr(), out.data_ptr(), n, c, h, w, 4, None))
+    torch.cuda.synchronize()
+    ref = oracle.correlation(f1, f2, 4, legacy=1)
+    assert ref.shape == (n, 81, h, w)
+    got = out.cpu().numpy()
+    scale = np.abs(ref).max()
+    np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-6 * scale)
+    # zero padding: displacements reaching outside the map give exact zeros on both sides
+    assert np.array_equal(got[:, 0, 0, :] == 0, ref[:, 0, 0, :] == 0)
+    ours = vsc.correlation(d1, d2, 4, legacy=1).cpu().numpy()
+    assert np.array_equal(ours, ref)
 
 
 def test_reference_warp_op_exact(rg, oracle, cuda):

@@ -9,6 +9,8 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
+from oracle_driver import run_oracle_stream
+
 pytestmark = pytest.mark.gpu
 RNG = np.random.Generator(np.random.PCG64(4321))
 
@@ -105,7 +107,7 @@ def _equal_up_to_zero_sign(a, b):
 # per-tile kernel; iteration counts not divisible by 8 end in a short launch
 @pytest.mark.parametrize("h,w,iters", [(9, 11, 0), (9, 11, 1), (9, 11, 2), (40, 56, 75), (3, 3, 5), (2, 2, 4),
                                        (67, 33, 150), (48, 200, 13), (540, 960, 75), (1080, 1920, 9),
-                                       (17, 4, 3), (100, 64, 150)])
+                                       (1080, 1920, 150), (17, 4, 3), (100, 64, 150)])
 def test_consist_out(vsc, oracle, cuda, h, w, iters):
     import torch
 
@@ -163,42 +165,10 @@ def _frames(w, h, n, seed):
     return [s.frame(i) for i in range(n)]
 
 
-def _run_oracle_stream(oracle, frames, flows=None, hp=None, downscale=1, occlusion=False):
-    """The reference's driver loop (stabilizefiles.cpp:108-131 with
-    videostabilizer.cpp:136-265) over the restatement."""
-    orig = [oracle.rgba_to_float(o) for o, _ in frames]
-    proc = [oracle.rgba_to_float(p) for _, p in frames]
-    h, w = orig[0].shape[:2]
-    last = proc[2]
-    outs = []
-    for t in range(1, len(frames) - 1):
-        if flows is not None:
-            ff, fb = flows[t]
-        elif downscale > 1:
-            fw, fh = int(round(w / downscale)), int(round(h / downscale))
-            small = [_nearest(orig[t], fw, fh), _nearest(orig[t + 1], fw, fh)]
-            ff = oracle.bilinear(oracle.flow_estimate(small[0], small[1]), w, h)
-            fb = oracle.bilinear(oracle.flow_estimate(small[1], small[0]), w, h)
-        else:
-            ff = oracle.flow_estimate(orig[t], orig[t + 1])
-            fb = oracle.flow_estimate(orig[t + 1], orig[t])
-        out, rgba = oracle.stab_pass(orig[t - 1:t + 2], proc[t - 1:t + 2], ff, fb, last, hp, occlusion_mask=occlusion)
-        outs.append((out, rgba, ff, fb))
-        last = out
-    return outs
-
-
-def _nearest(img, ow, oh):
-    h, w = img.shape[:2]
-    xs = np.minimum(w - 1, ((2 * np.arange(ow) + 1) * w) // (2 * ow))
-    ys = np.minimum(h - 1, ((2 * np.arange(oh) + 1) * h) // (2 * oh))
-    return np.ascontiguousarray(img[ys][:, xs])
-
-
 @pytest.mark.parametrize("w,h", [(96, 64), (70, 45)])
 def test_stabilizer_computed_flow_stream(vsc, oracle, cuda, w, h):
     frames = _frames(w, h, 6, seed=11)
-    ref = _run_oracle_stream(oracle, frames)
+    ref = run_oracle_stream(oracle, frames)
     st = vsc.Stabilizer(w, h)
     for i in range(3):
         st.load_frame(*frames[i])
@@ -223,7 +193,7 @@ def test_stabilizer_graph_replay_side_stream(vsc, oracle, cuda, use_graphs):
 
     w, h = 96, 64
     frames = _frames(w, h, 10, seed=21)
-    ref = _run_oracle_stream(oracle, frames[:8])
+    ref = run_oracle_stream(oracle, frames[:8])
     hp = oracle.default_hyper()
     hp.num_iter = 37
     side = torch.cuda.Stream()
@@ -299,7 +269,7 @@ def test_stabilizer_external_flows_host_io(vsc, oracle, cuda):
     frames = _frames(w, h, 5, seed=12)
     flows = {t: (RNG.normal(0, 3, (h, w, 2)).astype(np.float32), RNG.normal(0, 3, (h, w, 2)).astype(np.float32))
              for t in range(1, 4)}
-    ref = _run_oracle_stream(oracle, frames, flows=flows)
+    ref = run_oracle_stream(oracle, frames, flows=flows)
     st = vsc.Stabilizer(w, h, compute_flow=False, flow_channels=2)
     for i in range(3):
         st.load_frame(*frames[i])
@@ -365,8 +335,8 @@ def test_stabilizer_occlusion_mask(vsc, oracle, cuda, use_graphs):
         ff = RNG.normal(0, 2, (h, w, 2)).astype(np.float32)
         fb = (-ff + RNG.normal(0, 0.5, ff.shape)).astype(np.float32)
         flows[t] = (ff, fb)
-    ref_on = _run_oracle_stream(oracle, frames, flows=flows, occlusion=True)
-    ref_off = _run_oracle_stream(oracle, frames, flows=flows)
+    ref_on = run_oracle_stream(oracle, frames, flows=flows, occlusion=True)
+    ref_off = run_oracle_stream(oracle, frames, flows=flows)
     assert not np.array_equal(ref_on[0][0], ref_off[0][0])
     stream = torch.cuda.Stream()
     st = vsc.Stabilizer(w, h, compute_flow=False, flow_channels=2, stream=stream, use_graphs=use_graphs)
@@ -389,7 +359,7 @@ def test_stabilizer_hyper_params_and_downscale(vsc, oracle, cuda):
     frames = _frames(w, h, 4, seed=13)
     hp = oracle.default_hyper()
     hp.pyramid_levels, hp.num_iter, hp.gamma = 3, 40, 1.0
-    ref = _run_oracle_stream(oracle, frames, hp=hp, downscale=2)
+    ref = run_oracle_stream(oracle, frames, hp=hp, downscale=2)
     st = vsc.Stabilizer(w, h, flow_downscale=2)
     p = st.hyper_params
     p.pyramid_levels, p.num_iter, p.gamma = 3, 40, 1.0
@@ -436,6 +406,65 @@ def test_full_hd_step_deterministic(vsc, cuda):
     for a, b in zip(outs[0], outs[1]):
         assert np.array_equal(a, b)
     assert outs[0][1][..., 3].max() == 1
+
+
+@pytest.mark.parametrize("w,h,nframes", [(640, 360, 3), (1920, 1080, 4)])
+def test_whole_step_equals_restatement(vsc, oracle, cuda, w, h, nframes):
+    """doOneStep end to end at 640x360 (the small configuration, one step)
+    and 1920x1080 (the benchmark size, two steps, so the second starts from
+    the first's FP32 feedback): default hyper-parameters (2-level pyramid,
+    75 iterations at half size, 150 at full size: every solve ends in a
+    short launch after the unrolled 8-step ones), flows computed by the
+    estimator at full size.  Forward and backward flow, FP32 state and RGBA8
+    output equal the restatement's driver loop (videostabilizer.cpp:136-265
+    with :118-128, :226) bit for bit (values; a zero's sign may differ)."""
+    frames = _frames(w, h, nframes, seed=17)
+    ref = run_oracle_stream(oracle, frames)
+    st = vsc.Stabilizer(w, h)
+    for i in range(3):
+        st.load_frame(*frames[i])
+    for k, t in enumerate(range(1, nframes - 1)):
+        out = st.step().cpu().numpy()
+        r_out, r_rgba, r_ff, r_fb = ref[k]
+        assert np.array_equal(st.buffer(1).cpu().numpy(), r_ff), f"fwd flow, step {k}"
+        assert np.array_equal(st.buffer(2).cpu().numpy(), r_fb), f"bwd flow, step {k}"
+        assert _equal_up_to_zero_sign(st.buffer(0).cpu().numpy(), r_out), f"stabilized, step {k}"
+        assert np.array_equal(out, r_rgba), f"rgba, step {k}"
+        if t + 2 < nframes:
+            st.load_frame(*frames[t + 2])
+    st.close()
+
+
+def _psnr_rgb(a, b):
+    import math
+
+    d = a[..., :3].astype(np.float64) - b[..., :3].astype(np.float64)
+    mse = float(np.mean(d * d)) / 255.0 ** 2
+    return math.inf if mse == 0 else 10 * math.log10(1.0 / mse)
+
+
+def test_fast_form_quality_at_1080p(vsc, cuda):
+    """The benchmark's fast form (flow at 960x540 with bilinear upsampling,
+    BF16 tensor-core correlations) against the plain FP32 path on the same
+    1920x1080 stream: stabilized RGB at >= 40 dB PSNR in every one of six
+    consecutive frames (the feedback carries each frame's difference into
+    the next)."""
+    frames = _frames(1920, 1080, 8, seed=19)
+    sts = [vsc.Stabilizer(1920, 1080), vsc.Stabilizer(1920, 1080, flow_downscale=2, corr_dtype="bf16")]
+    for st in sts:
+        for i in range(3):
+            st.load_frame(*frames[i])
+    vals = []
+    for t in range(1, 7):
+        a, b = (st.step().cpu().numpy() for st in sts)
+        vals.append(_psnr_rgb(a, b))
+        if t + 2 < len(frames):
+            for st in sts:
+                st.load_frame(*frames[t + 2])
+    for st in sts:
+        st.close()
+    print("fast form vs plain, PSNR per frame (dB):", [round(v, 2) for v in vals])
+    assert min(vals) >= 40.0, vals
 
 
 def _multistream_vs_singles(vsc, sizes, forms, fused, num_iter, upsampler=None, steps=5, levels=2):
