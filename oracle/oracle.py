@@ -82,6 +82,7 @@ def lib():
         L.vo_consist_wt.argtypes = [_f32p, _f32p, _f32p, C.c_float, C.c_float, _i64]
         L.vo_bilinear.argtypes = [_f32p, _i, _i, _f32p, _i, _i, _i]
         L.vo_consist_out.argtypes = [_f32p, _f32p, _f32p, _i, C.c_float, C.c_float, _f32p, _i, _i]
+        L.vo_consist_out_fma.argtypes = [_f32p, _f32p, _f32p, _i, C.c_float, C.c_float, _f32p, _i, _i]
         L.vo_default_hyper.argtypes = [C.POINTER(Hyper)]
         L.vo_stab_pass.restype = _i
         L.vo_stab_pass.argtypes = [
@@ -92,6 +93,11 @@ def lib():
         L.vo_stab_pass_ex.argtypes = [
             _i, _i, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _f32p, _f32p, _i, _f32p,
             C.POINTER(Hyper), _i, _f32p, C.c_void_p,
+        ]
+        L.vo_stab_pass_form.restype = _i
+        L.vo_stab_pass_form.argtypes = [
+            _i, _i, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _f32p, _f32p, _i, _f32p,
+            C.POINTER(Hyper), _i, _i, _f32p, C.c_void_p,
         ]
         L.vo_flow_level_dims.argtypes = [_i, _i, _i, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)]
         L.vo_flow_feature_floats.restype = C.c_size_t
@@ -267,11 +273,13 @@ def bilinear(img, ow: int, oh: int):
     return out
 
 
-def consist_out(P, A, wt, num_iter, step, mom, O_init):
+def consist_out(P, A, wt, num_iter, step, mom, O_init, form: str = "exact"):
+    """form: 'exact' (kernel_consist_out's expression) or 'fma' (the
+    library's FMA form of the same iteration)."""
     O = _c(O_init, np.float32).copy()
     h, w = O.shape[:2]
-    lib().vo_consist_out(_c(P, np.float32), _c(A, np.float32), _c(wt, np.float32), int(num_iter),
-                         float(step), float(mom), O, w, h)
+    fn = lib().vo_consist_out_fma if form == "fma" else lib().vo_consist_out
+    fn(_c(P, np.float32), _c(A, np.float32), _c(wt, np.float32), int(num_iter), float(step), float(mom), O, w, h)
     return O
 
 
@@ -281,9 +289,11 @@ def default_hyper() -> Hyper:
     return hp
 
 
-def stab_pass(orig3, proc3, flow_fwd, flow_bwd, last_stab, hp: Hyper | None = None, occlusion_mask: bool = False):
+def stab_pass(orig3, proc3, flow_fwd, flow_bwd, last_stab, hp: Hyper | None = None, occlusion_mask: bool = False,
+              solver_form: str = "exact"):
     """One stabilization pass over frames (t-1, t, t+1); returns (float HWC3, RGBA8).
-    occlusion_mask applies the opt-in forward-backward consistency mask."""
+    occlusion_mask applies the opt-in forward-backward consistency mask;
+    solver_form 'fma' solves with the FMA form."""
     hp = hp or default_hyper()
     orig3 = [_c(a, np.float32) for a in orig3]
     proc3 = [_c(a, np.float32) for a in proc3]
@@ -295,8 +305,8 @@ def stab_pass(orig3, proc3, flow_fwd, flow_bwd, last_stab, hp: Hyper | None = No
     pp = (C.c_void_p * 3)(*[a.ctypes.data for a in proc3])
     out = np.empty((h, w, 3), np.float32)
     rgba = np.empty((h, w, 4), np.uint8)
-    rc = lib().vo_stab_pass_ex(w, h, po, pp, ff, fb, ff.shape[2], ls, C.byref(hp), int(bool(occlusion_mask)), out,
-                               rgba.ctypes.data)
+    rc = lib().vo_stab_pass_form(w, h, po, pp, ff, fb, ff.shape[2], ls, C.byref(hp), int(bool(occlusion_mask)),
+                                 int(solver_form == "fma"), out, rgba.ctypes.data)
     if rc != 0:
         raise ValueError("vo_stab_pass: invalid sizes")
     return out, rgba

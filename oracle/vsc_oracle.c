@@ -553,6 +553,92 @@ void vo_consist_out(const float* P, const float* A, const float* wt, int num_ite
     free(O2);
 }
 
+/* The library's FMA form of the same Jacobi iteration (vsc_get_consist_out_fma),
+ * restated for its parity tests.  kernel_consist_out's step (:193-258),
+ *   g = (lap_O - lap_P) - wt * (O - A),  O' = O + s*g (+ m*U),  U' = s*g,
+ * is regrouped around two per-pixel constants computed once per solve,
+ *   Cs = s * fma(wt, A, -lap_P)   (lap_P as in vo_consist_out),
+ *   nK = -(s * (cnt + wt)),
+ * and one step reads, with invalid neighbours as +0,
+ *   S = (left + right) + (up + down),
+ *   g = fma(nK, O, fma(s, S, Cs)),  O' = O + g, then fma(m, U, O') for k > 0,  U' = g.
+ * Algebraically the reference's step; rounded differently (fused products,
+ * another summation order), so it agrees with vo_consist_out within a
+ * tolerance and with the library's FMA kernels bit for bit. */
+void vo_consist_out_fma(const float* P, const float* A, const float* wt, int num_iter, float step, float mom, float* O,
+    int w, int h)
+{
+    const int64_t n = (int64_t)w * h * 3;
+    const int64_t rs = (int64_t)w * 3;
+    float* U = (float*)calloc((size_t)n, sizeof(float));
+    float* O2 = (float*)malloc((size_t)n * sizeof(float));
+    float* Cs = (float*)malloc((size_t)n * sizeof(float));
+    float* nK = (float*)malloc((size_t)n * sizeof(float));
+    _Pragma("omp parallel for schedule(static)") for (int y = 0; y < h; ++y)
+    {
+        for (int x = 0; x < w; ++x) {
+            const int64_t p = (int64_t)y * w + x;
+            for (int c = 0; c < 3; ++c) {
+                const int64_t i = p * 3 + c;
+                int cnt = 0;
+                float lap = 0.0f;
+                if ((x + 1) < (w - 1)) {
+                    lap += P[i + 3];
+                    cnt += 1;
+                }
+                if ((x - 1) >= 0) {
+                    lap += P[i - 3];
+                    cnt += 1;
+                }
+                if ((y + 1) < (h - 1)) {
+                    lap += P[i + rs];
+                    cnt += 1;
+                }
+                if ((y - 1) >= 0) {
+                    lap += P[i - rs];
+                    cnt += 1;
+                }
+                lap -= (float)cnt * P[i];
+                Cs[i] = step * fmaf(wt[i], A[i], -lap);
+                nK[i] = -(step * ((float)cnt + wt[i]));
+            }
+        }
+    }
+    float* cur = O;
+    float* nxt = O2;
+    for (int k = 0; k < num_iter; ++k) {
+        _Pragma("omp parallel for schedule(static)") for (int y = 0; y < h; ++y)
+        {
+            for (int x = 0; x < w; ++x) {
+                const int64_t p = (int64_t)y * w + x;
+                for (int c = 0; c < 3; ++c) {
+                    const int64_t i = p * 3 + c;
+                    const float right = (x + 1) < (w - 1) ? cur[i + 3] : 0.0f;
+                    const float left = (x - 1) >= 0 ? cur[i - 3] : 0.0f;
+                    const float down = (y + 1) < (h - 1) ? cur[i + rs] : 0.0f;
+                    const float up = (y - 1) >= 0 ? cur[i - rs] : 0.0f;
+                    const float S = (left + right) + (up + down);
+                    const float g = fmaf(nK[i], cur[i], fmaf(step, S, Cs[i]));
+                    float o = cur[i] + g;
+                    if (k)
+                        o = fmaf(mom, U[i], o);
+                    U[i] = g;
+                    nxt[i] = o;
+                }
+            }
+        }
+        float* t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+    if (cur != O)
+        memcpy(O, cur, (size_t)n * sizeof(float));
+    free(U);
+    free(O2);
+    free(Cs);
+    free(nK);
+}
+
 /* videostabilizer.cpp:104-112 */
 void vo_default_hyper(vo_hyper* hp)
 {
@@ -579,6 +665,14 @@ int vo_stab_pass(int w, int h, const float* const orig[3], const float* const pr
 int vo_stab_pass_ex(int w, int h, const float* const orig[3], const float* const proc[3], const float* flow_fwd,
     const float* flow_bwd, int fc, const float* last_stab, const vo_hyper* hp, int occlusion_mask, float* out_f32,
     uint8_t* out_rgba)
+{
+    return vo_stab_pass_form(w, h, orig, proc, flow_fwd, flow_bwd, fc, last_stab, hp, occlusion_mask, 0, out_f32,
+        out_rgba);
+}
+
+int vo_stab_pass_form(int w, int h, const float* const orig[3], const float* const proc[3], const float* flow_fwd,
+    const float* flow_bwd, int fc, const float* last_stab, const vo_hyper* hp, int occlusion_mask, int solver_form,
+    float* out_f32, uint8_t* out_rgba)
 {
     const int L = hp->pyramid_levels;
     if (L < 1 || L > 8 || (w >> (L - 1)) < 2 || (h >> (L - 1)) < 2)
@@ -640,7 +734,8 @@ int vo_stab_pass_ex(int w, int h, const float* const orig[3], const float* const
     for (int j = L - 1; j >= 0; --j) {
         if (j != L - 1)
             vo_bilinear(pO[j + 1], lw[j + 1], lh[j + 1], pO[j], lw[j], lh[j], 3);
-        vo_consist_out(pP[j], pA[j], pW[j], hp->num_iter / (j + 1), hp->step_size, hp->mom_fac, pO[j], lw[j], lh[j]);
+        (solver_form ? vo_consist_out_fma : vo_consist_out)(pP[j], pA[j], pW[j], hp->num_iter / (j + 1),
+            hp->step_size, hp->mom_fac, pO[j], lw[j], lh[j]);
     }
     memcpy(out_f32, pO[0], bytes);
     if (out_rgba)

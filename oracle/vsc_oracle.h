@@ -74,6 +74,9 @@ void vo_bilinear(const float* in, int iw, int ih, float* out, int ow, int oh, in
 /* :193-258 + :350-374, Jacobi; O holds the initial solution and receives the result. */
 void vo_consist_out(const float* P, const float* A, const float* wt, int num_iter, float step, float mom, float* O,
     int w, int h);
+/* The FMA form of the solver (the library's vsc_get_consist_out_fma). */
+void vo_consist_out_fma(const float* P, const float* A, const float* wt, int num_iter, float step, float mom, float* O,
+    int w, int h);
 
 typedef struct vo_hyper {
     float alpha, beta, gamma;
@@ -93,6 +96,10 @@ int vo_stab_pass(int w, int h, const float* const orig[3], const float* const pr
 int vo_stab_pass_ex(int w, int h, const float* const orig[3], const float* const proc[3], const float* flow_fwd,
     const float* flow_bwd, int fc, const float* last_stab, const vo_hyper* hp, int occlusion_mask, float* out_f32,
     uint8_t* out_rgba);
+/* vo_stab_pass_ex with the solver in the exact (0) or the FMA form (1). */
+int vo_stab_pass_form(int w, int h, const float* const orig[3], const float* const proc[3], const float* flow_fwd,
+    const float* flow_bwd, int fc, const float* last_stab, const vo_hyper* hp, int occlusion_mask, int solver_form,
+    float* out_f32, uint8_t* out_rgba);
 
 /* ---- weight-free flow estimator built from the two ops ---------------------
  * A coarse-to-fine stand-in for the missing PWC-Net weights: random-projection

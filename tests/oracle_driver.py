@@ -5,7 +5,7 @@ from __future__ import annotations
 import numpy as np
 
 
-def run_oracle_stream(oracle, frames, flows=None, hp=None, downscale=1, occlusion=False):
+def run_oracle_stream(oracle, frames, flows=None, hp=None, downscale=1, occlusion=False, solver_form="exact"):
     """The reference's driver loop (stabilizefiles.cpp:108-131 with
     videostabilizer.cpp:136-265) over the restatement."""
     orig = [oracle.rgba_to_float(o) for o, _ in frames]
@@ -24,7 +24,8 @@ def run_oracle_stream(oracle, frames, flows=None, hp=None, downscale=1, occlusio
         else:
             ff = oracle.flow_estimate(orig[t], orig[t + 1])
             fb = oracle.flow_estimate(orig[t + 1], orig[t])
-        out, rgba = oracle.stab_pass(orig[t - 1:t + 2], proc[t - 1:t + 2], ff, fb, last, hp, occlusion_mask=occlusion)
+        out, rgba = oracle.stab_pass(orig[t - 1:t + 2], proc[t - 1:t + 2], ff, fb, last, hp, occlusion_mask=occlusion,
+                                     solver_form=solver_form)
         outs.append((out, rgba, ff, fb))
         last = out
     return outs

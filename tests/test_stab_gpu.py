@@ -123,6 +123,47 @@ def test_consist_out(vsc, oracle, cuda, h, w, iters):
     assert np.array_equal(O2.cpu().numpy().view(np.uint32), O.cpu().numpy().view(np.uint32))
 
 
+# the FMA form: widths divisible by 4 take the TMA-fed kernel, others the
+# plain-load one; iteration counts not divisible by 8 end in a short launch
+@pytest.mark.parametrize("h,w,iters", [(9, 11, 0), (9, 11, 1), (9, 11, 2), (40, 56, 75), (3, 3, 5), (2, 2, 4),
+                                       (67, 33, 150), (48, 200, 13), (540, 960, 75), (1080, 1920, 150),
+                                       (17, 4, 3), (100, 64, 150), (61, 70, 19)])
+def test_consist_out_fma(vsc, oracle, cuda, h, w, iters):
+    """vsc_get_consist_out_fma equals the restatement's FMA form bit for bit,
+    and the exact form (kernel_consist_out's rounding) within the stated
+    tolerance: max-abs <= 2e-6 on [0, 1] images, PSNR >= 100 dB, RGBA8
+    bytes differing on at most 1e-3 of the values."""
+    import math
+
+    import torch
+
+    P, A, Wt, O0 = _img(h, w), _img(h, w), _img(h, w, hi=2.0), _img(h, w)
+    O = _t(O0, cuda)
+    vsc.get_consist_out(_t(P, cuda), _t(A, cuda), _t(Wt, cuda), iters, 0.15, 0.15, O, form="fma")
+    got = O.cpu().numpy()
+    ref = oracle.consist_out(P, A, Wt, iters, 0.15, 0.15, O0, form="fma")
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+    exact = oracle.consist_out(P, A, Wt, iters, 0.15, 0.15, O0)
+    d = np.abs(got.astype(np.float64) - exact)
+    mse = float(np.mean(d * d))
+    psnr = math.inf if mse == 0 else 10 * math.log10(1.0 / mse)
+    flips = float(np.mean(oracle.float_to_rgba(got)[..., :3] != oracle.float_to_rgba(exact)[..., :3]))
+    print(f"fma vs exact {w}x{h} x{iters}: max-abs {d.max():.3g}, PSNR {psnr:.1f} dB, RGBA8 byte flips {flips:.2e}")
+    assert d.max() <= 2e-6 and psnr >= 100.0 and flips <= 1e-3
+    # caller-provided workspace gives the same bits
+    ws = torch.empty(vsc.consist_out_workspace_size(w, h) // 4, dtype=torch.float32, device=cuda)
+    O2 = _t(O0, cuda)
+    vsc.get_consist_out(_t(P, cuda), _t(A, cuda), _t(Wt, cuda), iters, 0.15, 0.15, O2, workspace=ws, form="fma")
+    assert np.array_equal(O2.cpu().numpy().view(np.uint32), got.view(np.uint32))
+
+
+def test_consist_out_fma_single_tile_shape(vsc, cuda):
+    """The FMA form has one tile shape (64 x 48); the autotuner reports it
+    without measuring."""
+    assert vsc.solver_autotune(960, 544, form="fma") == 48
+    assert vsc.solver_tile_rows(960, 544, form="fma") == (48, False)
+
+
 def test_consist_out_zero_regions(vsc, oracle, cuda):
     """All-zero regions (black borders, zero weights) where the sign of a
     zero can differ from the oracle's: the values and the RGBA8 bytes are
@@ -435,6 +476,26 @@ def test_whole_step_equals_restatement(vsc, oracle, cuda, w, h, nframes):
     st.close()
 
 
+@pytest.mark.parametrize("w,h,nframes", [(640, 360, 3), (1920, 1080, 4), (70, 45, 4)])
+def test_whole_step_fma_form_equals_restatement(vsc, oracle, cuda, w, h, nframes):
+    """doOneStep with the FMA solver form equals the restatement's pass with
+    that form bit for bit (the warps, mask and combination are unchanged;
+    70x45 takes the plain-load kernel at both levels)."""
+    frames = _frames(w, h, nframes, seed=23)
+    ref = run_oracle_stream(oracle, frames, solver_form="fma")
+    st = vsc.Stabilizer(w, h, solver_form="fma")
+    for i in range(3):
+        st.load_frame(*frames[i])
+    for k, t in enumerate(range(1, nframes - 1)):
+        out = st.step().cpu().numpy()
+        r_out, r_rgba, _, _ = ref[k]
+        assert np.array_equal(st.buffer(0).cpu().numpy().view(np.uint32), r_out.view(np.uint32)), f"step {k}"
+        assert np.array_equal(out, r_rgba), f"rgba, step {k}"
+        if t + 2 < nframes:
+            st.load_frame(*frames[t + 2])
+    st.close()
+
+
 def _psnr_rgb(a, b):
     import math
 
@@ -443,14 +504,16 @@ def _psnr_rgb(a, b):
     return math.inf if mse == 0 else 10 * math.log10(1.0 / mse)
 
 
-def test_fast_form_quality_at_1080p(vsc, cuda):
+@pytest.mark.parametrize("solver_form", ["exact", "fma"])
+def test_fast_form_quality_at_1080p(vsc, cuda, solver_form):
     """The benchmark's fast form (flow at 960x540 with bilinear upsampling,
-    BF16 tensor-core correlations) against the plain FP32 path on the same
-    1920x1080 stream: stabilized RGB at >= 40 dB PSNR in every one of six
-    consecutive frames (the feedback carries each frame's difference into
-    the next)."""
+    BF16 tensor-core correlations, the solver in either form) against the
+    plain FP32 path on the same 1920x1080 stream: stabilized RGB at >= 40 dB
+    PSNR in every one of six consecutive frames (the feedback carries each
+    frame's difference into the next)."""
     frames = _frames(1920, 1080, 8, seed=19)
-    sts = [vsc.Stabilizer(1920, 1080), vsc.Stabilizer(1920, 1080, flow_downscale=2, corr_dtype="bf16")]
+    sts = [vsc.Stabilizer(1920, 1080),
+           vsc.Stabilizer(1920, 1080, flow_downscale=2, corr_dtype="bf16", solver_form=solver_form)]
     for st in sts:
         for i in range(3):
             st.load_frame(*frames[i])
@@ -463,11 +526,12 @@ def test_fast_form_quality_at_1080p(vsc, cuda):
                 st.load_frame(*frames[t + 2])
     for st in sts:
         st.close()
-    print("fast form vs plain, PSNR per frame (dB):", [round(v, 2) for v in vals])
+    print(f"fast form ({solver_form} solver) vs plain, PSNR per frame (dB):", [round(v, 2) for v in vals])
     assert min(vals) >= 40.0, vals
 
 
-def _multistream_vs_singles(vsc, sizes, forms, fused, num_iter, upsampler=None, steps=5, levels=2):
+def _multistream_vs_singles(vsc, sizes, forms, fused, num_iter, upsampler=None, steps=5, levels=2,
+                            solver_form="exact"):
     """Runs a MultiStream and one Stabilizer per stream (each with the
     stream's (flow_downscale, corr_dtype) form) on the same frames and
     asserts equal outputs, bit for bit, on the direct first step and on the
@@ -478,11 +542,13 @@ def _multistream_vs_singles(vsc, sizes, forms, fused, num_iter, upsampler=None, 
     side = torch.cuda.Stream()
     ms = vsc.MultiStream(sizes, flow_downscale=[f[0] for f in forms], corr_dtype=[f[1] for f in forms], stream=side)
     ms.set_fused(fused)
+    if solver_form != "exact":
+        ms.set_solver_form(solver_form)
     ms.hyper_params.num_iter = num_iter
     ms.hyper_params.pyramid_levels = levels
     singles = []
     for (w, h), (ds, dt) in zip(sizes, forms):
-        st = vsc.Stabilizer(w, h, flow_downscale=ds, corr_dtype=dt)
+        st = vsc.Stabilizer(w, h, flow_downscale=ds, corr_dtype=dt, solver_form=solver_form)
         st.hyper_params.num_iter = num_iter
         st.hyper_params.pyramid_levels = levels
         if upsampler is not None and ds > 1:
@@ -529,6 +595,15 @@ def test_multistream_equals_independent_stabilizers(vsc, cuda, fused, levels):
     n, grouped = _multistream_vs_singles(vsc, sizes, [(1, "f32")] * 3, fused, 60, levels=levels)
     assert grouped == fused
     assert n > (3 * 20 if not fused else 8)
+
+
+@pytest.mark.parametrize("fused", [True, False])
+def test_multistream_fma_solver_equals_independent_stabilizers(vsc, cuda, fused):
+    """The FMA solver form in a multistream step, grouped or not: every
+    stream's output equals its own stabilizer's with that form."""
+    sizes = [(96, 64), (128, 72), (80, 48)]
+    _, grouped = _multistream_vs_singles(vsc, sizes, [(1, "f32")] * 3, fused, 45, solver_form="fma")
+    assert grouped == fused
 
 
 def test_multistream_mixed_forms_with_upsampler(vsc, cuda):

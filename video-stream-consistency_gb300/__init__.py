@@ -47,6 +47,8 @@ EXPORTED = [
     "vsc_stabilizer_set_upsampler", "vsc_solver_autotune", "vsc_solver_tile_rows", "vsc_solver_set_autotune",
     "vsc_multistream_set_fused", "vsc_multistream_fused", "vsc_multistream_set_upsampler",
     "vsc_stabilizer_synchronize", "vsc_stabilizer_wait_output",
+    "vsc_get_consist_out_fma", "vsc_solver_autotune_form", "vsc_solver_tile_rows_form",
+    "vsc_stabilizer_set_solver_form", "vsc_multistream_set_solver_form",
 ]
 VSC_DTYPE_F32, VSC_DTYPE_BF16, VSC_DTYPE_F16 = 0, 1, 2
 VSC_OUT_HOST_ASYNC = 2
@@ -134,6 +136,10 @@ def load():
         "vsc_get_consist_wt": [IP, IP, IP, f32, f32, vp],
         "vsc_get_bilinear": [IP, IP, vp],
         "vsc_get_consist_out": [IP, IP, IP, i32, f32, f32, IP, vp, C.c_size_t, vp],
+        "vsc_get_consist_out_fma": [IP, IP, IP, i32, f32, f32, IP, vp, C.c_size_t, vp],
+        "vsc_solver_autotune_form": [i32, i32, i32, vp, C.POINTER(i32)],
+        "vsc_stabilizer_set_solver_form": [vp, i32],
+        "vsc_multistream_set_solver_form": [vp, i32],
         "vsc_get_consist_out_noalloc": [IP, IP, IP, i32, f32, f32, IP, vp],
         "vsc_stabilizer_create": [C.POINTER(StabilizerConfig), vp, C.POINTER(vp)],
         "vsc_stabilizer_destroy": [vp],
@@ -192,6 +198,8 @@ def load():
     L.vsc_solver_steps_per_launch.argtypes = []
     L.vsc_solver_tile_rows.restype = i32
     L.vsc_solver_tile_rows.argtypes = [i32, i32, C.POINTER(i32)]
+    L.vsc_solver_tile_rows_form.restype = i32
+    L.vsc_solver_tile_rows_form.argtypes = [i32, i32, i32, C.POINTER(i32)]
     L.vsc_solver_set_autotune.restype = None
     L.vsc_solver_set_autotune.argtypes = [i32]
     L.vsc_correlation_lowp_workspace_size.restype = C.c_size_t
@@ -437,17 +445,21 @@ def get_bilinear(inp, ow: int, oh: int, stream=None):
     return out
 
 
-def solver_autotune(w: int, h: int, stream=None) -> int:
-    """Time both solver tile shapes at w x h and keep the faster; returns its rows (32 or 48)."""
+SOLVER_FORMS = {"exact": 0, "fma": 1}  # VSC_SOLVER_EXACT, VSC_SOLVER_FMA
+
+
+def solver_autotune(w: int, h: int, stream=None, form: str = "exact") -> int:
+    """Time both tile shapes of the exact solver form at w x h and keep the
+    faster; returns its rows (exact: 32 or 48; the fma form has one, 48)."""
     rows = C.c_int32()
-    _check(load().vsc_solver_autotune(int(w), int(h), _stream(stream), C.byref(rows)))
+    _check(load().vsc_solver_autotune_form(int(w), int(h), SOLVER_FORMS[form], _stream(stream), C.byref(rows)))
     return rows.value
 
 
-def solver_tile_rows(w: int, h: int):
+def solver_tile_rows(w: int, h: int, form: str = "exact"):
     """(rows, tuned): the tile rows a solve at w x h uses, and whether they were measured."""
     tuned = C.c_int32()
-    rows = load().vsc_solver_tile_rows(int(w), int(h), C.byref(tuned))
+    rows = load().vsc_solver_tile_rows_form(int(w), int(h), SOLVER_FORMS[form], C.byref(tuned))
     return rows, bool(tuned.value)
 
 
@@ -460,13 +472,14 @@ def consist_out_workspace_size(w: int, h: int) -> int:
 
 
 def get_consist_out(crnt_pr, prev_stab_warp, cons_wt, num_iter, step_size, mom_fac, consis_out, workspace=None,
-                    stream=None):
-    """In place on consis_out (initial solution in, result out)."""
+                    stream=None, form: str = "exact"):
+    """In place on consis_out (initial solution in, result out); form
+    "exact" (vsc_get_consist_out) or "fma" (vsc_get_consist_out_fma)."""
     ws = workspace.data_ptr() if workspace is not None else None
     nbytes = workspace.numel() * workspace.element_size() if workspace is not None else 0
-    _check(load().vsc_get_consist_out(C.byref(image(crnt_pr)), C.byref(image(prev_stab_warp)),
-                                      C.byref(image(cons_wt)), int(num_iter), float(step_size), float(mom_fac),
-                                      C.byref(image(consis_out)), ws, nbytes, _stream(stream)))
+    fn = {"exact": load().vsc_get_consist_out, "fma": load().vsc_get_consist_out_fma}[form]
+    _check(fn(C.byref(image(crnt_pr)), C.byref(image(prev_stab_warp)), C.byref(image(cons_wt)), int(num_iter),
+              float(step_size), float(mom_fac), C.byref(image(consis_out)), ws, nbytes, _stream(stream)))
     return consis_out
 
 
@@ -558,9 +571,10 @@ class Stabilizer:
     """
 
     def __init__(self, width, height, compute_flow=True, flow_downscale=1, flow_channels=3, stream=None,
-                 use_graphs=True, corr_dtype: str = "f32"):
+                 use_graphs=True, corr_dtype: str = "f32", solver_form: str = "exact"):
         """corr_dtype: "f32" (the plain method), "bf16" or "fp16" (the flow
-        estimator's correlations on the tensor cores)."""
+        estimator's correlations on the tensor cores); solver_form: "exact"
+        (the reference's arithmetic) or "fma" (vsc_stabilizer_set_solver_form)."""
         import torch
 
         self.width, self.height = width, height
@@ -571,6 +585,12 @@ class Stabilizer:
         h = C.c_void_p()
         _check(load().vsc_stabilizer_create(C.byref(cfg), _stream(self._stream_obj), C.byref(h)))
         self._h = h
+        if solver_form != "exact":
+            self.set_solver_form(solver_form)
+
+    def set_solver_form(self, form: str):
+        """"exact" or "fma": the blend solver's form for the following steps."""
+        _check(load().vsc_stabilizer_set_solver_form(self._h, SOLVER_FORMS[form]))
 
     @property
     def hyper_params(self) -> HyperParams:
@@ -698,6 +718,10 @@ class MultiStream:
 
     def set_fused(self, on: bool):
         _check(load().vsc_multistream_set_fused(self._h, 1 if on else 0))
+
+    def set_solver_form(self, form: str):
+        """"exact" or "fma" for every stream's solves."""
+        _check(load().vsc_multistream_set_solver_form(self._h, SOLVER_FORMS[form]))
 
     def set_upsampler(self, upsampler, index: int = -1):
         """The learned upsampler for stream `index` (-1: every stream with

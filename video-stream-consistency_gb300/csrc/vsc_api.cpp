@@ -493,11 +493,12 @@ VSC_API size_t vsc_consist_out_workspace_size(int32_t width, int32_t height)
     return solver_workspace_floats(width, height) * sizeof(float);
 }
 
-VSC_API vsc_status vsc_get_consist_out(const vsc_image* crnt_pr, const vsc_image* prev_stab_warp,
+namespace {
+
+vsc_status consist_out_form(int form, const vsc_image* crnt_pr, const vsc_image* prev_stab_warp,
     const vsc_image* cons_wt, int32_t num_iter, float step_size, float mom_fac, const vsc_image* consis_out,
     void* workspace, size_t workspace_bytes, vsc_stream_t stream)
 {
-    clear_error();
     vsc_status s;
     if ((s = check_image(crnt_pr, "crntPr", 3, 3)) || (s = check_image(prev_stab_warp, "prevStabWarp", 3, 3)) ||
         (s = check_image(cons_wt, "consWt", 3, 3)) || (s = check_image(consis_out, "consisOut", 3, 3)) ||
@@ -521,19 +522,47 @@ VSC_API vsc_status vsc_get_consist_out(const vsc_image* crnt_pr, const vsc_image
         pooled = true;
     }
     cudaError_t e = run_solver(crnt_pr->data, prev_stab_warp->data, cons_wt->data, consis_out->data, w, h, num_iter,
-        step_size, mom_fac, static_cast<float*>(ws), cs(stream), nullptr);
+        step_size, mom_fac, static_cast<float*>(ws), cs(stream), nullptr, nullptr, form);
     if (pooled)
         cudaFreeAsync(ws, cs(stream));
     return check_cuda(e, "consist_out launch");
+}
+
+}  // namespace
+
+VSC_API vsc_status vsc_get_consist_out(const vsc_image* crnt_pr, const vsc_image* prev_stab_warp,
+    const vsc_image* cons_wt, int32_t num_iter, float step_size, float mom_fac, const vsc_image* consis_out,
+    void* workspace, size_t workspace_bytes, vsc_stream_t stream)
+{
+    clear_error();
+    return consist_out_form(kSolverExact, crnt_pr, prev_stab_warp, cons_wt, num_iter, step_size, mom_fac, consis_out,
+        workspace, workspace_bytes, stream);
+}
+
+VSC_API vsc_status vsc_get_consist_out_fma(const vsc_image* crnt_pr, const vsc_image* prev_stab_warp,
+    const vsc_image* cons_wt, int32_t num_iter, float step_size, float mom_fac, const vsc_image* consis_out,
+    void* workspace, size_t workspace_bytes, vsc_stream_t stream)
+{
+    clear_error();
+    return consist_out_form(kSolverFma, crnt_pr, prev_stab_warp, cons_wt, num_iter, step_size, mom_fac, consis_out,
+        workspace, workspace_bytes, stream);
 }
 
 VSC_API int32_t vsc_solver_steps_per_launch(void) { return solver_steps_per_launch(); }
 
 VSC_API vsc_status vsc_solver_autotune(int32_t width, int32_t height, vsc_stream_t stream, int32_t* tile_rows)
 {
+    return vsc_solver_autotune_form(width, height, VSC_SOLVER_EXACT, stream, tile_rows);
+}
+
+VSC_API vsc_status vsc_solver_autotune_form(int32_t width, int32_t height, int32_t form, vsc_stream_t stream,
+    int32_t* tile_rows)
+{
     clear_error();
     if (width < 1 || height < 1)
         return set_error(VSC_EINVAL, "solver_autotune: size %dx%d", width, height);
+    if (form != VSC_SOLVER_EXACT && form != VSC_SOLVER_FMA)
+        return set_error(VSC_EINVAL, "solver_autotune: unknown solver form %d", form);
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     vsc_status s = check_cuda(cudaStreamIsCapturing(cs(stream), &cap), "solver_autotune");
     if (s)
@@ -541,7 +570,7 @@ VSC_API vsc_status vsc_solver_autotune(int32_t width, int32_t height, vsc_stream
     if (cap != cudaStreamCaptureStatusNone)
         return set_error(VSC_ESTATE, "solver_autotune: the stream is being captured");
     int rows = 0;
-    s = check_cuda(solver_autotune(width, height, cs(stream), &rows), "solver_autotune");
+    s = check_cuda(solver_autotune(width, height, cs(stream), &rows, form), "solver_autotune");
     if (!s && tile_rows)
         *tile_rows = rows;
     return s;
@@ -549,8 +578,14 @@ VSC_API vsc_status vsc_solver_autotune(int32_t width, int32_t height, vsc_stream
 
 VSC_API int32_t vsc_solver_tile_rows(int32_t width, int32_t height, int32_t* tuned)
 {
+    return vsc_solver_tile_rows_form(width, height, VSC_SOLVER_EXACT, tuned);
+}
+
+VSC_API int32_t vsc_solver_tile_rows_form(int32_t width, int32_t height, int32_t form, int32_t* tuned)
+{
     bool t = false;
-    const int rows = width > 0 && height > 0 ? solver_tile_rows(width, height, &t) : 0;
+    const bool ok = width > 0 && height > 0 && (form == VSC_SOLVER_EXACT || form == VSC_SOLVER_FMA);
+    const int rows = ok ? solver_tile_rows(width, height, &t, form) : 0;
     if (tuned)
         *tuned = t ? 1 : 0;
     return rows;
@@ -676,6 +711,7 @@ struct vsc_stabilizer {
     FlowDims fd{};
     int last_launches = 0;
     bool occlusion = false;  // opt-in forward-backward consistency mask
+    int solver_form = kSolverExact;  // VSC_SOLVER_EXACT / VSC_SOLVER_FMA
     // learned flow upsampling (flow_downscale > 1); null: bilinear
     vsc_upsampler* upsampler = nullptr;
     float* up_work = nullptr;  // input (2 x w x h x 3), activations, residual
@@ -691,6 +727,7 @@ struct vsc_stabilizer {
         uint8_t* rgba = nullptr;
         vsc_hyper_params hp{};
         bool timing = false, occlusion = false;
+        int solver_form = kSolverExact;
         const vsc_upsampler* upsampler = nullptr;
         cudaGraphExec_t exec = nullptr;
         uint64_t used = 0;
@@ -889,6 +926,19 @@ vsc_status alloc_all(vsc_stabilizer* s)
     return check_cuda(e, "stabilizer allocation");
 }
 
+// The solver's tile shape of a form for the pyramid's sizes (a stream being
+// captured keeps the wave model; a failed measurement too).
+void tune_pyramid(vsc_stabilizer* s, int form)
+{
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s->st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone)
+        for (int j = 0; j < std::min(s->levels_alloc, 4); ++j)
+            if (solver_autotune(s->lw[j], s->lh[j], s->st, nullptr, form) != cudaSuccess) {
+                cudaGetLastError();
+                break;
+            }
+}
+
 }  // namespace
 
 extern "C" {
@@ -931,14 +981,7 @@ VSC_API vsc_status vsc_stabilizer_create(const vsc_stabilizer_config* cfg, vsc_s
         delete s;
         return st;
     }
-    // the solver's tile shape for the pyramid's sizes (a stream being captured keeps the model)
-    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    if (cudaStreamIsCapturing(s->st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone)
-        for (int j = 0; j < std::min(s->levels_alloc, 4); ++j)
-            if (solver_autotune(s->lw[j], s->lh[j], s->st, nullptr) != cudaSuccess) {
-                cudaGetLastError();  // a failed measurement leaves the model's choice
-                break;
-            }
+    tune_pyramid(s, kSolverExact);
     *out = s;
     return VSC_OK;
 }
@@ -1225,7 +1268,7 @@ cudaError_t enqueue_step(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t*
             ++nl;
         }
         run(run_solver(P[j], A[j], W[j], O[j], s->lw[j], s->lh[j], hp.num_iter / (j + 1), hp.step_size, hp.mom_fac,
-            s->solver_ws, st, &nl, j == 0 ? rgba_dev : nullptr));
+            s->solver_ws, st, &nl, j == 0 ? rgba_dev : nullptr, s->solver_form));
     }
     mark(s, kEvStep1);
     *launches = nl;
@@ -1243,7 +1286,8 @@ bool launch_step_graph(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t* r
     auto* hit = static_cast<vsc_stabilizer::GraphEntry*>(nullptr);
     for (auto& g : s->graphs)
         if (g.valid && g.head == s->head && g.ls_cur == s->ls_cur && g.rgba == rgba_dev && g.timing == s->timing &&
-            g.occlusion == s->occlusion && g.upsampler == s->upsampler && same_hp(g.hp, hp))
+            g.occlusion == s->occlusion && g.solver_form == s->solver_form && g.upsampler == s->upsampler &&
+            same_hp(g.hp, hp))
             hit = &g;
     if (!hit) {
         auto* slot = &s->graphs[0];
@@ -1282,6 +1326,7 @@ bool launch_step_graph(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t* r
         slot->rgba = rgba_dev;
         slot->timing = s->timing;
         slot->occlusion = s->occlusion;
+        slot->solver_form = s->solver_form;
         slot->upsampler = s->upsampler;
         slot->hp = hp;
         slot->nl = nl;
@@ -1624,6 +1669,22 @@ VSC_API vsc_status vsc_stabilizer_set_occlusion_mask(vsc_stabilizer* s, int32_t 
     return VSC_OK;
 }
 
+VSC_API vsc_status vsc_stabilizer_set_solver_form(vsc_stabilizer* s, int32_t form)
+{
+    clear_error();
+    if (!s)
+        return set_error(VSC_EINVAL, "set_solver_form: null stabilizer");
+    if (form != VSC_SOLVER_EXACT && form != VSC_SOLVER_FMA)
+        return set_error(VSC_EINVAL, "set_solver_form: unknown solver form %d", form);
+    DeviceGuard g(s->device);
+    if (form == VSC_SOLVER_FMA && !solver_tma_supported())
+        return set_error(VSC_EUNSUPPORTED, "set_solver_form: the FMA form needs the solver's shared-memory opt-in");
+    if (form != s->solver_form)
+        tune_pyramid(s, form);
+    s->solver_form = form;
+    return VSC_OK;
+}
+
 VSC_API vsc_status vsc_stabilizer_enable_timing(vsc_stabilizer* s, int32_t on)
 {
     clear_error();
@@ -1675,6 +1736,7 @@ struct vsc_multistream {
     bool fused_ok = false;  // every stream's level sizes take the TMA path
     std::vector<float*> lvl_ws;  // per stream: solver workspaces of levels 1 ..
     int tuned_levels = 0;        // levels whose group tile shape was autotuned
+    int solver_form = kSolverExact;
     std::vector<cudaStream_t> side;
     std::vector<cudaEvent_t> loaded, joined;
     cudaEvent_t fork = nullptr, done = nullptr;
@@ -1775,7 +1837,8 @@ cudaError_t ms_enqueue_fused(vsc_multistream* m, const std::vector<uint8_t*>& ou
             break;
         e = enqueue_pre_solve(s, hp, &lv[i], &nl);
         for (int j = 0; j < L && e == cudaSuccess; ++j) {
-            e = solver_lap(lv[i].P[j], s->lw[j], s->lh[j], ms_level_ws(m, i, j), s->st);
+            e = solver_prep(m->solver_form, lv[i].P[j], lv[i].A[j], lv[i].W[j], s->lw[j], s->lh[j], hp.step_size,
+                ms_level_ws(m, i, j), s->st);
             ++nl;
         }
         // videostabilizer.cpp:212-217: the coarsest level starts from P
@@ -1807,7 +1870,8 @@ cudaError_t ms_enqueue_fused(vsc_multistream* m, const std::vector<uint8_t*>& ou
             nl += static_cast<int>((n + 15) / 16);
         }
         if (e == cudaSuccess)
-            e = run_solver_group(im.data(), static_cast<int>(n), it, hp.step_size, hp.mom_fac, m->main, &nl);
+            e = run_solver_group(im.data(), static_cast<int>(n), it, hp.step_size, hp.mom_fac, m->main, &nl,
+                m->solver_form);
     }
     *launches = nl;
     return e;
@@ -1829,6 +1893,34 @@ bool ms_use_fused(vsc_multistream* m)
                 return false;
     }
     return true;
+}
+
+// The tile shape of each level's group for a solver form (a stream being
+// captured, or a failed measurement, keeps the wave model).
+void ms_tune(vsc_multistream* m, int form)
+{
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(m->main, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+        return;
+    int levels = 4;
+    for (vsc_stabilizer* st : m->st)
+        levels = std::min(levels, st->levels_alloc);
+    std::vector<int> ws(m->st.size()), hs(m->st.size());
+    for (int j = 0; j < levels; ++j) {
+        bool eligible = true;
+        for (size_t i = 0; i < m->st.size(); ++i) {
+            ws[i] = m->st[i]->lw[j];
+            hs[i] = m->st[i]->lh[j];
+            eligible = eligible && ws[i] % 4 == 0;
+        }
+        if (!eligible)
+            break;
+        if (solver_group_autotune(ws.data(), hs.data(), static_cast<int>(ws.size()), m->main, nullptr, form) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            break;
+        }
+    }
 }
 
 void ms_drop_graphs(vsc_multistream* m)
@@ -1966,28 +2058,8 @@ VSC_API vsc_status vsc_multistream_create(const vsc_stream_desc* desc, int32_t n
             break;
         m->lvl_ws.push_back(p);
     }
-    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    if (!s && cudaStreamIsCapturing(m->main, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone) {
-        int levels = 4;
-        for (vsc_stabilizer* st : m->st)
-            levels = std::min(levels, st->levels_alloc);
-        std::vector<int> ws(m->st.size()), hs(m->st.size());
-        for (int j = 0; j < levels; ++j) {
-            bool eligible = true;
-            for (size_t i = 0; i < m->st.size(); ++i) {
-                ws[i] = m->st[i]->lw[j];
-                hs[i] = m->st[i]->lh[j];
-                eligible = eligible && ws[i] % 4 == 0;
-            }
-            if (!eligible)
-                break;
-            if (solver_group_autotune(ws.data(), hs.data(), static_cast<int>(ws.size()), m->main, nullptr) !=
-                cudaSuccess) {
-                cudaGetLastError();  // a failed measurement leaves the model's choice
-                break;
-            }
-        }
-    }
+    if (!s)
+        ms_tune(m, kSolverExact);
     if (s) {
         const std::string msg = vsc_last_error();
         ms_free(m);
@@ -2029,6 +2101,26 @@ VSC_API vsc_status vsc_multistream_set_fused(vsc_multistream* m, int32_t on)
 }
 
 VSC_API int32_t vsc_multistream_fused(vsc_multistream* m) { return m && ms_use_fused(m) ? 1 : 0; }
+
+VSC_API vsc_status vsc_multistream_set_solver_form(vsc_multistream* m, int32_t form)
+{
+    clear_error();
+    if (!m)
+        return set_error(VSC_EINVAL, "multistream_set_solver_form: null argument");
+    if (form != VSC_SOLVER_EXACT && form != VSC_SOLVER_FMA)
+        return set_error(VSC_EINVAL, "multistream_set_solver_form: unknown solver form %d", form);
+    DeviceGuard g(m->device);
+    vsc_status s = check_cuda(cudaStreamSynchronize(m->main), "multistream_set_solver_form");
+    for (size_t i = 0; i < m->st.size() && !s; ++i)
+        s = vsc_stabilizer_set_solver_form(m->st[i], form);
+    if (s)
+        return s;
+    if (form != m->solver_form)
+        ms_tune(m, form);
+    m->solver_form = form;
+    ms_drop_graphs(m);
+    return VSC_OK;
+}
 
 VSC_API vsc_status vsc_multistream_set_upsampler(vsc_multistream* m, int32_t index, vsc_upsampler* u)
 {

@@ -138,31 +138,39 @@ cudaError_t launch_bilinear_group(const Img* in, const Img* out, int n, cudaStre
 // flowmodel.cpp:126-133): source = min(iw-1, ((2x+1)*iw) / (2*ow)).
 cudaError_t launch_resize_nearest(const float* in, int iw, int ih, float* out, int ow, int oh, cudaStream_t st);
 
-// Solver.  The workspace holds the Laplacian of the processed image, two
-// momentum images and the second Jacobi buffer: 4 * w*h*3 floats.
+// Solver.  The workspace holds the Laplacian of the processed image (the
+// FMA form: its per-pixel constant Cs), two momentum images and the second
+// Jacobi buffer: 4 * w*h*3 floats.
+//   kSolverExact: kernel_consist_out's expression, bit for bit;
+//   kSolverFma:   the same step regrouped around per-solve constants with
+//                 fused multiply-adds (within a tolerance of the exact form;
+//                 equal to the restatement's FMA form).
+enum SolverForm { kSolverExact = 0, kSolverFma = 1 };
 size_t solver_workspace_floats(int w, int h);
 int solver_steps_per_launch();  // Jacobi steps one solver launch performs (temporal blocking)
 // Tile-shape autotuner of the persistent solver kernels (same results either
 // way): solver_autotune times both shapes at (w, h) on scratch images and
 // keeps the faster for the current device (synchronises `st`; not during
 // stream capture); solver_tile_rows reports the rows of the tile a solve at
-// (w, h) uses (tuned, or the wave model's choice).
-cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out);
-int solver_tile_rows(int w, int h, bool* tuned);
+// (w, h) uses (tuned, or the wave model's choice); per solver form.
+cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out, int form = kSolverExact);
+int solver_tile_rows(int w, int h, bool* tuned, int form = kSolverExact);
 void solver_set_autotune(bool on);
 // The same for the sizes one grouped launch solves together (one image per
 // stream of a multi-stream step), keyed by the whole list.
-cudaError_t solver_group_autotune(const int* w, const int* h, int n, cudaStream_t st, int* rows_out);
-int solver_group_tile_rows(const int* w, const int* h, int n, bool* tuned);
+cudaError_t solver_group_autotune(const int* w, const int* h, int n, cudaStream_t st, int* rows_out,
+    int form = kSolverExact);
+int solver_group_tile_rows(const int* w, const int* h, int n, bool* tuned, int form = kSolverExact);
 // Runs num_iter iterations; O holds the initial solution and receives the
 // result.  Returns the number of kernels launched through *launches.
 cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,
-    float step, float mom, float* workspace, cudaStream_t st, int* launches, uint8_t* rgba_out = nullptr);
+    float step, float mom, float* workspace, cudaStream_t st, int* launches, uint8_t* rgba_out = nullptr,
+    int form = kSolverExact);
 
 // Grouped solve: n images of any sizes, the same iterations, each launch of
 // the persistent kernel walking the tiles of all of them (up to 16 images
 // per launch).  Per image, before run_solver_group on the same stream:
-// solver_lap(P) into its workspace, and the initial solution written to
+// solver_prep(form, ...) into its workspace, and the initial solution written to
 // solver_start_buffer(O, ...) (O itself or the workspace's second buffer,
 // whichever makes the last launch write O).  Needs solver_group_eligible
 // (width % 4 == 0 and 16-byte aligned images, the TMA path).
@@ -178,9 +186,12 @@ struct SolverImage {
 float* solver_start_buffer(float* O, int w, int h, int num_iter, float* workspace);
 bool solver_tma_supported();  // the persistent TMA kernels run on the current device
 cudaError_t solver_lap(const float* P, int w, int h, float* workspace, cudaStream_t st);
+// the per-solve precomputation of a form: lap P (exact) or Cs (FMA), into the workspace
+cudaError_t solver_prep(int form, const float* P, const float* A, const float* Wt, int w, int h, float step,
+    float* workspace, cudaStream_t st);
 bool solver_group_eligible(const SolverImage* im, int n);
 cudaError_t run_solver_group(const SolverImage* im, int n, int num_iter, float step, float mom, cudaStream_t st,
-    int* launches);
+    int* launches, int form = kSolverExact);
 
 // Device-side bounded waits record a timeout in a device flag instead of
 // hanging; this reads and clears it for the current device.

@@ -247,7 +247,6 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
     }
     __syncthreads();
 
-    // tiles whose every pixel has all four neighbours take the packed path
     // tiles whose every pixel has all four neighbours skip the validity selects
     const bool interior = ox >= 1 && oy >= 1 && ox + kTbEX - 1 <= w - 3 && oy + kTbEY - 1 <= h - 3;
     if (interior)
@@ -854,6 +853,414 @@ __global__ void __launch_bounds__(kPThreads, 1)
         bulk_wait_all();
 }
 
+// ---- FMA form of the solver ---------------------------------------------------
+// kernel_consist_out's step, g = (lap O - lap P) - w (O - A), O' = O + s g
+// (+ m U), U' = s g, regrouped around two per-pixel constants:
+//   Cs = s * fma(w, A, -lap P)   once per solve (solver_prep_fma_kernel),
+//   nK = -(s * (cnt + w))        when a tile is loaded (cnt = valid neighbours),
+// so that one step is
+//   S = (left + right) + (up + down),  g = fma(nK, O, fma(s, S, Cs)),
+//   O' = O + g, then O' = fma(m, U, O') after the first step,  U' = g,
+// with invalid neighbours read as +0: seven FP32 operations per pixel and
+// channel against twelve in the reference expression, and a tile loads four
+// images (O, U, consWt, Cs) instead of five.  The rounding differs from the
+// reference form's, so results agree with it within a tolerance (and with
+// the restatement's FMA form, vo_consist_out_fma, bit for bit).  Tiles: 64 x
+// 4*kWarps pixels, each thread a 2-column x 4-row block, register state O,
+// U, Cs, nK as column pairs per row and channel.
+
+// Cs = step * fma(wt, A, -lap P); lap P as lap_pr_kernel computes it.
+__global__ void solver_prep_fma_kernel(const float* __restrict__ P, const float* __restrict__ A,
+    const float* __restrict__ Wt, float* __restrict__ Cs, int w, int h, float step)
+{
+    pdl_enter();
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h)
+        return;
+    const int64_t i0 = pix_index(x, y, w) * 3;
+    const int64_t rs = static_cast<int64_t>(w) * 3;
+    for (int c = 0; c < 3; ++c) {
+        const int64_t i = i0 + c;
+        int cnt = 0;
+        float lap = 0.0f;
+        if ((x + 1) < (w - 1)) {
+            lap += P[i + 3];
+            cnt += 1;
+        }
+        if ((x - 1) >= 0) {
+            lap += P[i - 3];
+            cnt += 1;
+        }
+        if ((y + 1) < (h - 1)) {
+            lap += P[i + rs];
+            cnt += 1;
+        }
+        if ((y - 1) >= 0) {
+            lap += P[i - rs];
+            cnt += 1;
+        }
+        lap = __fsub_rn(lap, __fmul_rn(static_cast<float>(cnt), P[i]));
+        Cs[i] = __fmul_rn(step, __fmaf_rn(Wt[i], A[i], -lap));
+    }
+}
+
+template <int kWarps>
+struct FmaTile {
+    static constexpr int kThreads = 32 * kWarps;
+    static constexpr int kRows = 4 * kWarps;            // tile rows
+    static constexpr int kIRows = kRows - 2 * kTbT;     // interior rows
+    static constexpr int kStageFloats = kRows * kTbEX * 3;
+    static constexpr int kStageBytes = kStageFloats * static_cast<int>(sizeof(float));
+    static constexpr int kPlane = (kWarps + 2) * 2 * kTbPX;  // edge-row slots of one channel and buffer
+    static constexpr int kObuf = 2 * 3 * kPlane;
+    static constexpr int kSmem = 4 * kStageBytes + kObuf * static_cast<int>(sizeof(float)) + 16;
+    static_assert(kSmem <= 232448, "dynamic shared memory per CTA");
+    static_assert(kObuf >= 2 * kIRows * 3 * kIW, "the edge-row buffers hold a tile's interior O and U");
+    static_assert((kIRows * 3 * kIW * 4) % 128 == 0 && (4 * kStageBytes) % 128 == 0,
+        "TMA store sources on the 128-byte grid");
+};
+
+// 12 warps: three on each quarter of the SM's register file (16,384
+// registers), so up to 170 registers a thread; the state takes 96.  (With 14
+// warps, four on some quarters, a thread gets 128 and the state spills.)
+constexpr int kFmaWarps = 12;
+
+struct FmaState {
+    float2 o[4][3], u[4][3], c[4][3], nk[4][3];  // [row][channel] = (column 0, column 1)
+};
+
+// One step of a thread's 2 x 4 block: the previous iterate's edge rows of the
+// neighbouring warps come from `src`, the new top and bottom rows go to `dst`.
+template <bool kAll, int kPlane>
+__device__ __forceinline__ void fma_step(FmaState& s, const float* src, float* dst, bool mom_on, float step,
+    float mom, int px0, int warp, int gx0, int gy0, int w, int h)
+{
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        const float* S = src + ch * kPlane;
+        const float2 up = *reinterpret_cast<const float2*>(&S[(warp * 2 + 1) * kTbPX + px0 + 2]);
+        const float2 dn = *reinterpret_cast<const float2*>(&S[((warp + 2) * 2) * kTbPX + px0 + 2]);
+        float L[4], R[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            L[r] = __shfl_up_sync(0xffffffffu, s.o[r][ch].y, 1);
+            R[r] = __shfl_down_sync(0xffffffffu, s.o[r][ch].x, 1);
+        }
+        float2 on[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const float2 o = s.o[r][ch];
+            float2 u = r == 0 ? up : s.o[r - 1][ch];
+            float2 d = r == 3 ? dn : s.o[r + 1][ch];
+            float l0 = L[r], r0 = o.y, l1 = o.x, r1 = R[r];
+            if (!kAll) {
+                const Nb a = nb_of(gx0, gy0 + r, w, h), b = nb_of(gx0 + 1, gy0 + r, w, h);
+                l0 = a.vl ? l0 : 0.0f;
+                r0 = a.vr ? r0 : 0.0f;
+                u.x = a.vu ? u.x : 0.0f;
+                d.x = a.vd ? d.x : 0.0f;
+                l1 = b.vl ? l1 : 0.0f;
+                r1 = b.vr ? r1 : 0.0f;
+                u.y = b.vu ? u.y : 0.0f;
+                d.y = b.vd ? d.y : 0.0f;
+            }
+            // scalar FP32: the FMA pipe is the limit, where a packed f32x2
+            // operation costs both lanes' cycles and pairing its operands costs
+            // register moves on the same pipe (measured 11 % slower)
+            float2 g, n;
+            g.x = __fmaf_rn(s.nk[r][ch].x, o.x,
+                __fmaf_rn(step, __fadd_rn(__fadd_rn(l0, r0), __fadd_rn(u.x, d.x)), s.c[r][ch].x));
+            g.y = __fmaf_rn(s.nk[r][ch].y, o.y,
+                __fmaf_rn(step, __fadd_rn(__fadd_rn(l1, r1), __fadd_rn(u.y, d.y)), s.c[r][ch].y));
+            n.x = __fadd_rn(o.x, g.x);
+            n.y = __fadd_rn(o.y, g.y);
+            if (mom_on) {
+                n.x = __fmaf_rn(mom, s.u[r][ch].x, n.x);
+                n.y = __fmaf_rn(mom, s.u[r][ch].y, n.y);
+            }
+            s.u[r][ch] = g;
+            on[r] = n;
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+            s.o[r][ch] = on[r];
+        float* D = dst + ch * kPlane + ((warp + 1) * 2) * kTbPX + px0 + 2;
+        *reinterpret_cast<float2*>(D) = on[0];           // top row
+        *reinterpret_cast<float2*>(D + kTbPX) = on[3];   // bottom row
+    }
+}
+
+// Iteration k is needed on rows [ring - T + k + 1, kRows - ring + T - k - 1)
+// (ring = kTbT); a warp whose four rows all lie outside skips it.
+template <bool kAll, int kWarps>
+__device__ __forceinline__ void fma_iterate(FmaState& s, float* obuf, int T, int k0, float step, float mom, int px0,
+    int warp, int gx0, int gy0, int w, int h)
+{
+    using G = FmaTile<kWarps>;
+    const int r0 = 4 * warp;
+    if (T == kTbT) {
+        // full launches, unrolled; momentum is off only in the first step of a solve
+        const bool later = k0 > 0;
+#pragma unroll
+        for (int k = 0; k < kTbT; ++k) {
+            if (!(r0 + 3 < k + 1 || r0 >= G::kRows - k - 1))
+                fma_step<kAll, G::kPlane>(s, obuf + (k & 1) * 3 * G::kPlane, obuf + ((k & 1) ^ 1) * 3 * G::kPlane,
+                    k > 0 || later, step, mom, px0, warp, gx0, gy0, w, h);
+            __syncthreads();
+        }
+        return;
+    }
+    for (int k = 0; k < T; ++k) {
+        const int lo = kTbT - T + k + 1, hi = G::kRows - kTbT + T - k - 1;
+        if (!(r0 + 3 < lo || r0 >= hi))
+            fma_step<kAll, G::kPlane>(s, obuf + (k & 1) * 3 * G::kPlane, obuf + ((k & 1) ^ 1) * 3 * G::kPlane,
+                (k0 + k) > 0, step, mom, px0, warp, gx0, gy0, w, h);
+        __syncthreads();
+    }
+}
+
+// stage i of the FMA kernels holds map fma_map(i): O, U, consWt, Cs
+__device__ __forceinline__ int fma_map(int i) { return i < 2 ? i : i + 1; }
+
+__device__ __forceinline__ void fma_issue(float* stage, const CUtensorMap* m, int ox, int oy, int stage_floats,
+    int first, int last, uint64_t* bar)
+{
+    for (int i = first; i < last; ++i)
+        tma_load_2d(stage + i * stage_floats, m + fma_map(i), 3 * ox, oy, bar);
+}
+
+// The first tile of a launch: consWt and Cs, which no solver launch writes,
+// before the wait for the predecessor (a launch after the first of a solve);
+// O and U after it.
+__device__ __forceinline__ void fma_issue_first(float* stage, const CUtensorMap* m, int ox, int oy,
+    int stage_floats, uint32_t bytes, uint64_t* bar, bool early)
+{
+    if (early) {
+        mbar_expect_tx(bar, 4 * bytes);
+        fma_issue(stage, m, ox, oy, stage_floats, 2, 4, bar);
+    }
+    grid_dependency_wait();
+    if (early) {
+        fma_issue(stage, m, ox, oy, stage_floats, 0, 2, bar);
+    } else {
+        mbar_expect_tx(bar, 4 * bytes);
+        fma_issue(stage, m, ox, oy, stage_floats, 0, 4, bar);
+    }
+}
+
+// The images of a solve for the plain-load form of the FMA kernel (widths
+// that are not a multiple of 4, or images off the 16-byte grid): raw pointers
+// instead of tensor maps.
+struct FmaPlain {
+    const float *O, *U, *W, *C;
+    float *Oo, *Uo;
+    int w, h, tiles_x, ntiles;
+    uint8_t* rgba;
+};
+
+// Stage <- tile at (ox, oy) of the four images, zero outside the image.
+template <int kWarps>
+__device__ __forceinline__ void fma_plain_load(float* stage, const FmaPlain& p, int ox, int oy)
+{
+    using G = FmaTile<kWarps>;
+    const float* src[4] = {p.O, p.U, p.W, p.C};
+    for (int i = threadIdx.x; i < G::kRows * 3 * kTbEX; i += G::kThreads) {
+        const int row = i / (3 * kTbEX), col = i - row * (3 * kTbEX);
+        const int gy = oy + row, gx = ox + col / 3;
+        const bool in = gx >= 0 && gx < p.w && gy >= 0 && gy < p.h;
+        const int64_t idx = in ? pix_index(gx, gy, p.w) * 3 + col % 3 : 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+            stage[a * G::kStageFloats + i] = in ? src[a][idx] : 0.0f;
+    }
+}
+
+// The body of both FMA kernels: kTma = true walks the tiles of a SolverGroup
+// (TMA loads one tile ahead, TMA stores), false the tiles of one FmaPlain
+// image (plain loads and stores).
+template <int kN, int kWarps, bool kTma>
+__device__ __forceinline__ void fma_body(const SolverGroup<kN>& g, const FmaPlain& pl, int T, int k0, float step,
+    float mom)
+{
+    using G = FmaTile<kWarps>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* stage = reinterpret_cast<float*>(smem_raw);
+    float* obuf = stage + 4 * G::kStageFloats;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(obuf + G::kObuf);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int px0 = 2 * lane, py0 = 4 * warp;
+
+    for (int i = threadIdx.x; i < G::kObuf; i += G::kThreads)
+        obuf[i] = 0.0f;  // the apron slots start at zero
+    if (kTma && threadIdx.x == 0)
+        mbar_init(bar, 1);
+    __syncthreads();
+    const int ntiles = kTma ? g.tile0[g.count] : pl.ntiles;
+    int tile = blockIdx.x;
+    if (kTma && threadIdx.x == 0 && tile < ntiles) {
+        const TileLoc n = locate<kN, G::kIRows>(g, tile);
+        fma_issue_first(stage, g.map[n.p], n.ox, n.oy, G::kStageFloats, G::kStageBytes, bar, k0 > 0);
+    }
+    grid_dependency_wait();
+    uint32_t parity = 0;
+    for (; tile < ntiles; tile += gridDim.x) {
+        if (tile + static_cast<int>(gridDim.x) >= ntiles)
+            allow_dependent_launch();
+        int ox, oy, w, h, p = 0;
+        if (kTma) {
+            const TileLoc c = locate<kN, G::kIRows>(g, tile);
+            ox = c.ox;
+            oy = c.oy;
+            w = c.w;
+            h = c.h;
+            p = c.p;
+            if (!mbar_wait_bounded(bar, parity, kWaitSpins)) {
+                // the outputs are invalid and vsc_check_device reports VSC_ETIMEOUT
+                if (threadIdx.x == 0) {
+                    atomicExch(&g_device_timeout, 1);
+                    bulk_wait_all();
+                }
+                mbar_wait_bounded(bar, parity, kWaitSpins);  // let copies still in flight land
+                return;
+            }
+            parity ^= 1;
+        } else {
+            ox = (tile % pl.tiles_x) * kIW - kTbT;
+            oy = (tile / pl.tiles_x) * G::kIRows - kTbT;
+            w = pl.w;
+            h = pl.h;
+            __syncthreads();  // the previous tile's interior has left the staging
+            fma_plain_load<kWarps>(stage, pl, ox, oy);
+            __syncthreads();
+        }
+        const int gx0 = ox + px0, gy0 = oy + py0;
+        const bool interior = ox >= 1 && oy >= 1 && ox + kTbEX - 1 <= w - 3 && oy + G::kRows - 1 <= h - 3;
+
+        FmaState s;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            // six consecutive floats: both pixels' RGB (zero outside the image)
+            const float* row = stage + (py0 + r) * (3 * kTbEX) + 3 * px0;
+            float2 v[4][3];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                const float2 x01 = *reinterpret_cast<const float2*>(row + a * G::kStageFloats);
+                const float2 x23 = *reinterpret_cast<const float2*>(row + a * G::kStageFloats + 2);
+                const float2 x45 = *reinterpret_cast<const float2*>(row + a * G::kStageFloats + 4);
+                v[a][0] = make_float2(x01.x, x23.y);
+                v[a][1] = make_float2(x01.y, x45.x);
+                v[a][2] = make_float2(x23.x, x45.y);
+            }
+            float c0 = 4.0f, c1 = 4.0f;
+            if (!interior) {
+                c0 = nb_of(gx0, gy0 + r, w, h).cnt;
+                c1 = nb_of(gx0 + 1, gy0 + r, w, h).cnt;
+            }
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+                s.o[r][ch] = v[0][ch];
+                s.u[r][ch] = v[1][ch];
+                s.c[r][ch] = v[3][ch];
+                s.nk[r][ch] = make_float2(-__fmul_rn(step, __fadd_rn(c0, v[2][ch].x)),
+                    -__fmul_rn(step, __fadd_rn(c1, v[2][ch].y)));
+            }
+        }
+        if (kTma && threadIdx.x == 0)
+            bulk_wait_read();  // the previous tile's TMA stores have read the staging
+        __syncthreads();
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            float* D = obuf + ch * G::kPlane + ((warp + 1) * 2) * kTbPX + px0 + 2;  // buffer 0
+            *reinterpret_cast<float2*>(D) = s.o[0][ch];
+            *reinterpret_cast<float2*>(D + kTbPX) = s.o[3][ch];
+        }
+        __syncthreads();  // staging consumed, edge rows published
+        if (kTma && threadIdx.x == 0 && tile + static_cast<int>(gridDim.x) < ntiles) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            const TileLoc n = locate<kN, G::kIRows>(g, tile + gridDim.x);
+            mbar_expect_tx(bar, 4 * G::kStageBytes);
+            fma_issue(stage, g.map[n.p], n.ox, n.oy, G::kStageFloats, 0, 4, bar);
+        }
+
+        if (interior)
+            fma_iterate<true, kWarps>(s, obuf, T, k0, step, mom, px0, warp, gx0, gy0, w, h);
+        else
+            fma_iterate<false, kWarps>(s, obuf, T, k0, step, mom, px0, warp, gx0, gy0, w, h);
+
+        // interior out through the (now idle) edge-row slots; a thread's two
+        // pixels of a row are six consecutive floats, both inside or neither.
+        // (The staging overwrites the zero aprons: they then feed only the
+        // outermost ring, whose rows are never written back.)
+        float* so = obuf;
+        float* su = obuf + G::kIRows * 3 * kIW;
+        {
+            const int ix = px0 - kTbT;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int iy = py0 + r - kTbT;
+                if (ix < 0 || ix >= kIW || iy < 0 || iy >= G::kIRows)
+                    continue;
+                float2* o2 = reinterpret_cast<float2*>(so + iy * 3 * kIW + 3 * ix);
+                float2* u2 = reinterpret_cast<float2*>(su + iy * 3 * kIW + 3 * ix);
+                o2[0] = make_float2(s.o[r][0].x, s.o[r][1].x);
+                o2[1] = make_float2(s.o[r][2].x, s.o[r][0].y);
+                o2[2] = make_float2(s.o[r][1].y, s.o[r][2].y);
+                u2[0] = make_float2(s.u[r][0].x, s.u[r][1].x);
+                u2[1] = make_float2(s.u[r][2].x, s.u[r][0].y);
+                u2[2] = make_float2(s.u[r][1].y, s.u[r][2].y);
+            }
+        }
+        if (kTma) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
+            if (threadIdx.x == 0)
+                store_interior(g.map[p] + kMapOo, g.map[p] + kMapUo, ox, oy, so, su);
+        } else {
+            __syncthreads();
+            for (int i = threadIdx.x; i < G::kIRows * 3 * kIW; i += G::kThreads) {
+                const int iy = i / (3 * kIW), col = i - iy * (3 * kIW);
+                const int gy = oy + kTbT + iy, gx = ox + kTbT + col / 3;
+                if (gx < w && gy < h) {
+                    const int64_t idx = pix_index(gx, gy, w) * 3 + col % 3;
+                    pl.Oo[idx] = so[i];
+                    pl.Uo[idx] = su[i];
+                }
+            }
+        }
+        if (uint8_t* rgba = kTma ? g.rgba[p] : pl.rgba) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int r = q >> 1, c = q & 1;
+                const int px = px0 + c, py = py0 + r;
+                const int gx = ox + px, gy = oy + py;
+                if (gx < 0 || gx >= w || gy < 0 || gy >= h || px < kTbT || px >= kTbEX - kTbT || py < kTbT ||
+                    py >= G::kRows - kTbT)
+                    continue;
+                reinterpret_cast<uint32_t*>(rgba)[pix_index(gx, gy, w)] = c == 0
+                    ? pack_rgba(s.o[r][0].x, s.o[r][1].x, s.o[r][2].x)
+                    : pack_rgba(s.o[r][0].y, s.o[r][1].y, s.o[r][2].y);
+            }
+        }
+    }
+    if (kTma && threadIdx.x == 0)
+        bulk_wait_all();
+}
+
+template <int kN, int kWarps>
+__global__ void __launch_bounds__(32 * kWarps, 1)
+    solver_fma_kernel(const __grid_constant__ SolverGroup<kN> g, int T, int k0, float step, float mom)
+{
+    fma_body<kN, kWarps, true>(g, FmaPlain{}, T, k0, step, mom);
+}
+
+template <int kWarps>
+__global__ void __launch_bounds__(32 * kWarps, 1)
+    solver_fma_plain_kernel(const __grid_constant__ FmaPlain pl, int T, int k0, float step, float mom)
+{
+    fma_body<1, kWarps, false>(SolverGroup<1>{}, pl, T, k0, step, mom);
+}
+
 // An mbarrier nobody arrives on, waited for with a bounded spin: exercises
 // the timeout path of the bounded waits (sets g_device_timeout, returns).
 __global__ void bounded_wait_selftest_kernel(int spins)
@@ -903,10 +1310,10 @@ bool encode_image_map(CUtensorMap* m, const float* base, int w, int h, int box_r
 template <int kN>
 bool set_group_smem()
 {
-    return cudaFuncSetAttribute(solver_persistent_kernel<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-               kPsSmem) == cudaSuccess &&
-           cudaFuncSetAttribute(solver_tall_kernel<kN>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmem) ==
-               cudaSuccess;
+    constexpr auto kAttr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    return cudaFuncSetAttribute(solver_persistent_kernel<kN>, kAttr, kPsSmem) == cudaSuccess &&
+           cudaFuncSetAttribute(solver_tall_kernel<kN>, kAttr, kPSmem) == cudaSuccess &&
+           cudaFuncSetAttribute(solver_fma_kernel<kN, kFmaWarps>, kAttr, FmaTile<kFmaWarps>::kSmem) == cudaSuccess;
 }
 
 struct DeviceInfo {
@@ -935,7 +1342,9 @@ cudaError_t device_info(DeviceInfo** out)
         if ((e = cudaFuncSetAttribute(solver_tb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTbSmem)) !=
             cudaSuccess)
             return e;
-        d.ps_smem = set_group_smem<1>() && set_group_smem<4>() && set_group_smem<kGroupMax>();
+        d.ps_smem = set_group_smem<1>() && set_group_smem<4>() && set_group_smem<kGroupMax>() &&
+                    cudaFuncSetAttribute(solver_fma_plain_kernel<kFmaWarps>,
+                        cudaFuncAttributeMaxDynamicSharedMemorySize, FmaTile<kFmaWarps>::kSmem) == cudaSuccess;
         cudaGetLastError();
     }
     *out = &d;
@@ -945,16 +1354,17 @@ cudaError_t device_info(DeviceInfo** out)
 bool aligned16p(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
 // ---- tile-shape autotuner ------------------------------------------------------------
-// The two persistent kernels (64 x 32 and 64 x 48 tiles) give the same results
-// bit for bit; which is faster depends on how their tiles fill the waves of
-// one tile per SM.  solver_group_autotune times both on scratch images of the
-// sizes one launch solves (one image, or one image per stream of a
-// multi-stream step) and keeps the faster per (device, sizes); sizes never
-// tuned use the wave model: a 64 x 48 tile costs about 1.91 times a 64 x 32
-// one (GB300, 1920x1080 and 960x540).
+// The two persistent kernels of the exact form (64 x 32 and 64 x 48 tiles)
+// give the same results bit for bit; which is faster depends on how their
+// tiles fill the waves of one tile per SM.  solver_group_autotune times both
+// on scratch images of the sizes one launch solves (one image, or one image
+// per stream of a multi-stream step) and keeps the faster per (device, form,
+// sizes); sizes never tuned use a wave model: a 64 x 48 tile costs about 1.91
+// times a 64 x 32 one (GB300, 1920x1080 and 960x540).  The FMA form has one
+// shape, 64 x 48.
 struct ShapeTable {
     std::mutex mu;
-    std::map<std::vector<int>, int> rows;  // {device, w0, h0, w1, h1, ...} -> kPEY or kTbEY
+    std::map<std::vector<int>, int> rows;  // {device, form, w0, h0, w1, h1, ...} -> tile rows
     bool enabled = true;
 };
 ShapeTable& shape_table()
@@ -963,9 +1373,9 @@ ShapeTable& shape_table()
     return t;
 }
 
-std::vector<int> shape_key(int dev, const int* w, const int* h, int n)
+std::vector<int> shape_key(int dev, const int* w, const int* h, int n, int form)
 {
-    std::vector<int> k(1, dev);
+    std::vector<int> k{dev, form};
     for (int i = 0; i < n; ++i) {
         k.push_back(w[i]);
         k.push_back(h[i]);
@@ -975,8 +1385,12 @@ std::vector<int> shape_key(int dev, const int* w, const int* h, int n)
 
 int tiles_of(int w, int h, int ir) { return ((w + kIW - 1) / kIW) * ((h + ir - 1) / ir); }
 
-int model_rows(const int* w, const int* h, int n, int sms)
+constexpr int kFmaRows = FmaTile<kFmaWarps>::kRows;  // 48
+
+int model_rows(const int* w, const int* h, int n, int sms, int form)
 {
+    if (form == kSolverFma)
+        return kFmaRows;
     int64_t n_short = 0, n_tall = 0;
     for (int i = 0; i < n; ++i) {
         n_short += tiles_of(w[i], h[i], kIH);
@@ -986,17 +1400,17 @@ int model_rows(const int* w, const int* h, int n, int sms)
 }
 
 // the tile rows a launch over these sizes uses on the current device: tuned, else the model
-int chosen_rows(int dev, const int* w, const int* h, int n, int sms, bool* tuned = nullptr)
+int chosen_rows(int dev, const int* w, const int* h, int n, int sms, int form, bool* tuned = nullptr)
 {
     ShapeTable& t = shape_table();
     std::lock_guard<std::mutex> lock(t.mu);
-    auto it = t.rows.find(shape_key(dev, w, h, n));
+    auto it = t.rows.find(shape_key(dev, w, h, n, form));
     if (tuned)
         *tuned = it != t.rows.end();
-    return it != t.rows.end() ? it->second : model_rows(w, h, n, sms);
+    return it != t.rows.end() ? it->second : model_rows(w, h, n, sms, form);
 }
 
-int interior_rows(int rows) { return rows == kPEY ? kPIH : kIH; }
+int interior_rows(int rows) { return rows - 2 * kTbT; }
 
 // The tensor maps of one image's solve for both ping-pong phases: O[c] / U[c]
 // with the tile box (loads), Oo[c] / Uo[c] with the interior box (stores).
@@ -1039,11 +1453,12 @@ void group_set(SolverGroup<kN>& g, int p, const SolveMaps& m, int c, int li, int
     g.count = p + 1;
 }
 
-// One launch of a persistent kernel (`rows`-row tiles) over a group's tiles,
-// with programmatic dependent launch on the previous launch of the stream.
+// One launch of a persistent kernel of a form (`rows`-row tiles) over a
+// group's tiles, with programmatic dependent launch on the previous launch of
+// the stream.
 template <int kN>
-cudaError_t launch_group(int rows, const SolverGroup<kN>& g, int T, int k0, float step, float mom, int sms,
-    cudaStream_t st)
+cudaError_t launch_group(int form, int rows, const SolverGroup<kN>& g, int T, int k0, float step, float mom,
+    int sms, cudaStream_t st)
 {
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
@@ -1053,6 +1468,11 @@ cudaError_t launch_group(int rows, const SolverGroup<kN>& g, int T, int k0, floa
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     cfg.gridDim = dim3(std::min(g.tile0[g.count], sms));
+    if (form == kSolverFma) {
+        cfg.blockDim = dim3(FmaTile<kFmaWarps>::kThreads);
+        cfg.dynamicSmemBytes = FmaTile<kFmaWarps>::kSmem;
+        return cudaLaunchKernelEx(&cfg, solver_fma_kernel<kN, kFmaWarps>, g, T, k0, step, mom);
+    }
     if (rows == kPEY) {
         cfg.blockDim = dim3(kPThreads);
         cfg.dynamicSmemBytes = kPSmem;
@@ -1073,8 +1493,8 @@ struct GroupMember {
 // Steps k_first .. num_iter - 1 of a solve over all members, in launches of
 // T <= kTbT steps, kN problems per launch.
 template <int kN>
-cudaError_t launch_members(const std::vector<GroupMember>& mem, int rows, int num_iter, float step, float mom,
-    int sms, cudaStream_t st, int* nl, int k_first = 0)
+cudaError_t launch_members(int form, const std::vector<GroupMember>& mem, int rows, int num_iter, float step,
+    float mom, int sms, cudaStream_t st, int* nl, int k_first = 0)
 {
     const int nlaunch = (num_iter - k_first + kTbT - 1) / kTbT;
     SolverGroup<kN> g{};
@@ -1088,7 +1508,7 @@ cudaError_t launch_members(const std::vector<GroupMember>& mem, int rows, int nu
                 const GroupMember& m = mem[b + p];
                 group_set(g, p, m.maps, m.c0 ^ (li & 1), li, m.w, m.h, rows, li == nlaunch - 1 ? m.rgba : nullptr);
             }
-            e = launch_group(rows, g, T, k0, step, mom, sms, st);
+            e = launch_group(form, rows, g, T, k0, step, mom, sms, st);
             ++*nl;
         }
         k0 += T;
@@ -1107,18 +1527,18 @@ void solver_set_autotune(bool on)
         t.rows.clear();
 }
 
-int solver_group_tile_rows(const int* w, const int* h, int n, bool* tuned)
+int solver_group_tile_rows(const int* w, const int* h, int n, bool* tuned, int form)
 {
     int dev = 0;
     DeviceInfo* di = nullptr;
     if (n < 1 || cudaGetDevice(&dev) != cudaSuccess || device_info(&di) != cudaSuccess)
         return 0;
-    return chosen_rows(dev, w, h, n, di->sms, tuned);
+    return chosen_rows(dev, w, h, n, di->sms, form, tuned);
 }
 
-int solver_tile_rows(int w, int h, bool* tuned) { return solver_group_tile_rows(&w, &h, 1, tuned); }
+int solver_tile_rows(int w, int h, bool* tuned, int form) { return solver_group_tile_rows(&w, &h, 1, tuned, form); }
 
-cudaError_t solver_group_autotune(const int* w, const int* h, int n, cudaStream_t st, int* rows_out)
+cudaError_t solver_group_autotune(const int* w, const int* h, int n, cudaStream_t st, int* rows_out, int form)
 {
     DeviceInfo* di = nullptr;
     int dev = 0;
@@ -1129,20 +1549,20 @@ cudaError_t solver_group_autotune(const int* w, const int* h, int n, cudaStream_
         return e;
     if (n < 1)
         return cudaErrorInvalidValue;
-    bool eligible = di->ps_smem;
+    bool eligible = di->ps_smem && form != kSolverFma;  // the FMA form has one shape
     size_t total = 0;  // floats of one image per member, 16-byte multiples
     for (int i = 0; i < n; ++i) {
         eligible = eligible && (w[i] % 4) == 0 && w[i] >= 1 && h[i] >= 1;
         total += static_cast<size_t>(w[i]) * h[i] * 3;
     }
     ShapeTable& t = shape_table();
-    const std::vector<int> key = shape_key(dev, w, h, n);
+    const std::vector<int> key = shape_key(dev, w, h, n, form);
     {
         std::lock_guard<std::mutex> lock(t.mu);
         auto it = t.rows.find(key);
         if (it != t.rows.end() || !t.enabled || !eligible) {
             if (rows_out)
-                *rows_out = it != t.rows.end() ? it->second : model_rows(w, h, n, di->sms);
+                *rows_out = it != t.rows.end() ? it->second : model_rows(w, h, n, di->sms, form);
             return cudaSuccess;
         }
     }
@@ -1182,9 +1602,9 @@ cudaError_t solver_group_autotune(const int* w, const int* h, int n, cudaStream_
     }
     // the kernel instantiation the solves will use: one problem, up to 4, up to 16 per launch
     auto launch = [&](const std::vector<GroupMember>& m, int rows, int num_iter, int* nl) {
-        return n == 1 ? launch_members<1>(m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT)
-             : n <= 4 ? launch_members<4>(m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT)
-                      : launch_members<kGroupMax>(m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT);
+        return n == 1 ? launch_members<1>(form, m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT)
+             : n <= 4 ? launch_members<4>(form, m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT)
+                      : launch_members<kGroupMax>(form, m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT);
     };
     for (int round = 0; round < 5 && e == cudaSuccess; ++round) {
         for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
@@ -1212,7 +1632,7 @@ cudaError_t solver_group_autotune(const int* w, const int* h, int n, cudaStream_
     cudaFree(buf);
     if (e != cudaSuccess)
         return e;
-    const int best = best_ms[1] < best_ms[0] ? kPEY : kTbEY;
+    const int best = best_ms[1] < best_ms[0] ? shapes[1] : shapes[0];
     {
         std::lock_guard<std::mutex> lock(t.mu);
         if (t.enabled)
@@ -1223,9 +1643,9 @@ cudaError_t solver_group_autotune(const int* w, const int* h, int n, cudaStream_
     return cudaSuccess;
 }
 
-cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out)
+cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out, int form)
 {
-    return solver_group_autotune(&w, &h, 1, st, rows_out);
+    return solver_group_autotune(&w, &h, 1, st, rows_out, form);
 }
 
 size_t solver_workspace_floats(int w, int h) { return static_cast<size_t>(w) * h * 3 * 4; }
@@ -1275,6 +1695,19 @@ cudaError_t solver_lap(const float* P, int w, int h, float* workspace, cudaStrea
     return cudaGetLastError();
 }
 
+cudaError_t solver_prep(int form, const float* P, const float* A, const float* Wt, int w, int h, float step,
+    float* workspace, cudaStream_t st)
+{
+    if (form != kSolverFma)
+        return solver_lap(P, w, h, workspace, st);
+    const dim3 b(32, 8);
+    const cudaError_t e =
+        launch_pdl(solver_prep_fma_kernel, grid2d(w, h, b), b, 0, st, P, A, Wt, workspace, w, h, step);
+    if (e != cudaSuccess)
+        return e;
+    return cudaGetLastError();
+}
+
 bool solver_group_eligible(const SolverImage* im, int n)
 {
     DeviceInfo* di = nullptr;
@@ -1287,7 +1720,7 @@ bool solver_group_eligible(const SolverImage* im, int n)
 }
 
 cudaError_t run_solver_group(const SolverImage* im, int n, int num_iter, float step, float mom, cudaStream_t st,
-    int* launches)
+    int* launches, int form)
 {
     DeviceInfo* di = nullptr;
     cudaError_t e = device_info(&di);
@@ -1314,7 +1747,7 @@ cudaError_t run_solver_group(const SolverImage* im, int n, int num_iter, float s
         ws[i] = im[i].w;
         hs[i] = im[i].h;
     }
-    const int rows = chosen_rows(dev, ws.data(), hs.data(), n, di->sms);
+    const int rows = chosen_rows(dev, ws.data(), hs.data(), n, di->sms, form);
     const bool odd = solve_launches(num_iter) % 2 == 1;
     std::vector<GroupMember> mem(n);
     for (int i = 0; i < n; ++i) {
@@ -1328,8 +1761,8 @@ cudaError_t run_solver_group(const SolverImage* im, int n, int num_iter, float s
         mem[i].c0 = odd ? 1 : 0;
         mem[i].rgba = im[i].rgba;
     }
-    e = n <= 4 ? launch_members<4>(mem, rows, num_iter, step, mom, di->sms, st, &nl)
-               : launch_members<kGroupMax>(mem, rows, num_iter, step, mom, di->sms, st, &nl);
+    e = n <= 4 ? launch_members<4>(form, mem, rows, num_iter, step, mom, di->sms, st, &nl)
+               : launch_members<kGroupMax>(form, mem, rows, num_iter, step, mom, di->sms, st, &nl);
     if (launches)
         *launches += nl;
     if (e == cudaSuccess)
@@ -1338,7 +1771,7 @@ cudaError_t run_solver_group(const SolverImage* im, int n, int num_iter, float s
 }
 
 cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,
-    float step, float mom, float* workspace, cudaStream_t st, int* launches, uint8_t* rgba_out)
+    float step, float mom, float* workspace, cudaStream_t st, int* launches, uint8_t* rgba_out, int form)
 {
     const size_t n = static_cast<size_t>(w) * h * 3;
     const WsView v = ws_view(workspace, w, h);
@@ -1356,7 +1789,9 @@ cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O
     cudaError_t e0 = device_info(&di);
     if (e0 != cudaSuccess)
         return e0;
-    if ((e0 = solver_lap(P, w, h, v.L, st)) != cudaSuccess)
+    if (form == kSolverFma && !di->ps_smem)
+        return cudaErrorNotSupported;
+    if ((e0 = solver_prep(form, P, A, Wt, w, h, step, v.L, st)) != cudaSuccess)
         return e0;
     ++nl;
     // Launches of up to kTbT iterations; ping-pong O between O and O2 and U
@@ -1373,7 +1808,7 @@ cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O
     int dev = 0;
     if ((e0 = cudaGetDevice(&dev)) != cudaSuccess)
         return e0;
-    const int rows = chosen_rows(dev, &w, &h, 1, di->sms);
+    const int rows = chosen_rows(dev, &w, &h, 1, di->sms, form);
     GroupMember m{};
     bool tma = tma_eligible(di, w, O, v, A, Wt);
     if (tma) {
@@ -1387,13 +1822,33 @@ cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O
         m.c0 = cur == O ? 0 : 1;
         m.rgba = rgba_out;
         const std::vector<GroupMember> one(1, m);
-        cudaError_t e = launch_members<1>(one, rows, num_iter, step, mom, di->sms, st, &nl);
+        cudaError_t e = launch_members<1>(form, one, rows, num_iter, step, mom, di->sms, st, &nl);
         if (launches)
             *launches += nl;
         return e != cudaSuccess ? e : cudaGetLastError();
     }
     float* U[2] = {v.U0, v.U1};
     int k0 = 0;
+    if (form == kSolverFma) {
+        // plain loads and stores (widths not a multiple of 4, unaligned images)
+        const int ir = interior_rows(kFmaRows);
+        const int tx = (w + kIW - 1) / kIW, nt = tx * ((h + ir - 1) / ir);
+        cudaError_t e = cudaSuccess;
+        for (int li = 0; li < nlaunch && e == cudaSuccess; ++li) {
+            const int T = std::min(kTbT, num_iter - k0);
+            float* nxt = (cur == O) ? v.O2 : O;
+            const FmaPlain pl{cur, U[li & 1], Wt, v.L, nxt, U[(li + 1) & 1], w, h, tx, nt,
+                li == nlaunch - 1 ? rgba_out : nullptr};
+            e = launch_pdl(solver_fma_plain_kernel<kFmaWarps>, dim3(std::min(nt, di->sms)),
+                dim3(FmaTile<kFmaWarps>::kThreads), FmaTile<kFmaWarps>::kSmem, st, pl, T, k0, step, mom);
+            ++nl;
+            k0 += T;
+            cur = nxt;
+        }
+        if (launches)
+            *launches += nl;
+        return e != cudaSuccess ? e : cudaGetLastError();
+    }
     for (int li = 0; li < nlaunch; ++li) {
         const int T = std::min(kTbT, num_iter - k0);
         float* nxt = (cur == O) ? v.O2 : O;
@@ -1448,7 +1903,7 @@ cudaError_t run_solver_noalloc(const float* P, const float* A, const float* Wt, 
         return e;
     // Every workspace element (lap P, both momentum images, the second Jacobi
     // buffer) is written before it is read, so nothing is cleared.
-    return run_solver(P, A, Wt, O, w, h, num_iter, step, mom, ws, st, nullptr, nullptr);
+    return run_solver(P, A, Wt, O, w, h, num_iter, step, mom, ws, st, nullptr, nullptr, kSolverExact);
 }
 
 cudaError_t device_timeout_flag(int** flag)
