@@ -1,30 +1,39 @@
 """Benchmark: 1080p stabilized frames/s, the chosen form against the plain
-FP32 GPU path (and the PSNR between their outputs).
+FP32 GPU path (and the quality of its output against the plain path's).
 
-Workload (one step = one frame): the 1920x1080 synthetic stream (seeded
-Gaussian blobs advected by a smooth flow re-drawn every 30 frames, processed
-frames with colour shift and flicker; RGBA8 in and out).  Per frame: load the
-next frame (RGBA8 -> float, flow features), compute the forward and backward
-flow through the Correlation (81 displacements) and Warp kernels, then the
-stabilization pass (five warps, adaptive combination, consistency weights,
-2-level pyramid solve with 75 + 150 iterations) and the RGBA8 output —
+Workload (one step = one frame): a 1920x1080 synthetic stream of 120 frames
+(seeded Gaussian blobs advected by a smooth flow re-drawn every 30 frames,
+processed frames with colour shift and flicker; RGBA8 in and out); the timed
+steps cycle through it.  Per frame: load the next frame (RGBA8 -> float,
+flow features), compute the forward and backward flow through the
+Correlation (81 displacements) and Warp kernels, then the stabilization pass
+(five warps, adaptive combination, consistency weights, 2-level pyramid
+solve with 75 + 150 iterations) and the RGBA8 output —
 VideoStabilizer::doOneStep with its defaults.
 
-Forms (--form, default bf16_ds2): "plain" computes the flow with FP32
-correlations at full resolution, as the reference does; "bf16" / "fp16" run
-the flow estimator's correlations on the tensor cores; "bf16_ds2" also
-computes the flow at half resolution (FLOWDOWNSCALE=2, bilinear upsampling).
+Forms (--form, default bf16_ds2_fma): "plain" computes the flow with FP32
+correlations at full resolution and solves with kernel_consist_out's exact
+arithmetic, as the reference does; "bf16" / "fp16" run the flow estimator's
+correlations on the tensor cores; "bf16_ds2" also computes the flow at half
+resolution (FLOWDOWNSCALE=2, bilinear upsampling); the "_fma" forms solve
+with the FMA form of the same iteration (within 1e-6 of the exact one).
 Warps, mask and blend are FP32 in every form.
 
 value : frames/s of the chosen form with every input frame already resident
         in HBM (RGBA8); "plain" holds the plain path's figure, timed the same
-        way, and "psnr_vs_plain" the PSNR of the chosen form's output frames
-        against the plain path's.
-e2e   : the chosen form through the public C ABI with host buffers: each
-        step copies the next frame pair from pinned host memory and reads the
-        stabilized frame back, inside the timed region.
+        way, and "quality_vs_plain" the PSNR of the chosen form's output
+        frames, its flow error and its mask disagreement against the plain
+        path's.
+e2e   : the chosen form (and, under "plain", the plain path) through the
+        public C ABI with host buffers: each step copies the next frame pair
+        from pinned host memory and reads the stabilized frame back, inside
+        the timed region.
+Every stabilizer first runs six untimed steps that capture its step graphs
+(GRAPH_CAPTURE_STEPS), then the --warmup steps, then the --steps timed ones.
 The per-step working set (~0.6 GB) is far larger than L2, so no flush is
-needed between steps.
+needed between steps.  The default line also carries the Correlation's
+BF16/FP16 error against the FP64 restatement, the full-resolution BF16 form's
+quality, and the 16-stream workload (--no-extras skips them).
 
 --impl reference: the reference's CPU path on the host cores (the CPU
 restatement in oracle/, which for the two custom ops is bit-identical to the
@@ -52,6 +61,7 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 PKG = ROOT / "video-stream-consistency_gb300"
 W, H = 1920, 1080
+N_FRAMES = 120  # the 1080p stream's length; the timed steps cycle through it
 METRIC = "1080p stabilized frames/s, chosen form vs plain GPU at PSNR>=40 dB; HBM GB/s"
 # Solver Jacobi step, per pixel: reads O, U, lap(P), A, consWt (5 x 12 B),
 # writes O, U (2 x 12 B); the kernel performs vsc_solver_steps_per_launch()
@@ -380,11 +390,11 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def solver_roofline(vsc, dev, stream, iters: int = 144):
-    """Times the dominant kernel — the full-resolution solver — with CUDA
-    events on its stream: the time of one Jacobi step from an 8-step and an
-    (8 + iters)-step solve of the same size (both whole numbers of launches
-    for 4 or 8 steps per launch)."""
+def solver_roofline(vsc, dev, stream, iters: int = 144, form: str = "exact"):
+    """Times the dominant kernel — the full-resolution solver in the given
+    form — with CUDA events on its stream: the time of one Jacobi step from
+    an 8-step and an (8 + iters)-step solve of the same size (both whole
+    numbers of launches for 4 or 8 steps per launch)."""
     import torch
 
     peak, peak_src = peaks()
@@ -397,25 +407,37 @@ def solver_roofline(vsc, dev, stream, iters: int = 144):
     T = int(vsc.load().vsc_solver_steps_per_launch())
     torch.cuda.synchronize()
     for _ in range(2):
-        vsc.get_consist_out(P, A, Wt, iters, 0.15, 0.15, O, workspace=wsp, stream=stream)
+        vsc.get_consist_out(P, A, Wt, iters, 0.15, 0.15, O, workspace=wsp, stream=stream, form=form)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     ev[0].record(stream)
-    vsc.get_consist_out(P, A, Wt, 8, 0.15, 0.15, O, workspace=wsp, stream=stream)
+    vsc.get_consist_out(P, A, Wt, 8, 0.15, 0.15, O, workspace=wsp, stream=stream, form=form)
     ev[1].record(stream)
     ev[2].record(stream)
-    vsc.get_consist_out(P, A, Wt, 8 + iters, 0.15, 0.15, O, workspace=wsp, stream=stream)
+    vsc.get_consist_out(P, A, Wt, 8 + iters, 0.15, 0.15, O, workspace=wsp, stream=stream, form=form)
     ev[3].record(stream)
     ev[3].synchronize()
     step_ms = (ev[2].elapsed_time(ev[3]) - ev[0].elapsed_time(ev[1])) / iters
-    alg_bytes = SOLVER_BYTES_PER_PX * W * H * T  # T Jacobi steps per launch
     per_launch_ms = step_ms * T
+    kname, launch_bpp = SOLVER_KERNELS[form]
+    alg_bytes = launch_bpp * W * H  # each input image read once, O and U written once, per launch
     achieved = alg_bytes / (per_launch_ms / 1000.0) / 1e9
-    traffic = SOLVER_TRAFFIC_BYTES.get(T)
-    return {"bound": "hbm", "kernel": f"solver_tall_kernel (64x48 tiles; {T} Jacobi steps of kernel_consist_out per "
-                                      f"launch at 1920x1080; effective bytes = {SOLVER_BYTES_PER_PX} B/px per step)",
+    eff = SOLVER_BYTES_PER_PX * W * H * T / (per_launch_ms / 1000.0) / 1e9
+    traffic = SOLVER_TRAFFIC_BYTES.get(kname)
+    line = {"bound": "hbm", "kernel": f"{kname} (64x48 tiles; {T} Jacobi steps per launch at 1920x1080)",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes, "steps_per_launch": T,
-            "launch_ms": per_launch_ms, "ms_per_jacobi_step": step_ms, "peak_source": peak_src}
+            "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
+            "algorithmic_bytes_rule": f"{launch_bpp} B/px per launch: each input image read once and O, U "
+                                      "written once (the launch's compulsory bytes)",
+            "effective_gbs": eff, "frac_effective": eff / peak,
+            "effective_rule": f"{SOLVER_BYTES_PER_PX} B/px per Jacobi step x {T} steps per launch (the reference's "
+                              "one launch per step would move these bytes)",
+            "steps_per_launch": T, "launch_ms": per_launch_ms, "ms_per_jacobi_step": step_ms,
+            "peak_source": peak_src}
+    if traffic:
+        line["frac_dram"] = traffic / (per_launch_ms / 1000.0) / 1e9 / peak
+        line["traffic_source"] = SOLVER_TRAFFIC_SOURCE[kname]
+    line["pipe_counters"] = SOLVER_PIPE.get(kname)
+    return line
 
 
 MULTI_STREAMS = [(640, 360)] * 4 + [(1280, 720)] * 6 + [(1920, 1080)] * 4 + [(3840, 2160)] * 2
@@ -435,31 +457,23 @@ def multistream_forms(form):
     return out
 
 
-def run_multistream(args):
-    """--workload multistream: 16 concurrent synthetic streams of mixed
-    resolution (4x 640x360, 6x 1280x720, 4x 1920x1080, 2x 3840x2160;
-    31,334,400 px per step) stabilized in lockstep, one CUDA graph launch per
-    frame step (vsc_multistream), the solves of all 16 grouped: per pyramid
-    level, each launch of the persistent solver kernel (8 Jacobi steps)
-    walks the tiles of all 16 images (--ms-grouped off: each stream's solve
-    on its own CUDA stream).  The default form is BF16 correlations with the
-    learned upsampler on the 1080p and 4K streams.  A step is one frame of
-    every stream; each stream cycles through 8 generated frames (the work
-    per step does not depend on which).  Value: stream-frames/s and Mpx/s,
-    CUDA events on the multistream's stream."""
+def multistream_measure(vsc, dev, form: str, steps: int, warmup: int, grouped: bool, n_unique: int = 4):
+    """16 concurrent synthetic streams of mixed resolution (4x 640x360, 6x
+    1280x720, 4x 1920x1080, 2x 3840x2160; 31,334,400 px per step) stabilized
+    in lockstep, one CUDA graph launch per frame step (vsc_multistream),
+    the solves of all 16 grouped: per pyramid level, each launch of the
+    persistent solver kernel (8 Jacobi steps) walks the tiles of all 16
+    images (grouped=False: each stream's solve on its own CUDA stream).  A
+    step is one frame of every stream; each stream cycles through n_unique
+    generated frames (the work per step does not depend on which).  Value:
+    stream-frames/s and Mpx/s, CUDA events on the multistream's stream."""
     import torch
 
-    vsc = import_pkg()
-    vsc.build()
-    vsc.load()
     from vsc_gb300 import synth
 
-    dev = torch.device("cuda", 0)
-    form = args.form or "bf16_ds2_learned"
     kw, form_desc = FORMS[form]
     forms = multistream_forms(form)
     stream = torch.cuda.Stream(device=dev)
-    n_unique = 8
     frames = []
     for i, (w, h) in enumerate(MULTI_STREAMS):
         s_ = synth.SyntheticStream(w, h, seed=100 + i, device=str(dev))
@@ -467,7 +481,9 @@ def run_multistream(args):
     torch.cuda.synchronize()
     ms = vsc.MultiStream(MULTI_STREAMS, flow_downscale=[f[0] for f in forms], corr_dtype=[f[1] for f in forms],
                          stream=stream)
-    ms.set_fused(args.ms_grouped == "on")
+    ms.set_fused(grouped)
+    if kw.get("solver_form", "exact") != "exact":
+        ms.set_solver_form(kw["solver_form"])
     up = None
     if kw.get("upsampler"):
         up = vsc.Upsampler(kw["upsampler"])
@@ -488,28 +504,26 @@ def run_multistream(args):
             ms.step(outs)
         load()
 
-    for _ in range(args.warmup):
+    for _ in range(GRAPH_CAPTURE_STEPS + warmup):
         step()
     stream.synchronize()
-    clocks = ClockSampler(0)
+    clocks = ClockSampler(dev.index or 0)
     clocks.start()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         step()
     e1.record(stream)
     e1.synchronize()
     clk = clocks.stop()
     ms_total = e0.elapsed_time(e1)
     px = sum(w * h for w, h in MULTI_STREAMS)
-    grouped = ms.fused
-    line = {
-        "metric": "multi-stream stabilized stream-frames/s (16 mixed-resolution streams, one graph launch per step)",
-        "value": len(MULTI_STREAMS) * args.steps / (ms_total / 1000), "unit": "stream-frames/s",
-        "mpx_per_s": px * args.steps / (ms_total / 1000) / 1e6, "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": kw["corr_dtype"], "data": "synthetic",
+    is_grouped = ms.fused
+    res = {
+        "value": len(MULTI_STREAMS) * steps / (ms_total / 1000), "unit": "stream-frames/s",
+        "mpx_per_s": px * steps / (ms_total / 1000) / 1e6, "steps": steps, "warmup": warmup,
+        "ms_per_step": ms_total / steps,
         "config": {"workload": f"16 streams: 4x 640x360, 6x 1280x720, 4x 1920x1080, 2x 3840x2160; form "
                                f"'{form}': {form_desc}" + ("; learned upsampler on the 1080p and 4K streams only"
                                                          if kw.get("upsampler") else ""),
@@ -517,12 +531,32 @@ def run_multistream(args):
                    "per_stream": [{"size": [w, h], "flow_downscale": d, "corr_dtype": c}
                                   for (w, h), (d, c) in zip(MULTI_STREAMS, forms)],
                    "solves": "grouped: one persistent-kernel launch per 8 Jacobi steps covers all 16 images"
-                             if grouped else "per stream, each on its own CUDA stream"},
-        "grouped_solves": grouped, "gpu_launches": ms.last_launches * args.steps, "clocks": clk,
+                             if is_grouped else "per stream, each on its own CUDA stream"},
+        "grouped_solves": is_grouped, "gpu_launches_per_step": ms.last_launches, "clocks": clk,
     }
     ms.close()
     if up is not None:
         up.close()
+    return res
+
+
+def run_multistream(args):
+    """--workload multistream: the 16-stream workload as its own line (see
+    multistream_measure); default form BF16 correlations, the learned
+    upsampler on the 1080p and 4K streams, the solver in its FMA form."""
+    import torch
+
+    vsc = import_pkg()
+    vsc.build()
+    vsc.load()
+    dev = torch.device("cuda", 0)
+    form = args.form or DEFAULT_MS_FORM
+    res = multistream_measure(vsc, dev, form, args.steps, args.warmup, args.ms_grouped == "on", n_unique=8)
+    kw = FORMS[form][0]
+    line = {"metric": "multi-stream stabilized stream-frames/s (16 mixed-resolution streams, one graph launch per "
+                      "step)", "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": kw["corr_dtype"], "data": "synthetic", **res,
+            "gpu_launches": res["gpu_launches_per_step"] * args.steps}
     print(json.dumps(line))
 
 
@@ -639,7 +673,10 @@ def run_solver_only(args):
     vsc.load()
     dev = torch.device("cuda", 0)
     stream = torch.cuda.Stream(device=dev)
-    print(json.dumps(solver_roofline(vsc, dev, stream, iters=args.steps * 8)))
+    for form in ("exact", "fma"):
+        rows = vsc.solver_autotune(W, H, stream=stream, form=form)
+        print(json.dumps({"form": form, "tile_rows": rows,
+                          **solver_roofline(vsc, dev, stream, iters=args.steps * 8, form=form)}))
 
 
 def run_warpblend(args):
@@ -788,7 +825,23 @@ FORMS = {
     "bf16_ds2_learned": ({"corr_dtype": "bf16", "flow_downscale": 2, "upsampler": "default"},
                          "FLOWDOWNSCALE=2 with BF16 tensor-core Correlations and the learned 2x flow upsampler "
                          "(weights shipped with the package; bilinear fallback where its residual exceeds 0.5 px)"),
+    "plain_fma": ({"corr_dtype": "f32", "flow_downscale": 1, "solver_form": "fma"},
+                  "plain flow (FP32 correlations at full resolution) with the solver in its FMA form"),
+    "bf16_ds2_fma": ({"corr_dtype": "bf16", "flow_downscale": 2, "solver_form": "fma"},
+                     "FLOWDOWNSCALE=2 (flow at 960x540, bilinear upsampling) with BF16 tensor-core Correlations "
+                     "and the solver in its FMA form (fused multiply-adds around per-solve constants; within 1e-6 "
+                     "of the exact form)"),
+    "bf16_ds2_learned_fma": ({"corr_dtype": "bf16", "flow_downscale": 2, "upsampler": "default",
+                              "solver_form": "fma"},
+                             "FLOWDOWNSCALE=2 with BF16 tensor-core Correlations, the learned 2x flow upsampler and "
+                             "the solver in its FMA form"),
 }
+DEFAULT_FORM = "bf16_ds2_fma"
+DEFAULT_MS_FORM = "bf16_ds2_learned_fma"
+# Untimed steps run right after a stabilizer is made: its step CUDA graph is
+# captured once per window position (3) and feedback buffer (2), so six steps
+# keep every capture out of the warm-up and timed steps.
+GRAPH_CAPTURE_STEPS = 6
 
 
 def make_stabilizer(vsc, kw, stream):
@@ -821,7 +874,7 @@ def time_form(vsc, kw, dev_frames, stream, steps, warmup, ws, dev, clocks=None):
         state["nxt"] += 1
 
     with torch.cuda.stream(stream):
-        for _ in range(warmup):
+        for _ in range(GRAPH_CAPTURE_STEPS + warmup):
             step()
     stream.synchronize()
     if clocks:
@@ -869,7 +922,7 @@ def e2e_form(vsc, kw, pinned, stream, steps, warmup, ws, dev):
         state["nxt"] += 1
         state["k"] += 1
 
-    for _ in range(warmup):
+    for _ in range(GRAPH_CAPTURE_STEPS + warmup):
         step()
     stream.synchronize()
     barrier(ws)
@@ -886,29 +939,74 @@ def e2e_form(vsc, kw, pinned, stream, steps, warmup, ws, dev):
                           "stream, the host at most two steps ahead; uploads on its copy stream"}
 
 
-def psnr_vs_plain(vsc, kw, dev_frames, stream, n_steps: int = 12):
-    """Stabilized RGB of the form against the plain path, frame by frame."""
+def quality_vs_plain(vsc, kw, dev_frames, stream, n_steps: int = 12):
+    """The form against the plain path on the same frames, step by step:
+    PSNR of the stabilized RGB output; the forward flow's error (px, max-abs
+    and RMS over both components; the flow estimator has no FP64
+    restatement, so the plain path's FP32 flow is the reference); and the
+    consistency mask's disagreement rate — the fraction of consWt values
+    whose zero / non-zero decision (the 1e-3 clamp, flowconsistency.cu:
+    181-186) differs from the plain path's."""
     import torch
 
     sts = [make_stabilizer(vsc, FORMS["plain"][0], stream), make_stabilizer(vsc, kw, stream)]
     for st in sts:
         for i in range(3):
             st.load_frame(*dev_frames[i])
-    vals = []
+    psnr, fmax, fsq, dis = [], 0.0, [], []
     for t in range(n_steps):
-        outs = []
+        outs, flows, wts = [], [], []
         for st in sts:
             with torch.cuda.stream(stream):
                 outs.append(st.step()[..., :3].float())
+                flows.append(st.buffer(1)[..., :2].clone())
+                wts.append(st.buffer(4).clone())
         stream.synchronize()
         mse = float(torch.mean((outs[0] - outs[1]) ** 2)) / 255.0 ** 2
-        vals.append(99.0 if mse == 0 else 10 * math.log10(1.0 / mse))
+        psnr.append(99.0 if mse == 0 else 10 * math.log10(1.0 / mse))
+        d = (flows[1] - flows[0]).abs()
+        fmax = max(fmax, float(d.max()))
+        fsq.append(float(torch.mean(d.double() ** 2)))
+        dis.append(float(torch.mean(((wts[0] == 0) != (wts[1] == 0)).double())))
         for st in sts:
             st.load_frame(*dev_frames[(t + 3) % len(dev_frames)])
     for st in sts:
         st.close()
-    return {"min_db": min(vals), "mean_db": statistics.mean(vals), "frames": n_steps,
-            "note": "99 = identical frames"}
+    return {"psnr_min_db": min(psnr), "psnr_mean_db": statistics.mean(psnr), "frames": n_steps,
+            "flow_err_vs_plain_px": {"max_abs": fmax, "rms": math.sqrt(statistics.mean(fsq))},
+            "mask_disagreement_vs_plain": statistics.mean(dis),
+            "note": "PSNR 99 = identical frames; flow error and mask disagreement against the plain FP32 path"}
+
+
+def correlation_precision(vsc, dev, seed: int = 7):
+    """The Correlation op's error in BF16 and FP16 (tensor cores, FP32
+    accumulation) and in FP32 (CUDA cores) against the FP64 restatement, on
+    N(0, 1) feature pyramids of a 1920x1088 frame pair (the five PWC levels,
+    md 4): max-abs and RMS per level, and the error relative to the largest
+    |value| of the level."""
+    import numpy as np
+    import torch
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+
+    from vsc_gb300 import synth
+
+    O.build(ref=False)
+    O.set_threads(os.cpu_count() or 1)
+    out = {}
+    for (f1, f2), (lw, lh, lc) in zip(synth.feature_pyramid(W, H, seed), PWC_LEVELS_1080P):
+        ref = O.correlation(f1.astype(np.float64), f2.astype(np.float64), 4)
+        d1, d2 = torch.from_numpy(f1).to(dev), torch.from_numpy(f2).to(dev)
+        lev = {"shape": [lc, lh, lw], "max_abs_value": float(np.abs(ref).max())}
+        for name, call in (("f32", lambda: vsc.correlation(d1, d2, 4)),
+                           ("bf16", lambda: vsc.correlation_lowp(d1, d2, 4, "bf16")),
+                           ("fp16", lambda: vsc.correlation_lowp(d1, d2, 4, "fp16"))):
+            e = call().cpu().numpy().astype(np.float64) - ref
+            lev[name] = {"max_abs": float(np.abs(e).max()), "rms": float(np.sqrt(np.mean(e * e))),
+                         "max_rel_to_level_max": float(np.abs(e).max() / lev["max_abs_value"])}
+        out[f"{lw}x{lh}"] = lev
+    return {"levels": out, "reference": "FP64 restatement of correlation.cc (oracle/), N(0,1) features"}
 
 
 def run_gpu(args):
@@ -926,18 +1024,19 @@ def run_gpu(args):
     vsc.build()
     vsc.load()
 
-    n_frames = min(args.steps + args.warmup + 3, 120)
+    n_frames = N_FRAMES
     frames = make_frames(n_frames, seed=rank, device=str(dev))
     stream = torch.cuda.Stream(device=dev)
     dev_frames = [(torch.from_numpy(o).to(dev), torch.from_numpy(p).to(dev)) for o, p in frames]
     torch.cuda.synchronize()
-    form = args.form or "bf16_ds2"
+    form = args.form or DEFAULT_FORM
     kw, form_desc = FORMS[form]
 
-    # ---- device-resident: the chosen form (clocks sampled), then plain ----------
+    # ---- device-resident: the chosen form, then plain; clocks sampled from the
+    # first timed region to the last end-to-end one ------------------------------
     clocks = ClockSampler(local)
-    ms_max, launches_per_step, st = time_form(vsc, kw, dev_frames, stream, args.steps, args.warmup, ws, dev, clocks)
-    clk = clocks.stop()
+    clocks.start()
+    ms_max, launches_per_step, st = time_form(vsc, kw, dev_frames, stream, args.steps, args.warmup, ws, dev)
     value = ws * args.steps / (ms_max / 1000.0)
     plain = None
     if form != "plain":
@@ -945,6 +1044,13 @@ def run_gpu(args):
         pst.close()
         plain = {"value": ws * args.steps / (pms / 1000.0), "unit": "frames/s", "ms_per_step": pms / args.steps,
                  "gpu_launches_per_step": pl}
+
+    # ---- end to end through the public API with pinned host buffers ------------
+    pinned = [(torch.from_numpy(o).pin_memory(), torch.from_numpy(p).pin_memory()) for o, p in frames]
+    e2e = e2e_form(vsc, kw, pinned, stream, args.steps, args.warmup, ws, dev)
+    if plain:
+        plain["e2e"] = e2e_form(vsc, FORMS["plain"][0], pinned, stream, args.steps, args.warmup, ws, dev)
+    clk = clocks.stop()
 
     # ---- per-stage device time (separate pass; stage events synchronise) -------
     st.enable_timing(True)
@@ -956,32 +1062,34 @@ def run_gpu(args):
     stages_ms = {k: statistics.median(d[k] for d in stages) for k in stages[0]}
     st.close()
 
-    # ---- end to end through the public API with pinned host buffers ------------
-    pinned = [(torch.from_numpy(o).pin_memory(), torch.from_numpy(p).pin_memory()) for o, p in frames]
-    e2e = e2e_form(vsc, kw, pinned, stream, args.steps, args.warmup, ws, dev)
-    quality = psnr_vs_plain(vsc, kw, dev_frames, stream) if form != "plain" else None
-
-    roofline = solver_roofline(vsc, dev, stream)
-
+    roofline = solver_roofline(vsc, dev, stream, form=kw.get("solver_form", "exact"))
     line = {
         "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if kw["corr_dtype"] == "f32" else f"f32 ({kw['corr_dtype']} correlation)",
         "data": "synthetic",
-        "config": {"workload": f"1920x1080 synthetic stream, form '{form}': {form_desc}; 2-level pyramid, "
-                               "75+150 solver iterations, RGBA8 in/out",
+        "config": {"workload": f"1920x1080 synthetic stream of {n_frames} frames (flow re-drawn every 30), form "
+                               f"'{form}': {form_desc}; 2-level pyramid, 75+150 solver iterations, RGBA8 in/out",
                    "form": form, "width": W, "height": H, "frames_generated": n_frames,
+                   "graph_capture_steps": GRAPH_CAPTURE_STEPS,
                    "l2": "per-step working set ~0.6 GB > 129 MB L2; no flush",
                    "parallelism": f"replicas x{ws}"},
         "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "roofline": roofline, "clocks": clk,
         "stages_ms": stages_ms,
     }
     if plain:
+        plain["roofline"] = solver_roofline(vsc, dev, stream, form="exact")
         line["plain"] = plain
         line["speedup_vs_plain"] = value / plain["value"]
-        line["psnr_vs_plain"] = quality
+        line["e2e_speedup_vs_plain"] = e2e["value"] / plain["e2e"]["value"]
+        line["quality_vs_plain"] = quality_vs_plain(vsc, kw, dev_frames, stream)
+    if rank == 0 and ws == 1 and not args.no_extras:
+        line["precision_bf16_fullres"] = quality_vs_plain(vsc, FORMS["bf16"][0], dev_frames, stream)
+        line["correlation_precision"] = correlation_precision(vsc, dev)
+        line["multistream"] = multistream_measure(vsc, dev, args.ms_form or DEFAULT_MS_FORM, 12, 3, True)
     if rank == 0 and ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_sample(frames, os.cpu_count() or 1)
+        line["cpu_baseline"]["one_core"] = cpu_baseline_sample(frames, 1, n_frames=1)
     if rank == 0:
         print(json.dumps(line))
     if ws > 1:
@@ -990,11 +1098,28 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one solver launch at
-# 1920x1080, by Jacobi steps per launch, from the ncu capture summarised in
-# profiles/ (solver_tall_kernel, 8 steps, the mean of two launches:
-# 124,613,888 + 21,037,568 and 124,601,600 + 18,144,768 bytes).
-SOLVER_TRAFFIC_BYTES = {8: 144_198_912}
+# The full-resolution solver kernel of each form and its compulsory bytes per
+# launch (per pixel): exact form O, U, A, consWt, lap P in (60) + O, U out
+# (24); FMA form O, U, consWt, Cs in (48) + O, U out (24).
+SOLVER_KERNELS = {"exact": ("solver_tall_kernel", 84), "fma": ("solver_fma_kernel", 72)}
+# dram__bytes_read.sum + dram__bytes_write.sum of one 8-step launch at
+# 1920x1080 from the ncu captures summarised in profiles/ (the mean of the
+# captured launches), and where each comes from.
+SOLVER_TRAFFIC_BYTES = {"solver_tall_kernel": 144_198_912, "solver_fma_kernel": 120_321_152}
+SOLVER_TRAFFIC_SOURCE = {
+    "solver_tall_kernel": "profiles/solver_tall_1080p.md (mean of two launches: 124,613,888 + 21,037,568 and "
+                          "124,601,600 + 18,144,768 bytes)",
+    "solver_fma_kernel": "profiles/solver_fma_1080p.md (mean of two launches: 101,465,856 + 19,138,816 and "
+                         "100,983,296 + 19,054,336 bytes)",
+}
+# What bounds each solver kernel, from the same captures: the FP32 pipe and
+# its latency, not HBM (the time steps stay on chip): the FMA pipe's active
+# cycles per sub-partition cycle (sm__pipe_fma_cycles_active / 4 /
+# sm__cycles_active) and smsp__issue_active.
+SOLVER_PIPE = {
+    "solver_tall_kernel": {"fma_pipe_active": None, "issue_active": 0.585},
+    "solver_fma_kernel": {"fma_pipe_active": 0.527, "issue_active": 0.458},
+}
 
 
 def main():
@@ -1004,11 +1129,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the precision report and the 16-stream measurement of the default line")
+    ap.add_argument("--ms-form", choices=sorted(FORMS), default=None,
+                    help="form of the 16-stream measurement inside the default line")
     ap.add_argument("--workload", choices=["1080p", "multistream"], default="1080p",
                     help="multistream: the 16-stream mixed-resolution workload (a separate line)")
     ap.add_argument("--form", choices=sorted(FORMS), default=None,
                     help="the chosen form reported as value (the plain path is timed beside it); default "
-                         "bf16_ds2 (1080p) or bf16_ds2_learned (multistream)")
+                         f"{DEFAULT_FORM} (1080p) or {DEFAULT_MS_FORM} (multistream)")
     ap.add_argument("--ms-grouped", choices=["on", "off"], default="on",
                     help="multistream: group every stream's solve into shared solver launches")
     ap.add_argument("--kernel", choices=["step", "solver", "corr", "front", "upsampler", "warpblend"], default="step",
@@ -1017,12 +1146,6 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "ours":
-        # a step's CUDA graph is captured once per window position (3) and
-        # feedback buffer (2): six warm-up steps keep every capture out of
-        # the timed steps (the end-to-end loop, which waits for each result,
-        # would otherwise time them)
-        args.warmup = max(args.warmup, 6)
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "multistream":
