@@ -403,7 +403,7 @@ def solver_roofline(vsc, dev, stream, iters: int = 144, form: str = "exact"):
     A = torch.rand((H, W, 3), device=dev, generator=g)
     Wt = torch.rand((H, W, 3), device=dev, generator=g) * 2
     O = P.clone()
-    wsp = torch.empty(vsc.consist_out_workspace_size(W, H) // 4, dtype=torch.float32, device=dev)
+    wsp = torch.empty(vsc.consist_out_workspace_size(W, H, form=form) // 4, dtype=torch.float32, device=dev)
     T = int(vsc.load().vsc_solver_steps_per_launch())
     torch.cuda.synchronize()
     for _ in range(2):
@@ -423,7 +423,8 @@ def solver_roofline(vsc, dev, stream, iters: int = 144, form: str = "exact"):
     achieved = alg_bytes / (per_launch_ms / 1000.0) / 1e9
     eff = SOLVER_BYTES_PER_PX * W * H * T / (per_launch_ms / 1000.0) / 1e9
     traffic = SOLVER_TRAFFIC_BYTES.get(kname)
-    line = {"bound": "hbm", "kernel": f"{kname} (64x48 tiles; {T} Jacobi steps per launch at 1920x1080)",
+    tile = "128x72 tiles of one channel plane" if form == "fma" else "64x48 tiles of three channels"
+    line = {"bound": "hbm", "kernel": f"{kname} ({tile}; {T} Jacobi steps per launch at 1920x1080)",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
             "algorithmic_bytes_rule": f"{launch_bpp} B/px per launch: each input image read once and O, U "

@@ -92,14 +92,14 @@ VSC_API void vsc_solver_set_autotune(int32_t on);
  *                     and nK = -s*(cnt + w):  g = fma(nK, O, fma(s, S, Cs))
  *                     with S the sum of the valid neighbours, O' = O + g
  *                     (+ m*U), U' = g: seven FP32 operations per pixel and
- *                     channel instead of twelve, one image fewer loaded per
- *                     tile.  Differs from the exact form by rounding only: at
+ *                     channel instead of twelve, each channel solved as its
+ *                     own plane.  Differs from the exact form by rounding only: at
  *                     1920x1080 over a 150-iteration solve within 1e-6
  *                     absolute (images in [0, 1]), > 100 dB PSNR, and RGBA8
  *                     bytes differing on about 1e-5 of the values.
  * The autotuner chooses the exact form's tile shape (32 or 48 rows); the
- * FMA form has one (48 rows), which vsc_solver_autotune_form reports
- * without measuring. */
+ * FMA form has one (72 rows of a plane), which vsc_solver_autotune_form
+ * reports without measuring. */
 #define VSC_SOLVER_EXACT 0
 #define VSC_SOLVER_FMA 1
 VSC_API vsc_status vsc_solver_autotune_form(int32_t width, int32_t height, int32_t form, vsc_stream_t stream,
@@ -277,9 +277,12 @@ VSC_API vsc_status vsc_get_consist_out(const vsc_image* crnt_pr, const vsc_image
     const vsc_image* cons_wt, int32_t num_iter, float step_size, float mom_fac, const vsc_image* consis_out,
     void* workspace, size_t workspace_bytes, vsc_stream_t stream);
 
-/* vsc_get_consist_out in the VSC_SOLVER_FMA form: same arguments and
- * workspace; results within the tolerance stated at VSC_SOLVER_FMA of
+/* vsc_get_consist_out in the VSC_SOLVER_FMA form: same arguments; its
+ * workspace (vsc_consist_out_fma_workspace_size bytes, 16-byte aligned, or
+ * NULL for the library's stream-ordered pool) holds the solve as planes, 18
+ * floats a pixel.  Results within the tolerance stated at VSC_SOLVER_FMA of
  * vsc_get_consist_out's.  No counterpart in the reference. */
+VSC_API size_t vsc_consist_out_fma_workspace_size(int32_t width, int32_t height);
 VSC_API vsc_status vsc_get_consist_out_fma(const vsc_image* crnt_pr, const vsc_image* prev_stab_warp,
     const vsc_image* cons_wt, int32_t num_iter, float step_size, float mom_fac, const vsc_image* consis_out,
     void* workspace, size_t workspace_bytes, vsc_stream_t stream);

@@ -123,8 +123,10 @@ def test_consist_out(vsc, oracle, cuda, h, w, iters):
     assert np.array_equal(O2.cpu().numpy().view(np.uint32), O.cpu().numpy().view(np.uint32))
 
 
-# the FMA form: widths divisible by 4 take the TMA-fed kernel, others the
-# plain-load one; iteration counts not divisible by 8 end in a short launch
+# the FMA form: widths divisible by 4 take the TMA-fed kernel (128 x 72 tiles
+# of one plane: these sizes give one tile, several, partial tiles at the right
+# and bottom), others the plain-load one; iteration counts not divisible by 8
+# end in a short launch
 @pytest.mark.parametrize("h,w,iters", [(9, 11, 0), (9, 11, 1), (9, 11, 2), (40, 56, 75), (3, 3, 5), (2, 2, 4),
                                        (67, 33, 150), (48, 200, 13), (540, 960, 75), (1080, 1920, 150),
                                        (17, 4, 3), (100, 64, 150), (61, 70, 19)])
@@ -151,17 +153,23 @@ def test_consist_out_fma(vsc, oracle, cuda, h, w, iters):
     print(f"fma vs exact {w}x{h} x{iters}: max-abs {d.max():.3g}, PSNR {psnr:.1f} dB, RGBA8 byte flips {flips:.2e}")
     assert d.max() <= 2e-6 and psnr >= 100.0 and flips <= 1e-3
     # caller-provided workspace gives the same bits
-    ws = torch.empty(vsc.consist_out_workspace_size(w, h) // 4, dtype=torch.float32, device=cuda)
+    ws = torch.empty(vsc.consist_out_workspace_size(w, h, form="fma") // 4, dtype=torch.float32, device=cuda)
     O2 = _t(O0, cuda)
     vsc.get_consist_out(_t(P, cuda), _t(A, cuda), _t(Wt, cuda), iters, 0.15, 0.15, O2, workspace=ws, form="fma")
+    # a workspace of the exact form's size is too small for the FMA form
+    if iters:
+        small = torch.empty(vsc.consist_out_workspace_size(w, h) // 4, dtype=torch.float32, device=cuda)
+        with pytest.raises(vsc.VscError, match="ENOMEM"):
+            vsc.get_consist_out(_t(P, cuda), _t(A, cuda), _t(Wt, cuda), iters, 0.15, 0.15, O2, workspace=small,
+                                form="fma")
     assert np.array_equal(O2.cpu().numpy().view(np.uint32), got.view(np.uint32))
 
 
 def test_consist_out_fma_single_tile_shape(vsc, cuda):
-    """The FMA form has one tile shape (64 x 48); the autotuner reports it
-    without measuring."""
-    assert vsc.solver_autotune(960, 544, form="fma") == 48
-    assert vsc.solver_tile_rows(960, 544, form="fma") == (48, False)
+    """The FMA form has one tile shape (128 x 72 of a plane); the autotuner
+    reports it without measuring."""
+    assert vsc.solver_autotune(960, 544, form="fma") == 72
+    assert vsc.solver_tile_rows(960, 544, form="fma") == (72, False)
 
 
 def test_consist_out_zero_regions(vsc, oracle, cuda):

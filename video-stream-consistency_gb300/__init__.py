@@ -47,7 +47,8 @@ EXPORTED = [
     "vsc_stabilizer_set_upsampler", "vsc_solver_autotune", "vsc_solver_tile_rows", "vsc_solver_set_autotune",
     "vsc_multistream_set_fused", "vsc_multistream_fused", "vsc_multistream_set_upsampler",
     "vsc_stabilizer_synchronize", "vsc_stabilizer_wait_output",
-    "vsc_get_consist_out_fma", "vsc_solver_autotune_form", "vsc_solver_tile_rows_form",
+    "vsc_get_consist_out_fma", "vsc_consist_out_fma_workspace_size", "vsc_solver_autotune_form",
+    "vsc_solver_tile_rows_form",
     "vsc_stabilizer_set_solver_form", "vsc_multistream_set_solver_form",
 ]
 VSC_DTYPE_F32, VSC_DTYPE_BF16, VSC_DTYPE_F16 = 0, 1, 2
@@ -206,6 +207,8 @@ def load():
     L.vsc_correlation_lowp_workspace_size.argtypes = [i64, i64, i64, i64]
     L.vsc_consist_out_workspace_size.restype = C.c_size_t
     L.vsc_consist_out_workspace_size.argtypes = [i32, i32]
+    L.vsc_consist_out_fma_workspace_size.restype = C.c_size_t
+    L.vsc_consist_out_fma_workspace_size.argtypes = [i32, i32]
     L.vsc_default_hyper_params.restype = None
     L.vsc_default_hyper_params.argtypes = [C.POINTER(HyperParams)]
     L.vsc_stabilizer_hyper_params.restype = C.POINTER(HyperParams)
@@ -450,7 +453,7 @@ SOLVER_FORMS = {"exact": 0, "fma": 1}  # VSC_SOLVER_EXACT, VSC_SOLVER_FMA
 
 def solver_autotune(w: int, h: int, stream=None, form: str = "exact") -> int:
     """Time both tile shapes of the exact solver form at w x h and keep the
-    faster; returns its rows (exact: 32 or 48; the fma form has one, 48)."""
+    faster; returns its rows (exact: 32 or 48; the fma form has one, 72)."""
     rows = C.c_int32()
     _check(load().vsc_solver_autotune_form(int(w), int(h), SOLVER_FORMS[form], _stream(stream), C.byref(rows)))
     return rows.value
@@ -467,8 +470,9 @@ def solver_set_autotune(on: bool) -> None:
     load().vsc_solver_set_autotune(1 if on else 0)
 
 
-def consist_out_workspace_size(w: int, h: int) -> int:
-    return int(load().vsc_consist_out_workspace_size(w, h))
+def consist_out_workspace_size(w: int, h: int, form: str = "exact") -> int:
+    fn = load().vsc_consist_out_fma_workspace_size if form == "fma" else load().vsc_consist_out_workspace_size
+    return int(fn(w, h))
 
 
 def get_consist_out(crnt_pr, prev_stab_warp, cons_wt, num_iter, step_size, mom_fac, consis_out, workspace=None,

@@ -490,7 +490,14 @@ VSC_API size_t vsc_consist_out_workspace_size(int32_t width, int32_t height)
 {
     if (!dims_ok(width) || !dims_ok(height))
         return 0;
-    return solver_workspace_floats(width, height) * sizeof(float);
+    return solver_workspace_floats(width, height, kSolverExact) * sizeof(float);
+}
+
+VSC_API size_t vsc_consist_out_fma_workspace_size(int32_t width, int32_t height)
+{
+    if (!dims_ok(width) || !dims_ok(height))
+        return 0;
+    return solver_workspace_floats(width, height, kSolverFma) * sizeof(float);
 }
 
 namespace {
@@ -508,7 +515,7 @@ vsc_status consist_out_form(int form, const vsc_image* crnt_pr, const vsc_image*
     if (num_iter < 0)
         return set_error(VSC_EINVAL, "consist_out: negative iteration count");
     const int w = consis_out->width, h = consis_out->height;
-    const size_t need = vsc_consist_out_workspace_size(w, h);
+    const size_t need = solver_workspace_floats(w, h, form) * sizeof(float);
     void* ws = workspace;
     bool pooled = false;
     if (ws) {
@@ -890,7 +897,7 @@ vsc_status alloc_all(vsc_stabilizer* s)
         A(dalloc(&s->pyrW[j], m));
         A(dalloc(&s->pyrO[j], m));
     }
-    A(dalloc(&s->solver_ws, solver_workspace_floats(s->w, s->h)));
+    A(dalloc(&s->solver_ws, solver_workspace_floats(s->w, s->h, kSolverFma)));  // room for either form
     if (s->compute_flow) {
         s->fd = flow_dims(s->fw, s->fh);
         // the three frames' features in one allocation, so a flow pair can
@@ -1815,7 +1822,7 @@ float* ms_level_ws(vsc_multistream* m, size_t i, int j)
         return s->solver_ws;
     float* p = m->lvl_ws[i];
     for (int k = 1; k < j; ++k)
-        p += solver_workspace_floats(s->lw[k], s->lh[k]);
+        p += solver_workspace_floats(s->lw[k], s->lh[k], kSolverFma);
     return p;
 }
 
@@ -1845,7 +1852,7 @@ cudaError_t ms_enqueue_fused(vsc_multistream* m, const std::vector<uint8_t*>& ou
         const int it = hp.num_iter / L;
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(solver_start_buffer(lv[i].O[L - 1], s->lw[L - 1], s->lh[L - 1], it,
-                                    ms_level_ws(m, i, L - 1)),
+                                    ms_level_ws(m, i, L - 1), m->solver_form),
                 lv[i].P[L - 1], static_cast<size_t>(s->lw[L - 1]) * s->lh[L - 1] * 3 * sizeof(float),
                 cudaMemcpyDeviceToDevice, s->st);
         if (e == cudaSuccess && (e = cudaEventRecord(m->joined[i], m->side[i])) == cudaSuccess)
@@ -1862,7 +1869,8 @@ cudaError_t ms_enqueue_fused(vsc_multistream* m, const std::vector<uint8_t*>& ou
                 j == 0 ? outs[i] : nullptr};
             if (j != L - 1) {
                 up_in[i] = Img{lv[i].O[j + 1], s->lw[j + 1], s->lh[j + 1], 3};
-                up_out[i] = Img{solver_start_buffer(lv[i].O[j], s->lw[j], s->lh[j], it, ws), s->lw[j], s->lh[j], 3};
+                up_out[i] = Img{solver_start_buffer(lv[i].O[j], s->lw[j], s->lh[j], it, ws, m->solver_form), s->lw[j],
+                    s->lh[j], 3};
             }
         }
         if (j != L - 1) {
@@ -2052,7 +2060,7 @@ VSC_API vsc_status vsc_multistream_create(const vsc_stream_desc* desc, int32_t n
         vsc_stabilizer* st = m->st[i];
         size_t floats = 0;
         for (int j = 1; j < st->levels_alloc; ++j)
-            floats += solver_workspace_floats(st->lw[j], st->lh[j]);
+            floats += solver_workspace_floats(st->lw[j], st->lh[j], kSolverFma);  // room for either form
         float* p = nullptr;
         if (floats && (s = check_cuda(dalloc(&p, floats), "multistream_create level workspaces")))
             break;

@@ -138,15 +138,18 @@ cudaError_t launch_bilinear_group(const Img* in, const Img* out, int n, cudaStre
 // flowmodel.cpp:126-133): source = min(iw-1, ((2x+1)*iw) / (2*ow)).
 cudaError_t launch_resize_nearest(const float* in, int iw, int ih, float* out, int ow, int oh, cudaStream_t st);
 
-// Solver.  The workspace holds the Laplacian of the processed image (the
-// FMA form: its per-pixel constant Cs), two momentum images and the second
-// Jacobi buffer: 4 * w*h*3 floats.
-//   kSolverExact: kernel_consist_out's expression, bit for bit;
+// Solver.
+//   kSolverExact: kernel_consist_out's expression, bit for bit; workspace:
+//                 the Laplacian of the processed image, two momentum images
+//                 and the second Jacobi buffer, 4 * w*h*3 floats;
 //   kSolverFma:   the same step regrouped around per-solve constants with
-//                 fused multiply-adds (within a tolerance of the exact form;
-//                 equal to the restatement's FMA form).
+//                 fused multiply-adds, each channel solved as its own plane
+//                 (within a tolerance of the exact form; equal to the
+//                 restatement's FMA form); workspace: the constants Cs and
+//                 nK, two momentum images and two iterates, all as planes,
+//                 6 * w*h*3 floats.
 enum SolverForm { kSolverExact = 0, kSolverFma = 1 };
-size_t solver_workspace_floats(int w, int h);
+size_t solver_workspace_floats(int w, int h, int form = kSolverExact);
 int solver_steps_per_launch();  // Jacobi steps one solver launch performs (temporal blocking)
 // Tile-shape autotuner of the persistent solver kernels (same results either
 // way): solver_autotune times both shapes at (w, h) on scratch images and
@@ -180,16 +183,16 @@ struct SolverImage {
     const float* Wt;
     float* O;
     int w, h;
-    float* workspace;  // solver_workspace_floats(w, h)
+    float* workspace;  // solver_workspace_floats(w, h, form)
     uint8_t* rgba;     // RGBA8 copy of the result, or null
 };
-float* solver_start_buffer(float* O, int w, int h, int num_iter, float* workspace);
+float* solver_start_buffer(float* O, int w, int h, int num_iter, float* workspace, int form = kSolverExact);
 bool solver_tma_supported();  // the persistent TMA kernels run on the current device
 cudaError_t solver_lap(const float* P, int w, int h, float* workspace, cudaStream_t st);
 // the per-solve precomputation of a form: lap P (exact) or Cs (FMA), into the workspace
 cudaError_t solver_prep(int form, const float* P, const float* A, const float* Wt, int w, int h, float step,
     float* workspace, cudaStream_t st);
-bool solver_group_eligible(const SolverImage* im, int n);
+bool solver_group_eligible(const SolverImage* im, int n, int form = kSolverExact);
 cudaError_t run_solver_group(const SolverImage* im, int n, int num_iter, float step, float mom, cudaStream_t st,
     int* launches, int form = kSolverExact);
 

@@ -855,23 +855,52 @@ __global__ void __launch_bounds__(kPThreads, 1)
 
 // ---- FMA form of the solver ---------------------------------------------------
 // kernel_consist_out's step, g = (lap O - lap P) - w (O - A), O' = O + s g
-// (+ m U), U' = s g, regrouped around two per-pixel constants:
-//   Cs = s * fma(w, A, -lap P)   once per solve (solver_prep_fma_kernel),
-//   nK = -(s * (cnt + w))        when a tile is loaded (cnt = valid neighbours),
+// (+ m U), U' = s g, regrouped around two per-pixel constants computed once
+// per solve (solver_prep_fma_kernel):
+//   Cs = s * fma(w, A, -lap P),   nK = -(s * (cnt + w))   (cnt = valid neighbours),
 // so that one step is
 //   S = (left + right) + (up + down),  g = fma(nK, O, fma(s, S, Cs)),
 //   O' = O + g, then O' = fma(m, U, O') after the first step,  U' = g,
 // with invalid neighbours read as +0: seven FP32 operations per pixel and
-// channel against twelve in the reference expression, and a tile loads four
-// images (O, U, consWt, Cs) instead of five.  The rounding differs from the
-// reference form's, so results agree with it within a tolerance (and with
-// the restatement's FMA form, vo_consist_out_fma, bit for bit).  Tiles: 64 x
-// 4*kWarps pixels, each thread a 2-column x 4-row block, register state O,
-// U, Cs, nK as column pairs per row and channel.
+// channel against twelve in the reference expression.  The rounding differs
+// from the reference form's, so results agree with it within a tolerance
+// (and with the restatement's FMA form, vo_consist_out_fma, bit for bit).
+//
+// The three colour channels of the step never interact, so the form solves
+// each channel as its own image: the workspace holds O, U, Cs and nK as
+// planes (channel-major, solver_to_planar / solver_from_planar convert O at
+// the ends of a solve).  A tile is 128 x 72 pixels of one plane: each of the
+// 384 threads keeps a 4-column x 6-row block of O, U, Cs and nK in registers
+// (96 floats), a warp spans the tile's width, so the 8-pixel ring of the
+// temporal blocking leaves a 112 x 56 interior (68 % of the tile; the
+// interleaved 64 x 48 tile of three channels kept 50 %), horizontal
+// neighbours cost two shuffles per row for four pixels, and each warp
+// publishes its top and bottom row as two 16-byte stores per thread.
 
-// Cs = step * fma(wt, A, -lap P); lap P as lap_pr_kernel computes it.
+constexpr int kPlW = 128;                 // tile width (a warp: 32 lanes x 4 columns)
+constexpr int kPlIW = kPlW - 2 * kTbT;    // interior width (112)
+constexpr int kPlPX = kPlW + 8;           // edge-row pitch (a 16-byte apron each side)
+constexpr int kPlWarps = 12;
+constexpr int kPlThreads = 32 * kPlWarps;
+constexpr int kPlRPT = 6;                 // rows per thread
+constexpr int kPlRows = kPlRPT * kPlWarps;  // 72
+constexpr int kPlIRows = kPlRows - 2 * kTbT;  // 56
+constexpr int kPlStage = kPlRows * kPlW;  // floats of one input tile
+constexpr int kPlStageBytes = kPlStage * static_cast<int>(sizeof(float));
+constexpr int kPlSlotPlane = (kPlWarps + 2) * 2 * kPlPX;  // edge-row slots of one buffer
+constexpr int kPlOut = kPlIRows * kPlIW;  // floats of one interior tile
+constexpr int kPlSmem = 4 * kPlStageBytes + (2 * kPlSlotPlane + 2 * kPlOut) * static_cast<int>(sizeof(float)) + 16;
+static_assert(kPlSmem <= 232448, "dynamic shared memory per CTA");
+static_assert((kPlIW * 4) % 16 == 0 && (kTbT * 4) % 16 == 0, "TMA x coordinates must be 16-byte aligned");
+static_assert((4 * kPlStageBytes) % 128 == 0 && (2 * kPlSlotPlane * 4) % 128 == 0 && (kPlOut * 4) % 128 == 0,
+    "TMA sources and destinations on the 128-byte grid");
+
+// Cs = step * fma(wt, A, -lap P) and nK = -(step * (cnt + wt)) as planes
+// (lap P, cnt as lap_pr_kernel computes them); with O non-null, also O as
+// planes into Op.
 __global__ void solver_prep_fma_kernel(const float* __restrict__ P, const float* __restrict__ A,
-    const float* __restrict__ Wt, float* __restrict__ Cs, int w, int h, float step)
+    const float* __restrict__ Wt, const float* __restrict__ O, float* __restrict__ Cs, float* __restrict__ nK,
+    float* __restrict__ Op, int w, int h, float step)
 {
     pdl_enter();
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -880,6 +909,8 @@ __global__ void solver_prep_fma_kernel(const float* __restrict__ P, const float*
         return;
     const int64_t i0 = pix_index(x, y, w) * 3;
     const int64_t rs = static_cast<int64_t>(w) * 3;
+    const int64_t plane = static_cast<int64_t>(w) * h;
+    const int64_t q = pix_index(x, y, w);
     for (int c = 0; c < 3; ++c) {
         const int64_t i = i0 + c;
         int cnt = 0;
@@ -901,220 +932,278 @@ __global__ void solver_prep_fma_kernel(const float* __restrict__ P, const float*
             cnt += 1;
         }
         lap = __fsub_rn(lap, __fmul_rn(static_cast<float>(cnt), P[i]));
-        Cs[i] = __fmul_rn(step, __fmaf_rn(Wt[i], A[i], -lap));
+        const float wt = Wt[i];
+        Cs[c * plane + q] = __fmul_rn(step, __fmaf_rn(wt, A[i], -lap));
+        nK[c * plane + q] = -__fmul_rn(step, __fadd_rn(static_cast<float>(cnt), wt));
+        if (O)
+            Op[c * plane + q] = O[i];
     }
 }
 
-template <int kWarps>
-struct FmaTile {
-    static constexpr int kThreads = 32 * kWarps;
-    static constexpr int kRows = 4 * kWarps;            // tile rows
-    static constexpr int kIRows = kRows - 2 * kTbT;     // interior rows
-    static constexpr int kStageFloats = kRows * kTbEX * 3;
-    static constexpr int kStageBytes = kStageFloats * static_cast<int>(sizeof(float));
-    static constexpr int kPlane = (kWarps + 2) * 2 * kTbPX;  // edge-row slots of one channel and buffer
-    static constexpr int kObuf = 2 * 3 * kPlane;
-    static constexpr int kSmem = 4 * kStageBytes + kObuf * static_cast<int>(sizeof(float)) + 16;
-    static_assert(kSmem <= 232448, "dynamic shared memory per CTA");
-    static_assert(kObuf >= 2 * kIRows * 3 * kIW, "the edge-row buffers hold a tile's interior O and U");
-    static_assert((kIRows * 3 * kIW * 4) % 128 == 0 && (4 * kStageBytes) % 128 == 0,
-        "TMA store sources on the 128-byte grid");
+// Interleaved <-> planar copies of the images of up to kPlanarGroupMax solves
+// (one launch per level of a multi-stream step): to_planar = 1 reads the
+// interleaved src and writes dst as planes; 0 the reverse, and writes the
+// RGBA8 copy when rgba is non-null.
+constexpr int kPlanarGroupMax = 16;
+struct PlanarGroup {
+    const float* src[kPlanarGroupMax];
+    float* dst[kPlanarGroupMax];
+    uint8_t* rgba[kPlanarGroupMax];
+    int64_t npix[kPlanarGroupMax];
+    int block0[kPlanarGroupMax + 1];
+    int count;
 };
 
-// 12 warps: three on each quarter of the SM's register file (16,384
-// registers), so up to 170 registers a thread; the state takes 96.  (With 14
-// warps, four on some quarters, a thread gets 128 and the state spills.)
-constexpr int kFmaWarps = 12;
-
-struct FmaState {
-    float2 o[4][3], u[4][3], c[4][3], nk[4][3];  // [row][channel] = (column 0, column 1)
-};
-
-// One step of a thread's 2 x 4 block: the previous iterate's edge rows of the
-// neighbouring warps come from `src`, the new top and bottom rows go to `dst`.
-template <bool kAll, int kPlane>
-__device__ __forceinline__ void fma_step(FmaState& s, const float* src, float* dst, bool mom_on, float step,
-    float mom, int px0, int warp, int gx0, int gy0, int w, int h)
+__global__ void __launch_bounds__(256) planar_group_kernel(const __grid_constant__ PlanarGroup g, int to_planar)
 {
-#pragma unroll
-    for (int ch = 0; ch < 3; ++ch) {
-        const float* S = src + ch * kPlane;
-        const float2 up = *reinterpret_cast<const float2*>(&S[(warp * 2 + 1) * kTbPX + px0 + 2]);
-        const float2 dn = *reinterpret_cast<const float2*>(&S[((warp + 2) * 2) * kTbPX + px0 + 2]);
-        float L[4], R[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            L[r] = __shfl_up_sync(0xffffffffu, s.o[r][ch].y, 1);
-            R[r] = __shfl_down_sync(0xffffffffu, s.o[r][ch].x, 1);
-        }
-        float2 on[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const float2 o = s.o[r][ch];
-            float2 u = r == 0 ? up : s.o[r - 1][ch];
-            float2 d = r == 3 ? dn : s.o[r + 1][ch];
-            float l0 = L[r], r0 = o.y, l1 = o.x, r1 = R[r];
-            if (!kAll) {
-                const Nb a = nb_of(gx0, gy0 + r, w, h), b = nb_of(gx0 + 1, gy0 + r, w, h);
-                l0 = a.vl ? l0 : 0.0f;
-                r0 = a.vr ? r0 : 0.0f;
-                u.x = a.vu ? u.x : 0.0f;
-                d.x = a.vd ? d.x : 0.0f;
-                l1 = b.vl ? l1 : 0.0f;
-                r1 = b.vr ? r1 : 0.0f;
-                u.y = b.vu ? u.y : 0.0f;
-                d.y = b.vd ? d.y : 0.0f;
-            }
-            // scalar FP32: the FMA pipe is the limit, where a packed f32x2
-            // operation costs both lanes' cycles and pairing its operands costs
-            // register moves on the same pipe (measured 11 % slower)
-            float2 g, n;
-            g.x = __fmaf_rn(s.nk[r][ch].x, o.x,
-                __fmaf_rn(step, __fadd_rn(__fadd_rn(l0, r0), __fadd_rn(u.x, d.x)), s.c[r][ch].x));
-            g.y = __fmaf_rn(s.nk[r][ch].y, o.y,
-                __fmaf_rn(step, __fadd_rn(__fadd_rn(l1, r1), __fadd_rn(u.y, d.y)), s.c[r][ch].y));
-            n.x = __fadd_rn(o.x, g.x);
-            n.y = __fadd_rn(o.y, g.y);
-            if (mom_on) {
-                n.x = __fmaf_rn(mom, s.u[r][ch].x, n.x);
-                n.y = __fmaf_rn(mom, s.u[r][ch].y, n.y);
-            }
-            s.u[r][ch] = g;
-            on[r] = n;
-        }
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-            s.o[r][ch] = on[r];
-        float* D = dst + ch * kPlane + ((warp + 1) * 2) * kTbPX + px0 + 2;
-        *reinterpret_cast<float2*>(D) = on[0];           // top row
-        *reinterpret_cast<float2*>(D + kTbPX) = on[3];   // bottom row
+    pdl_enter();
+    int p = 0;
+    while (p + 1 < g.count && static_cast<int>(blockIdx.x) >= g.block0[p + 1])
+        ++p;
+    const int64_t i = static_cast<int64_t>(blockIdx.x - g.block0[p]) * blockDim.x + threadIdx.x;
+    const int64_t n = g.npix[p];
+    if (i >= n)
+        return;
+    if (to_planar) {
+        const float* s = g.src[p] + i * 3;
+        g.dst[p][i] = s[0];
+        g.dst[p][n + i] = s[1];
+        g.dst[p][2 * n + i] = s[2];
+        return;
     }
+    const float r = g.src[p][i], gg = g.src[p][n + i], b = g.src[p][2 * n + i];
+    float* d = g.dst[p] + i * 3;
+    d[0] = r;
+    d[1] = gg;
+    d[2] = b;
+    if (g.rgba[p])
+        reinterpret_cast<uint32_t*>(g.rgba[p])[i] = pack_rgba(r, gg, b);
 }
 
-// Iteration k is needed on rows [ring - T + k + 1, kRows - ring + T - k - 1)
-// (ring = kTbT); a warp whose four rows all lie outside skips it.
-template <bool kAll, int kWarps>
-__device__ __forceinline__ void fma_iterate(FmaState& s, float* obuf, int T, int k0, float step, float mom, int px0,
+struct PlState {
+    float4 o[kPlRPT], u[kPlRPT], c[kPlRPT], nk[kPlRPT];  // [row] = (column 0 .. 3)
+};
+
+__device__ __forceinline__ float& f4(float4& v, int j) { return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w; }
+__device__ __forceinline__ float f4c(const float4& v, int j) { return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w; }
+
+// One step of a thread's 4 x 6 block: the previous iterate's edge rows of the
+// neighbouring warps come from `src`, the new top and bottom rows go to `dst`.
+template <bool kAll>
+__device__ __forceinline__ void pl_step(PlState& s, const float* src, float* dst, bool mom_on, float step, float mom,
+    int lane, int warp, int gx0, int gy0, int w, int h)
+{
+    const float4 up = *reinterpret_cast<const float4*>(&src[(warp * 2 + 1) * kPlPX + 4 * lane + 4]);
+    const float4 dn = *reinterpret_cast<const float4*>(&src[((warp + 2) * 2) * kPlPX + 4 * lane + 4]);
+    float L[kPlRPT], R[kPlRPT];
+#pragma unroll
+    for (int r = 0; r < kPlRPT; ++r) {
+        L[r] = __shfl_up_sync(0xffffffffu, s.o[r].w, 1);
+        R[r] = __shfl_down_sync(0xffffffffu, s.o[r].x, 1);
+    }
+    float4 on[kPlRPT];
+#pragma unroll
+    for (int r = 0; r < kPlRPT; ++r) {
+        const float4 o = s.o[r];
+        const float4 u = r == 0 ? up : s.o[r - 1];
+        const float4 d = r == kPlRPT - 1 ? dn : s.o[r + 1];
+        bool vu = true, vd = true;
+        if (!kAll) {
+            vu = (gy0 + r - 1) >= 0;
+            vd = (gy0 + r + 1) < (h - 1);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float left = j == 0 ? L[r] : f4c(o, j - 1);
+            float right = j == 3 ? R[r] : f4c(o, j + 1);
+            float upv = f4c(u, j), dnv = f4c(d, j);
+            if (!kAll) {
+                const int gx = gx0 + j;
+                left = (gx - 1) >= 0 ? left : 0.0f;
+                right = (gx + 1) < (w - 1) ? right : 0.0f;
+                upv = vu ? upv : 0.0f;
+                dnv = vd ? dnv : 0.0f;
+            }
+            const float oj = f4c(o, j);
+            const float g = __fmaf_rn(f4c(s.nk[r], j), oj,
+                __fmaf_rn(step, __fadd_rn(__fadd_rn(left, right), __fadd_rn(upv, dnv)), f4c(s.c[r], j)));
+            float n = __fadd_rn(oj, g);
+            if (mom_on)
+                n = __fmaf_rn(mom, f4c(s.u[r], j), n);
+            f4(s.u[r], j) = g;
+            f4(on[r], j) = n;
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < kPlRPT; ++r)
+        s.o[r] = on[r];
+    float* D = dst + ((warp + 1) * 2) * kPlPX + 4 * lane + 4;
+    *reinterpret_cast<float4*>(D) = on[0];                   // top row
+    *reinterpret_cast<float4*>(D + kPlPX) = on[kPlRPT - 1];  // bottom row
+}
+
+// Iteration k is needed on rows [ring - T + k + 1, kPlRows - ring + T - k - 1)
+// (ring = kTbT); a warp whose rows all lie outside skips it.
+template <bool kAll>
+__device__ __forceinline__ void pl_iterate(PlState& s, float* slots, int T, int k0, float step, float mom, int lane,
     int warp, int gx0, int gy0, int w, int h)
 {
-    using G = FmaTile<kWarps>;
-    const int r0 = 4 * warp;
+    const int r0 = kPlRPT * warp;
     if (T == kTbT) {
         // full launches, unrolled; momentum is off only in the first step of a solve
         const bool later = k0 > 0;
 #pragma unroll
         for (int k = 0; k < kTbT; ++k) {
-            if (!(r0 + 3 < k + 1 || r0 >= G::kRows - k - 1))
-                fma_step<kAll, G::kPlane>(s, obuf + (k & 1) * 3 * G::kPlane, obuf + ((k & 1) ^ 1) * 3 * G::kPlane,
-                    k > 0 || later, step, mom, px0, warp, gx0, gy0, w, h);
+            if (!(r0 + kPlRPT - 1 < k + 1 || r0 >= kPlRows - k - 1))
+                pl_step<kAll>(s, slots + (k & 1) * kPlSlotPlane, slots + ((k & 1) ^ 1) * kPlSlotPlane,
+                    k > 0 || later, step, mom, lane, warp, gx0, gy0, w, h);
             __syncthreads();
         }
         return;
     }
     for (int k = 0; k < T; ++k) {
-        const int lo = kTbT - T + k + 1, hi = G::kRows - kTbT + T - k - 1;
-        if (!(r0 + 3 < lo || r0 >= hi))
-            fma_step<kAll, G::kPlane>(s, obuf + (k & 1) * 3 * G::kPlane, obuf + ((k & 1) ^ 1) * 3 * G::kPlane,
-                (k0 + k) > 0, step, mom, px0, warp, gx0, gy0, w, h);
+        const int lo = kTbT - T + k + 1, hi = kPlRows - kTbT + T - k - 1;
+        if (!(r0 + kPlRPT - 1 < lo || r0 >= hi))
+            pl_step<kAll>(s, slots + (k & 1) * kPlSlotPlane, slots + ((k & 1) ^ 1) * kPlSlotPlane, (k0 + k) > 0,
+                step, mom, lane, warp, gx0, gy0, w, h);
         __syncthreads();
     }
 }
 
-// stage i of the FMA kernels holds map fma_map(i): O, U, consWt, Cs
-__device__ __forceinline__ int fma_map(int i) { return i < 2 ? i : i + 1; }
+// A tile of the planar solve: problem, channel plane and origin (ring included).
+struct PlTile {
+    int p, c, ox, oy, w, h;
+};
 
-__device__ __forceinline__ void fma_issue(float* stage, const CUtensorMap* m, int ox, int oy, int stage_floats,
-    int first, int last, uint64_t* bar)
+int pl_tiles_x(int w) { return (w + kPlIW - 1) / kPlIW; }
+int pl_tiles(int w, int h) { return 3 * pl_tiles_x(w) * ((h + kPlIRows - 1) / kPlIRows); }
+
+// tile -> problem by a scan of the first-tile table, then channel and position
+template <int kN>
+__device__ __forceinline__ PlTile pl_locate(const SolverGroup<kN>& g, int tile)
 {
-    for (int i = first; i < last; ++i)
-        tma_load_2d(stage + i * stage_floats, m + fma_map(i), 3 * ox, oy, bar);
+    int p = 0;
+    if (kN > 1) {
+#pragma unroll 1
+        while (p + 1 < g.count && tile >= g.tile0[p + 1])
+            ++p;
+    }
+    const int per_plane = (g.tile0[p + 1] - g.tile0[p]) / 3;
+    int t = tile - g.tile0[p];
+    PlTile l;
+    l.p = p;
+    l.c = t / per_plane;
+    t -= l.c * per_plane;
+    l.ox = (t % g.tiles_x[p]) * kPlIW - kTbT;
+    l.oy = (t / g.tiles_x[p]) * kPlIRows - kTbT;
+    l.w = g.w[p];
+    l.h = g.h[p];
+    return l;
 }
 
-// The first tile of a launch: consWt and Cs, which no solver launch writes,
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, int x, int y, int z, const void* src)
+{
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+        "r"(x), "r"(y), "r"(z), "r"(smem_u32(src))
+        : "memory");
+}
+
+// stage i holds map pl_map(i): O, U, nK (the consWt slot), Cs (the lap slot)
+__device__ __forceinline__ int pl_map(int i) { return i < 2 ? i : i + 1; }
+
+__device__ __forceinline__ void pl_issue(float* stage, const CUtensorMap* m, const PlTile& t, int first, int last,
+    uint64_t* bar)
+{
+    for (int i = first; i < last; ++i)
+        tma_load_3d(stage + i * kPlStage, m + pl_map(i), t.ox, t.oy, t.c, bar);
+}
+
+// The first tile of a launch: nK and Cs, which no solver launch writes,
 // before the wait for the predecessor (a launch after the first of a solve);
 // O and U after it.
-__device__ __forceinline__ void fma_issue_first(float* stage, const CUtensorMap* m, int ox, int oy,
-    int stage_floats, uint32_t bytes, uint64_t* bar, bool early)
+__device__ __forceinline__ void pl_issue_first(float* stage, const CUtensorMap* m, const PlTile& t, uint64_t* bar,
+    bool early)
 {
     if (early) {
-        mbar_expect_tx(bar, 4 * bytes);
-        fma_issue(stage, m, ox, oy, stage_floats, 2, 4, bar);
+        mbar_expect_tx(bar, 4 * kPlStageBytes);
+        pl_issue(stage, m, t, 2, 4, bar);
     }
     grid_dependency_wait();
     if (early) {
-        fma_issue(stage, m, ox, oy, stage_floats, 0, 2, bar);
+        pl_issue(stage, m, t, 0, 2, bar);
     } else {
-        mbar_expect_tx(bar, 4 * bytes);
-        fma_issue(stage, m, ox, oy, stage_floats, 0, 4, bar);
+        mbar_expect_tx(bar, 4 * kPlStageBytes);
+        pl_issue(stage, m, t, 0, 4, bar);
     }
 }
 
-// The images of a solve for the plain-load form of the FMA kernel (widths
-// that are not a multiple of 4, or images off the 16-byte grid): raw pointers
-// instead of tensor maps.
-struct FmaPlain {
-    const float *O, *U, *W, *C;
+// The planes of one solve for the plain-load form of the kernel (widths that
+// are not a multiple of 4, or planes off the 16-byte grid).
+struct PlPlain {
+    const float *O, *U, *K, *C;
     float *Oo, *Uo;
     int w, h, tiles_x, ntiles;
-    uint8_t* rgba;
 };
 
-// Stage <- tile at (ox, oy) of the four images, zero outside the image.
-template <int kWarps>
-__device__ __forceinline__ void fma_plain_load(float* stage, const FmaPlain& p, int ox, int oy)
+// Stage <- tile (c, ox, oy) of the four planes, zero outside the image.
+__device__ __forceinline__ void pl_plain_load(float* stage, const PlPlain& p, int c, int ox, int oy)
 {
-    using G = FmaTile<kWarps>;
-    const float* src[4] = {p.O, p.U, p.W, p.C};
-    for (int i = threadIdx.x; i < G::kRows * 3 * kTbEX; i += G::kThreads) {
-        const int row = i / (3 * kTbEX), col = i - row * (3 * kTbEX);
-        const int gy = oy + row, gx = ox + col / 3;
+    const float* src[4] = {p.O, p.U, p.K, p.C};
+    const int64_t base = static_cast<int64_t>(c) * p.w * p.h;
+    for (int i = threadIdx.x; i < kPlStage; i += kPlThreads) {
+        const int row = i / kPlW, col = i - row * kPlW;
+        const int gy = oy + row, gx = ox + col;
         const bool in = gx >= 0 && gx < p.w && gy >= 0 && gy < p.h;
-        const int64_t idx = in ? pix_index(gx, gy, p.w) * 3 + col % 3 : 0;
+        const int64_t idx = in ? base + pix_index(gx, gy, p.w) : 0;
 #pragma unroll
         for (int a = 0; a < 4; ++a)
-            stage[a * G::kStageFloats + i] = in ? src[a][idx] : 0.0f;
+            stage[a * kPlStage + i] = in ? src[a][idx] : 0.0f;
     }
 }
 
-// The body of both FMA kernels: kTma = true walks the tiles of a SolverGroup
-// (TMA loads one tile ahead, TMA stores), false the tiles of one FmaPlain
-// image (plain loads and stores).
-template <int kN, int kWarps, bool kTma>
-__device__ __forceinline__ void fma_body(const SolverGroup<kN>& g, const FmaPlain& pl, int T, int k0, float step,
+// The body of both planar kernels: kTma = true walks the tiles of a
+// SolverGroup (TMA loads one tile ahead, TMA stores), false the tiles of one
+// PlPlain image (plain loads and stores).
+template <int kN, bool kTma>
+__device__ __forceinline__ void pl_body(const SolverGroup<kN>& g, const PlPlain& pl, int T, int k0, float step,
     float mom)
 {
-    using G = FmaTile<kWarps>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* stage = reinterpret_cast<float*>(smem_raw);
-    float* obuf = stage + 4 * G::kStageFloats;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(obuf + G::kObuf);
+    float* slots = stage + 4 * kPlStage;
+    float* so = slots + 2 * kPlSlotPlane;
+    float* su = so + kPlOut;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(su + kPlOut);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int px0 = 2 * lane, py0 = 4 * warp;
+    const int px0 = 4 * lane, py0 = kPlRPT * warp;
 
-    for (int i = threadIdx.x; i < G::kObuf; i += G::kThreads)
-        obuf[i] = 0.0f;  // the apron slots start at zero
+    for (int i = threadIdx.x; i < 2 * kPlSlotPlane; i += kPlThreads)
+        slots[i] = 0.0f;  // the apron slots stay zero
     if (kTma && threadIdx.x == 0)
         mbar_init(bar, 1);
     __syncthreads();
     const int ntiles = kTma ? g.tile0[g.count] : pl.ntiles;
     int tile = blockIdx.x;
-    if (kTma && threadIdx.x == 0 && tile < ntiles) {
-        const TileLoc n = locate<kN, G::kIRows>(g, tile);
-        fma_issue_first(stage, g.map[n.p], n.ox, n.oy, G::kStageFloats, G::kStageBytes, bar, k0 > 0);
-    }
+    if (kTma && threadIdx.x == 0 && tile < ntiles)
+        pl_issue_first(stage, g.map[pl_locate<kN>(g, tile).p], pl_locate<kN>(g, tile), bar, k0 > 0);
     grid_dependency_wait();
     uint32_t parity = 0;
     for (; tile < ntiles; tile += gridDim.x) {
         if (tile + static_cast<int>(gridDim.x) >= ntiles)
             allow_dependent_launch();
-        int ox, oy, w, h, p = 0;
+        PlTile t;
         if (kTma) {
-            const TileLoc c = locate<kN, G::kIRows>(g, tile);
-            ox = c.ox;
-            oy = c.oy;
-            w = c.w;
-            h = c.h;
-            p = c.p;
+            t = pl_locate<kN>(g, tile);
             if (!mbar_wait_bounded(bar, parity, kWaitSpins)) {
                 // the outputs are invalid and vsc_check_device reports VSC_ETIMEOUT
                 if (threadIdx.x == 0) {
@@ -1126,139 +1215,101 @@ __device__ __forceinline__ void fma_body(const SolverGroup<kN>& g, const FmaPlai
             }
             parity ^= 1;
         } else {
-            ox = (tile % pl.tiles_x) * kIW - kTbT;
-            oy = (tile / pl.tiles_x) * G::kIRows - kTbT;
-            w = pl.w;
-            h = pl.h;
-            __syncthreads();  // the previous tile's interior has left the staging
-            fma_plain_load<kWarps>(stage, pl, ox, oy);
+            const int per_plane = pl.ntiles / 3;
+            t.p = 0;
+            t.c = tile / per_plane;
+            const int r = tile - t.c * per_plane;
+            t.ox = (r % pl.tiles_x) * kPlIW - kTbT;
+            t.oy = (r / pl.tiles_x) * kPlIRows - kTbT;
+            t.w = pl.w;
+            t.h = pl.h;
+            pl_plain_load(stage, pl, t.c, t.ox, t.oy);
             __syncthreads();
         }
-        const int gx0 = ox + px0, gy0 = oy + py0;
-        const bool interior = ox >= 1 && oy >= 1 && ox + kTbEX - 1 <= w - 3 && oy + G::kRows - 1 <= h - 3;
+        const int w = t.w, h = t.h;
+        const int gx0 = t.ox + px0, gy0 = t.oy + py0;
+        const bool interior = t.ox >= 1 && t.oy >= 1 && t.ox + kPlW - 1 <= w - 3 && t.oy + kPlRows - 1 <= h - 3;
 
-        FmaState s;
+        PlState s;
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            // six consecutive floats: both pixels' RGB (zero outside the image)
-            const float* row = stage + (py0 + r) * (3 * kTbEX) + 3 * px0;
-            float2 v[4][3];
-#pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                const float2 x01 = *reinterpret_cast<const float2*>(row + a * G::kStageFloats);
-                const float2 x23 = *reinterpret_cast<const float2*>(row + a * G::kStageFloats + 2);
-                const float2 x45 = *reinterpret_cast<const float2*>(row + a * G::kStageFloats + 4);
-                v[a][0] = make_float2(x01.x, x23.y);
-                v[a][1] = make_float2(x01.y, x45.x);
-                v[a][2] = make_float2(x23.x, x45.y);
-            }
-            float c0 = 4.0f, c1 = 4.0f;
-            if (!interior) {
-                c0 = nb_of(gx0, gy0 + r, w, h).cnt;
-                c1 = nb_of(gx0 + 1, gy0 + r, w, h).cnt;
-            }
-#pragma unroll
-            for (int ch = 0; ch < 3; ++ch) {
-                s.o[r][ch] = v[0][ch];
-                s.u[r][ch] = v[1][ch];
-                s.c[r][ch] = v[3][ch];
-                s.nk[r][ch] = make_float2(-__fmul_rn(step, __fadd_rn(c0, v[2][ch].x)),
-                    -__fmul_rn(step, __fadd_rn(c1, v[2][ch].y)));
-            }
+        for (int r = 0; r < kPlRPT; ++r) {
+            const float* row = stage + (py0 + r) * kPlW + px0;
+            s.o[r] = *reinterpret_cast<const float4*>(row);
+            s.u[r] = *reinterpret_cast<const float4*>(row + kPlStage);
+            s.nk[r] = *reinterpret_cast<const float4*>(row + 2 * kPlStage);
+            s.c[r] = *reinterpret_cast<const float4*>(row + 3 * kPlStage);
         }
         if (kTma && threadIdx.x == 0)
-            bulk_wait_read();  // the previous tile's TMA stores have read the staging
-        __syncthreads();
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) {
-            float* D = obuf + ch * G::kPlane + ((warp + 1) * 2) * kTbPX + px0 + 2;  // buffer 0
-            *reinterpret_cast<float2*>(D) = s.o[0][ch];
-            *reinterpret_cast<float2*>(D + kTbPX) = s.o[3][ch];
+            bulk_wait_read();  // the previous tile's TMA stores have read the out staging
+        __syncthreads();       // staging consumed
+        {
+            float* D = slots + ((warp + 1) * 2) * kPlPX + px0 + 4;  // buffer 0
+            *reinterpret_cast<float4*>(D) = s.o[0];
+            *reinterpret_cast<float4*>(D + kPlPX) = s.o[kPlRPT - 1];
         }
-        __syncthreads();  // staging consumed, edge rows published
         if (kTma && threadIdx.x == 0 && tile + static_cast<int>(gridDim.x) < ntiles) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            const TileLoc n = locate<kN, G::kIRows>(g, tile + gridDim.x);
-            mbar_expect_tx(bar, 4 * G::kStageBytes);
-            fma_issue(stage, g.map[n.p], n.ox, n.oy, G::kStageFloats, 0, 4, bar);
+            const PlTile n = pl_locate<kN>(g, tile + gridDim.x);
+            mbar_expect_tx(bar, 4 * kPlStageBytes);
+            pl_issue(stage, g.map[n.p], n, 0, 4, bar);
         }
+        __syncthreads();  // edge rows published
 
         if (interior)
-            fma_iterate<true, kWarps>(s, obuf, T, k0, step, mom, px0, warp, gx0, gy0, w, h);
+            pl_iterate<true>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h);
         else
-            fma_iterate<false, kWarps>(s, obuf, T, k0, step, mom, px0, warp, gx0, gy0, w, h);
+            pl_iterate<false>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h);
 
-        // interior out through the (now idle) edge-row slots; a thread's two
-        // pixels of a row are six consecutive floats, both inside or neither.
-        // (The staging overwrites the zero aprons: they then feed only the
-        // outermost ring, whose rows are never written back.)
-        float* so = obuf;
-        float* su = obuf + G::kIRows * 3 * kIW;
+        // interior out: a thread's four columns are all inside or all outside
         {
             const int ix = px0 - kTbT;
 #pragma unroll
-            for (int r = 0; r < 4; ++r) {
+            for (int r = 0; r < kPlRPT; ++r) {
                 const int iy = py0 + r - kTbT;
-                if (ix < 0 || ix >= kIW || iy < 0 || iy >= G::kIRows)
+                if (ix < 0 || ix >= kPlIW || iy < 0 || iy >= kPlIRows)
                     continue;
-                float2* o2 = reinterpret_cast<float2*>(so + iy * 3 * kIW + 3 * ix);
-                float2* u2 = reinterpret_cast<float2*>(su + iy * 3 * kIW + 3 * ix);
-                o2[0] = make_float2(s.o[r][0].x, s.o[r][1].x);
-                o2[1] = make_float2(s.o[r][2].x, s.o[r][0].y);
-                o2[2] = make_float2(s.o[r][1].y, s.o[r][2].y);
-                u2[0] = make_float2(s.u[r][0].x, s.u[r][1].x);
-                u2[1] = make_float2(s.u[r][2].x, s.u[r][0].y);
-                u2[2] = make_float2(s.u[r][1].y, s.u[r][2].y);
+                *reinterpret_cast<float4*>(so + iy * kPlIW + ix) = s.o[r];
+                *reinterpret_cast<float4*>(su + iy * kPlIW + ix) = s.u[r];
             }
         }
         if (kTma) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncthreads();
-            if (threadIdx.x == 0)
-                store_interior(g.map[p] + kMapOo, g.map[p] + kMapUo, ox, oy, so, su);
+            if (threadIdx.x == 0) {
+                tma_store_3d(g.map[t.p] + kMapOo, t.ox + kTbT, t.oy + kTbT, t.c, so);
+                tma_store_3d(g.map[t.p] + kMapUo, t.ox + kTbT, t.oy + kTbT, t.c, su);
+                bulk_commit();
+            }
         } else {
             __syncthreads();
-            for (int i = threadIdx.x; i < G::kIRows * 3 * kIW; i += G::kThreads) {
-                const int iy = i / (3 * kIW), col = i - iy * (3 * kIW);
-                const int gy = oy + kTbT + iy, gx = ox + kTbT + col / 3;
+            const int64_t base = static_cast<int64_t>(t.c) * w * h;
+            for (int i = threadIdx.x; i < kPlOut; i += kPlThreads) {
+                const int iy = i / kPlIW, ix = i - iy * kPlIW;
+                const int gy = t.oy + kTbT + iy, gx = t.ox + kTbT + ix;
                 if (gx < w && gy < h) {
-                    const int64_t idx = pix_index(gx, gy, w) * 3 + col % 3;
+                    const int64_t idx = base + pix_index(gx, gy, w);
                     pl.Oo[idx] = so[i];
                     pl.Uo[idx] = su[i];
                 }
             }
-        }
-        if (uint8_t* rgba = kTma ? g.rgba[p] : pl.rgba) {
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const int r = q >> 1, c = q & 1;
-                const int px = px0 + c, py = py0 + r;
-                const int gx = ox + px, gy = oy + py;
-                if (gx < 0 || gx >= w || gy < 0 || gy >= h || px < kTbT || px >= kTbEX - kTbT || py < kTbT ||
-                    py >= G::kRows - kTbT)
-                    continue;
-                reinterpret_cast<uint32_t*>(rgba)[pix_index(gx, gy, w)] = c == 0
-                    ? pack_rgba(s.o[r][0].x, s.o[r][1].x, s.o[r][2].x)
-                    : pack_rgba(s.o[r][0].y, s.o[r][1].y, s.o[r][2].y);
-            }
+            __syncthreads();  // the staging is free for the next tile's loads
         }
     }
     if (kTma && threadIdx.x == 0)
         bulk_wait_all();
 }
 
-template <int kN, int kWarps>
-__global__ void __launch_bounds__(32 * kWarps, 1)
+template <int kN>
+__global__ void __launch_bounds__(kPlThreads, 1)
     solver_fma_kernel(const __grid_constant__ SolverGroup<kN> g, int T, int k0, float step, float mom)
 {
-    fma_body<kN, kWarps, true>(g, FmaPlain{}, T, k0, step, mom);
+    pl_body<kN, true>(g, PlPlain{}, T, k0, step, mom);
 }
 
-template <int kWarps>
-__global__ void __launch_bounds__(32 * kWarps, 1)
-    solver_fma_plain_kernel(const __grid_constant__ FmaPlain pl, int T, int k0, float step, float mom)
+__global__ void __launch_bounds__(kPlThreads, 1)
+    solver_fma_plain_kernel(const __grid_constant__ PlPlain pl, int T, int k0, float step, float mom)
 {
-    fma_body<1, kWarps, false>(SolverGroup<1>{}, pl, T, k0, step, mom);
+    pl_body<1, false>(SolverGroup<1>{}, pl, T, k0, step, mom);
 }
 
 // An mbarrier nobody arrives on, waited for with a bounded spin: exercises
@@ -1313,7 +1364,7 @@ bool set_group_smem()
     constexpr auto kAttr = cudaFuncAttributeMaxDynamicSharedMemorySize;
     return cudaFuncSetAttribute(solver_persistent_kernel<kN>, kAttr, kPsSmem) == cudaSuccess &&
            cudaFuncSetAttribute(solver_tall_kernel<kN>, kAttr, kPSmem) == cudaSuccess &&
-           cudaFuncSetAttribute(solver_fma_kernel<kN, kFmaWarps>, kAttr, FmaTile<kFmaWarps>::kSmem) == cudaSuccess;
+           cudaFuncSetAttribute(solver_fma_kernel<kN>, kAttr, kPlSmem) == cudaSuccess;
 }
 
 struct DeviceInfo {
@@ -1343,8 +1394,8 @@ cudaError_t device_info(DeviceInfo** out)
             cudaSuccess)
             return e;
         d.ps_smem = set_group_smem<1>() && set_group_smem<4>() && set_group_smem<kGroupMax>() &&
-                    cudaFuncSetAttribute(solver_fma_plain_kernel<kFmaWarps>,
-                        cudaFuncAttributeMaxDynamicSharedMemorySize, FmaTile<kFmaWarps>::kSmem) == cudaSuccess;
+                    cudaFuncSetAttribute(solver_fma_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                        kPlSmem) == cudaSuccess;
         cudaGetLastError();
     }
     *out = &d;
@@ -1361,7 +1412,7 @@ bool aligned16p(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) ==
 // per stream of a multi-stream step) and keeps the faster per (device, form,
 // sizes); sizes never tuned use a wave model: a 64 x 48 tile costs about 1.91
 // times a 64 x 32 one (GB300, 1920x1080 and 960x540).  The FMA form has one
-// shape, 64 x 48.
+// shape, 128 x 72 pixels of one channel plane.
 struct ShapeTable {
     std::mutex mu;
     std::map<std::vector<int>, int> rows;  // {device, form, w0, h0, w1, h1, ...} -> tile rows
@@ -1385,12 +1436,10 @@ std::vector<int> shape_key(int dev, const int* w, const int* h, int n, int form)
 
 int tiles_of(int w, int h, int ir) { return ((w + kIW - 1) / kIW) * ((h + ir - 1) / ir); }
 
-constexpr int kFmaRows = FmaTile<kFmaWarps>::kRows;  // 48
-
 int model_rows(const int* w, const int* h, int n, int sms, int form)
 {
     if (form == kSolverFma)
-        return kFmaRows;
+        return kPlRows;
     int64_t n_short = 0, n_tall = 0;
     for (int i = 0; i < n; ++i) {
         n_short += tiles_of(w[i], h[i], kIH);
@@ -1431,10 +1480,42 @@ bool encode_solve(SolveMaps* m, float* const O[2], float* const U[2], const floa
     return ok;
 }
 
+// 3D map over the three w x h planes of a planar image (x, y, channel).
+bool encode_plane_map(CUtensorMap* m, const float* base, int w, int h, int box_w, int box_h)
+{
+    EncodeTiledFn fn = encode_fn();
+    if (!fn)
+        return false;
+    const cuuint64_t dims[3] = {static_cast<cuuint64_t>(w), static_cast<cuuint64_t>(h), 3};
+    const cuuint64_t strides[2] = {static_cast<cuuint64_t>(w) * sizeof(float),
+        static_cast<cuuint64_t>(w) * h * sizeof(float)};
+    const cuuint32_t box[3] = {static_cast<cuuint32_t>(box_w), static_cast<cuuint32_t>(box_h), 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The FMA form's maps over its planes: O[c] / U[c] / nK (in the W slot) / Cs
+// (in the L slot) with the tile box, Oo[c] / Uo[c] with the interior box.
+bool encode_solve_planar(SolveMaps* m, float* const O[2], float* const U[2], const float* nK, const float* Cs,
+    int w, int h)
+{
+    bool ok = encode_plane_map(&m->W, nK, w, h, kPlW, kPlRows) && encode_plane_map(&m->L, Cs, w, h, kPlW, kPlRows);
+    m->A = m->W;  // unused by the FMA kernel
+    for (int c = 0; c < 2 && ok; ++c)
+        ok = encode_plane_map(&m->O[c], O[c], w, h, kPlW, kPlRows) &&
+             encode_plane_map(&m->U[c], U[c], w, h, kPlW, kPlRows) &&
+             encode_plane_map(&m->Oo[c], O[c], w, h, kPlIW, kPlIRows) &&
+             encode_plane_map(&m->Uo[c], U[c], w, h, kPlIW, kPlIRows);
+    return ok;
+}
+
 // problem p of a launch: launch li of the solve reads O[c] and U[li & 1] and
 // writes O[c ^ 1] and U[(li + 1) & 1]
 template <int kN>
-void group_set(SolverGroup<kN>& g, int p, const SolveMaps& m, int c, int li, int w, int h, int rows, uint8_t* rgba)
+void group_set(SolverGroup<kN>& g, int p, const SolveMaps& m, int c, int li, int w, int h, int rows, uint8_t* rgba,
+    int form)
 {
     g.map[p][kMapO] = m.O[c];
     g.map[p][kMapU] = m.U[li & 1];
@@ -1445,11 +1526,12 @@ void group_set(SolverGroup<kN>& g, int p, const SolveMaps& m, int c, int li, int
     g.map[p][kMapUo] = m.Uo[(li + 1) & 1];
     g.w[p] = w;
     g.h[p] = h;
-    g.tiles_x[p] = (w + kIW - 1) / kIW;
-    g.rgba[p] = rgba;
+    const bool planar = form == kSolverFma;
+    g.tiles_x[p] = planar ? pl_tiles_x(w) : (w + kIW - 1) / kIW;
+    g.rgba[p] = planar ? nullptr : rgba;  // the planar form writes RGBA8 when it leaves the planes
     if (p == 0)
         g.tile0[0] = 0;
-    g.tile0[p + 1] = g.tile0[p] + tiles_of(w, h, interior_rows(rows));
+    g.tile0[p + 1] = g.tile0[p] + (planar ? pl_tiles(w, h) : tiles_of(w, h, interior_rows(rows)));
     g.count = p + 1;
 }
 
@@ -1469,9 +1551,9 @@ cudaError_t launch_group(int form, int rows, const SolverGroup<kN>& g, int T, in
     cfg.numAttrs = 1;
     cfg.gridDim = dim3(std::min(g.tile0[g.count], sms));
     if (form == kSolverFma) {
-        cfg.blockDim = dim3(FmaTile<kFmaWarps>::kThreads);
-        cfg.dynamicSmemBytes = FmaTile<kFmaWarps>::kSmem;
-        return cudaLaunchKernelEx(&cfg, solver_fma_kernel<kN, kFmaWarps>, g, T, k0, step, mom);
+        cfg.blockDim = dim3(kPlThreads);
+        cfg.dynamicSmemBytes = kPlSmem;
+        return cudaLaunchKernelEx(&cfg, solver_fma_kernel<kN>, g, T, k0, step, mom);
     }
     if (rows == kPEY) {
         cfg.blockDim = dim3(kPThreads);
@@ -1506,7 +1588,8 @@ cudaError_t launch_members(int form, const std::vector<GroupMember>& mem, int ro
             const int cnt = static_cast<int>(std::min(mem.size() - b, static_cast<size_t>(kN)));
             for (int p = 0; p < cnt; ++p) {
                 const GroupMember& m = mem[b + p];
-                group_set(g, p, m.maps, m.c0 ^ (li & 1), li, m.w, m.h, rows, li == nlaunch - 1 ? m.rgba : nullptr);
+                group_set(g, p, m.maps, m.c0 ^ (li & 1), li, m.w, m.h, rows, li == nlaunch - 1 ? m.rgba : nullptr,
+                    form);
             }
             e = launch_group(form, rows, g, T, k0, step, mom, sms, st);
             ++*nl;
@@ -1648,7 +1731,10 @@ cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out, int fo
     return solver_group_autotune(&w, &h, 1, st, rows_out, form);
 }
 
-size_t solver_workspace_floats(int w, int h) { return static_cast<size_t>(w) * h * 3 * 4; }
+size_t solver_workspace_floats(int w, int h, int form)
+{
+    return static_cast<size_t>(w) * h * 3 * (form == kSolverFma ? 6 : 4);
+}
 
 int solver_steps_per_launch() { return kTbT; }
 
@@ -1667,10 +1753,92 @@ WsView ws_view(float* ws, int w, int h)
     return WsView{ws, ws + n, ws + 2 * n, ws + 3 * n};
 }
 
+// The FMA form's workspace: six planar images (three w x h planes each).
+struct PlWs {
+    float *C, *K, *U[2], *O[2];
+};
+PlWs pl_view(float* ws, int w, int h)
+{
+    const size_t n = static_cast<size_t>(w) * h * 3;
+    return PlWs{ws, ws + n, {ws + 2 * n, ws + 3 * n}, {ws + 4 * n, ws + 5 * n}};
+}
+
 bool tma_eligible(const DeviceInfo* di, int w, const float* O, const WsView& v, const float* A, const float* Wt)
 {
     return di->ps_smem && (w % 4) == 0 && aligned16p(O) && aligned16p(v.O2) && aligned16p(v.U0) &&
            aligned16p(v.U1) && aligned16p(A) && aligned16p(Wt) && aligned16p(v.L);
+}
+
+// planes of a width that is a multiple of 4 in a 16-byte aligned workspace
+// (each plane then starts on the 16-byte grid)
+bool pl_tma_eligible(const DeviceInfo* di, int w, const float* ws) { return di->ps_smem && (w % 4) == 0 && aligned16p(ws); }
+
+struct PlanarCopy {
+    const float* src;
+    float* dst;
+    uint8_t* rgba;
+    int64_t npix;
+};
+
+// Interleaved <-> planar copies of n images, kPlanarGroupMax per launch.
+cudaError_t launch_planar(const PlanarCopy* c, int n, int to_planar, cudaStream_t st, int* nl)
+{
+    for (int b0 = 0; b0 < n; b0 += kPlanarGroupMax) {
+        PlanarGroup g{};
+        g.count = std::min(n - b0, kPlanarGroupMax);
+        g.block0[0] = 0;
+        for (int p = 0; p < g.count; ++p) {
+            g.src[p] = c[b0 + p].src;
+            g.dst[p] = c[b0 + p].dst;
+            g.rgba[p] = c[b0 + p].rgba;
+            g.npix[p] = c[b0 + p].npix;
+            g.block0[p + 1] = g.block0[p] + static_cast<int>((c[b0 + p].npix + 255) / 256);
+        }
+        const cudaError_t e = launch_pdl(planar_group_kernel, dim3(g.block0[g.count]), dim3(256), 0, st, g, to_planar);
+        if (e != cudaSuccess)
+            return e;
+        ++*nl;
+    }
+    return cudaGetLastError();
+}
+
+// The FMA form of run_solver: constants and O's planes, the launches, O (and
+// the RGBA8 copy) back from its planes.
+cudaError_t run_solver_fma(const DeviceInfo* di, const float* P, const float* A, const float* Wt, float* O, int w,
+    int h, int num_iter, float step, float mom, float* workspace, cudaStream_t st, int* nl, uint8_t* rgba_out)
+{
+    const PlWs v = pl_view(workspace, w, h);
+    const dim3 b(32, 8);
+    cudaError_t e = launch_pdl(solver_prep_fma_kernel, grid2d(w, h, b), b, 0, st, P, A, Wt,
+        static_cast<const float*>(O), v.C, v.K, v.O[0], w, h, step);
+    ++*nl;
+    const int nlaunch = solve_launches(num_iter);
+    if (e == cudaSuccess && pl_tma_eligible(di, w, workspace)) {
+        GroupMember m{};
+        if (!encode_solve_planar(&m.maps, v.O, v.U, v.K, v.C, w, h))
+            return cudaErrorInvalidValue;
+        m.w = w;
+        m.h = h;
+        const std::vector<GroupMember> one(1, m);
+        e = launch_members<1>(kSolverFma, one, kPlRows, num_iter, step, mom, di->sms, st, nl);
+    } else {
+        // plain loads and stores (widths not a multiple of 4, an unaligned workspace)
+        const int tx = pl_tiles_x(w), nt = pl_tiles(w, h);
+        int k0 = 0;
+        for (int li = 0; li < nlaunch && e == cudaSuccess; ++li) {
+            const int T = std::min(kTbT, num_iter - k0);
+            const PlPlain pl{v.O[li & 1], v.U[li & 1], v.K, v.C, v.O[(li + 1) & 1], v.U[(li + 1) & 1], w, h, tx, nt};
+            e = launch_pdl(solver_fma_plain_kernel, dim3(std::min(nt, di->sms)), dim3(kPlThreads), kPlSmem, st, pl, T,
+                k0, step, mom);
+            ++*nl;
+            k0 += T;
+        }
+    }
+    if (e == cudaSuccess) {
+        const PlanarCopy back{v.O[nlaunch & 1], O, rgba_out, static_cast<int64_t>(w) * h};
+        e = launch_planar(&back, 1, 0, st, nl);
+    }
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 }  // namespace
@@ -1681,8 +1849,10 @@ bool solver_tma_supported()
     return device_info(&di) == cudaSuccess && di->ps_smem;
 }
 
-float* solver_start_buffer(float* O, int w, int h, int num_iter, float* workspace)
+float* solver_start_buffer(float* O, int w, int h, int num_iter, float* workspace, int form)
 {
+    if (form == kSolverFma)
+        return O;  // the solve copies O into its planes first
     return solve_launches(num_iter) % 2 == 0 ? O : ws_view(workspace, w, h).O2;
 }
 
@@ -1700,22 +1870,28 @@ cudaError_t solver_prep(int form, const float* P, const float* A, const float* W
 {
     if (form != kSolverFma)
         return solver_lap(P, w, h, workspace, st);
+    const PlWs v = pl_view(workspace, w, h);
     const dim3 b(32, 8);
-    const cudaError_t e =
-        launch_pdl(solver_prep_fma_kernel, grid2d(w, h, b), b, 0, st, P, A, Wt, workspace, w, h, step);
+    const cudaError_t e = launch_pdl(solver_prep_fma_kernel, grid2d(w, h, b), b, 0, st, P, A, Wt,
+        static_cast<const float*>(nullptr), v.C, v.K, static_cast<float*>(nullptr), w, h, step);
     if (e != cudaSuccess)
         return e;
     return cudaGetLastError();
 }
 
-bool solver_group_eligible(const SolverImage* im, int n)
+bool solver_group_eligible(const SolverImage* im, int n, int form)
 {
     DeviceInfo* di = nullptr;
     if (n < 1 || device_info(&di) != cudaSuccess)
         return false;
-    for (int i = 0; i < n; ++i)
-        if (!tma_eligible(di, im[i].w, im[i].O, ws_view(im[i].workspace, im[i].w, im[i].h), im[i].A, im[i].Wt))
+    for (int i = 0; i < n; ++i) {
+        const bool ok = form == kSolverFma
+                            ? pl_tma_eligible(di, im[i].w, im[i].workspace)
+                            : tma_eligible(di, im[i].w, im[i].O, ws_view(im[i].workspace, im[i].w, im[i].h), im[i].A,
+                                  im[i].Wt);
+        if (!ok)
             return false;
+    }
     return true;
 }
 
@@ -1726,7 +1902,7 @@ cudaError_t run_solver_group(const SolverImage* im, int n, int num_iter, float s
     cudaError_t e = device_info(&di);
     if (e != cudaSuccess)
         return e;
-    if (!solver_group_eligible(im, n))
+    if (!solver_group_eligible(im, n, form))
         return cudaErrorInvalidValue;
     int nl = 0;
     if (num_iter <= 0) {
@@ -1750,19 +1926,35 @@ cudaError_t run_solver_group(const SolverImage* im, int n, int num_iter, float s
     const int rows = chosen_rows(dev, ws.data(), hs.data(), n, di->sms, form);
     const bool odd = solve_launches(num_iter) % 2 == 1;
     std::vector<GroupMember> mem(n);
+    std::vector<PlanarCopy> to(n), back(n);
     for (int i = 0; i < n; ++i) {
-        const WsView v = ws_view(im[i].workspace, im[i].w, im[i].h);
-        float* const O[2] = {im[i].O, v.O2};
-        float* const U[2] = {v.U0, v.U1};
-        if (!encode_solve(&mem[i].maps, O, U, im[i].A, im[i].Wt, v.L, im[i].w, im[i].h, rows))
-            return cudaErrorInvalidValue;
+        if (form == kSolverFma) {
+            const PlWs v = pl_view(im[i].workspace, im[i].w, im[i].h);
+            if (!encode_solve_planar(&mem[i].maps, v.O, v.U, v.K, v.C, im[i].w, im[i].h))
+                return cudaErrorInvalidValue;
+            const int64_t np = static_cast<int64_t>(im[i].w) * im[i].h;
+            to[i] = PlanarCopy{im[i].O, v.O[0], nullptr, np};
+            back[i] = PlanarCopy{v.O[solve_launches(num_iter) & 1], im[i].O, im[i].rgba, np};
+            mem[i].c0 = 0;
+        } else {
+            const WsView v = ws_view(im[i].workspace, im[i].w, im[i].h);
+            float* const O[2] = {im[i].O, v.O2};
+            float* const U[2] = {v.U0, v.U1};
+            if (!encode_solve(&mem[i].maps, O, U, im[i].A, im[i].Wt, v.L, im[i].w, im[i].h, rows))
+                return cudaErrorInvalidValue;
+            mem[i].c0 = odd ? 1 : 0;
+            mem[i].rgba = im[i].rgba;
+        }
         mem[i].w = im[i].w;
         mem[i].h = im[i].h;
-        mem[i].c0 = odd ? 1 : 0;
-        mem[i].rgba = im[i].rgba;
     }
-    e = n <= 4 ? launch_members<4>(form, mem, rows, num_iter, step, mom, di->sms, st, &nl)
-               : launch_members<kGroupMax>(form, mem, rows, num_iter, step, mom, di->sms, st, &nl);
+    if (form == kSolverFma)
+        e = launch_planar(to.data(), n, 1, st, &nl);
+    if (e == cudaSuccess)
+        e = n <= 4 ? launch_members<4>(form, mem, rows, num_iter, step, mom, di->sms, st, &nl)
+                   : launch_members<kGroupMax>(form, mem, rows, num_iter, step, mom, di->sms, st, &nl);
+    if (e == cudaSuccess && form == kSolverFma)
+        e = launch_planar(back.data(), n, 0, st, &nl);
     if (launches)
         *launches += nl;
     if (e == cudaSuccess)
@@ -1789,15 +1981,21 @@ cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O
     cudaError_t e0 = device_info(&di);
     if (e0 != cudaSuccess)
         return e0;
-    if (form == kSolverFma && !di->ps_smem)
-        return cudaErrorNotSupported;
-    if ((e0 = solver_prep(form, P, A, Wt, w, h, step, v.L, st)) != cudaSuccess)
+    if (form == kSolverFma) {
+        if (!di->ps_smem)
+            return cudaErrorNotSupported;
+        const cudaError_t e = run_solver_fma(di, P, A, Wt, O, w, h, num_iter, step, mom, workspace, st, &nl, rgba_out);
+        if (launches)
+            *launches += nl;
+        return e;
+    }
+    if ((e0 = solver_lap(P, w, h, v.L, st)) != cudaSuccess)
         return e0;
     ++nl;
     // Launches of up to kTbT iterations; ping-pong O between O and O2 and U
     // between its two buffers so that the last launch writes O.
     const int nlaunch = solve_launches(num_iter);
-    float* cur = solver_start_buffer(O, w, h, num_iter, workspace);
+    float* cur = solver_start_buffer(O, w, h, num_iter, workspace, kSolverExact);
     if (cur != O) {
         cudaError_t e = cudaMemcpyAsync(v.O2, O, n * sizeof(float), cudaMemcpyDeviceToDevice, st);
         if (e != cudaSuccess)
@@ -1808,7 +2006,7 @@ cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O
     int dev = 0;
     if ((e0 = cudaGetDevice(&dev)) != cudaSuccess)
         return e0;
-    const int rows = chosen_rows(dev, &w, &h, 1, di->sms, form);
+    const int rows = chosen_rows(dev, &w, &h, 1, di->sms, kSolverExact);
     GroupMember m{};
     bool tma = tma_eligible(di, w, O, v, A, Wt);
     if (tma) {
@@ -1822,33 +2020,13 @@ cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O
         m.c0 = cur == O ? 0 : 1;
         m.rgba = rgba_out;
         const std::vector<GroupMember> one(1, m);
-        cudaError_t e = launch_members<1>(form, one, rows, num_iter, step, mom, di->sms, st, &nl);
+        cudaError_t e = launch_members<1>(kSolverExact, one, rows, num_iter, step, mom, di->sms, st, &nl);
         if (launches)
             *launches += nl;
         return e != cudaSuccess ? e : cudaGetLastError();
     }
     float* U[2] = {v.U0, v.U1};
     int k0 = 0;
-    if (form == kSolverFma) {
-        // plain loads and stores (widths not a multiple of 4, unaligned images)
-        const int ir = interior_rows(kFmaRows);
-        const int tx = (w + kIW - 1) / kIW, nt = tx * ((h + ir - 1) / ir);
-        cudaError_t e = cudaSuccess;
-        for (int li = 0; li < nlaunch && e == cudaSuccess; ++li) {
-            const int T = std::min(kTbT, num_iter - k0);
-            float* nxt = (cur == O) ? v.O2 : O;
-            const FmaPlain pl{cur, U[li & 1], Wt, v.L, nxt, U[(li + 1) & 1], w, h, tx, nt,
-                li == nlaunch - 1 ? rgba_out : nullptr};
-            e = launch_pdl(solver_fma_plain_kernel<kFmaWarps>, dim3(std::min(nt, di->sms)),
-                dim3(FmaTile<kFmaWarps>::kThreads), FmaTile<kFmaWarps>::kSmem, st, pl, T, k0, step, mom);
-            ++nl;
-            k0 += T;
-            cur = nxt;
-        }
-        if (launches)
-            *launches += nl;
-        return e != cudaSuccess ? e : cudaGetLastError();
-    }
     for (int li = 0; li < nlaunch; ++li) {
         const int T = std::min(kTbT, num_iter - k0);
         float* nxt = (cur == O) ? v.O2 : O;
