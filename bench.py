@@ -1106,12 +1106,12 @@ SOLVER_KERNELS = {"exact": ("solver_tall_kernel", 84), "fma": ("solver_fma_kerne
 # dram__bytes_read.sum + dram__bytes_write.sum of one 8-step launch at
 # 1920x1080 from the ncu captures summarised in profiles/ (the mean of the
 # captured launches), and where each comes from.
-SOLVER_TRAFFIC_BYTES = {"solver_tall_kernel": 144_198_912, "solver_fma_kernel": 120_321_152}
+SOLVER_TRAFFIC_BYTES = {"solver_tall_kernel": 144_198_912, "solver_fma_kernel": 116_517_248}
 SOLVER_TRAFFIC_SOURCE = {
     "solver_tall_kernel": "profiles/solver_tall_1080p.md (mean of two launches: 124,613,888 + 21,037,568 and "
                           "124,601,600 + 18,144,768 bytes)",
-    "solver_fma_kernel": "profiles/solver_fma_1080p.md (mean of two launches: 101,465,856 + 19,138,816 and "
-                         "100,983,296 + 19,054,336 bytes)",
+    "solver_fma_kernel": "profiles/solver_fma_1080p.md (planar kernel; mean of two launches: 99,942,400 + "
+                         "16,809,472 and 99,815,424 + 16,467,200 bytes)",
 }
 # What bounds each solver kernel, from the same captures: the FP32 pipe and
 # its latency, not HBM (the time steps stay on chip): the FMA pipe's active
@@ -1119,7 +1119,7 @@ SOLVER_TRAFFIC_SOURCE = {
 # sm__cycles_active) and smsp__issue_active.
 SOLVER_PIPE = {
     "solver_tall_kernel": {"fma_pipe_active": None, "issue_active": 0.585},
-    "solver_fma_kernel": {"fma_pipe_active": 0.527, "issue_active": 0.458},
+    "solver_fma_kernel": {"fma_pipe_active": 0.487, "issue_active": 0.396},
 }
 
 
