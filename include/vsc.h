@@ -305,8 +305,9 @@ VSC_API vsc_status vsc_get_consist_out_fma(const vsc_image* crnt_pr, const vsc_i
  * it needs to start at zero), so calls that overlap on the GPU — on two
  * streams, or from two threads — race and must be serialised by the caller.
  * The first call on a device looks up the array's device address (once per
- * device, with that device current); make that first call before any
- * stream capture. */
+ * device, with that device current; again after a device reset, which gives
+ * the device a new context); make that first call before any stream
+ * capture. */
 VSC_API vsc_status vsc_get_consist_out_noalloc(const vsc_image* crnt_pr, const vsc_image* prev_stab_warp,
     const vsc_image* cons_wt, int32_t num_iter, float step_size, float mom_fac, const vsc_image* consis_out,
     vsc_stream_t stream);

@@ -48,7 +48,8 @@ def build(ref: bool = True) -> None:
     if shutil.which("nvcc") or Path("/usr/local/cuda/bin/nvcc").exists():
         targets.append("_build/librefgpu.so")
     subprocess.run(["make", "-s", "-C", str(HERE), *targets], check=True)
-    refdir = os.environ.get("VSC_REFERENCE_ROOT", "/root/reference")
+    # the reference checkout: VSC_REFERENCE_ROOT, else "reference" beside this checkout
+    refdir = os.environ.get("VSC_REFERENCE_ROOT", str(HERE.parent.parent / "reference"))
     if ref and Path(refdir, "src", "ort_custom_ops").is_dir():
         subprocess.run(["make", "-s", "-C", str(HERE), "ref", "refgpu", f"REF={refdir}"], check=True)
 

@@ -494,11 +494,14 @@ __global__ void __launch_bounds__(kTbEX / 2 * kTbEY / 2, 1)
         const TileLoc c = locate<kN, kIH>(g, tile);
         const int ox = c.ox, oy = c.oy, w = c.w, h = c.h;
         if (!mbar_wait_bounded(bar, parity, kWaitSpins)) {
+            // the outputs are invalid and vsc_check_device reports VSC_ETIMEOUT; the
+            // second bounded wait gives copies still in flight a chance to land
+            // before the CTA exits
             if (tid == 0) {
                 atomicExch(&g_device_timeout, 1);
                 bulk_wait_all();
             }
-            mbar_wait_bounded(bar, parity, kWaitSpins);  // let copies still in flight land
+            mbar_wait_bounded(bar, parity, kWaitSpins);
             return;
         }
         parity ^= 1;
@@ -751,11 +754,14 @@ __global__ void __launch_bounds__(kPThreads, 1)
         const TileLoc c = locate<kN, kPIH>(g, tile);
         const int ox = c.ox, oy = c.oy, w = c.w, h = c.h;
         if (!mbar_wait_bounded(bar, parity, kWaitSpins)) {
+            // the outputs are invalid and vsc_check_device reports VSC_ETIMEOUT; the
+            // second bounded wait gives copies still in flight a chance to land
+            // before the CTA exits
             if (threadIdx.x == 0) {
                 atomicExch(&g_device_timeout, 1);
                 bulk_wait_all();
             }
-            mbar_wait_bounded(bar, parity, kWaitSpins);  // let copies still in flight land
+            mbar_wait_bounded(bar, parity, kWaitSpins);
             return;
         }
         parity ^= 1;
@@ -2043,33 +2049,74 @@ cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O
     return cudaGetLastError();
 }
 
-// ---- solver workspace for callers that cannot allocate ------------------------
-// A file-scope device array (every GPU that loads the library holds it until
-// the process exits).  In host code g_noalloc_ws is only a stand-in symbol,
-// not a device address: its device address is looked up once per device with
-// cudaGetSymbolAddress, with that device current, and handed to the kernels.
-static __device__ __align__(256) float g_noalloc_ws[kNoAllocWorkspaceFloats];
+// ---- device addresses of file-scope device arrays -----------------------------
+// In host code a __device__ variable's name is only a stand-in symbol, not a
+// device address.  Its address is looked up with cudaGetSymbolAddress, with
+// the device current, once per device and context: the address belongs to
+// the module loaded into the context, so after a device reset (a new primary
+// context) it is looked up again.  The context is told apart by its id
+// (cuCtxGetId, fetched from the driver at run time); without that entry
+// point every call looks the address up.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
 
-cudaError_t noalloc_workspace(float** out)
+bool current_context_id(unsigned long long* id)
 {
-    static std::mutex mu;
-    static float* addr[64] = {};
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(p);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(p);
+    });
+    CUcontext ctx = nullptr;
+    return get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx && get_id(ctx, id) == CUDA_SUCCESS;
+}
+
+struct SymbolCache {
+    std::mutex mu;
+    void* addr[64] = {};
+    unsigned long long ctx[64] = {};
+};
+
+cudaError_t symbol_address(SymbolCache& c, const void* symbol, void** out)
+{
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess)
         return e;
     if (dev < 0 || dev >= 64)
         return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
-        float* p = nullptr;
-        e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_noalloc_ws);
-        if (e != cudaSuccess)
+    unsigned long long id = 0;
+    std::lock_guard<std::mutex> lock(c.mu);
+    if (!c.addr[dev] || !current_context_id(&id) || c.ctx[dev] != id) {
+        void* p = nullptr;
+        if ((e = cudaGetSymbolAddress(&p, symbol)) != cudaSuccess)
             return e;
-        addr[dev] = p;
+        // the lookup made the device's context current
+        c.addr[dev] = p;
+        c.ctx[dev] = current_context_id(&id) ? id : 0;
     }
-    *out = addr[dev];
+    *out = c.addr[dev];
     return cudaSuccess;
+}
+
+// ---- solver workspace for callers that cannot allocate ------------------------
+// A file-scope device array (every GPU that loads the library holds it until
+// the process exits), handed to the kernels by its device address
+// (symbol_address: looked up once per device and context).
+static __device__ __align__(256) float g_noalloc_ws[kNoAllocWorkspaceFloats];
+
+cudaError_t noalloc_workspace(float** out)
+{
+    static SymbolCache cache;
+    return symbol_address(cache, g_noalloc_ws, reinterpret_cast<void**>(out));
 }
 
 cudaError_t run_solver_noalloc(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,
@@ -2086,19 +2133,8 @@ cudaError_t run_solver_noalloc(const float* P, const float* A, const float* Wt, 
 
 cudaError_t device_timeout_flag(int** flag)
 {
-    static std::mutex mu;
-    static int* addr[64] = {};
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess)
-        return e;
-    if (dev < 0 || dev >= 64)
-        return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev] && (e = cudaGetSymbolAddress(reinterpret_cast<void**>(&addr[dev]), g_device_timeout)) != cudaSuccess)
-        return e;
-    *flag = addr[dev];
-    return cudaSuccess;
+    static SymbolCache cache;
+    return symbol_address(cache, &g_device_timeout, reinterpret_cast<void**>(flag));
 }
 
 cudaError_t check_device_timeout(int* flagged)
