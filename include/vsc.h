@@ -509,10 +509,13 @@ VSC_API vsc_status vsc_multistream_set_solver_form(vsc_multistream* m, int32_t f
 VSC_API vsc_status vsc_multistream_set_upsampler(vsc_multistream* m, int32_t index, vsc_upsampler* u);
 
 /* ---- frame directories (FileStabilizer, stabilizefiles.cpp:37-149) ----------
- * Image files: PNG (8-bit gray, gray+alpha, RGB or RGBA, not interlaced) and
- * binary PPM (P6, maxval 255), read into RGBA8 host buffers (alpha 255 where
- * the file has none).  JPEG, which the reference also reads through Qt, is
- * reported as VSC_EUNSUPPORTED.  Flow files: Middlebury .flo (flowIO.cpp). */
+ * Image files: PNG (8-bit gray, gray+alpha, RGB or RGBA, not interlaced),
+ * binary PPM (P6, maxval 255) and baseline JPEG (sequential DCT, Huffman
+ * coding, 8-bit, grey or YCbCr, any sampling factors, restart markers; as the
+ * reference reads *.jpg through Qt; progressive JPEG is VSC_EUNSUPPORTED),
+ * read into RGBA8 host buffers (alpha 255 where the file has none).  A JPEG
+ * decoder's output is not fixed by the standard: pixels can differ by a few
+ * levels from another decoder's.  Flow files: Middlebury .flo (flowIO.cpp). */
 VSC_API vsc_status vsc_image_file_info(const char* path, int32_t* width, int32_t* height);
 VSC_API vsc_status vsc_read_image_file(const char* path, uint8_t* rgba, int32_t width, int32_t height);
 /* Writes an 8-bit RGB PNG (the alpha of rgba is dropped). */
@@ -523,8 +526,17 @@ VSC_API vsc_status vsc_flo_info(const char* path, int32_t* width, int32_t* heigh
 VSC_API vsc_status vsc_read_flo(const char* path, float* flow, int32_t width, int32_t height);
 VSC_API vsc_status vsc_write_flo(const char* path, const float* flow, int32_t width, int32_t height);
 
+/* Writes width x height RGBA8 (alpha ignored) as a baseline JFIF JPEG:
+ * quality 1..100 scales the standard's example quantisation tables as the
+ * IJG library does; flags bit 0: 4:4:4 chroma (else 4:2:0), bit 1: a
+ * restart marker after every MCU row, bit 2: one grey component (the
+ * luma).  Replaces the reference's
+ * QImage::save(".jpg") of its output frames (stabilizefiles.cpp:104-106). */
+VSC_API vsc_status vsc_write_jpeg(const char* path, const uint8_t* rgba, int32_t width, int32_t height,
+    int32_t quality, int32_t flags);
+
 typedef struct vsc_files_config {
-    const char* original_dir;  /* original frames, *.png / *.ppm in name order */
+    const char* original_dir;  /* original frames, *.png / *.jpg / *.jpeg / *.ppm in name order */
     const char* processed_dir; /* per-frame processed frames, same count */
     const char* output_dir;    /* created if missing; receives 000000.png ... */
     const char* flow_dir;      /* NULL: flows computed by the library; else
@@ -535,6 +547,10 @@ typedef struct vsc_files_config {
     int32_t flow_downscale;    /* FLOWDOWNSCALE, computed flows only; 0 or 1 = none */
     int32_t corr_dtype;        /* vsc_stabilizer_config.corr_dtype */
     const vsc_hyper_params* hyper; /* NULL: the defaults */
+    int32_t jpeg_quality;      /* 0: PNG outputs (lossless); 1..100: .jpg outputs at
+                                  that quality, as the reference writes its frames
+                                  (QImage::save, stabilizefiles.cpp:104-106; Qt's
+                                  default quality is 75) */
 } vsc_files_config;
 
 /* Stabilizes every frame of the directories: frame 0 is the processed frame,

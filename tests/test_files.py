@@ -1,10 +1,14 @@
 """Frame-directory driver (the FileStabilizer equivalent) and its file
-formats: PNG / PPM images and Middlebury .flo flows.
+formats: PNG / PPM / JPEG images and Middlebury .flo flows.
 
 CPU tests: the library's PNG decoder against files made here with Python's
 zlib (stored, fixed and dynamic Huffman blocks; every row filter), its PNG
 writer read back with Python's zlib, PPM, and .flo round trips with the
-reference's error cases (flowIO.cpp:31-80, imagehelpers.cpp:42-50).
+reference's error cases (flowIO.cpp:31-80, imagehelpers.cpp:42-50), and the
+baseline JPEG codec: encode -> decode round trips in every mode it writes
+(4:2:0 / 4:4:4 / grey, restart markers), with PSNR bars stated per mode (a
+JPEG decoder's output is not fixed by the standard, so there are no exact
+reference pixels), and the coding processes it refuses.
 GPU tests: a whole directory stabilized through vsc_stabilize_files equals,
 frame for frame and bit for bit, the reference's frame loop run over the CPU
 restatement (computed flows, and flows read from a flow directory)."""
@@ -114,8 +118,8 @@ def test_ppm_and_unsupported_inputs(vsc, tmp_path):
     got = vsc.read_image(p)
     assert np.array_equal(got[..., :3], pix) and np.all(got[..., 3] == 255)
     j = tmp_path / "b.jpg"
-    j.write_bytes(b"\xff\xd8\xff\xe0" + bytes(100))
-    with pytest.raises(vsc.VscError, match="EUNSUPPORTED.*JPEG"):
+    j.write_bytes(b"\xff\xd8\xff\xe0" + bytes(100))  # a JPEG start, then a zero segment length
+    with pytest.raises(vsc.VscError, match="EINVAL.*corrupt JPEG"):
         vsc.read_image(j)
     bad = tmp_path / "c.png"
     data = bytearray(_png_bytes(pix, 2, 6))
@@ -144,6 +148,95 @@ def test_flo_round_trip_and_errors(vsc, tmp_path):
         with pytest.raises(vsc.VscError, match=word):
             vsc.read_flo(q)
     del C
+
+
+def _smooth_rgba(h, w, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ys, xs = np.mgrid[0:h, 0:w]
+    img = np.zeros((h, w, 3))
+    for _ in range(12):
+        cx, cy, sg = rng.uniform(0, w), rng.uniform(0, h), rng.uniform(3, max(4, w / 3))
+        img += np.exp(-((xs - cx) ** 2 + (ys - cy) ** 2) / (2 * sg * sg))[..., None] * rng.uniform(0, 1, 3)
+    out = np.full((h, w, 4), 255, np.uint8)
+    out[..., :3] = np.clip(np.rint(img / img.max() * 255), 0, 255)
+    return out
+
+
+def _psnr8(a, b):
+    import math
+
+    m = float(np.mean((a[..., :3].astype(np.float64) - b[..., :3]) ** 2))
+    return math.inf if m == 0 else 10 * math.log10(255.0 ** 2 / m)
+
+
+# (quality, 4:4:4, grey, PSNR bar in dB) for smooth images
+JPEG_MODES = [(95, True, False, 45.0), (75, False, False, 32.0), (90, False, True, 45.0), (40, False, False, 28.0)]
+
+
+@pytest.mark.parametrize("h,w", [(48, 64), (23, 37), (1, 1), (9, 17), (130, 200)])
+def test_jpeg_round_trip(vsc, tmp_path, h, w):
+    img = _smooth_rgba(h, w, h * 1000 + w)
+    p = tmp_path / "a.jpg"
+    for q, c444, grey, bar in JPEG_MODES:
+        vsc.write_jpeg(p, img, q, chroma_444=c444, grey=grey)
+        assert p.read_bytes()[:4] == b"\xff\xd8\xff\xe0"
+        got = vsc.read_image(p)
+        assert got.shape == (h, w, 4) and (got[..., 3] == 255).all()
+        ref = img
+        if grey:
+            y = np.clip(np.rint(0.299 * img[..., 0] + 0.587 * img[..., 1] + 0.114 * img[..., 2]), 0, 255)
+            ref = np.repeat(y[..., None], 4, -1).astype(np.uint8)
+            assert (got[..., 0] == got[..., 1]).all() and (got[..., 1] == got[..., 2]).all()
+        assert _psnr8(got, ref) >= bar, (q, c444, grey)
+        # restart markers after every MCU row change the file, not the pixels
+        vsc.write_jpeg(tmp_path / "r.jpg", img, q, chroma_444=c444, grey=grey, restart_rows=True)
+        if h > 16:
+            assert (tmp_path / "r.jpg").read_bytes() != p.read_bytes()
+        assert np.array_equal(vsc.read_image(tmp_path / "r.jpg"), got)
+
+
+def test_jpeg_constant_colour(vsc, tmp_path):
+    img = np.zeros((40, 56, 4), np.uint8)
+    img[...] = (200, 30, 90, 255)
+    vsc.write_jpeg(tmp_path / "c.jpg", img, 90)
+    got = vsc.read_image(tmp_path / "c.jpg")
+    assert np.abs(got[..., :3].astype(int) - img[..., :3]).max() <= 2
+
+
+def test_jpeg_refused_and_corrupt(vsc, tmp_path):
+    import ctypes as C
+
+    # a progressive frame header (SOF2): refused as unsupported
+    sof2 = bytes([0xFF, 0xD8, 0xFF, 0xC2, 0x00, 0x11, 0x08, 0x00, 0x10, 0x00, 0x10, 0x03,
+                  0x01, 0x22, 0x00, 0x02, 0x11, 0x01, 0x03, 0x11, 0x01, 0xFF, 0xD9])
+    (tmp_path / "p.jpg").write_bytes(sof2)
+    with pytest.raises(vsc.VscError, match="EUNSUPPORTED.*SOF2"):
+        vsc.read_image(tmp_path / "p.jpg")
+    # 12-bit samples: refused
+    (tmp_path / "t.jpg").write_bytes(sof2.replace(bytes([0xC2, 0x00, 0x11, 0x08]), bytes([0xC1, 0x00, 0x11, 0x0C])))
+    with pytest.raises(vsc.VscError, match="EUNSUPPORTED"):
+        vsc.read_image(tmp_path / "t.jpg")
+    # truncated files and a corrupt segment length: errors, no crash
+    good = tmp_path / "g.jpg"
+    vsc.write_jpeg(good, _smooth_rgba(32, 32, 5), 80)
+    data = good.read_bytes()
+    for cut in (4, 30, 200, 600):
+        (tmp_path / "x.jpg").write_bytes(data[:cut])
+        try:
+            vsc.read_image(tmp_path / "x.jpg")
+        except vsc.VscError:
+            pass
+    bad = bytearray(data)
+    bad[4:6] = b"\xff\xff"  # APP0 length past the end
+    (tmp_path / "y.jpg").write_bytes(bytes(bad))
+    with pytest.raises(vsc.VscError, match="EINVAL"):
+        vsc.read_image(tmp_path / "y.jpg")
+    # header-only size query
+    w, h = C.c_int32(), C.c_int32()
+    vsc._check(vsc.load().vsc_image_file_info(str(good).encode(), C.byref(w), C.byref(h)))
+    assert (w.value, h.value) == (32, 32)
+    with pytest.raises(vsc.VscError, match="EINVAL"):
+        vsc.write_jpeg(good, _smooth_rgba(8, 8, 1), 0)
 
 
 def _write_stream(vsc, tmp_path, frames):
@@ -180,6 +273,36 @@ def test_stabilize_files_computed_flow(vsc, oracle, cuda, tmp_path):
     for idx in (0, 5):
         back = oracle.float_to_rgba(oracle.rgba_to_float(frames[idx][1]))
         assert np.array_equal(vsc.read_image(out / f"{idx:06d}.png")[..., :3], back[..., :3])
+
+
+@pytest.mark.gpu
+def test_stabilize_files_jpeg_frames(vsc, oracle, cuda, tmp_path):
+    """A frame directory of JPEG files, as the reference reads them, stabilized
+    into .jpg outputs as the reference writes them: the stabilized frames
+    equal the restatement's loop over the decoded input frames (bit for bit
+    before the output encoding); the written .jpg files decode to within
+    35 dB of those frames."""
+    from oracle_driver import run_oracle_stream
+    from vsc_gb300 import synth
+
+    w, h = 96, 64
+    s = synth.SyntheticStream(w, h, seed=45)
+    frames = [tuple(a.copy() for a in s.frame(i)) for i in range(5)]
+    od, pd = tmp_path / "orig", tmp_path / "proc"
+    od.mkdir()
+    pd.mkdir()
+    for i, (o, p) in enumerate(frames):
+        vsc.write_jpeg(od / f"{i:06d}.jpg", o, 92)
+        vsc.write_jpeg(pd / f"frame{i:04d}.jpeg", p, 92)
+    decoded = [(vsc.read_image(od / f"{i:06d}.jpg"), vsc.read_image(pd / f"frame{i:04d}.jpeg")) for i in range(5)]
+    ref = run_oracle_stream(oracle, decoded)
+    out_png, out_jpg = tmp_path / "out_png", tmp_path / "out_jpg"
+    assert vsc.stabilize_files(od, pd, out_png) == 5
+    assert vsc.stabilize_files(od, pd, out_jpg, jpeg_quality=90) == 5
+    assert sorted(f.name for f in out_jpg.iterdir()) == [f"{i:06d}.jpg" for i in range(5)]
+    for t in range(1, 4):
+        assert np.array_equal(vsc.read_image(out_png / f"{t:06d}.png")[..., :3], ref[t - 1][1][..., :3]), t
+        assert _psnr8(vsc.read_image(out_jpg / f"{t:06d}.jpg"), ref[t - 1][1]) >= 35.0, t
 
 
 @pytest.mark.gpu

@@ -49,7 +49,7 @@ EXPORTED = [
     "vsc_stabilizer_synchronize", "vsc_stabilizer_wait_output",
     "vsc_get_consist_out_fma", "vsc_consist_out_fma_workspace_size", "vsc_solver_autotune_form",
     "vsc_solver_tile_rows_form",
-    "vsc_stabilizer_set_solver_form", "vsc_multistream_set_solver_form",
+    "vsc_stabilizer_set_solver_form", "vsc_multistream_set_solver_form", "vsc_write_jpeg",
 ]
 VSC_DTYPE_F32, VSC_DTYPE_BF16, VSC_DTYPE_F16 = 0, 1, 2
 VSC_OUT_HOST_ASYNC = 2
@@ -82,7 +82,7 @@ class FilesConfig(C.Structure):
     _fields_ = [
         ("original_dir", C.c_char_p), ("processed_dir", C.c_char_p), ("output_dir", C.c_char_p),
         ("flow_dir", C.c_char_p), ("width", C.c_int32), ("height", C.c_int32), ("flow_downscale", C.c_int32),
-        ("corr_dtype", C.c_int32), ("hyper", C.c_void_p),
+        ("corr_dtype", C.c_int32), ("hyper", C.c_void_p), ("jpeg_quality", C.c_int32),
     ]
 
 
@@ -166,6 +166,7 @@ def load():
         "vsc_image_file_info": [C.c_char_p, C.POINTER(i32), C.POINTER(i32)],
         "vsc_read_image_file": [C.c_char_p, vp, i32, i32],
         "vsc_write_png": [C.c_char_p, vp, i32, i32],
+        "vsc_write_jpeg": [C.c_char_p, vp, i32, i32, i32, i32],
         "vsc_flo_info": [C.c_char_p, C.POINTER(i32), C.POINTER(i32)],
         "vsc_read_flo": [C.c_char_p, vp, i32, i32],
         "vsc_write_flo": [C.c_char_p, vp, i32, i32],
@@ -506,7 +507,7 @@ def get_consist_out_noalloc(crnt_pr, prev_stab_warp, cons_wt, num_iter, step_siz
 # ---- files ----------------------------------------------------------------------
 
 def read_image(path):
-    """RGBA8 numpy array of a PNG / PPM file."""
+    """RGBA8 numpy array of a PNG / PPM / JPEG file."""
     import numpy as np
 
     w, h = C.c_int32(), C.c_int32()
@@ -521,6 +522,16 @@ def write_png(path, rgba):
 
     a = np.ascontiguousarray(rgba, dtype=np.uint8)
     _check(load().vsc_write_png(str(path).encode(), a.ctypes.data, a.shape[1], a.shape[0]))
+
+
+def write_jpeg(path, rgba, quality: int = 75, chroma_444: bool = False, restart_rows: bool = False,
+               grey: bool = False):
+    """Baseline JFIF JPEG of an RGBA8 array (alpha ignored)."""
+    import numpy as np
+
+    a = np.ascontiguousarray(rgba, dtype=np.uint8)
+    flags = (1 if chroma_444 else 0) | (2 if restart_rows else 0) | (4 if grey else 0)
+    _check(load().vsc_write_jpeg(str(path).encode(), a.ctypes.data, a.shape[1], a.shape[0], int(quality), flags))
 
 
 def read_flo(path):
@@ -541,12 +552,13 @@ def write_flo(path, flow):
 
 
 def stabilize_files(original_dir, processed_dir, output_dir, flow_dir=None, width=0, height=0, flow_downscale=1,
-                    corr_dtype: str = "f32", hyper: "HyperParams | None" = None) -> int:
-    """Headless FileStabilizer: stabilizes a frame directory; returns the number of frames written."""
+                    corr_dtype: str = "f32", hyper: "HyperParams | None" = None, jpeg_quality: int = 0) -> int:
+    """Headless FileStabilizer: stabilizes a frame directory; returns the number
+    of frames written (PNG files, or .jpg at jpeg_quality 1..100)."""
     code = {"f32": VSC_DTYPE_F32, "bf16": VSC_DTYPE_BF16, "fp16": VSC_DTYPE_F16}[corr_dtype]
     cfg = FilesConfig(str(original_dir).encode(), str(processed_dir).encode(), str(output_dir).encode(),
                       str(flow_dir).encode() if flow_dir else None, width, height, flow_downscale, code,
-                      C.cast(C.pointer(hyper), C.c_void_p) if hyper is not None else None)
+                      C.cast(C.pointer(hyper), C.c_void_p) if hyper is not None else None, int(jpeg_quality))
     n = C.c_int32()
     _check(load().vsc_stabilize_files(C.byref(cfg), C.byref(n)))
     return n.value

@@ -23,7 +23,7 @@ LIB = PKG / "libvsc.so"
 INCLUDE = PKG.parent / "include"
 
 SOURCES = ["vsc_ops.cu", "vsc_stab.cu", "vsc_solver.cu", "vsc_flow.cu", "vsc_corr_tc.cu", "vsc_upsampler.cu",
-           "vsc_upsampler_tc.cu", "vsc_api.cpp", "vsc_files.cpp"]
+           "vsc_upsampler_tc.cu", "vsc_api.cpp", "vsc_files.cpp", "vsc_jpeg.cpp"]
 HEADERS = ["vsc_internal.h", "vsc_math.cuh", "vsc_ptx.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -7,9 +7,11 @@
 //   * binary PPM (P6, maxval 255), read and written;
 //   * Middlebury .flo (flowIO.cpp:31-107): tag 202021.25, width, height,
 //     then interleaved (u, v) floats, little-endian.
-// The reference reads *.png and *.jpg through Qt and writes JPEG; JPEG has no
-// codec here (a .jpg input is reported as unsupported) and the outputs are
-// PNG files named like the reference's (six-digit frame index).
+//   * baseline JPEG, read and written (vsc_jpeg.cpp).
+// The reference reads *.png and *.jpg through Qt and writes JPEG
+// (stabilizefiles.cpp:104-106); here the outputs are PNG files by default
+// (lossless) or, with jpeg_quality set, .jpg files as the reference writes
+// them, named like the reference's (six-digit frame index).
 #include <cuda_runtime.h>
 #include <dirent.h>
 #include <sys/stat.h>
@@ -29,6 +31,10 @@ namespace vsc {
 // set_error lives in vsc_api.cpp
 vsc_status set_error(vsc_status s, const char* fmt, ...);
 void clear_error();
+// vsc_jpeg.cpp
+vsc_status jpeg_decode(const uint8_t* d, size_t n, const char* path, int* w, int* h, std::vector<uint8_t>* rgba,
+    bool header_only);
+vsc_status jpeg_encode(const uint8_t* rgba, int w, int h, int quality, int flags, std::vector<uint8_t>* out);
 }  // namespace vsc
 
 namespace {
@@ -445,7 +451,7 @@ vsc_status load_image(const char* path, Image* img, bool header_only)
     if (d.size() >= 2 && d[0] == 'P' && d[1] == '6')
         return decode_ppm(d, path, img, header_only);
     if (d.size() >= 3 && d[0] == 0xFF && d[1] == 0xD8 && d[2] == 0xFF)
-        return set_error(VSC_EUNSUPPORTED, "%s: JPEG input is not supported (PNG or PPM)", path);
+        return vsc::jpeg_decode(d.data(), d.size(), path, &img->w, &img->h, &img->rgba, header_only);
     return set_error(VSC_EINVAL, "%s: unknown image format", path);
 }
 
@@ -509,6 +515,21 @@ vsc_status write_png_rgb(const char* path, const uint8_t* rgba, int w, int h)
 }
 
 // ---- .flo (flowIO.cpp:31-107) -----------------------------------------------------
+vsc_status write_jpeg_rgb(const char* path, const uint8_t* rgba, int w, int h, int quality, int flags)
+{
+    std::vector<uint8_t> file;
+    vsc_status s = vsc::jpeg_encode(rgba, w, h, quality, flags, &file);
+    if (s)
+        return s;
+    FILE* f = std::fopen(path, "wb");
+    if (!f)
+        return set_error(VSC_EINVAL, "%s: cannot write (%s)", path, std::strerror(errno));
+    const bool ok = std::fwrite(file.data(), 1, file.size(), f) == file.size();
+    if (std::fclose(f) != 0 || !ok)
+        return set_error(VSC_EINVAL, "%s: write failed", path);
+    return VSC_OK;
+}
+
 vsc_status flo_read(const char* path, std::vector<float>* flow, int* w, int* h)
 {
     std::vector<uint8_t> d;
@@ -559,7 +580,7 @@ bool has_image_ext(const std::string& n)
         const size_t l = std::strlen(e);
         return n.size() > l && n.compare(n.size() - l, l, e) == 0;
     };
-    return ends(".png") || ends(".jpg") || ends(".ppm");
+    return ends(".png") || ends(".jpg") || ends(".jpeg") || ends(".ppm");
 }
 
 vsc_status list_frames(const char* dir, std::vector<std::string>* out)
@@ -690,6 +711,17 @@ VSC_API vsc_status vsc_write_png(const char* path, const uint8_t* rgba, int32_t 
     return write_png_rgb(path, rgba, width, height);
 }
 
+VSC_API vsc_status vsc_write_jpeg(const char* path, const uint8_t* rgba, int32_t width, int32_t height,
+    int32_t quality, int32_t flags)
+{
+    vsc::clear_error();
+    if (!path || !rgba || width < 1 || height < 1)
+        return set_error(VSC_EINVAL, "write_jpeg: null argument or empty image");
+    if (flags & ~7)
+        return set_error(VSC_EINVAL, "write_jpeg: unknown flags 0x%x", flags);
+    return write_jpeg_rgb(path, rgba, width, height, quality, flags);
+}
+
 VSC_API vsc_status vsc_flo_info(const char* path, int32_t* width, int32_t* height)
 {
     vsc::clear_error();
@@ -748,6 +780,8 @@ VSC_API vsc_status vsc_stabilize_files(const vsc_files_config* cfg, int32_t* fra
     const int n = static_cast<int>(std::min(orig.size(), proc.size()));
     if (n < 3)
         return set_error(VSC_EINVAL, "stabilize_files: %d frames, at least 3 are needed", n);
+    if (cfg->jpeg_quality < 0 || cfg->jpeg_quality > 100)
+        return set_error(VSC_EINVAL, "stabilize_files: jpeg_quality %d outside [0, 100]", cfg->jpeg_quality);
     mkdir(cfg->output_dir, 0755);
     int w = cfg->width, h = cfg->height;
     if (w <= 0 || h <= 0) {
@@ -782,8 +816,10 @@ VSC_API vsc_status vsc_stabilize_files(const vsc_files_config* cfg, int32_t* fra
     std::vector<uint8_t> out(static_cast<size_t>(w) * h * 4), rt;
     std::vector<float> ffwd, fbwd;
     Image window[3];
+    const int jq = cfg->jpeg_quality;
     auto write = [&](int idx, const uint8_t* rgba) {
-        vsc_status r = write_png_rgb((out_dir + "/" + index6(idx) + ".png").c_str(), rgba, w, h);
+        vsc_status r = jq > 0 ? write_jpeg_rgb((out_dir + "/" + index6(idx) + ".jpg").c_str(), rgba, w, h, jq, 0)
+                              : write_png_rgb((out_dir + "/" + index6(idx) + ".png").c_str(), rgba, w, h);
         if (!r)
             ++written;
         return r;
