@@ -394,7 +394,7 @@ def solver_roofline(vsc, dev, stream, iters: int = 144, form: str = "exact"):
     """Times the dominant kernel — the full-resolution solver in the given
     form — with CUDA events on its stream: the time of one Jacobi step from
     an 8-step and an (8 + iters)-step solve of the same size (both whole
-    numbers of launches for 4 or 8 steps per launch)."""
+    numbers of 8-step rounds), reported per round."""
     import torch
 
     peak, peak_src = peaks()
@@ -417,25 +417,32 @@ def solver_roofline(vsc, dev, stream, iters: int = 144, form: str = "exact"):
     ev[3].record(stream)
     ev[3].synchronize()
     step_ms = (ev[2].elapsed_time(ev[3]) - ev[0].elapsed_time(ev[1])) / iters
-    per_launch_ms = step_ms * T
-    kname, launch_bpp = SOLVER_KERNELS[form]
-    alg_bytes = launch_bpp * W * H  # each input image read once, O and U written once, per launch
-    achieved = alg_bytes / (per_launch_ms / 1000.0) / 1e9
-    eff = SOLVER_BYTES_PER_PX * W * H * T / (per_launch_ms / 1000.0) / 1e9
+    round_ms = step_ms * T
+    kname, round_bpp = SOLVER_KERNELS[form]
+    alg_bytes = round_bpp * W * H  # each input image read once, O and U written once, per round
+    achieved = alg_bytes / (round_ms / 1000.0) / 1e9
+    eff = SOLVER_BYTES_PER_PX * W * H * T / (round_ms / 1000.0) / 1e9
     traffic = SOLVER_TRAFFIC_BYTES.get(kname)
-    tile = "128x72 tiles of one channel plane" if form == "fma" else "64x48 tiles of three channels"
-    line = {"bound": "hbm", "kernel": f"{kname} ({tile}; {T} Jacobi steps per launch at 1920x1080)",
+    if form == "fma":
+        desc = (f"{kname} (one persistent launch per solve: rounds of {T} Jacobi steps on 128x72 tiles of one "
+                "channel plane, tiles taken in round order, each waiting for its neighbours' previous round; "
+                "1920x1080)")
+    else:
+        desc = f"{kname} (one launch per round of {T} Jacobi steps on 64x48 tiles of three channels; 1920x1080)"
+    line = {"bound": "hbm", "kernel": desc,
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
-            "algorithmic_bytes_rule": f"{launch_bpp} B/px per launch: each input image read once and O, U "
-                                      "written once (the launch's compulsory bytes)",
+            "traffic": traffic, "algorithmic_bytes_per_round": alg_bytes,
+            "algorithmic_bytes_rule": f"{round_bpp} B/px per {T}-step round: each input image read once and O, U "
+                                      "written once (a round's compulsory bytes)",
             "effective_gbs": eff, "frac_effective": eff / peak,
-            "effective_rule": f"{SOLVER_BYTES_PER_PX} B/px per Jacobi step x {T} steps per launch (the reference's "
+            "effective_rule": f"{SOLVER_BYTES_PER_PX} B/px per Jacobi step x {T} steps per round (the reference's "
                               "one launch per step would move these bytes)",
-            "steps_per_launch": T, "launch_ms": per_launch_ms, "ms_per_jacobi_step": step_ms,
+            "steps_per_round": T, "round_ms": round_ms, "ms_per_jacobi_step": step_ms,
+            "timing_rule": f"CUDA events on the solver's stream: (time of an ({T} + {iters})-step solve - time of "
+                           f"a {T}-step solve) / {iters} per step, x {T} per round",
             "peak_source": peak_src}
     if traffic:
-        line["frac_dram"] = traffic / (per_launch_ms / 1000.0) / 1e9 / peak
+        line["frac_dram"] = traffic / (round_ms / 1000.0) / 1e9 / peak
         line["traffic_source"] = SOLVER_TRAFFIC_SOURCE[kname]
     line["pipe_counters"] = SOLVER_PIPE.get(kname)
     return line
@@ -1100,18 +1107,16 @@ def run_gpu(args):
 
 
 # The full-resolution solver kernel of each form and its compulsory bytes per
-# launch (per pixel): exact form O, U, A, consWt, lap P in (60) + O, U out
-# (24); FMA form O, U, consWt, Cs in (48) + O, U out (24).
-SOLVER_KERNELS = {"exact": ("solver_tall_kernel", 84), "fma": ("solver_fma_kernel", 72)}
-# dram__bytes_read.sum + dram__bytes_write.sum of one 8-step launch at
-# 1920x1080 from the ncu captures summarised in profiles/ (the mean of the
-# captured launches), and where each comes from.
-SOLVER_TRAFFIC_BYTES = {"solver_tall_kernel": 144_198_912, "solver_fma_kernel": 116_517_248}
+# 8-step round (per pixel): exact form O, U, A, consWt, lap P in (60) + O, U
+# out (24); FMA form O, U, nK, Cs in (48) + O, U out (24).
+SOLVER_KERNELS = {"exact": ("solver_tall_kernel", 84), "fma": ("solver_fma_solve_kernel", 72)}
+# dram__bytes_read.sum + dram__bytes_write.sum of one 8-step round at
+# 1920x1080 from the ncu captures summarised in profiles/, and where each
+# comes from.
+SOLVER_TRAFFIC_BYTES = {"solver_tall_kernel": 144_198_912}
 SOLVER_TRAFFIC_SOURCE = {
-    "solver_tall_kernel": "profiles/solver_tall_1080p.md (mean of two launches: 124,613,888 + 21,037,568 and "
-                          "124,601,600 + 18,144,768 bytes)",
-    "solver_fma_kernel": "profiles/solver_fma_1080p.md (planar kernel; mean of two launches: 99,942,400 + "
-                         "16,809,472 and 99,815,424 + 16,467,200 bytes)",
+    "solver_tall_kernel": "profiles/solver_tall_1080p.md (one launch per round; mean of two launches: "
+                          "124,613,888 + 21,037,568 and 124,601,600 + 18,144,768 bytes)",
 }
 # What bounds each solver kernel, from the same captures: the FP32 pipe and
 # its latency, not HBM (the time steps stay on chip): the FMA pipe's active
@@ -1119,7 +1124,6 @@ SOLVER_TRAFFIC_SOURCE = {
 # sm__cycles_active) and smsp__issue_active.
 SOLVER_PIPE = {
     "solver_tall_kernel": {"fma_pipe_active": None, "issue_active": 0.585},
-    "solver_fma_kernel": {"fma_pipe_active": 0.487, "issue_active": 0.396},
 }
 
 

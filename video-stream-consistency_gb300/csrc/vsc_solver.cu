@@ -903,12 +903,15 @@ static_assert((4 * kPlStageBytes) % 128 == 0 && (2 * kPlSlotPlane * 4) % 128 == 
 
 // Cs = step * fma(wt, A, -lap P) and nK = -(step * (cnt + wt)) as planes
 // (lap P, cnt as lap_pr_kernel computes them); with O non-null, also O as
-// planes into Op.
+// planes into Op; with cnt non-null, the ncnt solve counters zeroed.
 __global__ void solver_prep_fma_kernel(const float* __restrict__ P, const float* __restrict__ A,
     const float* __restrict__ Wt, const float* __restrict__ O, float* __restrict__ Cs, float* __restrict__ nK,
-    float* __restrict__ Op, int w, int h, float step)
+    float* __restrict__ Op, int w, int h, float step, unsigned* __restrict__ cnt, int ncnt)
 {
     pdl_enter();
+    if (cnt && blockIdx.x == 0 && blockIdx.y == 0)  // the solve kernel's counters start at zero
+        for (int i = threadIdx.y * blockDim.x + threadIdx.x; i < ncnt; i += blockDim.x * blockDim.y)
+            cnt[i] = 0;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h)
@@ -955,6 +958,8 @@ struct PlanarGroup {
     const float* src[kPlanarGroupMax];
     float* dst[kPlanarGroupMax];
     uint8_t* rgba[kPlanarGroupMax];
+    unsigned* cnt[kPlanarGroupMax];  // solve counters zeroed on the way in, or null
+    int ncnt[kPlanarGroupMax];
     int64_t npix[kPlanarGroupMax];
     int block0[kPlanarGroupMax + 1];
     int count;
@@ -966,6 +971,9 @@ __global__ void __launch_bounds__(256) planar_group_kernel(const __grid_constant
     int p = 0;
     while (p + 1 < g.count && static_cast<int>(blockIdx.x) >= g.block0[p + 1])
         ++p;
+    if (g.cnt[p] && static_cast<int>(blockIdx.x) == g.block0[p])
+        for (int k = threadIdx.x; k < g.ncnt[p]; k += blockDim.x)
+            g.cnt[p][k] = 0;
     const int64_t i = static_cast<int64_t>(blockIdx.x - g.block0[p]) * blockDim.x + threadIdx.x;
     const int64_t n = g.npix[p];
     if (i >= n)
@@ -1076,36 +1084,8 @@ __device__ __forceinline__ void pl_iterate(PlState& s, float* slots, int T, int 
     }
 }
 
-// A tile of the planar solve: problem, channel plane and origin (ring included).
-struct PlTile {
-    int p, c, ox, oy, w, h;
-};
-
 int pl_tiles_x(int w) { return (w + kPlIW - 1) / kPlIW; }
 int pl_tiles(int w, int h) { return 3 * pl_tiles_x(w) * ((h + kPlIRows - 1) / kPlIRows); }
-
-// tile -> problem by a scan of the first-tile table, then channel and position
-template <int kN>
-__device__ __forceinline__ PlTile pl_locate(const SolverGroup<kN>& g, int tile)
-{
-    int p = 0;
-    if (kN > 1) {
-#pragma unroll 1
-        while (p + 1 < g.count && tile >= g.tile0[p + 1])
-            ++p;
-    }
-    const int per_plane = (g.tile0[p + 1] - g.tile0[p]) / 3;
-    int t = tile - g.tile0[p];
-    PlTile l;
-    l.p = p;
-    l.c = t / per_plane;
-    t -= l.c * per_plane;
-    l.ox = (t % g.tiles_x[p]) * kPlIW - kTbT;
-    l.oy = (t / g.tiles_x[p]) * kPlIRows - kTbT;
-    l.w = g.w[p];
-    l.h = g.h[p];
-    return l;
-}
 
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar)
 {
@@ -1122,35 +1102,6 @@ __device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, int x, int 
                      reinterpret_cast<uint64_t>(map)),
         "r"(x), "r"(y), "r"(z), "r"(smem_u32(src))
         : "memory");
-}
-
-// stage i holds map pl_map(i): O, U, nK (the consWt slot), Cs (the lap slot)
-__device__ __forceinline__ int pl_map(int i) { return i < 2 ? i : i + 1; }
-
-__device__ __forceinline__ void pl_issue(float* stage, const CUtensorMap* m, const PlTile& t, int first, int last,
-    uint64_t* bar)
-{
-    for (int i = first; i < last; ++i)
-        tma_load_3d(stage + i * kPlStage, m + pl_map(i), t.ox, t.oy, t.c, bar);
-}
-
-// The first tile of a launch: nK and Cs, which no solver launch writes,
-// before the wait for the predecessor (a launch after the first of a solve);
-// O and U after it.
-__device__ __forceinline__ void pl_issue_first(float* stage, const CUtensorMap* m, const PlTile& t, uint64_t* bar,
-    bool early)
-{
-    if (early) {
-        mbar_expect_tx(bar, 4 * kPlStageBytes);
-        pl_issue(stage, m, t, 2, 4, bar);
-    }
-    grid_dependency_wait();
-    if (early) {
-        pl_issue(stage, m, t, 0, 2, bar);
-    } else {
-        mbar_expect_tx(bar, 4 * kPlStageBytes);
-        pl_issue(stage, m, t, 0, 4, bar);
-    }
 }
 
 // The planes of one solve for the plain-load form of the kernel (widths that
@@ -1177,12 +1128,261 @@ __device__ __forceinline__ void pl_plain_load(float* stage, const PlPlain& p, in
     }
 }
 
-// The body of both planar kernels: kTma = true walks the tiles of a
-// SolverGroup (TMA loads one tile ahead, TMA stores), false the tiles of one
-// PlPlain image (plain loads and stores).
-template <int kN, bool kTma>
-__device__ __forceinline__ void pl_body(const SolverGroup<kN>& g, const PlPlain& pl, int T, int k0, float step,
-    float mom)
+// The plain-load form (widths that are not a multiple of 4, or a workspace off
+// the 16-byte grid): one launch per round of up to kTbT steps, each CTA
+// walking the round's tiles with plain loads and stores.
+__device__ __forceinline__ void pl_plain_body(const PlPlain& pl, int T, int k0, float step, float mom)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* stage = reinterpret_cast<float*>(smem_raw);
+    float* slots = stage + 4 * kPlStage;
+    float* so = slots + 2 * kPlSlotPlane;
+    float* su = so + kPlOut;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int px0 = 4 * lane, py0 = kPlRPT * warp;
+
+    for (int i = threadIdx.x; i < 2 * kPlSlotPlane; i += kPlThreads)
+        slots[i] = 0.0f;  // the apron slots stay zero
+    grid_dependency_wait();
+    const int per_plane = pl.ntiles / 3;
+    for (int tile = blockIdx.x; tile < pl.ntiles; tile += gridDim.x) {
+        if (tile + static_cast<int>(gridDim.x) >= pl.ntiles)
+            allow_dependent_launch();
+        const int c = tile / per_plane, r = tile - c * per_plane;
+        const int ox = (r % pl.tiles_x) * kPlIW - kTbT, oy = (r / pl.tiles_x) * kPlIRows - kTbT;
+        const int w = pl.w, h = pl.h;
+        __syncthreads();  // the previous tile has left the staging and the slots
+        pl_plain_load(stage, pl, c, ox, oy);
+        __syncthreads();
+        const int gx0 = ox + px0, gy0 = oy + py0;
+        const bool interior = ox >= 1 && oy >= 1 && ox + kPlW - 1 <= w - 3 && oy + kPlRows - 1 <= h - 3;
+
+        PlState s;
+#pragma unroll
+        for (int rr = 0; rr < kPlRPT; ++rr) {
+            const float* row = stage + (py0 + rr) * kPlW + px0;
+            s.o[rr] = *reinterpret_cast<const float4*>(row);
+            s.u[rr] = *reinterpret_cast<const float4*>(row + kPlStage);
+            s.nk[rr] = *reinterpret_cast<const float4*>(row + 2 * kPlStage);
+            s.c[rr] = *reinterpret_cast<const float4*>(row + 3 * kPlStage);
+        }
+        {
+            float* D = slots + ((warp + 1) * 2) * kPlPX + px0 + 4;  // buffer 0
+            *reinterpret_cast<float4*>(D) = s.o[0];
+            *reinterpret_cast<float4*>(D + kPlPX) = s.o[kPlRPT - 1];
+        }
+        __syncthreads();  // edge rows published
+        if (interior)
+            pl_iterate<true>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h);
+        else
+            pl_iterate<false>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h);
+        {
+            const int ix = px0 - kTbT;
+#pragma unroll
+            for (int rr = 0; rr < kPlRPT; ++rr) {
+                const int iy = py0 + rr - kTbT;
+                if (ix < 0 || ix >= kPlIW || iy < 0 || iy >= kPlIRows)
+                    continue;
+                *reinterpret_cast<float4*>(so + iy * kPlIW + ix) = s.o[rr];
+                *reinterpret_cast<float4*>(su + iy * kPlIW + ix) = s.u[rr];
+            }
+        }
+        __syncthreads();
+        const int64_t base = static_cast<int64_t>(c) * w * h;
+        for (int i = threadIdx.x; i < kPlOut; i += kPlThreads) {
+            const int iy = i / kPlIW, ix = i - iy * kPlIW;
+            const int gy = oy + kTbT + iy, gx = ox + kTbT + ix;
+            if (gx < w && gy < h) {
+                const int64_t idx = base + pix_index(gx, gy, w);
+                pl.Oo[idx] = so[i];
+                pl.Uo[idx] = su[i];
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kPlThreads, 1)
+    solver_fma_plain_kernel(const __grid_constant__ PlPlain pl, int T, int k0, float step, float mom)
+{
+    pl_plain_body(pl, T, k0, step, mom);
+}
+
+// ---- the FMA form's solve in one persistent launch -----------------------------
+// A solve of L launches' worth of 8-step rounds over N tiles is one kernel:
+// each CTA takes (round k, tile t) tickets in order from a global counter
+// (k = ticket / N, t = ticket % N), waits until the tile's 3x3 neighbourhood
+// has finished round k - 1 (per-tile counters of finished rounds, released
+// after the tile's TMA stores complete), runs the tile's steps and signals
+// its counter.  Round k reads O[k & 1], U[k & 1] and writes O[(k + 1) & 1],
+// U[(k + 1) & 1]; waiting for the neighbours' round k - 1 orders both the
+// reads of round k after those writes and the writes of round k after the
+// neighbours' round-(k - 1) reads of the same buffer region.  A ticket only
+// waits for earlier tickets, whose CTAs already run, so the order cannot
+// deadlock whatever else occupies the GPU; every wait is bounded all the
+// same.  Rounds overlap: a CTA moves on to round k + 1 while the last tiles of
+// round k finish elsewhere, which removes the per-launch tail (1,080 tiles
+// per round at 1920x1080 leave the eighth of eight rounds 11 % full) and the
+// launch boundaries.  The next ticket's loads are issued while the current
+// tile iterates when its neighbours are ready (normally: they finished about
+// N / #SMs tiles earlier); otherwise the CTA first finishes and signals its
+// current tile, then waits.
+enum { kPmO0, kPmO1, kPmU0, kPmU1, kPmK, kPmC, kPmOo0, kPmOo1, kPmUo0, kPmUo1, kPlMaps };
+
+template <int kN>
+struct PlSolve {
+    CUtensorMap map[kN][kPlMaps];
+    unsigned* done[kN];  // per problem and tile: rounds finished (zeroed before the launch)
+    int w[kN], h[kN], tiles_x[kN];
+    int tile0[kN + 1];   // first tile of problem p in a round's tile list; tile0[count] = N
+    int count, nround, num_iter;
+    unsigned* ticket;    // the next ticket (zeroed before the launch)
+};
+
+struct PlJob {
+    int k;                   // round
+    int p, c, tx, ty, local;  // problem, plane, tile position, tile index within the problem
+    int ox, oy, w, h;
+};
+
+template <int kN>
+__device__ __forceinline__ PlJob pl_job(const PlSolve<kN>& g, int ticket)
+{
+    const int N = g.tile0[g.count];
+    PlJob j;
+    j.k = ticket / N;
+    const int tile = ticket - j.k * N;
+    int p = 0;
+    if (kN > 1) {
+#pragma unroll 1
+        while (p + 1 < g.count && tile >= g.tile0[p + 1])
+            ++p;
+    }
+    j.p = p;
+    j.local = tile - g.tile0[p];
+    const int per_plane = (g.tile0[p + 1] - g.tile0[p]) / 3;
+    j.c = j.local / per_plane;
+    const int r = j.local - j.c * per_plane;
+    j.tx = r % g.tiles_x[p];
+    j.ty = r / g.tiles_x[p];
+    j.ox = j.tx * kPlIW - kTbT;
+    j.oy = j.ty * kPlIRows - kTbT;
+    j.w = g.w[p];
+    j.h = g.h[p];
+    return j;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Round k - 1 finished on the tile's 3x3 neighbourhood (spins <= 1: one look).
+template <int kN>
+__device__ __forceinline__ bool pl_deps(const PlSolve<kN>& g, const PlJob& j, int spins)
+{
+    if (j.k == 0)
+        return true;
+    const int tx_n = g.tiles_x[j.p];
+    const int per_plane = (g.tile0[j.p + 1] - g.tile0[j.p]) / 3;
+    const int ty_n = per_plane / tx_n;
+    const unsigned* d = g.done[j.p] + j.c * per_plane;
+    for (int dy = -1; dy <= 1; ++dy) {
+        const int y = j.ty + dy;
+        if (y < 0 || y >= ty_n)
+            continue;
+        for (int dx = -1; dx <= 1; ++dx) {
+            const int x = j.tx + dx;
+            if (x < 0 || x >= tx_n)
+                continue;
+            const unsigned* f = d + y * tx_n + x;
+            int i = 0;
+            while (ld_acquire_u32(f) < static_cast<unsigned>(j.k)) {
+                if (++i >= spins)
+                    return false;
+                if (i > 32)
+                    __nanosleep(256);
+            }
+        }
+    }
+    return true;
+}
+
+// the tile's four input planes for its round, after its neighbours' stores
+template <int kN>
+__device__ __forceinline__ void pl_job_loads(float* stage, const PlSolve<kN>& g, const PlJob& j, uint64_t* bar)
+{
+    asm volatile("fence.proxy.async.global;" ::: "memory");  // the acquired stores, before the async-proxy reads
+    const CUtensorMap* m = g.map[j.p];
+    const int par = j.k & 1;
+    mbar_expect_tx(bar, 4 * kPlStageBytes);
+    tma_load_3d(stage, m + (par ? kPmO1 : kPmO0), j.ox, j.oy, j.c, bar);
+    tma_load_3d(stage + kPlStage, m + (par ? kPmU1 : kPmU0), j.ox, j.oy, j.c, bar);
+    tma_load_3d(stage + 2 * kPlStage, m + kPmK, j.ox, j.oy, j.c, bar);
+    tma_load_3d(stage + 3 * kPlStage, m + kPmC, j.ox, j.oy, j.c, bar);
+}
+
+__device__ __forceinline__ void st_relaxed_u32(unsigned* p, unsigned v)
+{
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// the tile's stores are complete: publish its round (the release store
+// orders the completed async-proxy writes, brought into the generic proxy
+// by the proxy fence, before the counter)
+template <int kN>
+__device__ __forceinline__ void pl_job_signal(const PlSolve<kN>& g, const PlJob& j)
+{
+    bulk_wait_all();
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    st_release_u32(g.done[j.p] + j.local, static_cast<unsigned>(j.k + 1));
+}
+
+// Warp 0 looks at the 3x3 neighbourhood of job j in two halves, so that the
+// L2 round trip can overlap a tile's steps.  Issue: lanes 0..8 each start one
+// relaxed load of a neighbour's counter (a lane without a neighbour, or a job
+// that waits for nothing, yields ~0u).
+template <int kN>
+__device__ __forceinline__ unsigned pl_deps_issue(const PlSolve<kN>& g, const PlJob& j, bool valid, int lane)
+{
+    unsigned v = ~0u;
+    if (valid && j.k > 0 && lane < 9) {
+        const int tx_n = g.tiles_x[j.p];
+        const int per_plane = (g.tile0[j.p + 1] - g.tile0[j.p]) / 3;
+        const int ty_n = per_plane / tx_n;
+        const int x = j.tx + lane % 3 - 1, y = j.ty + lane / 3 - 1;
+        if (x >= 0 && x < tx_n && y >= 0 && y < ty_n)
+            asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];"
+                         : "=r"(v)
+                         : "l"(g.done[j.p] + j.c * per_plane + y * tx_n + x)
+                         : "memory");
+    }
+    return v;
+}
+
+// Take, all lanes of warp 0: every neighbour has finished round k - 1.  A yes
+// is followed by an acquire fence in the lanes that read the counters and a
+// warp barrier, which order the counters' published stores before the
+// warp's later accesses (lane 0's TMA loads of the job).
+__device__ __forceinline__ bool pl_deps_take(unsigned v, int k)
+{
+    const bool ok = __all_sync(0xffffffffu, v >= static_cast<unsigned>(k));
+    if (ok) {
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        __syncwarp();
+    }
+    return ok;
+}
+
+template <int kN>
+__global__ void __launch_bounds__(kPlThreads, 1)
+    solver_fma_solve_kernel(const __grid_constant__ PlSolve<kN> g, float step, float mom)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* stage = reinterpret_cast<float*>(smem_raw);
@@ -1190,51 +1390,89 @@ __device__ __forceinline__ void pl_body(const SolverGroup<kN>& g, const PlPlain&
     float* so = slots + 2 * kPlSlotPlane;
     float* su = so + kPlOut;
     uint64_t* bar = reinterpret_cast<uint64_t*>(su + kPlOut);
+    __shared__ int s_next, s_deferred, s_abort;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int px0 = 4 * lane, py0 = kPlRPT * warp;
+    const int total = g.tile0[g.count] * g.nround;
 
     for (int i = threadIdx.x; i < 2 * kPlSlotPlane; i += kPlThreads)
         slots[i] = 0.0f;  // the apron slots stay zero
-    if (kTma && threadIdx.x == 0)
+    if (threadIdx.x == 0) {
         mbar_init(bar, 1);
+        s_abort = 0;
+    }
     __syncthreads();
-    const int ntiles = kTma ? g.tile0[g.count] : pl.ntiles;
-    int tile = blockIdx.x;
-    if (kTma && threadIdx.x == 0 && tile < ntiles)
-        pl_issue_first(stage, g.map[pl_locate<kN>(g, tile).p], pl_locate<kN>(g, tile), bar, k0 > 0);
     grid_dependency_wait();
-    uint32_t parity = 0;
-    for (; tile < ntiles; tile += gridDim.x) {
-        if (tile + static_cast<int>(gridDim.x) >= ntiles)
-            allow_dependent_launch();
-        PlTile t;
-        if (kTma) {
-            t = pl_locate<kN>(g, tile);
-            if (!mbar_wait_bounded(bar, parity, kWaitSpins)) {
-                // the outputs are invalid and vsc_check_device reports VSC_ETIMEOUT
-                if (threadIdx.x == 0) {
-                    atomicExch(&g_device_timeout, 1);
-                    bulk_wait_all();
-                }
-                mbar_wait_bounded(bar, parity, kWaitSpins);  // let copies still in flight land
-                return;
-            }
-            parity ^= 1;
-        } else {
-            const int per_plane = pl.ntiles / 3;
-            t.p = 0;
-            t.c = tile / per_plane;
-            const int r = tile - t.c * per_plane;
-            t.ox = (r % pl.tiles_x) * kPlIW - kTbT;
-            t.oy = (r / pl.tiles_x) * kPlIRows - kTbT;
-            t.w = pl.w;
-            t.h = pl.h;
-            pl_plain_load(stage, pl, t.c, t.ox, t.oy);
-            __syncthreads();
+    // Tickets are taken two ahead: while a CTA runs its current tile, warp 0
+    // holds the next ticket (t1, loaded during the current tile) and takes the
+    // one after (t2), whose neighbours it checks across the current tile's
+    // steps; the atomic and the counter reads stay off the critical path.
+    int t1 = 0;
+    bool t1_ready = false;  // warp 0: t1's neighbours were seen finished
+    if (warp == 0) {
+        int a = 0, b = 0;
+        if (lane == 0) {
+            a = static_cast<int>(atomicAdd(g.ticket, 1u));
+            b = static_cast<int>(atomicAdd(g.ticket, 1u));
         }
-        const int w = t.w, h = t.h;
-        const int gx0 = t.ox + px0, gy0 = t.oy + py0;
-        const bool interior = t.ox >= 1 && t.oy >= 1 && t.ox + kPlW - 1 <= w - 3 && t.oy + kPlRows - 1 <= h - 3;
+        a = __shfl_sync(0xffffffffu, a, 0);
+        t1 = __shfl_sync(0xffffffffu, b, 0);
+        if (lane == 0) {
+            s_next = a;
+            if (a < total) {
+                const PlJob n = pl_job(g, a);
+                if (pl_deps(g, n, kWaitSpins)) {
+                    pl_job_loads(stage, g, n, bar);
+                } else {
+                    atomicExch(&g_device_timeout, 1);
+                    s_abort = 1;
+                }
+            }
+        }
+        const bool valid = t1 < total;
+        const PlJob n = valid ? pl_job(g, t1) : PlJob{};
+        t1_ready = pl_deps_take(pl_deps_issue(g, n, valid, lane), n.k);
+    }
+    __syncthreads();
+    int cur = s_next;
+    uint32_t parity = 0;
+    int prev = -1;  // thread 0: the ticket of a tile whose round is not yet published
+    while (cur < total && !s_abort) {
+        const PlJob j = pl_job(g, cur);
+        int t2 = 0;
+        if (warp == 0 && lane == 0)
+            t2 = static_cast<int>(atomicAdd(g.ticket, 1u));  // used after the tile's first barrier
+        if (!mbar_wait_bounded(bar, parity, kWaitSpins)) {
+            // the outputs are invalid and vsc_check_device reports VSC_ETIMEOUT
+            if (threadIdx.x == 0) {
+                atomicExch(&g_device_timeout, 1);
+                bulk_wait_all();
+            }
+            mbar_wait_bounded(bar, parity, kWaitSpins);  // let copies still in flight land
+            return;
+        }
+        parity ^= 1;
+        if (warp == 0) {
+            // One fence a tile, taken while the other warps stage their
+            // registers: it releases the previous tile's completed stores
+            // (published by the relaxed counter store after it) and acquires
+            // the neighbour counters read for t1 during that tile's steps.
+            if (lane == 0 && prev >= 0) {
+                bulk_wait_all();
+                asm volatile("fence.proxy.async.global;" ::: "memory");
+            }
+            __syncwarp();
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
+            __syncwarp();
+            if (lane == 0 && prev >= 0) {
+                const PlJob pj = pl_job(g, prev);
+                st_relaxed_u32(g.done[pj.p] + pj.local, static_cast<unsigned>(pj.k + 1));
+            }
+            prev = -1;
+        }
+        const int w = j.w, h = j.h;
+        const int gx0 = j.ox + px0, gy0 = j.oy + py0;
+        const bool interior = j.ox >= 1 && j.oy >= 1 && j.ox + kPlW - 1 <= w - 3 && j.oy + kPlRows - 1 <= h - 3;
 
         PlState s;
 #pragma unroll
@@ -1245,7 +1483,7 @@ __device__ __forceinline__ void pl_body(const SolverGroup<kN>& g, const PlPlain&
             s.nk[r] = *reinterpret_cast<const float4*>(row + 2 * kPlStage);
             s.c[r] = *reinterpret_cast<const float4*>(row + 3 * kPlStage);
         }
-        if (kTma && threadIdx.x == 0)
+        if (threadIdx.x == 0)
             bulk_wait_read();  // the previous tile's TMA stores have read the out staging
         __syncthreads();       // staging consumed
         {
@@ -1253,20 +1491,40 @@ __device__ __forceinline__ void pl_body(const SolverGroup<kN>& g, const PlPlain&
             *reinterpret_cast<float4*>(D) = s.o[0];
             *reinterpret_cast<float4*>(D + kPlPX) = s.o[kPlRPT - 1];
         }
-        if (kTma && threadIdx.x == 0 && tile + static_cast<int>(gridDim.x) < ntiles) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            const PlTile n = pl_locate<kN>(g, tile + gridDim.x);
-            mbar_expect_tx(bar, 4 * kPlStageBytes);
-            pl_issue(stage, g.map[n.p], n, 0, 4, bar);
+        if (warp == 0) {
+            // load the next tile now if its neighbours are finished (seen
+            // across the previous tile, else one look now)
+            const bool valid = t1 < total;
+            const PlJob n = valid ? pl_job(g, t1) : PlJob{};
+            const bool ready = t1_ready || pl_deps_take(pl_deps_issue(g, n, valid, lane), n.k);
+            if (lane == 0) {
+                s_next = t1;
+                s_deferred = 0;
+                if (valid) {
+                    if (ready) {
+                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        pl_job_loads(stage, g, n, bar);
+                    } else {
+                        s_deferred = 1;
+                    }
+                }
+            }
         }
         __syncthreads();  // edge rows published
-
+        unsigned t2_look = ~0u;
+        int t2_round = 0;
+        if (warp == 0) {
+            t2 = __shfl_sync(0xffffffffu, t2, 0);
+            const bool valid = t2 < total;
+            const PlJob n = valid ? pl_job(g, t2) : PlJob{};
+            t2_look = pl_deps_issue(g, n, valid, lane);
+            t2_round = n.k;
+        }
+        const int k0 = j.k * kTbT, T = min(kTbT, g.num_iter - k0);
         if (interior)
             pl_iterate<true>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h);
         else
             pl_iterate<false>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h);
-
-        // interior out: a thread's four columns are all inside or all outside
         {
             const int ix = px0 - kTbT;
 #pragma unroll
@@ -1278,44 +1536,42 @@ __device__ __forceinline__ void pl_body(const SolverGroup<kN>& g, const PlPlain&
                 *reinterpret_cast<float4*>(su + iy * kPlIW + ix) = s.u[r];
             }
         }
-        if (kTma) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                tma_store_3d(g.map[t.p] + kMapOo, t.ox + kTbT, t.oy + kTbT, t.c, so);
-                tma_store_3d(g.map[t.p] + kMapUo, t.ox + kTbT, t.oy + kTbT, t.c, su);
-                bulk_commit();
-            }
-        } else {
-            __syncthreads();
-            const int64_t base = static_cast<int64_t>(t.c) * w * h;
-            for (int i = threadIdx.x; i < kPlOut; i += kPlThreads) {
-                const int iy = i / kPlIW, ix = i - iy * kPlIW;
-                const int gy = t.oy + kTbT + iy, gx = t.ox + kTbT + ix;
-                if (gx < w && gy < h) {
-                    const int64_t idx = base + pix_index(gx, gy, w);
-                    pl.Oo[idx] = so[i];
-                    pl.Uo[idx] = su[i];
+        if (warp == 0) {
+            // acquired by the fence at the top of the next tile
+            t1_ready = __all_sync(0xffffffffu, t2_look >= static_cast<unsigned>(t2_round));
+            t1 = t2;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const CUtensorMap* m = g.map[j.p];
+            const int par = (j.k + 1) & 1;
+            tma_store_3d(m + (par ? kPmOo1 : kPmOo0), j.ox + kTbT, j.oy + kTbT, j.c, so);
+            tma_store_3d(m + (par ? kPmUo1 : kPmUo0), j.ox + kTbT, j.oy + kTbT, j.c, su);
+            bulk_commit();
+            prev = cur;
+            if (s_deferred) {
+                // the next tile's neighbours were not finished: publish this
+                // tile first (the next one may need it), then wait
+                pl_job_signal(g, j);
+                prev = -1;
+                const PlJob n = pl_job(g, s_next);
+                if (pl_deps(g, n, kWaitSpins)) {
+                    pl_job_loads(stage, g, n, bar);
+                } else {
+                    atomicExch(&g_device_timeout, 1);
+                    s_abort = 1;
                 }
             }
-            __syncthreads();  // the staging is free for the next tile's loads
         }
+        __syncthreads();  // s_next, s_abort
+        cur = s_next;
     }
-    if (kTma && threadIdx.x == 0)
+    if (threadIdx.x == 0) {
+        if (prev >= 0)
+            pl_job_signal(g, pl_job(g, prev));
         bulk_wait_all();
-}
-
-template <int kN>
-__global__ void __launch_bounds__(kPlThreads, 1)
-    solver_fma_kernel(const __grid_constant__ SolverGroup<kN> g, int T, int k0, float step, float mom)
-{
-    pl_body<kN, true>(g, PlPlain{}, T, k0, step, mom);
-}
-
-__global__ void __launch_bounds__(kPlThreads, 1)
-    solver_fma_plain_kernel(const __grid_constant__ PlPlain pl, int T, int k0, float step, float mom)
-{
-    pl_body<1, false>(SolverGroup<1>{}, pl, T, k0, step, mom);
+    }
 }
 
 // An mbarrier nobody arrives on, waited for with a bounded spin: exercises
@@ -1370,7 +1626,7 @@ bool set_group_smem()
     constexpr auto kAttr = cudaFuncAttributeMaxDynamicSharedMemorySize;
     return cudaFuncSetAttribute(solver_persistent_kernel<kN>, kAttr, kPsSmem) == cudaSuccess &&
            cudaFuncSetAttribute(solver_tall_kernel<kN>, kAttr, kPSmem) == cudaSuccess &&
-           cudaFuncSetAttribute(solver_fma_kernel<kN>, kAttr, kPlSmem) == cudaSuccess;
+           cudaFuncSetAttribute(solver_fma_solve_kernel<kN>, kAttr, kPlSmem) == cudaSuccess;
 }
 
 struct DeviceInfo {
@@ -1502,26 +1758,10 @@ bool encode_plane_map(CUtensorMap* m, const float* base, int w, int h, int box_w
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// The FMA form's maps over its planes: O[c] / U[c] / nK (in the W slot) / Cs
-// (in the L slot) with the tile box, Oo[c] / Uo[c] with the interior box.
-bool encode_solve_planar(SolveMaps* m, float* const O[2], float* const U[2], const float* nK, const float* Cs,
-    int w, int h)
-{
-    bool ok = encode_plane_map(&m->W, nK, w, h, kPlW, kPlRows) && encode_plane_map(&m->L, Cs, w, h, kPlW, kPlRows);
-    m->A = m->W;  // unused by the FMA kernel
-    for (int c = 0; c < 2 && ok; ++c)
-        ok = encode_plane_map(&m->O[c], O[c], w, h, kPlW, kPlRows) &&
-             encode_plane_map(&m->U[c], U[c], w, h, kPlW, kPlRows) &&
-             encode_plane_map(&m->Oo[c], O[c], w, h, kPlIW, kPlIRows) &&
-             encode_plane_map(&m->Uo[c], U[c], w, h, kPlIW, kPlIRows);
-    return ok;
-}
-
 // problem p of a launch: launch li of the solve reads O[c] and U[li & 1] and
 // writes O[c ^ 1] and U[(li + 1) & 1]
 template <int kN>
-void group_set(SolverGroup<kN>& g, int p, const SolveMaps& m, int c, int li, int w, int h, int rows, uint8_t* rgba,
-    int form)
+void group_set(SolverGroup<kN>& g, int p, const SolveMaps& m, int c, int li, int w, int h, int rows, uint8_t* rgba)
 {
     g.map[p][kMapO] = m.O[c];
     g.map[p][kMapU] = m.U[li & 1];
@@ -1532,21 +1772,20 @@ void group_set(SolverGroup<kN>& g, int p, const SolveMaps& m, int c, int li, int
     g.map[p][kMapUo] = m.Uo[(li + 1) & 1];
     g.w[p] = w;
     g.h[p] = h;
-    const bool planar = form == kSolverFma;
-    g.tiles_x[p] = planar ? pl_tiles_x(w) : (w + kIW - 1) / kIW;
-    g.rgba[p] = planar ? nullptr : rgba;  // the planar form writes RGBA8 when it leaves the planes
+    g.tiles_x[p] = (w + kIW - 1) / kIW;
+    g.rgba[p] = rgba;
     if (p == 0)
         g.tile0[0] = 0;
-    g.tile0[p + 1] = g.tile0[p] + (planar ? pl_tiles(w, h) : tiles_of(w, h, interior_rows(rows)));
+    g.tile0[p + 1] = g.tile0[p] + tiles_of(w, h, interior_rows(rows));
     g.count = p + 1;
 }
 
-// One launch of a persistent kernel of a form (`rows`-row tiles) over a
-// group's tiles, with programmatic dependent launch on the previous launch of
-// the stream.
+// One launch of a persistent kernel of the exact form (`rows`-row tiles)
+// over a group's tiles, with programmatic dependent launch on the previous
+// launch of the stream.
 template <int kN>
-cudaError_t launch_group(int form, int rows, const SolverGroup<kN>& g, int T, int k0, float step, float mom,
-    int sms, cudaStream_t st)
+cudaError_t launch_group(int rows, const SolverGroup<kN>& g, int T, int k0, float step, float mom, int sms,
+    cudaStream_t st)
 {
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
@@ -1556,11 +1795,6 @@ cudaError_t launch_group(int form, int rows, const SolverGroup<kN>& g, int T, in
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     cfg.gridDim = dim3(std::min(g.tile0[g.count], sms));
-    if (form == kSolverFma) {
-        cfg.blockDim = dim3(kPlThreads);
-        cfg.dynamicSmemBytes = kPlSmem;
-        return cudaLaunchKernelEx(&cfg, solver_fma_kernel<kN>, g, T, k0, step, mom);
-    }
     if (rows == kPEY) {
         cfg.blockDim = dim3(kPThreads);
         cfg.dynamicSmemBytes = kPSmem;
@@ -1581,8 +1815,8 @@ struct GroupMember {
 // Steps k_first .. num_iter - 1 of a solve over all members, in launches of
 // T <= kTbT steps, kN problems per launch.
 template <int kN>
-cudaError_t launch_members(int form, const std::vector<GroupMember>& mem, int rows, int num_iter, float step,
-    float mom, int sms, cudaStream_t st, int* nl, int k_first = 0)
+cudaError_t launch_members(const std::vector<GroupMember>& mem, int rows, int num_iter, float step, float mom,
+    int sms, cudaStream_t st, int* nl, int k_first = 0)
 {
     const int nlaunch = (num_iter - k_first + kTbT - 1) / kTbT;
     SolverGroup<kN> g{};
@@ -1594,10 +1828,9 @@ cudaError_t launch_members(int form, const std::vector<GroupMember>& mem, int ro
             const int cnt = static_cast<int>(std::min(mem.size() - b, static_cast<size_t>(kN)));
             for (int p = 0; p < cnt; ++p) {
                 const GroupMember& m = mem[b + p];
-                group_set(g, p, m.maps, m.c0 ^ (li & 1), li, m.w, m.h, rows, li == nlaunch - 1 ? m.rgba : nullptr,
-                    form);
+                group_set(g, p, m.maps, m.c0 ^ (li & 1), li, m.w, m.h, rows, li == nlaunch - 1 ? m.rgba : nullptr);
             }
-            e = launch_group(form, rows, g, T, k0, step, mom, sms, st);
+            e = launch_group(rows, g, T, k0, step, mom, sms, st);
             ++*nl;
         }
         k0 += T;
@@ -1691,9 +1924,9 @@ cudaError_t solver_group_autotune(const int* w, const int* h, int n, cudaStream_
     }
     // the kernel instantiation the solves will use: one problem, up to 4, up to 16 per launch
     auto launch = [&](const std::vector<GroupMember>& m, int rows, int num_iter, int* nl) {
-        return n == 1 ? launch_members<1>(form, m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT)
-             : n <= 4 ? launch_members<4>(form, m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT)
-                      : launch_members<kGroupMax>(form, m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT);
+        return n == 1 ? launch_members<1>(m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT)
+             : n <= 4 ? launch_members<4>(m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT)
+                      : launch_members<kGroupMax>(m, rows, num_iter, 0.15f, 0.15f, di->sms, st, nl, kTbT);
     };
     for (int round = 0; round < 5 && e == cudaSuccess; ++round) {
         for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
@@ -1737,9 +1970,15 @@ cudaError_t solver_autotune(int w, int h, cudaStream_t st, int* rows_out, int fo
     return solver_group_autotune(&w, &h, 1, st, rows_out, form);
 }
 
+// The FMA form's workspace ends in the solve kernel's counters: the ticket,
+// padding to 64 bytes, one finished-round counter per tile; rounded up to
+// 256 bytes so that a workspace placed after it stays aligned.
+int pl_counter_floats(int w, int h) { return (16 + pl_tiles(w, h) + 63) / 64 * 64; }
+
 size_t solver_workspace_floats(int w, int h, int form)
 {
-    return static_cast<size_t>(w) * h * 3 * (form == kSolverFma ? 6 : 4);
+    const size_t img = static_cast<size_t>(w) * h * 3;
+    return form == kSolverFma ? 6 * img + pl_counter_floats(w, h) : 4 * img;
 }
 
 int solver_steps_per_launch() { return kTbT; }
@@ -1759,14 +1998,18 @@ WsView ws_view(float* ws, int w, int h)
     return WsView{ws, ws + n, ws + 2 * n, ws + 3 * n};
 }
 
-// The FMA form's workspace: six planar images (three w x h planes each).
+// The FMA form's workspace: six planar images (three w x h planes each),
+// then the solve kernel's counters.
 struct PlWs {
     float *C, *K, *U[2], *O[2];
+    unsigned* cnt;
+    int ncnt;
 };
 PlWs pl_view(float* ws, int w, int h)
 {
     const size_t n = static_cast<size_t>(w) * h * 3;
-    return PlWs{ws, ws + n, {ws + 2 * n, ws + 3 * n}, {ws + 4 * n, ws + 5 * n}};
+    return PlWs{ws, ws + n, {ws + 2 * n, ws + 3 * n}, {ws + 4 * n, ws + 5 * n},
+        reinterpret_cast<unsigned*>(ws + 6 * n), pl_counter_floats(w, h)};
 }
 
 bool tma_eligible(const DeviceInfo* di, int w, const float* O, const WsView& v, const float* A, const float* Wt)
@@ -1784,6 +2027,8 @@ struct PlanarCopy {
     float* dst;
     uint8_t* rgba;
     int64_t npix;
+    unsigned* cnt = nullptr;  // solve counters to zero on the way in
+    int ncnt = 0;
 };
 
 // Interleaved <-> planar copies of n images, kPlanarGroupMax per launch.
@@ -1797,6 +2042,8 @@ cudaError_t launch_planar(const PlanarCopy* c, int n, int to_planar, cudaStream_
             g.src[p] = c[b0 + p].src;
             g.dst[p] = c[b0 + p].dst;
             g.rgba[p] = c[b0 + p].rgba;
+            g.cnt[p] = c[b0 + p].cnt;
+            g.ncnt[p] = c[b0 + p].ncnt;
             g.npix[p] = c[b0 + p].npix;
             g.block0[p + 1] = g.block0[p] + static_cast<int>((c[b0 + p].npix + 255) / 256);
         }
@@ -1808,26 +2055,73 @@ cudaError_t launch_planar(const PlanarCopy* c, int n, int to_planar, cudaStream_
     return cudaGetLastError();
 }
 
-// The FMA form of run_solver: constants and O's planes, the launches, O (and
-// the RGBA8 copy) back from its planes.
+// One launch of the FMA form's solve kernel per kN members (each member's
+// counters zeroed beforehand; the first member's ticket serves the launch).
+template <int kN>
+cudaError_t launch_solve(const std::vector<PlWs>& v, const int* w, const int* h, int n, int num_iter, float step,
+    float mom, int sms, cudaStream_t st, int* nl)
+{
+    const int nround = solve_launches(num_iter);
+    for (int b0 = 0; b0 < n; b0 += kN) {
+        PlSolve<kN> g{};
+        g.count = std::min(n - b0, kN);
+        g.tile0[0] = 0;
+        for (int p = 0; p < g.count; ++p) {
+            const PlWs& m = v[b0 + p];
+            const int W = w[b0 + p], H = h[b0 + p];
+            CUtensorMap* mp = g.map[p];
+            bool ok = true;
+            for (int c = 0; c < 2 && ok; ++c)
+                ok = encode_plane_map(&mp[c ? kPmO1 : kPmO0], m.O[c], W, H, kPlW, kPlRows) &&
+                     encode_plane_map(&mp[c ? kPmU1 : kPmU0], m.U[c], W, H, kPlW, kPlRows) &&
+                     encode_plane_map(&mp[c ? kPmOo1 : kPmOo0], m.O[c], W, H, kPlIW, kPlIRows) &&
+                     encode_plane_map(&mp[c ? kPmUo1 : kPmUo0], m.U[c], W, H, kPlIW, kPlIRows);
+            if (!ok || !encode_plane_map(&mp[kPmK], m.K, W, H, kPlW, kPlRows) ||
+                !encode_plane_map(&mp[kPmC], m.C, W, H, kPlW, kPlRows))
+                return cudaErrorInvalidValue;
+            g.done[p] = m.cnt + 16;
+            g.w[p] = W;
+            g.h[p] = H;
+            g.tiles_x[p] = pl_tiles_x(W);
+            g.tile0[p + 1] = g.tile0[p] + pl_tiles(W, H);
+        }
+        g.nround = nround;
+        g.num_iter = num_iter;
+        g.ticket = v[b0].cnt;
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.stream = st;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cfg.gridDim = dim3(static_cast<unsigned>(std::min<int64_t>(static_cast<int64_t>(g.tile0[g.count]) * nround, sms)));
+        cfg.blockDim = dim3(kPlThreads);
+        cfg.dynamicSmemBytes = kPlSmem;
+        const cudaError_t e = cudaLaunchKernelEx(&cfg, solver_fma_solve_kernel<kN>, g, step, mom);
+        if (e != cudaSuccess)
+            return e;
+        ++*nl;
+    }
+    return cudaGetLastError();
+}
+
+// The FMA form of run_solver: constants, O's planes and zeroed counters, the
+// solve (one launch; per round on the plain-load path), O (and the RGBA8
+// copy) back from its planes.
 cudaError_t run_solver_fma(const DeviceInfo* di, const float* P, const float* A, const float* Wt, float* O, int w,
     int h, int num_iter, float step, float mom, float* workspace, cudaStream_t st, int* nl, uint8_t* rgba_out)
 {
     const PlWs v = pl_view(workspace, w, h);
     const dim3 b(32, 8);
     cudaError_t e = launch_pdl(solver_prep_fma_kernel, grid2d(w, h, b), b, 0, st, P, A, Wt,
-        static_cast<const float*>(O), v.C, v.K, v.O[0], w, h, step);
+        static_cast<const float*>(O), v.C, v.K, v.O[0], w, h, step, v.cnt, v.ncnt);
     ++*nl;
     const int nlaunch = solve_launches(num_iter);
     if (e == cudaSuccess && pl_tma_eligible(di, w, workspace)) {
-        GroupMember m{};
-        if (!encode_solve_planar(&m.maps, v.O, v.U, v.K, v.C, w, h))
-            return cudaErrorInvalidValue;
-        m.w = w;
-        m.h = h;
-        const std::vector<GroupMember> one(1, m);
-        e = launch_members<1>(kSolverFma, one, kPlRows, num_iter, step, mom, di->sms, st, nl);
-    } else {
+        const std::vector<PlWs> one(1, v);
+        e = launch_solve<1>(one, &w, &h, 1, num_iter, step, mom, di->sms, st, nl);
+    } else if (e == cudaSuccess) {
         // plain loads and stores (widths not a multiple of 4, an unaligned workspace)
         const int tx = pl_tiles_x(w), nt = pl_tiles(w, h);
         int k0 = 0;
@@ -1879,7 +2173,8 @@ cudaError_t solver_prep(int form, const float* P, const float* A, const float* W
     const PlWs v = pl_view(workspace, w, h);
     const dim3 b(32, 8);
     const cudaError_t e = launch_pdl(solver_prep_fma_kernel, grid2d(w, h, b), b, 0, st, P, A, Wt,
-        static_cast<const float*>(nullptr), v.C, v.K, static_cast<float*>(nullptr), w, h, step);
+        static_cast<const float*>(nullptr), v.C, v.K, static_cast<float*>(nullptr), w, h, step,
+        static_cast<unsigned*>(nullptr), 0);
     if (e != cudaSuccess)
         return e;
     return cudaGetLastError();
@@ -1931,36 +2226,40 @@ cudaError_t run_solver_group(const SolverImage* im, int n, int num_iter, float s
     }
     const int rows = chosen_rows(dev, ws.data(), hs.data(), n, di->sms, form);
     const bool odd = solve_launches(num_iter) % 2 == 1;
-    std::vector<GroupMember> mem(n);
-    std::vector<PlanarCopy> to(n), back(n);
-    for (int i = 0; i < n; ++i) {
-        if (form == kSolverFma) {
-            const PlWs v = pl_view(im[i].workspace, im[i].w, im[i].h);
-            if (!encode_solve_planar(&mem[i].maps, v.O, v.U, v.K, v.C, im[i].w, im[i].h))
-                return cudaErrorInvalidValue;
+    if (form == kSolverFma) {
+        // O into planes (counters zeroed), one solve launch per 16 images, O back
+        std::vector<PlWs> v(n);
+        std::vector<PlanarCopy> to(n), back(n);
+        for (int i = 0; i < n; ++i) {
+            v[i] = pl_view(im[i].workspace, im[i].w, im[i].h);
             const int64_t np = static_cast<int64_t>(im[i].w) * im[i].h;
-            to[i] = PlanarCopy{im[i].O, v.O[0], nullptr, np};
-            back[i] = PlanarCopy{v.O[solve_launches(num_iter) & 1], im[i].O, im[i].rgba, np};
-            mem[i].c0 = 0;
-        } else {
-            const WsView v = ws_view(im[i].workspace, im[i].w, im[i].h);
-            float* const O[2] = {im[i].O, v.O2};
-            float* const U[2] = {v.U0, v.U1};
-            if (!encode_solve(&mem[i].maps, O, U, im[i].A, im[i].Wt, v.L, im[i].w, im[i].h, rows))
-                return cudaErrorInvalidValue;
-            mem[i].c0 = odd ? 1 : 0;
-            mem[i].rgba = im[i].rgba;
+            to[i] = PlanarCopy{im[i].O, v[i].O[0], nullptr, np, v[i].cnt, v[i].ncnt};
+            back[i] = PlanarCopy{v[i].O[solve_launches(num_iter) & 1], im[i].O, im[i].rgba, np};
         }
+        e = launch_planar(to.data(), n, 1, st, &nl);
+        if (e == cudaSuccess)
+            e = n <= 4 ? launch_solve<4>(v, ws.data(), hs.data(), n, num_iter, step, mom, di->sms, st, &nl)
+                       : launch_solve<kGroupMax>(v, ws.data(), hs.data(), n, num_iter, step, mom, di->sms, st, &nl);
+        if (e == cudaSuccess)
+            e = launch_planar(back.data(), n, 0, st, &nl);
+        if (launches)
+            *launches += nl;
+        return e != cudaSuccess ? e : cudaGetLastError();
+    }
+    std::vector<GroupMember> mem(n);
+    for (int i = 0; i < n; ++i) {
+        const WsView v = ws_view(im[i].workspace, im[i].w, im[i].h);
+        float* const O[2] = {im[i].O, v.O2};
+        float* const U[2] = {v.U0, v.U1};
+        if (!encode_solve(&mem[i].maps, O, U, im[i].A, im[i].Wt, v.L, im[i].w, im[i].h, rows))
+            return cudaErrorInvalidValue;
+        mem[i].c0 = odd ? 1 : 0;
+        mem[i].rgba = im[i].rgba;
         mem[i].w = im[i].w;
         mem[i].h = im[i].h;
     }
-    if (form == kSolverFma)
-        e = launch_planar(to.data(), n, 1, st, &nl);
-    if (e == cudaSuccess)
-        e = n <= 4 ? launch_members<4>(form, mem, rows, num_iter, step, mom, di->sms, st, &nl)
-                   : launch_members<kGroupMax>(form, mem, rows, num_iter, step, mom, di->sms, st, &nl);
-    if (e == cudaSuccess && form == kSolverFma)
-        e = launch_planar(back.data(), n, 0, st, &nl);
+    e = n <= 4 ? launch_members<4>(mem, rows, num_iter, step, mom, di->sms, st, &nl)
+               : launch_members<kGroupMax>(mem, rows, num_iter, step, mom, di->sms, st, &nl);
     if (launches)
         *launches += nl;
     if (e == cudaSuccess)
@@ -2026,7 +2325,7 @@ cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O
         m.c0 = cur == O ? 0 : 1;
         m.rgba = rgba_out;
         const std::vector<GroupMember> one(1, m);
-        cudaError_t e = launch_members<1>(kSolverExact, one, rows, num_iter, step, mom, di->sms, st, &nl);
+        cudaError_t e = launch_members<1>(one, rows, num_iter, step, mom, di->sms, st, &nl);
         if (launches)
             *launches += nl;
         return e != cudaSuccess ? e : cudaGetLastError();
