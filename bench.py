@@ -81,6 +81,34 @@ def import_pkg():
     return mod
 
 
+GATE_CYCLES = 40_000_000  # ~19 ms at 2.07 GHz
+
+
+def device_ms(stream, call, n):
+    """Device time per call of n back-to-back calls (call(k), k = 0 .. n-1):
+    a spin kernel holds the stream while the host enqueues them, so the CUDA
+    events bracket device work only, not the API's host-side cost (for
+    kernels of a few microseconds that cost would otherwise dominate).
+    Returns (ms per call, host enqueue ms); the gate covers the enqueue when
+    the latter stays below the gate's ~19 ms."""
+    import time
+
+    import torch
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        torch.cuda._sleep(GATE_CYCLES)
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for k in range(n):
+        call(k)
+    e1.record(stream)
+    host_ms = (time.perf_counter() - t0) * 1000.0
+    e1.synchronize()
+    return e0.elapsed_time(e1) / n, host_ms
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -601,14 +629,8 @@ def run_corr_only(args):
         for name, fn in calls.items():
             for _ in range(max(args.warmup, 3)):
                 fn()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for _ in range(args.steps):
-                fn()
-            e1.record(stream)
-            e1.synchronize()
-            ms = e0.elapsed_time(e1) / args.steps
-            lev[name] = {"ms": ms, "gbs": alg / (ms / 1000) / 1e9}
+            ms, host_ms = device_ms(stream, lambda k: fn(), args.steps)
+            lev[name] = {"ms": ms, "gbs": alg / (ms / 1000) / 1e9, "host_enqueue_ms": host_ms}
         res[f"{lw}x{lh}"] = lev
     tot = {k: sum(v[k]["ms"] for v in res.values()) for k in ("f32", "bf16", "fp16")}
     print(json.dumps({"kernel": "correlation, PWC pyramid of one 1920x1088 direction", "levels": res,
@@ -658,17 +680,11 @@ def run_front_only(args):
     for name, (bpp, call) in forms.items():
         for _ in range(max(args.warmup, 3)):
             call()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
-            call()
-        e1.record(stream)
-        e1.synchronize()
-        ms = e0.elapsed_time(e1) / args.steps
+        ms, host_ms = device_ms(stream, lambda k: call(), args.steps)
         alg = bpp * W * H
         res.append({"kernel": name + " 1920x1080", "ms": ms, "bytes_per_px": bpp,
                     "achieved_gbs": alg / (ms / 1000) / 1e9, "frac": alg / (ms / 1000) / 1e9 / peak,
-                    "algorithmic_bytes": alg})
+                    "algorithmic_bytes": alg, "host_enqueue_ms": host_ms})
     print(json.dumps({"forms": res, "peak_gbs": peak, "peak_source": peak_src}))
 
 
@@ -697,8 +713,9 @@ def run_warpblend(args):
     input and output pixel, the Warp op 4 (2 C + 2) B per pixel (a batch of
     8 at the 480x272, 32-channel PWC level), RGBA8 <-> float 16 B/px.
     K calls back to back between two CUDA events on the kernels' stream,
-    each call on the next of four input sets, so that consecutive calls
-    never find their inputs in L2 (every case's four sets exceed 129 MB)."""
+    enqueued while a spin kernel holds the stream (device_ms), each call on
+    the next of four input sets, so that consecutive calls never find their
+    inputs in L2 (every case's four sets exceed 129 MB)."""
     import torch
 
     vsc = import_pkg()
@@ -760,15 +777,9 @@ def run_warpblend(args):
     for name, alg, call in cases:
         for k in range(max(args.warmup, 3)):
             call(sets[k % nsets])
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for k in range(args.steps):
-            call(sets[k % nsets])
-        e1.record(stream)
-        e1.synchronize()
-        ms = e0.elapsed_time(e1) / args.steps
+        ms, host_ms = device_ms(stream, lambda k: call(sets[k % nsets]), args.steps)
         res.append({"kernel": name, "ms": ms, "algorithmic_bytes": alg, "achieved_gbs": alg / (ms / 1000) / 1e9,
-                    "frac": alg / (ms / 1000) / 1e9 / peak})
+                    "frac": alg / (ms / 1000) / 1e9 / peak, "host_enqueue_ms": host_ms})
     print(json.dumps({"kernels": res, "peak_gbs": peak, "peak_source": peak_src}))
 
 
@@ -797,14 +808,8 @@ def run_upsampler_only(args):
     for _ in range(max(args.warmup, 3)):
         vsc.load().vsc_upsampler_apply(up._h, *(vsc.C.byref(vsc.image(t)) for t in (coarse, frame, out)),
                                       vsc._stream(stream))
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        vsc._check(vsc.load().vsc_upsampler_apply(up._h, *(vsc.C.byref(vsc.image(t)) for t in (coarse, frame, out)),
-                                                  vsc._stream(stream)))
-    e1.record(stream)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
+    ms, _ = device_ms(stream, lambda k: vsc._check(vsc.load().vsc_upsampler_apply(
+        up._h, *(vsc.C.byref(vsc.image(t)) for t in (coarse, frame, out)), vsc._stream(stream))), args.steps)
     peak, peak_src = peaks()
     alg = 423 * W * H
     flops = 2 * 9 * (16 * 32 + 32 * 32 + 32 * 32 + 32 * 16) * W * H

@@ -401,7 +401,11 @@ VSC_API vsc_status vsc_stabilizer_synchronize(vsc_stabilizer* s);
 
 /* Device pointers to internal state, for inspection (valid until the next call):
  * which = 0: last stabilized frame (float HWC3), 1: forward flow, 2: backward flow
- * (float HWC, 3 channels when computed), 3: adapCmbPr, 4: consWt. */
+ * (float HWC, 3 channels when computed), 3: adapCmbPr, 4: consWt.  With
+ * flow_downscale > 1 and bilinear upsampling (no learned upsampler, no
+ * occlusion mask) a step's front pass samples the coarse flows directly; the
+ * first request for 1 or 2 after such a step upsamples them (the values the
+ * step used) and waits for the stabilizer's stream. */
 VSC_API vsc_status vsc_stabilizer_buffer(vsc_stabilizer* s, int32_t which, const float** dev_ptr);
 
 /* Number of kernels the last vsc_stabilizer_step (or load_frame) enqueued. */

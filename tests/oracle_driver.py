@@ -17,7 +17,9 @@ def run_oracle_stream(oracle, frames, flows=None, hp=None, downscale=1, occlusio
         if flows is not None:
             ff, fb = flows[t]
         elif downscale > 1:
-            fw, fh = int(round(w / downscale)), int(round(h / downscale))
+            # videostabilizer.cpp:93-94: C round(), halves away from zero
+            fw, fh = int(np.floor(np.float32(w) / np.float32(downscale) + 0.5)), int(
+                np.floor(np.float32(h) / np.float32(downscale) + 0.5))
             small = [nearest(orig[t], fw, fh), nearest(orig[t + 1], fw, fh)]
             ff = oracle.bilinear(oracle.flow_estimate(small[0], small[1]), w, h)
             fb = oracle.bilinear(oracle.flow_estimate(small[1], small[0]), w, h)

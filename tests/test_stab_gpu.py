@@ -85,11 +85,32 @@ def test_adap_comb_and_weights(vsc, oracle, cuda, alpha, beta, gamma):
 
 
 @pytest.mark.parametrize("src,dst", [((64, 48), (32, 24)), ((33, 21), (16, 10)), ((16, 10), (33, 21)),
-                                     ((1920, 1080), (960, 540)), ((960, 540), (1920, 1080))])
+                                     ((1920, 1080), (960, 540)), ((960, 540), (1920, 1080)),
+                                     # exact 2x (the staged kernel): partial blocks, rows that are
+                                     # not 16-byte aligned, one pixel, one block's window edges
+                                     ((16, 10), (32, 20)), ((481, 67), (962, 134)), ((1, 1), (2, 2)),
+                                     ((65, 5), (130, 10)), ((640, 360), (1280, 720))])
 def test_bilinear(vsc, oracle, cuda, src, dst):
     img = _img(src[1], src[0])
     got = vsc.get_bilinear(_t(img, cuda), dst[0], dst[1]).cpu().numpy()
     assert np.array_equal(got, oracle.bilinear(img, dst[0], dst[1]))
+
+
+def test_bilinear_2x_special_values(vsc, oracle, cuda):
+    """The staged exact-2x path propagates Inf and NaN and keeps signed zeros
+    exactly as the per-pixel expression does."""
+    img = _img(37, 70)
+    img[3, 5, 0] = np.inf
+    img[10, 20, 1] = -np.inf
+    img[20, 33, 2] = np.nan
+    img[0, 0, :] = -0.0
+    img[-1, -1, :] = np.float32(3.0e38)
+    got = vsc.get_bilinear(_t(img, cuda), 140, 74).cpu().numpy()
+    ref = oracle.bilinear(img, 140, 74)
+    nan = np.isnan(ref)
+    assert nan.any() and np.isinf(ref).any()
+    assert np.array_equal(np.isnan(got), nan)  # NaN payloads differ between CPU and GPU arithmetic
+    assert np.array_equal(got[~nan].view(np.uint32), ref[~nan].view(np.uint32))
 
 
 def _equal_up_to_zero_sign(a, b):
@@ -134,7 +155,8 @@ def test_consist_out_fma(vsc, oracle, cuda, h, w, iters):
     """vsc_get_consist_out_fma equals the restatement's FMA form bit for bit,
     and the exact form (kernel_consist_out's rounding) within the stated
     tolerance: max-abs <= 2e-6 on [0, 1] images, PSNR >= 100 dB, RGBA8
-    bytes differing on at most 1e-3 of the values."""
+    bytes differing on at most 1e-3 of the values (at least one byte: a
+    value within 2e-6 of a rounding edge of the 8-bit conversion may flip)."""
     import math
 
     import torch
@@ -149,9 +171,10 @@ def test_consist_out_fma(vsc, oracle, cuda, h, w, iters):
     d = np.abs(got.astype(np.float64) - exact)
     mse = float(np.mean(d * d))
     psnr = math.inf if mse == 0 else 10 * math.log10(1.0 / mse)
-    flips = float(np.mean(oracle.float_to_rgba(got)[..., :3] != oracle.float_to_rgba(exact)[..., :3]))
+    flipped = oracle.float_to_rgba(got)[..., :3] != oracle.float_to_rgba(exact)[..., :3]
+    flips = float(np.mean(flipped))
     print(f"fma vs exact {w}x{h} x{iters}: max-abs {d.max():.3g}, PSNR {psnr:.1f} dB, RGBA8 byte flips {flips:.2e}")
-    assert d.max() <= 2e-6 and psnr >= 100.0 and flips <= 1e-3
+    assert d.max() <= 2e-6 and psnr >= 100.0 and int(flipped.sum()) <= max(1, int(1e-3 * flipped.size))
     # caller-provided workspace gives the same bits
     ws = torch.empty(vsc.consist_out_workspace_size(w, h, form="fma") // 4, dtype=torch.float32, device=cuda)
     O2 = _t(O0, cuda)
@@ -417,6 +440,33 @@ def test_stabilizer_hyper_params_and_downscale(vsc, oracle, cuda):
     out = st.step().cpu().numpy()
     assert np.array_equal(st.buffer(1).cpu().numpy(), ref[0][2])
     assert np.array_equal(out, ref[0][1])
+    st.close()
+
+
+@pytest.mark.parametrize("w,h", [(128, 72), (134, 77)])
+def test_stabilizer_fma_downscale_fused_paths(vsc, oracle, cuda, w, h):
+    """FMA solver form with FLOWDOWNSCALE=2 and three pyramid levels: the
+    front pass samples the coarse flows itself and each finer level's setup
+    upsamples the coarser solution (no separate upsampling launches); two
+    steps equal the restatement's driver loop bit for bit, and the flows
+    read back on request are the upsampled ones the oracle uses."""
+    frames = _frames(w, h, 5, seed=17)
+    hp = oracle.default_hyper()
+    hp.pyramid_levels, hp.num_iter, hp.gamma = 3, 24, 1.0
+    ref = run_oracle_stream(oracle, frames, hp=hp, downscale=2, solver_form="fma")
+    st = vsc.Stabilizer(w, h, flow_downscale=2, solver_form="fma")
+    p = st.hyper_params
+    p.pyramid_levels, p.num_iter, p.gamma = 3, 24, 1.0
+    for i in range(3):
+        st.load_frame(*frames[i])
+    for k in range(2):
+        out = st.step().cpu().numpy()
+        assert np.array_equal(out, ref[k][1]), f"output, step {k}"
+        assert np.array_equal(st.buffer(0).cpu().numpy(), ref[k][0]), f"stabilized, step {k}"
+        assert np.array_equal(st.buffer(1).cpu().numpy(), ref[k][2]), f"fwd flow, step {k}"
+        assert np.array_equal(st.buffer(2).cpu().numpy(), ref[k][3]), f"bwd flow, step {k}"
+        if k + 3 < len(frames):
+            st.load_frame(*frames[k + 3])
     st.close()
 
 

@@ -718,6 +718,9 @@ struct vsc_stabilizer {
     FlowDims fd{};
     int last_launches = 0;
     bool occlusion = false;  // opt-in forward-backward consistency mask
+    // the last step's front pass sampled the coarse flows (bilinear
+    // FLOWDOWNSCALE): flow_fwd / flow_bwd are upsampled only on request
+    bool flows_pending = false;
     int solver_form = kSolverExact;  // VSC_SOLVER_EXACT / VSC_SOLVER_FMA
     // learned flow upsampling (flow_downscale > 1); null: bilinear
     vsc_upsampler* upsampler = nullptr;
@@ -761,6 +764,15 @@ struct DeviceGuard {
 };
 
 enum { kEvLoad0, kEvLoad1, kEvStep0, kEvFlow, kEvFront, kEvCoarse, kEvStep1 };
+
+// FLOWDOWNSCALE with bilinear upsampling (flowmodel.cpp:158-161) and no
+// occlusion mask: the front pass samples the coarse 3-channel flows where it
+// uses them, with the upsampling's expression, instead of reading upsampled
+// copies (the same values; the full-size flows are not written).
+bool front_samples_small_flows(const vsc_stabilizer* s)
+{
+    return s->compute_flow && s->downscale > 1 && !s->upsampler && !s->occlusion && s->fc == 3;
+}
 
 void mark(vsc_stabilizer* s, int which)
 {
@@ -1209,7 +1221,7 @@ cudaError_t enqueue_pre_solve(vsc_stabilizer* s, const vsc_hyper_params& hp, Lev
             // learned upsampling of both flows in one batch (the luma of
             // frame t for the forward flow, of frame t+1 for the backward one)
             run(upsampler_apply_pair(s, st, &nl));
-        } else if (small) {
+        } else if (small && !front_samples_small_flows(s)) {
             // flowmodel.cpp:158-161: bilinear upsampling, vectors not rescaled
             run(launch_bilinear(Img{s->flow_small, s->fw, s->fh, 3}, Img{s->flow_fwd, s->w, s->h, 3}, st));
             run(launch_bilinear(Img{s->flow_small + fs, s->fw, s->fh, 3}, Img{s->flow_bwd, s->w, s->h, 3}, st));
@@ -1220,9 +1232,17 @@ cudaError_t enqueue_pre_solve(vsc_stabilizer* s, const vsc_hyper_params& hp, Lev
     mark(s, kEvFlow);
     float* ls_in = s->last_stab[s->ls_cur];
     float* ls_out = s->last_stab[s->ls_cur ^ 1];
-    run(launch_fused_front(s->orig[s0], s->orig[s1], s->orig[s2], s->proc[s0], s->proc[s1], s->proc[s2], ls_in,
-        s->flow_fwd, s->flow_bwd, s->fc, s->adap_pr, s->cons_wt, s->w, s->h, hp.alpha, hp.beta, hp.gamma, st,
-        s->occlusion));
+    if (front_samples_small_flows(s)) {
+        // the upsampling of both flows happens inside the front pass
+        const int64_t fs = static_cast<int64_t>(s->fw) * s->fh * 3;
+        run(launch_fused_front(s->orig[s0], s->orig[s1], s->orig[s2], s->proc[s0], s->proc[s1], s->proc[s2], ls_in,
+            s->flow_small, s->flow_small + fs, 3, s->adap_pr, s->cons_wt, s->w, s->h, hp.alpha, hp.beta, hp.gamma,
+            st, false, s->fw, s->fh));
+    } else {
+        run(launch_fused_front(s->orig[s0], s->orig[s1], s->orig[s2], s->proc[s0], s->proc[s1], s->proc[s2], ls_in,
+            s->flow_fwd, s->flow_bwd, s->fc, s->adap_pr, s->cons_wt, s->w, s->h, hp.alpha, hp.beta, hp.gamma, st,
+            s->occlusion));
+    }
     ++nl;
 
     // pyramid (videostabilizer.cpp:203-217)
@@ -1270,12 +1290,20 @@ cudaError_t enqueue_step(vsc_stabilizer* s, const vsc_hyper_params& hp, uint8_t*
     for (int j = L - 1; j >= 0; --j) {
         if (j == 0)
             mark(s, kEvCoarse);
+        const int iters = hp.num_iter / (j + 1);
+        uint8_t* rgba = j == 0 ? rgba_dev : nullptr;
+        if (j != L - 1 && s->solver_form == kSolverFma && iters > 0) {
+            // the FMA form upsamples the coarser solution in its setup pass
+            run(run_solver_from_coarse(P[j], A[j], W[j], O[j], s->lw[j], s->lh[j], O[j + 1], s->lw[j + 1],
+                s->lh[j + 1], iters, hp.step_size, hp.mom_fac, s->solver_ws, st, &nl, rgba));
+            continue;
+        }
         if (j != L - 1) {
             run(launch_bilinear(Img{O[j + 1], s->lw[j + 1], s->lh[j + 1], 3}, Img{O[j], s->lw[j], s->lh[j], 3}, st));
             ++nl;
         }
-        run(run_solver(P[j], A[j], W[j], O[j], s->lw[j], s->lh[j], hp.num_iter / (j + 1), hp.step_size, hp.mom_fac,
-            s->solver_ws, st, &nl, j == 0 ? rgba_dev : nullptr, s->solver_form));
+        run(run_solver(P[j], A[j], W[j], O[j], s->lw[j], s->lh[j], iters, hp.step_size, hp.mom_fac, s->solver_ws, st,
+            &nl, rgba, s->solver_form));
     }
     mark(s, kEvStep1);
     *launches = nl;
@@ -1355,6 +1383,7 @@ void finish_step(vsc_stabilizer* s, int launches)
     s->head = (s->head + 1) % 3;
     s->count -= 1;
     s->last_launches = launches;
+    s->flows_pending = front_samples_small_flows(s);
 }
 
 vsc_status step_preconditions(vsc_stabilizer* s, const vsc_hyper_params& hp)
@@ -1473,6 +1502,23 @@ VSC_API vsc_status vsc_stabilizer_buffer(vsc_stabilizer* s, int32_t which, const
     clear_error();
     if (!s || !dev_ptr)
         return set_error(VSC_EINVAL, "buffer: null argument");
+    if ((which == 1 || which == 2) && s->flows_pending) {
+        // the last step sampled the coarse flows in its front pass: upsample
+        // them now (the values the step used), in stream order
+        DeviceGuard g(s->device);
+        const int64_t fs = static_cast<int64_t>(s->fw) * s->fh * 3;
+        vsc_status st = check_cuda(
+            launch_bilinear(Img{s->flow_small, s->fw, s->fh, 3}, Img{s->flow_fwd, s->w, s->h, 3}, s->st), "buffer");
+        if (!st)
+            st = check_cuda(launch_bilinear(Img{s->flow_small + fs, s->fw, s->fh, 3}, Img{s->flow_bwd, s->w, s->h, 3},
+                                s->st),
+                "buffer");
+        if (!st)
+            st = check_cuda(cudaStreamSynchronize(s->st), "buffer");
+        if (st)
+            return st;
+        s->flows_pending = false;
+    }
     switch (which) {
         case 0:
             *dev_ptr = s->last_stab[s->ls_cur];

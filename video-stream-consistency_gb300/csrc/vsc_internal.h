@@ -169,6 +169,12 @@ int solver_group_tile_rows(const int* w, const int* h, int n, bool* tuned, int f
 cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,
     float step, float mom, float* workspace, cudaStream_t st, int* launches, uint8_t* rgba_out = nullptr,
     int form = kSolverExact);
+// The FMA form started from the cw x ch solution Oc upsampled to w x h with
+// kernel_bilinear's expression (the pyramid's next level), the upsampling
+// fused into the solve's setup; O receives the result only.  num_iter >= 1.
+cudaError_t run_solver_from_coarse(const float* P, const float* A, const float* Wt, float* O, int w, int h,
+    const float* Oc, int cw, int ch, int num_iter, float step, float mom, float* workspace, cudaStream_t st,
+    int* launches, uint8_t* rgba_out);
 
 // Grouped solve: n images of any sizes, the same iterations, each launch of
 // the persistent kernel walking the tiles of all of them (up to 16 images
@@ -211,10 +217,14 @@ cudaError_t run_solver_noalloc(const float* P, const float* A, const float* Wt, 
     float step, float mom, cudaStream_t st);
 
 // Fused five-warp + adaptive combination + consistency weights for the
-// orchestrator: writes adapCmbPr and consWt only.
+// orchestrator: writes adapCmbPr and consWt only.  With fw, fh > 0 the flows
+// are the 3-channel fw x fh flows that the step upsamples bilinearly to
+// w x h, sampled where they are used (same outputs as upsampling them first);
+// not with the occlusion mask.
 cudaError_t launch_fused_front(const float* o0, const float* o1, const float* o2, const float* p0, const float* p1,
     const float* p2, const float* last_stab, const float* flow_fwd, const float* flow_bwd, int fc, float* adap_pr,
-    float* cons_wt, int w, int h, float alpha, float beta, float gamma, cudaStream_t st, bool occlusion_mask = false);
+    float* cons_wt, int w, int h, float alpha, float beta, float gamma, cudaStream_t st, bool occlusion_mask = false,
+    int fw = 0, int fh = 0);
 // fused_front on the RGBA8 words of the six frames (4-byte aligned, w x h
 // words each); same outputs bit for bit
 cudaError_t launch_fused_front_rgba(const uint8_t* o0, const uint8_t* o1, const uint8_t* o2, const uint8_t* p0,

@@ -80,6 +80,30 @@ __device__ __forceinline__ void pdl_enter()
 
 __device__ __forceinline__ int64_t pix_index(int x, int y, int w) { return static_cast<int64_t>(y) * w + x; }
 
+// One output pixel of kernel_bilinear (flowconsistency.cu:50-75): the c
+// channels of the iw x ih image `in` sampled at (ox * iw / ow, oy * ih / oh),
+// taps clamped to the last row and column, in the reference's expression.
+__device__ __forceinline__ void bilinear_px(const float* __restrict__ in, int iw, int ih, int ow, int oh, int c,
+    int ox, int oy, float* __restrict__ dst)
+{
+    const float xx = static_cast<float>(ox) * static_cast<float>(iw) / static_cast<float>(ow);
+    const float yy = static_cast<float>(oy) * static_cast<float>(ih) / static_cast<float>(oh);
+    // xx < iw for every size the API accepts; the clamp only guards the index
+    const int ix = min(static_cast<int>(floorf(xx)), iw - 1);
+    const int iy = min(static_cast<int>(floorf(yy)), ih - 1);
+    const float fx = xx - static_cast<float>(ix);
+    const float fy = yy - static_cast<float>(iy);
+    const int ix1 = min(ix + 1, iw - 1);
+    const int iy1 = min(iy + 1, ih - 1);
+    for (int k = 0; k < c; ++k) {
+        const float v00 = in[pix_index(ix, iy, iw) * c + k];
+        const float v10 = in[pix_index(ix1, iy, iw) * c + k];
+        const float v01 = in[pix_index(ix, iy1, iw) * c + k];
+        const float v11 = in[pix_index(ix1, iy1, iw) * c + k];
+        dst[k] = v00 * (1 - fx) * (1 - fy) + v10 * fx * (1 - fy) + v01 * (1 - fx) * fy + v11 * fx * fy;
+    }
+}
+
 // RGBA8 quantisation of gpuimage.cu:64: (uint8)__float2uint_rd(|v| * 255),
 // alpha = 1.
 __device__ __forceinline__ uint8_t quantize(float v)

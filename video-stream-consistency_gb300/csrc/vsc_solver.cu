@@ -903,10 +903,14 @@ static_assert((4 * kPlStageBytes) % 128 == 0 && (2 * kPlSlotPlane * 4) % 128 == 
 
 // Cs = step * fma(wt, A, -lap P) and nK = -(step * (cnt + wt)) as planes
 // (lap P, cnt as lap_pr_kernel computes them); with O non-null, also O as
-// planes into Op; with cnt non-null, the ncnt solve counters zeroed.
+// planes into Op, or with Oc non-null the cw x ch image Oc upsampled to w x h
+// as kernel_bilinear does (bilinear_px: the pyramid's initial solution of
+// this level, written straight into the planes); with cnt non-null, the ncnt
+// solve counters zeroed.
 __global__ void solver_prep_fma_kernel(const float* __restrict__ P, const float* __restrict__ A,
     const float* __restrict__ Wt, const float* __restrict__ O, float* __restrict__ Cs, float* __restrict__ nK,
-    float* __restrict__ Op, int w, int h, float step, unsigned* __restrict__ cnt, int ncnt)
+    float* __restrict__ Op, int w, int h, float step, unsigned* __restrict__ cnt, int ncnt,
+    const float* __restrict__ Oc, int cw, int ch)
 {
     pdl_enter();
     if (cnt && blockIdx.x == 0 && blockIdx.y == 0)  // the solve kernel's counters start at zero
@@ -920,6 +924,9 @@ __global__ void solver_prep_fma_kernel(const float* __restrict__ P, const float*
     const int64_t rs = static_cast<int64_t>(w) * 3;
     const int64_t plane = static_cast<int64_t>(w) * h;
     const int64_t q = pix_index(x, y, w);
+    float up[3];
+    if (Oc)
+        bilinear_px(Oc, cw, ch, w, h, 3, x, y, up);
     for (int c = 0; c < 3; ++c) {
         const int64_t i = i0 + c;
         int cnt = 0;
@@ -944,7 +951,9 @@ __global__ void solver_prep_fma_kernel(const float* __restrict__ P, const float*
         const float wt = Wt[i];
         Cs[c * plane + q] = __fmul_rn(step, __fmaf_rn(wt, A[i], -lap));
         nK[c * plane + q] = -__fmul_rn(step, __fadd_rn(static_cast<float>(cnt), wt));
-        if (O)
+        if (Oc)
+            Op[c * plane + q] = up[c];
+        else if (O)
             Op[c * plane + q] = O[i];
     }
 }
@@ -2106,16 +2115,17 @@ cudaError_t launch_solve(const std::vector<PlWs>& v, const int* w, const int* h,
     return cudaGetLastError();
 }
 
-// The FMA form of run_solver: constants, O's planes and zeroed counters, the
-// solve (one launch; per round on the plain-load path), O (and the RGBA8
-// copy) back from its planes.
+// The FMA form of run_solver: constants, O's planes (or the upsampled coarse
+// solution Oc) and zeroed counters, the solve (one launch; per round on the
+// plain-load path), O (and the RGBA8 copy) back from its planes.
 cudaError_t run_solver_fma(const DeviceInfo* di, const float* P, const float* A, const float* Wt, float* O, int w,
-    int h, int num_iter, float step, float mom, float* workspace, cudaStream_t st, int* nl, uint8_t* rgba_out)
+    int h, int num_iter, float step, float mom, float* workspace, cudaStream_t st, int* nl, uint8_t* rgba_out,
+    const float* Oc, int cw, int ch)
 {
     const PlWs v = pl_view(workspace, w, h);
     const dim3 b(32, 8);
     cudaError_t e = launch_pdl(solver_prep_fma_kernel, grid2d(w, h, b), b, 0, st, P, A, Wt,
-        static_cast<const float*>(O), v.C, v.K, v.O[0], w, h, step, v.cnt, v.ncnt);
+        static_cast<const float*>(O), v.C, v.K, v.O[0], w, h, step, v.cnt, v.ncnt, Oc, cw, ch);
     ++*nl;
     const int nlaunch = solve_launches(num_iter);
     if (e == cudaSuccess && pl_tma_eligible(di, w, workspace)) {
@@ -2174,7 +2184,7 @@ cudaError_t solver_prep(int form, const float* P, const float* A, const float* W
     const dim3 b(32, 8);
     const cudaError_t e = launch_pdl(solver_prep_fma_kernel, grid2d(w, h, b), b, 0, st, P, A, Wt,
         static_cast<const float*>(nullptr), v.C, v.K, static_cast<float*>(nullptr), w, h, step,
-        static_cast<unsigned*>(nullptr), 0);
+        static_cast<unsigned*>(nullptr), 0, static_cast<const float*>(nullptr), 0, 0);
     if (e != cudaSuccess)
         return e;
     return cudaGetLastError();
@@ -2267,6 +2277,25 @@ cudaError_t run_solver_group(const SolverImage* im, int n, int num_iter, float s
     return e;
 }
 
+cudaError_t run_solver_from_coarse(const float* P, const float* A, const float* Wt, float* O, int w, int h,
+    const float* Oc, int cw, int ch, int num_iter, float step, float mom, float* workspace, cudaStream_t st,
+    int* launches, uint8_t* rgba_out)
+{
+    if (num_iter <= 0 || !Oc || cw <= 0 || ch <= 0)
+        return cudaErrorInvalidValue;
+    DeviceInfo* di = nullptr;
+    cudaError_t e = device_info(&di);
+    if (e != cudaSuccess)
+        return e;
+    if (!di->ps_smem)
+        return cudaErrorNotSupported;
+    int nl = 0;
+    e = run_solver_fma(di, P, A, Wt, O, w, h, num_iter, step, mom, workspace, st, &nl, rgba_out, Oc, cw, ch);
+    if (launches)
+        *launches += nl;
+    return e;
+}
+
 cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O, int w, int h, int num_iter,
     float step, float mom, float* workspace, cudaStream_t st, int* launches, uint8_t* rgba_out, int form)
 {
@@ -2289,7 +2318,8 @@ cudaError_t run_solver(const float* P, const float* A, const float* Wt, float* O
     if (form == kSolverFma) {
         if (!di->ps_smem)
             return cudaErrorNotSupported;
-        const cudaError_t e = run_solver_fma(di, P, A, Wt, O, w, h, num_iter, step, mom, workspace, st, &nl, rgba_out);
+        const cudaError_t e = run_solver_fma(di, P, A, Wt, O, w, h, num_iter, step, mom, workspace, st, &nl, rgba_out,
+            nullptr, 0, 0);
         if (launches)
             *launches += nl;
         return e;

@@ -98,11 +98,8 @@ struct WarpTapT {
 using WarpTap = WarpTapT<int64_t>;
 
 template <class I = int64_t>
-__device__ __forceinline__ WarpTapT<I> warp_tap(const float* __restrict__ flow, int fc, int x, int y, int w, int h)
+__device__ __forceinline__ WarpTapT<I> warp_tap_uv(float flo_x, float flo_y, int x, int y, int w, int h)
 {
-    const I fi = (static_cast<I>(y) * w + x) * fc;
-    const float flo_x = flow[fi + 0];
-    const float flo_y = flow[fi + 1];
     const float map_fx = fmaxf(0.0f, fminf(static_cast<float>(x) + flo_x, static_cast<float>(w - 3)));
     const float map_fy = fmaxf(0.0f, fminf(static_cast<float>(y) + flo_y, static_cast<float>(h - 3)));
     const int map_ix = static_cast<int>(floorf(map_fx));
@@ -115,6 +112,40 @@ __device__ __forceinline__ WarpTapT<I> warp_tap(const float* __restrict__ flow, 
     t.o0 = t.q0 * 3;
     t.o1 = t.q1 * 3;
     return t;
+}
+
+template <class I = int64_t>
+__device__ __forceinline__ WarpTapT<I> warp_tap(const float* __restrict__ flow, int fc, int x, int y, int w, int h)
+{
+    const I fi = (static_cast<I>(y) * w + x) * fc;
+    return warp_tap_uv<I>(flow[fi + 0], flow[fi + 1], x, y, w, h);
+}
+
+// The first two channels of a 3-channel flow of fw x fh, bilinearly sampled
+// at pixel (x, y) of a w x h frame: the value kernel_bilinear's upsampling to
+// w x h stores there (bilinear_px: same positions, clamps and expression,
+// so the same bits), computed where it is used instead of stored.
+__device__ __forceinline__ void flow_upsampled_uv(const float* __restrict__ small, int fw, int fh, int w, int h, int x,
+    int y, float& u, float& v)
+{
+    const float xx = static_cast<float>(x) * static_cast<float>(fw) / static_cast<float>(w);
+    const float yy = static_cast<float>(y) * static_cast<float>(fh) / static_cast<float>(h);
+    const int ix = min(static_cast<int>(floorf(xx)), fw - 1);
+    const int iy = min(static_cast<int>(floorf(yy)), fh - 1);
+    const float fx = xx - static_cast<float>(ix);
+    const float fy = yy - static_cast<float>(iy);
+    const int ix1 = min(ix + 1, fw - 1);
+    const int iy1 = min(iy + 1, fh - 1);
+    const float* r0 = small + static_cast<int64_t>(iy) * fw * 3;
+    const float* r1 = small + static_cast<int64_t>(iy1) * fw * 3;
+    float out[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const float v00 = r0[ix * 3 + k], v10 = r0[ix1 * 3 + k], v01 = r1[ix * 3 + k], v11 = r1[ix1 * 3 + k];
+        out[k] = v00 * (1 - fx) * (1 - fy) + v10 * fx * (1 - fy) + v01 * (1 - fx) * fy + v11 * fx * fy;
+    }
+    u = out[0];
+    v = out[1];
 }
 
 // the bilinear blend of the four taps, in kernel_warp's operation order
@@ -302,28 +333,7 @@ __global__ void consist_wt4_kernel(const float4* __restrict__ ci, const float4* 
         consist_wt_px<kNonPos>(c.z, a.z, beta, gamma), consist_wt_px<kNonPos>(c.w, a.w, beta, gamma));
 }
 
-// ---- kernel_bilinear (flowconsistency.cu:50-75) -----------------------------
-__device__ __forceinline__ void bilinear_px(const float* __restrict__ in, int iw, int ih, int ow, int oh, int c,
-    int ox, int oy, float* __restrict__ dst)
-{
-    const float xx = static_cast<float>(ox) * static_cast<float>(iw) / static_cast<float>(ow);
-    const float yy = static_cast<float>(oy) * static_cast<float>(ih) / static_cast<float>(oh);
-    // xx < iw for every size the API accepts; the clamp only guards the index
-    const int ix = min(static_cast<int>(floorf(xx)), iw - 1);
-    const int iy = min(static_cast<int>(floorf(yy)), ih - 1);
-    const float fx = xx - static_cast<float>(ix);
-    const float fy = yy - static_cast<float>(iy);
-    const int ix1 = min(ix + 1, iw - 1);
-    const int iy1 = min(iy + 1, ih - 1);
-    for (int k = 0; k < c; ++k) {
-        const float v00 = in[pix_index(ix, iy, iw) * c + k];
-        const float v10 = in[pix_index(ix1, iy, iw) * c + k];
-        const float v01 = in[pix_index(ix, iy1, iw) * c + k];
-        const float v11 = in[pix_index(ix1, iy1, iw) * c + k];
-        dst[k] = v00 * (1 - fx) * (1 - fy) + v10 * fx * (1 - fy) + v01 * (1 - fx) * fy + v11 * fx * fy;
-    }
-}
-
+// ---- kernel_bilinear (flowconsistency.cu:50-75): bilinear_px in vsc_math.cuh ----
 __global__ void bilinear_kernel(const float* __restrict__ in, int iw, int ih, float* __restrict__ out, int ow, int oh,
     int c)
 {
@@ -385,6 +395,92 @@ __global__ void bilinear4_kernel(const float* __restrict__ in, int iw, int ih, f
         blockIdx.y * blockDim.y + threadIdx.y);
 }
 
+// Exact 2x upsampling of 3-channel images (ow == 2 iw, oh == 2 ih): the
+// sample positions ox * iw / ow and oy * ih / oh are exactly ox / 2 and
+// oy / 2, so a 128 x 8 output block (32 x 8 threads, 4 pixels each) reads
+// the 65 x 5 input window that starts at (ox_b / 2, oy_b / 2).  The window is
+// staged in shared memory by coalesced loads (its clamped columns and rows
+// repeat the last ones, as the clamped indices of bilinear_px do), each
+// output is the same expression of the same values as bilinear_px, and each
+// warp's output row leaves through shared memory as coalesced 16-byte
+// stores.  Same bits as bilinear4_kernel<3>.
+constexpr int kB2W = 128, kB2H = 8;
+constexpr int kB2InW = kB2W / 2 + 1, kB2InH = kB2H / 2 + 1;
+struct Bilinear2xSmem {
+    float tile[kB2InH][kB2InW * 3];
+    __align__(16) float row[kB2H][kB2W * 3];
+};
+
+__device__ __forceinline__ void bilinear2x3_block(Bilinear2xSmem& sm, const float* __restrict__ in, int iw, int ih,
+    float* __restrict__ out, int ow, int oh, int bx, int by)
+{
+    const int ox_b = bx * kB2W, oy_b = by * kB2H;
+    const int ix_b = ox_b / 2, iy_b = oy_b / 2;
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    for (int i = tid; i < kB2InH * kB2InW * 3; i += 32 * kB2H) {
+        const int r = i / (kB2InW * 3), q = i - r * (kB2InW * 3);
+        const int col = q / 3, ch = q - col * 3;
+        const int iy = min(iy_b + r, ih - 1), ix = min(ix_b + col, iw - 1);
+        sm.tile[r][q] = in[(static_cast<int64_t>(iy) * iw + ix) * 3 + ch];
+    }
+    __syncthreads();
+    const int oy = oy_b + threadIdx.y;
+    if (oy >= oh)
+        return;  // no barrier follows
+    const float yy = static_cast<float>(oy) * static_cast<float>(ih) / static_cast<float>(oh);
+    const int iy = min(static_cast<int>(floorf(yy)), ih - 1);
+    const float fy = yy - static_cast<float>(iy);
+    const float* t0 = sm.tile[iy - iy_b];
+    const float* t1 = sm.tile[iy - iy_b + 1];  // the clamped row min(iy + 1, ih - 1)
+    float* rb = sm.row[threadIdx.y];
+    float v[12];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int ox = min(ox_b + 4 * static_cast<int>(threadIdx.x) + j, ow - 1);
+        const float xx = static_cast<float>(ox) * static_cast<float>(iw) / static_cast<float>(ow);
+        const int ix = min(static_cast<int>(floorf(xx)), iw - 1);
+        const float fx = xx - static_cast<float>(ix);
+        const int c0 = (ix - ix_b) * 3, c1 = c0 + 3;  // column c1 is the clamped min(ix + 1, iw - 1)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float v00 = t0[c0 + k], v10 = t0[c1 + k], v01 = t1[c0 + k], v11 = t1[c1 + k];
+            v[j * 3 + k] = v00 * (1 - fx) * (1 - fy) + v10 * fx * (1 - fy) + v01 * (1 - fx) * fy + v11 * fx * fy;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q)  // the thread's 12 floats, 48 bytes: conflict-free 16-byte stores
+        reinterpret_cast<float4*>(rb)[3 * threadIdx.x + q] =
+            make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    __syncwarp();
+    const int n = min(kB2W, ow - ox_b) * 3;  // floats of this row segment
+    float* dst = out + (static_cast<int64_t>(oy) * ow + ox_b) * 3;
+    if (n == kB2W * 3 && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+            reinterpret_cast<float4*>(dst)[threadIdx.x + 32 * q] =
+                reinterpret_cast<const float4*>(rb)[threadIdx.x + 32 * q];
+    } else {
+        for (int q = threadIdx.x; q < n; q += 32)
+            dst[q] = rb[q];
+    }
+}
+
+__global__ void __launch_bounds__(256) bilinear2x3_kernel(const float* __restrict__ in, int iw, int ih,
+    float* __restrict__ out, int ow, int oh)
+{
+    pdl_enter();
+    __shared__ Bilinear2xSmem sm;
+    bilinear2x3_block(sm, in, iw, ih, out, ow, oh, blockIdx.x, blockIdx.y);
+}
+
+// the exact-2x form applies: twice the size, and every product ox * iw and
+// oy * ih exact in float (below 2^24), so the positions are exactly ox / 2, oy / 2
+bool bilinear_is_2x(int iw, int ih, int ow, int oh)
+{
+    return ow == 2 * iw && oh == 2 * ih && static_cast<int64_t>(ow) * iw < (int64_t{1} << 24) &&
+           static_cast<int64_t>(oh) * ih < (int64_t{1} << 24);
+}
+
 // bilinear4_kernel<3> over up to kBilinearGroupMax images of any sizes in one
 // launch (one per stream of a multi-stream step): a flat list of 32 x 8
 // blocks, each image's blocks after the previous image's.
@@ -394,17 +490,23 @@ struct BilinearGroup {
     float* out[kBilinearGroupMax];
     int iw[kBilinearGroupMax], ih[kBilinearGroupMax], ow[kBilinearGroupMax], oh[kBilinearGroupMax];
     int bx[kBilinearGroupMax];              // blocks per output row band
+    int two_x[kBilinearGroupMax];           // bilinear_is_2x: the staged exact-2x form
     int block0[kBilinearGroupMax + 1];      // first block of each image
     int count;
 };
 
 __global__ void __launch_bounds__(256) bilinear4_group_kernel(const __grid_constant__ BilinearGroup g)
 {
+    __shared__ Bilinear2xSmem sm;
     int p = 0;
     while (p + 1 < g.count && static_cast<int>(blockIdx.x) >= g.block0[p + 1])
         ++p;
     const int b = blockIdx.x - g.block0[p];
     const int bx = b % g.bx[p], by = b / g.bx[p];
+    if (g.two_x[p]) {
+        bilinear2x3_block(sm, g.in[p], g.iw[p], g.ih[p], g.out[p], g.ow[p], g.oh[p], bx, by);
+        return;
+    }
     bilinear4_px<3>(g.in[p], g.iw[p], g.ih[p], g.out[p], g.ow[p], g.oh[p], (bx * 32 + threadIdx.x) * 4,
         by * 8 + threadIdx.y);
 }
@@ -430,22 +532,36 @@ __global__ void pyr_down3_kernel(const float* __restrict__ P, const float* __res
 // arithmetic), alpha and beta are finite and >= 0 and |gamma| <= 1e30
 // (expf_cw_nonpos for the three weights): the same outputs bit for bit,
 // about a sixth fewer instructions and fewer registers.
-template <bool kOcc, bool kFast>
+// kHalf (without kOcc): ffwd and fbwd are the 3-channel flows of fw x fh that
+// the step upsamples bilinearly to w x h (FLOWDOWNSCALE); each pixel samples
+// them with flow_upsampled_uv, the value the upsampled flow holds there, so
+// the full-size flows are neither written nor read.
+template <bool kOcc, bool kFast, bool kHalf = false>
 __global__ void __launch_bounds__(256) fused_front_kernel(const float* __restrict__ o0,
     const float* __restrict__ o1,
     const float* __restrict__ o2, const float* __restrict__ p0, const float* __restrict__ p1,
     const float* __restrict__ p2, const float* __restrict__ ls, const float* __restrict__ ffwd,
     const float* __restrict__ fbwd, int fc, float* __restrict__ adap_pr, float* __restrict__ cons_wt, int w, int h,
-    float alpha, float beta, float gamma)
+    float alpha, float beta, float gamma, int fw = 0, int fh = 0)
 {
+    static_assert(!(kHalf && kOcc), "the occlusion mask samples the flows at warped positions");
     pdl_enter();
     using I = typename std::conditional<kFast, int, int64_t>::type;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h)
         return;
-    const WarpTapT<I> tb = warp_tap<I>(fbwd, fc, x, y, w, h);
-    const WarpTapT<I> tf = warp_tap<I>(ffwd, fc, x, y, w, h);
+    WarpTapT<I> tb, tf;
+    if (kHalf) {
+        float u, v;
+        flow_upsampled_uv(fbwd, fw, fh, w, h, x, y, u, v);
+        tb = warp_tap_uv<I>(u, v, x, y, w, h);
+        flow_upsampled_uv(ffwd, fw, fh, w, h, x, y, u, v);
+        tf = warp_tap_uv<I>(u, v, x, y, w, h);
+    } else {
+        tb = warp_tap<I>(fbwd, fc, x, y, w, h);
+        tf = warp_tap<I>(ffwd, fc, x, y, w, h);
+    }
     float mp = 1.0f, mn = 1.0f;
     if (kOcc) {
         mp = occl_check(fbwd, ffwd, fc, x, y, w, h);
@@ -651,6 +767,8 @@ cudaError_t launch_bilinear(Img in, Img out, cudaStream_t st)
     const dim3 b(32, 8);
     if (out.c == 2 || out.c == 3) {
         const dim3 g((out.w + 4 * b.x - 1) / (4 * b.x), (out.h + b.y - 1) / b.y);
+        if (out.c == 3 && in.c == 3 && bilinear_is_2x(in.w, in.h, out.w, out.h))
+            return launch_pdl(bilinear2x3_kernel, g, b, 0, st, in.d, in.w, in.h, out.d, out.w, out.h);
         if (out.c == 3)
             return launch_pdl(bilinear4_kernel<3>, g, b, 0, st, in.d, in.w, in.h, out.d, out.w, out.h);
         else
@@ -678,6 +796,7 @@ cudaError_t launch_bilinear_group(const Img* in, const Img* out, int n, cudaStre
             g.ih[p] = i.h;
             g.ow[p] = o.w;
             g.oh[p] = o.h;
+            g.two_x[p] = bilinear_is_2x(i.w, i.h, o.w, o.h) ? 1 : 0;
             g.bx[p] = (o.w + 127) / 128;
             g.block0[p + 1] = g.block0[p] + g.bx[p] * ((o.h + 7) / 8);
         }
@@ -710,14 +829,19 @@ static bool front_fast_ok(int w, int h, int fc, float alpha, float beta, float g
 
 cudaError_t launch_fused_front(const float* o0, const float* o1, const float* o2, const float* p0, const float* p1,
     const float* p2, const float* last_stab, const float* flow_fwd, const float* flow_bwd, int fc, float* adap_pr,
-    float* cons_wt, int w, int h, float alpha, float beta, float gamma, cudaStream_t st, bool occlusion_mask)
+    float* cons_wt, int w, int h, float alpha, float beta, float gamma, cudaStream_t st, bool occlusion_mask, int fw,
+    int fh)
 {
     const dim3 b(32, 8);
+    const bool half = fw > 0 && fh > 0;
+    if (half && (occlusion_mask || fc != 3))
+        return cudaErrorInvalidValue;
     const bool fast = front_fast_ok(w, h, fc, alpha, beta, gamma);
-    auto k = occlusion_mask ? (fast ? fused_front_kernel<true, true> : fused_front_kernel<true, false>)
-                            : (fast ? fused_front_kernel<false, true> : fused_front_kernel<false, false>);
-    const cudaError_t el = launch_pdl(k, grid2d(w, h, b), b, 0, st,
-        o0, o1, o2, p0, p1, p2, last_stab, flow_fwd, flow_bwd, fc, adap_pr, cons_wt, w, h, alpha, beta, gamma);
+    auto k = half ? (fast ? fused_front_kernel<false, true, true> : fused_front_kernel<false, false, true>)
+                  : occlusion_mask ? (fast ? fused_front_kernel<true, true> : fused_front_kernel<true, false>)
+                                   : (fast ? fused_front_kernel<false, true> : fused_front_kernel<false, false>);
+    const cudaError_t el = launch_pdl(k, grid2d(w, h, b), b, 0, st, o0, o1, o2, p0, p1, p2, last_stab, flow_fwd,
+        flow_bwd, fc, adap_pr, cons_wt, w, h, alpha, beta, gamma, fw, fh);
     return el != cudaSuccess ? el : cudaGetLastError();
 }
 
