@@ -1118,10 +1118,13 @@ SOLVER_KERNELS = {"exact": ("solver_tall_kernel", 84), "fma": ("solver_fma_solve
 # dram__bytes_read.sum + dram__bytes_write.sum of one 8-step round at
 # 1920x1080 from the ncu captures summarised in profiles/, and where each
 # comes from.
-SOLVER_TRAFFIC_BYTES = {"solver_tall_kernel": 144_198_912}
+SOLVER_TRAFFIC_BYTES = {"solver_tall_kernel": 144_198_912, "solver_fma_solve_kernel": 141_152_768}
 SOLVER_TRAFFIC_SOURCE = {
     "solver_tall_kernel": "profiles/solver_tall_1080p.md (one launch per round; mean of two launches: "
                           "124,613,888 + 21,037,568 and 124,601,600 + 18,144,768 bytes)",
+    "solver_fma_solve_kernel": "profiles/solver_fma_solve_1080p.md (one launch per solve; per round, the "
+                               "difference of a 40-step and an 8-step solve over 4 rounds: (468,436,992 - "
+                               "99,783,936) read + (213,648,896 - 17,690,880) written, / 4)",
 }
 # What bounds each solver kernel, from the same captures: the FP32 pipe and
 # its latency, not HBM (the time steps stay on chip): the FMA pipe's active
@@ -1129,6 +1132,7 @@ SOLVER_TRAFFIC_SOURCE = {
 # sm__cycles_active) and smsp__issue_active.
 SOLVER_PIPE = {
     "solver_tall_kernel": {"fma_pipe_active": None, "issue_active": 0.585},
+    "solver_fma_solve_kernel": {"fma_pipe_active": 0.544, "issue_active": 0.420},
 }
 
 

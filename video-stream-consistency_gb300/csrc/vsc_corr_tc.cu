@@ -338,8 +338,13 @@ __global__ void __launch_bounds__((2 + 4 * kMaxEpiGroups) * 32, 1)
 
 // ---- operand preparation ---------------------------------------------------------
 // |max| of a tensor as the bits of a non-negative float (ordered like uint).
-__global__ void absmax_kernel(const float* __restrict__ a, int64_t n, unsigned int* __restrict__ result)
+// max |a| as float bits (non-negative floats order like their bit patterns):
+// a grid-stride pass, a warp and then a block reduction, one atomic per
+// block (blockDim.x == 256)
+__global__ void __launch_bounds__(256) absmax_kernel(const float* __restrict__ a, int64_t n,
+    unsigned int* __restrict__ result)
 {
+    __shared__ float wm[8];
     float m = 0.0f;
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x)
@@ -347,7 +352,15 @@ __global__ void absmax_kernel(const float* __restrict__ a, int64_t n, unsigned i
     for (int o = 16; o > 0; o >>= 1)
         m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0)
-        atomicMax(result, __float_as_uint(m));
+        wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < 8 ? wm[threadIdx.x] : 0.0f;
+        for (int o = 4; o > 0; o >>= 1)
+            m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0)
+            atomicMax(result, __float_as_uint(m));
+    }
 }
 
 // scale = 2^k with |max| * 2^k in [2^13, 2^14); 1 for zero or non-finite maxima.
@@ -657,7 +670,8 @@ cudaError_t launch_corr_tc(const float* f1, const float* f2, float* out, int N, 
     if (e != cudaSuccess)
         return e;
     const int64_t total = static_cast<int64_t>(N) * C * H * W;
-    const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 4096));
+    // a few blocks per SM, each thread striding over ~2^4+ values
+    const unsigned blocks = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((total + 4095) / 4096, 1216)));
     absmax_kernel<<<blocks, 256, 0, st>>>(f1, total, maxbits);
     absmax_kernel<<<blocks, 256, 0, st>>>(f2, total, maxbits + 1);
     scales_kernel<<<1, 32, 0, st>>>(maxbits, scales);

@@ -1262,9 +1262,17 @@ __device__ __forceinline__ PlJob pl_job(const PlSolve<kN>& g, int ticket)
     const int tile = ticket - j.k * N;
     int p = 0;
     if (kN > 1) {
+        // the last problem whose first tile is <= tile (binary search: a job is
+        // decoded several times per tile, partly on thread 0's critical path)
+        int hi = g.count - 1;
 #pragma unroll 1
-        while (p + 1 < g.count && tile >= g.tile0[p + 1])
-            ++p;
+        while (p < hi) {
+            const int mid = (p + hi + 1) >> 1;
+            if (g.tile0[mid] <= tile)
+                p = mid;
+            else
+                hi = mid - 1;
+        }
     }
     j.p = p;
     j.local = tile - g.tile0[p];
