@@ -249,10 +249,11 @@ __global__ void up2_kernel(const float* __restrict__ in, int sw, int sh, float* 
 }
 
 // One thread per pixel, 64 per block: the pixel's 81 cost values are first
-// copied to its own column of shared memory (independent loads, issued
-// nine at a time), then the arg-max, the soft centroid and the confidence
-// read them from there -- the same operations in the same order as a direct
-// walk over the cost volume, without a chain of dependent global loads.
+// copied to its own column of shared memory (81 independent loads, all in
+// flight before the first store: one round trip, which the coarse levels'
+// few blocks cannot hide nine times over), then the arg-max, the soft
+// centroid and the confidence read them from there -- the same operations
+// in the same order as a direct walk over the cost volume.
 constexpr int kDecodeThreads = 64;
 
 __global__ void __launch_bounds__(kDecodeThreads) decode_kernel(const float* __restrict__ cv, float* __restrict__ res,
@@ -267,9 +268,15 @@ __global__ void __launch_bounds__(kDecodeThreads) decode_kernel(const float* __r
     cv += blockIdx.z * bs;
     res += blockIdx.z * bs;
     conf += blockIdx.z * bs;
-#pragma unroll 9
-    for (int d = 0; d < 81; ++d)
-        sv[d][t] = cv[d * plane + p];
+    {
+        float v[81];
+#pragma unroll
+        for (int d = 0; d < 81; ++d)
+            v[d] = __ldg(cv + d * plane + p);
+#pragma unroll
+        for (int d = 0; d < 81; ++d)
+            sv[d][t] = v[d];
+    }
     int best = 0;
     float cmax = sv[0][t] - prior * 32.0f;
     float csum = sv[0][t];
