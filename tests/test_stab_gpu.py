@@ -737,6 +737,37 @@ def test_stab_front_equals_separate_calls(vsc, oracle, cuda, fc, occ, hp):
     assert np.array_equal(wt.cpu().numpy(), rwt)
 
 
+@pytest.mark.parametrize("kind", ["smooth", "mixed", "shift"])
+@pytest.mark.parametrize("hp", [(20.0, 30.0, 2.0), (20.0, 30.0, 2e30)])
+def test_stab_front_flow_kinds(vsc, oracle, cuda, kind, hp):
+    """The front pass on the flows a stream produces: smooth flows, smooth
+    flows with a noisy patch, and a large uniform shift that pins taps to
+    the clamped frame border.  Equal to the restatement bit for bit."""
+    h, w = 75, 141
+    base = _img(h, w)
+    ims = [np.clip(base + RNG.normal(0, s_, base.shape), 0, 1).astype(np.float32)
+           for s_ in (0.03, 0.0, 0.02, 0.02, 0.01, 0.03, 0.01)]
+    o3, p3, ls = ims[0:3], ims[3:6], ims[6]
+    yy, xx = np.meshgrid(np.arange(h), np.arange(w), indexing="ij")
+    ff = np.zeros((h, w, 3), np.float32)
+    ff[..., 0] = 3.0 * np.sin(xx / 17.0) + 0.37
+    ff[..., 1] = 2.0 * np.cos(yy / 13.0) - 0.21
+    if kind == "mixed":
+        ff[20:45, 40:90, :2] += RNG.normal(0, 8, (25, 50, 2)).astype(np.float32)
+    elif kind == "shift":
+        ff[..., 0] += 60.0
+        ff[..., 1] -= 40.0
+    fb = (-ff + 0.3 * np.sin(xx / 11.0)[..., None]).astype(np.float32)
+    d = lambda a: _t(a, cuda)  # noqa: E731
+    alpha, beta, gamma = hp
+    apr, wt = vsc.stab_front([d(a) for a in o3], [d(a) for a in p3], d(ls), d(ff), d(fb), alpha, beta, gamma)
+    warps = [oracle.stab_warp(src, fl) for src, fl in ((o3[0], fb), (p3[0], fb), (o3[2], ff), (p3[2], ff),
+                                                       (ls, fb))]
+    ain, rpr = oracle.adap_comb(o3[1], p3[1], warps[0], warps[1], warps[2], warps[3], warps[4], alpha)
+    assert np.array_equal(apr.cpu().numpy(), rpr)
+    assert np.array_equal(wt.cpu().numpy(), oracle.consist_wt(o3[1], ain, beta, gamma))
+
+
 @pytest.mark.parametrize("fc,occ", [(3, False), (2, True), (3, True)])
 def test_stab_front_rgba_equals_restatement(vsc, oracle, cuda, fc, occ):
     """vsc_stab_front_rgba (taps gathered as RGBA8 words) equals the
