@@ -693,7 +693,6 @@ struct vsc_stabilizer {
     cudaStream_t dst = nullptr;
     cudaEvent_t step_done = nullptr, d2h_done[2] = {};
     int d2h_last = -1, d2h_prev = -1;  // buffers of the last two host copies
-    float* small = nullptr;  // frame resized to the flow size (downscale mode)
     float* flow_fwd = nullptr;
     float* flow_bwd = nullptr;
     float* flow_small = nullptr;  // flow at the flow size before upsampling
@@ -801,7 +800,6 @@ void free_all(vsc_stabilizer* s)
     f(s->stage[1]);
     f(s->out_rgba);
     f(s->out_rgba_b);
-    f(s->small);
     f(s->flow_fwd);
     f(s->flow_small);
     f(s->last_stab[0]);
@@ -937,7 +935,6 @@ vsc_status alloc_all(vsc_stabilizer* s)
                 A(cudaMemcpy(s->tc_scales, sc, sizeof(sc), cudaMemcpyHostToDevice));
         }
         if (s->downscale > 1) {
-            A(dalloc(&s->small, static_cast<size_t>(s->fw) * s->fh * 3));
             A(dalloc(&s->flow_small, 2 * static_cast<size_t>(s->fw) * s->fh * 3));
         }
         A(flow_upload_weights());
@@ -1068,17 +1065,11 @@ VSC_API vsc_status vsc_stabilizer_load_frame(vsc_stabilizer* s, const uint8_t* o
         ++nl;
     }
     if (s->compute_flow) {
-        const float* fimg = s->orig[slot];
-        if (s->downscale > 1) {
-            vsc_status st = check_cuda(launch_resize_nearest(s->orig[slot], s->w, s->h, s->small, s->fw, s->fh, s->st),
-                "load_frame resize");
-            if (st)
-                return st;
-            ++nl;
-            fimg = s->small;
-        }
-        vsc_status st = check_cuda(
-            launch_flow_features(fimg, s->fw, s->fh, s->fd, s->feat[slot], s->feat_scratch, s->st, &nl),
+        // FLOWDOWNSCALE (flowmodel.cpp:126-133): the pyramid reads the frame
+        // through the nearest-neighbour resize mapping, no resized copy
+        const bool small = s->downscale > 1;
+        vsc_status st = check_cuda(launch_flow_features(s->orig[slot], s->fw, s->fh, s->fd, s->feat[slot],
+                                       s->feat_scratch, s->st, &nl, small ? s->orig[slot] : nullptr, s->w, s->h),
             "load_frame features");
         if (st)
             return st;

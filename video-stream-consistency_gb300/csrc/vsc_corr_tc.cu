@@ -459,11 +459,13 @@ __global__ void to_chunked_levels_kernel(const __grid_constant__ ChunkLevels cl,
 // custom::Warp (the single-precision arithmetic of warp_op_kernel) writing
 // the chunked 16-bit operand layout directly, scaled by *scale: the warped
 // second-frame features of the flow estimator go straight to the tensor-core
-// correlation.  One thread per pixel and chunk of 8 channels.
-template <bool kBf16>
+// correlation.  One thread per pixel and chunk of 8 channels.  kUp: `flow`
+// is the estimator's coarser cw x chh level, upsampled 2x here (up2_sample)
+// instead of read from an upsampled copy.
+template <bool kBf16, bool kUp>
 __global__ void warp_to_chunked_kernel(const float* __restrict__ in, const float* __restrict__ flow,
     uint4* __restrict__ out, const float* __restrict__ scale, int C, int H, int W, int chunks, int64_t sin,
-    int64_t sfl, int64_t sout)
+    int64_t sfl, int64_t sout, int cw, int chh)
 {
     pdl_enter();
     const int64_t HW = static_cast<int64_t>(H) * W;
@@ -475,8 +477,8 @@ __global__ void warp_to_chunked_kernel(const float* __restrict__ in, const float
     const int y = HW < (int64_t(1) << 31) ? static_cast<int>(p) / W : static_cast<int>(p / W);
     const int x = static_cast<int>(p - static_cast<int64_t>(y) * W);
     const float* fl = flow + n * sfl;
-    const float xf = static_cast<float>(x) + __ldg(fl + p);
-    const float yf = static_cast<float>(y) + __ldg(fl + HW + p);
+    const float xf = static_cast<float>(x) + (kUp ? up2_sample(fl, cw, chh, x, y, 0) : __ldg(fl + p));
+    const float yf = static_cast<float>(y) + (kUp ? up2_sample(fl, cw, chh, x, y, 1) : __ldg(fl + HW + p));
     const float fxl = floorf(xf), fyt = floorf(yf);
     const float a = xf - fxl, b = yf - fyt;
     const float xR = fxl + 1.0f, yB = fyt + 1.0f;
@@ -644,14 +646,17 @@ cudaError_t launch_to_chunked_levels(const float* const* in, void* const* out, c
 }
 
 cudaError_t launch_warp_to_chunked(const float* in, const float* flow, void* out, const float* scale, int N, int C,
-    int H, int W, int64_t sin, int64_t sfl, int64_t sout_bytes, bool bf16, cudaStream_t st)
+    int H, int W, int64_t sin, int64_t sfl, int64_t sout_bytes, bool bf16, cudaStream_t st, int cw, int chh)
 {
     const int chunks = tc_padded_channels(C) / 8;
     const int64_t HW = static_cast<int64_t>(H) * W;
     const dim3 g(static_cast<unsigned>((HW + 255) / 256), chunks, N);
     const int64_t so = sout_bytes / 16;
-    const cudaError_t e = launch_pdl(bf16 ? warp_to_chunked_kernel<true> : warp_to_chunked_kernel<false>, g, dim3(256),
-        0, st, in, flow, static_cast<uint4*>(out), scale, C, H, W, chunks, sin, sfl, so);
+    const bool up = cw > 0 && chh > 0;
+    auto k = bf16 ? (up ? warp_to_chunked_kernel<true, true> : warp_to_chunked_kernel<true, false>)
+                  : (up ? warp_to_chunked_kernel<false, true> : warp_to_chunked_kernel<false, false>);
+    const cudaError_t e = launch_pdl(k, g, dim3(256), 0, st, in, flow, static_cast<uint4*>(out), scale, C, H, W,
+        chunks, sin, sfl, so, cw, chh);
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 

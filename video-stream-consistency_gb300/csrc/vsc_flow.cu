@@ -52,78 +52,124 @@ uint64_t splitmix64(uint64_t* s)
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-// bilinear sample with half-pixel centres (align_corners = False), 3 channels
-__device__ __forceinline__ void sample_hp3(const float* __restrict__ src, int sw, int sh, float sx, float sy,
-    float* res)
+// the column (row) of the FW-wide (FH-high) frame that the nearest-neighbour
+// resize to w (h) samples at x (y)
+__device__ __forceinline__ int nearest_src(int x, int w, int FW)
 {
-    if (sx < 0.0f)
-        sx = 0.0f;
-    if (sy < 0.0f)
-        sy = 0.0f;
-    int x0 = static_cast<int>(floorf(sx)), y0 = static_cast<int>(floorf(sy));
-    if (x0 > sw - 1)
-        x0 = sw - 1;
-    if (y0 > sh - 1)
-        y0 = sh - 1;
-    const int x1 = x0 + 1 < sw ? x0 + 1 : sw - 1;
-    const int y1 = y0 + 1 < sh ? y0 + 1 : sh - 1;
-    const float lx = sx - static_cast<float>(x0), ly = sy - static_cast<float>(y0);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float v00 = src[(static_cast<int64_t>(y0) * sw + x0) * 3 + k];
-        const float v01 = src[(static_cast<int64_t>(y0) * sw + x1) * 3 + k];
-        const float v10 = src[(static_cast<int64_t>(y1) * sw + x0) * 3 + k];
-        const float v11 = src[(static_cast<int64_t>(y1) * sw + x1) * 3 + k];
-        const float top = (1.0f - lx) * v00 + lx * v01;
-        const float bot = (1.0f - lx) * v10 + lx * v11;
-        res[k] = (1.0f - ly) * top + ly * bot;
-    }
+    const int64_t num = (2 * static_cast<int64_t>(x) + 1) * FW;
+    const int v = num < (int64_t{1} << 31) ? static_cast<int>(static_cast<int>(num) / (2 * w))
+                                           : static_cast<int>(num / (2 * static_cast<int64_t>(w)));
+    return min(FW - 1, v);
 }
 
-__global__ void level0_image_kernel(const float* __restrict__ img, int w, int h, float* __restrict__ lev, int lw,
-    int lh)
+struct PyrOut {
+    float* lev[kFlowLevels];
+    int lw0, lh0;
+};
+
+// The estimator's image pyramid in one launch.  Level 0 (a quarter of the
+// frame padded to a multiple of 64) averages 4 x 4 half-pixel bilinear
+// samples of the image per pixel; level l + 1 is the 2 x 2 mean of level l.
+// A block of 16 x 16 threads computes a 16 x 16 tile of level 0 and pools it
+// in shared memory to the tile's pixels of levels 1-4: level 0 is a
+// multiple of 16 in both directions, so each level-4 pixel comes from one
+// block.  kNearest: the w x h image is the nearest-neighbour resize of the
+// FW x FH frame `full` (FLOWDOWNSCALE: the reference scales the frame with
+// Qt::FastTransformation, flowmodel.cpp:126-133; pixel x samples column
+// min(FW - 1, (2x + 1) FW / (2w)), rows alike) and is read through that
+// mapping, not from a resized copy.  Same values, same operation order as
+// the restatement.
+template <bool kNearest>
+__global__ void __launch_bounds__(256) pyramid_kernel(const float* __restrict__ img, int w, int h,
+    const float* __restrict__ full, int FW, int FH, PyrOut po)
 {
     pdl_enter();
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= lw || y >= lh)
-        return;
-    const int pw = lw * 4, ph = lh * 4;
-    const float scx = static_cast<float>(w) / static_cast<float>(pw);
-    const float scy = static_cast<float>(h) / static_cast<float>(ph);
-    float acc[3] = {0.0f, 0.0f, 0.0f};
-    for (int j = 0; j < 4; ++j) {
-        const float sy = (static_cast<float>(y * 4 + j) + 0.5f) * scy - 0.5f;
+    __shared__ float t[2][16 * 16 * 3];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int x = blockIdx.x * 16 + tx, y = blockIdx.y * 16 + ty;  // inside level 0 (a multiple of 16)
+    const int lw = po.lw0, lh = po.lh0;
+    {
+        const int pw = lw * 4, ph = lh * 4;
+        const float scx = static_cast<float>(w) / static_cast<float>(pw);
+        const float scy = static_cast<float>(h) / static_cast<float>(ph);
+        // the 4 sample columns and rows of this pixel (half-pixel centres,
+        // clamped taps), their element offsets in the source and fractions
+        const float* src = kNearest ? full : img;
+        const int sw = kNearest ? FW : w;
+        int64_t cx0[4], cx1[4], ry0[4], ry1[4];
+        float lxs[4], lys[4];
+#pragma unroll
         for (int i = 0; i < 4; ++i) {
-            const float sx = (static_cast<float>(x * 4 + i) + 0.5f) * scx - 0.5f;
-            float v[3];
-            sample_hp3(img, w, h, sx, sy, v);
-            acc[0] += v[0];
-            acc[1] += v[1];
-            acc[2] += v[2];
+            float sx = (static_cast<float>(x * 4 + i) + 0.5f) * scx - 0.5f;
+            if (sx < 0.0f)
+                sx = 0.0f;
+            int x0 = static_cast<int>(floorf(sx));
+            if (x0 > w - 1)
+                x0 = w - 1;
+            const int x1 = x0 + 1 < w ? x0 + 1 : w - 1;
+            lxs[i] = sx - static_cast<float>(x0);
+            cx0[i] = 3 * static_cast<int64_t>(kNearest ? nearest_src(x0, w, FW) : x0);
+            cx1[i] = 3 * static_cast<int64_t>(kNearest ? nearest_src(x1, w, FW) : x1);
+            float sy = (static_cast<float>(y * 4 + i) + 0.5f) * scy - 0.5f;
+            if (sy < 0.0f)
+                sy = 0.0f;
+            int y0 = static_cast<int>(floorf(sy));
+            if (y0 > h - 1)
+                y0 = h - 1;
+            const int y1 = y0 + 1 < h ? y0 + 1 : h - 1;
+            lys[i] = sy - static_cast<float>(y0);
+            ry0[i] = static_cast<int64_t>(kNearest ? nearest_src(y0, h, FH) : y0) * sw * 3;
+            ry1[i] = static_cast<int64_t>(kNearest ? nearest_src(y1, h, FH) : y1) * sw * 3;
+        }
+        float acc[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float ly = lys[j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float lx = lxs[i];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const float v00 = src[ry0[j] + cx0[i] + k];
+                    const float v01 = src[ry0[j] + cx1[i] + k];
+                    const float v10 = src[ry1[j] + cx0[i] + k];
+                    const float v11 = src[ry1[j] + cx1[i] + k];
+                    const float top = (1.0f - lx) * v00 + lx * v01;
+                    const float bot = (1.0f - lx) * v10 + lx * v11;
+                    acc[k] += (1.0f - ly) * top + ly * bot;
+                }
+            }
+        }
+        float* o = po.lev[0] + (static_cast<int64_t>(y) * lw + x) * 3;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float v = acc[k] * 0.0625f;
+            o[k] = v;
+            t[0][(ty * 16 + tx) * 3 + k] = v;
         }
     }
-    float* o = lev + (static_cast<int64_t>(y) * lw + x) * 3;
-    o[0] = acc[0] * 0.0625f;
-    o[1] = acc[1] * 0.0625f;
-    o[2] = acc[2] * 0.0625f;
-}
-
-__global__ void pool2_kernel(const float* __restrict__ s, float* __restrict__ d, int cw, int chh)
-{
-    pdl_enter();
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= cw || y >= chh)
-        return;
-    const int fw = cw * 2;
+    // levels 1..4: tile side 8, 4, 2, 1; source tile in t[(l - 1) & 1], side s
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float a = s[(static_cast<int64_t>(2 * y) * fw + 2 * x) * 3 + k];
-        const float b = s[(static_cast<int64_t>(2 * y) * fw + 2 * x + 1) * 3 + k];
-        const float c = s[(static_cast<int64_t>(2 * y + 1) * fw + 2 * x) * 3 + k];
-        const float e = s[(static_cast<int64_t>(2 * y + 1) * fw + 2 * x + 1) * 3 + k];
-        d[(static_cast<int64_t>(y) * cw + x) * 3 + k] = ((a + b) + (c + e)) * 0.25f;
+    for (int l = 1; l < kFlowLevels; ++l) {
+        __syncthreads();
+        const int s = 16 >> (l - 1), n = s >> 1;
+        const float* src = t[(l - 1) & 1];
+        float* dst = t[l & 1];
+        if (tx < n && ty < n) {
+            const int cw = lw >> l;
+            const int gx = blockIdx.x * n + tx, gy = blockIdx.y * n + ty;
+            float* o = po.lev[l] + (static_cast<int64_t>(gy) * cw + gx) * 3;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float a = src[((2 * ty) * s + 2 * tx) * 3 + k];
+                const float b = src[((2 * ty) * s + 2 * tx + 1) * 3 + k];
+                const float c = src[((2 * ty + 1) * s + 2 * tx) * 3 + k];
+                const float e = src[((2 * ty + 1) * s + 2 * tx + 1) * 3 + k];
+                const float v = ((a + b) + (c + e)) * 0.25f;
+                o[k] = v;
+                dst[(ty * n + tx) * 3 + k] = v;
+            }
+        }
     }
 }
 
@@ -224,28 +270,10 @@ __global__ void up2_kernel(const float* __restrict__ in, int sw, int sh, float* 
         return;
     in += blockIdx.z * bs;
     out += blockIdx.z * bs;
-    const int64_t sp = static_cast<int64_t>(sw) * sh, dp = static_cast<int64_t>(dw) * dh;
-    float sx = (static_cast<float>(x) + 0.5f) * 0.5f - 0.5f;
-    float sy = (static_cast<float>(y) + 0.5f) * 0.5f - 0.5f;
-    if (sx < 0.0f)
-        sx = 0.0f;
-    if (sy < 0.0f)
-        sy = 0.0f;
-    int x0 = static_cast<int>(floorf(sx)), y0 = static_cast<int>(floorf(sy));
-    if (x0 > sw - 1)
-        x0 = sw - 1;
-    if (y0 > sh - 1)
-        y0 = sh - 1;
-    const int x1 = x0 + 1 < sw ? x0 + 1 : sw - 1;
-    const int y1 = y0 + 1 < sh ? y0 + 1 : sh - 1;
-    const float lx = sx - static_cast<float>(x0), ly = sy - static_cast<float>(y0);
+    const int64_t dp = static_cast<int64_t>(dw) * dh;
 #pragma unroll
-    for (int ch = 0; ch < 2; ++ch) {
-        const float* s = in + ch * sp;
-        const float top = (1.0f - lx) * s[static_cast<int64_t>(y0) * sw + x0] + lx * s[static_cast<int64_t>(y0) * sw + x1];
-        const float bot = (1.0f - lx) * s[static_cast<int64_t>(y1) * sw + x0] + lx * s[static_cast<int64_t>(y1) * sw + x1];
-        out[ch * dp + static_cast<int64_t>(y) * dw + x] = ((1.0f - ly) * top + ly * bot) * 2.0f;
-    }
+    for (int ch = 0; ch < 2; ++ch)
+        out[ch * dp + static_cast<int64_t>(y) * dw + x] = up2_sample(in, sw, sh, x, y, ch);
 }
 
 // One thread per pixel, 64 per block: the pixel's 81 cost values are first
@@ -313,9 +341,11 @@ __global__ void __launch_bounds__(kDecodeThreads) decode_kernel(const float* __r
 }
 
 // confidence-weighted 3x3 mean (edge clamp) of the refinement, added to the
-// upsampled coarser flow (zero at the coarsest level)
+// upsampled coarser flow (zero at the coarsest level): read from `up`, or
+// with `coarse` non-null upsampled here from the cw x chh coarser flow
 __global__ void smooth_kernel(const float* __restrict__ res, const float* __restrict__ conf,
-    const float* __restrict__ up, float* __restrict__ out, int lw, int lh, int64_t bs)
+    const float* __restrict__ up, float* __restrict__ out, int lw, int lh, int64_t bs,
+    const float* __restrict__ coarse, int cw, int chh)
 {
     pdl_enter();
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -344,8 +374,15 @@ __global__ void smooth_kernel(const float* __restrict__ res, const float* __rest
     }
     const int64_t p = static_cast<int64_t>(y) * lw + x;
     const float den = sw + kEps;
-    const float ux = up ? up[p] : 0.0f;
-    const float uy = up ? up[plane + p] : 0.0f;
+    float ux = 0.0f, uy = 0.0f;
+    if (coarse) {
+        coarse += blockIdx.z * bs;
+        ux = up2_sample(coarse, cw, chh, x, y, 0);
+        uy = up2_sample(coarse, cw, chh, x, y, 1);
+    } else if (up) {
+        ux = up[p];
+        uy = up[plane + p];
+    }
     out[p] = ux + __fdiv_rn(sx, den);
     out[plane + p] = uy + __fdiv_rn(sy, den);
 }
@@ -455,23 +492,24 @@ size_t flow_feature_scratch_floats(const FlowDims& d)
 }
 
 cudaError_t launch_flow_features(const float* img, int w, int h, const FlowDims& d, float* feats, float* scratch,
-    cudaStream_t st, int* launches)
+    cudaStream_t st, int* launches, const float* full, int FW, int FH)
 {
-    const dim3 b(32, 8);
     float* lev[kFlowLevels];
     size_t off = 0;
+    PyrOut po{};
     for (int l = 0; l < kFlowLevels; ++l) {
         lev[l] = scratch + off;
+        po.lev[l] = lev[l];
         off += static_cast<size_t>(d.lw[l]) * d.lh[l] * 3;
     }
-    cudaError_t e = launch_pdl(level0_image_kernel, g2(d.lw[0], d.lh[0], b), b, 0, st, img, w, h, lev[0], d.lw[0],
-        d.lh[0]);
+    po.lw0 = d.lw[0];
+    po.lh0 = d.lh[0];
+    if (d.lw[0] % 16 != 0 || d.lh[0] % 16 != 0 || (d.lw[0] >> (kFlowLevels - 1)) * 16 != d.lw[0])
+        return cudaErrorInvalidValue;  // flow_dims pads the frame to a multiple of 64: never
+    const dim3 g(static_cast<unsigned>(d.lw[0] / 16), static_cast<unsigned>(d.lh[0] / 16));
+    cudaError_t e = full ? launch_pdl(pyramid_kernel<true>, g, dim3(256), 0, st, img, w, h, full, FW, FH, po)
+                         : launch_pdl(pyramid_kernel<false>, g, dim3(256), 0, st, img, w, h, full, FW, FH, po);
     int nl = 1;
-    for (int l = 1; l < kFlowLevels; ++l) {
-        if (e == cudaSuccess)
-            e = launch_pdl(pool2_kernel, g2(d.lw[l], d.lh[l], b), b, 0, st, lev[l - 1], lev[l], d.lw[l], d.lh[l]);
-        ++nl;
-    }
     FeatLevels fl{};
     fl.block0[0] = 0;
     for (int k = 0; k < kFlowLevels; ++k) {
@@ -565,20 +603,22 @@ cudaError_t launch_flow_pair(const float* featA, int64_t sA, const float* featB,
         const float* fa = featA + d.off[l];
         const float* fb = featB + d.off[l];
         const float* upp = nullptr;
+        const float* coarse = nullptr;  // the tensor-core form upsamples the coarser flow where it reads it
         const float* fb_use = fb;
         int64_t sb_use = sB;
         if (l < kFlowLevels - 1) {
-            dim3 g = g2(lw, lh, b);
-            g.z = 2;
-            if ((e = launch_pdl(up2_kernel, g, b, 0, st, sm[cur], d.lw[l + 1], d.lh[l + 1], up, lw, lh, bs)) !=
-                cudaSuccess)
-                return e;
-            ++nl;
-            upp = up;
             if (tc) {
-                e = launch_warp_to_chunked(fb, up, tc->warped, tc->scales, 2, lc, lh, lw, sB, bs,
-                    static_cast<int64_t>(tc_warped_bytes(d)), tc->bf16, st);
+                coarse = sm[cur];
+                e = launch_warp_to_chunked(fb, coarse, tc->warped, tc->scales, 2, lc, lh, lw, sB, bs,
+                    static_cast<int64_t>(tc_warped_bytes(d)), tc->bf16, st, d.lw[l + 1], d.lh[l + 1]);
             } else {
+                dim3 g = g2(lw, lh, b);
+                g.z = 2;
+                if ((e = launch_pdl(up2_kernel, g, b, 0, st, sm[cur], d.lw[l + 1], d.lh[l + 1], up, lw, lh, bs)) !=
+                    cudaSuccess)
+                    return e;
+                ++nl;
+                upp = up;
                 e = launch_warp_op(fb, up, warped, 2, lc, lh, lw, st, sB, bs, bs);
                 fb_use = warped;
                 sb_use = bs;
@@ -618,7 +658,9 @@ cudaError_t launch_flow_pair(const float* featA, int64_t sA, const float* featB,
         cur ^= 1;
         dim3 g = g2(lw, lh, b);
         g.z = 2;
-        if ((e = launch_pdl(smooth_kernel, g, b, 0, st, raw, raw + 2 * plane, upp, sm[cur], lw, lh, bs)) != cudaSuccess)
+        const int cw = coarse ? d.lw[l + 1] : 0, chh = coarse ? d.lh[l + 1] : 0;
+        if ((e = launch_pdl(smooth_kernel, g, b, 0, st, raw, raw + 2 * plane, upp, sm[cur], lw, lh, bs, coarse, cw,
+                 chh)) != cudaSuccess)
             return e;
         ++nl;
     }

@@ -78,8 +78,10 @@ cudaError_t launch_to_chunked_levels(const float* const* in, void* const* out, c
     const int* W, int n, const float* scale, bool bf16, cudaStream_t st);
 // custom::Warp (single precision) with the chunked 16-bit layout as output;
 // batch n reads in + n * sin, flow + n * sfl (floats), writes out + n * sout_bytes.
+// With cw, chh > 0 the flow is the flow estimator's coarser cw x chh level,
+// upsampled 2x where it is read (the estimator's upsampled flow's values).
 cudaError_t launch_warp_to_chunked(const float* in, const float* flow, void* out, const float* scale, int N, int C,
-    int H, int W, int64_t sin, int64_t sfl, int64_t sout_bytes, bool bf16, cudaStream_t st);
+    int H, int W, int64_t sin, int64_t sfl, int64_t sout_bytes, bool bf16, cudaStream_t st, int cw = 0, int chh = 0);
 
 // ---- learned flow upsampler (vsc_upsampler.cu, vsc_upsampler_tc.cu) ----------------
 // Layer table: input / output channels, offsets of the weights (laid out
@@ -133,11 +135,6 @@ cudaError_t launch_consist_wt(Img ai, Img ci, Img wt, float beta, float gamma, c
 cudaError_t launch_bilinear(Img in, Img out, cudaStream_t st);
 // launch_bilinear for n 3-channel images in one launch per 16 (same bits)
 cudaError_t launch_bilinear_group(const Img* in, const Img* out, int n, cudaStream_t st);
-// Nearest-neighbour resize of a float HWC3 image for the FLOWDOWNSCALE mode
-// (the reference scales the QImage with Qt::FastTransformation,
-// flowmodel.cpp:126-133): source = min(iw-1, ((2x+1)*iw) / (2*ow)).
-cudaError_t launch_resize_nearest(const float* in, int iw, int ih, float* out, int ow, int oh, cudaStream_t st);
-
 // Solver.
 //   kSolverExact: kernel_consist_out's expression, bit for bit; workspace:
 //                 the Laplacian of the processed image, two momentum images
@@ -248,8 +245,10 @@ FlowDims flow_dims(int w, int h);
 cudaError_t flow_upload_weights();
 // scratch for one frame's feature extraction: level images
 size_t flow_feature_scratch_floats(const FlowDims& d);
+// With `full` non-null the w x h image is the nearest-neighbour resize of the
+// FW x FH frame `full` (FLOWDOWNSCALE) and `img` is not read.
 cudaError_t launch_flow_features(const float* img, int w, int h, const FlowDims& d, float* feats, float* scratch,
-    cudaStream_t st, int* launches);
+    cudaStream_t st, int* launches, const float* full = nullptr, int FW = 0, int FH = 0);
 // The tensor-core form of the estimator's correlations: each frame's
 // features also kept in the chunked 16-bit layout (level l at byte offset
 // tc_level_offset(d, l)), scaled by scales[0] (|f| <= 1 after the features'

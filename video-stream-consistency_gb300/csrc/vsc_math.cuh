@@ -80,6 +80,32 @@ __device__ __forceinline__ void pdl_enter()
 
 __device__ __forceinline__ int64_t pix_index(int x, int y, int w) { return static_cast<int64_t>(y) * w + x; }
 
+// The flow estimator's coarse-to-fine step: channel ch of the 2-channel
+// planar sw x sh flow `in` upsampled 2x at pixel (x, y) (half-pixel centres,
+// clamped taps) and doubled -- the value the estimator's upsampled flow holds
+// there, computed where it is used.
+__device__ __forceinline__ float up2_sample(const float* __restrict__ in, int sw, int sh, int x, int y, int ch)
+{
+    float sx = (static_cast<float>(x) + 0.5f) * 0.5f - 0.5f;
+    float sy = (static_cast<float>(y) + 0.5f) * 0.5f - 0.5f;
+    if (sx < 0.0f)
+        sx = 0.0f;
+    if (sy < 0.0f)
+        sy = 0.0f;
+    int x0 = static_cast<int>(floorf(sx)), y0 = static_cast<int>(floorf(sy));
+    if (x0 > sw - 1)
+        x0 = sw - 1;
+    if (y0 > sh - 1)
+        y0 = sh - 1;
+    const int x1 = x0 + 1 < sw ? x0 + 1 : sw - 1;
+    const int y1 = y0 + 1 < sh ? y0 + 1 : sh - 1;
+    const float lx = sx - static_cast<float>(x0), ly = sy - static_cast<float>(y0);
+    const float* s = in + static_cast<int64_t>(ch) * sw * sh;
+    const float top = (1.0f - lx) * s[static_cast<int64_t>(y0) * sw + x0] + lx * s[static_cast<int64_t>(y0) * sw + x1];
+    const float bot = (1.0f - lx) * s[static_cast<int64_t>(y1) * sw + x0] + lx * s[static_cast<int64_t>(y1) * sw + x1];
+    return ((1.0f - ly) * top + ly * bot) * 2.0f;
+}
+
 // One output pixel of kernel_bilinear (flowconsistency.cu:50-75): the c
 // channels of the iw x ih image `in` sampled at (ox * iw / ow, oy * ih / oh),
 // taps clamped to the last row and column, in the reference's expression.

@@ -647,23 +647,6 @@ __global__ void __launch_bounds__(256) fused_front_rgba_kernel(const uint32_t* _
     }
 }
 
-__global__ void resize_nearest_kernel(const float* __restrict__ in, int iw, int ih, float* __restrict__ out, int ow,
-    int oh)
-{
-    pdl_enter();
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= ow || y >= oh)
-        return;
-    const int sx = min(iw - 1, static_cast<int>(((2 * static_cast<int64_t>(x) + 1) * iw) / (2 * static_cast<int64_t>(ow))));
-    const int sy = min(ih - 1, static_cast<int>(((2 * static_cast<int64_t>(y) + 1) * ih) / (2 * static_cast<int64_t>(oh))));
-    const float* s = in + pix_index(sx, sy, iw) * 3;
-    float* d = out + pix_index(x, y, ow) * 3;
-    d[0] = s[0];
-    d[1] = s[1];
-    d[2] = s[2];
-}
-
 inline dim3 grid2d(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h + b.y - 1) / b.y); }
 
 }  // namespace
@@ -858,15 +841,6 @@ cudaError_t launch_fused_front_rgba(const uint8_t* o0, const uint8_t* o1, const 
     else
         fused_front_rgba_kernel<false><<<grid2d(w, h, b), b, 0, st>>>(u(o0), u(o1), u(o2), u(p0), u(p1), u(p2),
             last_stab, flow_fwd, flow_bwd, fc, adap_pr, cons_wt, w, h, alpha, beta, gamma);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_resize_nearest(const float* in, int iw, int ih, float* out, int ow, int oh, cudaStream_t st)
-{
-    const dim3 b(32, 8);
-    const cudaError_t e = launch_pdl(resize_nearest_kernel, grid2d(ow, oh, b), b, 0, st, in, iw, ih, out, ow, oh);
-    if (e != cudaSuccess)
-        return e;
     return cudaGetLastError();
 }
 
