@@ -11,11 +11,12 @@
 // over K = channels (padded to a multiple of 16 with zeros), accumulated in
 // Tensor Memory; both operands come from shared memory, staged by one 5-D TMA
 // load each from the features in a "chunked" layout
-//     [n][y][c / 8][x][c % 8]  (16-bit elements, channels padded to Cp),
-// which the TMA box {8, pixels, Cp / 8} turns directly into the operand's
-// 8-row x 16-byte core-matrix grid (K-adjacent core matrices pixels x 16 B
-// apart, M/N-adjacent ones 128 B apart).  Rows y + dy and columns outside
-// the map are zero-filled by the TMA, which is the operator's zero outside.
+//     [n][y][c / 16][x][c % 16]  (16-bit elements, channels padded to Cp),
+// which the TMA box {16, pixels, Cp / 16} with the 32-byte swizzle turns
+// directly into the K-major operand layout of that swizzle: one chunk plane
+// per MMA K step (pixels x 32 bytes), every box row one 32-byte L2 sector.
+// Rows y + dy and columns outside the map are zero-filled by the TMA, which
+// is the operator's zero outside.
 // The epilogue reads each warp's 32 lanes x 48 columns of D_dy out of Tensor
 // Memory, stages them in shared memory and picks the diagonal band.
 //
@@ -75,7 +76,7 @@ __host__ uint32_t tc_smem_need(int cp, int sa, int sb, int g)
 // epilogue groups are given up in that order (208 channels: 1, 2, 2).
 __host__ TcPlan tc_plan(int cp)
 {
-    TcPlan p{2, 4, kMaxEpiGroups, 0};
+    TcPlan p{kMaxStagesA, kMaxStagesB, kMaxEpiGroups, 0};
     while (tc_smem_need(cp, p.stages_a, p.stages_b, p.groups) > static_cast<uint32_t>(kTcSmemLimit)) {
         if (p.stages_b > 2)
             --p.stages_b;
@@ -251,8 +252,9 @@ __global__ void __launch_bounds__((2 + 4 * kMaxEpiGroups) * 32, 1)
                     const uint32_t a0 = ptx::smem_u32(sh.a + sa * sh.a_stride), b0 = ptx::smem_u32(sh.b + sb * sh.b_stride);
                     const uint32_t dcol = tmem + sd * kDStride;
                     for (int kk = 0; kk < Cp / 16; ++kk) {
-                        const uint64_t ad = ptx::umma_desc_kmajor(a0 + kk * 2 * kTcM * 16, kTcM * 16, 128);
-                        const uint64_t bd = ptx::umma_desc_kmajor(b0 + kk * 2 * kTcN * 16, kTcN * 16, 128);
+                        // K step kk = the tile's chunk plane kk (rows x 32 bytes, swizzled)
+                        const uint64_t ad = ptx::umma_desc_kmajor_sw32(a0 + kk * kTcM * 32);
+                        const uint64_t bd = ptx::umma_desc_kmajor_sw32(b0 + kk * kTcN * 32);
                         ptx::umma_f16(dcol, ad, bd, idesc, kk > 0);
                     }
                     ptx::umma_commit(&sh.full_d[sd]);   // accumulator ready
@@ -379,6 +381,14 @@ __global__ void scales_kernel(const unsigned int* __restrict__ maxbits, float* _
     scales[i] = s;
 }
 
+// The chunked 16-bit layout [n][y][c / 16][x][c % 16]: row (n, y) of the
+// map, 16-channel chunks, each pixel's 16 channels 32 bytes.  A thread that
+// packs 8 channels (chunk8 q of `chunks8`) writes the uint4 at this index.
+__device__ __forceinline__ int64_t chunked_index(int64_t row, int q, int x, int W, int chunks8)
+{
+    return ((row * (chunks8 >> 1) + (q >> 1)) * W + x) * 2 + (q & 1);
+}
+
 template <bool kBf16>
 __device__ __forceinline__ uint32_t pack2(float a, float b)
 {
@@ -391,10 +401,10 @@ __device__ __forceinline__ uint32_t pack2(float a, float b)
     }
 }
 
-// NCHW float -> chunked 16-bit [n][y][c / 8][x][c % 8], scaled, zero-padded
-// to chunks * 8 channels.  One thread per pixel and chunk of 8 channels
-// (the small pyramid levels have few pixels and up to 25 chunks); reads
-// coalesced along x for every channel, one 16-byte store.
+// NCHW float -> chunked 16-bit [n][y][c / 16][x][c % 16], scaled,
+// zero-padded to chunks * 8 channels.  One thread per pixel and 8 channels
+// (the small pyramid levels have few pixels and up to 26 such groups);
+// reads coalesced along x for every channel, one 16-byte store.
 template <bool kBf16>
 __global__ void to_chunked_kernel(const float* __restrict__ in, uint4* __restrict__ out, const float* __restrict__ scale,
     int C, int H, int W, int chunks)
@@ -415,7 +425,7 @@ __global__ void to_chunked_kernel(const float* __restrict__ in, uint4* __restric
         const int c = q * 8 + j;
         v[j] = c < C ? src[c * HW] * s : 0.0f;
     }
-    out[((static_cast<int64_t>(n) * H + y) * chunks + q) * W + x] = make_uint4(pack2<kBf16>(v[0], v[1]),
+    out[chunked_index(static_cast<int64_t>(n) * H + y, q, x, W, chunks)] = make_uint4(pack2<kBf16>(v[0], v[1]),
         pack2<kBf16>(v[2], v[3]), pack2<kBf16>(v[4], v[5]), pack2<kBf16>(v[6], v[7]));
 }
 
@@ -452,7 +462,7 @@ __global__ void to_chunked_levels_kernel(const __grid_constant__ ChunkLevels cl,
         const int c = q * 8 + j;
         v[j] = c < C ? src[static_cast<int64_t>(c) * HW] * s : 0.0f;
     }
-    cl.out[l][(static_cast<int64_t>(y) * chunks + q) * W + x] = make_uint4(pack2<kBf16>(v[0], v[1]),
+    cl.out[l][chunked_index(y, q, x, W, chunks)] = make_uint4(pack2<kBf16>(v[0], v[1]),
         pack2<kBf16>(v[2], v[3]), pack2<kBf16>(v[4], v[5]), pack2<kBf16>(v[6], v[7]));
 }
 
@@ -513,24 +523,26 @@ __global__ void warp_to_chunked_kernel(const float* __restrict__ in, const float
         }
         v[j] = val * s;
     }
-    out[n * sout + (static_cast<int64_t>(y) * chunks + q) * W + x] =
+    out[n * sout + chunked_index(y, q, x, W, chunks)] =
         make_uint4(pack2<kBf16>(v[0], v[1]), pack2<kBf16>(v[2], v[3]), pack2<kBf16>(v[4], v[5]), pack2<kBf16>(v[6], v[7]));
 }
 
-// 5-D map over a chunked tensor: {c % 8, x, c / 8, y, n}, box {8, pixels, cp / 8, 1, 1}.
+// 5-D map over a chunked tensor: {c % 16, x, c / 16, y, n}, box {16, pixels,
+// cp / 16, 1, 1}, 32-byte swizzle: each box row is one 32-byte sector and
+// the tile lands in the operand layout umma_desc_kmajor_sw32 describes.
 bool encode_chunked_map(CUtensorMap* m, const void* base, int N, int H, int W, int cp, int box_pixels)
 {
     EncodeTiledFn fn = tensor_map_encoder();
     if (!fn)
         return false;
-    const cuuint64_t q = static_cast<cuuint64_t>(cp / 8);
-    const cuuint64_t dims[5] = {8, static_cast<cuuint64_t>(W), q, static_cast<cuuint64_t>(H),
+    const cuuint64_t q = static_cast<cuuint64_t>(cp / 16);
+    const cuuint64_t dims[5] = {16, static_cast<cuuint64_t>(W), q, static_cast<cuuint64_t>(H),
         static_cast<cuuint64_t>(N)};
-    const cuuint64_t strides[4] = {16, static_cast<cuuint64_t>(W) * 16, q * W * 16, static_cast<cuuint64_t>(H) * q * W * 16};
-    const cuuint32_t box[5] = {8, static_cast<cuuint32_t>(box_pixels), static_cast<cuuint32_t>(q), 1, 1};
+    const cuuint64_t strides[4] = {32, static_cast<cuuint64_t>(W) * 32, q * W * 32, static_cast<cuuint64_t>(H) * q * W * 32};
+    const cuuint32_t box[5] = {16, static_cast<cuuint32_t>(box_pixels), static_cast<cuuint32_t>(q), 1, 1};
     const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT16, 5, const_cast<void*>(base), dims, strides, box, estr,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 

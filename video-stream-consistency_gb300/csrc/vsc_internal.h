@@ -62,7 +62,7 @@ size_t corr_tc_workspace_bytes(int N, int C, int H, int W);
 // From float NCHW (scaled per tensor, converted in the workspace).
 cudaError_t launch_corr_tc(const float* f1, const float* f2, float* out, int N, int C, int H, int W, int md,
     bool bf16, void* workspace, cudaStream_t st);
-// From operands already in the chunked 16-bit layout [n][y][c / 8][x][c % 8]
+// From operands already in the chunked 16-bit layout [n][y][c / 16][x][c % 16]
 // (Cp channels) with their scales (2 floats: f1, f2) on the device.
 cudaError_t launch_corr_tc_chunked(const void* f1c, const void* f2c, float* out, const float* scales, int N, int Cp,
     int H, int W, int md, bool bf16, cudaStream_t st);

@@ -114,6 +114,22 @@ __device__ __forceinline__ uint64_t umma_desc_kmajor(uint32_t smem_addr, uint32_
     return d;
 }
 
+// Shared-memory descriptor of a K-major operand in the 32-byte swizzle layout
+// (what a TMA load with CU_TENSOR_MAP_SWIZZLE_32B and a 32-byte inner box
+// writes): rows of 32 bytes (16 K-elements of 16 bits, one MMA's K), 8-row
+// groups 256 bytes apart (the stride offset); the leading offset is unused
+// because an MMA's K spans one swizzle row.  Layout type 6 = 32-byte
+// swizzle in bits [61, 64); the start must sit on a 256-byte boundary.
+__device__ __forceinline__ uint64_t umma_desc_kmajor_sw32(uint32_t smem_addr)
+{
+    uint64_t d = static_cast<uint64_t>((smem_addr & 0x3FFFFu) >> 4);
+    d |= static_cast<uint64_t>(1) << 16;           // leading offset (unused): 16 bytes
+    d |= static_cast<uint64_t>(256 >> 4) << 32;    // stride offset: 8 rows x 32 bytes
+    d |= static_cast<uint64_t>(1) << 46;
+    d |= static_cast<uint64_t>(6) << 61;
+    return d;
+}
+
 // Instruction descriptor of kind::f16 with an FP32 accumulator, both
 // operands K-major: D format in [4,6) (1 = F32), A and B formats in [7,10)
 // and [10,13) (0 = F16, 1 = BF16; A and B always the same type here),
