@@ -1223,16 +1223,22 @@ cudaError_t enqueue_pre_solve(vsc_stabilizer* s, const vsc_hyper_params& hp, Lev
     mark(s, kEvFlow);
     float* ls_in = s->last_stab[s->ls_cur];
     float* ls_out = s->last_stab[s->ls_cur ^ 1];
+    // the pyramid's first level (videostabilizer.cpp:203-217) comes out of the
+    // front pass when it is an exact half (same values as pyr_down3)
+    const bool down = L > 1 && !s->occlusion && front_down_fusable(s->w, s->h, s->lw[1], s->lh[1]);
+    float* dP = down ? s->pyrP[1] : nullptr;
+    float* dA = down ? s->pyrA[1] : nullptr;
+    float* dW = down ? s->pyrW[1] : nullptr;
     if (front_samples_small_flows(s)) {
         // the upsampling of both flows happens inside the front pass
         const int64_t fs = static_cast<int64_t>(s->fw) * s->fh * 3;
         run(launch_fused_front(s->orig[s0], s->orig[s1], s->orig[s2], s->proc[s0], s->proc[s1], s->proc[s2], ls_in,
             s->flow_small, s->flow_small + fs, 3, s->adap_pr, s->cons_wt, s->w, s->h, hp.alpha, hp.beta, hp.gamma,
-            st, false, s->fw, s->fh));
+            st, false, s->fw, s->fh, dP, dA, dW, s->lw[1], s->lh[1]));
     } else {
         run(launch_fused_front(s->orig[s0], s->orig[s1], s->orig[s2], s->proc[s0], s->proc[s1], s->proc[s2], ls_in,
             s->flow_fwd, s->flow_bwd, s->fc, s->adap_pr, s->cons_wt, s->w, s->h, hp.alpha, hp.beta, hp.gamma, st,
-            s->occlusion));
+            s->occlusion, 0, 0, dP, dA, dW, s->lw[1], s->lh[1]));
     }
     ++nl;
 
@@ -1250,6 +1256,8 @@ cudaError_t enqueue_pre_solve(vsc_stabilizer* s, const vsc_hyper_params& hp, Lev
         A[j] = s->pyrA[j];
         W[j] = s->pyrW[j];
         O[j] = s->pyrO[j];
+        if (j == 1 && down)
+            continue;  // written by the front pass
         run(launch_pyr_down3(P[j - 1], A[j - 1], W[j - 1], s->lw[j - 1], s->lh[j - 1], P[j], A[j], W[j], s->lw[j],
             s->lh[j], st));
         ++nl;

@@ -218,10 +218,15 @@ cudaError_t run_solver_noalloc(const float* P, const float* A, const float* Wt, 
 // are the 3-channel fw x fh flows that the step upsamples bilinearly to
 // w x h, sampled where they are used (same outputs as upsampling them first);
 // not with the occlusion mask.
+// With down_p non-null (no occlusion mask, front_down_fusable) it also writes
+// the next pyramid level's P, A, Wt (ow x oh = w/2 x h/2), pyr_down3's values.
 cudaError_t launch_fused_front(const float* o0, const float* o1, const float* o2, const float* p0, const float* p1,
     const float* p2, const float* last_stab, const float* flow_fwd, const float* flow_bwd, int fc, float* adap_pr,
     float* cons_wt, int w, int h, float alpha, float beta, float gamma, cudaStream_t st, bool occlusion_mask = false,
-    int fw = 0, int fh = 0);
+    int fw = 0, int fh = 0, float* down_p = nullptr, float* down_a = nullptr, float* down_w = nullptr, int ow = 0,
+    int oh = 0);
+// the pyramid's first downsampling can be fused into the front pass (exact 2x)
+bool front_down_fusable(int w, int h, int ow, int oh);
 // fused_front on the RGBA8 words of the six frames (4-byte aligned, w x h
 // words each); same outputs bit for bit
 cudaError_t launch_fused_front_rgba(const uint8_t* o0, const uint8_t* o1, const uint8_t* o2, const uint8_t* p0,

@@ -536,49 +536,100 @@ __global__ void pyr_down3_kernel(const float* __restrict__ P, const float* __res
 // the step upsamples bilinearly to w x h (FLOWDOWNSCALE); each pixel samples
 // them with flow_upsampled_uv, the value the upsampled flow holds there, so
 // the full-size flows are neither written nor read.
-template <bool kOcc, bool kFast, bool kHalf = false>
+// kDown (w and h even): also the next pyramid level, w/2 x h/2, of the
+// processed frame, adapCmbPr and consWt (pyr_down3_kernel's bilinear_px
+// downsampling, whose taps are exactly the 2 x 2 group (2 ox .. 2 ox + 1,
+// 2 oy .. 2 oy + 1) with zero fractions): the block's 32 x 8 pixels pass
+// their values through shared memory and one thread per 2 x 2 group
+// evaluates bilinear_px's expression on them.  The same bits as the
+// separate pass, without reading the three full-size images again.
+struct FrontDown {
+    float* P;
+    float* A;
+    float* W;
+    int ow, oh;
+};
+
+template <bool kOcc, bool kFast, bool kHalf = false, bool kDown = false>
 __global__ void __launch_bounds__(256) fused_front_kernel(const float* __restrict__ o0,
     const float* __restrict__ o1,
     const float* __restrict__ o2, const float* __restrict__ p0, const float* __restrict__ p1,
     const float* __restrict__ p2, const float* __restrict__ ls, const float* __restrict__ ffwd,
     const float* __restrict__ fbwd, int fc, float* __restrict__ adap_pr, float* __restrict__ cons_wt, int w, int h,
-    float alpha, float beta, float gamma, int fw = 0, int fh = 0)
+    float alpha, float beta, float gamma, int fw, int fh, FrontDown dn)
 {
     static_assert(!(kHalf && kOcc), "the occlusion mask samples the flows at warped positions");
+    static_assert(!(kDown && kOcc), "the downsampling is fused into the unmasked pass only");
     pdl_enter();
     using I = typename std::conditional<kFast, int, int64_t>::type;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= w || y >= h)
+    const bool in = x < w && y < h;
+    if (!kDown && !in)
         return;
-    WarpTapT<I> tb, tf;
-    if (kHalf) {
-        float u, v;
-        flow_upsampled_uv(fbwd, fw, fh, w, h, x, y, u, v);
-        tb = warp_tap_uv<I>(u, v, x, y, w, h);
-        flow_upsampled_uv(ffwd, fw, fh, w, h, x, y, u, v);
-        tf = warp_tap_uv<I>(u, v, x, y, w, h);
-    } else {
-        tb = warp_tap<I>(fbwd, fc, x, y, w, h);
-        tf = warp_tap<I>(ffwd, fc, x, y, w, h);
-    }
-    float mp = 1.0f, mn = 1.0f;
-    if (kOcc) {
-        mp = occl_check(fbwd, ffwd, fc, x, y, w, h);
-        mn = occl_check(ffwd, fbwd, fc, x, y, w, h);
-    }
-    const I o = (static_cast<I>(y) * w + x) * 3;
+    float pv[3], av[3], wv[3];  // kDown: this pixel's P, adapCmbPr, consWt
+    if (in) {
+        WarpTapT<I> tb, tf;
+        if (kHalf) {
+            float u, v;
+            flow_upsampled_uv(fbwd, fw, fh, w, h, x, y, u, v);
+            tb = warp_tap_uv<I>(u, v, x, y, w, h);
+            flow_upsampled_uv(ffwd, fw, fh, w, h, x, y, u, v);
+            tf = warp_tap_uv<I>(u, v, x, y, w, h);
+        } else {
+            tb = warp_tap<I>(fbwd, fc, x, y, w, h);
+            tf = warp_tap<I>(ffwd, fc, x, y, w, h);
+        }
+        float mp = 1.0f, mn = 1.0f;
+        if (kOcc) {
+            mp = occl_check(fbwd, ffwd, fc, x, y, w, h);
+            mn = occl_check(ffwd, fbwd, fc, x, y, w, h);
+        }
+        const I o = (static_cast<I>(y) * w + x) * 3;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const float pwi = warp_sample(o0, tb, c);
-        const float pwp = warp_sample(p0, tb, c);
-        const float nwi = warp_sample(o2, tf, c);
-        const float nwp = warp_sample(p2, tf, c);
-        const float lsw = warp_sample(ls, tb, c);
-        const float ci = o1[o + c];
-        const Comb r = adap_comb_px<kFast>(ci, p1[o + c], pwi, pwp, nwi, nwp, lsw, alpha, mp, mn, kOcc);
-        adap_pr[o + c] = r.apr;
-        cons_wt[o + c] = consist_wt_px<kFast>(ci, r.ain, beta, gamma);
+        for (int c = 0; c < 3; ++c) {
+            const float pwi = warp_sample(o0, tb, c);
+            const float pwp = warp_sample(p0, tb, c);
+            const float nwi = warp_sample(o2, tf, c);
+            const float nwp = warp_sample(p2, tf, c);
+            const float lsw = warp_sample(ls, tb, c);
+            const float ci = o1[o + c];
+            const float cp = p1[o + c];
+            const Comb r = adap_comb_px<kFast>(ci, cp, pwi, pwp, nwi, nwp, lsw, alpha, mp, mn, kOcc);
+            const float wt = consist_wt_px<kFast>(ci, r.ain, beta, gamma);
+            adap_pr[o + c] = r.apr;
+            cons_wt[o + c] = wt;
+            pv[c] = cp;
+            av[c] = r.apr;
+            wv[c] = wt;
+        }
+    }
+    if (kDown) {
+        __shared__ float sd[8][32][9];
+        const int tx = threadIdx.x, ty = threadIdx.y;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            sd[ty][tx][c] = in ? pv[c] : 0.0f;
+            sd[ty][tx][3 + c] = in ? av[c] : 0.0f;
+            sd[ty][tx][6 + c] = in ? wv[c] : 0.0f;
+        }
+        __syncthreads();
+        if (in && !(tx & 1) && !(ty & 1)) {
+            const int ox = x >> 1, oy = y >> 1;  // < w / 2, h / 2
+            // bilinear_px at (ox, oy): taps 2 ox, 2 ox + 1 and 2 oy, 2 oy + 1 (inside: w, h even)
+            const float xx = static_cast<float>(ox) * static_cast<float>(w) / static_cast<float>(dn.ow);
+            const float yy = static_cast<float>(oy) * static_cast<float>(h) / static_cast<float>(dn.oh);
+            const float fx = xx - static_cast<float>(x), fy = yy - static_cast<float>(y);
+            const int64_t q = (static_cast<int64_t>(oy) * dn.ow + ox) * 3;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                const float v00 = sd[ty][tx][k], v10 = sd[ty][tx + 1][k];
+                const float v01 = sd[ty + 1][tx][k], v11 = sd[ty + 1][tx + 1][k];
+                const float v = v00 * (1 - fx) * (1 - fy) + v10 * fx * (1 - fy) + v01 * (1 - fx) * fy + v11 * fx * fy;
+                float* dst = k < 3 ? dn.P : k < 6 ? dn.A : dn.W;
+                dst[q + k % 3] = v;
+            }
+        }
     }
 }
 
@@ -810,21 +861,36 @@ static bool front_fast_ok(int w, int h, int fc, float alpha, float beta, float g
            std::fabs(gamma) <= 1e30f;
 }
 
+bool front_down_fusable(int w, int h, int ow, int oh)
+{
+    return w % 2 == 0 && h % 2 == 0 && ow == w / 2 && oh == h / 2 && static_cast<int64_t>(ow) * w < (int64_t{1} << 24) &&
+           static_cast<int64_t>(oh) * h < (int64_t{1} << 24);
+}
+
 cudaError_t launch_fused_front(const float* o0, const float* o1, const float* o2, const float* p0, const float* p1,
     const float* p2, const float* last_stab, const float* flow_fwd, const float* flow_bwd, int fc, float* adap_pr,
     float* cons_wt, int w, int h, float alpha, float beta, float gamma, cudaStream_t st, bool occlusion_mask, int fw,
-    int fh)
+    int fh, float* down_p, float* down_a, float* down_w, int ow, int oh)
 {
     const dim3 b(32, 8);
     const bool half = fw > 0 && fh > 0;
-    if (half && (occlusion_mask || fc != 3))
+    const bool down = down_p != nullptr;
+    if ((half && (occlusion_mask || fc != 3)) || (down && (occlusion_mask || !front_down_fusable(w, h, ow, oh))))
         return cudaErrorInvalidValue;
     const bool fast = front_fast_ok(w, h, fc, alpha, beta, gamma);
-    auto k = half ? (fast ? fused_front_kernel<false, true, true> : fused_front_kernel<false, false, true>)
-                  : occlusion_mask ? (fast ? fused_front_kernel<true, true> : fused_front_kernel<true, false>)
-                                   : (fast ? fused_front_kernel<false, true> : fused_front_kernel<false, false>);
+    using K = decltype(&fused_front_kernel<false, false>);
+    K k;
+    if (occlusion_mask)
+        k = fast ? fused_front_kernel<true, true> : fused_front_kernel<true, false>;
+    else if (half)
+        k = down ? (fast ? fused_front_kernel<false, true, true, true> : fused_front_kernel<false, false, true, true>)
+                 : (fast ? fused_front_kernel<false, true, true> : fused_front_kernel<false, false, true>);
+    else
+        k = down ? (fast ? fused_front_kernel<false, true, false, true> : fused_front_kernel<false, false, false, true>)
+                 : (fast ? fused_front_kernel<false, true> : fused_front_kernel<false, false>);
+    const FrontDown dn{down_p, down_a, down_w, ow, oh};
     const cudaError_t el = launch_pdl(k, grid2d(w, h, b), b, 0, st, o0, o1, o2, p0, p1, p2, last_stab, flow_fwd,
-        flow_bwd, fc, adap_pr, cons_wt, w, h, alpha, beta, gamma, fw, fh);
+        flow_bwd, fc, adap_pr, cons_wt, w, h, alpha, beta, gamma, fw, fh, dn);
     return el != cudaSuccess ? el : cudaGetLastError();
 }
 
