@@ -78,6 +78,15 @@ __device__ __forceinline__ void pdl_enter()
     asm volatile("griddepcontrol.launch_dependents;" :::);
 }
 
+// Asks L2 for the line holding *p (a hint: no result, nothing waits for it).
+// A gather kernel issues it for its own pixel's position in each source
+// before the flow read, so the source lines come from DRAM while the flow
+// is in flight and the taps, near that position, find them in L2.
+__device__ __forceinline__ void prefetch_l2(const void* p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ int64_t pix_index(int x, int y, int w) { return static_cast<int64_t>(y) * w + x; }
 
 // The flow estimator's coarse-to-fine step: channel ch of the 2-channel

@@ -1010,11 +1010,35 @@ struct PlState {
 __device__ __forceinline__ float& f4(float4& v, int j) { return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w; }
 __device__ __forceinline__ float f4c(const float4& v, int j) { return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w; }
 
+// Neighbour tests of the planar step.  kernel_consist_out reads a neighbour as
+// +0 unless it lies in [0, w - 2] x [0, h - 2] (left: gx - 1 >= 0, right:
+// gx + 1 < w - 1, up: gy - 1 >= 0, down: gy + 1 < h - 1), so the only pixels of
+// the frame with a neighbour read as +0 are column 0 (left), columns w - 2 and
+// w - 1 (right), row 0 (up) and rows h - 2 and h - 1 (down); every other read
+// of a pixel inside the frame is of a pixel inside the frame.  Pixels outside
+// the frame (the ring of a border tile) are computed too, but no pixel inside
+// the frame reads them unmasked, so their values never reach the output.
+//   kPlAll:   an interior tile, no test.
+//   kPlLanes: a border tile of a frame whose width, like the tile origins, is
+//             a multiple of 4: column 0 is then column j = 0 of the thread
+//             with gx0 = 0 and columns w - 2, w - 1 are j = 2, 3 of the thread
+//             with gx0 = w - 4 (three selects a row); row 0 of a tile at
+//             oy = -8 is row 2 of warp 1 and rows h - 2, h - 1 of a tile at
+//             oy = h - 64 are rows 2, 3 of warp 10 (a select of a row's up or
+//             down neighbours in every warp, true only in that one).  A tile
+//             holding row 0, h - 2 or h - 1 elsewhere (frames of few rows)
+//             takes kPlEvery.  Same bits as kPlEvery for every pixel inside
+//             the frame, without its four tests a pixel.
+//   kPlEvery: every neighbour tested.
+enum { kPlAll, kPlLanes, kPlEvery };
+
 // One step of a thread's 4 x 6 block: the previous iterate's edge rows of the
 // neighbouring warps come from `src`, the new top and bottom rows go to `dst`.
-template <bool kAll>
+// zl / zr (kPlLanes): this thread holds column 0 / columns w - 4 .. w - 1;
+// zt / zb: its row 2 is row 0 / its rows 2 and 3 are rows h - 2 and h - 1.
+template <int kMode>
 __device__ __forceinline__ void pl_step(PlState& s, const float* src, float* dst, bool mom_on, float step, float mom,
-    int lane, int warp, int gx0, int gy0, int w, int h)
+    int lane, int warp, int gx0, int gy0, int w, int h, bool zl, bool zr, bool zt, bool zb)
 {
     const float4 up = *reinterpret_cast<const float4*>(&src[(warp * 2 + 1) * kPlPX + 4 * lane + 4]);
     const float4 dn = *reinterpret_cast<const float4*>(&src[((warp + 2) * 2) * kPlPX + 4 * lane + 4]);
@@ -1028,19 +1052,29 @@ __device__ __forceinline__ void pl_step(PlState& s, const float* src, float* dst
 #pragma unroll
     for (int r = 0; r < kPlRPT; ++r) {
         const float4 o = s.o[r];
-        const float4 u = r == 0 ? up : s.o[r - 1];
-        const float4 d = r == kPlRPT - 1 ? dn : s.o[r + 1];
+        float4 u = r == 0 ? up : s.o[r - 1];
+        float4 d = r == kPlRPT - 1 ? dn : s.o[r + 1];
+        if (kMode == kPlLanes && r == 2 && zt)
+            u = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (kMode == kPlLanes && (r == 2 || r == 3) && zb)
+            d = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         bool vu = true, vd = true;
-        if (!kAll) {
+        if (kMode == kPlEvery) {
             vu = (gy0 + r - 1) >= 0;
             vd = (gy0 + r + 1) < (h - 1);
         }
+        float lft = L[r], rgt = R[r], o3 = o.w;  // left of column 0, right of columns 3 and 2
+        if (kMode == kPlLanes) {
+            lft = zl ? 0.0f : lft;
+            rgt = zr ? 0.0f : rgt;
+            o3 = zr ? 0.0f : o3;
+        }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            float left = j == 0 ? L[r] : f4c(o, j - 1);
-            float right = j == 3 ? R[r] : f4c(o, j + 1);
+            float left = j == 0 ? lft : f4c(o, j - 1);
+            float right = j == 3 ? rgt : (j == 2 ? o3 : f4c(o, j + 1));
             float upv = f4c(u, j), dnv = f4c(d, j);
-            if (!kAll) {
+            if (kMode == kPlEvery) {
                 const int gx = gx0 + j;
                 left = (gx - 1) >= 0 ? left : 0.0f;
                 right = (gx + 1) < (w - 1) ? right : 0.0f;
@@ -1065,21 +1099,38 @@ __device__ __forceinline__ void pl_step(PlState& s, const float* src, float* dst
     *reinterpret_cast<float4*>(D + kPlPX) = on[kPlRPT - 1];  // bottom row
 }
 
+// The planar step's test mode for a tile at (ox, oy) of a w x h frame.
+__device__ __forceinline__ int pl_mode(int ox, int oy, int w, int h)
+{
+    if (ox >= 1 && oy >= 1 && ox + kPlW - 1 <= w - 3 && oy + kPlRows - 1 <= h - 3)
+        return kPlAll;
+    const bool row0 = oy <= 0 && oy + kPlRows - 1 >= 0;
+    const bool last2 = oy <= h - 1 && oy + kPlRows - 1 >= h - 2;
+    if ((w & 3) == 0 && (ox & 3) == 0 && (!row0 || oy == -kTbT) && (!last2 || oy == h - kPlRows + kTbT))
+        return kPlLanes;
+    return kPlEvery;
+}
+
 // Iteration k is needed on rows [ring - T + k + 1, kPlRows - ring + T - k - 1)
 // (ring = kTbT); a warp whose rows all lie outside skips it.
-template <bool kAll>
+template <int kMode>
 __device__ __forceinline__ void pl_iterate(PlState& s, float* slots, int T, int k0, float step, float mom, int lane,
-    int warp, int gx0, int gy0, int w, int h)
+    int warp, int gx0, int gy0, int w, int h, int oy)
 {
     const int r0 = kPlRPT * warp;
+    const bool zl = gx0 == 0, zr = gx0 == w - 4;
+    const bool zt = oy == -kTbT && warp == 1, zb = oy == h - kPlRows + kTbT && warp == 10;
+    auto one = [&](int k, bool mom_on) {
+        pl_step<kMode>(s, slots + (k & 1) * kPlSlotPlane, slots + ((k & 1) ^ 1) * kPlSlotPlane, mom_on, step, mom,
+            lane, warp, gx0, gy0, w, h, zl, zr, zt, zb);
+    };
     if (T == kTbT) {
         // full launches, unrolled; momentum is off only in the first step of a solve
         const bool later = k0 > 0;
 #pragma unroll
         for (int k = 0; k < kTbT; ++k) {
             if (!(r0 + kPlRPT - 1 < k + 1 || r0 >= kPlRows - k - 1))
-                pl_step<kAll>(s, slots + (k & 1) * kPlSlotPlane, slots + ((k & 1) ^ 1) * kPlSlotPlane,
-                    k > 0 || later, step, mom, lane, warp, gx0, gy0, w, h);
+                one(k, k > 0 || later);
             __syncthreads();
         }
         return;
@@ -1087,8 +1138,7 @@ __device__ __forceinline__ void pl_iterate(PlState& s, float* slots, int T, int 
     for (int k = 0; k < T; ++k) {
         const int lo = kTbT - T + k + 1, hi = kPlRows - kTbT + T - k - 1;
         if (!(r0 + kPlRPT - 1 < lo || r0 >= hi))
-            pl_step<kAll>(s, slots + (k & 1) * kPlSlotPlane, slots + ((k & 1) ^ 1) * kPlSlotPlane, (k0 + k) > 0,
-                step, mom, lane, warp, gx0, gy0, w, h);
+            one(k, (k0 + k) > 0);
         __syncthreads();
     }
 }
@@ -1182,9 +1232,9 @@ __device__ __forceinline__ void pl_plain_body(const PlPlain& pl, int T, int k0, 
         }
         __syncthreads();  // edge rows published
         if (interior)
-            pl_iterate<true>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h);
+            pl_iterate<kPlAll>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, oy);
         else
-            pl_iterate<false>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h);
+            pl_iterate<kPlEvery>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, oy);
         {
             const int ix = px0 - kTbT;
 #pragma unroll
@@ -1285,6 +1335,15 @@ __device__ __forceinline__ PlJob pl_job(const PlSolve<kN>& g, int ticket)
     j.oy = j.ty * kPlIRows - kTbT;
     j.w = g.w[p];
     j.h = g.h[p];
+    // The bottom row of tiles is moved up until its interior ends on the
+    // frame's last row (rows h - 2 and h - 1 then sit in warp 10, rows 2 and 3,
+    // where pl_step tests them without per-pixel tests), when its 8-row top
+    // ring still lies in the row of tiles above (the 3 x 3 dependency holds).
+    // Its interior then overlaps that row's: both compute the shared rows from
+    // the same inputs with the same arithmetic and store the same bits.
+    const int ty_n = per_plane / g.tiles_x[p];
+    if (j.ty == ty_n - 1 && j.ty > 0 && j.h - j.ty * kPlIRows >= kTbT)
+        j.oy = j.h - kPlRows + kTbT;
     return j;
 }
 
@@ -1489,7 +1548,6 @@ __global__ void __launch_bounds__(kPlThreads, 1)
         }
         const int w = j.w, h = j.h;
         const int gx0 = j.ox + px0, gy0 = j.oy + py0;
-        const bool interior = j.ox >= 1 && j.oy >= 1 && j.ox + kPlW - 1 <= w - 3 && j.oy + kPlRows - 1 <= h - 3;
 
         PlState s;
 #pragma unroll
@@ -1538,10 +1596,13 @@ __global__ void __launch_bounds__(kPlThreads, 1)
             t2_round = n.k;
         }
         const int k0 = j.k * kTbT, T = min(kTbT, g.num_iter - k0);
-        if (interior)
-            pl_iterate<true>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h);
+        const int mode = pl_mode(j.ox, j.oy, w, h);
+        if (mode == kPlAll)
+            pl_iterate<kPlAll>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, j.oy);
+        else if (mode == kPlLanes)
+            pl_iterate<kPlLanes>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, j.oy);
         else
-            pl_iterate<false>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h);
+            pl_iterate<kPlEvery>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, j.oy);
         {
             const int ix = px0 - kTbT;
 #pragma unroll

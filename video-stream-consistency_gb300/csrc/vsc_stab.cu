@@ -569,6 +569,12 @@ __global__ void __launch_bounds__(256) fused_front_kernel(const float* __restric
         return;
     float pv[3], av[3], wv[3];  // kDown: this pixel's P, adapCmbPr, consWt
     if (in) {
+        const I o = (static_cast<I>(y) * w + x) * 3;
+        prefetch_l2(o0 + o);
+        prefetch_l2(p0 + o);
+        prefetch_l2(ls + o);
+        prefetch_l2(o2 + o);
+        prefetch_l2(p2 + o);
         WarpTapT<I> tb, tf;
         if (kHalf) {
             float u, v;
@@ -585,7 +591,6 @@ __global__ void __launch_bounds__(256) fused_front_kernel(const float* __restric
             mp = occl_check(fbwd, ffwd, fc, x, y, w, h);
             mn = occl_check(ffwd, fbwd, fc, x, y, w, h);
         }
-        const I o = (static_cast<I>(y) * w + x) * 3;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const float pwi = warp_sample(o0, tb, c);
