@@ -928,33 +928,59 @@ def e2e_form(vsc, kw, pinned, stream, steps, warmup, ws, dev):
     st = make_stabilizer(vsc, kw, stream)
     for i in range(3):
         st.load_frame(pinned[i][0].numpy(), pinned[i][1].numpy())
-    state = {"nxt": 3, "k": 0, "checksum": 0}
+    state = {"nxt": 3, "k": 0, "checksum": 0, "wait_s": 0.0, "enq_s": []}
 
     def step():
         k = state["k"]
         if k >= 2:
+            t = time.perf_counter()
             st.wait_output(1)  # step k - 2's frame is on the host
+            state["wait_s"] += time.perf_counter() - t
             state["checksum"] += int(outs[k % 2][0, 0, 0])
+        t = time.perf_counter()
         st.step(outs[k % 2], asynchronous=True)
         o, p = pinned[state["nxt"] % n_frames]
         st.load_frame(o.numpy(), p.numpy())
+        state["enq_s"].append(time.perf_counter() - t)
         state["nxt"] += 1
         state["k"] += 1
 
     for _ in range(GRAPH_CAPTURE_STEPS + warmup):
         step()
-    windows = []
+    windows, host = [], []
     for _ in range(3):
         st.synchronize()
         barrier(ws)
         torch.cuda.synchronize()
+        state["wait_s"], state["enq_s"] = 0.0, []
         t0 = time.perf_counter()
         for _ in range(steps):
             step()
         st.synchronize()  # the last two results
-        windows.append(ws * steps / reduce_max(time.perf_counter() - t0, ws, dev))
+        t = time.perf_counter() - t0
+        windows.append(ws * steps / reduce_max(t, ws, dev))
+        # where the host's time went: blocked on results (GPU-bound) or
+        # enqueueing a step and its upload (host-bound when it nears a step)
+        host.append({"wait_frac": round(state["wait_s"] / t, 3),
+                     "enqueue_us_median": round(1e6 * statistics.median(state["enq_s"]), 1),
+                     "enqueue_us_max": round(1e6 * max(state["enq_s"]), 1)})
     st.close()
-    return {"value": statistics.median(windows), "unit": "frames/s", "windows": windows,
+    # the copy bandwidths of this run's pinned buffers (a slow host link shows
+    # here, not in the kernels): one frame pair up, one frame down, CUDA events
+    pair = torch.empty((2, H, W, 4), dtype=torch.uint8, device=dev)
+    src = torch.stack([pinned[0][0], pinned[0][1]]).pin_memory()
+    gbs = {"h2d": [], "d2h": []}
+    with torch.cuda.stream(stream):
+        for _ in range(5):
+            for kind, dst_t, src_t in (("h2d", pair, src), ("d2h", outs[0], pair[0])):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                dst_t.copy_(src_t, non_blocking=True)
+                e1.record(stream)
+                e1.synchronize()
+                gbs[kind].append(dst_t.numel() / (e0.elapsed_time(e1) * 1e6))
+    return {"value": statistics.median(windows), "unit": "frames/s", "windows": windows, "host": host,
+            "copy_gbs": {k: round(statistics.median(v), 1) for k, v in gbs.items()},
             "h2d_bytes_per_step": 2 * W * H * 4, "d2h_bytes_per_step": W * H * 4,
             "pipelining": "results read back asynchronously into pinned memory on the stabilizer's download "
                           "stream, the host at most two steps ahead; uploads on its copy stream"}
@@ -1126,13 +1152,13 @@ SOLVER_KERNELS = {"exact": ("solver_tall_kernel", 84), "fma": ("solver_fma_solve
 # dram__bytes_read.sum + dram__bytes_write.sum of one 8-step round at
 # 1920x1080 from the ncu captures summarised in profiles/, and where each
 # comes from.
-SOLVER_TRAFFIC_BYTES = {"solver_tall_kernel": 144_198_912, "solver_fma_solve_kernel": 141_152_768}
+SOLVER_TRAFFIC_BYTES = {"solver_tall_kernel": 144_198_912, "solver_fma_solve_kernel": 143_518_400}
 SOLVER_TRAFFIC_SOURCE = {
     "solver_tall_kernel": "profiles/solver_tall_1080p.md (one launch per round; mean of two launches: "
                           "124,613,888 + 21,037,568 and 124,601,600 + 18,144,768 bytes)",
     "solver_fma_solve_kernel": "profiles/solver_fma_solve_1080p.md (one launch per solve; per round, the "
-                               "difference of a 40-step and an 8-step solve over 4 rounds: (468,436,992 - "
-                               "99,783,936) read + (213,648,896 - 17,690,880) written, / 4)",
+                               "difference of a 40-step and an 8-step solve over 4 rounds: (477,521,920 - "
+                               "99,679,232) read + (214,155,776 - 17,924,864) written, / 4)",
 }
 # What bounds each solver kernel, from the same captures: the FP32 pipe and
 # its latency, not HBM (the time steps stay on chip): the FMA pipe's active
@@ -1140,7 +1166,7 @@ SOLVER_TRAFFIC_SOURCE = {
 # sm__cycles_active) and smsp__issue_active.
 SOLVER_PIPE = {
     "solver_tall_kernel": {"fma_pipe_active": None, "issue_active": 0.585},
-    "solver_fma_solve_kernel": {"fma_pipe_active": 0.544, "issue_active": 0.420},
+    "solver_fma_solve_kernel": {"fma_pipe_active": 0.559, "issue_active": 0.397},
 }
 
 

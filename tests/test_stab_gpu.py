@@ -148,13 +148,16 @@ def test_consist_out(vsc, oracle, cuda, h, w, iters):
 # of one plane: these sizes give one tile, several, partial tiles at the right
 # and bottom), others the plain-load one; iteration counts not divisible by 8
 # end in a short launch.  Border tiles test the frame's rows 0, h - 2 and
-# h - 1 per warp and its columns 0, w - 2 and w - 1 per lane: 61 rows put
-# rows h - 2 and h - 1 in two warps, 1 row makes row 0 also row h - 1, 8
-# columns put columns 0 and w - 2 in neighbouring lanes.
+# h - 1 and its columns 0, w - 2 and w - 1 at fixed places when the bottom row
+# of tiles can be moved to end on the frame's last row, per pixel otherwise:
+# 61 rows leave it in place (rows h - 2 and h - 1 in two warps), 72, 100, 120
+# and 130 rows move it over the row above by different amounts; 1 row makes
+# row 0 also row h - 1, 8 columns put columns 0 and w - 2 in neighbouring
+# lanes.
 @pytest.mark.parametrize("h,w,iters", [(9, 11, 0), (9, 11, 1), (9, 11, 2), (40, 56, 75), (3, 3, 5), (2, 2, 4),
                                        (67, 33, 150), (48, 200, 13), (540, 960, 75), (1080, 1920, 150),
                                        (17, 4, 3), (100, 64, 150), (61, 70, 19), (61, 72, 24), (1, 8, 9),
-                                       (2, 4, 16), (130, 236, 40)])
+                                       (2, 4, 16), (130, 236, 40), (72, 128, 16), (120, 96, 24)])
 def test_consist_out_fma(vsc, oracle, cuda, h, w, iters):
     """vsc_get_consist_out_fma equals the restatement's FMA form bit for bit,
     and the exact form (kernel_consist_out's rounding) within the stated
