@@ -1112,10 +1112,13 @@ __device__ __forceinline__ int pl_mode(int ox, int oy, int w, int h)
 }
 
 // Iteration k is needed on rows [ring - T + k + 1, kPlRows - ring + T - k - 1)
-// (ring = kTbT); a warp whose rows all lie outside skips it.
-template <int kMode>
+// (ring = kTbT); a warp whose rows all lie outside skips it.  `idle` runs in
+// the warps that skip the sixth step of a full round (warps 0 and 11: work a
+// caller keeps off the steps' critical path, as long as it fits a step), and
+// before the steps of a shorter round.
+template <int kMode, class Idle>
 __device__ __forceinline__ void pl_iterate(PlState& s, float* slots, int T, int k0, float step, float mom, int lane,
-    int warp, int gx0, int gy0, int w, int h, int oy)
+    int warp, int gx0, int gy0, int w, int h, int oy, Idle&& idle)
 {
     const int r0 = kPlRPT * warp;
     const bool zl = gx0 == 0, zr = gx0 == w - 4;
@@ -1131,10 +1134,13 @@ __device__ __forceinline__ void pl_iterate(PlState& s, float* slots, int T, int 
         for (int k = 0; k < kTbT; ++k) {
             if (!(r0 + kPlRPT - 1 < k + 1 || r0 >= kPlRows - k - 1))
                 one(k, k > 0 || later);
+            else if (k == kTbT - 3)
+                idle();
             __syncthreads();
         }
         return;
     }
+    idle();
     for (int k = 0; k < T; ++k) {
         const int lo = kTbT - T + k + 1, hi = kPlRows - kTbT + T - k - 1;
         if (!(r0 + kPlRPT - 1 < lo || r0 >= hi))
@@ -1232,9 +1238,9 @@ __device__ __forceinline__ void pl_plain_body(const PlPlain& pl, int T, int k0, 
         }
         __syncthreads();  // edge rows published
         if (interior)
-            pl_iterate<kPlAll>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, oy);
+            pl_iterate<kPlAll>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, oy, [] {});
         else
-            pl_iterate<kPlEvery>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, oy);
+            pl_iterate<kPlEvery>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, oy, [] {});
         {
             const int ix = px0 - kTbT;
 #pragma unroll
@@ -1420,6 +1426,13 @@ __device__ __forceinline__ void pl_job_signal(const PlSolve<kN>& g, const PlJob&
     st_release_u32(g.done[j.p] + j.local, static_cast<unsigned>(j.k + 1));
 }
 
+__device__ __forceinline__ void pl_counter_signal(unsigned* done, unsigned v)
+{
+    bulk_wait_all();
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    st_release_u32(done, v);
+}
+
 // Warp 0 looks at the 3x3 neighbourhood of job j in two halves, so that the
 // L2 round trip can overlap a tile's steps.  Issue: lanes 0..8 each start one
 // relaxed load of a neighbour's counter (a lane without a neighbour, or a job
@@ -1467,6 +1480,9 @@ __global__ void __launch_bounds__(kPlThreads, 1)
     float* su = so + kPlOut;
     uint64_t* bar = reinterpret_cast<uint64_t*>(su + kPlOut);
     __shared__ int s_next, s_deferred, s_abort;
+    // decoded jobs: the next tile's (read by every thread at its top) and the
+    // one after it (decoded by warp 0 while the current tile runs)
+    __shared__ PlJob s_job, s_job2;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int px0 = 4 * lane, py0 = kPlRPT * warp;
     const int total = g.tile0[g.count] * g.nround;
@@ -1497,6 +1513,7 @@ __global__ void __launch_bounds__(kPlThreads, 1)
             s_next = a;
             if (a < total) {
                 const PlJob n = pl_job(g, a);
+                s_job = n;
                 if (pl_deps(g, n, kWaitSpins)) {
                     pl_job_loads(stage, g, n, bar);
                 } else {
@@ -1507,14 +1524,18 @@ __global__ void __launch_bounds__(kPlThreads, 1)
         }
         const bool valid = t1 < total;
         const PlJob n = valid ? pl_job(g, t1) : PlJob{};
+        if (lane == 0)
+            s_job2 = n;
         t1_ready = pl_deps_take(pl_deps_issue(g, n, valid, lane), n.k);
     }
     __syncthreads();
     int cur = s_next;
     uint32_t parity = 0;
-    int prev = -1;  // thread 0: the ticket of a tile whose round is not yet published
+    // thread 0: the counter and value of a tile whose round is not yet published
+    unsigned* prev_done = nullptr;
+    unsigned prev_val = 0;
     while (cur < total && !s_abort) {
-        const PlJob j = pl_job(g, cur);
+        const PlJob j = s_job;
         int t2 = 0;
         if (warp == 0 && lane == 0)
             t2 = static_cast<int>(atomicAdd(g.ticket, 1u));  // used after the tile's first barrier
@@ -1533,18 +1554,16 @@ __global__ void __launch_bounds__(kPlThreads, 1)
             // registers: it releases the previous tile's completed stores
             // (published by the relaxed counter store after it) and acquires
             // the neighbour counters read for t1 during that tile's steps.
-            if (lane == 0 && prev >= 0) {
+            if (lane == 0 && prev_done) {
                 bulk_wait_all();
                 asm volatile("fence.proxy.async.global;" ::: "memory");
             }
             __syncwarp();
             asm volatile("fence.acq_rel.gpu;" ::: "memory");
             __syncwarp();
-            if (lane == 0 && prev >= 0) {
-                const PlJob pj = pl_job(g, prev);
-                st_relaxed_u32(g.done[pj.p] + pj.local, static_cast<unsigned>(pj.k + 1));
-            }
-            prev = -1;
+            if (lane == 0 && prev_done)
+                st_relaxed_u32(prev_done, prev_val);
+            prev_done = nullptr;
         }
         const int w = j.w, h = j.h;
         const int gx0 = j.ox + px0, gy0 = j.oy + py0;
@@ -1570,10 +1589,11 @@ __global__ void __launch_bounds__(kPlThreads, 1)
             // load the next tile now if its neighbours are finished (seen
             // across the previous tile, else one look now)
             const bool valid = t1 < total;
-            const PlJob n = valid ? pl_job(g, t1) : PlJob{};
+            const PlJob n = s_job2;  // decoded while the previous tile ran
             const bool ready = t1_ready || pl_deps_take(pl_deps_issue(g, n, valid, lane), n.k);
             if (lane == 0) {
                 s_next = t1;
+                s_job = n;
                 s_deferred = 0;
                 if (valid) {
                     if (ready) {
@@ -1588,21 +1608,27 @@ __global__ void __launch_bounds__(kPlThreads, 1)
         __syncthreads();  // edge rows published
         unsigned t2_look = ~0u;
         int t2_round = 0;
-        if (warp == 0) {
-            t2 = __shfl_sync(0xffffffffu, t2, 0);
-            const bool valid = t2 < total;
-            const PlJob n = valid ? pl_job(g, t2) : PlJob{};
-            t2_look = pl_deps_issue(g, n, valid, lane);
-            t2_round = n.k;
-        }
+        // warp 0, in a step it skips: decode t2 and start reading its
+        // neighbours' counters (taken after the steps)
+        auto idle = [&] {
+            if (warp == 0) {
+                t2 = __shfl_sync(0xffffffffu, t2, 0);
+                const bool valid = t2 < total;
+                const PlJob n = valid ? pl_job(g, t2) : PlJob{};
+                if (lane == 0)
+                    s_job2 = n;
+                t2_look = pl_deps_issue(g, n, valid, lane);
+                t2_round = n.k;
+            }
+        };
         const int k0 = j.k * kTbT, T = min(kTbT, g.num_iter - k0);
         const int mode = pl_mode(j.ox, j.oy, w, h);
         if (mode == kPlAll)
-            pl_iterate<kPlAll>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, j.oy);
+            pl_iterate<kPlAll>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, j.oy, idle);
         else if (mode == kPlLanes)
-            pl_iterate<kPlLanes>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, j.oy);
+            pl_iterate<kPlLanes>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, j.oy, idle);
         else
-            pl_iterate<kPlEvery>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, j.oy);
+            pl_iterate<kPlEvery>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, j.oy, idle);
         {
             const int ix = px0 - kTbT;
 #pragma unroll
@@ -1627,13 +1653,14 @@ __global__ void __launch_bounds__(kPlThreads, 1)
             tma_store_3d(m + (par ? kPmOo1 : kPmOo0), j.ox + kTbT, j.oy + kTbT, j.c, so);
             tma_store_3d(m + (par ? kPmUo1 : kPmUo0), j.ox + kTbT, j.oy + kTbT, j.c, su);
             bulk_commit();
-            prev = cur;
+            prev_done = g.done[j.p] + j.local;
+            prev_val = static_cast<unsigned>(j.k + 1);
             if (s_deferred) {
                 // the next tile's neighbours were not finished: publish this
                 // tile first (the next one may need it), then wait
                 pl_job_signal(g, j);
-                prev = -1;
-                const PlJob n = pl_job(g, s_next);
+                prev_done = nullptr;
+                const PlJob n = s_job;
                 if (pl_deps(g, n, kWaitSpins)) {
                     pl_job_loads(stage, g, n, bar);
                 } else {
@@ -1646,8 +1673,8 @@ __global__ void __launch_bounds__(kPlThreads, 1)
         cur = s_next;
     }
     if (threadIdx.x == 0) {
-        if (prev >= 0)
-            pl_job_signal(g, pl_job(g, prev));
+        if (prev_done)
+            pl_counter_signal(prev_done, prev_val);
         bulk_wait_all();
     }
 }
