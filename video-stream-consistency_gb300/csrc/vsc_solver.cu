@@ -1112,10 +1112,11 @@ __device__ __forceinline__ int pl_mode(int ox, int oy, int w, int h)
 }
 
 // Iteration k is needed on rows [ring - T + k + 1, kPlRows - ring + T - k - 1)
-// (ring = kTbT); a warp whose rows all lie outside skips it.  `idle` runs in
-// the warps that skip the sixth step of a full round (warps 0 and 11: work a
-// caller keeps off the steps' critical path, as long as it fits a step), and
-// before the steps of a shorter round.
+// (ring = kTbT); a warp whose rows all lie outside skips it.  idle(k) runs in
+// the warps that skip the last three steps k of a full round (warps 0 and
+// 11: work a caller keeps off the steps' critical path, as long as each part
+// fits a step); in a shorter round idle(kTbT - 3) runs before its steps and
+// the other two after them.
 template <int kMode, class Idle>
 __device__ __forceinline__ void pl_iterate(PlState& s, float* slots, int T, int k0, float step, float mom, int lane,
     int warp, int gx0, int gy0, int w, int h, int oy, Idle&& idle)
@@ -1134,19 +1135,21 @@ __device__ __forceinline__ void pl_iterate(PlState& s, float* slots, int T, int 
         for (int k = 0; k < kTbT; ++k) {
             if (!(r0 + kPlRPT - 1 < k + 1 || r0 >= kPlRows - k - 1))
                 one(k, k > 0 || later);
-            else if (k == kTbT - 3)
-                idle();
+            else if (k >= kTbT - 3)
+                idle(k);
             __syncthreads();
         }
         return;
     }
-    idle();
+    idle(kTbT - 3);
     for (int k = 0; k < T; ++k) {
         const int lo = kTbT - T + k + 1, hi = kPlRows - kTbT + T - k - 1;
         if (!(r0 + kPlRPT - 1 < lo || r0 >= hi))
             one(k, (k0 + k) > 0);
         __syncthreads();
     }
+    idle(kTbT - 2);
+    idle(kTbT - 1);
 }
 
 int pl_tiles_x(int w) { return (w + kPlIW - 1) / kPlIW; }
@@ -1238,9 +1241,9 @@ __device__ __forceinline__ void pl_plain_body(const PlPlain& pl, int T, int k0, 
         }
         __syncthreads();  // edge rows published
         if (interior)
-            pl_iterate<kPlAll>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, oy, [] {});
+            pl_iterate<kPlAll>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, oy, [](int) {});
         else
-            pl_iterate<kPlEvery>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, oy, [] {});
+            pl_iterate<kPlEvery>(s, slots, T, k0, step, mom, lane, warp, gx0, gy0, w, h, oy, [](int) {});
         {
             const int ix = px0 - kTbT;
 #pragma unroll
@@ -1486,6 +1489,10 @@ __global__ void __launch_bounds__(kPlThreads, 1)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int px0 = 4 * lane, py0 = kPlRPT * warp;
     const int total = g.tile0[g.count] * g.nround;
+    // Many tiles a round (ticketed several tiles' time before their
+    // dependents): a tile's round is published while the next tile runs, in
+    // steps warp 0 skips, instead of on that tile's critical path.
+    const bool lag = g.tile0[g.count] >= 3 * static_cast<int>(gridDim.x);
 
     for (int i = threadIdx.x; i < 2 * kPlSlotPlane; i += kPlThreads)
         slots[i] = 0.0f;  // the apron slots stay zero
@@ -1549,11 +1556,12 @@ __global__ void __launch_bounds__(kPlThreads, 1)
             return;
         }
         parity ^= 1;
-        if (warp == 0) {
+        if (warp == 0 && !lag) {
             // One fence a tile, taken while the other warps stage their
             // registers: it releases the previous tile's completed stores
             // (published by the relaxed counter store after it) and acquires
             // the neighbour counters read for t1 during that tile's steps.
+            // (With `lag`, the same happens in the previous tile's last step.)
             if (lane == 0 && prev_done) {
                 bulk_wait_all();
                 asm volatile("fence.proxy.async.global;" ::: "memory");
@@ -1608,10 +1616,15 @@ __global__ void __launch_bounds__(kPlThreads, 1)
         __syncthreads();  // edge rows published
         unsigned t2_look = ~0u;
         int t2_round = 0;
-        // warp 0, in a step it skips: decode t2 and start reading its
-        // neighbours' counters (taken after the steps)
-        auto idle = [&] {
-            if (warp == 0) {
+        // warp 0, in the steps it skips: decode t2 and start reading its
+        // neighbours' counters; with `lag`, wait for the previous tile's
+        // stores (long complete by then); take the counters and, with `lag`,
+        // one fence that acquires them (for t2's loads at the top of the next
+        // tile) and releases the previous tile's stores, published after it
+        auto idle = [&](int k) {
+            if (warp != 0)
+                return;
+            if (k == kTbT - 3) {
                 t2 = __shfl_sync(0xffffffffu, t2, 0);
                 const bool valid = t2 < total;
                 const PlJob n = valid ? pl_job(g, t2) : PlJob{};
@@ -1619,6 +1632,21 @@ __global__ void __launch_bounds__(kPlThreads, 1)
                     s_job2 = n;
                 t2_look = pl_deps_issue(g, n, valid, lane);
                 t2_round = n.k;
+            } else if (k == kTbT - 2) {
+                if (lag && lane == 0 && prev_done) {
+                    bulk_wait_all();
+                    asm volatile("fence.proxy.async.global;" ::: "memory");
+                }
+            } else {
+                t1_ready = __all_sync(0xffffffffu, t2_look >= static_cast<unsigned>(t2_round));
+                if (lag) {
+                    __syncwarp();
+                    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0 && prev_done)
+                        st_relaxed_u32(prev_done, prev_val);
+                    prev_done = nullptr;
+                }
             }
         };
         const int k0 = j.k * kTbT, T = min(kTbT, g.num_iter - k0);
@@ -1640,11 +1668,8 @@ __global__ void __launch_bounds__(kPlThreads, 1)
                 *reinterpret_cast<float4*>(su + iy * kPlIW + ix) = s.u[r];
             }
         }
-        if (warp == 0) {
-            // acquired by the fence at the top of the next tile
-            t1_ready = __all_sync(0xffffffffu, t2_look >= static_cast<unsigned>(t2_round));
-            t1 = t2;
-        }
+        if (warp == 0)
+            t1 = t2;  // t1_ready: taken in the last step, acquired by its fence or the next top's
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (threadIdx.x == 0) {
