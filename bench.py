@@ -1152,13 +1152,13 @@ SOLVER_KERNELS = {"exact": ("solver_tall_kernel", 84), "fma": ("solver_fma_solve
 # dram__bytes_read.sum + dram__bytes_write.sum of one 8-step round at
 # 1920x1080 from the ncu captures summarised in profiles/, and where each
 # comes from.
-SOLVER_TRAFFIC_BYTES = {"solver_tall_kernel": 144_198_912, "solver_fma_solve_kernel": 143_518_400}
+SOLVER_TRAFFIC_BYTES = {"solver_tall_kernel": 144_198_912, "solver_fma_solve_kernel": 140_631_616}
 SOLVER_TRAFFIC_SOURCE = {
     "solver_tall_kernel": "profiles/solver_tall_1080p.md (one launch per round; mean of two launches: "
                           "124,613,888 + 21,037,568 and 124,601,600 + 18,144,768 bytes)",
     "solver_fma_solve_kernel": "profiles/solver_fma_solve_1080p.md (one launch per solve; per round, the "
-                               "difference of a 40-step and an 8-step solve over 4 rounds: (477,521,920 - "
-                               "99,679,232) read + (214,155,776 - 17,924,864) written, / 4)",
+                               "difference of a 40-step and an 8-step solve over 4 rounds: (466,624,512 - "
+                               "99,649,280) read + (212,874,752 - 17,323,520) written, / 4)",
 }
 # What bounds each solver kernel, from the same captures: the FP32 pipe and
 # its latency, not HBM (the time steps stay on chip): the FMA pipe's active
@@ -1166,7 +1166,7 @@ SOLVER_TRAFFIC_SOURCE = {
 # sm__cycles_active) and smsp__issue_active.
 SOLVER_PIPE = {
     "solver_tall_kernel": {"fma_pipe_active": None, "issue_active": 0.585},
-    "solver_fma_solve_kernel": {"fma_pipe_active": 0.559, "issue_active": 0.397},
+    "solver_fma_solve_kernel": {"fma_pipe_active": 0.647, "issue_active": 0.448},
 }
 
 
