@@ -1614,7 +1614,7 @@ __global__ void __launch_bounds__(kPlThreads, 1)
             }
         }
         __syncthreads();  // edge rows published
-        unsigned t2_look = ~0u;
+        unsigned t2_look = ~0u, t1_look = ~0u;
         int t2_round = 0;
         // warp 0, in the steps it skips: decode t2 and start reading its
         // neighbours' counters; with `lag`, wait for the previous tile's
@@ -1632,10 +1632,28 @@ __global__ void __launch_bounds__(kPlThreads, 1)
                     s_job2 = n;
                 t2_look = pl_deps_issue(g, n, valid, lane);
                 t2_round = n.k;
+                // a deferred next tile (few tiles a round): look again now
+                if (!lag && s_deferred)
+                    t1_look = pl_deps_issue(g, s_job, true, lane);
             } else if (k == kTbT - 2) {
                 if (lag && lane == 0 && prev_done) {
                     bulk_wait_all();
                     asm volatile("fence.proxy.async.global;" ::: "memory");
+                }
+                if (!lag && s_deferred) {
+                    // its neighbours finished during this tile's steps: load it
+                    // now instead of after the tile (ordered as at the top)
+                    const PlJob n = s_job;
+                    if (__all_sync(0xffffffffu, t1_look >= static_cast<unsigned>(n.k))) {
+                        __syncwarp();
+                        asm volatile("fence.acq_rel.gpu;" ::: "memory");
+                        __syncwarp();
+                        if (lane == 0) {
+                            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                            pl_job_loads(stage, g, n, bar);
+                            s_deferred = 0;
+                        }
+                    }
                 }
             } else {
                 t1_ready = __all_sync(0xffffffffu, t2_look >= static_cast<unsigned>(t2_round));
