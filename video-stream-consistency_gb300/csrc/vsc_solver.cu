@@ -1292,8 +1292,11 @@ __global__ void __launch_bounds__(kPlThreads, 1)
 // per round at 1920x1080 leave the eighth of eight rounds 11 % full) and the
 // launch boundaries.  The next ticket's loads are issued while the current
 // tile iterates when its neighbours are ready (normally: they finished about
-// N / #SMs tiles earlier); otherwise the CTA first finishes and signals its
-// current tile, then waits.
+// N / #SMs tiles earlier); otherwise warp 0 looks again during the steps it
+// skips, and failing that the CTA first finishes and signals its current
+// tile, then waits.  The tickets' bookkeeping (decoding, neighbour checks,
+// and with many tiles a round the fence that publishes a tile) runs in those
+// skipped steps, not between a tile's data and its first step.
 enum { kPmO0, kPmO1, kPmU0, kPmU1, kPmK, kPmC, kPmOo0, kPmOo1, kPmUo0, kPmUo1, kPlMaps };
 
 template <int kN>
@@ -1504,8 +1507,9 @@ __global__ void __launch_bounds__(kPlThreads, 1)
     grid_dependency_wait();
     // Tickets are taken two ahead: while a CTA runs its current tile, warp 0
     // holds the next ticket (t1, loaded during the current tile) and takes the
-    // one after (t2), whose neighbours it checks across the current tile's
-    // steps; the atomic and the counter reads stay off the critical path.
+    // one after (t2), which it decodes and whose neighbours it checks in the
+    // steps it skips; the atomic, the divisions and the counter reads stay off
+    // the critical path.
     int t1 = 0;
     bool t1_ready = false;  // warp 0: t1's neighbours were seen finished
     if (warp == 0) {
