@@ -132,7 +132,6 @@ __global__ void __launch_bounds__((2 + 4 * kMaxEpiGroups) * 32, 1)
         float* __restrict__ out2, int nprob, const float* __restrict__ scales, int N, int H, int W, int Cp, int md,
         uint32_t idesc, int stages_a, int stages_b, int groups, int ndyg, int* __restrict__ timeout_flag)
 {
-    pdl_enter();
     extern __shared__ unsigned char smem_raw[];
     const uint32_t bytesA = kTcM * Cp * 2;
     const uint32_t bytesB = kTcN * Cp * 2;
@@ -191,6 +190,9 @@ __global__ void __launch_bounds__((2 + 4 * kMaxEpiGroups) * 32, 1)
     __syncthreads();
     ptx::tc_fence_after();
     const uint32_t tmem = *sh.tmem_slot;
+    // the setup above (Tensor Memory, barriers) overlaps the previous
+    // kernel's tail; its outputs (this launch's operands) are read from here
+    pdl_enter();
 
     if (warp == 0) {
         // ---- TMA producer ------------------------------------------------------
